@@ -1,0 +1,1241 @@
+/*
+ * pbd_oracle.c -- CPU restatement of the reference PBD cloth step.
+ *
+ * TEST INFRASTRUCTURE ONLY (the checker, never the product): loaded by
+ * tests/, __graft_entry__.smoke() and bench.py's cpu_baseline leg.
+ *
+ * Reference paths are relative to
+ * PositionBasedDynamicsCUDA/PositionBasedDynamicsCUDA/ of
+ * vivienldy/PositionBasedDynamicsOld ("P/" below).  Each routine states the
+ * reference lines it follows; where the reference reads uninitialised memory
+ * or divides by zero the restatement says what it does instead.
+ *
+ * Build: cc -O2 -ffp-contract=off -fPIC -shared (see oracle/build_oracle.py).
+ */
+#include "pbd_oracle.h"
+
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+
+/* ------------------------------------------------------------------ */
+/* float3 arithmetic in the operation order of the reference's host code */
+/* ------------------------------------------------------------------ */
+typedef struct { float x, y, z; } f3;
+
+static inline f3 mk(float x, float y, float z) { f3 r = {x, y, z}; return r; }
+static inline f3 ld3(const float *p) { return mk(p[0], p[1], p[2]); }
+static inline void st3(float *p, f3 v) { p[0] = v.x; p[1] = v.y; p[2] = v.z; }
+static inline f3 add(f3 a, f3 b) { return mk(a.x + b.x, a.y + b.y, a.z + b.z); }
+static inline f3 sub(f3 a, f3 b) { return mk(a.x - b.x, a.y - b.y, a.z - b.z); }
+static inline f3 mul(f3 a, float s) { return mk(a.x * s, a.y * s, a.z * s); }
+static inline f3 divs(f3 a, float s) { return mk(a.x / s, a.y / s, a.z / s); }
+static inline float dot(f3 a, f3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+static inline f3 cross(f3 a, f3 b)
+{
+    return mk(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
+}
+/* normalize: v * (1/sqrt(v.v)) -- the host form used by P/CCD.cpp */
+static inline f3 nrm(f3 v)
+{
+    float inv = 1.0f / sqrtf(dot(v, v));
+    return mul(v, inv);
+}
+/* Distance (P/PBD_cuda.cu:3-6, P/PBD_Basic.cuh:321-324): the sum of the
+ * three squared differences, then the square root.  The reference spells
+ * both as powf (x^2 and s^0.5); with g_pow_distance set the oracle does the
+ * same (used when pinning against the reference's compiled code), otherwise
+ * it uses the correctly rounded x*x and sqrtf that the CUDA kernels use. */
+static int g_pow_distance = 0;
+void orc_set_pow_distance(int on) { g_pow_distance = on; }
+static inline float dist3(f3 a, f3 b)
+{
+    float dx = a.x - b.x, dy = a.y - b.y, dz = a.z - b.z;
+    if (g_pow_distance)
+        return powf(powf(dx, 2.0f) + powf(dy, 2.0f) + powf(dz, 2.0f), 0.5f);
+    return sqrtf(dx * dx + dy * dy + dz * dz);
+}
+/* stp (P/CCD_Basic.h:181): u . (v x w) in float */
+static inline float stp(f3 u, f3 v, f3 w) { return dot(u, cross(v, w)); }
+/* pos (P/CCD.cpp:8-11): the double t is narrowed to float for the product */
+static inline f3 lerp_t(f3 a, f3 b, double t)
+{
+    float tf = (float)t;
+    f3 d = sub(b, a);
+    return add(a, mk(tf * d.x, tf * d.y, tf * d.z));
+}
+/* BarycentricCoord (P/CCD.cpp:115-130): weights of p0, p1, p2 from the
+ * Gram matrix of the two edges out of p2 (Ericson, Real-Time Collision
+ * Detection, 3.4). */
+static inline f3 bary(f3 pos, f3 p0, f3 p1, f3 p2)
+{
+    f3 ab = sub(p0, p2), ac = sub(p1, p2), ap = sub(pos, p2);
+    float d00 = dot(ac, ac), d01 = dot(ac, ab), d02 = dot(ac, ap);
+    float d11 = dot(ab, ab), d12 = dot(ab, ap);
+    float inv = 1.0f / (d00 * d11 - d01 * d01);
+    float v = (d11 * d02 - d01 * d12) * inv;
+    float u = (d00 * d12 - d01 * d02) * inv;
+    float w = 1.0f - u - v;
+    return mk(u, v, w);
+}
+
+/* ------------------------------------------------------------------ */
+/* constraint graph and coloring                                        */
+/* ------------------------------------------------------------------ */
+
+int64_t orc_prim2prims(int n_prims, const int *prim_list, const int *indices,
+                       int n_points, int *adj_start_num, int *adj_idx)
+{
+    /* point -> prims map in prim id order (GenePoint2PrimsMap,
+     * P/PBD_cuda.cu:155-168) as CSR */
+    int *cnt = (int *)calloc((size_t)n_points + 1, sizeof(int));
+    for (int p = 0; p < n_prims; ++p)
+        for (int i = 0; i < prim_list[2 * p + 1]; ++i)
+            cnt[indices[prim_list[2 * p] + i] + 1]++;
+    for (int i = 0; i < n_points; ++i) cnt[i + 1] += cnt[i];
+    int64_t total_inc = cnt[n_points];
+    int *inc = (int *)malloc(sizeof(int) * (size_t)(total_inc > 0 ? total_inc : 1));
+    int *fill = (int *)malloc(sizeof(int) * ((size_t)n_points + 1));
+    memcpy(fill, cnt, sizeof(int) * ((size_t)n_points + 1));
+    for (int p = 0; p < n_prims; ++p)
+        for (int i = 0; i < prim_list[2 * p + 1]; ++i)
+            inc[fill[indices[prim_list[2 * p] + i]]++] = p;
+    /* prim -> linked prims (GenePrim2PrimsMap, P/PBD_cuda.cu:170-202) */
+    int64_t total = 0;
+    for (int p = 0; p < n_prims; ++p) {
+        int64_t start = total;
+        for (int i = 0; i < prim_list[2 * p + 1]; ++i) {
+            int pt = indices[prim_list[2 * p] + i];
+            for (int j = cnt[pt]; j < cnt[pt + 1]; ++j) {
+                int q = inc[j];
+                if (q == p) continue;
+                if (adj_idx) adj_idx[total] = q;
+                total++;
+            }
+        }
+        if (adj_start_num) {
+            adj_start_num[2 * p] = (int)start;
+            adj_start_num[2 * p + 1] = (int)(total - start);
+        }
+    }
+    free(cnt);
+    free(inc);
+    free(fill);
+    return total;
+}
+
+/* speculative color of one prim: first color not used by a coloured
+ * neighbour, searched in windows of 64 (P/PBD_cuda.cu:335-370) */
+static int first_free_color(int idx, const int *adj_start_num, const int *adj_idx,
+                            const int *color)
+{
+    int nidx = adj_start_num[2 * idx];
+    int nlast = nidx + adj_start_num[2 * idx + 1];
+    int offset = 0;
+    for (;;) {
+        uint64_t forbidden = 0;
+        for (int i = nidx; i < nlast; ++i) {
+            int nc = color[adj_idx[i]] - offset;
+            if (nc >= 0 && nc < 64) forbidden |= (1ull << nc);
+        }
+        if (forbidden != ~0ull) return offset + __builtin_ctzll(~forbidden);
+        offset += 64;
+    }
+}
+
+void orc_assign_colors(int n_prims, const int *adj_start_num, const int *adj_idx,
+                       const int *color, int *prd_color)
+{
+    for (int idx = 0; idx < n_prims; ++idx) {
+        if (color[idx] >= 0) continue;
+        prd_color[idx] = first_free_color(idx, adj_start_num, adj_idx, color);
+    }
+}
+
+/* conflict test (P/PBD_cuda.cu:400-422): a neighbour with the same
+ * speculative color wins if it has more points, or as many and a lower id */
+static int loses(int idx, const int *prim_list, const int *adj_start_num,
+                 const int *adj_idx, const int *prd_color)
+{
+    int c = prd_color[idx];
+    int npt = prim_list[2 * idx + 1];
+    int nidx = adj_start_num[2 * idx];
+    int nlast = nidx + adj_start_num[2 * idx + 1];
+    for (int i = nidx; i < nlast; ++i) {
+        int n = adj_idx[i];
+        if (prd_color[n] != c) continue;
+        int nnpt = prim_list[2 * n + 1];
+        if (nnpt > npt || (nnpt == npt && n < idx)) return 1;
+    }
+    return 0;
+}
+
+int orc_resolve_conflicts_gpu(int n_prims, const int *prim_list,
+                              const int *adj_start_num, const int *adj_idx,
+                              int *color, const int *prd_color)
+{
+    int flag = 0;
+    for (int idx = 0; idx < n_prims; ++idx) {
+        if (color[idx] >= 0) continue;
+        if (loses(idx, prim_list, adj_start_num, adj_idx, prd_color))
+            flag = 1;
+        else
+            color[idx] = prd_color[idx];
+    }
+    return flag;
+}
+
+int orc_resolve_conflicts_cpu(int n_prims, const int *prim_list,
+                              const int *adj_start_num, const int *adj_idx,
+                              int *color, const int *prd_color)
+{
+    for (int idx = 0; idx < n_prims; ++idx) {
+        if (color[idx] >= 0) continue;
+        if (loses(idx, prim_list, adj_start_num, adj_idx, prd_color)) return 1;
+        color[idx] = prd_color[idx];
+    }
+    return 0;
+}
+
+int orc_edge_coloring_gpu(int n_prims, const int *prim_list,
+                          const int *adj_start_num, const int *adj_idx,
+                          int *color, int *prd_color, int max_iters)
+{
+    int it = 0;
+    while (it < max_iters) {
+        orc_assign_colors(n_prims, adj_start_num, adj_idx, color, prd_color);
+        int flag = orc_resolve_conflicts_gpu(n_prims, prim_list, adj_start_num,
+                                             adj_idx, color, prd_color);
+        ++it;
+        if (!flag) break;
+    }
+    return it;
+}
+
+int orc_edge_coloring_cpu(int n_prims, const int *prim_list,
+                          const int *adj_start_num, const int *adj_idx,
+                          int *color, int *prd_color, int max_iters)
+{
+    int it = 0;
+    while (it < max_iters) {
+        orc_assign_colors(n_prims, adj_start_num, adj_idx, color, prd_color);
+        int flag = orc_resolve_conflicts_cpu(n_prims, prim_list, adj_start_num,
+                                             adj_idx, color, prd_color);
+        ++it;
+        if (!flag) break;
+    }
+    return it;
+}
+
+void orc_sort_edges_colors(int n, int *color, int *sorted_prim_id)
+{
+    /* stable counting sort on color (colors are >= -1) */
+    if (n <= 0) return;
+    int cmax = -1;
+    for (int i = 0; i < n; ++i) if (color[i] > cmax) cmax = color[i];
+    int nb = cmax + 2;
+    int *cnt = (int *)calloc((size_t)nb + 1, sizeof(int));
+    for (int i = 0; i < n; ++i) cnt[color[i] + 2]++;
+    for (int b = 0; b < nb; ++b) cnt[b + 1] += cnt[b];
+    int *c2 = (int *)malloc(sizeof(int) * (size_t)n);
+    int *s2 = (int *)malloc(sizeof(int) * (size_t)n);
+    for (int i = 0; i < n; ++i) {
+        int pos = cnt[color[i] + 1]++;
+        c2[pos] = color[i];
+        s2[pos] = sorted_prim_id[i];
+    }
+    memcpy(color, c2, sizeof(int) * (size_t)n);
+    memcpy(sorted_prim_id, s2, sizeof(int) * (size_t)n);
+    free(cnt);
+    free(c2);
+    free(s2);
+}
+
+int orc_eval_worksets(int n, const int *sorted_color, int *worksets)
+{
+    int nw = 0;
+    int start = 0;
+    for (int i = 1; i <= n; ++i) {
+        if (i == n || sorted_color[i] != sorted_color[i - 1]) {
+            if (n > 0) {
+                worksets[2 * nw] = start;
+                worksets[2 * nw + 1] = i - start;
+                nw++;
+            }
+            start = i;
+        }
+    }
+    return nw;
+}
+
+/* ------------------------------------------------------------------ */
+/* solver                                                               */
+/* ------------------------------------------------------------------ */
+
+void orc_advect_gpu(int n, float dt, float damp_pow, const float *gravity,
+                    const float *mass, float *vel, float *prdp, const float *pos)
+{
+    f3 g = ld3(gravity);
+    for (int i = 0; i < n; ++i) {
+        f3 v = ld3(vel + 3 * i);
+        /* v += gravity*dt*mass; v *= damping^dt; p = x + v*dt
+         * (P/PBD_cuda.cu:968-972) */
+        f3 gdt = mul(g, dt);
+        v = add(v, mul(gdt, mass[i]));
+        v = mul(v, damp_pow);
+        st3(vel + 3 * i, v);
+        st3(prdp + 3 * i, add(ld3(pos + 3 * i), mul(v, dt)));
+    }
+}
+
+void orc_advect_cpu(int n, float dt, const float *gravity, float *vel,
+                    float *prdp, const float *pos)
+{
+    f3 g = ld3(gravity);
+    for (int i = 0; i < n; ++i) {
+        f3 v = add(ld3(vel + 3 * i), mul(g, dt)); /* P/PBD_cuda.cu:1005 */
+        st3(vel + 3 * i, v);
+        st3(prdp + 3 * i, add(ld3(pos + 3 * i), mul(v, dt)));
+    }
+}
+
+void orc_integrate(int n, float dt, float *vel, const float *prdp, float *pos)
+{
+    for (int i = 0; i < n; ++i) {
+        f3 p = ld3(prdp + 3 * i);
+        st3(vel + 3 * i, divs(sub(p, ld3(pos + 3 * i)), dt));
+        st3(pos + 3 * i, p);
+    }
+}
+
+/* k = 1 - (1-s)^(1/(iter+1)) (P/PBD_cuda.cu:1282); the exponent is computed
+ * in double and narrowed to float by powf's parameter. */
+static inline float stiff_k(float s, int iter)
+{
+    return 1.0f - powf(1.0f - s, (float)(1.0 / (double)(iter + 1)));
+}
+
+static void project_distance(int i0, int i1, float rest, float k,
+                             const float *mass, float *prdp)
+{
+    f3 p0 = ld3(prdp + 3 * i0), p1 = ld3(prdp + 3 * i1);
+    float m0 = mass[i0], m1 = mass[i1];
+    float msum = m0 + m1;
+    float d = dist3(p0, p1);
+    if (msum == 0.0f || d == 0.0f) return;
+    f3 v = sub(p0, p1);
+    /* P/PBD_cuda.cu:1280-1290 */
+    float s0 = -m0 / msum * (d - rest);
+    float s1 = m1 / msum * (d - rest);
+    f3 dp0 = divs(mul(v, s0), d);
+    f3 dp1 = divs(mul(v, s1), d);
+    dp0 = mul(dp0, k);
+    dp1 = mul(dp1, k);
+    st3(prdp + 3 * i0, add(p0, dp0));
+    st3(prdp + 3 * i1, add(ld3(prdp + 3 * i1), dp1));
+}
+
+/* ---- dihedral bending (no reference code: P/PBD_cuda.cu:110-123 is an
+ * empty stub).  Constraint C = theta - theta0 on the signed dihedral angle
+ * theta = atan2((n1^ x n2^).e^, n1^.n2^), projected with the PBD step of
+ * Mueller et al. 2007 (dp_i = -w_i C grad_i / sum_j w_j |grad_j|^2) using the
+ * gradients of Bridson, Marino & Fedkiw 2003: grad_i theta = -u_i with
+ *   u_wA = |E| nA/|nA|^2, u_wB = |E| nB/|nB|^2,
+ *   u_e0 = ((wA-e1).E/|E|) nA/|nA|^2 + ((wB-e1).E/|E|) nB/|nB|^2,
+ *   u_e1 = -((wA-e0).E/|E|) nA/|nA|^2 - ((wB-e0).E/|E|) nB/|nB|^2,
+ * nA = (wA-e0)x(wA-e1), nB = (wB-e1)x(wB-e0), E = e1-e0.
+ * Point order of a bending prim: e0, e1 (hinge), wA, wB (wings). */
+int orc_bending_project_f32(float *P0, float *P1, float *P2, float *P3,
+                            const float *w, float rest_angle, float k)
+{
+    f3 e0 = ld3(P0), e1 = ld3(P1), wa = ld3(P2), wb = ld3(P3);
+    f3 E = sub(e1, e0);
+    f3 na = cross(sub(wa, e0), sub(wa, e1));
+    f3 nb = cross(sub(wb, e1), sub(wb, e0));
+    float na2 = dot(na, na), nb2 = dot(nb, nb), el2 = dot(E, E);
+    if (na2 == 0.0f || nb2 == 0.0f || el2 == 0.0f) return 0;
+    float el = sqrtf(el2);
+    float sn = dot(cross(na, nb), E) / el;
+    float cs = dot(na, nb);
+    float c = atan2f(sn, cs) - rest_angle;
+    if (c > 3.14159265f) c -= 6.28318531f;
+    if (c < -3.14159265f) c += 6.28318531f;
+    f3 a = divs(na, na2), b = divs(nb, nb2);
+    f3 uwa = mul(a, el), uwb = mul(b, el);
+    f3 ue0 = add(mul(a, dot(sub(wa, e1), E) / el), mul(b, dot(sub(wb, e1), E) / el));
+    f3 ue1 = sub(mul(a, -dot(sub(wa, e0), E) / el), mul(b, dot(sub(wb, e0), E) / el));
+    float den = w[0] * dot(ue0, ue0) + w[1] * dot(ue1, ue1) + w[2] * dot(uwa, uwa) +
+                w[3] * dot(uwb, uwb);
+    if (!(den > 0.0f)) return 0;
+    float s = k * c / den;
+    st3(P0, add(e0, mul(ue0, w[0] * s)));
+    st3(P1, add(e1, mul(ue1, w[1] * s)));
+    st3(P2, add(wa, mul(uwa, w[2] * s)));
+    st3(P3, add(wb, mul(uwb, w[3] * s)));
+    return 1;
+}
+
+typedef struct { double x, y, z; } d3;
+static inline d3 dmk(double x, double y, double z) { d3 r = {x, y, z}; return r; }
+static inline d3 dld(const double *p) { return dmk(p[0], p[1], p[2]); }
+static inline void dst(double *p, d3 v) { p[0] = v.x; p[1] = v.y; p[2] = v.z; }
+static inline d3 dadd(d3 a, d3 b) { return dmk(a.x + b.x, a.y + b.y, a.z + b.z); }
+static inline d3 dsub(d3 a, d3 b) { return dmk(a.x - b.x, a.y - b.y, a.z - b.z); }
+static inline d3 dmul(d3 a, double s) { return dmk(a.x * s, a.y * s, a.z * s); }
+static inline double ddot(d3 a, d3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+static inline d3 dcross(d3 a, d3 b)
+{
+    return dmk(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
+}
+
+double orc_dihedral_angle(const double *P0, const double *P1, const double *P2,
+                          const double *P3)
+{
+    d3 e0 = dld(P0), e1 = dld(P1), wa = dld(P2), wb = dld(P3);
+    d3 E = dsub(e1, e0);
+    d3 na = dcross(dsub(wa, e0), dsub(wa, e1));
+    d3 nb = dcross(dsub(wb, e1), dsub(wb, e0));
+    double el = sqrt(ddot(E, E));
+    if (el == 0.0) return 0.0;
+    return atan2(ddot(dcross(na, nb), E) / el, ddot(na, nb));
+}
+
+int orc_bending_project_f64(double *P0, double *P1, double *P2, double *P3,
+                            const double *w, double rest_angle, double k)
+{
+    d3 e0 = dld(P0), e1 = dld(P1), wa = dld(P2), wb = dld(P3);
+    d3 E = dsub(e1, e0);
+    d3 na = dcross(dsub(wa, e0), dsub(wa, e1));
+    d3 nb = dcross(dsub(wb, e1), dsub(wb, e0));
+    double na2 = ddot(na, na), nb2 = ddot(nb, nb), el2 = ddot(E, E);
+    if (na2 == 0.0 || nb2 == 0.0 || el2 == 0.0) return 0;
+    double el = sqrt(el2);
+    double c = atan2(ddot(dcross(na, nb), E) / el, ddot(na, nb)) - rest_angle;
+    if (c > M_PI) c -= 2.0 * M_PI;
+    if (c < -M_PI) c += 2.0 * M_PI;
+    d3 a = dmul(na, 1.0 / na2), b = dmul(nb, 1.0 / nb2);
+    d3 uwa = dmul(a, el), uwb = dmul(b, el);
+    d3 ue0 = dadd(dmul(a, ddot(dsub(wa, e1), E) / el), dmul(b, ddot(dsub(wb, e1), E) / el));
+    d3 ue1 = dsub(dmul(a, -ddot(dsub(wa, e0), E) / el), dmul(b, ddot(dsub(wb, e0), E) / el));
+    double den = w[0] * ddot(ue0, ue0) + w[1] * ddot(ue1, ue1) + w[2] * ddot(uwa, uwa) +
+                 w[3] * ddot(uwb, uwb);
+    if (!(den > 0.0)) return 0;
+    double s = k * c / den;
+    dst(P0, dadd(e0, dmul(ue0, w[0] * s)));
+    dst(P1, dadd(e1, dmul(ue1, w[1] * s)));
+    dst(P2, dadd(wa, dmul(uwa, w[2] * s)));
+    dst(P3, dadd(wb, dmul(uwb, w[3] * s)));
+    return 1;
+}
+
+static void project_bending(const orc_constraints *c, int prim, float k,
+                            const float *mass, float *prdp, int fp64)
+{
+    const int *ix = c->indices + c->prim_list[2 * prim];
+    float rest = c->rest_angle ? c->rest_angle[prim] : 0.0f;
+    if (!fp64) {
+        float w[4] = {mass[ix[0]], mass[ix[1]], mass[ix[2]], mass[ix[3]]};
+        orc_bending_project_f32(prdp + 3 * ix[0], prdp + 3 * ix[1], prdp + 3 * ix[2],
+                                prdp + 3 * ix[3], w, rest, k);
+        return;
+    }
+    double p[4][3], w[4];
+    for (int j = 0; j < 4; ++j) {
+        for (int d = 0; d < 3; ++d) p[j][d] = prdp[3 * ix[j] + d];
+        w[j] = mass[ix[j]];
+    }
+    if (orc_bending_project_f64(p[0], p[1], p[2], p[3], w, rest, k))
+        for (int j = 0; j < 4; ++j)
+            for (int d = 0; d < 3; ++d) prdp[3 * ix[j] + d] = (float)p[j][d];
+}
+
+void orc_project_one(const orc_constraints *c, int prim, int iter,
+                     const float *mass, float *prdp, int bending_fp64)
+{
+    int t = c->ctype[prim];
+    int s = c->prim_list[2 * prim];
+    if (t == ORC_DISTANCE) {
+        float k = stiff_k(c->stiffness[prim], iter);
+        project_distance(c->indices[s], c->indices[s + 1], c->rest_length[prim], k,
+                         mass, prdp);
+    } else if (t == ORC_BENDING) {
+        float k = stiff_k(c->stiffness[prim], iter);
+        project_bending(c, prim, k, mass, prdp, bending_fp64);
+    } else if (t == ORC_ANCHOR) {
+        /* anchor: snap the point to its rest position (P/PBD_cuda.cu:1298-1305,
+         * with the rest position stored per anchor prim) */
+        if (c->rest_pos) {
+            int i = c->indices[s];
+            prdp[3 * i] = c->rest_pos[3 * prim];
+            prdp[3 * i + 1] = c->rest_pos[3 * prim + 1];
+            prdp[3 * i + 2] = c->rest_pos[3 * prim + 2];
+        }
+    }
+}
+
+void orc_project_colored(const orc_constraints *c, const int *sorted_prim_id,
+                         int n_worksets, const int *worksets, int iter_begin,
+                         int iter_end, const float *mass, float *prdp,
+                         int bending_fp64)
+{
+    for (int it = iter_begin; it < iter_end; ++it)
+        for (int w = 0; w < n_worksets; ++w)
+            for (int i = worksets[2 * w]; i < worksets[2 * w] + worksets[2 * w + 1]; ++i)
+                orc_project_one(c, sorted_prim_id[i], it, mass, prdp, bending_fp64);
+}
+
+void orc_colli_sphere(int n, float *prdp, const float *center, float radius)
+{
+    f3 o = ld3(center);
+    for (int i = 0; i < n; ++i) {
+        f3 p = ld3(prdp + 3 * i);
+        float d = dist3(p, o);
+        if (d - radius > 0.001f) continue; /* ColliderSphere, P/PBD_cuda.cu:1542-1553 */
+        /* GenerateMoveVectorSphere (P/PBD_cuda.cu:1567-1573) */
+        float move = radius - dist3(o, p);
+        f3 dir = divs(sub(p, o), dist3(o, p));
+        st3(prdp + 3 * i, add(p, mul(dir, move)));
+    }
+}
+
+void orc_project_cpu(const orc_constraints *c, int iterations,
+                     const float *mass, float *prdp, int n_points,
+                     const float *sphere_center, float sphere_radius)
+{
+    for (int ii = 0; ii < iterations; ++ii) {
+        for (int i = 0; i < c->n_prims; ++i) {
+            if (c->prim_list[2 * i + 1] != 2) continue;
+            int i0 = c->indices[c->prim_list[2 * i]];
+            int i1 = c->indices[c->prim_list[2 * i] + 1];
+            f3 p0 = ld3(prdp + 3 * i0), p1 = ld3(prdp + 3 * i1);
+            float d = dist3(p0, p1);
+            /* normalize as compiled in the reference's .cu translation unit:
+             * the host rsqrtf there evaluates 1/sqrt in double */
+            f3 r0 = sub(p0, p1);
+            f3 r = mul(r0, (float)(1.0 / sqrt((double)dot(r0, r0))));
+            float m0 = mass[i0], m1 = mass[i1];
+            float rest = c->rest_length[i];
+            /* P/PBD_cuda.cu:1113-1123, k = 1 */
+            f3 dp1 = mk(-m0 / (m0 + m1) * (d - rest) * r.x, -m0 / (m0 + m1) * (d - rest) * r.y,
+                        -m0 / (m0 + m1) * (d - rest) * r.z);
+            f3 dp2 = mk(m1 / (m0 + m1) * (d - rest) * r.x, m1 / (m0 + m1) * (d - rest) * r.y,
+                        m1 / (m0 + m1) * (d - rest) * r.z);
+            dp1 = mul(dp1, 1.0f);
+            dp2 = mul(dp2, 1.0f);
+            st3(prdp + 3 * i0, add(p0, dp1));
+            st3(prdp + 3 * i1, add(ld3(prdp + 3 * i1), dp2));
+        }
+        if (sphere_center) orc_colli_sphere(n_points, prdp, sphere_center, sphere_radius);
+    }
+}
+
+double orc_residual(const orc_constraints *c, const float *prdp,
+                    const float *hinge_rest, double *num_out, double *den_out)
+{
+    double num = 0.0, den = 0.0;
+    for (int p = 0; p < c->n_prims; ++p) {
+        const int *ix = c->indices + c->prim_list[2 * p];
+        if (c->ctype[p] == ORC_DISTANCE) {
+            double d[3];
+            for (int k = 0; k < 3; ++k) d[k] = (double)prdp[3 * ix[0] + k] - prdp[3 * ix[1] + k];
+            double l = c->rest_length[p];
+            double cc = sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]) - l;
+            num += cc * cc;
+            den += l * l;
+        } else if (c->ctype[p] == ORC_BENDING) {
+            double q[4][3];
+            for (int j = 0; j < 4; ++j)
+                for (int k = 0; k < 3; ++k) q[j][k] = prdp[3 * ix[j] + k];
+            double th = orc_dihedral_angle(q[0], q[1], q[2], q[3]);
+            double cc = th - (c->rest_angle ? c->rest_angle[p] : 0.0);
+            if (cc > M_PI) cc -= 2.0 * M_PI;
+            if (cc < -M_PI) cc += 2.0 * M_PI;
+            double e[3];
+            for (int k = 0; k < 3; ++k) e[k] = q[1][k] - q[0][k];
+            double el = sqrt(e[0] * e[0] + e[1] * e[1] + e[2] * e[2]);
+            double lr = hinge_rest ? hinge_rest[p] : el;
+            num += (cc * el) * (cc * el);
+            den += lr * lr;
+        }
+    }
+    if (num_out) *num_out = num;
+    if (den_out) *den_out = den;
+    return den > 0.0 ? sqrt(num) / sqrt(den) : 0.0;
+}
+
+/* ------------------------------------------------------------------ */
+/* broadphase                                                           */
+/* ------------------------------------------------------------------ */
+
+void orc_grid_init(orc_grid *g, const float *center, const int *size,
+                   const float *cell, int bounded)
+{
+    for (int k = 0; k < 3; ++k) {
+        g->size[k] = size ? size[k] : 0;
+        g->cell[k] = cell[k];
+        /* shift = (gridSize * cellSize) / 2 (P/SpatialHashSystem.cpp:91-94) */
+        float shift = ((float)(unsigned)g->size[k] * cell[k]) / 2.0f;
+        g->start[k] = center[k] - shift;
+    }
+    g->bounded = bounded;
+}
+
+static inline void tri_cell(const orc_grid *g, const int *tri, const float *pos,
+                            int *out)
+{
+    f3 a = ld3(pos + 3 * tri[0]), b = ld3(pos + 3 * tri[1]), c = ld3(pos + 3 * tri[2]);
+    /* centroid (P/SpatialHashSystem.cpp:291-293) and cell
+     * (P/SpatialHashSystem.cpp:394-396) */
+    float cx = (a.x + b.x + c.x) / 3.0f;
+    float cy = (a.y + b.y + c.y) / 3.0f;
+    float cz = (a.z + b.z + c.z) / 3.0f;
+    out[0] = (int)floorf((cx - g->start[0]) / g->cell[0]);
+    out[1] = (int)floorf((cy - g->start[1]) / g->cell[1]);
+    out[2] = (int)floorf((cz - g->start[2]) / g->cell[2]);
+}
+
+void orc_tri_cells(const orc_grid *g, int n_tris, const int *tri_idx,
+                   const float *pos, int *cell_xyz)
+{
+    for (int t = 0; t < n_tris; ++t) tri_cell(g, tri_idx + 3 * t, pos, cell_xyz + 3 * t);
+}
+
+static inline int outside(const orc_grid *g, const int *c)
+{
+    return c[0] < 0 || c[1] < 0 || c[2] < 0 || c[0] >= g->size[0] ||
+           c[1] >= g->size[1] || c[2] >= g->size[2];
+}
+
+int orc_cell_hash(const orc_grid *g, const int *c)
+{
+    if (outside(g, c)) return -1;
+    return (int)(((unsigned)c[2] * (unsigned)g->size[1]) * (unsigned)g->size[0] +
+                 (unsigned)c[1] * (unsigned)g->size[0] + (unsigned)c[0]);
+}
+
+/* 64-bit key of an unbounded cell: 21 bits per axis, offset 2^20 */
+static inline uint64_t cell_key(const int *c)
+{
+    return ((uint64_t)(uint32_t)(c[2] + (1 << 20)) << 42) |
+           ((uint64_t)(uint32_t)(c[1] + (1 << 20)) << 21) |
+           (uint64_t)(uint32_t)(c[0] + (1 << 20));
+}
+
+typedef struct { uint64_t key; int id; } keyid;
+static int cmp_keyid(const void *a, const void *b)
+{
+    const keyid *x = (const keyid *)a, *y = (const keyid *)b;
+    if (x->key != y->key) return x->key < y->key ? -1 : 1;
+    return x->id - y->id; /* stable: ties by id */
+}
+
+/* sorted (cell key, triangle id) table with lookup */
+typedef struct { keyid *e; int n; } cell_table;
+
+static cell_table build_table(const orc_grid *g, int n_tris, const int *tri_idx,
+                              const float *pos, int *cells)
+{
+    cell_table t;
+    t.e = (keyid *)malloc(sizeof(keyid) * (size_t)(n_tris > 0 ? n_tris : 1));
+    t.n = 0;
+    for (int i = 0; i < n_tris; ++i) {
+        tri_cell(g, tri_idx + 3 * i, pos, cells + 3 * i);
+        if (g->bounded && outside(g, cells + 3 * i)) continue;
+        uint64_t k = g->bounded ? (uint64_t)orc_cell_hash(g, cells + 3 * i)
+                                : cell_key(cells + 3 * i);
+        t.e[t.n].key = k;
+        t.e[t.n].id = i;
+        t.n++;
+    }
+    qsort(t.e, (size_t)t.n, sizeof(keyid), cmp_keyid);
+    return t;
+}
+
+static int table_lower(const cell_table *t, uint64_t key)
+{
+    int lo = 0, hi = t->n;
+    while (lo < hi) {
+        int mid = (lo + hi) >> 1;
+        if (t->e[mid].key < key) lo = mid + 1; else hi = mid;
+    }
+    return lo;
+}
+
+int64_t orc_find_neighbors_all(const orc_grid *g, int n_tris, const int *tri_idx,
+                               const float *pos, int *out_start_num, int *out_idx)
+{
+    int *cells = (int *)malloc(sizeof(int) * 3 * (size_t)(n_tris > 0 ? n_tris : 1));
+    cell_table t = build_table(g, n_tris, tri_idx, pos, cells);
+    int64_t total = 0;
+    for (int tri = 0; tri < n_tris; ++tri) {
+        int64_t start = total;
+        const int *c = cells + 3 * tri;
+        if (!(g->bounded && outside(g, c))) {
+            for (int z = -1; z <= 1; ++z)
+                for (int y = -1; y <= 1; ++y)
+                    for (int x = -1; x <= 1; ++x) {
+                        int nc[3] = {c[0] + x, c[1] + y, c[2] + z};
+                        if (g->bounded && outside(g, nc)) continue;
+                        uint64_t key = g->bounded ? (uint64_t)orc_cell_hash(g, nc) : cell_key(nc);
+                        for (int i = table_lower(&t, key); i < t.n && t.e[i].key == key; ++i) {
+                            if (t.e[i].id == tri) continue;
+                            if (out_idx) out_idx[total] = t.e[i].id;
+                            total++;
+                        }
+                    }
+        }
+        if (out_start_num) {
+            out_start_num[2 * tri] = (int)start;
+            out_start_num[2 * tri + 1] = (int)(total - start);
+        }
+    }
+    free(t.e);
+    free(cells);
+    return total;
+}
+
+/* ------------------------------------------------------------------ */
+/* narrowphase                                                          */
+/* ------------------------------------------------------------------ */
+
+static inline double sgn(double x) { return x < 0 ? -1.0 : 1.0; }
+
+int orc_solve_quadratic(double a, double b, double c, double x[2])
+{
+    /* P/CCD.cpp:96-113 */
+    double d = b * b - 4 * a * c;
+    if (d < 0) {
+        x[0] = -b / (2 * a);
+        return 0;
+    }
+    double q = -(b + sgn(b) * sqrt(d)) / 2;
+    int i = 0;
+    if (fabs(a) > 1e-12 * fabs(q)) x[i++] = q / a;
+    if (fabs(q) > 1e-12 * fabs(c)) x[i++] = c / q;
+    if (i == 2 && x[0] > x[1]) {
+        double s = x[0];
+        x[0] = x[1];
+        x[1] = s;
+    }
+    return i;
+}
+
+double orc_newtons_method(double a, double b, double c, double d, double x0,
+                          int init_dir)
+{
+    /* P/CCD.cpp:75-94 */
+    if (init_dir != 0) {
+        double y0 = d + x0 * (c + x0 * (b + x0 * a));
+        double ddy0 = 2 * b + x0 * (6 * a);
+        x0 += init_dir * sqrt(fabs(2 * y0 / ddy0));
+    }
+    for (int iter = 0; iter < 100; iter++) {
+        double y = d + x0 * (c + x0 * (b + x0 * a));
+        double dy = c + x0 * (2 * b + x0 * 3 * a);
+        if (dy == 0) return x0;
+        double x1 = x0 - y / dy;
+        if (fabs(x0 - x1) < 1e-6) return x0;
+        x0 = x1;
+    }
+    return x0;
+}
+
+int orc_solve_cubic(double a, double b, double c, double d, double x[3])
+{
+    /* P/CCD.cpp:48-73.  When the derivative quadratic yields no critical
+     * point without writing one (d >= 0 and both guards fail), the reference
+     * starts Newton from an uninitialised value; 0.0 is used here. */
+    double xc[2] = {0.0, 0.0};
+    int ncrit = orc_solve_quadratic(3 * a, 2 * b, c, xc);
+    if (ncrit == 0) {
+        x[0] = orc_newtons_method(a, b, c, d, xc[0], 0);
+        return 1;
+    } else if (ncrit == 1) {
+        return orc_solve_quadratic(b, c, d, x);
+    } else {
+        double yc[2] = {d + xc[0] * (c + xc[0] * (b + xc[0] * a)),
+                        d + xc[1] * (c + xc[1] * (b + xc[1] * a))};
+        int i = 0;
+        if (yc[0] * a >= 0) x[i++] = orc_newtons_method(a, b, c, d, xc[0], -1);
+        if (yc[0] * yc[1] <= 0) {
+            int closer = fabs(yc[0]) < fabs(yc[1]) ? 0 : 1;
+            x[i++] = orc_newtons_method(a, b, c, d, xc[closer], closer == 0 ? 1 : -1);
+        }
+        if (yc[1] * a <= 0) x[i++] = orc_newtons_method(a, b, c, d, xc[1], 1);
+        return i;
+    }
+}
+
+static void sort_small(double *t, int n)
+{
+    for (int i = 1; i < n; ++i) {
+        double v = t[i];
+        int j = i - 1;
+        while (j >= 0 && t[j] > v) {
+            t[j + 1] = t[j];
+            --j;
+        }
+        t[j + 1] = v;
+    }
+}
+
+/* cubic coefficients of the coplanarity condition (P/CCD.cpp:1740-1743) */
+static void vf_cubic(const float *x, const float *p, double *a)
+{
+    f3 x0 = ld3(x), v0 = sub(ld3(p), x0);
+    f3 x1 = sub(ld3(x + 3), x0), x2 = sub(ld3(x + 6), x0), x3 = sub(ld3(x + 9), x0);
+    f3 v1 = sub(sub(ld3(p + 3), ld3(x + 3)), v0);
+    f3 v2 = sub(sub(ld3(p + 6), ld3(x + 6)), v0);
+    f3 v3 = sub(sub(ld3(p + 9), ld3(x + 9)), v0);
+    a[0] = stp(x1, x2, x3);
+    a[1] = stp(v1, x2, x3) + stp(x1, v2, x3) + stp(x1, x2, v3);
+    a[2] = stp(x1, v2, v3) + stp(v1, x2, v3) + stp(v1, v2, x3);
+    a[3] = stp(v1, v2, v3);
+}
+
+/* inside test with the thickness-relative epsilon (P/CCD.cpp:1768-1781);
+ * the division by 3.0 is in double */
+static inline int inside_eps(f3 w, float e1, float e2, float e3, float thickness)
+{
+    float eps = (float)((double)thickness / ((double)(e1 + e2 + e3) / 3.0));
+    return (w.x <= (1 + eps)) && (w.x >= (-eps)) && (w.y <= (1 + eps)) &&
+           (w.y >= (-eps)) && (w.z <= (1 + eps)) && (w.z >= (-eps));
+}
+
+int orc_extended_vf_test(const float *x, const float *p, float thickness,
+                         int i0, int i1, int i2, int i3, orc_contact *ct)
+{
+    if (i0 == i1 || i0 == i2 || i0 == i3) return 0;
+    double a[4];
+    vf_cubic(x, p, a);
+    double t[5];
+    int nsol = orc_solve_cubic(a[3], a[2], a[1], a[0], t);
+    t[nsol] = 1;
+    t[nsol + 1] = 0;
+    sort_small(t, nsol + 2);
+    f3 X0 = ld3(x), X1 = ld3(x + 3), X2 = ld3(x + 6), X3 = ld3(x + 9);
+    f3 P0 = ld3(p), P1 = ld3(p + 3), P2 = ld3(p + 6), P3 = ld3(p + 9);
+    for (int i = 0; i < nsol + 2; ++i) {
+        if (t[i] < 0 || t[i] > 1) continue;
+        f3 c0 = lerp_t(X0, P0, t[i]), c1 = lerp_t(X1, P1, t[i]);
+        f3 c2 = lerp_t(X2, P2, t[i]), c3 = lerp_t(X3, P3, t[i]);
+        f3 n = nrm(cross(sub(P2, P1), sub(P3, P1)));
+        f3 cn = nrm(cross(sub(c2, c1), sub(c3, c1)));
+        double dist = dot(sub(c0, c1), cn);
+        f3 w = bary(c0, c1, c2, c3);
+        if (ct) {
+            ct->t = (float)t[i];
+            ct->n[0] = n.x; ct->n[1] = n.y; ct->n[2] = n.z;
+            ct->w[0] = 1; ct->w[1] = w.x; ct->w[2] = w.y; ct->w[3] = w.z;
+        }
+        int in = inside_eps(w, dist3(c1, c2), dist3(c1, c3), dist3(c2, c3), thickness);
+        /* P/CCD.cpp:1800 */
+        if ((fabs(dist) - (double)(2.0f * thickness) < -1e-6) && in) return 1;
+    }
+    return 0;
+}
+
+int orc_narrow_vf_ccd_test(const float *x, const float *p, float thickness,
+                           int i0, int i1, int i2, int i3, orc_contact *ct)
+{
+    if (i0 == i1 || i0 == i2 || i0 == i3) return 0;
+    double a[4];
+    vf_cubic(x, p, a);
+    double t[4];
+    int nsol = orc_solve_cubic(a[3], a[2], a[1], a[0], t);
+    f3 X0 = ld3(x), X1 = ld3(x + 3), X2 = ld3(x + 6), X3 = ld3(x + 9);
+    f3 P0 = ld3(p), P1 = ld3(p + 3), P2 = ld3(p + 6), P3 = ld3(p + 9);
+    for (int i = 0; i < nsol; ++i) {
+        if (t[i] < 0 || t[i] > 1) continue;
+        f3 c0 = lerp_t(X0, P0, t[i]), c1 = lerp_t(X1, P1, t[i]);
+        f3 c2 = lerp_t(X2, P2, t[i]), c3 = lerp_t(X3, P3, t[i]);
+        f3 n = nrm(cross(sub(P2, P1), sub(P3, P1)));
+        f3 cn = nrm(cross(sub(c2, c1), sub(c3, c1)));
+        double d = dot(sub(c0, c1), cn);
+        f3 w = bary(c0, c1, c2, c3);
+        if (ct) {
+            ct->t = (float)t[i];
+            ct->n[0] = n.x; ct->n[1] = n.y; ct->n[2] = n.z;
+            ct->w[0] = 1; ct->w[1] = w.x; ct->w[2] = w.y; ct->w[3] = w.z;
+        }
+        /* P/CCD.cpp:1845-1863: epsilon from the predicted edges */
+        int in = inside_eps(w, dist3(P1, P2), dist3(P1, P3), dist3(P2, P3), thickness);
+        if (fabs(d) < 1e-6 && in) return 1;
+    }
+    return 0;
+}
+
+static void gather4(const int *ids, const float *src, float *dst)
+{
+    for (int j = 0; j < 4; ++j)
+        for (int k = 0; k < 3; ++k) dst[3 * j + k] = src[3 * ids[j] + k];
+}
+
+int64_t orc_ccd_sh_extended_ref(const orc_grid *g, int n_tris, const int *tri_idx,
+                                const float *pos, const float *prdp,
+                                float thickness, orc_contact *out, int64_t cap)
+{
+    /* UpdateSH(prdP) then, per triangle, FindNeighbors and the
+     * point x neighbor loop (P/CCD.cpp:1530-1586) */
+    int64_t nn = orc_find_neighbors_all(g, n_tris, tri_idx, prdp, NULL, NULL);
+    int *sn = (int *)malloc(sizeof(int) * 2 * (size_t)(n_tris > 0 ? n_tris : 1));
+    int *nb = (int *)malloc(sizeof(int) * (size_t)(nn > 0 ? nn : 1));
+    orc_find_neighbors_all(g, n_tris, tri_idx, prdp, sn, nb);
+    int64_t h = 0;
+    int64_t hcap = 1024;
+    int *keys = (int *)malloc(sizeof(int) * 4 * (size_t)hcap);
+    for (int tri = 0; tri < n_tris; ++tri) {
+        for (int j = 0; j < 3; ++j) {
+            int ids[4];
+            ids[0] = tri_idx[3 * tri + j];
+            for (int q = sn[2 * tri]; q < sn[2 * tri] + sn[2 * tri + 1]; ++q) {
+                int nt = nb[q];
+                ids[1] = tri_idx[3 * nt];
+                ids[2] = tri_idx[3 * nt + 1];
+                ids[3] = tri_idx[3 * nt + 2];
+                float xs[12], ps[12];
+                gather4(ids, pos, xs);
+                gather4(ids, prdp, ps);
+                orc_contact ct;
+                if (!orc_extended_vf_test(xs, ps, thickness, ids[0], ids[1], ids[2], ids[3], &ct))
+                    continue;
+                /* IsDuplicated: linear scan of the stored contacts */
+                int dup = 0;
+                for (int64_t k = 0; k < h; ++k)
+                    if (keys[4 * k] == ids[0] && keys[4 * k + 1] == ids[1] &&
+                        keys[4 * k + 2] == ids[2] && keys[4 * k + 3] == ids[3]) {
+                        dup = 1;
+                        break;
+                    }
+                if (dup) continue;
+                if (h == hcap) {
+                    hcap *= 2;
+                    keys = (int *)realloc(keys, sizeof(int) * 4 * (size_t)hcap);
+                }
+                memcpy(keys + 4 * h, ids, sizeof(ids));
+                ct.v = ids[0]; ct.f0 = ids[1]; ct.f1 = ids[2]; ct.f2 = ids[3];
+                ct.face = nt;
+                if (out && h < cap) out[h] = ct;
+                h++;
+            }
+        }
+    }
+    free(keys);
+    free(sn);
+    free(nb);
+    return h;
+}
+
+typedef struct { int face; orc_contact c; } hit_rec;
+static int cmp_hit(const void *a, const void *b)
+{
+    return ((const hit_rec *)a)->face - ((const hit_rec *)b)->face;
+}
+
+int64_t orc_ccd_vf_pairs(const orc_grid *g, int n_points, int n_tris,
+                         const int *tri_idx, const int *tri_inst,
+                         const int *point_inst, const float *pos,
+                         const float *prdp, float thickness, orc_contact *out,
+                         int64_t cap)
+{
+    int *cells = (int *)malloc(sizeof(int) * 3 * (size_t)(n_tris > 0 ? n_tris : 1));
+    cell_table t = build_table(g, n_tris, tri_idx, prdp, cells);
+    /* point -> incident triangles */
+    int *pc = (int *)calloc((size_t)n_points + 1, sizeof(int));
+    for (int i = 0; i < 3 * n_tris; ++i) pc[tri_idx[i] + 1]++;
+    for (int i = 0; i < n_points; ++i) pc[i + 1] += pc[i];
+    int *pt = (int *)malloc(sizeof(int) * (size_t)(3 * n_tris > 0 ? 3 * n_tris : 1));
+    int *fill = (int *)malloc(sizeof(int) * ((size_t)n_points + 1));
+    memcpy(fill, pc, sizeof(int) * ((size_t)n_points + 1));
+    for (int i = 0; i < 3 * n_tris; ++i) pt[fill[tri_idx[i]]++] = i / 3;
+    int64_t h = 0;
+    int hcap = 256;
+    hit_rec *hits = (hit_rec *)malloc(sizeof(hit_rec) * (size_t)hcap);
+    int *cc = (int *)malloc(sizeof(int) * 3 * 64);
+    for (int v = 0; v < n_points; ++v) {
+        /* centroid cells of the incident triangles (those in the grid) */
+        int nc = 0;
+        for (int q = pc[v]; q < pc[v + 1] && nc < 64; ++q) {
+            const int *c = cells + 3 * pt[q];
+            if (g->bounded && outside(g, c)) continue;
+            cc[3 * nc] = c[0]; cc[3 * nc + 1] = c[1]; cc[3 * nc + 2] = c[2];
+            nc++;
+        }
+        if (nc == 0) continue;
+        int lo[3], hi[3];
+        for (int k = 0; k < 3; ++k) { lo[k] = cc[k]; hi[k] = cc[k]; }
+        for (int i = 1; i < nc; ++i)
+            for (int k = 0; k < 3; ++k) {
+                if (cc[3 * i + k] < lo[k]) lo[k] = cc[3 * i + k];
+                if (cc[3 * i + k] > hi[k]) hi[k] = cc[3 * i + k];
+            }
+        int nh = 0;
+        for (int z = lo[2] - 1; z <= hi[2] + 1; ++z)
+            for (int y = lo[1] - 1; y <= hi[1] + 1; ++y)
+                for (int x = lo[0] - 1; x <= hi[0] + 1; ++x) {
+                    int cell[3] = {x, y, z};
+                    int near = 0;
+                    for (int i = 0; i < nc && !near; ++i)
+                        near = abs(cc[3 * i] - x) <= 1 && abs(cc[3 * i + 1] - y) <= 1 &&
+                               abs(cc[3 * i + 2] - z) <= 1;
+                    if (!near) continue;
+                    if (g->bounded && outside(g, cell)) continue;
+                    uint64_t key = g->bounded ? (uint64_t)orc_cell_hash(g, cell) : cell_key(cell);
+                    for (int e = table_lower(&t, key); e < t.n && t.e[e].key == key; ++e) {
+                        int f = t.e[e].id;
+                        if (tri_inst && point_inst && tri_inst[f] != point_inst[v]) continue;
+                        int ids[4] = {v, tri_idx[3 * f], tri_idx[3 * f + 1], tri_idx[3 * f + 2]};
+                        float xs[12], ps[12];
+                        gather4(ids, pos, xs);
+                        gather4(ids, prdp, ps);
+                        orc_contact ct;
+                        if (!orc_extended_vf_test(xs, ps, thickness, ids[0], ids[1], ids[2],
+                                                  ids[3], &ct))
+                            continue;
+                        ct.v = ids[0]; ct.f0 = ids[1]; ct.f1 = ids[2]; ct.f2 = ids[3];
+                        ct.face = f;
+                        if (nh == hcap) {
+                            hcap *= 2;
+                            hits = (hit_rec *)realloc(hits, sizeof(hit_rec) * (size_t)hcap);
+                        }
+                        hits[nh].face = f;
+                        hits[nh].c = ct;
+                        nh++;
+                    }
+                }
+        qsort(hits, (size_t)nh, sizeof(hit_rec), cmp_hit);
+        for (int i = 0; i < nh; ++i) {
+            if (out && h < cap) out[h] = hits[i].c;
+            h++;
+        }
+    }
+    free(cc);
+    free(hits);
+    free(pc);
+    free(pt);
+    free(fill);
+    free(t.e);
+    free(cells);
+    return h;
+}
+
+/* RelativePos (P/CCD.cpp:13-25): side of the start-of-step plane */
+static inline int side_of(f3 v, f3 p, f3 n) { return dot(sub(v, p), n) >= 0; }
+
+int orc_vf_resolve_test(const float *x, const float *p, float thickness)
+{
+    /* P/CCD.cpp:1996-2032 */
+    f3 X0 = ld3(x), X1 = ld3(x + 3), X2 = ld3(x + 6), X3 = ld3(x + 9);
+    f3 P0 = ld3(p), P1 = ld3(p + 3), P2 = ld3(p + 6), P3 = ld3(p + 9);
+    f3 fn = nrm(cross(sub(X2, X1), sub(X3, X1)));
+    int dir = side_of(X0, X1, fn);
+    f3 pn = nrm(cross(sub(P2, P1), sub(P3, P1)));
+    f3 pr = cross(sub(P2, P1), sub(P3, P1));
+    if ((double)dot(pr, pr) <= 1e-6) return 0;
+    float depth = (float)((double)dot(sub(P0, P1), mul(pn, dir ? 1.0f : -1.0f)) -
+                          2.0 * (double)thickness);
+    return !(depth >= -1e-6);
+}
+
+void orc_vf_resolve_new(const float *x, float *p, float thickness)
+{
+    /* P/CCD.cpp:2034-2077 */
+    f3 X0 = ld3(x), X1 = ld3(x + 3), X2 = ld3(x + 6), X3 = ld3(x + 9);
+    f3 P0 = ld3(p), P1 = ld3(p + 3), P2 = ld3(p + 6), P3 = ld3(p + 9);
+    f3 fn = nrm(cross(sub(X2, X1), sub(X3, X1)));
+    int dir = side_of(X0, X1, fn);
+    f3 pn = nrm(cross(sub(P2, P1), sub(P3, P1)));
+    float sg = dir ? 1.0f : -1.0f;
+    f3 p1proj = add(P1, mul(mul(mul(pn, sg), 2.0f), thickness));
+    float depth = (float)((double)dot(sub(p1proj, P0), mul(pn, sg)) * 0.5);
+    f3 vfix = mul(mul(pn, sg), depth);
+    f3 ffix = mul(mul(pn, -sg), depth);
+    f3 w = bary(P0, P1, P2, P3);
+    float sw = w.x * w.x + w.y * w.y + w.z * w.z;
+    st3(p, add(P0, vfix));
+    st3(p + 3, add(P1, divs(mul(ffix, w.x), sw)));
+    st3(p + 6, add(P2, divs(mul(ffix, w.y), sw)));
+    st3(p + 9, add(P3, divs(mul(ffix, w.z), sw)));
+}
+
+void orc_collision_resolve_ref(int n_contacts, const orc_contact *cts,
+                               const float *pos, float *prdp, int iterations,
+                               float thickness)
+{
+    for (int it = 0; it < iterations; ++it)
+        for (int c = 0; c < n_contacts; ++c) {
+            int ids[4] = {cts[c].v, cts[c].f0, cts[c].f1, cts[c].f2};
+            float xs[12], ps[12];
+            gather4(ids, pos, xs);
+            gather4(ids, prdp, ps);
+            if (!orc_vf_resolve_test(xs, ps, thickness)) continue;
+            orc_vf_resolve_new(xs, ps, thickness);
+            for (int j = 0; j < 4; ++j)
+                for (int k = 0; k < 3; ++k) prdp[3 * ids[j] + k] = ps[3 * j + k];
+        }
+}
+
+int orc_vf_resolve_deltas(const float *x, const float *p, const float *wm,
+                          float thickness, int mass_weighted, float *delta)
+{
+    f3 X0 = ld3(x), X1 = ld3(x + 3), X2 = ld3(x + 6), X3 = ld3(x + 9);
+    f3 P0 = ld3(p), P1 = ld3(p + 3), P2 = ld3(p + 6), P3 = ld3(p + 9);
+    f3 e1 = sub(P2, P1), e2 = sub(P3, P1);
+    f3 pr = cross(e1, e2);
+    float pr2 = dot(pr, pr);
+    if (!mass_weighted) {
+        /* reference degeneracy guard: |n|^2 <= 1e-6 (P/CCD.cpp:2007) */
+        if ((double)pr2 <= 1e-6) return 0;
+    } else {
+        /* scale-free guard: sin^2 of the corner angle <= 1e-12 */
+        if (!(pr2 > 1e-12f * (dot(e1, e1) * dot(e2, e2)))) return 0;
+    }
+    f3 fn = nrm(cross(sub(X2, X1), sub(X3, X1)));
+    int dir = side_of(X0, X1, fn);
+    f3 pn = nrm(pr);
+    float sg = dir ? 1.0f : -1.0f;
+    f3 ns = mul(pn, sg);
+    float gap = (float)((double)dot(sub(P0, P1), ns) - 2.0 * (double)thickness);
+    if (gap >= -1e-6f) return 0;
+    f3 p1proj = add(P1, mul(mul(ns, 2.0f), thickness));
+    float depth = (float)((double)dot(sub(p1proj, P0), ns) * 0.5);
+    f3 w = bary(P0, P1, P2, P3);
+    f3 dv, d1, d2, d3;
+    if (!mass_weighted) {
+        /* VFResolveNew split: point moves depth, face point moves depth */
+        f3 vfix = mul(ns, depth);
+        f3 ffix = mul(mul(pn, -sg), depth);
+        float sw = w.x * w.x + w.y * w.y + w.z * w.z;
+        dv = vfix;
+        d1 = divs(mul(ffix, w.x), sw);
+        d2 = divs(mul(ffix, w.y), sw);
+        d3 = divs(mul(ffix, w.z), sw);
+    } else {
+        /* inverse-mass split of the separation 2*depth: the point takes
+         * alpha = m_v/(m_v + m_f), m_f = sum w_i^2 m_i / sum w_i^2; face
+         * point i moves -(1-alpha) 2 depth w_i m_i / sum_j w_j^2 m_j.  Equal
+         * masses reduce to the reference split. */
+        float sw = w.x * w.x + w.y * w.y + w.z * w.z;
+        float swm = w.x * w.x * wm[1] + w.y * w.y * wm[2] + w.z * w.z * wm[3];
+        float mf = swm / sw;
+        float msum = wm[0] + mf;
+        if (!(msum > 0.0f) || !(sw > 0.0f)) return 0;
+        float alpha = wm[0] / msum;
+        float sep = 2.0f * depth;
+        dv = mul(ns, sep * alpha);
+        float fs = swm > 0.0f ? -sep * (1.0f - alpha) / swm : 0.0f;
+        d1 = mul(ns, fs * w.x * wm[1]);
+        d2 = mul(ns, fs * w.y * wm[2]);
+        d3 = mul(ns, fs * w.z * wm[3]);
+    }
+    st3(delta, dv);
+    st3(delta + 3, d1);
+    st3(delta + 6, d2);
+    st3(delta + 9, d3);
+    return 1;
+}
+
+void orc_collision_resolve_jacobi(int n_points, int n_contacts,
+                                  const orc_contact *cts, const float *pos,
+                                  float *prdp, const float *mass, int iterations,
+                                  float thickness, int mass_weighted)
+{
+    float *acc = (float *)malloc(sizeof(float) * 3 * (size_t)(n_points > 0 ? n_points : 1));
+    int *cnt = (int *)malloc(sizeof(int) * (size_t)(n_points > 0 ? n_points : 1));
+    float *dl = (float *)malloc(sizeof(float) * 12 * (size_t)(n_contacts > 0 ? n_contacts : 1));
+    int *act = (int *)malloc(sizeof(int) * (size_t)(n_contacts > 0 ? n_contacts : 1));
+    for (int it = 0; it < iterations; ++it) {
+        for (int c = 0; c < n_contacts; ++c) {
+            int ids[4] = {cts[c].v, cts[c].f0, cts[c].f1, cts[c].f2};
+            float xs[12], ps[12], wm[4];
+            gather4(ids, pos, xs);
+            gather4(ids, prdp, ps);
+            for (int j = 0; j < 4; ++j) wm[j] = mass ? mass[ids[j]] : 1.0f;
+            act[c] = orc_vf_resolve_deltas(xs, ps, wm, thickness, mass_weighted, dl + 12 * c);
+        }
+        /* each point: mean of its active corrections, summed in contact
+         * order (contacts are sorted by point, then face) */
+        memset(acc, 0, sizeof(float) * 3 * (size_t)n_points);
+        memset(cnt, 0, sizeof(int) * (size_t)n_points);
+        for (int c = 0; c < n_contacts; ++c) {
+            if (!act[c]) continue;
+            int ids[4] = {cts[c].v, cts[c].f0, cts[c].f1, cts[c].f2};
+            for (int j = 0; j < 4; ++j) {
+                for (int k = 0; k < 3; ++k) acc[3 * ids[j] + k] += dl[12 * c + 3 * j + k];
+                cnt[ids[j]]++;
+            }
+        }
+        for (int i = 0; i < n_points; ++i)
+            if (cnt[i] > 0)
+                for (int k = 0; k < 3; ++k)
+                    prdp[3 * i + k] = prdp[3 * i + k] + acc[3 * i + k] / (float)cnt[i];
+    }
+    free(acc);
+    free(cnt);
+    free(dl);
+    free(act);
+}
+
+/* ------------------------------------------------------------------ */
+/* substeps                                                             */
+/* ------------------------------------------------------------------ */
+
+int64_t orc_substep_gpu(int n_points, const orc_constraints *c,
+                        const int *sorted_prim_id, int n_worksets,
+                        const int *worksets, int iterations, float dt,
+                        float damping, const float *gravity, const float *mass,
+                        float *pos, float *vel, float *prdp, int bending_fp64,
+                        const orc_colli_params *colli)
+{
+    float damp_pow = powf(damping, dt);
+    orc_advect_gpu(n_points, dt, damp_pow, gravity, mass, vel, prdp, pos);
+    int64_t nct = 0;
+    orc_contact *cts = NULL;
+    int use = colli && colli->enabled;
+    if (use) cts = (orc_contact *)malloc(sizeof(orc_contact) * (size_t)(colli->contact_cap > 0 ? colli->contact_cap : 1));
+    for (int ii = 0; ii < iterations; ++ii) {
+        if (use && (ii % colli->ccd_every == 0 || ii == iterations - 1)) {
+            nct = orc_ccd_vf_pairs(&colli->grid, n_points, colli->n_tris, colli->tri_idx,
+                                   colli->tri_inst, colli->point_inst, pos, prdp,
+                                   colli->thickness, cts, colli->contact_cap);
+            if (nct > colli->contact_cap) nct = colli->contact_cap;
+        }
+        orc_project_colored(c, sorted_prim_id, n_worksets, worksets, ii, ii + 1, mass,
+                            prdp, bending_fp64);
+        if (use && nct > 0)
+            orc_collision_resolve_jacobi(n_points, (int)nct, cts, pos, prdp, mass,
+                                         colli->resolve_passes, colli->thickness,
+                                         colli->mass_weighted);
+    }
+    orc_integrate(n_points, dt, vel, prdp, pos);
+    free(cts);
+    return nct;
+}
+
+int64_t orc_substep_cpu_ref(int n_points, const orc_constraints *c, int iterations,
+                            float dt, const float *gravity, const float *mass,
+                            float *pos, float *vel, float *prdp,
+                            const orc_colli_params *colli,
+                            const float *sphere_center, float sphere_radius)
+{
+    orc_advect_cpu(n_points, dt, gravity, vel, prdp, pos);
+    int64_t nct = 0;
+    if (!(colli && colli->enabled)) {
+        orc_project_cpu(c, iterations, mass, prdp, n_points, sphere_center, sphere_radius);
+    } else {
+        orc_contact *cts = (orc_contact *)malloc(sizeof(orc_contact) * (size_t)(colli->contact_cap > 0 ? colli->contact_cap : 1));
+        for (int ii = 0; ii < iterations; ++ii) {
+            if (ii % colli->ccd_every == 0 || ii == iterations - 1) {
+                nct = orc_ccd_sh_extended_ref(&colli->grid, colli->n_tris, colli->tri_idx, pos,
+                                              prdp, colli->thickness, cts, colli->contact_cap);
+                if (nct > colli->contact_cap) nct = colli->contact_cap;
+            }
+            orc_project_cpu(c, 1, mass, prdp, n_points, NULL, 0.0f);
+            orc_collision_resolve_ref((int)nct, cts, pos, prdp, 1, colli->thickness);
+            if (sphere_center) orc_colli_sphere(n_points, prdp, sphere_center, sphere_radius);
+        }
+        free(cts);
+    }
+    orc_integrate(n_points, dt, vel, prdp, pos);
+    return nct;
+}

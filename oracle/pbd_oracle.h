@@ -1,0 +1,307 @@
+/*
+ * pbd_oracle.h -- CPU restatement of the reference PBD cloth step.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This library is the checker for the CUDA
+ * implementation in positionbaseddynamicsold_gb300/: only tests/, the smoke
+ * check in __graft_entry__.py and the cpu_baseline leg of bench.py may load it.
+ * Nothing on the product path links or calls it.
+ *
+ * Every routine restates one function of the reference
+ * (vivienldy/PositionBasedDynamicsOld, paths relative to
+ * PositionBasedDynamicsCUDA/PositionBasedDynamicsCUDA/) and cites it.
+ * Parity pin: tests/test_oracle_golden.py checks these routines against
+ * fixtures produced by the reference's own code compiled from its sources
+ * (tests/golden/make_golden.py drives oracle/ref_adapter.cpp).
+ *
+ * Layout conventions follow the reference: positions/velocities are float3
+ * AoS (3 floats per point), primList is int2 (start, count) into `indices`,
+ * colorWorksets is int2 (start, count) into sortedPrimId.
+ *
+ * Compile with -ffp-contract=off: the reference's host code performs
+ * plain IEEE float operations (no fused multiply-add).
+ */
+#ifndef PBD_ORACLE_H
+#define PBD_ORACLE_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Distance() spelled as powf like the reference (1) or as sqrtf of the
+ * squared sum like the CUDA kernels (0, default). */
+void orc_set_pow_distance(int on);
+
+/* constraint type bits, P/PBD_Basic.cuh:38-43 */
+#define ORC_DISTANCE 0x001
+#define ORC_BENDING 0x010
+#define ORC_ANCHOR 0x100
+
+/* ------------------------------------------------------------------ */
+/* constraint graph and coloring                                        */
+/* ------------------------------------------------------------------ */
+
+/* GenePoint2PrimsMap + GenePrim2PrimsMap (P/PBD_cuda.cu:155-202).
+ * adj_start_num: int2 per prim (start, count); adj_idx: neighbor prim ids.
+ * Pass adj_idx == NULL to only count; returns total neighbor entries. */
+int64_t orc_prim2prims(int n_prims, const int *prim_list, const int *indices,
+                       int n_points, int *adj_start_num, int *adj_idx);
+
+/* AssignColorsGPU (P/PBD_cuda.cu:313-372), one sweep over all prims. */
+void orc_assign_colors(int n_prims, const int *adj_start_num, const int *adj_idx,
+                       const int *color, int *prd_color);
+
+/* ResolveConflictsGPU (P/PBD_cuda.cu:374-431), one sweep; returns the
+ * conflict flag (non-zero if any prim kept its speculative color rejected). */
+int orc_resolve_conflicts_gpu(int n_prims, const int *prim_list,
+                              const int *adj_start_num, const int *adj_idx,
+                              int *color, const int *prd_color);
+
+/* ResolveConflictsCPU (P/PBD_cuda.cu:256-310): stops the sweep at the first
+ * conflict. */
+int orc_resolve_conflicts_cpu(int n_prims, const int *prim_list,
+                              const int *adj_start_num, const int *adj_idx,
+                              int *color, const int *prd_color);
+
+/* EdgeColoringGPU schedule (P/PBD_cuda.cu:487-544): assign+resolve sweeps
+ * until no conflict or max_iters.  color/prd_color must be initialised
+ * (-1 = uncoloured).  Returns the number of sweeps run. */
+int orc_edge_coloring_gpu(int n_prims, const int *prim_list,
+                          const int *adj_start_num, const int *adj_idx,
+                          int *color, int *prd_color, int max_iters);
+
+/* EdgeColoringCPU schedule (P/PBD_cuda.cu:448-485) with an early exit once
+ * a sweep accepts every prim.  Returns sweeps run. */
+int orc_edge_coloring_cpu(int n_prims, const int *prim_list,
+                          const int *adj_start_num, const int *adj_idx,
+                          int *color, int *prd_color, int max_iters);
+
+/* SortEdgesColors (P/PBD_cuda.cu:546-587): stable sort of (color, prim id),
+ * in place on both arrays. */
+void orc_sort_edges_colors(int n, int *color, int *sorted_prim_id);
+
+/* EvalWorksets (P/PBD_cuda.cu:589-625) as run-length encoding of the sorted
+ * colors; worksets gets 2 ints per run.  Returns the number of runs. */
+int orc_eval_worksets(int n, const int *sorted_color, int *worksets);
+
+/* ------------------------------------------------------------------ */
+/* solver step                                                          */
+/* ------------------------------------------------------------------ */
+
+typedef struct orc_constraints {
+    int n_prims;
+    const int *prim_list;     /* 2 per prim: start, count            */
+    const int *indices;       /* point ids                            */
+    const int *ctype;         /* ORC_DISTANCE / ORC_BENDING / ORC_ANCHOR */
+    const float *rest_length; /* per prim (distance)                  */
+    const float *stiffness;   /* per prim                             */
+    const float *rest_angle;  /* per prim (bending), may be NULL      */
+    const float *rest_pos;    /* 3 per prim (anchor), may be NULL     */
+} orc_constraints;
+
+/* AdvectGPUKernel (P/PBD_cuda.cu:949-979).  damp_pow = powf(dampingRate, dt)
+ * evaluated once by the caller. */
+void orc_advect_gpu(int n, float dt, float damp_pow, const float *gravity,
+                    const float *mass, float *vel, float *prdp, const float *pos);
+
+/* advectCPU (P/PBD_cuda.cu:997-1009): ignores mass and damping. */
+void orc_advect_cpu(int n, float dt, const float *gravity, float *vel,
+                    float *prdp, const float *pos);
+
+/* IntegrationGPUKernel / integrationCPU (P/PBD_cuda.cu:1453-1482). */
+void orc_integrate(int n, float dt, float *vel, const float *prdp, float *pos);
+
+/* projectConstraintGPU (P/PBD_cuda.cu:1240-1435): for each iteration, for
+ * each workset (colour) in order, apply every constraint of the workset.
+ * Every constraint of a workset is processed (the reference's integer
+ * division launch shortfall at P/PBD_cuda.cu:1336-1337 is not reproduced).
+ * Distance: ProjectContraintsGPUKernel arithmetic.  Bending: dihedral
+ * constraint (no reference code; see orc_bending_project).  Anchor: snap to
+ * rest_pos.  A distance constraint whose two inverse masses sum to zero is
+ * skipped (the reference divides by zero there). */
+void orc_project_colored(const orc_constraints *c, const int *sorted_prim_id,
+                         int n_worksets, const int *worksets, int iter_begin,
+                         int iter_end, const float *mass, float *prdp,
+                         int bending_fp64);
+
+/* One constraint of the colored GS, iteration `iter` (stiffness schedule
+ * k = 1 - (1-s)^(1/(iter+1)), P/PBD_cuda.cu:1282). */
+void orc_project_one(const orc_constraints *c, int prim, int iter,
+                     const float *mass, float *prdp, int bending_fp64);
+
+/* projectConstraintCPU (P/PBD_cuda.cu:1090-1127): sequential GS over every
+ * 2-point prim in id order, k = 1, then ColliWithShpGrd per iteration. */
+void orc_project_cpu(const orc_constraints *c, int iterations,
+                     const float *mass, float *prdp, int n_points,
+                     const float *sphere_center, float sphere_radius);
+
+/* ColliWithShpGrd (P/PBD_cuda.cu:1519-1573). */
+void orc_colli_sphere(int n, float *prdp, const float *center, float radius);
+
+/* Dihedral bending projection of the four points p[0..3]
+ * (p0,p1 = hinge edge, p2,p3 = opposite points), signed angle with
+ * gradients of Bridson, Marino & Fedkiw 2003 inside the PBD projection of
+ * Mueller et al. 2007.  Float version: same operation order as the CUDA
+ * kernel.  Returns 1 if a correction was applied. */
+int orc_bending_project_f32(float *p0, float *p1, float *p2, float *p3,
+                            const float *w, float rest_angle, float k);
+int orc_bending_project_f64(double *p0, double *p1, double *p2, double *p3,
+                            const double *w, double rest_angle, double k);
+/* Signed dihedral angle of the hinge (p0,p1) with wings p2, p3. */
+double orc_dihedral_angle(const double *p0, const double *p1, const double *p2,
+                          const double *p3);
+
+/* Relative constraint residual sqrt(sum C^2)/sqrt(sum L^2): distance
+ * C = |pa-pb| - l, L = l; bending C = (theta - theta0)*|hinge|,
+ * L = rest hinge length (hinge_rest per prim, may be NULL -> current).
+ * FP64 accumulation. */
+double orc_residual(const orc_constraints *c, const float *prdp,
+                    const float *hinge_rest, double *num_out, double *den_out);
+
+/* ------------------------------------------------------------------ */
+/* broadphase (SpatialHashSystem)                                       */
+/* ------------------------------------------------------------------ */
+
+typedef struct orc_grid {
+    float start[3];   /* m_girdStartPos                                  */
+    float cell[3];    /* m_cellSize                                      */
+    int size[3];      /* m_gridSize (bounded mode)                       */
+    int bounded;      /* 1: reference bounded grid; 0: unbounded grid      */
+} orc_grid;
+
+/* InitSH (P/SpatialHashSystem.cpp:88-98): start = center - size*cell/2. */
+void orc_grid_init(orc_grid *g, const float *center, const int *size,
+                   const float *cell, int bounded);
+
+/* evalTriCentroids + calcGridPosCPU (P/SpatialHashSystem.cpp:276-298,
+ * 391-399): cell coordinates of each triangle centroid. */
+void orc_tri_cells(const orc_grid *g, int n_tris, const int *tri_idx,
+                   const float *pos, int *cell_xyz);
+
+/* calcGridHashCPU (P/SpatialHashSystem.cpp:401-413): -1 outside. */
+int orc_cell_hash(const orc_grid *g, const int *cell_xyz);
+
+/* UpdateSH + FindNeighbors for every triangle (P/SpatialHashSystem.cpp:
+ * 100-121, 134-187, 326-389) on a fresh grid: neighbor lists in the
+ * reference's order (27 cells z,y,x; within a cell the stable sort order).
+ * out_start_num: 2 ints per triangle.  Pass out_idx NULL to count. */
+int64_t orc_find_neighbors_all(const orc_grid *g, int n_tris, const int *tri_idx,
+                               const float *pos, int *out_start_num, int *out_idx);
+
+/* ------------------------------------------------------------------ */
+/* narrowphase (CCD)                                                    */
+/* ------------------------------------------------------------------ */
+
+typedef struct orc_contact {
+    int v, f0, f1, f2;  /* ctxIndices i0..i3                 */
+    int face;           /* triangle id of the face           */
+    float t;            /* Contact::t                        */
+    double w[4];        /* Contact::w                        */
+    float n[3];         /* Contact::n                        */
+} orc_contact;
+
+/* solve_cubic / newtons_method / solve_quadratic (P/CCD.cpp:48-113). */
+int orc_solve_cubic(double a, double b, double c, double d, double x[3]);
+int orc_solve_quadratic(double a, double b, double c, double x[2]);
+double orc_newtons_method(double a, double b, double c, double d, double x0,
+                          int init_dir);
+
+/* free ExtendedVFTest (P/CCD.cpp:1733-1808).  x[12] = start positions of
+ * vertex, p1, p2, p3; p[12] = predicted positions.  Returns 1 on hit and
+ * fills t, w, n. */
+int orc_extended_vf_test(const float *x, const float *p, float thickness,
+                         int i0, int i1, int i2, int i3, orc_contact *ct);
+
+/* free NarrowVFCCDTest (P/CCD.cpp:1810-1872). */
+int orc_narrow_vf_ccd_test(const float *x, const float *p, float thickness,
+                           int i0, int i1, int i2, int i3, orc_contact *ct);
+
+/* free CCD_SH_Extended (P/CCD.cpp:1522-1587) restated loop for loop:
+ * triangles in id order, their points, neighbor triangles, IsDuplicated
+ * de-duplication (P/CCD.cpp:132-147).  Contacts come out in the
+ * reference's order.  Returns the number of contacts (<= cap written). */
+int64_t orc_ccd_sh_extended_ref(const orc_grid *g, int n_tris, const int *tri_idx,
+                                const float *pos, const float *prdp,
+                                float thickness, orc_contact *out, int64_t cap);
+
+/* Same contact set, computed once per distinct (point, triangle) pair
+ * using point -> incident triangle lists (the evaluation order the CUDA
+ * path uses); contacts sorted by (point, face triangle).  inst (may be
+ * NULL) restricts pairs to points and triangles of the same instance. */
+int64_t orc_ccd_vf_pairs(const orc_grid *g, int n_points, int n_tris,
+                         const int *tri_idx, const int *tri_inst,
+                         const int *point_inst, const float *pos,
+                         const float *prdp, float thickness, orc_contact *out,
+                         int64_t cap);
+
+/* free VFResolveTest (P/CCD.cpp:1996-2032). */
+int orc_vf_resolve_test(const float *x, const float *p, float thickness);
+
+/* free VFResolveNew (P/CCD.cpp:2034-2090), in place on p[12]. */
+void orc_vf_resolve_new(const float *x, float *p, float thickness);
+
+/* free CollisionResolveNew (P/CCD.cpp:1874-1994): `iterations` sequential
+ * passes over the contacts in order. */
+void orc_collision_resolve_ref(int n_contacts, const orc_contact *cts,
+                               const float *pos, float *prdp, int iterations,
+                               float thickness);
+
+/* Contact response as the CUDA path runs it: per pass every contact
+ * evaluates VFResolveTest on the pass-start positions and, if active,
+ * computes its four corrections; each point then moves by the mean of the
+ * corrections of its active contacts.  mass_weighted=0 uses the reference
+ * split (VFResolveNew); 1 uses the inverse-mass split (see the CUDA
+ * kernel for the formula). */
+void orc_collision_resolve_jacobi(int n_points, int n_contacts,
+                                  const orc_contact *cts, const float *pos,
+                                  float *prdp, const float *mass, int iterations,
+                                  float thickness, int mass_weighted);
+
+/* The four corrections of one contact (Jacobi form); returns 1 if active. */
+int orc_vf_resolve_deltas(const float *x, const float *p, const float *w_mass,
+                          float thickness, int mass_weighted, float *delta);
+
+/* ------------------------------------------------------------------ */
+/* whole substeps                                                        */
+/* ------------------------------------------------------------------ */
+
+typedef struct orc_colli_params {
+    int enabled;
+    orc_grid grid;
+    float thickness;
+    int resolve_passes;     /* passes of the response per GS iteration   */
+    int mass_weighted;
+    int ccd_every;          /* CCD when ii % ccd_every == 0 or last (10)  */
+    int n_tris;
+    const int *tri_idx;
+    const int *tri_inst;    /* may be NULL */
+    const int *point_inst;  /* may be NULL */
+    int64_t contact_cap;
+} orc_colli_params;
+
+/* GPU-semantics substep: advect, iterations x (optional CCD, colored GS
+ * sweep, optional response), integrate.  Returns contacts found in the
+ * last CCD pass (or 0). */
+int64_t orc_substep_gpu(int n_points, const orc_constraints *c,
+                        const int *sorted_prim_id, int n_worksets,
+                        const int *worksets, int iterations, float dt,
+                        float damping, const float *gravity, const float *mass,
+                        float *pos, float *vel, float *prdp, int bending_fp64,
+                        const orc_colli_params *colli);
+
+/* Reference CPU substep (P/PBD_cuda.cu:997-1009 advectCPU,
+ * 1130-1210 projectConstraintWithColliCPU or 1090-1127 projectConstraintCPU,
+ * 1453-1465 integrationCPU) with the reference's triangle-ordered CCD
+ * (P/CCD.cpp:210-274) and one sequential response pass per iteration
+ * (P/CCD.cpp:372-484).  Used as the CPU baseline. */
+int64_t orc_substep_cpu_ref(int n_points, const orc_constraints *c, int iterations,
+                            float dt, const float *gravity, const float *mass,
+                            float *pos, float *vel, float *prdp,
+                            const orc_colli_params *colli,
+                            const float *sphere_center, float sphere_radius);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
