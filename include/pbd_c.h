@@ -1,0 +1,214 @@
+/*
+ * pbd_c.h -- C ABI of the GB300 PBD cloth step (libpbd_gb300.so).
+ *
+ * Drop-in boundary for the reference's cloth-step path
+ * (vivienldy/PositionBasedDynamicsOld; paths relative to
+ * PositionBasedDynamicsCUDA/PositionBasedDynamicsCUDA/).  The reference is a
+ * set of C++ classes linked into one executable; each entry point below
+ * replaces the method cited beside it.  Plain pointers and sizes only.
+ *
+ * Conventions
+ *  - Every call returns PBD_OK (0) or a PBD_ERR_* code; pbd_last_error()
+ *    gives a one-line message for the calling thread's last failure.
+ *  - The library owns device memory.  Host arrays are copied in and out
+ *    explicitly; float3 data is 3 floats per point (the reference's AoS).
+ *  - Each object owns one CUDA stream; solver, hash and collision calls on an
+ *    object are asynchronous on that stream.  Copy-out calls synchronise it.
+ *    Handles are not thread-safe.
+ *  - massBuffer semantics follow the reference: the value is the inverse
+ *    mass in the projection and the gravity gate in advection; 0 pins.
+ */
+#ifndef PBD_C_H
+#define PBD_C_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+    PBD_OK = 0,
+    PBD_ERR_ARG = 1,      /* bad argument or size                        */
+    PBD_ERR_OOM = 2,      /* device allocation failed                    */
+    PBD_ERR_CUDA = 3,     /* CUDA runtime error                          */
+    PBD_ERR_TIMEOUT = 4,  /* coloring did not converge in max sweeps     */
+    PBD_ERR_OVERFLOW = 5, /* candidate / contact capacity exceeded       */
+    PBD_ERR_STATE = 6     /* call out of order (e.g. no coloring yet)    */
+};
+
+/* ConstraintType, P/PBD_Basic.cuh:38-43 */
+enum { PBD_DISTANCE = 0x001, PBD_BENDING = 0x010, PBD_ANCHOR = 0x100 };
+/* SolverType, P/PBD_Basic.cuh:46-51 (only Gauss-Seidel is implemented by the
+ * reference and here) */
+enum { PBD_JACOBI = 0, PBD_GAUSSSEIDEL = 1 };
+/* contact response variants */
+enum {
+    PBD_RESPONSE_REFERENCE = 0,    /* VFResolveTest/VFResolveNew arithmetic (P/CCD.cpp:1996-2090) */
+    PBD_RESPONSE_MASS_WEIGHTED = 1 /* same split, weighted by massBuffer; scale-free degeneracy guard */
+};
+
+typedef struct pbd_object pbd_object;
+typedef struct pbd_solver pbd_solver;
+typedef struct pbd_shs pbd_shs;
+typedef struct pbd_colli pbd_colli;
+
+/* Scene description: the buffers of PBDObject and ConstraintPBD
+ * (P/PBD_Basic.cuh:89-211). */
+typedef struct pbd_object_desc {
+    int n_points;
+    const float *pos;             /* meshTopol.posBuffer, 3*n_points            */
+    const float *vel;             /* velBuffer, 3*n_points (NULL = zero)         */
+    const float *mass;            /* massBuffer, n_points                        */
+    int n_tris;
+    const int *tri_idx;           /* meshTopol.indices, 3*n_tris (may be 0/NULL) */
+    int n_prims;
+    const int *prim_list;         /* constrPBDBuffer.topol.primList, 2*n_prims   */
+    const int *indices;           /* constrPBDBuffer.topol.indices               */
+    const int *constraint_type;   /* constraintType, n_prims                     */
+    const float *rest_length;     /* restLengthBuffer, n_prims                   */
+    const float *stiffness;       /* stiffnessBuffer, n_prims                    */
+    const float *rest_angle;      /* bending rest angles, n_prims (NULL = 0)     */
+    const float *rest_pos;        /* anchor rest positions, 3*n_prims (NULL)     */
+    const int *point_inst;        /* instance id per point (NULL = one cloth)    */
+    const int *tri_inst;          /* instance id per triangle (NULL)             */
+    float damping_rate;           /* PBDObject::dampingRate                      */
+    float gravity[3];             /* PBDObject::gravity                          */
+} pbd_object_desc;
+
+const char *pbd_last_error(void);
+int pbd_version(void);
+
+/* ---- PBDObject ----------------------------------------------------------- */
+/* PBDObject(damping, gravity, ht) + Init(topol, constr) (P/PBD_cuda.cu:650-658):
+ * uploads the scene, builds Point2PrimsMap/Prim2PrimsMap on the device. */
+int pbd_object_create(const pbd_object_desc *desc, pbd_object **out);
+/* PBDObject(damping, gravity, resX, resY, sizeX, sizeY, ht) + SetConstrOption
+ * + Init() (P/PBD_cuda.cu:644-869): the reference's own grid, distance
+ * stencil and anchors.  stiffness[3] = {distance, bending, anchor}. */
+int pbd_object_create_grid(float damping, const float *gravity, int res_x, int res_y,
+                           float size_x, float size_y, unsigned ct_mask,
+                           const float *stiffness, pbd_object **out);
+/* ~PBDObject / freeGPUBuffers (P/PBD_cuda.cu:752-794) */
+int pbd_object_destroy(pbd_object *obj);
+int pbd_object_sizes(const pbd_object *obj, int *n_points, int *n_tris, int *n_prims);
+/* meshTopol.posBuffer / velBuffer / constrPBDBuffer.prdPBuffer copy-out and
+ * copy-in (Buffer::LoadToHost / LoadToDevice, P/Buffer.cuh:123-165) */
+int pbd_object_get_positions(pbd_object *obj, float *pos3);
+int pbd_object_get_velocities(pbd_object *obj, float *vel3);
+int pbd_object_get_predicted(pbd_object *obj, float *prdp3);
+int pbd_object_set_positions(pbd_object *obj, const float *pos3);
+int pbd_object_set_velocities(pbd_object *obj, const float *vel3);
+int pbd_object_set_predicted(pbd_object *obj, const float *prdp3);
+/* the object's CUDA stream (cudaStream_t) */
+int pbd_object_stream(pbd_object *obj, void **stream);
+int pbd_object_sync(pbd_object *obj);
+
+/* ---- ConstraintPBD ------------------------------------------------------- */
+/* EdgeColoring / EdgeColoringGPU (P/PBD_cuda.cu:433-544): speculative greedy
+ * coloring on the device, run until every constraint is coloured (the
+ * reference runs a fixed count and never reads its flag).  Returns
+ * PBD_ERR_TIMEOUT if max_iterations sweeps do not suffice. */
+int pbd_constraints_edge_coloring(pbd_object *obj, int max_iterations, int *sweeps);
+/* SortEdgesColors (P/PBD_cuda.cu:546-587): stable device sort of prim ids by
+ * color; also builds the per-color constraint records the solver reads. */
+int pbd_constraints_sort_edges_colors(pbd_object *obj);
+/* EvalWorksets (P/PBD_cuda.cu:589-625): (start, count) per color. */
+int pbd_constraints_eval_worksets(pbd_object *obj, int *n_worksets);
+/* install an externally computed coloring (color per prim id, >= 0) */
+int pbd_constraints_set_colors(pbd_object *obj, const int *color);
+int pbd_constraints_get_colors(pbd_object *obj, int *color);
+int pbd_constraints_get_sorted(pbd_object *obj, int *sorted_color, int *sorted_prim_id);
+int pbd_constraints_get_worksets(pbd_object *obj, int *worksets, int cap, int *n);
+/* Prim2PrimsMap (P/PBD_cuda.cu:170-202): startNumList (2 per prim) and
+ * indices; pass adj NULL to query the total. */
+int pbd_constraints_get_adjacency(pbd_object *obj, int *start_num, int *adj,
+                                  long long cap, long long *total);
+/* relative residual sqrt(sum C^2)/sqrt(sum L^2) of the predicted positions
+ * (distance: C=|pa-pb|-l, L=l; bending: C=(theta-theta0)|hinge|,
+ * L=rest hinge length).  No reference counterpart (the reference has no
+ * convergence measure). */
+int pbd_constraints_residual(pbd_object *obj, double *residual);
+
+/* ---- SolverPBD (P/PBD_Basic.cuh:213-259) --------------------------------- */
+int pbd_solver_create(pbd_solver **out);
+int pbd_solver_destroy(pbd_solver *s);
+/* SolverPBD::SetTarget */
+int pbd_solver_set_target(pbd_solver *s, pbd_object *obj);
+/* SolverPBD::Advect / AdvectGPUKernel (P/PBD_cuda.cu:949-1052) */
+int pbd_solver_advect(pbd_solver *s, float dt);
+/* SolverPBD::ProjectConstraint / projectConstraintGPU (P/PBD_cuda.cu:1054-1070,
+ * 1240-1435): `iterations` colored Gauss-Seidel sweeps over every color
+ * (distance, bending and anchor constraints).  Iteration numbering for the
+ * stiffness schedule starts at 0 on each call. */
+int pbd_solver_project_constraint(pbd_solver *s, int solver_type, int iterations);
+/* SolverPBD::ProjectConstraintWithColli (P/PBD_cuda.cu:1072-1088, CPU form
+ * 1130-1210): per iteration ii, CCD when ii % 10 == 0 or last, one GS sweep,
+ * the collision response, the analytic obstacles. */
+int pbd_solver_project_constraint_with_colli(pbd_solver *s, int solver_type, int iterations,
+                                             pbd_colli *colli);
+/* SolverPBD::Integration / IntegrationGPUKernel (P/PBD_cuda.cu:1437-1518) */
+int pbd_solver_integration(pbd_solver *s, float dt);
+/* analytic obstacles of ColliWithShpGrd (P/PBD_cuda.cu:1519-1573), applied
+ * after every GS iteration when enabled: sphere push-out (the reference's
+ * fixed unit sphere, tolerance 0.001) and the ground plane CollideGround. */
+int pbd_solver_set_sphere(pbd_solver *s, int enable, const float *center, float radius);
+int pbd_solver_set_ground(pbd_solver *s, int enable, float height);
+/* whole substeps: Advect, ProjectConstraint[WithColli], Integration, repeated
+ * `substeps` times; recorded into a CUDA graph on first use (use_graph=1)
+ * and replayed.  colli may be NULL. */
+int pbd_solver_step(pbd_solver *s, float dt, int substeps, int iterations, pbd_colli *colli,
+                    int use_graph);
+
+/* ---- SpatialHashSystem (P/SpatialHashSystem.h:10-96) ---------------------- */
+/* SpatialHashSystem(posBuffer, triIdxBuffer, ht, gridCenter, gridSize,
+ * cellSize): bounded uniform grid over triangle centroids. */
+int pbd_shs_create(pbd_object *obj, const float *grid_center, const int *grid_size,
+                   const float *cell_size, pbd_shs **out);
+/* Unbounded grid hashed into 2^log2_table buckets; a bucket entry is used
+ * only for its own cell, so results equal an unbounded uniform grid. */
+int pbd_shs_create_hashed(pbd_object *obj, const float *cell_size, int log2_table,
+                          pbd_shs **out);
+int pbd_shs_destroy(pbd_shs *shs);
+int pbd_shs_set_grid_center(pbd_shs *shs, const float *center);
+int pbd_shs_set_grid_size(pbd_shs *shs, const int *size);
+int pbd_shs_set_division(pbd_shs *shs, const float *cell_size);
+/* InitSH / UpdateSH (P/SpatialHashSystem.cpp:88-121): bin the triangles by
+ * the centroids of the object's predicted positions. */
+int pbd_shs_init(pbd_shs *shs);
+int pbd_shs_update(pbd_shs *shs);
+/* FindNeighbors (P/SpatialHashSystem.cpp:134-187) for one triangle / all
+ * triangles (start_num: 2 per triangle). */
+int pbd_shs_find_neighbors(pbd_shs *shs, int tri, int *out, int cap, int *n);
+int pbd_shs_find_neighbors_all(pbd_shs *shs, int *start_num, int *out, long long cap,
+                               long long *total);
+
+/* ---- CollisionSolver (P/CCD_Basic.h:33-135) ------------------------------- */
+int pbd_colli_create(pbd_colli **out);
+int pbd_colli_destroy(pbd_colli *c);
+int pbd_colli_set_target(pbd_colli *c, pbd_object *obj);       /* SetTarget      */
+int pbd_colli_set_acce_struct(pbd_colli *c, pbd_shs *shs);     /* SetAcceStruct  */
+int pbd_colli_set_thickness(pbd_colli *c, float thickness);    /* SetThickness   */
+int pbd_colli_set_iterations(pbd_colli *c, int iterations);    /* SetIterations: response passes */
+int pbd_colli_set_response(pbd_colli *c, int mode);            /* PBD_RESPONSE_* */
+int pbd_colli_set_capacity(pbd_colli *c, long long candidates, long long contacts);
+/* CCD_SH_Extended (P/CCD.cpp:210-274, 1522-1587): UpdateSH on the predicted
+ * positions, then the vertex-face ExtendedVFTest over every distinct
+ * (point, neighbour triangle) pair; contacts kept on the device, sorted by
+ * (point, face triangle). */
+int pbd_colli_ccd_sh_extended(pbd_colli *c);
+/* CollisionResolveNew (P/CCD.cpp:372-484, 1874-1994): `iterations` passes of
+ * the response over the current contacts; within a pass every contact
+ * reads the pass-start positions and each point moves by the mean of its
+ * active contacts' corrections. */
+int pbd_colli_collision_resolve_new(pbd_colli *c);
+/* contactData (P/CCD_Basic.h:12-31) copy-out: ids 4 per contact (i0..i3),
+ * face triangle, t, w (4 doubles), n (3 floats); any output may be NULL. */
+int pbd_colli_get_contacts(pbd_colli *c, int *ids, int *face, float *t, double *w, float *n,
+                           long long cap, long long *count);
+/* number of broadphase candidate pairs that reached the narrow phase in
+ * the last CCD call, and the overflow flag */
+int pbd_colli_stats(pbd_colli *c, long long *candidates, long long *contacts, int *overflow);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

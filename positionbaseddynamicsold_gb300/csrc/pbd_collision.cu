@@ -1,0 +1,1048 @@
+// pbd_collision.cu -- SpatialHashSystem and CollisionSolver on the GPU.
+//
+// Broadphase (per CCD call, all device-resident so it can sit in a graph):
+//   1. per triangle: centroid of its predicted positions, cell
+//      floor((c - start)/cell) (SpatialHashSystem.cpp:276-298, 391-399),
+//      bucket key (bounded grid: the reference's linear cell id; hashed:
+//      Teschner et al. 2003 hash of the cell mod 2^k), swept AABB;
+//   2. stable radix sort of (bucket, triangle id) and a bucket -> [start, end)
+//      table (the reference's cellStart/cellEnd, reset each update);
+//   3. one thread per point: the union of the 27-cell neighbourhoods of the
+//      centroid cells of its incident triangles (CCD_SH_Extended,
+//      P/CCD.cpp:1541-1586, tests every (point, neighbour) pair; the union
+//      holds each distinct pair once), exact-cell check per bucket entry,
+//      then two conservative FP32 filters that cannot reject a pair the
+//      ExtendedVFTest would accept (swept-AABB overlap with margin 5.5 h and
+//      a lower bound on the point-triangle distance over the step);
+//      survivors are appended with one atomic per warp.
+// Narrowphase: one thread per surviving pair runs ExtendedVFTest
+// (P/CCD.cpp:1733-1808) with the reference's arithmetic: float triple
+// products widened to double, the double cubic solve (P/CCD.cpp:48-113), the
+// float barycentric inside test.  Contacts are sorted by (point, triangle).
+// Response: per pass every contact computes its four corrections from the
+// pass-start positions (VFResolveTest + VFResolveNew, P/CCD.cpp:1996-2090);
+// each point then moves by the mean of its active corrections, summed in
+// contact order (deterministic, no float atomics).
+//
+// Compiled with -fmad=false: products round separately as in the reference.
+#include <cooperative_groups.h>
+
+#include <cmath>
+#include <cstring>
+
+#include "pbd_common.cuh"
+
+namespace cg = cooperative_groups;
+
+namespace pbd {
+namespace {
+
+constexpr int kMaxInc = 16;  // incident triangles considered per point
+
+struct v3 {
+    float x, y, z;
+};
+__device__ __forceinline__ v3 mk3(float x, float y, float z) { return {x, y, z}; }
+__device__ __forceinline__ v3 ld3(float4 a) { return {a.x, a.y, a.z}; }
+__device__ __forceinline__ v3 sub3(v3 a, v3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+__device__ __forceinline__ v3 add3(v3 a, v3 b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
+__device__ __forceinline__ v3 mul3(v3 a, float s) { return {a.x * s, a.y * s, a.z * s}; }
+__device__ __forceinline__ v3 div3(v3 a, float s) { return {a.x / s, a.y / s, a.z / s}; }
+__device__ __forceinline__ float dot3(v3 a, v3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+__device__ __forceinline__ v3 cross3(v3 a, v3 b) {
+    return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
+}
+// normalize with a correctly rounded reciprocal square root, as the
+// reference's host build computes it (1.0f / sqrtf)
+__device__ __forceinline__ v3 nrm3(v3 v) {
+    float inv = 1.0f / sqrtf(dot3(v, v));
+    return mul3(v, inv);
+}
+__device__ __forceinline__ float dist3(v3 a, v3 b) {
+    float dx = a.x - b.x, dy = a.y - b.y, dz = a.z - b.z;
+    return sqrtf(dx * dx + dy * dy + dz * dz);
+}
+__device__ __forceinline__ float stp(v3 u, v3 v, v3 w) { return dot3(u, cross3(v, w)); }
+__device__ __forceinline__ v3 lerp_t(v3 a, v3 b, double t) {
+    float tf = (float)t;
+    v3 d = sub3(b, a);
+    return add3(a, mk3(tf * d.x, tf * d.y, tf * d.z));
+}
+// BarycentricCoord (P/CCD.cpp:115-130)
+__device__ __forceinline__ v3 bary(v3 pos, v3 p0, v3 p1, v3 p2) {
+    v3 ab = sub3(p0, p2), ac = sub3(p1, p2), ap = sub3(pos, p2);
+    float d00 = dot3(ac, ac), d01 = dot3(ac, ab), d02 = dot3(ac, ap);
+    float d11 = dot3(ab, ab), d12 = dot3(ab, ap);
+    float inv = 1.0f / (d00 * d11 - d01 * d01);
+    float v = (d11 * d02 - d01 * d12) * inv;
+    float u = (d00 * d12 - d01 * d02) * inv;
+    float w = 1.0f - u - v;
+    return mk3(u, v, w);
+}
+
+// ---- cubic root isolation (P/CCD.cpp:48-113), double precision ----------
+__device__ __forceinline__ double sgnd(double x) { return x < 0 ? -1.0 : 1.0; }
+
+__device__ int solve_quadratic(double a, double b, double c, double x[2]) {
+    double d = b * b - 4 * a * c;
+    if (d < 0) {
+        x[0] = -b / (2 * a);
+        return 0;
+    }
+    double q = -(b + sgnd(b) * sqrt(d)) / 2;
+    int i = 0;
+    if (fabs(a) > 1e-12 * fabs(q)) x[i++] = q / a;
+    if (fabs(q) > 1e-12 * fabs(c)) x[i++] = c / q;
+    if (i == 2 && x[0] > x[1]) {
+        double s = x[0];
+        x[0] = x[1];
+        x[1] = s;
+    }
+    return i;
+}
+
+__device__ double newtons_method(double a, double b, double c, double d, double x0, int dir) {
+    if (dir != 0) {
+        double y0 = d + x0 * (c + x0 * (b + x0 * a));
+        double ddy0 = 2 * b + x0 * (6 * a);
+        x0 += dir * sqrt(fabs(2 * y0 / ddy0));
+    }
+    for (int iter = 0; iter < 100; iter++) {
+        double y = d + x0 * (c + x0 * (b + x0 * a));
+        double dy = c + x0 * (2 * b + x0 * 3 * a);
+        if (dy == 0) return x0;
+        double x1 = x0 - y / dy;
+        if (fabs(x0 - x1) < 1e-6) return x0;
+        x0 = x1;
+    }
+    return x0;
+}
+
+// when the derivative has no critical point and none was written, Newton
+// starts from 0 (the reference reads an uninitialised value there)
+__device__ int solve_cubic(double a, double b, double c, double d, double x[3]) {
+    double xc[2] = {0.0, 0.0};
+    int ncrit = solve_quadratic(3 * a, 2 * b, c, xc);
+    if (ncrit == 0) {
+        x[0] = newtons_method(a, b, c, d, xc[0], 0);
+        return 1;
+    } else if (ncrit == 1) {
+        return solve_quadratic(b, c, d, x);
+    }
+    double yc[2] = {d + xc[0] * (c + xc[0] * (b + xc[0] * a)),
+                    d + xc[1] * (c + xc[1] * (b + xc[1] * a))};
+    int i = 0;
+    if (yc[0] * a >= 0) x[i++] = newtons_method(a, b, c, d, xc[0], -1);
+    if (yc[0] * yc[1] <= 0) {
+        int closer = fabs(yc[0]) < fabs(yc[1]) ? 0 : 1;
+        x[i++] = newtons_method(a, b, c, d, xc[closer], closer == 0 ? 1 : -1);
+    }
+    if (yc[1] * a <= 0) x[i++] = newtons_method(a, b, c, d, xc[1], 1);
+    return i;
+}
+
+struct VFResult {
+    float t;
+    v3 n;
+    double w[4];
+};
+
+// ExtendedVFTest (P/CCD.cpp:1733-1808); X/P = start/predicted positions of
+// point, f0, f1, f2
+__device__ bool extended_vf_test(const v3 *X, const v3 *P, float th, VFResult &res) {
+    v3 x0 = X[0], v0 = sub3(P[0], x0);
+    v3 x1 = sub3(X[1], x0), x2 = sub3(X[2], x0), x3 = sub3(X[3], x0);
+    v3 v1 = sub3(sub3(P[1], X[1]), v0), v2 = sub3(sub3(P[2], X[2]), v0),
+       v3_ = sub3(sub3(P[3], X[3]), v0);
+    double a0 = stp(x1, x2, x3);
+    double a1 = stp(v1, x2, x3) + stp(x1, v2, x3) + stp(x1, x2, v3_);
+    double a2 = stp(x1, v2, v3_) + stp(v1, x2, v3_) + stp(v1, v2, x3);
+    double a3 = stp(v1, v2, v3_);
+    double t[5];
+    int nsol = solve_cubic(a3, a2, a1, a0, t);
+    t[nsol] = 1;
+    t[nsol + 1] = 0;
+    int m = nsol + 2;
+    for (int i = 1; i < m; ++i) {
+        double v = t[i];
+        int j = i - 1;
+        while (j >= 0 && t[j] > v) {
+            t[j + 1] = t[j];
+            --j;
+        }
+        t[j + 1] = v;
+    }
+    for (int i = 0; i < m; ++i) {
+        if (t[i] < 0 || t[i] > 1) continue;
+        v3 c0 = lerp_t(X[0], P[0], t[i]), c1 = lerp_t(X[1], P[1], t[i]);
+        v3 c2 = lerp_t(X[2], P[2], t[i]), c3 = lerp_t(X[3], P[3], t[i]);
+        v3 n = nrm3(cross3(sub3(P[2], P[1]), sub3(P[3], P[1])));
+        v3 cn = nrm3(cross3(sub3(c2, c1), sub3(c3, c1)));
+        double dist = dot3(sub3(c0, c1), cn);
+        v3 w = bary(c0, c1, c2, c3);
+        res.t = (float)t[i];
+        res.n = n;
+        res.w[0] = 1;
+        res.w[1] = w.x;
+        res.w[2] = w.y;
+        res.w[3] = w.z;
+        float e1 = dist3(c1, c2), e2 = dist3(c1, c3), e3 = dist3(c2, c3);
+        float eps = (float)((double)th / ((double)(e1 + e2 + e3) / 3.0));
+        bool in = (w.x <= (1 + eps)) && (w.x >= (-eps)) && (w.y <= (1 + eps)) &&
+                  (w.y >= (-eps)) && (w.z <= (1 + eps)) && (w.z >= (-eps));
+        if ((fabs(dist) - (double)(2.0f * th) < -1e-6) && in) return true;
+    }
+    return false;
+}
+
+// closest distance from point p to triangle abc (Ericson, Real-Time
+// Collision Detection, 5.1.5), float
+__device__ float point_tri_dist(v3 p, v3 a, v3 b, v3 c) {
+    v3 ab = sub3(b, a), ac = sub3(c, a), ap = sub3(p, a);
+    float d1 = dot3(ab, ap), d2 = dot3(ac, ap);
+    if (d1 <= 0.f && d2 <= 0.f) return sqrtf(dot3(ap, ap));
+    v3 bp = sub3(p, b);
+    float d3 = dot3(ab, bp), d4 = dot3(ac, bp);
+    if (d3 >= 0.f && d4 <= d3) return sqrtf(dot3(bp, bp));
+    float vc = d1 * d4 - d3 * d2;
+    if (vc <= 0.f && d1 >= 0.f && d3 <= 0.f) {
+        float v = d1 / (d1 - d3);
+        v3 q = sub3(p, add3(a, mul3(ab, v)));
+        return sqrtf(dot3(q, q));
+    }
+    v3 cp = sub3(p, c);
+    float d5 = dot3(ab, cp), d6 = dot3(ac, cp);
+    if (d6 >= 0.f && d5 <= d6) return sqrtf(dot3(cp, cp));
+    float vb = d5 * d2 - d1 * d6;
+    if (vb <= 0.f && d2 >= 0.f && d6 <= 0.f) {
+        float w = d2 / (d2 - d6);
+        v3 q = sub3(p, add3(a, mul3(ac, w)));
+        return sqrtf(dot3(q, q));
+    }
+    float va = d3 * d6 - d5 * d4;
+    if (va <= 0.f && (d4 - d3) >= 0.f && (d5 - d6) >= 0.f) {
+        float w = (d4 - d3) / ((d4 - d3) + (d5 - d6));
+        v3 q = sub3(p, add3(b, mul3(sub3(c, b), w)));
+        return sqrtf(dot3(q, q));
+    }
+    float den = 1.f / (va + vb + vc);
+    float v = vb * den, w = vc * den;
+    v3 q = sub3(p, add3(a, add3(mul3(ab, v), mul3(ac, w))));
+    return sqrtf(dot3(q, q));
+}
+
+__device__ __forceinline__ bool sliver(v3 a, v3 b, v3 c) {
+    v3 e1 = sub3(b, a), e2 = sub3(c, a);
+    v3 n = cross3(e1, e2);
+    return !(dot3(n, n) > 1e-10f * (dot3(e1, e1) * dot3(e2, e2)));
+}
+
+__device__ __forceinline__ uint32_t teschner(int x, int y, int z) {
+    return ((uint32_t)x * 73856093u) ^ ((uint32_t)y * 19349663u) ^ ((uint32_t)z * 83492791u);
+}
+
+struct GridParams {
+    float3 start, cell;
+    int3 size;
+    int hashed;
+    uint32_t nb;  // buckets (bounded: cells; sentinel key = nb)
+};
+
+__device__ __forceinline__ bool outside(const GridParams &g, int x, int y, int z) {
+    return x < 0 || y < 0 || z < 0 || x >= g.size.x || y >= g.size.y || z >= g.size.z;
+}
+__device__ __forceinline__ uint32_t bucket_of(const GridParams &g, int x, int y, int z) {
+    if (g.hashed) return teschner(x, y, z) & (g.nb - 1u);
+    return ((uint32_t)z * (uint32_t)g.size.y) * (uint32_t)g.size.x +
+           (uint32_t)y * (uint32_t)g.size.x + (uint32_t)x;
+}
+
+// one atomic per group of lanes that reach this call together
+__device__ __forceinline__ int agg_inc(int *counter) {
+    cg::coalesced_group g = cg::coalesced_threads();
+    int base = 0;
+    if (g.thread_rank() == 0) base = atomicAdd(counter, (int)g.size());
+    return g.shfl(base, 0) + (int)g.thread_rank();
+}
+
+// ---------------------------------------------------------------------------
+__global__ void k_reset_buckets(const uint32_t *skey, const int *n_prev, uint32_t nb, int *bstart,
+                                int *bend, long long cap) {
+    long long n = *n_prev;
+    if (n > cap) n = cap;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x) {
+        uint32_t k = skey[i];
+        if (k < nb) {
+            bstart[k] = 0;
+            bend[k] = 0;
+        }
+    }
+}
+
+__global__ void __launch_bounds__(256) k_tri_cells(int nt, GridParams g, float margin,
+                                                   const int4 *__restrict__ tri,
+                                                   const float4 *__restrict__ x,
+                                                   const float4 *__restrict__ p, int4 *tcell,
+                                                   float4 *tlo, float4 *thi, uint32_t *key,
+                                                   int *id, int *n_valid) {
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    bool valid = false;
+    if (t < nt) {
+        int4 f = tri[t];
+        v3 a = ld3(p[f.x]), b = ld3(p[f.y]), c = ld3(p[f.z]);
+        // centroid (P/SpatialHashSystem.cpp:291-293) and cell (:394-396)
+        float cx = (a.x + b.x + c.x) / 3.0f;
+        float cy = (a.y + b.y + c.y) / 3.0f;
+        float cz = (a.z + b.z + c.z) / 3.0f;
+        int ix = (int)floorf((cx - g.start.x) / g.cell.x);
+        int iy = (int)floorf((cy - g.start.y) / g.cell.y);
+        int iz = (int)floorf((cz - g.start.z) / g.cell.z);
+        valid = g.hashed || !outside(g, ix, iy, iz);
+        tcell[t] = make_int4(ix, iy, iz, f.w);
+        key[t] = valid ? bucket_of(g, ix, iy, iz) : g.nb;
+        id[t] = t;
+        v3 xa = ld3(x[f.x]), xb = ld3(x[f.y]), xc = ld3(x[f.z]);
+        if (sliver(a, b, c) || sliver(xa, xb, xc)) {
+            tlo[t] = make_float4(-INFINITY, -INFINITY, -INFINITY, 1.f);
+            thi[t] = make_float4(INFINITY, INFINITY, INFINITY, 1.f);
+        } else {
+            float lx = fminf(fminf(fminf(a.x, b.x), fminf(c.x, xa.x)), fminf(xb.x, xc.x));
+            float ly = fminf(fminf(fminf(a.y, b.y), fminf(c.y, xa.y)), fminf(xb.y, xc.y));
+            float lz = fminf(fminf(fminf(a.z, b.z), fminf(c.z, xa.z)), fminf(xb.z, xc.z));
+            float hx = fmaxf(fmaxf(fmaxf(a.x, b.x), fmaxf(c.x, xa.x)), fmaxf(xb.x, xc.x));
+            float hy = fmaxf(fmaxf(fmaxf(a.y, b.y), fmaxf(c.y, xa.y)), fmaxf(xb.y, xc.y));
+            float hz = fmaxf(fmaxf(fmaxf(a.z, b.z), fmaxf(c.z, xa.z)), fmaxf(xb.z, xc.z));
+            tlo[t] = make_float4(lx - margin, ly - margin, lz - margin, 0.f);
+            thi[t] = make_float4(hx + margin, hy + margin, hz + margin, 0.f);
+        }
+    }
+    unsigned m = __ballot_sync(0xffffffffu, valid);
+    if ((threadIdx.x & 31) == 0 && m) atomicAdd(n_valid, __popc(m));
+}
+
+__global__ void k_bucket_ranges(const uint32_t *skey, const int *sid, const int *n_valid,
+                                const int4 *tcell, int *bstart, int *bend, int4 *scell) {
+    int n = *n_valid;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        uint32_t k = skey[i];
+        if (i == 0 || skey[i - 1] != k) bstart[k] = i;
+        if (i == n - 1 || skey[i + 1] != k) bend[k] = i + 1;
+        scell[i] = tcell[sid[i]];
+    }
+}
+
+// FindNeighbors (P/SpatialHashSystem.cpp:134-187) for every triangle:
+// count (out == nullptr) or fill
+__global__ void k_find_neighbors(int nt, GridParams g, const int4 *tcell, const int *bstart,
+                                 const int *bend, const int4 *scell, const int *sid,
+                                 const int *off, int *cnt, int *out) {
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nt) return;
+    int4 c = tcell[t];
+    int k = 0, o = out ? off[t] : 0;
+    if (g.hashed || !outside(g, c.x, c.y, c.z)) {
+        for (int z = -1; z <= 1; ++z)
+            for (int y = -1; y <= 1; ++y)
+                for (int x = -1; x <= 1; ++x) {
+                    int nx = c.x + x, ny = c.y + y, nz = c.z + z;
+                    if (!g.hashed && outside(g, nx, ny, nz)) continue;
+                    uint32_t b = bucket_of(g, nx, ny, nz);
+                    for (int i = bstart[b]; i < bend[b]; ++i) {
+                        int4 sc = scell[i];
+                        if (sc.x != nx || sc.y != ny || sc.z != nz) continue;
+                        int id = sid[i];
+                        if (id == t) continue;
+                        if (out) out[o + k] = id;
+                        ++k;
+                    }
+                }
+    }
+    if (cnt) cnt[t] = k;
+}
+
+// candidate pairs: one thread per point
+__global__ void __launch_bounds__(128) k_candidates(
+    int n, GridParams g, float margin, float reach, const int4 *__restrict__ tri,
+    const int *__restrict__ pt_first, const int *__restrict__ pt_last,
+    const int *__restrict__ pt_tri, const int *__restrict__ point_inst,
+    const float4 *__restrict__ x, const float4 *__restrict__ p, const int4 *__restrict__ tcell,
+    const float4 *__restrict__ tlo, const float4 *__restrict__ thi,
+    const int *__restrict__ bstart, const int *__restrict__ bend,
+    const int4 *__restrict__ scell, const int *__restrict__ sid, int2 *cand, long long cap,
+    int *counters) {
+    int v = blockIdx.x * blockDim.x + threadIdx.x;
+    bool active = v < n;
+    int cx[kMaxInc], cy[kMaxInc], cz[kMaxInc];
+    int nc = 0;
+    int lo[3] = {0, 0, 0}, hi[3] = {-1, -1, -1};
+    v3 X0 = mk3(0, 0, 0), P0 = mk3(0, 0, 0);
+    float plo[3], phi[3];
+    int inst = 0;
+    if (active) {
+        int f0 = pt_first[v], f1 = pt_last[v];
+        if (f1 - f0 > kMaxInc) atomicOr(counters + 2, 4);
+        for (int q = f0; q < f1 && nc < kMaxInc; ++q) {
+            int4 c = tcell[pt_tri[q]];
+            if (!g.hashed && outside(g, c.x, c.y, c.z)) continue;
+            cx[nc] = c.x;
+            cy[nc] = c.y;
+            cz[nc] = c.z;
+            if (nc == 0) {
+                lo[0] = hi[0] = c.x;
+                lo[1] = hi[1] = c.y;
+                lo[2] = hi[2] = c.z;
+            } else {
+                lo[0] = min(lo[0], c.x); hi[0] = max(hi[0], c.x);
+                lo[1] = min(lo[1], c.y); hi[1] = max(hi[1], c.y);
+                lo[2] = min(lo[2], c.z); hi[2] = max(hi[2], c.z);
+            }
+            ++nc;
+        }
+        X0 = ld3(x[v]);
+        P0 = ld3(p[v]);
+        // swept AABB of the point, grown by the per-axis reach of a hit
+        plo[0] = fminf(X0.x, P0.x) - margin; phi[0] = fmaxf(X0.x, P0.x) + margin;
+        plo[1] = fminf(X0.y, P0.y) - margin; phi[1] = fmaxf(X0.y, P0.y) + margin;
+        plo[2] = fminf(X0.z, P0.z) - margin; phi[2] = fmaxf(X0.z, P0.z) + margin;
+        if (point_inst) inst = point_inst[v];
+    }
+    if (!active || nc == 0) {
+        lo[0] = 1; hi[0] = -1;  // empty cell loop
+    }
+    v3 D0 = sub3(P0, X0);
+    for (int z = lo[2] - 1; z <= hi[2] + 1; ++z)
+        for (int y = lo[1] - 1; y <= hi[1] + 1; ++y)
+            for (int xx = lo[0] - 1; xx <= hi[0] + 1; ++xx) {
+                bool near = false;
+                for (int i = 0; i < nc && !near; ++i)
+                    near = abs(cx[i] - xx) <= 1 && abs(cy[i] - y) <= 1 && abs(cz[i] - z) <= 1;
+                if (!near) continue;
+                if (!g.hashed && outside(g, xx, y, z)) continue;
+                uint32_t b = bucket_of(g, xx, y, z);
+                int e1 = bend[b];
+                for (int e = bstart[b]; e < e1; ++e) {
+                    int4 sc = scell[e];
+                    if (sc.x != xx || sc.y != y || sc.z != z) continue;
+                    if (point_inst && sc.w != inst) continue;
+                    int f = sid[e];
+                    float4 bl = tlo[f], bh = thi[f];
+                    if (plo[0] > bh.x || phi[0] < bl.x || plo[1] > bh.y || phi[1] < bl.y ||
+                        plo[2] > bh.z || phi[2] < bl.z)
+                        continue;
+                    int4 fi = tri[f];
+                    if (fi.x == v || fi.y == v || fi.z == v) continue;
+                    if (bl.w == 0.f) {
+                        // lower bound of the point-triangle distance over the step
+                        v3 xa = ld3(x[fi.x]), xb = ld3(x[fi.y]), xc = ld3(x[fi.z]);
+                        v3 pa = ld3(p[fi.x]), pb = ld3(p[fi.y]), pc = ld3(p[fi.z]);
+                        float d0 = point_tri_dist(X0, xa, xb, xc);
+                        float d1 = point_tri_dist(P0, pa, pb, pc);
+                        v3 ua = sub3(sub3(pa, xa), D0), ub = sub3(sub3(pb, xb), D0),
+                           uc = sub3(sub3(pc, xc), D0);
+                        float U = sqrtf(fmaxf(fmaxf(dot3(ua, ua), dot3(ub, ub)), dot3(uc, uc)));
+                        if ((d0 + d1 - U) * 0.5f > reach) continue;
+                    }
+                    long long slot = agg_inc(counters);
+                    if (slot < cap)
+                        cand[slot] = make_int2(v, f);
+                    else
+                        atomicOr(counters + 2, 1);
+                }
+            }
+}
+
+__global__ void __launch_bounds__(128) k_narrow(const int2 *__restrict__ cand, long long cap,
+                                                int nt, float th, const int4 *__restrict__ tri,
+                                                const float4 *__restrict__ x,
+                                                const float4 *__restrict__ p, int *counters,
+                                                long long ccap, unsigned long long *ckey,
+                                                int *cperm, int4 *cids, int *cface, float4 *ctn,
+                                                double4 *cw) {
+    long long n = counters[0];
+    if (n > cap) n = cap;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x) {
+        int2 c = cand[i];
+        int4 f = tri[c.y];
+        v3 X[4] = {ld3(x[c.x]), ld3(x[f.x]), ld3(x[f.y]), ld3(x[f.z])};
+        v3 P[4] = {ld3(p[c.x]), ld3(p[f.x]), ld3(p[f.y]), ld3(p[f.z])};
+        VFResult r;
+        if (!extended_vf_test(X, P, th, r)) continue;
+        int slot = agg_inc(counters + 1);
+        if (slot >= ccap) {
+            atomicOr(counters + 2, 2);
+            continue;
+        }
+        ckey[slot] = (unsigned long long)c.x * (unsigned long long)nt + (unsigned long long)c.y;
+        cperm[slot] = slot;
+        cids[slot] = make_int4(c.x, f.x, f.y, f.z);
+        cface[slot] = c.y;
+        ctn[slot] = make_float4(r.t, r.n.x, r.n.y, r.n.z);
+        cw[slot] = make_double4(r.w[0], r.w[1], r.w[2], r.w[3]);
+    }
+}
+
+__global__ void k_clamp_counts(int *counters, long long cap, long long ccap) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) {
+        if (counters[1] > ccap) counters[1] = (int)ccap;
+        counters[3] = 4 * counters[1];
+        if (counters[0] > cap) counters[0] = (int)cap;
+    }
+}
+
+__global__ void k_gather_contacts(const int *counters, const int *perm, const int4 *ids_raw,
+                                  const int *face_raw, const float4 *tn_raw,
+                                  const double4 *w_raw, int4 *ids, int *face, float4 *tn,
+                                  double4 *w, uint32_t *ekey, int *eval_) {
+    int n = counters[1];
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        int j = perm[i];
+        int4 a = ids_raw[j];
+        ids[i] = a;
+        face[i] = face_raw[j];
+        tn[i] = tn_raw[j];
+        w[i] = w_raw[j];
+        ekey[4 * i] = (uint32_t)a.x;
+        ekey[4 * i + 1] = (uint32_t)a.y;
+        ekey[4 * i + 2] = (uint32_t)a.z;
+        ekey[4 * i + 3] = (uint32_t)a.w;
+        eval_[4 * i] = 4 * i;
+        eval_[4 * i + 1] = 4 * i + 1;
+        eval_[4 * i + 2] = 4 * i + 2;
+        eval_[4 * i + 3] = 4 * i + 3;
+    }
+}
+
+// corrections of one contact (VFResolveTest + VFResolveNew, P/CCD.cpp:1996-2090)
+__global__ void __launch_bounds__(128) k_contact_deltas(const int *counters, const int4 *ids,
+                                                        const float4 *__restrict__ x,
+                                                        const float4 *__restrict__ p, float th,
+                                                        int mass_weighted, float4 *delta) {
+    int n = counters[1];
+    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < n; c += gridDim.x * blockDim.x) {
+        int4 id = ids[c];
+        float4 q0 = x[id.x], q1 = x[id.y], q2 = x[id.z], q3 = x[id.w];
+        v3 X0 = ld3(q0), X1 = ld3(q1), X2 = ld3(q2), X3 = ld3(q3);
+        v3 P0 = ld3(p[id.x]), P1 = ld3(p[id.y]), P2 = ld3(p[id.z]), P3 = ld3(p[id.w]);
+        float wm0 = q0.w, wm1 = q1.w, wm2 = q2.w, wm3 = q3.w;
+        float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
+        float4 out[4] = {zero, zero, zero, zero};
+        v3 e1 = sub3(P2, P1), e2 = sub3(P3, P1);
+        v3 pr = cross3(e1, e2);
+        float pr2 = dot3(pr, pr);
+        bool ok = mass_weighted ? (pr2 > 1e-12f * (dot3(e1, e1) * dot3(e2, e2)))
+                                : !((double)pr2 <= 1e-6);
+        if (ok) {
+            v3 fn = nrm3(cross3(sub3(X2, X1), sub3(X3, X1)));
+            bool dir = dot3(sub3(X0, X1), fn) >= 0;  // RelativePos
+            v3 pn = nrm3(pr);
+            float sg = dir ? 1.0f : -1.0f;
+            v3 ns = mul3(pn, sg);
+            float gap = (float)((double)dot3(sub3(P0, P1), ns) - 2.0 * (double)th);
+            if (gap < -1e-6f) {
+                v3 p1proj = add3(P1, mul3(mul3(ns, 2.0f), th));
+                float depth = (float)((double)dot3(sub3(p1proj, P0), ns) * 0.5);
+                v3 w = bary(P0, P1, P2, P3);
+                v3 dv, d1, d2, d3;
+                bool act = true;
+                if (!mass_weighted) {
+                    v3 vfix = mul3(ns, depth);
+                    v3 ffix = mul3(mul3(pn, -sg), depth);
+                    float sw = w.x * w.x + w.y * w.y + w.z * w.z;
+                    dv = vfix;
+                    d1 = div3(mul3(ffix, w.x), sw);
+                    d2 = div3(mul3(ffix, w.y), sw);
+                    d3 = div3(mul3(ffix, w.z), sw);
+                } else {
+                    float sw = w.x * w.x + w.y * w.y + w.z * w.z;
+                    float swm = w.x * w.x * wm1 + w.y * w.y * wm2 + w.z * w.z * wm3;
+                    float mf = swm / sw;
+                    float msum = wm0 + mf;
+                    if (!(msum > 0.0f) || !(sw > 0.0f)) {
+                        act = false;
+                    } else {
+                        float alpha = wm0 / msum;
+                        float sep = 2.0f * depth;
+                        dv = mul3(ns, sep * alpha);
+                        float fs = swm > 0.0f ? -sep * (1.0f - alpha) / swm : 0.0f;
+                        d1 = mul3(ns, fs * w.x * wm1);
+                        d2 = mul3(ns, fs * w.y * wm2);
+                        d3 = mul3(ns, fs * w.z * wm3);
+                    }
+                }
+                if (act) {
+                    out[0] = make_float4(dv.x, dv.y, dv.z, 1.f);
+                    out[1] = make_float4(d1.x, d1.y, d1.z, 1.f);
+                    out[2] = make_float4(d2.x, d2.y, d2.z, 1.f);
+                    out[3] = make_float4(d3.x, d3.y, d3.z, 1.f);
+                }
+            }
+        }
+        delta[4 * c] = out[0];
+        delta[4 * c + 1] = out[1];
+        delta[4 * c + 2] = out[2];
+        delta[4 * c + 3] = out[3];
+    }
+}
+
+// mean of the active corrections per point, summed in contact order
+__global__ void k_apply_deltas(const int *counters, const uint32_t *sekey, const int *seval,
+                               const float4 *delta, float4 *p) {
+    int n = counters[3];
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        uint32_t pt = sekey[i];
+        if (i > 0 && sekey[i - 1] == pt) continue;
+        float ax = 0.f, ay = 0.f, az = 0.f;
+        int cnt = 0;
+        for (int e = i; e < n && sekey[e] == pt; ++e) {
+            float4 d = delta[seval[e]];
+            if (d.w != 0.f) {
+                ax = ax + d.x;
+                ay = ay + d.y;
+                az = az + d.z;
+                ++cnt;
+            }
+        }
+        if (cnt) {
+            float4 P = p[pt];
+            float fc = (float)cnt;
+            p[pt] = make_float4(P.x + ax / fc, P.y + ay / fc, P.z + az / fc, P.w);
+        }
+    }
+}
+
+int bits_for(long long maxval) {
+    int b = 0;
+    while (b < 63 && (1LL << b) <= maxval) ++b;
+    return b < 1 ? 1 : b;
+}
+int round8(int b) { return (b + 7) / 8 * 8; }
+
+GridParams params_of(const pbd_shs *h) {
+    GridParams g;
+    g.start = make_float3(h->start[0], h->start[1], h->start[2]);
+    g.cell = make_float3(h->cell[0], h->cell[1], h->cell[2]);
+    g.size = make_int3(h->size[0], h->size[1], h->size[2]);
+    g.hashed = h->hashed;
+    g.nb = (uint32_t)h->n_buckets;
+    return g;
+}
+
+constexpr int kPersistentBlocks = 8 * kNumSMs;
+
+}  // namespace
+
+// UpdateSH on the object's predicted positions
+int shs_update(pbd_shs *h) {
+    PBD_CHECK(h->initialized, PBD_ERR_STATE, "spatial hash used before InitSH");
+    pbd_object *o = h->obj;
+    cudaStream_t s = o->stream;
+    GridParams g = params_of(h);
+    if (o->nt == 0) return PBD_OK;
+    // clear the ranges of the buckets the previous update filled
+    k_reset_buckets<<<kPersistentBlocks, 256, 0, s>>>(h->skey, h->n_valid.p, g.nb, h->bstart.p,
+                                                      h->bend.p, o->nt);
+    PBD_CUDA(cudaMemsetAsync(h->n_valid.p, 0, sizeof(int), s));
+    float margin = 0.0f;  // AABB margin is added per collision solver (see ccd_detect)
+    k_tri_cells<<<grid_for(o->nt, 256), 256, 0, s>>>(o->nt, g, margin, o->tri.p, o->x.p, o->p.p,
+                                                     h->tcell.p, h->tlo.p, h->thi.p, h->key.p,
+                                                     h->id.p, h->n_valid.p);
+    PBD_LAUNCH();
+    PBD_TRY(radix_sort<uint32_t>(h->key.p, h->id.p, h->key_alt.p, h->id_alt.p, o->nt, nullptr,
+                                 round8(h->key_bits), h->scr, s, &h->skey, &h->sid));
+    k_bucket_ranges<<<kPersistentBlocks, 256, 0, s>>>(h->skey, h->sid, h->n_valid.p, h->tcell.p,
+                                                      h->bstart.p, h->bend.p, h->scell.p);
+    PBD_LAUNCH();
+    return PBD_OK;
+}
+
+static int colli_alloc(pbd_colli *c) {
+    pbd_object *o = c->obj;
+    PBD_TRY(c->cand.alloc(c->cand_cap));
+    PBD_TRY(c->counters.alloc(8));
+    size_t H = (size_t)c->contact_cap;
+    PBD_TRY(c->ckey.alloc(H));
+    PBD_TRY(c->ckey_alt.alloc(H));
+    PBD_TRY(c->cperm.alloc(H));
+    PBD_TRY(c->cperm_alt.alloc(H));
+    PBD_TRY(c->cids_raw.alloc(H));
+    PBD_TRY(c->cids.alloc(H));
+    PBD_TRY(c->cface_raw.alloc(H));
+    PBD_TRY(c->cface.alloc(H));
+    PBD_TRY(c->ctn_raw.alloc(H));
+    PBD_TRY(c->ctn.alloc(H));
+    PBD_TRY(c->cw_raw.alloc(H));
+    PBD_TRY(c->cw.alloc(H));
+    PBD_TRY(c->delta.alloc(4 * H));
+    PBD_TRY(c->ekey.alloc(4 * H));
+    PBD_TRY(c->ekey_alt.alloc(4 * H));
+    PBD_TRY(c->eval_.alloc(4 * H));
+    PBD_TRY(c->eval_alt.alloc(4 * H));
+    PBD_TRY(c->scr.hist.alloc(radix_hist_size(4 * (long long)H)));
+    PBD_TRY(c->scr.carry.alloc(256));
+    (void)o;
+    return PBD_OK;
+}
+
+// CCD_SH_Extended on the device; no host synchronisation
+int ccd_detect(pbd_colli *c) {
+    PBD_CHECK(c && c->obj && c->shs, PBD_ERR_STATE, "collision solver needs a target and a hash");
+    PBD_CHECK(c->shs->obj == c->obj, PBD_ERR_ARG, "hash and collision solver target differ");
+    pbd_object *o = c->obj;
+    pbd_shs *h = c->shs;
+    cudaStream_t s = o->stream;
+    if (!c->cand.p) PBD_TRY(colli_alloc(c));
+    PBD_CUDA(cudaMemsetAsync(c->counters.p, 0, sizeof(int) * 8, s));
+    if (o->nt == 0) return PBD_OK;
+    PBD_TRY(shs_update(h));
+    GridParams g = params_of(h);
+    float th = c->thickness;
+    // per-axis reach of a hit: 2h off the plane + 3h inside the inflated
+    // triangle (barycentric epsilon = h / mean edge), with slack
+    float margin = 5.5f * th + 2e-6f;
+    float reach = 4.5f * th + 2e-6f;
+    // add the margin to the triangle AABBs (those not flagged as slivers)
+    // inside k_candidates by expanding the point AABB instead
+    (void)margin;
+    k_candidates<<<grid_for(o->n, 128), 128, 0, s>>>(
+        o->n, g, margin, reach, o->tri.p, o->pt_tri_first.p, o->pt_tri_last.p, o->pt_tri.p,
+        o->has_inst ? o->point_inst.p : nullptr, o->x.p, o->p.p, h->tcell.p, h->tlo.p, h->thi.p,
+        h->bstart.p, h->bend.p, h->scell.p, h->sid, c->cand.p, c->cand_cap, c->counters.p);
+    PBD_LAUNCH();
+    k_narrow<<<kPersistentBlocks, 128, 0, s>>>(c->cand.p, c->cand_cap, o->nt, th, o->tri.p, o->x.p,
+                                               o->p.p, c->counters.p, c->contact_cap, c->ckey.p,
+                                               c->cperm.p, c->cids_raw.p, c->cface_raw.p,
+                                               c->ctn_raw.p, c->cw_raw.p);
+    k_clamp_counts<<<1, 32, 0, s>>>(c->counters.p, c->cand_cap, c->contact_cap);
+    PBD_LAUNCH();
+    unsigned long long *sk;
+    int *sp;
+    int kb = round8(bits_for((long long)o->n * (long long)o->nt));
+    PBD_TRY(radix_sort<unsigned long long>(c->ckey.p, c->cperm.p, c->ckey_alt.p, c->cperm_alt.p,
+                                           c->contact_cap, c->counters.p + 1, kb, c->scr, s, &sk,
+                                           &sp));
+    k_gather_contacts<<<kPersistentBlocks, 256, 0, s>>>(c->counters.p, sp, c->cids_raw.p,
+                                                        c->cface_raw.p, c->ctn_raw.p, c->cw_raw.p,
+                                                        c->cids.p, c->cface.p, c->ctn.p, c->cw.p,
+                                                        c->ekey.p, c->eval_.p);
+    PBD_LAUNCH();
+    PBD_TRY(radix_sort<uint32_t>(c->ekey.p, c->eval_.p, c->ekey_alt.p, c->eval_alt.p,
+                                 4 * c->contact_cap, c->counters.p + 3, round8(bits_for(o->n)),
+                                 c->scr, s, &c->sekey, &c->seval));
+    return PBD_OK;
+}
+
+int ccd_resolve(pbd_colli *c, int passes) {
+    pbd_object *o = c->obj;
+    cudaStream_t s = o->stream;
+    if (!c->cand.p || o->nt == 0) return PBD_OK;
+    for (int k = 0; k < passes; ++k) {
+        k_contact_deltas<<<kPersistentBlocks, 128, 0, s>>>(c->counters.p, c->cids.p, o->x.p, o->p.p,
+                                                           c->thickness,
+                                                           c->response == PBD_RESPONSE_MASS_WEIGHTED,
+                                                           c->delta.p);
+        k_apply_deltas<<<kPersistentBlocks, 256, 0, s>>>(c->counters.p, c->sekey, c->seval,
+                                                         c->delta.p, o->p.p);
+        PBD_LAUNCH();
+    }
+    return PBD_OK;
+}
+
+}  // namespace pbd
+
+using namespace pbd;
+
+extern "C" {
+
+static int shs_alloc(pbd_shs *h) {
+    pbd_object *o = h->obj;
+    size_t nt = o->nt ? o->nt : 1;
+    PBD_TRY(h->tcell.alloc(nt));
+    PBD_TRY(h->tlo.alloc(nt));
+    PBD_TRY(h->thi.alloc(nt));
+    PBD_TRY(h->key.alloc(nt));
+    PBD_TRY(h->key_alt.alloc(nt));
+    PBD_TRY(h->id.alloc(nt));
+    PBD_TRY(h->id_alt.alloc(nt));
+    PBD_TRY(h->scell.alloc(nt));
+    PBD_TRY(h->n_valid.alloc(1));
+    PBD_TRY(h->bstart.alloc((size_t)h->n_buckets + 1));
+    PBD_TRY(h->bend.alloc((size_t)h->n_buckets + 1));
+    PBD_TRY(h->scr.hist.alloc(radix_hist_size((long long)nt)));
+    PBD_TRY(h->scr.carry.alloc(256));
+    PBD_CUDA(cudaMemsetAsync(h->bstart.p, 0, sizeof(int) * (h->n_buckets + 1), o->stream));
+    PBD_CUDA(cudaMemsetAsync(h->bend.p, 0, sizeof(int) * (h->n_buckets + 1), o->stream));
+    PBD_CUDA(cudaMemsetAsync(h->n_valid.p, 0, sizeof(int), o->stream));
+    h->skey = h->key.p;
+    h->sid = h->id.p;
+    return PBD_OK;
+}
+
+int pbd_shs_create(pbd_object *obj, const float *center, const int *size, const float *cell,
+                   pbd_shs **out) {
+    PBD_CHECK(obj && center && size && cell && out, PBD_ERR_ARG, "null argument");
+    PBD_CHECK(size[0] > 0 && size[1] > 0 && size[2] > 0, PBD_ERR_ARG, "grid size must be > 0");
+    long long ncell = (long long)size[0] * size[1] * size[2];
+    PBD_CHECK(ncell < (1LL << 30), PBD_ERR_ARG, "grid has too many cells (%lld)", ncell);
+    PBD_CHECK(cell[0] > 0 && cell[1] > 0 && cell[2] > 0, PBD_ERR_ARG, "cell size must be > 0");
+    pbd_shs *h = new pbd_shs();
+    h->obj = obj;
+    for (int k = 0; k < 3; ++k) {
+        h->center[k] = center[k];
+        h->size[k] = size[k];
+        h->cell[k] = cell[k];
+    }
+    h->n_buckets = (int)ncell;
+    h->key_bits = bits_for(ncell);  // keys 0..ncell (ncell = outside)
+    *out = h;
+    return PBD_OK;
+}
+
+int pbd_shs_create_hashed(pbd_object *obj, const float *cell, int log2_table, pbd_shs **out) {
+    PBD_CHECK(obj && cell && out, PBD_ERR_ARG, "null argument");
+    PBD_CHECK(log2_table >= 4 && log2_table <= 28, PBD_ERR_ARG, "log2_table must be 4..28");
+    PBD_CHECK(cell[0] > 0 && cell[1] > 0 && cell[2] > 0, PBD_ERR_ARG, "cell size must be > 0");
+    pbd_shs *h = new pbd_shs();
+    h->obj = obj;
+    h->hashed = true;
+    h->log2_table = log2_table;
+    for (int k = 0; k < 3; ++k) {
+        h->cell[k] = cell[k];
+        h->size[k] = 0;
+    }
+    h->n_buckets = 1 << log2_table;
+    h->key_bits = log2_table;
+    *out = h;
+    return PBD_OK;
+}
+
+int pbd_shs_destroy(pbd_shs *h) {
+    if (h && h->obj && h->obj->stream) cudaStreamSynchronize(h->obj->stream);
+    delete h;
+    return PBD_OK;
+}
+
+int pbd_shs_set_grid_center(pbd_shs *h, const float *c) {
+    PBD_CHECK(h && c, PBD_ERR_ARG, "null argument");
+    for (int k = 0; k < 3; ++k) h->center[k] = c[k];
+    h->initialized = false;
+    return PBD_OK;
+}
+
+int pbd_shs_set_grid_size(pbd_shs *h, const int *size) {
+    PBD_CHECK(h && size && !h->hashed, PBD_ERR_ARG, "bad argument");
+    long long ncell = (long long)size[0] * size[1] * size[2];
+    PBD_CHECK(size[0] > 0 && size[1] > 0 && size[2] > 0 && ncell < (1LL << 30), PBD_ERR_ARG,
+              "bad grid size");
+    for (int k = 0; k < 3; ++k) h->size[k] = size[k];
+    h->n_buckets = (int)ncell;
+    h->key_bits = bits_for(ncell);
+    h->initialized = false;
+    h->bstart.release();
+    return PBD_OK;
+}
+
+int pbd_shs_set_division(pbd_shs *h, const float *cell) {
+    PBD_CHECK(h && cell && cell[0] > 0 && cell[1] > 0 && cell[2] > 0, PBD_ERR_ARG, "bad cell");
+    for (int k = 0; k < 3; ++k) h->cell[k] = cell[k];
+    h->initialized = false;
+    return PBD_OK;
+}
+
+int pbd_shs_init(pbd_shs *h) {
+    PBD_CHECK(h, PBD_ERR_ARG, "null argument");
+    // m_girdStartPos = center - (gridSize * cellSize) / 2 (P/SpatialHashSystem.cpp:91-94)
+    for (int k = 0; k < 3; ++k) {
+        float shift = ((float)(unsigned)h->size[k] * h->cell[k]) / 2.0f;
+        h->start[k] = h->center[k] - shift;
+    }
+    if (!h->bstart.p || h->bstart.n < (size_t)h->n_buckets + 1) PBD_TRY(shs_alloc(h));
+    h->initialized = true;
+    return shs_update(h);
+}
+
+int pbd_shs_update(pbd_shs *h) {
+    PBD_CHECK(h, PBD_ERR_ARG, "null argument");
+    return shs_update(h);
+}
+
+int pbd_shs_find_neighbors_all(pbd_shs *h, int *start_num, int *out, long long cap,
+                               long long *total) {
+    PBD_CHECK(h && total, PBD_ERR_ARG, "null argument");
+    PBD_CHECK(h->initialized, PBD_ERR_STATE, "InitSH has not run");
+    pbd_object *o = h->obj;
+    cudaStream_t s = o->stream;
+    int nt = o->nt;
+    *total = 0;
+    if (!nt) return PBD_OK;
+    DBuf<int> cnt, off, tot;
+    PBD_TRY(cnt.alloc(nt));
+    PBD_TRY(off.alloc(nt));
+    PBD_TRY(tot.alloc(1));
+    GridParams g = params_of(h);
+    k_find_neighbors<<<grid_for(nt, 128), 128, 0, s>>>(nt, g, h->tcell.p, h->bstart.p, h->bend.p,
+                                                       h->scell.p, h->sid, nullptr, cnt.p, nullptr);
+    PBD_LAUNCH();
+    PBD_TRY(exclusive_scan(cnt.p, off.p, nt, tot.p, s));
+    int t = 0;
+    PBD_CUDA(cudaMemcpyAsync(&t, tot.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+    PBD_CUDA(cudaStreamSynchronize(s));
+    *total = t;
+    if (start_num) {
+        std::vector<int> hc(nt), ho(nt);
+        PBD_CUDA(cudaMemcpyAsync(hc.data(), cnt.p, sizeof(int) * nt, cudaMemcpyDeviceToHost, s));
+        PBD_CUDA(cudaMemcpyAsync(ho.data(), off.p, sizeof(int) * nt, cudaMemcpyDeviceToHost, s));
+        PBD_CUDA(cudaStreamSynchronize(s));
+        for (int i = 0; i < nt; ++i) {
+            start_num[2 * i] = ho[i];
+            start_num[2 * i + 1] = hc[i];
+        }
+    }
+    if (out && t > 0) {
+        PBD_CHECK(cap >= t, PBD_ERR_OVERFLOW, "neighbor output needs %d entries", t);
+        DBuf<int> dout;
+        PBD_TRY(dout.alloc(t));
+        k_find_neighbors<<<grid_for(nt, 128), 128, 0, s>>>(nt, g, h->tcell.p, h->bstart.p,
+                                                           h->bend.p, h->scell.p, h->sid, off.p,
+                                                           nullptr, dout.p);
+        PBD_LAUNCH();
+        PBD_CUDA(cudaMemcpyAsync(out, dout.p, sizeof(int) * t, cudaMemcpyDeviceToHost, s));
+        PBD_CUDA(cudaStreamSynchronize(s));
+    }
+    return PBD_OK;
+}
+
+int pbd_shs_find_neighbors(pbd_shs *h, int tri, int *out, int cap, int *n) {
+    PBD_CHECK(h && n && h->obj && tri >= 0 && tri < h->obj->nt, PBD_ERR_ARG, "bad argument");
+    long long total = 0;
+    std::vector<int> sn(2 * (size_t)h->obj->nt);
+    PBD_TRY(pbd_shs_find_neighbors_all(h, sn.data(), nullptr, 0, &total));
+    std::vector<int> all(total > 0 ? total : 1);
+    PBD_TRY(pbd_shs_find_neighbors_all(h, nullptr, all.data(), total, &total));
+    *n = sn[2 * tri + 1];
+    for (int i = 0; i < *n && i < cap && out; ++i) out[i] = all[sn[2 * tri] + i];
+    return PBD_OK;
+}
+
+int pbd_colli_create(pbd_colli **out) {
+    PBD_CHECK(out, PBD_ERR_ARG, "null argument");
+    *out = new pbd_colli();
+    return PBD_OK;
+}
+
+int pbd_colli_destroy(pbd_colli *c) {
+    if (c && c->obj && c->obj->stream) cudaStreamSynchronize(c->obj->stream);
+    delete c;
+    return PBD_OK;
+}
+
+int pbd_colli_set_target(pbd_colli *c, pbd_object *o) {
+    PBD_CHECK(c && o, PBD_ERR_ARG, "null argument");
+    c->obj = o;
+    return PBD_OK;
+}
+int pbd_colli_set_acce_struct(pbd_colli *c, pbd_shs *h) {
+    PBD_CHECK(c && h, PBD_ERR_ARG, "null argument");
+    c->shs = h;
+    return PBD_OK;
+}
+int pbd_colli_set_thickness(pbd_colli *c, float th) {
+    PBD_CHECK(c && th >= 0.f, PBD_ERR_ARG, "bad thickness");
+    c->thickness = th;
+    return PBD_OK;
+}
+int pbd_colli_set_iterations(pbd_colli *c, int it) {
+    PBD_CHECK(c && it >= 0, PBD_ERR_ARG, "bad iterations");
+    c->iterations = it;
+    return PBD_OK;
+}
+int pbd_colli_set_response(pbd_colli *c, int mode) {
+    PBD_CHECK(c && (mode == PBD_RESPONSE_REFERENCE || mode == PBD_RESPONSE_MASS_WEIGHTED),
+              PBD_ERR_ARG, "bad response mode");
+    c->response = mode;
+    return PBD_OK;
+}
+int pbd_colli_set_capacity(pbd_colli *c, long long cand, long long contacts) {
+    PBD_CHECK(c && cand > 0 && contacts > 0 && cand < (1LL << 31) && 4 * contacts < (1LL << 31),
+              PBD_ERR_ARG, "bad capacity");
+    c->cand_cap = cand;
+    c->contact_cap = contacts;
+    c->cand.release();
+    return PBD_OK;
+}
+
+int pbd_colli_ccd_sh_extended(pbd_colli *c) {
+    PBD_CHECK(c, PBD_ERR_ARG, "null argument");
+    PBD_TRY(ccd_detect(c));
+    int hc[4] = {0, 0, 0, 0};
+    PBD_CUDA(cudaMemcpyAsync(hc, c->counters.p, sizeof(hc), cudaMemcpyDeviceToHost, c->obj->stream));
+    PBD_CUDA(cudaStreamSynchronize(c->obj->stream));
+    PBD_CHECK(!(hc[2] & 3), PBD_ERR_OVERFLOW,
+              "CCD capacity exceeded (flags %d): raise pbd_colli_set_capacity", hc[2]);
+    return PBD_OK;
+}
+
+int pbd_colli_collision_resolve_new(pbd_colli *c) {
+    PBD_CHECK(c && c->obj, PBD_ERR_STATE, "collision solver has no target");
+    return ccd_resolve(c, c->iterations);
+}
+
+int pbd_colli_get_contacts(pbd_colli *c, int *ids, int *face, float *t, double *w, float *n,
+                           long long cap, long long *count) {
+    PBD_CHECK(c && count, PBD_ERR_ARG, "null argument");
+    *count = 0;
+    if (!c->counters.p) return PBD_OK;
+    cudaStream_t s = c->obj->stream;
+    int hc[4];
+    PBD_CUDA(cudaMemcpyAsync(hc, c->counters.p, sizeof(hc), cudaMemcpyDeviceToHost, s));
+    PBD_CUDA(cudaStreamSynchronize(s));
+    long long h = hc[1];
+    *count = h;
+    long long m = std::min(h, cap);
+    if (m <= 0) return PBD_OK;
+    std::vector<int4> hi(m);
+    std::vector<float4> htn(m);
+    std::vector<double4> hw(m);
+    PBD_CUDA(cudaMemcpyAsync(hi.data(), c->cids.p, sizeof(int4) * m, cudaMemcpyDeviceToHost, s));
+    PBD_CUDA(cudaMemcpyAsync(htn.data(), c->ctn.p, sizeof(float4) * m, cudaMemcpyDeviceToHost, s));
+    PBD_CUDA(cudaMemcpyAsync(hw.data(), c->cw.p, sizeof(double4) * m, cudaMemcpyDeviceToHost, s));
+    if (face) PBD_CUDA(cudaMemcpyAsync(face, c->cface.p, sizeof(int) * m, cudaMemcpyDeviceToHost, s));
+    PBD_CUDA(cudaStreamSynchronize(s));
+    for (long long i = 0; i < m; ++i) {
+        if (ids) {
+            ids[4 * i] = hi[i].x;
+            ids[4 * i + 1] = hi[i].y;
+            ids[4 * i + 2] = hi[i].z;
+            ids[4 * i + 3] = hi[i].w;
+        }
+        if (t) t[i] = htn[i].x;
+        if (n) {
+            n[3 * i] = htn[i].y;
+            n[3 * i + 1] = htn[i].z;
+            n[3 * i + 2] = htn[i].w;
+        }
+        if (w) {
+            w[4 * i] = hw[i].x;
+            w[4 * i + 1] = hw[i].y;
+            w[4 * i + 2] = hw[i].z;
+            w[4 * i + 3] = hw[i].w;
+        }
+    }
+    return PBD_OK;
+}
+
+int pbd_colli_stats(pbd_colli *c, long long *cand, long long *contacts, int *overflow) {
+    PBD_CHECK(c, PBD_ERR_ARG, "null argument");
+    int hc[4] = {0, 0, 0, 0};
+    if (c->counters.p) {
+        PBD_CUDA(cudaMemcpyAsync(hc, c->counters.p, sizeof(hc), cudaMemcpyDeviceToHost, c->obj->stream));
+        PBD_CUDA(cudaStreamSynchronize(c->obj->stream));
+    }
+    if (cand) *cand = hc[0];
+    if (contacts) *contacts = hc[1];
+    if (overflow) *overflow = hc[2];
+    return PBD_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,230 @@
+// pbd_common.cuh -- shared plumbing of libpbd_gb300: error reporting, device
+// buffers, launch helpers, and the object / solver / collision structs.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <cstdarg>
+#include <cstdio>
+#include <string>
+#include <vector>
+
+#include "pbd_c.h"
+
+namespace pbd {
+
+void set_error(const char *fmt, ...);
+
+#define PBD_CUDA(call)                                                                  \
+    do {                                                                                \
+        cudaError_t e_ = (call);                                                        \
+        if (e_ != cudaSuccess) {                                                        \
+            ::pbd::set_error("%s failed: %s (%s:%d)", #call, cudaGetErrorString(e_),    \
+                             __FILE__, __LINE__);                                       \
+            return e_ == cudaErrorMemoryAllocation ? PBD_ERR_OOM : PBD_ERR_CUDA;        \
+        }                                                                               \
+    } while (0)
+
+#define PBD_CHECK(cond, code, ...)          \
+    do {                                    \
+        if (!(cond)) {                      \
+            ::pbd::set_error(__VA_ARGS__);  \
+            return code;                    \
+        }                                   \
+    } while (0)
+
+#define PBD_TRY(expr)                \
+    do {                             \
+        int r_ = (expr);             \
+        if (r_ != PBD_OK) return r_; \
+    } while (0)
+
+// launch-error check after a kernel launch (no synchronisation)
+#define PBD_LAUNCH() PBD_CUDA(cudaGetLastError())
+
+constexpr int kNumSMs = 152;
+
+inline int grid_for(long long n, int block) {
+    long long g = (n + block - 1) / block;
+    if (g < 1) g = 1;
+    if (g > 0x7fffffffLL) g = 0x7fffffff;
+    return (int)g;
+}
+
+// Owning device allocation; sizes in elements.
+template <class T>
+struct DBuf {
+    T *p = nullptr;
+    size_t n = 0;
+    DBuf() = default;
+    DBuf(const DBuf &) = delete;
+    DBuf &operator=(const DBuf &) = delete;
+    ~DBuf() { release(); }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+    }
+    int alloc(size_t count) {
+        if (count <= n && p) return PBD_OK;
+        release();
+        size_t bytes = (count ? count : 1) * sizeof(T);
+        cudaError_t e = cudaMalloc((void **)&p, bytes);
+        if (e != cudaSuccess) {
+            p = nullptr;
+            set_error("cudaMalloc(%zu bytes) failed: %s", bytes, cudaGetErrorString(e));
+            return e == cudaErrorMemoryAllocation ? PBD_ERR_OOM : PBD_ERR_CUDA;
+        }
+        n = count;
+        return PBD_OK;
+    }
+    int upload(const T *h, size_t count, cudaStream_t s) {
+        PBD_TRY(alloc(count));
+        if (count) PBD_CUDA(cudaMemcpyAsync(p, h, count * sizeof(T), cudaMemcpyHostToDevice, s));
+        return PBD_OK;
+    }
+};
+
+// ---- stable LSD radix sort (8-bit digits) of (key, int value) pairs --------
+// Sorts n elements (n read from d_count when non-null, capped by n_cap),
+// `bits` low key bits.  Buffers: keys/vals in and alt (same capacity), hist
+// of hist_size(n_cap) ints.  Returns the pointers holding the result.
+struct SortScratch {
+    DBuf<int> hist;
+    DBuf<int> carry;
+};
+int radix_hist_size(long long n_cap);
+template <class K>
+int radix_sort(K *keys, int *vals, K *keys_alt, int *vals_alt, long long n_cap,
+               const int *d_count, int bits, SortScratch &scr, cudaStream_t s,
+               K **keys_out, int **vals_out);
+// exclusive scan of n ints (single-block, chunked); out may alias in
+int exclusive_scan(const int *in, int *out, long long n, int *d_total, cudaStream_t s);
+
+}  // namespace pbd
+
+// ---- handle structs ------------------------------------------------------
+struct pbd_object {
+    int n = 0, nt = 0, np = 0, n_idx = 0;
+    cudaStream_t stream = nullptr;
+    float damping = 1.0f;
+    float gravity[3] = {0, 0, 0};
+    bool has_inst = false;
+    // state (w of x and p = massBuffer value)
+    pbd::DBuf<float4> x, p, v;
+    pbd::DBuf<float> mass;
+    // meshTopol triangles: (i0, i1, i2, instance)
+    pbd::DBuf<int4> tri;
+    pbd::DBuf<int> pt_tri_first, pt_tri_last, pt_tri;  // point -> incident triangles
+    pbd::DBuf<int> point_inst;
+    // constraint buffers by prim id
+    pbd::DBuf<int2> prim_list;
+    pbd::DBuf<int> indices, ctype;
+    pbd::DBuf<float> rest_length, stiffness, rest_angle;
+    pbd::DBuf<float4> rest_pos;
+    std::vector<int> h_prim_count;          // points per prim (host copy)
+    std::vector<int> h_ctype;
+    // Prim2PrimsMap
+    pbd::DBuf<int2> adj_sn;
+    pbd::DBuf<int> adj;
+    long long n_adj = 0;
+    // coloring
+    pbd::DBuf<int> color, prd_color, flag;
+    bool colored = false;
+    int n_colors = 0;
+    pbd::DBuf<int> sorted_color, sorted_prim;   // SortEdgesColors result
+    bool sorted = false;
+    std::vector<int> h_worksets;                // 2 per color
+    // per-color solver records
+    pbd::DBuf<int4> drec;                       // i0, i1, rest, stiffness
+    pbd::DBuf<int4> bidx;                       // e0, e1, wA, wB
+    pbd::DBuf<float2> bpar;                     // rest angle, stiffness
+    pbd::DBuf<float4> arec;                     // rest xyz, point id bits
+    std::vector<int> h_dseg, h_bseg, h_aseg;    // n_colors+1 starts each
+    // residual
+    double res_den = 0.0;
+    pbd::DBuf<double> res_part;
+    pbd::DBuf<double> res_out;
+    pbd::SortScratch scr;
+};
+
+struct pbd_shs {
+    pbd_object *obj = nullptr;
+    bool hashed = false;
+    int log2_table = 0;
+    float center[3] = {0, 0, 0};
+    int size[3] = {1, 1, 1};
+    float cell[3] = {1, 1, 1};
+    float start[3] = {0, 0, 0};
+    bool initialized = false;
+    int n_buckets = 0;
+    int key_bits = 0;
+    // per triangle (by id)
+    pbd::DBuf<int4> tcell;       // cell xyz, valid
+    pbd::DBuf<float4> tlo, thi;  // swept AABB of the triangle
+    pbd::DBuf<uint32_t> key, key_alt;
+    pbd::DBuf<int> id, id_alt;
+    uint32_t *skey = nullptr;    // sorted result pointers (into key/key_alt)
+    int *sid = nullptr;
+    pbd::DBuf<int4> scell;       // cell of sorted entry
+    pbd::DBuf<int> bstart, bend; // bucket -> [start, end) in sorted order
+    pbd::DBuf<int> n_valid;
+    bool table_clean = false;
+    pbd::DBuf<uint32_t> prev_keys;
+    pbd::DBuf<int> n_prev;
+    pbd::SortScratch scr;
+};
+
+struct pbd_colli {
+    pbd_object *obj = nullptr;
+    pbd_shs *shs = nullptr;
+    float thickness = 0.0f;
+    int iterations = 1;
+    int response = PBD_RESPONSE_REFERENCE;
+    long long cand_cap = 1 << 22;
+    long long contact_cap = 1 << 20;
+    // candidates (point, triangle)
+    pbd::DBuf<int2> cand;
+    pbd::DBuf<int> counters;    // [0] candidates, [1] contacts, [2] overflow, [3] entries
+    // contacts (unsorted, then sorted)
+    pbd::DBuf<unsigned long long> ckey, ckey_alt;
+    pbd::DBuf<int> cperm, cperm_alt;
+    pbd::DBuf<int4> cids_raw, cids;     // i0..i3
+    pbd::DBuf<int> cface_raw, cface;
+    pbd::DBuf<float4> ctn_raw, ctn;     // t, n
+    pbd::DBuf<double4> cw_raw, cw;
+    // response
+    pbd::DBuf<float4> delta;            // 4 per contact, w = active
+    pbd::DBuf<uint32_t> ekey, ekey_alt; // point id per entry
+    pbd::DBuf<int> eval_, eval_alt;
+    uint32_t *sekey = nullptr;
+    int *seval = nullptr;
+    pbd::SortScratch scr;
+};
+
+struct pbd_solver {
+    pbd_object *obj = nullptr;
+    int sphere_on = 0;
+    float sphere_c[3] = {0, 0, 0};
+    float sphere_r = 1.0f;
+    int ground_on = 0;
+    float ground_h = 0.0f;
+    // cached graph of pbd_solver_step
+    cudaGraphExec_t gexec = nullptr;
+    float g_dt = 0;
+    int g_sub = 0, g_it = 0;
+    pbd_colli *g_colli = nullptr;
+    int g_sig = 0;
+};
+
+// internal entry points shared between translation units
+namespace pbd {
+int launch_advect(pbd_object *o, float dt);
+int launch_integrate(pbd_object *o, float dt);
+int launch_sweep(pbd_object *o, int iter);
+int launch_obstacles(pbd_solver *s);
+int ccd_detect(pbd_colli *c);
+int ccd_resolve(pbd_colli *c, int passes);
+int shs_update(pbd_shs *h);
+}  // namespace pbd

@@ -1,0 +1,1201 @@
+// pbd_object.cu -- PBDObject, ConstraintPBD and SolverPBD on the GPU.
+//
+// Data layout in HBM (per object):
+//   x, p, v        float4 per point; x.w = p.w = massBuffer value (inverse
+//                  mass / gravity gate, 0 = pinned), so a projection reads its
+//                  weights with the positions in one 16-byte load.
+//   drec           int4 per distance constraint {i0, i1, rest, stiffness},
+//                  grouped by color (color-major), 16 B per record.
+//   bidx / bpar    int4 {e0, e1, wA, wB} + float2 {rest angle, stiffness}
+//                  per bending constraint, grouped by color.
+//   arec           float4 {rest xyz, point id} per anchor, grouped by color.
+// One kernel launch per color applies every constraint of that color; no
+// two constraints of a color share a point, so the launch has no races and
+// its result does not depend on thread order.
+//
+// Arithmetic mirrors the reference kernels operation by operation; this
+// translation unit is compiled with -fmad=false so no multiply-add is fused
+// (the reference's host path rounds every product separately).
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+
+#include "pbd_common.cuh"
+
+namespace pbd {
+
+static thread_local std::string g_err;
+void set_error(const char *fmt, ...) {
+    char buf[1024];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    g_err = buf;
+}
+
+static int bits_for(long long maxval) {
+    int b = 0;
+    while (b < 63 && (1LL << b) <= maxval) ++b;
+    return b < 1 ? 1 : b;
+}
+static int round8(int b) { return (b + 7) / 8 * 8; }
+
+// ---------------------------------------------------------------------------
+// construction kernels
+// ---------------------------------------------------------------------------
+__global__ void k_pack_state(int n, const float *pos, const float *vel, const float *mass,
+                             float4 *x, float4 *p, float4 *v) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float m = mass[i];
+    float4 a = make_float4(pos[3 * i], pos[3 * i + 1], pos[3 * i + 2], m);
+    x[i] = a;
+    p[i] = a;
+    v[i] = vel ? make_float4(vel[3 * i], vel[3 * i + 1], vel[3 * i + 2], 0.f)
+               : make_float4(0.f, 0.f, 0.f, 0.f);
+}
+
+__global__ void k_pack_tris(int nt, const int *tri, const int *inst, int4 *out) {
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nt) return;
+    out[t] = make_int4(tri[3 * t], tri[3 * t + 1], tri[3 * t + 2], inst ? inst[t] : 0);
+}
+
+// entries (point, owner) for CSR builds: owner k emits `cnt` entries
+__global__ void k_emit_prim_points(int np, const int2 *prim_list, const int *indices,
+                                   const int *eoff, uint32_t *key, int *val) {
+    int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= np) return;
+    int2 pl = prim_list[p];
+    int o = eoff[p];
+    for (int i = 0; i < pl.y; ++i) {
+        key[o + i] = (uint32_t)indices[pl.x + i];
+        val[o + i] = p;
+    }
+}
+
+__global__ void k_emit_tri_points(int nt, const int4 *tri, uint32_t *key, int *val) {
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nt) return;
+    int4 a = tri[t];
+    key[3 * t] = (uint32_t)a.x;
+    key[3 * t + 1] = (uint32_t)a.y;
+    key[3 * t + 2] = (uint32_t)a.z;
+    val[3 * t] = t;
+    val[3 * t + 1] = t;
+    val[3 * t + 2] = t;
+}
+
+// run bounds of a sorted key array: first[k] = start, last[k] = end (excl.)
+__global__ void k_run_bounds(long long n, const uint32_t *skey, int *first, int *last) {
+    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    uint32_t k = skey[i];
+    if (i == 0 || skey[i - 1] != k) first[k] = (int)i;
+    if (i == n - 1 || skey[i + 1] != k) last[k] = (int)(i + 1);
+}
+
+__global__ void k_prim_counts(int np, const int2 *prim_list, int *cnt) {
+    int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p < np) cnt[p] = prim_list[p].y;
+}
+
+// GenePrim2PrimsMap (P/PBD_cuda.cu:170-202): for each point of the prim (in
+// order), every other prim on that point (ascending id)
+__global__ void k_adj_count(int np, const int2 *prim_list, const int *indices, const int *pfirst,
+                            const int *plast, const int *pprim, int *deg) {
+    int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= np) return;
+    int2 pl = prim_list[p];
+    int d = 0;
+    for (int i = 0; i < pl.y; ++i) {
+        int pt = indices[pl.x + i];
+        for (int j = pfirst[pt]; j < plast[pt]; ++j) d += pprim[j] != p;
+    }
+    deg[p] = d;
+}
+
+__global__ void k_adj_fill(int np, const int2 *prim_list, const int *indices, const int *pfirst,
+                           const int *plast, const int *pprim, const int *off, int2 *sn,
+                           int *adj) {
+    int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= np) return;
+    int2 pl = prim_list[p];
+    int o = off[p], o0 = o;
+    for (int i = 0; i < pl.y; ++i) {
+        int pt = indices[pl.x + i];
+        for (int j = pfirst[pt]; j < plast[pt]; ++j) {
+            int q = pprim[j];
+            if (q != p) adj[o++] = q;
+        }
+    }
+    sn[p] = make_int2(o0, o - o0);
+}
+
+// ---------------------------------------------------------------------------
+// coloring (AssignColorsGPU / ResolveConflictsGPU, P/PBD_cuda.cu:313-431)
+// ---------------------------------------------------------------------------
+__global__ void k_assign_colors(int np, const int2 *__restrict__ sn, const int *__restrict__ adj,
+                                const int *__restrict__ color, int *__restrict__ prd) {
+    int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= np) return;
+    if (color[idx] >= 0) return;
+    int2 r = sn[idx];
+    int offset = 0;
+    for (;;) {
+        unsigned long long forbidden = 0ull;
+        for (int i = r.x; i < r.x + r.y; ++i) {
+            int nc = color[adj[i]] - offset;
+            if (nc >= 0 && nc < 64) forbidden |= (1ull << nc);
+        }
+        if (forbidden != ~0ull) {
+            prd[idx] = offset + __ffsll((long long)~forbidden) - 1;
+            return;
+        }
+        offset += 64;
+    }
+}
+
+__global__ void k_resolve_conflicts(int np, const int2 *__restrict__ prim_list,
+                                    const int2 *__restrict__ sn, const int *__restrict__ adj,
+                                    int *__restrict__ color, const int *__restrict__ prd,
+                                    int *flag) {
+    int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= np) return;
+    if (color[idx] >= 0) return;
+    int c = prd[idx];
+    int npt = prim_list[idx].y;
+    int2 r = sn[idx];
+    for (int i = r.x; i < r.x + r.y; ++i) {
+        int n = adj[i];
+        if (prd[n] != c) continue;
+        int nnpt = prim_list[n].y;
+        if (nnpt > npt || (nnpt == npt && n < idx)) {
+            *flag = 1;
+            return;
+        }
+    }
+    color[idx] = c;
+}
+
+__global__ void k_max_color(int np, const int *color, int *out) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < np) atomicMax(out, color[i]);
+}
+
+__global__ void k_iota_keys(int np, const int *color, uint32_t *key, int *val) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= np) return;
+    key[i] = (uint32_t)color[i];
+    val[i] = i;
+}
+
+__device__ __forceinline__ int cls_of(int t) {
+    return t == PBD_DISTANCE ? 0 : t == PBD_BENDING ? 1 : t == PBD_ANCHOR ? 2 : 3;
+}
+
+// class-major key: class * n_colors + color
+__global__ void k_class_keys(int np, const int *color, const int *ctype, int nc, uint32_t *key,
+                             int *val) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= np) return;
+    key[i] = (uint32_t)(cls_of(ctype[i]) * nc + color[i]);
+    val[i] = i;
+}
+
+__global__ void k_build_records(int n_rec, const int *sprim, const int2 *prim_list,
+                                const int *indices, const float *rest_length,
+                                const float *stiffness, const float *rest_angle,
+                                const float4 *rest_pos, int nd, int nb, int na, int4 *drec,
+                                int4 *bidx, float2 *bpar, float4 *arec) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n_rec) return;
+    int p = sprim[i];
+    int s = prim_list[p].x;
+    if (i < nd) {
+        drec[i] = make_int4(indices[s], indices[s + 1], __float_as_int(rest_length[p]),
+                            __float_as_int(stiffness[p]));
+    } else if (i < nd + nb) {
+        int j = i - nd;
+        bidx[j] = make_int4(indices[s], indices[s + 1], indices[s + 2], indices[s + 3]);
+        bpar[j] = make_float2(rest_angle ? rest_angle[p] : 0.f, stiffness[p]);
+    } else if (i < nd + nb + na) {
+        int j = i - nd - nb;
+        float4 r = rest_pos ? rest_pos[p] : make_float4(0.f, 0.f, 0.f, 0.f);
+        arec[j] = make_float4(r.x, r.y, r.z, __int_as_float(indices[s]));
+    }
+}
+
+// ---------------------------------------------------------------------------
+// solver kernels
+// ---------------------------------------------------------------------------
+
+// AdvectGPUKernel (P/PBD_cuda.cu:949-979): v += (g*dt)*m; v *= damping^dt;
+// p = x + v*dt.  gdt = g*dt and damp_pow = powf(damping, dt) come from the host.
+__global__ void __launch_bounds__(256) k_advect(int n, float dt, float damp_pow, float3 gdt,
+                                                const float4 *__restrict__ x,
+                                                float4 *__restrict__ v, float4 *__restrict__ p) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float4 X = x[i], V = v[i];
+    float m = X.w;
+    V.x = V.x + gdt.x * m;
+    V.y = V.y + gdt.y * m;
+    V.z = V.z + gdt.z * m;
+    V.x = V.x * damp_pow;
+    V.y = V.y * damp_pow;
+    V.z = V.z * damp_pow;
+    v[i] = make_float4(V.x, V.y, V.z, 0.f);
+    p[i] = make_float4(X.x + V.x * dt, X.y + V.y * dt, X.z + V.z * dt, m);
+}
+
+// IntegrationGPUKernel (P/PBD_cuda.cu:1467-1482): v = (p - x)/dt; x = p
+__global__ void __launch_bounds__(256) k_integrate(int n, float dt, float4 *__restrict__ x,
+                                                   float4 *__restrict__ v,
+                                                   const float4 *__restrict__ p) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float4 P = p[i], X = x[i];
+    v[i] = make_float4((P.x - X.x) / dt, (P.y - X.y) / dt, (P.z - X.z) / dt, 0.f);
+    x[i] = make_float4(P.x, P.y, P.z, X.w);
+}
+
+// distance constraint of ProjectContraintsGPUKernel (P/PBD_cuda.cu:1264-1294)
+__device__ __forceinline__ void project_distance(int4 r, float4 *__restrict__ p, float expk) {
+    float4 P0 = p[r.x], P1 = p[r.y];
+    float m0 = P0.w, m1 = P1.w;
+    float msum = m0 + m1;
+    float dx = P0.x - P1.x, dy = P0.y - P1.y, dz = P0.z - P1.z;
+    float d = sqrtf(dx * dx + dy * dy + dz * dz);
+    if (msum == 0.f || d == 0.f) return;
+    float rest = __int_as_float(r.z), s = __int_as_float(r.w);
+    float k = 1.f - powf(1.f - s, expk);
+    float s0 = -m0 / msum * (d - rest);
+    float s1 = m1 / msum * (d - rest);
+    p[r.x] = make_float4(P0.x + ((dx * s0) / d) * k, P0.y + ((dy * s0) / d) * k,
+                         P0.z + ((dz * s0) / d) * k, m0);
+    p[r.y] = make_float4(P1.x + ((dx * s1) / d) * k, P1.y + ((dy * s1) / d) * k,
+                         P1.z + ((dz * s1) / d) * k, m1);
+}
+
+struct v3 {
+    float x, y, z;
+};
+__device__ __forceinline__ v3 mk3(float x, float y, float z) { return {x, y, z}; }
+__device__ __forceinline__ v3 sub3(v3 a, v3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+__device__ __forceinline__ v3 add3(v3 a, v3 b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
+__device__ __forceinline__ v3 mul3(v3 a, float s) { return {a.x * s, a.y * s, a.z * s}; }
+__device__ __forceinline__ v3 div3(v3 a, float s) { return {a.x / s, a.y / s, a.z / s}; }
+__device__ __forceinline__ float dot3(v3 a, v3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+__device__ __forceinline__ v3 cross3(v3 a, v3 b) {
+    return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
+}
+
+// dihedral bending: signed angle theta = atan2((nA x nB).E/|E|, nA.nB),
+// C = theta - theta0, dp_i = w_i * k*C/sum_j w_j|u_j|^2 * u_i with the
+// Bridson-Marino-Fedkiw (2003) gradients grad_i theta = -u_i, inside the
+// PBD projection of Mueller et al. (2007).  Same operation order as the
+// oracle's orc_bending_project_f32.
+__device__ __forceinline__ void project_bending(int4 r, float2 par, float4 *__restrict__ p,
+                                                float expk) {
+    float4 Q0 = p[r.x], Q1 = p[r.y], Q2 = p[r.z], Q3 = p[r.w];
+    v3 e0 = mk3(Q0.x, Q0.y, Q0.z), e1 = mk3(Q1.x, Q1.y, Q1.z);
+    v3 wa = mk3(Q2.x, Q2.y, Q2.z), wb = mk3(Q3.x, Q3.y, Q3.z);
+    v3 E = sub3(e1, e0);
+    v3 na = cross3(sub3(wa, e0), sub3(wa, e1));
+    v3 nb = cross3(sub3(wb, e1), sub3(wb, e0));
+    float na2 = dot3(na, na), nb2 = dot3(nb, nb), el2 = dot3(E, E);
+    if (na2 == 0.f || nb2 == 0.f || el2 == 0.f) return;
+    float el = sqrtf(el2);
+    float sn = dot3(cross3(na, nb), E) / el;
+    float cs = dot3(na, nb);
+    float c = atan2f(sn, cs) - par.x;
+    if (c > 3.14159265f) c -= 6.28318531f;
+    if (c < -3.14159265f) c += 6.28318531f;
+    v3 a = div3(na, na2), b = div3(nb, nb2);
+    v3 uwa = mul3(a, el), uwb = mul3(b, el);
+    v3 ue0 = add3(mul3(a, dot3(sub3(wa, e1), E) / el), mul3(b, dot3(sub3(wb, e1), E) / el));
+    v3 ue1 = sub3(mul3(a, -dot3(sub3(wa, e0), E) / el), mul3(b, dot3(sub3(wb, e0), E) / el));
+    float den = Q0.w * dot3(ue0, ue0) + Q1.w * dot3(ue1, ue1) + Q2.w * dot3(uwa, uwa) +
+                Q3.w * dot3(uwb, uwb);
+    if (!(den > 0.f)) return;
+    float k = 1.f - powf(1.f - par.y, expk);
+    float s = k * c / den;
+    v3 n0 = add3(e0, mul3(ue0, Q0.w * s));
+    v3 n1 = add3(e1, mul3(ue1, Q1.w * s));
+    v3 n2 = add3(wa, mul3(uwa, Q2.w * s));
+    v3 n3 = add3(wb, mul3(uwb, Q3.w * s));
+    p[r.x] = make_float4(n0.x, n0.y, n0.z, Q0.w);
+    p[r.y] = make_float4(n1.x, n1.y, n1.z, Q1.w);
+    p[r.z] = make_float4(n2.x, n2.y, n2.z, Q2.w);
+    p[r.w] = make_float4(n3.x, n3.y, n3.z, Q3.w);
+}
+
+// one color phase: distance, then bending, then anchor records of the color
+__global__ void __launch_bounds__(256) k_project_color(const int4 *__restrict__ drec, int nd,
+                                                       const int4 *__restrict__ bidx,
+                                                       const float2 *__restrict__ bpar, int nb,
+                                                       const float4 *__restrict__ arec, int na,
+                                                       float4 *__restrict__ p, float expk) {
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < nd) {
+        project_distance(drec[t], p, expk);
+    } else if (t < nd + nb) {
+        int j = t - nd;
+        project_bending(bidx[j], bpar[j], p, expk);
+    } else if (t < nd + nb + na) {
+        // ANCHOR (P/PBD_cuda.cu:1298-1305): snap the point to its rest position
+        float4 a = arec[t - nd - nb];
+        int i = __float_as_int(a.w);
+        p[i] = make_float4(a.x, a.y, a.z, p[i].w);
+    }
+}
+
+// ColliWithShpGrd (P/PBD_cuda.cu:1519-1573): sphere push-out and ground plane
+__global__ void k_obstacles(int n, float4 *p, int sphere_on, float3 c, float r, int ground_on,
+                            float gh) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float4 P = p[i];
+    if (sphere_on) {
+        float dx = P.x - c.x, dy = P.y - c.y, dz = P.z - c.z;
+        float d = sqrtf(dx * dx + dy * dy + dz * dz);
+        if (!(d - r > 0.001f)) {
+            float ex = c.x - P.x, ey = c.y - P.y, ez = c.z - P.z;
+            float d2 = sqrtf(ex * ex + ey * ey + ez * ez);
+            float move = r - d2;
+            float mx = (dx / d2) * move, my = (dy / d2) * move, mz = (dz / d2) * move;
+            P.x = P.x + mx;
+            P.y = P.y + my;
+            P.z = P.z + mz;
+        }
+    }
+    if (ground_on && P.y - gh < 0.001f) P.y = gh;
+    p[i] = P;
+}
+
+// residual: FP64 per constraint, warp-shuffle + block reduction
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    return v;
+}
+
+__global__ void __launch_bounds__(256) k_residual(const int4 *__restrict__ drec, int nd,
+                                                  const int4 *__restrict__ bidx,
+                                                  const float2 *__restrict__ bpar, int nb,
+                                                  const float4 *__restrict__ p, double *part) {
+    __shared__ double ws[8];
+    double acc = 0.0;
+    int stride = gridDim.x * blockDim.x;
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < nd + nb; t += stride) {
+        if (t < nd) {
+            int4 r = drec[t];
+            float4 a = p[r.x], b = p[r.y];
+            double dx = (double)a.x - b.x, dy = (double)a.y - b.y, dz = (double)a.z - b.z;
+            double c = sqrt(dx * dx + dy * dy + dz * dz) - (double)__int_as_float(r.z);
+            acc += c * c;
+        } else {
+            int j = t - nd;
+            int4 r = bidx[j];
+            float4 q0 = p[r.x], q1 = p[r.y], q2 = p[r.z], q3 = p[r.w];
+            double E[3] = {(double)q1.x - q0.x, (double)q1.y - q0.y, (double)q1.z - q0.z};
+            double A0[3] = {(double)q2.x - q0.x, (double)q2.y - q0.y, (double)q2.z - q0.z};
+            double A1[3] = {(double)q2.x - q1.x, (double)q2.y - q1.y, (double)q2.z - q1.z};
+            double B1[3] = {(double)q3.x - q1.x, (double)q3.y - q1.y, (double)q3.z - q1.z};
+            double B0[3] = {(double)q3.x - q0.x, (double)q3.y - q0.y, (double)q3.z - q0.z};
+            double na[3] = {A0[1] * A1[2] - A0[2] * A1[1], A0[2] * A1[0] - A0[0] * A1[2],
+                            A0[0] * A1[1] - A0[1] * A1[0]};
+            double nb_[3] = {B1[1] * B0[2] - B1[2] * B0[1], B1[2] * B0[0] - B1[0] * B0[2],
+                             B1[0] * B0[1] - B1[1] * B0[0]};
+            double cx[3] = {na[1] * nb_[2] - na[2] * nb_[1], na[2] * nb_[0] - na[0] * nb_[2],
+                            na[0] * nb_[1] - na[1] * nb_[0]};
+            double el = sqrt(E[0] * E[0] + E[1] * E[1] + E[2] * E[2]);
+            double th = el > 0.0 ? atan2((cx[0] * E[0] + cx[1] * E[1] + cx[2] * E[2]) / el,
+                                         na[0] * nb_[0] + na[1] * nb_[1] + na[2] * nb_[2])
+                                 : 0.0;
+            double c = th - (double)bpar[j].x;
+            if (c > 3.141592653589793) c -= 6.283185307179586;
+            if (c < -3.141592653589793) c += 6.283185307179586;
+            acc += (c * el) * (c * el);
+        }
+    }
+    acc = warp_sum(acc);
+    if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double s = 0.0;
+        for (int w = 0; w < 8; ++w) s += ws[w];
+        part[blockIdx.x] = s;
+    }
+}
+
+__global__ void k_sum_parts(int n, const double *part, double *out) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) {
+        double s = 0.0;
+        for (int i = 0; i < n; ++i) s += part[i];
+        out[0] = s;
+    }
+}
+
+constexpr int kResidualBlocks = 4 * kNumSMs;
+
+// ---------------------------------------------------------------------------
+// host helpers
+// ---------------------------------------------------------------------------
+int launch_advect(pbd_object *o, float dt) {
+    float dp = powf(o->damping, dt);
+    float3 gdt = make_float3(o->gravity[0] * dt, o->gravity[1] * dt, o->gravity[2] * dt);
+    k_advect<<<grid_for(o->n, 256), 256, 0, o->stream>>>(o->n, dt, dp, gdt, o->x.p, o->v.p, o->p.p);
+    PBD_LAUNCH();
+    return PBD_OK;
+}
+
+int launch_integrate(pbd_object *o, float dt) {
+    k_integrate<<<grid_for(o->n, 256), 256, 0, o->stream>>>(o->n, dt, o->x.p, o->v.p, o->p.p);
+    PBD_LAUNCH();
+    return PBD_OK;
+}
+
+int launch_sweep(pbd_object *o, int iter) {
+    PBD_CHECK(o->sorted, PBD_ERR_STATE,
+              "no color-sorted constraints: run edge coloring and SortEdgesColors first");
+    float expk = (float)(1.0 / (double)(iter + 1));
+    for (int c = 0; c < o->n_colors; ++c) {
+        int d0 = o->h_dseg[c], nd = o->h_dseg[c + 1] - d0;
+        int b0 = o->h_bseg[c], nb = o->h_bseg[c + 1] - b0;
+        int a0 = o->h_aseg[c], na = o->h_aseg[c + 1] - a0;
+        int tot = nd + nb + na;
+        if (!tot) continue;
+        k_project_color<<<grid_for(tot, 256), 256, 0, o->stream>>>(
+            o->drec.p + d0, nd, o->bidx.p + b0, o->bpar.p + b0, nb, o->arec.p + a0, na, o->p.p,
+            expk);
+    }
+    PBD_LAUNCH();
+    return PBD_OK;
+}
+
+int launch_obstacles(pbd_solver *s) {
+    if (!s->sphere_on && !s->ground_on) return PBD_OK;
+    pbd_object *o = s->obj;
+    k_obstacles<<<grid_for(o->n, 256), 256, 0, o->stream>>>(
+        o->n, o->p.p, s->sphere_on, make_float3(s->sphere_c[0], s->sphere_c[1], s->sphere_c[2]),
+        s->sphere_r, s->ground_on, s->ground_h);
+    PBD_LAUNCH();
+    return PBD_OK;
+}
+
+static int build_point_csr(pbd_object *o, int n_entries, const int *d_owner_counts, int n_owners,
+                           bool tris, DBuf<int> &first, DBuf<int> &last, DBuf<int> &owner) {
+    cudaStream_t s = o->stream;
+    DBuf<uint32_t> key, key2;
+    DBuf<int> val, val2, eoff;
+    PBD_TRY(key.alloc(n_entries));
+    PBD_TRY(key2.alloc(n_entries));
+    PBD_TRY(val.alloc(n_entries));
+    PBD_TRY(val2.alloc(n_entries));
+    if (tris) {
+        k_emit_tri_points<<<grid_for(o->nt, 256), 256, 0, s>>>(o->nt, o->tri.p, key.p, val.p);
+    } else {
+        PBD_TRY(eoff.alloc(n_owners + 1));
+        PBD_TRY(exclusive_scan(d_owner_counts, eoff.p, n_owners, nullptr, s));
+        k_emit_prim_points<<<grid_for(n_owners, 256), 256, 0, s>>>(n_owners, o->prim_list.p,
+                                                                    o->indices.p, eoff.p, key.p,
+                                                                    val.p);
+    }
+    PBD_LAUNCH();
+    uint32_t *sk;
+    int *sv;
+    PBD_TRY(radix_sort<uint32_t>(key.p, val.p, key2.p, val2.p, n_entries, nullptr,
+                                 round8(bits_for(o->n)), o->scr, s, &sk, &sv));
+    PBD_TRY(first.alloc(o->n + 1));
+    PBD_TRY(last.alloc(o->n + 1));
+    PBD_TRY(owner.alloc(n_entries));
+    PBD_CUDA(cudaMemsetAsync(first.p, 0, sizeof(int) * (o->n + 1), s));
+    PBD_CUDA(cudaMemsetAsync(last.p, 0, sizeof(int) * (o->n + 1), s));
+    if (n_entries) {
+        k_run_bounds<<<grid_for(n_entries, 256), 256, 0, s>>>(n_entries, sk, first.p, last.p);
+        PBD_CUDA(cudaMemcpyAsync(owner.p, sv, sizeof(int) * n_entries, cudaMemcpyDeviceToDevice, s));
+    }
+    PBD_LAUNCH();
+    PBD_CUDA(cudaStreamSynchronize(s));
+    return PBD_OK;
+}
+
+}  // namespace pbd
+
+using namespace pbd;
+
+// ===========================================================================
+// C ABI
+// ===========================================================================
+extern "C" {
+
+const char *pbd_last_error(void) { return pbd::g_err.c_str(); }
+int pbd_version(void) { return 1; }
+
+int pbd_object_create(const pbd_object_desc *d, pbd_object **out) {
+    PBD_CHECK(d && out, PBD_ERR_ARG, "null argument");
+    *out = nullptr;
+    PBD_CHECK(d->n_points > 0 && d->pos && d->mass, PBD_ERR_ARG, "need n_points > 0, pos, mass");
+    PBD_CHECK(d->n_tris >= 0 && (d->n_tris == 0 || d->tri_idx), PBD_ERR_ARG, "bad triangles");
+    PBD_CHECK(d->n_prims >= 0 && (d->n_prims == 0 || (d->prim_list && d->indices &&
+                                                      d->constraint_type && d->stiffness)),
+              PBD_ERR_ARG, "bad constraint buffers");
+    // host-side validation of the constraint topology
+    int n_idx = 0;
+    std::vector<int> cnt(d->n_prims), ct(d->n_prims);
+    for (int p = 0; p < d->n_prims; ++p) {
+        int s = d->prim_list[2 * p], c = d->prim_list[2 * p + 1];
+        int t = d->constraint_type[p];
+        int need = t == PBD_DISTANCE ? 2 : t == PBD_BENDING ? 4 : t == PBD_ANCHOR ? 1 : -1;
+        PBD_CHECK(need > 0, PBD_ERR_ARG, "prim %d: unknown constraint type %d", p, t);
+        PBD_CHECK(c == need && s >= 0, PBD_ERR_ARG, "prim %d: type %d needs %d points, has %d", p,
+                  t, need, c);
+        PBD_CHECK(t != PBD_DISTANCE || d->rest_length, PBD_ERR_ARG, "rest_length missing");
+        if (s + c > n_idx) n_idx = s + c;
+        cnt[p] = c;
+        ct[p] = t;
+    }
+    for (int i = 0; i < n_idx; ++i)
+        PBD_CHECK(d->indices[i] >= 0 && d->indices[i] < d->n_points, PBD_ERR_ARG,
+                  "constraint index %d out of range", i);
+    for (long long i = 0; i < 3LL * d->n_tris; ++i)
+        PBD_CHECK(d->tri_idx[i] >= 0 && d->tri_idx[i] < d->n_points, PBD_ERR_ARG,
+                  "triangle index %lld out of range", i);
+
+    pbd_object *o = new pbd_object();
+    auto fail = [&](int r) {
+        pbd_object_destroy(o);
+        return r;
+    };
+    o->n = d->n_points;
+    o->nt = d->n_tris;
+    o->np = d->n_prims;
+    o->n_idx = n_idx;
+    o->damping = d->damping_rate;
+    for (int k = 0; k < 3; ++k) o->gravity[k] = d->gravity[k];
+    o->h_prim_count = cnt;
+    o->h_ctype = ct;
+    int r;
+    if (cudaStreamCreateWithFlags(&o->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        set_error("cudaStreamCreate failed: %s", cudaGetErrorString(cudaGetLastError()));
+        delete o;
+        return PBD_ERR_CUDA;
+    }
+    cudaStream_t s = o->stream;
+    {
+        DBuf<float> hp, hv, hm;
+        if ((r = hp.upload(d->pos, 3 * (size_t)o->n, s)) || (r = hm.upload(d->mass, o->n, s)))
+            return fail(r);
+        if (d->vel && (r = hv.upload(d->vel, 3 * (size_t)o->n, s))) return fail(r);
+        if ((r = o->x.alloc(o->n)) || (r = o->p.alloc(o->n)) || (r = o->v.alloc(o->n)) ||
+            (r = o->mass.upload(d->mass, o->n, s)))
+            return fail(r);
+        k_pack_state<<<grid_for(o->n, 256), 256, 0, s>>>(o->n, hp.p, d->vel ? hv.p : nullptr,
+                                                         hm.p, o->x.p, o->p.p, o->v.p);
+        if (cudaStreamSynchronize(s) != cudaSuccess) {
+            set_error("state upload failed: %s", cudaGetErrorString(cudaGetLastError()));
+            return fail(PBD_ERR_CUDA);
+        }
+    }
+    // triangles
+    if (o->nt) {
+        DBuf<int> ht, hi;
+        if ((r = ht.upload(d->tri_idx, 3 * (size_t)o->nt, s))) return fail(r);
+        if (d->tri_inst && (r = hi.upload(d->tri_inst, o->nt, s))) return fail(r);
+        if ((r = o->tri.alloc(o->nt))) return fail(r);
+        k_pack_tris<<<grid_for(o->nt, 256), 256, 0, s>>>(o->nt, ht.p, d->tri_inst ? hi.p : nullptr,
+                                                         o->tri.p);
+        if ((r = build_point_csr(o, 3 * o->nt, nullptr, 0, true, o->pt_tri_first, o->pt_tri_last,
+                                 o->pt_tri)))
+            return fail(r);
+    }
+    o->has_inst = d->point_inst != nullptr;
+    if (d->point_inst && (r = o->point_inst.upload(d->point_inst, o->n, s))) return fail(r);
+    // constraint buffers
+    if (o->np) {
+        if ((r = o->prim_list.upload((const int2 *)d->prim_list, o->np, s)) ||
+            (r = o->indices.upload(d->indices, n_idx, s)) ||
+            (r = o->ctype.upload(d->constraint_type, o->np, s)) ||
+            (r = o->stiffness.upload(d->stiffness, o->np, s)))
+            return fail(r);
+        std::vector<float> zero(o->np, 0.f);
+        if ((r = o->rest_length.upload(d->rest_length ? d->rest_length : zero.data(), o->np, s)) ||
+            (r = o->rest_angle.upload(d->rest_angle ? d->rest_angle : zero.data(), o->np, s)))
+            return fail(r);
+        std::vector<float4> rp(o->np, make_float4(0, 0, 0, 0));
+        if (d->rest_pos)
+            for (int p = 0; p < o->np; ++p)
+                rp[p] = make_float4(d->rest_pos[3 * p], d->rest_pos[3 * p + 1],
+                                    d->rest_pos[3 * p + 2], 0.f);
+        if ((r = o->rest_pos.upload(rp.data(), o->np, s))) return fail(r);
+        if (cudaStreamSynchronize(s) != cudaSuccess) return fail(PBD_ERR_CUDA);
+        // Point2PrimsMap as CSR, then Prim2PrimsMap
+        DBuf<int> pc, pfirst, plast, pprim, deg, off;
+        if ((r = pc.alloc(o->np))) return fail(r);
+        k_prim_counts<<<grid_for(o->np, 256), 256, 0, s>>>(o->np, o->prim_list.p, pc.p);
+        long long n_entries = 0;
+        for (int p = 0; p < o->np; ++p) n_entries += cnt[p];
+        if ((r = build_point_csr(o, (int)n_entries, pc.p, o->np, false, pfirst, plast, pprim)))
+            return fail(r);
+        if ((r = deg.alloc(o->np)) || (r = off.alloc(o->np)) || (r = o->flag.alloc(4)))
+            return fail(r);
+        k_adj_count<<<grid_for(o->np, 256), 256, 0, s>>>(o->np, o->prim_list.p, o->indices.p,
+                                                          pfirst.p, plast.p, pprim.p, deg.p);
+        if ((r = exclusive_scan(deg.p, off.p, o->np, o->flag.p, s))) return fail(r);
+        int total = 0;
+        if (cudaMemcpyAsync(&total, o->flag.p, sizeof(int), cudaMemcpyDeviceToHost, s) ||
+            cudaStreamSynchronize(s)) {
+            set_error("adjacency count failed: %s", cudaGetErrorString(cudaGetLastError()));
+            return fail(PBD_ERR_CUDA);
+        }
+        o->n_adj = total;
+        if ((r = o->adj_sn.alloc(o->np)) || (r = o->adj.alloc(total))) return fail(r);
+        k_adj_fill<<<grid_for(o->np, 256), 256, 0, s>>>(o->np, o->prim_list.p, o->indices.p,
+                                                         pfirst.p, plast.p, pprim.p, off.p,
+                                                         o->adj_sn.p, o->adj.p);
+        if ((r = o->color.alloc(o->np)) || (r = o->prd_color.alloc(o->np))) return fail(r);
+        if (cudaMemsetAsync(o->color.p, 0xff, sizeof(int) * o->np, s) ||
+            cudaMemsetAsync(o->prd_color.p, 0xff, sizeof(int) * o->np, s) ||
+            cudaStreamSynchronize(s)) {
+            set_error("adjacency build failed: %s", cudaGetErrorString(cudaGetLastError()));
+            return fail(PBD_ERR_CUDA);
+        }
+        // residual denominator: rest lengths and hinge lengths of the
+        // initial positions
+        double den = 0.0;
+        for (int p = 0; p < o->np; ++p) {
+            const int *ix = d->indices + d->prim_list[2 * p];
+            if (ct[p] == PBD_DISTANCE) {
+                double l = d->rest_length[p];
+                den += l * l;
+            } else if (ct[p] == PBD_BENDING) {
+                double e2 = 0.0;
+                for (int k = 0; k < 3; ++k) {
+                    double dd = (double)d->pos[3 * ix[1] + k] - d->pos[3 * ix[0] + k];
+                    e2 += dd * dd;
+                }
+                den += e2;
+            }
+        }
+        o->res_den = den;
+    }
+    if ((r = o->res_part.alloc(kResidualBlocks)) || (r = o->res_out.alloc(1))) return fail(r);
+    *out = o;
+    return PBD_OK;
+}
+
+int pbd_object_create_grid(float damping, const float *gravity, int res_x, int res_y,
+                           float size_x, float size_y, unsigned ct_mask, const float *stiffness,
+                           pbd_object **out) {
+    PBD_CHECK(gravity && stiffness && out && res_x >= 2 && res_y >= 2, PBD_ERR_ARG,
+              "bad grid arguments");
+    int n = res_x * res_y;
+    // initPosition (P/PBD_cuda.cu:831-852)
+    std::vector<float> pos(3 * (size_t)n), vel(3 * (size_t)n, 0.f), mass(n, 1.f);
+    float lx = size_x / (res_x - 1), lz = size_y / (res_y - 1);
+    for (int i = 0; i < res_y; ++i)
+        for (int j = 0; j < res_x; ++j) {
+            int k = i * res_x + j;
+            pos[3 * k] = 0.0f + j * lx;
+            pos[3 * k + 1] = 0.0f;
+            pos[3 * k + 2] = 0.0f + i * lz;
+        }
+    // initMeshTopolIndices (P/PBD_cuda.cu:854-869)
+    std::vector<int> tri;
+    for (int i = 0; i < n - res_x; ++i) {
+        if (i % res_x == res_x - 1) continue;
+        int t[6] = {i, i + res_x, i + res_x + 1, i, i + res_x + 1, i + 1};
+        tri.insert(tri.end(), t, t + 6);
+    }
+    std::vector<int> pl, idx, ctv;
+    std::vector<float> rl, st, ra, rp;
+    auto dist = [&](int a, int b) {  // Distance (P/PBD_cuda.cu:3-6)
+        float dx = pos[3 * a] - pos[3 * b], dy = pos[3 * a + 1] - pos[3 * b + 1],
+              dz = pos[3 * a + 2] - pos[3 * b + 2];
+        return powf(powf(dx, 2) + powf(dy, 2) + powf(dz, 2), 0.5f);
+    };
+    auto add_prim = [&](std::initializer_list<int> pts, int type, float rest, float stf) {
+        pl.push_back((int)idx.size());
+        pl.push_back((int)pts.size());
+        for (int q : pts) idx.push_back(q);
+        ctv.push_back(type);
+        rl.push_back(rest);
+        st.push_back(stf);
+        ra.push_back(0.f);
+        rp.push_back(0.f);
+        rp.push_back(0.f);
+        rp.push_back(0.f);
+    };
+    if (ct_mask & PBD_DISTANCE) {
+        // InitDistanceIndices stencil (P/PBD_cuda.cu:19-54)
+        std::vector<int> e;
+        for (int i = 0; i < n - res_x; ++i) {
+            if (i % res_x == 0) {
+                int a[4] = {i, i + 1, i, i + res_x};
+                e.insert(e.end(), a, a + 4);
+            } else if (i % res_x == res_x - 1) {
+                int a[4] = {i, i + res_x, i, i + res_x - 1};
+                e.insert(e.end(), a, a + 4);
+            } else {
+                int a[6] = {i, i + 1, i, i + res_x, i, i + res_x - 1};
+                e.insert(e.end(), a, a + 6);
+            }
+        }
+        for (int i = n - res_x; i < n - 1; ++i) {
+            e.push_back(i);
+            e.push_back(i + 1);
+        }
+        for (size_t k = 0; k < e.size(); k += 2)
+            add_prim({e[k], e[k + 1]}, PBD_DISTANCE, dist(e[k], e[k + 1]), stiffness[0]);
+    }
+    if (ct_mask & PBD_BENDING) {
+        // InitBendingConstr is an empty stub in the reference (P/PBD_cuda.cu:
+        // 110-123); here BENDING adds a dihedral constraint on every interior
+        // mesh edge, rest angle 0 (the grid is flat).
+        std::vector<long long> keys;
+        std::vector<int> opp;
+        int ntri = (int)tri.size() / 3;
+        for (int t = 0; t < ntri; ++t)
+            for (int k = 0; k < 3; ++k) {
+                int a = tri[3 * t + k], b = tri[3 * t + (k + 1) % 3], c = tri[3 * t + (k + 2) % 3];
+                keys.push_back(((long long)std::min(a, b) << 32) | (unsigned)std::max(a, b));
+                opp.push_back(c);
+                (void)c;
+            }
+        std::vector<int> order(keys.size());
+        for (size_t i = 0; i < order.size(); ++i) order[i] = (int)i;
+        std::stable_sort(order.begin(), order.end(),
+                         [&](int a, int b) { return keys[a] < keys[b]; });
+        for (size_t i = 0; i + 1 < order.size(); ++i) {
+            if (keys[order[i]] != keys[order[i + 1]]) continue;
+            int ea = order[i], eb = order[i + 1];
+            int t = ea / 3, k = ea % 3;
+            int e0 = tri[3 * t + k], e1 = tri[3 * t + (k + 1) % 3];
+            add_prim({e0, e1, opp[ea], opp[eb]}, PBD_BENDING, 0.f, stiffness[1]);
+            ++i;
+        }
+    }
+    if (ct_mask & PBD_ANCHOR) {
+        // InitAnchorConstr (P/PBD_cuda.cu:125-153): points 0 and res_y-1, rest
+        // positions of points 0 and res_x-1 (initPosition, :850-851)
+        int pts[2] = {0, res_y - 1}, restp[2] = {0, res_x - 1};
+        for (int a = 0; a < 2; ++a) {
+            add_prim({pts[a]}, PBD_ANCHOR, 0.f, stiffness[2]);
+            for (int k = 0; k < 3; ++k) rp[rp.size() - 3 + k] = pos[3 * restp[a] + k];
+        }
+    }
+    pbd_object_desc d;
+    memset(&d, 0, sizeof(d));
+    d.n_points = n;
+    d.pos = pos.data();
+    d.vel = vel.data();
+    d.mass = mass.data();
+    d.n_tris = (int)tri.size() / 3;
+    d.tri_idx = tri.data();
+    d.n_prims = (int)ctv.size();
+    d.prim_list = pl.data();
+    d.indices = idx.data();
+    d.constraint_type = ctv.data();
+    d.rest_length = rl.data();
+    d.stiffness = st.data();
+    d.rest_angle = ra.data();
+    d.rest_pos = rp.data();
+    d.damping_rate = damping;
+    for (int k = 0; k < 3; ++k) d.gravity[k] = gravity[k];
+    return pbd_object_create(&d, out);
+}
+
+int pbd_object_destroy(pbd_object *o) {
+    if (!o) return PBD_OK;
+    if (o->stream) cudaStreamSynchronize(o->stream);
+    cudaStream_t s = o->stream;
+    delete o;  // DBuf members free their memory
+    if (s) cudaStreamDestroy(s);
+    return PBD_OK;
+}
+
+int pbd_object_sizes(const pbd_object *o, int *n, int *nt, int *np) {
+    PBD_CHECK(o, PBD_ERR_ARG, "null object");
+    if (n) *n = o->n;
+    if (nt) *nt = o->nt;
+    if (np) *np = o->np;
+    return PBD_OK;
+}
+
+static int copy_out3(pbd_object *o, const float4 *src, float *dst) {
+    PBD_CHECK(o && dst, PBD_ERR_ARG, "null argument");
+    std::vector<float4> h(o->n);
+    PBD_CUDA(cudaMemcpyAsync(h.data(), src, sizeof(float4) * o->n, cudaMemcpyDeviceToHost, o->stream));
+    PBD_CUDA(cudaStreamSynchronize(o->stream));
+    for (int i = 0; i < o->n; ++i) {
+        dst[3 * i] = h[i].x;
+        dst[3 * i + 1] = h[i].y;
+        dst[3 * i + 2] = h[i].z;
+    }
+    return PBD_OK;
+}
+
+static int copy_in3(pbd_object *o, float4 *dst, const float *src, bool keep_w) {
+    PBD_CHECK(o && src, PBD_ERR_ARG, "null argument");
+    std::vector<float4> h(o->n);
+    std::vector<float> m;
+    if (keep_w) {
+        m.resize(o->n);
+        PBD_CUDA(cudaMemcpyAsync(m.data(), o->mass.p, sizeof(float) * o->n, cudaMemcpyDeviceToHost,
+                                 o->stream));
+        PBD_CUDA(cudaStreamSynchronize(o->stream));
+    }
+    for (int i = 0; i < o->n; ++i)
+        h[i] = make_float4(src[3 * i], src[3 * i + 1], src[3 * i + 2], keep_w ? m[i] : 0.f);
+    PBD_CUDA(cudaMemcpyAsync(dst, h.data(), sizeof(float4) * o->n, cudaMemcpyHostToDevice, o->stream));
+    PBD_CUDA(cudaStreamSynchronize(o->stream));
+    return PBD_OK;
+}
+
+int pbd_object_get_positions(pbd_object *o, float *v) { return copy_out3(o, o ? o->x.p : nullptr, v); }
+int pbd_object_get_velocities(pbd_object *o, float *v) { return copy_out3(o, o ? o->v.p : nullptr, v); }
+int pbd_object_get_predicted(pbd_object *o, float *v) { return copy_out3(o, o ? o->p.p : nullptr, v); }
+int pbd_object_set_positions(pbd_object *o, const float *v) { return copy_in3(o, o ? o->x.p : nullptr, v, true); }
+int pbd_object_set_velocities(pbd_object *o, const float *v) { return copy_in3(o, o ? o->v.p : nullptr, v, false); }
+int pbd_object_set_predicted(pbd_object *o, const float *v) { return copy_in3(o, o ? o->p.p : nullptr, v, true); }
+
+int pbd_object_stream(pbd_object *o, void **s) {
+    PBD_CHECK(o && s, PBD_ERR_ARG, "null argument");
+    *s = (void *)o->stream;
+    return PBD_OK;
+}
+
+int pbd_object_sync(pbd_object *o) {
+    PBD_CHECK(o, PBD_ERR_ARG, "null object");
+    PBD_CUDA(cudaStreamSynchronize(o->stream));
+    return PBD_OK;
+}
+
+// ---- ConstraintPBD --------------------------------------------------------
+static int finish_coloring(pbd_object *o) {
+    cudaStream_t s = o->stream;
+    PBD_TRY(o->flag.alloc(4));
+    PBD_CUDA(cudaMemsetAsync(o->flag.p, 0xff, sizeof(int), s));
+    k_max_color<<<grid_for(o->np, 256), 256, 0, s>>>(o->np, o->color.p, o->flag.p);
+    PBD_LAUNCH();
+    int mx = -1;
+    PBD_CUDA(cudaMemcpyAsync(&mx, o->flag.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+    PBD_CUDA(cudaStreamSynchronize(s));
+    o->n_colors = mx + 1;
+    o->colored = true;
+    o->sorted = false;
+    return PBD_OK;
+}
+
+int pbd_constraints_edge_coloring(pbd_object *o, int max_iterations, int *sweeps) {
+    PBD_CHECK(o, PBD_ERR_ARG, "null object");
+    if (sweeps) *sweeps = 0;
+    if (!o->np) {
+        o->colored = true;
+        o->n_colors = 0;
+        return PBD_OK;
+    }
+    cudaStream_t s = o->stream;
+    PBD_CUDA(cudaMemsetAsync(o->color.p, 0xff, sizeof(int) * o->np, s));
+    PBD_CUDA(cudaMemsetAsync(o->prd_color.p, 0xff, sizeof(int) * o->np, s));
+    const int window = 16;
+    int done = 0, it = 0;
+    while (it < max_iterations && !done) {
+        int w = std::min(window, max_iterations - it);
+        for (int k = 0; k < w; ++k) {
+            k_assign_colors<<<grid_for(o->np, 256), 256, 0, s>>>(o->np, o->adj_sn.p, o->adj.p,
+                                                                 o->color.p, o->prd_color.p);
+            if (k == w - 1) PBD_CUDA(cudaMemsetAsync(o->flag.p, 0, sizeof(int), s));
+            k_resolve_conflicts<<<grid_for(o->np, 256), 256, 0, s>>>(
+                o->np, o->prim_list.p, o->adj_sn.p, o->adj.p, o->color.p, o->prd_color.p,
+                o->flag.p);
+        }
+        PBD_LAUNCH();
+        it += w;
+        int f = 1;
+        PBD_CUDA(cudaMemcpyAsync(&f, o->flag.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+        PBD_CUDA(cudaStreamSynchronize(s));
+        done = (f == 0);
+    }
+    if (sweeps) *sweeps = it;
+    PBD_CHECK(done, PBD_ERR_TIMEOUT, "edge coloring did not converge in %d sweeps", max_iterations);
+    return finish_coloring(o);
+}
+
+int pbd_constraints_set_colors(pbd_object *o, const int *color) {
+    PBD_CHECK(o && (color || !o->np), PBD_ERR_ARG, "null argument");
+    for (int p = 0; p < o->np; ++p) PBD_CHECK(color[p] >= 0, PBD_ERR_ARG, "color %d < 0", p);
+    if (o->np) PBD_CUDA(cudaMemcpyAsync(o->color.p, color, sizeof(int) * o->np, cudaMemcpyHostToDevice, o->stream));
+    return finish_coloring(o);
+}
+
+int pbd_constraints_get_colors(pbd_object *o, int *color) {
+    PBD_CHECK(o && color, PBD_ERR_ARG, "null argument");
+    if (!o->np) return PBD_OK;
+    PBD_CUDA(cudaMemcpyAsync(color, o->color.p, sizeof(int) * o->np, cudaMemcpyDeviceToHost, o->stream));
+    PBD_CUDA(cudaStreamSynchronize(o->stream));
+    return PBD_OK;
+}
+
+int pbd_constraints_sort_edges_colors(pbd_object *o) {
+    PBD_CHECK(o, PBD_ERR_ARG, "null object");
+    PBD_CHECK(o->colored, PBD_ERR_STATE, "constraints are not colored");
+    int np = o->np;
+    cudaStream_t s = o->stream;
+    o->h_worksets.assign(2 * (size_t)o->n_colors, 0);
+    o->h_dseg.assign(o->n_colors + 1, 0);
+    o->h_bseg.assign(o->n_colors + 1, 0);
+    o->h_aseg.assign(o->n_colors + 1, 0);
+    if (!np) {
+        o->sorted = true;
+        return PBD_OK;
+    }
+    int nc = o->n_colors;
+    DBuf<uint32_t> k1, k2;
+    DBuf<int> v1, v2, first, last;
+    PBD_TRY(k1.alloc(np));
+    PBD_TRY(k2.alloc(np));
+    PBD_TRY(v1.alloc(np));
+    PBD_TRY(v2.alloc(np));
+    PBD_TRY(o->sorted_color.alloc(np));
+    PBD_TRY(o->sorted_prim.alloc(np));
+    // SortEdgesColors: stable sort of prim ids by color
+    k_iota_keys<<<grid_for(np, 256), 256, 0, s>>>(np, o->color.p, k1.p, v1.p);
+    PBD_LAUNCH();
+    uint32_t *sk;
+    int *sv;
+    PBD_TRY(radix_sort<uint32_t>(k1.p, v1.p, k2.p, v2.p, np, nullptr, round8(bits_for(nc)), o->scr,
+                                 s, &sk, &sv));
+    PBD_CUDA(cudaMemcpyAsync(o->sorted_color.p, sk, sizeof(int) * np, cudaMemcpyDeviceToDevice, s));
+    PBD_CUDA(cudaMemcpyAsync(o->sorted_prim.p, sv, sizeof(int) * np, cudaMemcpyDeviceToDevice, s));
+    // solver records: class-major, then color, then prim id
+    k_class_keys<<<grid_for(np, 256), 256, 0, s>>>(np, o->color.p, o->ctype.p, nc, k1.p, v1.p);
+    PBD_LAUNCH();
+    PBD_TRY(radix_sort<uint32_t>(k1.p, v1.p, k2.p, v2.p, np, nullptr, round8(bits_for(4LL * nc)),
+                                 o->scr, s, &sk, &sv));
+    PBD_TRY(first.alloc(4 * (size_t)nc + 1));
+    PBD_TRY(last.alloc(4 * (size_t)nc + 1));
+    PBD_CUDA(cudaMemsetAsync(first.p, 0, sizeof(int) * (4 * nc + 1), s));
+    PBD_CUDA(cudaMemsetAsync(last.p, 0, sizeof(int) * (4 * nc + 1), s));
+    k_run_bounds<<<grid_for(np, 256), 256, 0, s>>>(np, sk, first.p, last.p);
+    PBD_LAUNCH();
+    std::vector<int> hf(4 * nc), hl(4 * nc);
+    PBD_CUDA(cudaMemcpyAsync(hf.data(), first.p, sizeof(int) * 4 * nc, cudaMemcpyDeviceToHost, s));
+    PBD_CUDA(cudaMemcpyAsync(hl.data(), last.p, sizeof(int) * 4 * nc, cudaMemcpyDeviceToHost, s));
+    PBD_CUDA(cudaStreamSynchronize(s));
+    int nrec[4] = {0, 0, 0, 0};
+    std::vector<int> *segs[3] = {&o->h_dseg, &o->h_bseg, &o->h_aseg};
+    for (int c = 0; c < 4; ++c)
+        for (int col = 0; col < nc; ++col) {
+            int cntv = hl[c * nc + col] - hf[c * nc + col];
+            if (c < 3) (*segs[c])[col + 1] = (*segs[c])[col] + cntv;
+            nrec[c] += cntv;
+        }
+    PBD_TRY(o->drec.alloc(nrec[0]));
+    PBD_TRY(o->bidx.alloc(nrec[1]));
+    PBD_TRY(o->bpar.alloc(nrec[1]));
+    PBD_TRY(o->arec.alloc(nrec[2]));
+    k_build_records<<<grid_for(np, 256), 256, 0, s>>>(
+        nrec[0] + nrec[1] + nrec[2], sv, o->prim_list.p, o->indices.p, o->rest_length.p,
+        o->stiffness.p, o->rest_angle.p, o->rest_pos.p, nrec[0], nrec[1], nrec[2], o->drec.p,
+        o->bidx.p, o->bpar.p, o->arec.p);
+    PBD_LAUNCH();
+    PBD_CUDA(cudaStreamSynchronize(s));
+    // worksets over the color-sorted prim list
+    int start = 0;
+    for (int col = 0; col < nc; ++col) {
+        int cntv = 0;
+        for (int c = 0; c < 4; ++c) cntv += hl[c * nc + col] - hf[c * nc + col];
+        o->h_worksets[2 * col] = start;
+        o->h_worksets[2 * col + 1] = cntv;
+        start += cntv;
+    }
+    o->sorted = true;
+    return PBD_OK;
+}
+
+int pbd_constraints_eval_worksets(pbd_object *o, int *n) {
+    PBD_CHECK(o, PBD_ERR_ARG, "null object");
+    PBD_CHECK(o->sorted, PBD_ERR_STATE, "SortEdgesColors has not run");
+    if (n) *n = o->n_colors;
+    return PBD_OK;
+}
+
+int pbd_constraints_get_sorted(pbd_object *o, int *sc, int *sp) {
+    PBD_CHECK(o && sc && sp, PBD_ERR_ARG, "null argument");
+    PBD_CHECK(o->sorted, PBD_ERR_STATE, "SortEdgesColors has not run");
+    if (!o->np) return PBD_OK;
+    PBD_CUDA(cudaMemcpyAsync(sc, o->sorted_color.p, sizeof(int) * o->np, cudaMemcpyDeviceToHost, o->stream));
+    PBD_CUDA(cudaMemcpyAsync(sp, o->sorted_prim.p, sizeof(int) * o->np, cudaMemcpyDeviceToHost, o->stream));
+    PBD_CUDA(cudaStreamSynchronize(o->stream));
+    return PBD_OK;
+}
+
+int pbd_constraints_get_worksets(pbd_object *o, int *ws, int cap, int *n) {
+    PBD_CHECK(o && n, PBD_ERR_ARG, "null argument");
+    PBD_CHECK(o->sorted, PBD_ERR_STATE, "SortEdgesColors has not run");
+    *n = o->n_colors;
+    for (int i = 0; i < o->n_colors && i < cap && ws; ++i) {
+        ws[2 * i] = o->h_worksets[2 * i];
+        ws[2 * i + 1] = o->h_worksets[2 * i + 1];
+    }
+    return PBD_OK;
+}
+
+int pbd_constraints_get_adjacency(pbd_object *o, int *sn, int *adj, long long cap,
+                                  long long *total) {
+    PBD_CHECK(o && total, PBD_ERR_ARG, "null argument");
+    *total = o->n_adj;
+    if (sn && o->np)
+        PBD_CUDA(cudaMemcpyAsync(sn, o->adj_sn.p, sizeof(int2) * o->np, cudaMemcpyDeviceToHost, o->stream));
+    if (adj && o->n_adj) {
+        long long m = std::min(cap, o->n_adj);
+        PBD_CUDA(cudaMemcpyAsync(adj, o->adj.p, sizeof(int) * m, cudaMemcpyDeviceToHost, o->stream));
+    }
+    PBD_CUDA(cudaStreamSynchronize(o->stream));
+    return PBD_OK;
+}
+
+int pbd_constraints_residual(pbd_object *o, double *res) {
+    PBD_CHECK(o && res, PBD_ERR_ARG, "null argument");
+    PBD_CHECK(o->sorted, PBD_ERR_STATE, "SortEdgesColors has not run");
+    int nd = o->h_dseg.empty() ? 0 : o->h_dseg.back();
+    int nb = o->h_bseg.empty() ? 0 : o->h_bseg.back();
+    k_residual<<<kResidualBlocks, 256, 0, o->stream>>>(o->drec.p, nd, o->bidx.p, o->bpar.p, nb,
+                                                       o->p.p, o->res_part.p);
+    k_sum_parts<<<1, 32, 0, o->stream>>>(kResidualBlocks, o->res_part.p, o->res_out.p);
+    PBD_LAUNCH();
+    double num = 0.0;
+    PBD_CUDA(cudaMemcpyAsync(&num, o->res_out.p, sizeof(double), cudaMemcpyDeviceToHost, o->stream));
+    PBD_CUDA(cudaStreamSynchronize(o->stream));
+    *res = o->res_den > 0.0 ? sqrt(num) / sqrt(o->res_den) : 0.0;
+    return PBD_OK;
+}
+
+// ---- SolverPBD ------------------------------------------------------------
+int pbd_solver_create(pbd_solver **out) {
+    PBD_CHECK(out, PBD_ERR_ARG, "null argument");
+    *out = new pbd_solver();
+    return PBD_OK;
+}
+
+int pbd_solver_destroy(pbd_solver *s) {
+    if (!s) return PBD_OK;
+    if (s->gexec) cudaGraphExecDestroy(s->gexec);
+    delete s;
+    return PBD_OK;
+}
+
+int pbd_solver_set_target(pbd_solver *s, pbd_object *o) {
+    PBD_CHECK(s && o, PBD_ERR_ARG, "null argument");
+    s->obj = o;
+    if (s->gexec) cudaGraphExecDestroy(s->gexec);
+    s->gexec = nullptr;
+    return PBD_OK;
+}
+
+int pbd_solver_advect(pbd_solver *s, float dt) {
+    PBD_CHECK(s && s->obj, PBD_ERR_STATE, "solver has no target");
+    return launch_advect(s->obj, dt);
+}
+
+int pbd_solver_integration(pbd_solver *s, float dt) {
+    PBD_CHECK(s && s->obj, PBD_ERR_STATE, "solver has no target");
+    return launch_integrate(s->obj, dt);
+}
+
+int pbd_solver_project_constraint(pbd_solver *s, int st, int iterations) {
+    PBD_CHECK(s && s->obj, PBD_ERR_STATE, "solver has no target");
+    PBD_CHECK(st == PBD_GAUSSSEIDEL, PBD_ERR_ARG, "only Gauss-Seidel is implemented");
+    for (int i = 0; i < iterations; ++i) {
+        PBD_TRY(launch_sweep(s->obj, i));
+        PBD_TRY(launch_obstacles(s));
+    }
+    return PBD_OK;
+}
+
+int pbd_solver_set_sphere(pbd_solver *s, int on, const float *c, float r) {
+    PBD_CHECK(s && (!on || c), PBD_ERR_ARG, "null argument");
+    s->sphere_on = on;
+    if (c)
+        for (int k = 0; k < 3; ++k) s->sphere_c[k] = c[k];
+    s->sphere_r = r;
+    return PBD_OK;
+}
+
+int pbd_solver_set_ground(pbd_solver *s, int on, float h) {
+    PBD_CHECK(s, PBD_ERR_ARG, "null argument");
+    s->ground_on = on;
+    s->ground_h = h;
+    return PBD_OK;
+}
+
+static int project_with_colli(pbd_solver *s, int iterations, pbd_colli *c) {
+    for (int ii = 0; ii < iterations; ++ii) {
+        if (c && (ii % 10 == 0 || ii == iterations - 1)) PBD_TRY(ccd_detect(c));
+        PBD_TRY(launch_sweep(s->obj, ii));
+        if (c) PBD_TRY(ccd_resolve(c, c->iterations));
+        PBD_TRY(launch_obstacles(s));
+    }
+    return PBD_OK;
+}
+
+int pbd_solver_project_constraint_with_colli(pbd_solver *s, int st, int iterations,
+                                             pbd_colli *c) {
+    PBD_CHECK(s && s->obj, PBD_ERR_STATE, "solver has no target");
+    PBD_CHECK(st == PBD_GAUSSSEIDEL, PBD_ERR_ARG, "only Gauss-Seidel is implemented");
+    PBD_CHECK(!c || c->obj == s->obj, PBD_ERR_ARG, "collision solver targets another object");
+    return project_with_colli(s, iterations, c);
+}
+
+static int record_steps(pbd_solver *s, float dt, int substeps, int iterations, pbd_colli *c) {
+    for (int k = 0; k < substeps; ++k) {
+        PBD_TRY(launch_advect(s->obj, dt));
+        PBD_TRY(project_with_colli(s, iterations, c));
+        PBD_TRY(launch_integrate(s->obj, dt));
+    }
+    return PBD_OK;
+}
+
+int pbd_solver_step(pbd_solver *s, float dt, int substeps, int iterations, pbd_colli *c,
+                    int use_graph) {
+    PBD_CHECK(s && s->obj, PBD_ERR_STATE, "solver has no target");
+    PBD_CHECK(s->obj->sorted, PBD_ERR_STATE, "constraints are not color-sorted");
+    PBD_CHECK(!c || c->obj == s->obj, PBD_ERR_ARG, "collision solver targets another object");
+    if (!use_graph) return record_steps(s, dt, substeps, iterations, c);
+    int sig = s->sphere_on * 3 + s->ground_on * 7 + (c ? c->response * 11 + c->iterations * 13 : 0);
+    if (s->gexec && (s->g_dt != dt || s->g_sub != substeps || s->g_it != iterations ||
+                     s->g_colli != c || s->g_sig != sig)) {
+        cudaGraphExecDestroy(s->gexec);
+        s->gexec = nullptr;
+    }
+    cudaStream_t st = s->obj->stream;
+    if (!s->gexec) {
+        if (c) PBD_TRY(ccd_detect(c));  // sizes every buffer before capture
+        PBD_CUDA(cudaStreamSynchronize(st));
+        cudaGraph_t g;
+        PBD_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+        int r = record_steps(s, dt, substeps, iterations, c);
+        cudaError_t e = cudaStreamEndCapture(st, &g);
+        if (r != PBD_OK) {
+            if (e == cudaSuccess) cudaGraphDestroy(g);
+            return r;
+        }
+        PBD_CUDA(e);
+        cudaError_t ei = cudaGraphInstantiate(&s->gexec, g, 0);
+        cudaGraphDestroy(g);
+        PBD_CUDA(ei);
+        s->g_dt = dt;
+        s->g_sub = substeps;
+        s->g_it = iterations;
+        s->g_colli = c;
+        s->g_sig = sig;
+    }
+    PBD_CUDA(cudaGraphLaunch(s->gexec, st));
+    return PBD_OK;
+}
+
+}  // extern "C"

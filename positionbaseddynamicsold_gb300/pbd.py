@@ -1,0 +1,454 @@
+"""Python mirror of the reference's cloth-step classes over the C ABI.
+
+``PBDObject``, ``SolverPBD``, ``SpatialHashSystem`` and ``CollisionSolver``
+keep the reference's names and method meanings (P/PBD_Basic.cuh:145-259,
+P/SpatialHashSystem.h:10-96, P/CCD_Basic.h:33-135; P/ =
+PositionBasedDynamicsCUDA/PositionBasedDynamicsCUDA/).  Every method is one
+call into libpbd_gb300.so (include/pbd_c.h); there is no Python or CPU
+fallback: if the library cannot be loaded, or a call fails, PBDError is
+raised.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import build as _build
+
+DISTANCE, BENDING, ANCHOR = 0x001, 0x010, 0x100
+JACOBI, GAUSSSEIDEL = 0, 1
+RESPONSE_REFERENCE, RESPONSE_MASS_WEIGHTED = 0, 1
+_ERRS = {1: "ARG", 2: "OOM", 3: "CUDA", 4: "TIMEOUT", 5: "OVERFLOW", 6: "STATE"}
+
+
+class PBDError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("PBD_ERR_%s: %s" % (_ERRS.get(code, code), msg))
+        self.code = code
+
+
+class _Desc(C.Structure):
+    _fields_ = [("n_points", C.c_int), ("pos", C.c_void_p), ("vel", C.c_void_p),
+                ("mass", C.c_void_p), ("n_tris", C.c_int), ("tri_idx", C.c_void_p),
+                ("n_prims", C.c_int), ("prim_list", C.c_void_p), ("indices", C.c_void_p),
+                ("constraint_type", C.c_void_p), ("rest_length", C.c_void_p),
+                ("stiffness", C.c_void_p), ("rest_angle", C.c_void_p), ("rest_pos", C.c_void_p),
+                ("point_inst", C.c_void_p), ("tri_inst", C.c_void_p),
+                ("damping_rate", C.c_float), ("gravity", C.c_float * 3)]
+
+
+_LIB = None
+
+# every symbol include/pbd_c.h declares
+EXPORTS = [
+    "pbd_last_error", "pbd_version", "pbd_object_create", "pbd_object_create_grid",
+    "pbd_object_destroy", "pbd_object_sizes", "pbd_object_get_positions",
+    "pbd_object_get_velocities", "pbd_object_get_predicted", "pbd_object_set_positions",
+    "pbd_object_set_velocities", "pbd_object_set_predicted", "pbd_object_stream",
+    "pbd_object_sync", "pbd_constraints_edge_coloring", "pbd_constraints_sort_edges_colors",
+    "pbd_constraints_eval_worksets", "pbd_constraints_set_colors", "pbd_constraints_get_colors",
+    "pbd_constraints_get_sorted", "pbd_constraints_get_worksets",
+    "pbd_constraints_get_adjacency", "pbd_constraints_residual", "pbd_solver_create",
+    "pbd_solver_destroy", "pbd_solver_set_target", "pbd_solver_advect",
+    "pbd_solver_project_constraint", "pbd_solver_project_constraint_with_colli",
+    "pbd_solver_integration", "pbd_solver_set_sphere", "pbd_solver_set_ground",
+    "pbd_solver_step", "pbd_shs_create", "pbd_shs_create_hashed", "pbd_shs_destroy",
+    "pbd_shs_set_grid_center", "pbd_shs_set_grid_size", "pbd_shs_set_division", "pbd_shs_init",
+    "pbd_shs_update", "pbd_shs_find_neighbors", "pbd_shs_find_neighbors_all",
+    "pbd_colli_create", "pbd_colli_destroy", "pbd_colli_set_target",
+    "pbd_colli_set_acce_struct", "pbd_colli_set_thickness", "pbd_colli_set_iterations",
+    "pbd_colli_set_response", "pbd_colli_set_capacity", "pbd_colli_ccd_sh_extended",
+    "pbd_colli_collision_resolve_new", "pbd_colli_get_contacts", "pbd_colli_stats",
+]
+
+
+def lib_path() -> str:
+    return _build.LIB
+
+
+def load(build_if_missing: bool = True) -> C.CDLL:
+    """Load libpbd_gb300.so (building it with nvcc if absent)."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    path = _build.LIB
+    if not os.path.exists(path):
+        if not build_if_missing:
+            raise PBDError(3, "libpbd_gb300.so not built: run python -m positionbaseddynamicsold_gb300.build")
+        path = _build.build()
+    L = C.CDLL(path)
+    for name in EXPORTS:
+        f = getattr(L, name)
+        f.restype = C.c_int
+    L.pbd_last_error.restype = C.c_char_p
+    L.pbd_solver_advect.argtypes = [C.c_void_p, C.c_float]
+    L.pbd_solver_integration.argtypes = [C.c_void_p, C.c_float]
+    L.pbd_solver_project_constraint.argtypes = [C.c_void_p, C.c_int, C.c_int]
+    L.pbd_solver_project_constraint_with_colli.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_void_p]
+    L.pbd_solver_step.argtypes = [C.c_void_p, C.c_float, C.c_int, C.c_int, C.c_void_p, C.c_int]
+    L.pbd_solver_set_sphere.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_float]
+    L.pbd_solver_set_ground.argtypes = [C.c_void_p, C.c_int, C.c_float]
+    L.pbd_colli_set_thickness.argtypes = [C.c_void_p, C.c_float]
+    L.pbd_colli_set_capacity.argtypes = [C.c_void_p, C.c_longlong, C.c_longlong]
+    L.pbd_object_create_grid.argtypes = [C.c_float, C.c_void_p, C.c_int, C.c_int, C.c_float,
+                                         C.c_float, C.c_uint, C.c_void_p, C.c_void_p]
+    L.pbd_constraints_get_adjacency.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p,
+                                                C.c_longlong, C.c_void_p]
+    L.pbd_shs_find_neighbors_all.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_longlong,
+                                             C.c_void_p]
+    L.pbd_colli_get_contacts.argtypes = [C.c_void_p] + [C.c_void_p] * 5 + [C.c_longlong, C.c_void_p]
+    _LIB = L
+    return L
+
+
+def _check(rc):
+    if rc != 0:
+        raise PBDError(rc, _LIB.pbd_last_error().decode(errors="replace"))
+
+
+def _p(a):
+    return None if a is None else C.c_void_p(a.ctypes.data)
+
+
+def _f32(a, shape=None):
+    a = np.ascontiguousarray(a, dtype=np.float32)
+    return a if shape is None else a.reshape(shape)
+
+
+def _i32(a):
+    return np.ascontiguousarray(a, dtype=np.int32)
+
+
+class PBDObject:
+    """PBDObject + ConstraintPBD (P/PBD_Basic.cuh:97-211) resident on the GPU."""
+
+    def __init__(self, scene=None, damping=1.0, gravity=(0.0, -9.8, 0.0), _handle=None):
+        self.L = load()
+        self.h = C.c_void_p()
+        if _handle is not None:
+            self.h = _handle
+        else:
+            self._create(scene, damping, gravity)
+        n, nt, np_ = C.c_int(), C.c_int(), C.c_int()
+        _check(self.L.pbd_object_sizes(self.h, C.byref(n), C.byref(nt), C.byref(np_)))
+        self.n_points, self.n_tris, self.n_prims = n.value, nt.value, np_.value
+
+    def _create(self, s, damping, gravity):
+        keep = []
+
+        def k(a):
+            keep.append(a)
+            return _p(a)
+
+        d = _Desc()
+        pos = _f32(s["pos"]).reshape(-1)
+        d.n_points = len(pos) // 3
+        d.pos = k(pos)
+        d.vel = k(_f32(s["vel"]).reshape(-1)) if s.get("vel") is not None else None
+        d.mass = k(_f32(s["mass"]))
+        tri = _i32(s.get("tri_idx", np.zeros((0, 3), np.int32))).reshape(-1)
+        d.n_tris = len(tri) // 3
+        d.tri_idx = k(tri) if len(tri) else None
+        ct = _i32(s.get("ctype", np.zeros(0, np.int32)))
+        d.n_prims = len(ct)
+        if len(ct):
+            d.prim_list = k(_i32(s["prim_list"]).reshape(-1))
+            d.indices = k(_i32(s["indices"]))
+            d.constraint_type = k(ct)
+            d.rest_length = k(_f32(s["rest_length"]))
+            d.stiffness = k(_f32(s["stiffness"]))
+            if s.get("rest_angle") is not None:
+                d.rest_angle = k(_f32(s["rest_angle"]))
+            if s.get("rest_pos") is not None:
+                d.rest_pos = k(_f32(s["rest_pos"]).reshape(-1))
+        if s.get("point_inst") is not None:
+            d.point_inst = k(_i32(s["point_inst"]))
+            d.tri_inst = k(_i32(s["tri_inst"]))
+        d.damping_rate = damping
+        for i in range(3):
+            d.gravity[i] = gravity[i]
+        _check(self.L.pbd_object_create(C.byref(d), C.byref(self.h)))
+
+    @classmethod
+    def grid(cls, res_x, res_y, size_x, size_y, ct=DISTANCE, stiffness=(1.0, 0.1, -1.0),
+             damping=1.0, gravity=(0.0, -9.8, 0.0)):
+        """PBDObject(damping, gravity, resX, resY, sizeX, sizeY) + SetConstrOption + Init()."""
+        L = load()
+        h = C.c_void_p()
+        g = np.asarray(gravity, np.float32)
+        st = np.asarray(stiffness, np.float32)
+        _check(L.pbd_object_create_grid(damping, _p(g), res_x, res_y, size_x, size_y, ct, _p(st),
+                                        C.byref(h)))
+        return cls(_handle=h)
+
+    def close(self):
+        if self.h:
+            self.L.pbd_object_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _get3(self, fn):
+        out = np.empty((self.n_points, 3), np.float32)
+        _check(fn(self.h, _p(out)))
+        return out
+
+    def positions(self):
+        return self._get3(self.L.pbd_object_get_positions)
+
+    def velocities(self):
+        return self._get3(self.L.pbd_object_get_velocities)
+
+    def predicted(self):
+        return self._get3(self.L.pbd_object_get_predicted)
+
+    def set_positions(self, a):
+        _check(self.L.pbd_object_set_positions(self.h, _p(_f32(a, (-1,)))))
+
+    def set_velocities(self, a):
+        _check(self.L.pbd_object_set_velocities(self.h, _p(_f32(a, (-1,)))))
+
+    def set_predicted(self, a):
+        _check(self.L.pbd_object_set_predicted(self.h, _p(_f32(a, (-1,)))))
+
+    def stream(self) -> int:
+        s = C.c_void_p()
+        _check(self.L.pbd_object_stream(self.h, C.byref(s)))
+        return s.value or 0
+
+    def sync(self):
+        _check(self.L.pbd_object_sync(self.h))
+
+    # ConstraintPBD
+    def edge_coloring(self, iterations=20000):
+        sw = C.c_int()
+        _check(self.L.pbd_constraints_edge_coloring(self.h, iterations, C.byref(sw)))
+        return sw.value
+
+    def sort_edges_colors(self):
+        _check(self.L.pbd_constraints_sort_edges_colors(self.h))
+
+    def eval_worksets(self):
+        n = C.c_int()
+        _check(self.L.pbd_constraints_eval_worksets(self.h, C.byref(n)))
+        return n.value
+
+    def set_colors(self, color):
+        _check(self.L.pbd_constraints_set_colors(self.h, _p(_i32(color))))
+
+    def colors(self):
+        out = np.empty(self.n_prims, np.int32)
+        _check(self.L.pbd_constraints_get_colors(self.h, _p(out)))
+        return out
+
+    def sorted(self):
+        sc = np.empty(self.n_prims, np.int32)
+        sp = np.empty(self.n_prims, np.int32)
+        _check(self.L.pbd_constraints_get_sorted(self.h, _p(sc), _p(sp)))
+        return sc, sp
+
+    def worksets(self):
+        n = C.c_int()
+        _check(self.L.pbd_constraints_get_worksets(self.h, None, 0, C.byref(n)))
+        out = np.empty((max(n.value, 1), 2), np.int32)
+        _check(self.L.pbd_constraints_get_worksets(self.h, _p(out), n.value, C.byref(n)))
+        return out[:n.value]
+
+    def adjacency(self):
+        tot = C.c_longlong()
+        sn = np.empty((self.n_prims, 2), np.int32)
+        _check(self.L.pbd_constraints_get_adjacency(self.h, _p(sn), None, 0, C.byref(tot)))
+        adj = np.empty(max(tot.value, 1), np.int32)
+        _check(self.L.pbd_constraints_get_adjacency(self.h, None, _p(adj), tot.value, C.byref(tot)))
+        return sn, adj[:tot.value]
+
+    def residual(self):
+        r = C.c_double()
+        _check(self.L.pbd_constraints_residual(self.h, C.byref(r)))
+        return r.value
+
+    def prepare(self, iterations=20000):
+        """EdgeColoring + SortEdgesColors + EvalWorksets; returns sweeps."""
+        sw = self.edge_coloring(iterations)
+        self.sort_edges_colors()
+        self.eval_worksets()
+        return sw
+
+
+class SpatialHashSystem:
+    """SpatialHashSystem (P/SpatialHashSystem.h:10-96) over an object's triangles."""
+
+    def __init__(self, obj: PBDObject, grid_center=(0.0, 0.0, 0.0), grid_size=None,
+                 cell_size=(1.0, 1.0, 1.0), log2_table=None):
+        self.L = load()
+        self.obj = obj
+        self.h = C.c_void_p()
+        cell = np.broadcast_to(np.asarray(cell_size, np.float32), (3,)).copy()
+        if grid_size is None:
+            _check(self.L.pbd_shs_create_hashed(obj.h, _p(cell), int(log2_table or 20), C.byref(self.h)))
+            if any(grid_center):
+                _check(self.L.pbd_shs_set_grid_center(self.h, _p(np.asarray(grid_center, np.float32))))
+        else:
+            _check(self.L.pbd_shs_create(obj.h, _p(np.asarray(grid_center, np.float32)),
+                                         _p(np.asarray(grid_size, np.int32)), _p(cell),
+                                         C.byref(self.h)))
+
+    def close(self):
+        if self.h:
+            self.L.pbd_shs_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def init(self):
+        _check(self.L.pbd_shs_init(self.h))
+
+    def update(self):
+        _check(self.L.pbd_shs_update(self.h))
+
+    def find_neighbors_all(self):
+        tot = C.c_longlong()
+        sn = np.empty((self.obj.n_tris, 2), np.int32)
+        _check(self.L.pbd_shs_find_neighbors_all(self.h, _p(sn), None, 0, C.byref(tot)))
+        out = np.empty(max(tot.value, 1), np.int32)
+        _check(self.L.pbd_shs_find_neighbors_all(self.h, None, _p(out), tot.value, C.byref(tot)))
+        return sn, out[:tot.value]
+
+    def find_neighbors(self, tri):
+        n = C.c_int()
+        _check(self.L.pbd_shs_find_neighbors(self.h, tri, None, 0, C.byref(n)))
+        out = np.empty(max(n.value, 1), np.int32)
+        _check(self.L.pbd_shs_find_neighbors(self.h, tri, _p(out), n.value, C.byref(n)))
+        return out[:n.value]
+
+
+class CollisionSolver:
+    """CollisionSolver (P/CCD_Basic.h:33-135)."""
+
+    def __init__(self, obj: PBDObject = None, shs: SpatialHashSystem = None, thickness=0.0,
+                 iterations=1, response=RESPONSE_REFERENCE):
+        self.L = load()
+        self.h = C.c_void_p()
+        _check(self.L.pbd_colli_create(C.byref(self.h)))
+        if obj is not None:
+            self.set_target(obj)
+        if shs is not None:
+            self.set_acce_struct(shs)
+        self.set_thickness(thickness)
+        self.set_iterations(iterations)
+        self.set_response(response)
+
+    def close(self):
+        if self.h:
+            self.L.pbd_colli_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_target(self, obj):
+        self.obj = obj
+        _check(self.L.pbd_colli_set_target(self.h, obj.h))
+
+    def set_acce_struct(self, shs):
+        self.shs = shs
+        _check(self.L.pbd_colli_set_acce_struct(self.h, shs.h))
+
+    def set_thickness(self, t):
+        _check(self.L.pbd_colli_set_thickness(self.h, float(t)))
+
+    def set_iterations(self, it):
+        _check(self.L.pbd_colli_set_iterations(self.h, int(it)))
+
+    def set_response(self, mode):
+        _check(self.L.pbd_colli_set_response(self.h, int(mode)))
+
+    def set_capacity(self, candidates, contacts):
+        _check(self.L.pbd_colli_set_capacity(self.h, int(candidates), int(contacts)))
+
+    def ccd_sh_extended(self):
+        _check(self.L.pbd_colli_ccd_sh_extended(self.h))
+
+    def collision_resolve_new(self):
+        _check(self.L.pbd_colli_collision_resolve_new(self.h))
+
+    def contacts(self):
+        cnt = C.c_longlong()
+        _check(self.L.pbd_colli_get_contacts(self.h, None, None, None, None, None, 0, C.byref(cnt)))
+        h = cnt.value
+        ids = np.empty((max(h, 1), 4), np.int32)
+        face = np.empty(max(h, 1), np.int32)
+        t = np.empty(max(h, 1), np.float32)
+        w = np.empty((max(h, 1), 4), np.float64)
+        n = np.empty((max(h, 1), 3), np.float32)
+        _check(self.L.pbd_colli_get_contacts(self.h, _p(ids), _p(face), _p(t), _p(w), _p(n), h,
+                                             C.byref(cnt)))
+        return {"ids": ids[:h], "face": face[:h], "t": t[:h], "w": w[:h], "n": n[:h]}
+
+    def stats(self):
+        a, b, c = C.c_longlong(), C.c_longlong(), C.c_int()
+        _check(self.L.pbd_colli_stats(self.h, C.byref(a), C.byref(b), C.byref(c)))
+        return {"candidates": a.value, "contacts": b.value, "overflow": c.value}
+
+
+class SolverPBD:
+    """SolverPBD (P/PBD_Basic.cuh:213-259)."""
+
+    def __init__(self, obj: PBDObject = None):
+        self.L = load()
+        self.h = C.c_void_p()
+        _check(self.L.pbd_solver_create(C.byref(self.h)))
+        if obj is not None:
+            self.set_target(obj)
+
+    def close(self):
+        if self.h:
+            self.L.pbd_solver_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_target(self, obj):
+        self.obj = obj
+        _check(self.L.pbd_solver_set_target(self.h, obj.h))
+
+    def advect(self, dt):
+        _check(self.L.pbd_solver_advect(self.h, dt))
+
+    def project_constraint(self, iterations, solver_type=GAUSSSEIDEL):
+        _check(self.L.pbd_solver_project_constraint(self.h, solver_type, iterations))
+
+    def project_constraint_with_colli(self, iterations, colli, solver_type=GAUSSSEIDEL):
+        _check(self.L.pbd_solver_project_constraint_with_colli(self.h, solver_type, iterations,
+                                                               colli.h if colli else None))
+
+    def integration(self, dt):
+        _check(self.L.pbd_solver_integration(self.h, dt))
+
+    def set_sphere(self, enable, center=(0.0, 0.0, 0.0), radius=1.0):
+        c = np.asarray(center, np.float32)
+        _check(self.L.pbd_solver_set_sphere(self.h, int(enable), _p(c), radius))
+
+    def set_ground(self, enable, height=0.0):
+        _check(self.L.pbd_solver_set_ground(self.h, int(enable), height))
+
+    def step(self, dt, substeps=1, iterations=20, colli=None, use_graph=True):
+        _check(self.L.pbd_solver_step(self.h, dt, substeps, iterations,
+                                      colli.h if colli else None, int(use_graph)))

@@ -1,0 +1,163 @@
+"""GPU parity of the broadphase, CCD and response.
+
+Candidate/neighbor sets and CCD hit sets are compared exactly with the
+reference's own outputs (tests/golden, produced by its compiled code) and
+with the oracle; positions after the response within 1e-6 m (same float
+operations, same summation order), and a whole collision substep within
+1e-5 m.
+"""
+import numpy as np
+import pytest
+
+from positionbaseddynamicsold_gb300 import scenes
+from positionbaseddynamicsold_gb300.pbd import (RESPONSE_MASS_WEIGHTED, RESPONSE_REFERENCE,
+                                                CollisionSolver, PBDObject, SolverPBD,
+                                                SpatialHashSystem)
+
+pytestmark = pytest.mark.gpu
+
+
+def mesh_object(pos, prdp, tri, mass=None):
+    sc = {"pos": pos, "mass": np.ones(len(pos), np.float32) if mass is None else mass,
+          "tri_idx": tri}
+    obj = PBDObject(sc)
+    obj.set_predicted(prdp)
+    return obj
+
+
+def test_find_neighbors_matches_reference(golden):
+    g = golden("neighbors")
+    obj = mesh_object(g["pos"], g["pos"], g["tri_idx"])
+    shs = SpatialHashSystem(obj, g["center"], g["size"], g["cell"])
+    shs.init()
+    sn, nb = shs.find_neighbors_all()
+    np.testing.assert_array_equal(sn, g["start_num"])
+    np.testing.assert_array_equal(nb, g["nbrs"])
+    np.testing.assert_array_equal(shs.find_neighbors(5), g["nbrs"][g["start_num"][5, 0]:g["start_num"][5, 0] + g["start_num"][5, 1]])
+
+
+def ccd_gpu(g, hashed=False, iterations=0, response=RESPONSE_REFERENCE):
+    obj = mesh_object(g["pos"], g["prdp"], g["tri_idx"])
+    if hashed:
+        shs = SpatialHashSystem(obj, cell_size=g["cell"], log2_table=10)
+    else:
+        shs = SpatialHashSystem(obj, g["center"], g["size"], g["cell"])
+    shs.init()
+    cs = CollisionSolver(obj, shs, thickness=float(g["thickness"]), iterations=iterations,
+                         response=response)
+    cs.ccd_sh_extended()
+    return obj, cs
+
+
+@pytest.mark.parametrize("hashed", [False, True])
+def test_ccd_hit_set_matches_reference(golden, hashed):
+    g = golden("ccd")
+    obj, cs = ccd_gpu(g, hashed)
+    ct = cs.contacts()
+    assert len(ct["ids"]) == len(g["ids"])
+    ref = {tuple(k): (t, tuple(w), tuple(n)) for k, t, w, n in
+           zip(g["ids"].tolist(), g["t"].tolist(), g["w"].tolist(), g["n"].tolist())}
+    got = {tuple(k): (t, tuple(w), tuple(n)) for k, t, w, n in
+           zip(ct["ids"].tolist(), ct["t"].tolist(), ct["w"].tolist(), ct["n"].tolist())}
+    assert set(got) == set(ref)
+    for k in ref:
+        assert got[k] == ref[k], k
+    # sorted by (point, face triangle)
+    key = ct["ids"][:, 0].astype(np.int64) * len(g["tri_idx"]) + ct["face"]
+    assert (np.diff(key) > 0).all()
+
+
+def test_ccd_matches_oracle_pairs(orc, golden):
+    g = golden("ccd")
+    obj, cs = ccd_gpu(g)
+    grid = orc.grid(g["center"], g["size"], g["cell"], True)
+    oc, h = orc.ccd(grid, g["tri_idx"], g["pos"], g["prdp"], float(g["thickness"]))
+    ct = cs.contacts()
+    np.testing.assert_array_equal(ct["ids"], oc["ids"])
+    np.testing.assert_array_equal(ct["face"], oc["face"])
+    np.testing.assert_array_equal(ct["t"], oc["t"])
+    np.testing.assert_array_equal(ct["w"], oc["w"])
+
+
+@pytest.mark.parametrize("mw", [0, 1])
+def test_resolve_matches_oracle(orc, golden, mw):
+    g = golden("ccd")
+    obj, cs = ccd_gpu(g, iterations=2, response=RESPONSE_MASS_WEIGHTED if mw else RESPONSE_REFERENCE)
+    ids = cs.contacts()["ids"]
+    cs.collision_resolve_new()
+    want = orc.resolve_jacobi(ids, g["pos"], g["prdp"], np.ones(len(g["pos"]), np.float32), 2,
+                              float(g["thickness"]), mw)
+    assert np.abs(obj.predicted() - want).max() <= 1e-6
+
+
+def test_resolve_reference_split_when_contacts_disjoint(orc, golden):
+    """With vertex-disjoint contacts the Jacobi response is the reference's
+    sequential CollisionResolveNew."""
+    g = golden("ccd")
+    obj, cs = ccd_gpu(g, iterations=1)
+    ids = cs.contacts()["ids"]
+    used, keep = set(), []
+    for i, row in enumerate(ids.tolist()):
+        if used.isdisjoint(row):
+            keep.append(i)
+            used.update(row)
+    sub = ids[keep]
+    seq = orc.resolve_ref(sub, g["pos"], g["prdp"], 1, float(g["thickness"]))
+    jac = orc.resolve_jacobi(sub, g["pos"], g["prdp"], None, 1, float(g["thickness"]), 0)
+    np.testing.assert_array_equal(seq, jac)
+
+
+def drape_small(seed=0):
+    """20x20 cloth (0.6 m) just above an icosphere (level 2, r=0.2), moving
+    down at 1 m/s: contacts from the first substep."""
+    cloth = scenes.grid_cloth(20, 20, 0.6, 0.6, origin=(-0.3, 0.2015, -0.3), jitter=1e-4,
+                              seed=seed)
+    cloth["vel"][:, 1] = -1.0
+    sp, st = scenes.icosphere(2, 0.2)
+    sc = scenes.add_static_mesh(cloth, sp, st)
+    sc["cell"] = 2.0 * scenes.mean_rest_edge(cloth)
+    return sc
+
+
+def test_collision_substep_matches_oracle(orc):
+    sc = drape_small()
+    G = np.array([0, -9.8, 0], np.float32)
+    obj = PBDObject(sc, damping=1.0, gravity=G)
+    obj.prepare()
+    shs = SpatialHashSystem(obj, cell_size=sc["cell"], log2_table=16)
+    shs.init()
+    cs = CollisionSolver(obj, shs, thickness=1e-3, iterations=1, response=RESPONSE_MASS_WEIGHTED)
+    s = SolverPBD(obj)
+    dt = 1.0 / 600
+    s.advect(dt)
+    s.project_constraint_with_colli(15, cs)
+    s.integration(dt)
+    _, sid, ws = orc.sort_worksets(obj.colors())
+    st = {"pos": sc["pos"].copy(), "vel": sc["vel"].copy()}
+    colli = {"center": (0, 0, 0), "cell": sc["cell"], "bounded": False, "thickness": 1e-3,
+             "tri_idx": sc["tri_idx"], "mass_weighted": 1, "resolve_passes": 1}
+    nct = orc.substep_gpu(sc, st, sid, ws, 15, dt, 1.0, G, colli=colli)
+    assert nct > 0
+    assert cs.stats()["contacts"] == nct
+    err = np.abs(obj.positions() - st["pos"]).max()
+    assert err <= 1e-5, err
+    # the static sphere does not move
+    ns = len(sc["pos"]) - 400
+    np.testing.assert_array_equal(obj.positions()[400:], sc["pos"][400:])
+    assert ns > 0
+
+
+def test_collision_graph_equals_eager():
+    sc = drape_small(1)
+    G = np.array([0, -9.8, 0], np.float32)
+    res = []
+    for graph in (False, True):
+        obj = PBDObject(sc, damping=1.0, gravity=G)
+        obj.prepare()
+        shs = SpatialHashSystem(obj, cell_size=sc["cell"], log2_table=16)
+        shs.init()
+        cs = CollisionSolver(obj, shs, thickness=1e-3, iterations=1, response=RESPONSE_MASS_WEIGHTED)
+        s = SolverPBD(obj)
+        s.step(1.0 / 600, substeps=3, iterations=15, colli=cs, use_graph=graph)
+        res.append(obj.positions())
+    np.testing.assert_array_equal(res[0], res[1])
