@@ -1,0 +1,393 @@
+"""Throughput of the PBD cloth step on GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--workload drape256|fold1024|hanging32]
+
+Workload (default, drape256): a 256x256 cloth (2 m x 2 m, 130,050 triangles,
+195,585 distance + 194,565 bending constraints) released flat at y = 0.5
+above a fixed icosphere (r = 0.4, 20,480 triangles); spatial hash with cell =
+2 x mean rest edge and 2^20 buckets, vertex-face CCD with thickness 1e-3
+(cloth-sphere and self collision), FP32 positions, FP64 cubic; dt = 1/600
+(10 substeps per 1/60 frame), 15 colored Gauss-Seidel iterations, CCD at
+iterations 0, 10 and 14.  One step = one substep: advect, 15 x (CCD when
+due, one sweep over all colors, one response pass), integrate.  Before the
+warm-up the cloth is simulated 120 substeps (untimed) so it touches the
+sphere and the timed substeps include contacts.  L2 is flushed (a 256 MiB
+write) before every timed substep; each substep is timed with CUDA events on
+the object's stream.
+
+Metric: cloth substeps/s.  `e2e` is the same step through the C ABI with
+the state in host memory: upload positions and velocities, step, read them
+back, every step.  `cpu_baseline` times the reference's CPU path (the
+oracle's restatement: sequential GS, triangle-ordered CCD with
+de-duplication by scan, sequential response) for one full substep of the
+same state on one host thread.
+
+Multi-GPU: a single cloth does not shard; N GPUs run N independent replicas
+(value = replicas x substeps / slowest replica's time).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "cloth substeps/s"
+G = np.array([0.0, -9.8, 0.0], np.float32)
+DT = 1.0 / 600.0
+ITERS = 15
+
+
+def load_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def make_workload(name):
+    from positionbaseddynamicsold_gb300 import scenes
+    if name == "drape256":
+        sc = scenes.drape_over_sphere(res=256, seed=0)
+        cfg = {"workload": "drape256: 256x256 cloth over a fixed icosphere (20,480 tris), "
+                           "vertex-face CCD + self collision",
+               "grid": 256, "substep_dt": DT, "gs_iterations": ITERS, "ccd_passes_per_substep": 3,
+               "hash_buckets": 2 ** 20, "thickness": 1e-3, "cell": sc["colli"]["cell"]}
+        return sc, cfg, True, 20
+    if name == "fold1024":
+        sc = scenes.folding_cloth(res=1024, seed=0)
+        cfg = {"workload": "fold1024: 1024x1024 cloth dropped onto a ground plane, self CCD",
+               "grid": 1024, "substep_dt": DT, "gs_iterations": ITERS,
+               "ccd_passes_per_substep": 3, "hash_buckets": 2 ** 24, "thickness": 1e-3,
+               "cell": sc["colli"]["cell"]}
+        return sc, cfg, True, 24
+    if name == "hanging32":
+        sc = scenes.hanging_cloth(32, seed=0)
+        cfg = {"workload": "hanging32: 32x32 hanging cloth, no collisions", "grid": 32,
+               "substep_dt": DT, "gs_iterations": 20}
+        return sc, cfg, False, 0
+    raise SystemExit("unknown workload " + name)
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle sampling during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.samples = []
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.FIELDS,
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) == 6:
+                self.samples.append(parts)
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for s in self.samples for i in range(4)
+                          if s[2 + i].lower().startswith("active")})
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
+                "samples": len(self.samples)}
+
+
+def setup(sc, colli_on, table_log2):
+    from positionbaseddynamicsold_gb300.pbd import (RESPONSE_MASS_WEIGHTED, CollisionSolver,
+                                                    PBDObject, SolverPBD, SpatialHashSystem)
+    obj = PBDObject(sc, damping=1.0, gravity=G)
+    obj.prepare()
+    solver = SolverPBD(obj)
+    shs = cs = None
+    if colli_on:
+        shs = SpatialHashSystem(obj, cell_size=sc["colli"]["cell"], log2_table=table_log2)
+        shs.init()
+        cs = CollisionSolver(obj, shs, thickness=sc["colli"]["thickness"], iterations=1,
+                             response=RESPONSE_MASS_WEIGHTED)
+        n = obj.n_points
+        cs.set_capacity(max(1 << 22, 64 * n), max(1 << 20, 4 * n))
+        if "ground" in sc["colli"]:
+            solver.set_ground(True, sc["colli"]["ground"])
+    return obj, solver, shs, cs
+
+
+def run_ours(args, rank, world):
+    import torch
+    from positionbaseddynamicsold_gb300 import scenes
+
+    torch.cuda.set_device(0 if world == 1 else int(os.environ.get("LOCAL_RANK", rank)))
+    sc, cfg, colli_on, tl = make_workload(args.workload)
+    obj, solver, shs, cs = setup(sc, colli_on, tl)
+    stream = torch.cuda.ExternalStream(obj.stream())
+    nd = int((sc["ctype"] == scenes.DISTANCE).sum())
+    nb = int((sc["ctype"] == scenes.BENDING).sum())
+    n_colors = obj.eval_worksets()
+    iters = cfg["gs_iterations"]
+
+    def step():
+        solver.step(DT, 1, iters, cs, True)
+
+    # pre-roll so the timed substeps include contacts
+    for _ in range(args.preroll):
+        step()
+    for _ in range(args.warmup):
+        step()
+    obj.sync()
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(args.steps)]
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    clocks = ClockSampler(torch.cuda.current_device())
+    clocks.start()
+    t_wall = time.perf_counter()
+    with torch.cuda.stream(stream):
+        for k in range(args.steps):
+            flush.fill_(k & 255)
+            ev[k][0].record(stream)
+            step()
+            ev[k][1].record(stream)
+    torch.cuda.synchronize()
+    t_wall = time.perf_counter() - t_wall
+    clk = clocks.stop()
+    ms = sum(a.elapsed_time(b) for a, b in ev)
+    if world > 1:
+        t = torch.tensor([ms], device="cuda", dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+        torch.distributed.barrier()
+    value = world * args.steps / (ms / 1e3)
+    stats = cs.stats() if cs is not None else {}
+    residual = obj.residual()
+    launches = solver.graph_kernels()
+
+    # roofline of the dominant kernel (the per-color GS launch): one eager
+    # 15-iteration projection on the same state, timed with events on the
+    # object's stream; algorithmic bytes per sweep = 84*nd + 164*nb
+    pos_save = obj.positions()
+    prd_save = obj.predicted()
+    bytes_sweep = 84.0 * nd + 164.0 * nb
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    solver.project_constraint(iters)
+    obj.sync()
+    reps = 3
+    with torch.cuda.stream(stream):
+        e0.record(stream)
+        for _ in range(reps):
+            solver.project_constraint(iters)
+        e1.record(stream)
+    torch.cuda.synchronize()
+    gs_ms = e0.elapsed_time(e1)
+    n_launch = reps * iters * n_colors
+    achieved = reps * iters * bytes_sweep / (gs_ms / 1e3) / 1e9
+    obj.set_positions(pos_save)
+    obj.set_predicted(prd_save)
+    peak, peak_kind = load_peaks()
+
+    # end to end through the C ABI with host buffers
+    x_h = obj.positions()
+    v_h = obj.velocities()
+    e2e_steps = max(10, min(args.steps, 100))
+    obj.sync()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        obj.set_positions(x_h)
+        obj.set_velocities(v_h)
+        step()
+        x_h = obj.positions()
+        v_h = obj.velocities()
+    e2e_s = time.perf_counter() - t0
+    e2e = {"value": world * e2e_steps / e2e_s, "unit": "substeps/s",
+           "h2d_bytes_per_step": 2 * 12 * obj.n_points, "d2h_bytes_per_step": 2 * 12 * obj.n_points}
+
+    out = {
+        "metric": METRIC, "value": value, "unit": "substeps/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64(ccd cubic)",
+        "data": "synthetic (seeded scene generators)",
+        "config": dict(cfg, l2="flushed (256 MiB write) before every timed substep",
+                       parallelism="replicas only" if world > 1 else "single GPU",
+                       colors=n_colors, points=obj.n_points, triangles=obj.n_tris,
+                       distance_constraints=nd, bending_constraints=nb,
+                       preroll_substeps=args.preroll),
+        "e2e": e2e,
+        "gpu_launches": launches * args.steps,
+        "roofline": {"bound": "hbm", "kernel": "k_project_color", "achieved": achieved,
+                     "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "peak_source": peak_kind, "traffic": args.traffic,
+                     "launches_timed": n_launch, "avg_launch_us": gs_ms * 1e3 / n_launch,
+                     "bytes_per_sweep": bytes_sweep},
+        "clocks": clk,
+        "wall_s_timed_region": t_wall,
+        "last_step": {"candidates": stats.get("candidates"), "contacts": stats.get("contacts"),
+                      "overflow": stats.get("overflow"), "relative_residual": residual},
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        out["cpu_baseline"] = cpu_baseline(sc, cfg, colli_on, obj)
+    return out
+
+
+def oracle_state(sc, obj):
+    st = {"pos": obj.positions(), "vel": obj.velocities()}
+    return st
+
+
+def cpu_colli(sc):
+    return {"center": (0.0, 0.0, 0.0), "cell": sc["colli"]["cell"], "bounded": False,
+            "thickness": sc["colli"]["thickness"], "tri_idx": sc["tri_idx"], "mass_weighted": 0,
+            "resolve_passes": 1, "contact_cap": 1 << 21}
+
+
+def cpu_baseline(sc, cfg, colli_on, obj):
+    """The reference CPU path (oracle restatement) on one thread, one full
+    substep of the current state."""
+    from oracle.oracle import Oracle
+    orc = Oracle()
+    st = oracle_state(sc, obj)
+    t0 = time.perf_counter()
+    orc.substep_cpu_ref(sc, st, cfg["gs_iterations"], DT, G,
+                        colli=cpu_colli(sc) if colli_on else None)
+    dt = time.perf_counter() - t0
+    return {"value": 1.0 / dt, "unit": "substeps/s", "cores": 1, "kind": "port",
+            "sample": "1 full substep (%d GS iterations%s) of the timed state, 1 host thread"
+                      % (cfg["gs_iterations"], ", 3 CCD passes" if colli_on else ""),
+            "host_cores_available": os.cpu_count()}
+
+
+def run_reference(args):
+    """The reference's CPU implementation of the path (the oracle's
+    restatement of it: the reference sources are not present on the GPU
+    host).  One step = one fifteenth of a substep: one sequential GS
+    iteration, one response pass and a fifth of a CCD pass (triangle slice
+    in the reference's loop order); 15 steps hold one substep's work."""
+    import ctypes as C
+    from oracle.oracle import Oracle, OrcContact, _ptr
+    sc, cfg, colli_on, tl = make_workload(args.workload)
+    orc = Oracle()
+    L = orc.lib
+    c = orc.constraints(sc)
+    pos = sc["pos"].copy()
+    # start from a contact state like the timed arm: drop the cloth onto the sphere
+    if args.workload == "drape256":
+        pos[:sc["n_cloth_points"], 1] -= np.float32(0.099)
+    vel = sc["vel"].copy()
+    prdp = pos.copy()
+    n = len(pos)
+    iters = cfg["gs_iterations"]
+    slices = iters
+    ccd_slices = 5
+    colli = orc._colli(cpu_colli(sc)) if colli_on else None
+    cap = 1 << 21
+    arr = (OrcContact * cap)()
+    nt = len(sc["tri_idx"])
+    tri = np.ascontiguousarray(sc["tri_idx"], np.int32)
+    g = np.ascontiguousarray(G)
+    mass = np.ascontiguousarray(sc["mass"])
+
+    def ref_step(k):
+        s = k % slices
+        if s == 0:
+            L.orc_advect_cpu(n, C.c_float(DT), _ptr(g), _ptr(vel), _ptr(prdp), _ptr(pos))
+        h = 0
+        if colli_on:
+            q = s % ccd_slices
+            t0, t1 = q * nt // ccd_slices, (q + 1) * nt // ccd_slices
+            h = L.orc_ccd_sh_extended_ref_range(C.byref(colli.grid), nt, _ptr(tri), _ptr(pos),
+                                                _ptr(prdp), C.c_float(colli.thickness), t0, t1,
+                                                arr, C.c_int64(cap))
+        L.orc_project_cpu(C.byref(c), 1, _ptr(mass), _ptr(prdp), n, None, C.c_float(0.0))
+        if colli_on:
+            L.orc_collision_resolve_ref(int(min(h, cap)), arr, _ptr(pos), _ptr(prdp), 1,
+                                        C.c_float(colli.thickness))
+        if s == slices - 1:
+            L.orc_integrate(n, C.c_float(DT), _ptr(vel), _ptr(prdp), _ptr(pos))
+
+    L.orc_ccd_sh_extended_ref_range.restype = C.c_int64
+    for k in range(args.warmup):
+        ref_step(k)
+    t0 = time.perf_counter()
+    for k in range(args.steps):
+        ref_step(args.warmup + k)
+    dt = time.perf_counter() - t0
+    value = args.steps / dt / slices
+    sample = ("each step = 1/%d substep: one sequential GS iteration, one response pass%s; "
+              "1 host thread" % (slices, ", 1/5 of a CCD pass" if colli_on else ""))
+    return {"impl": "reference", "metric": METRIC, "value": value, "unit": "substeps/s",
+            "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": dt * 1e3 / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32+f64(ccd cubic)", "data": "synthetic",
+            "config": cfg,
+            "cpu_baseline": {"value": value, "unit": "substeps/s", "cores": 1, "kind": "port",
+                             "sample": sample, "host_cores_available": os.cpu_count()},
+            "e2e": {"value": value, "unit": "substeps/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="drape256", choices=["drape256", "fold1024", "hanging32"])
+    ap.add_argument("--preroll", type=int, default=120)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--traffic", type=float, default=None,
+                    help="ncu dram bytes per launch of the dominant kernel (from profiles/)")
+    args = ap.parse_args()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if args.impl == "reference":
+        if rank == 0:
+            print(json.dumps(run_reference(args)))
+        return
+    if world > 1:
+        import torch
+        torch.distributed.init_process_group("nccl")
+    out = run_ours(args, rank, world)
+    if rank == 0:
+        print(json.dumps(out))
+    if world > 1:
+        import torch
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -158,6 +158,10 @@ int pbd_solver_set_ground(pbd_solver *s, int enable, float height);
 int pbd_solver_step(pbd_solver *s, float dt, int substeps, int iterations, pbd_colli *colli,
                     int use_graph);
 
+/* kernel launches recorded in the cached pbd_solver_step graph (no
+ * reference counterpart; used to report launches per step) */
+int pbd_solver_graph_kernels(pbd_solver *s, long long *n);
+
 /* ---- SpatialHashSystem (P/SpatialHashSystem.h:10-96) ---------------------- */
 /* SpatialHashSystem(posBuffer, triIdxBuffer, ht, gridCenter, gridSize,
  * cellSize): bounded uniform grid over triangle centroids. */

@@ -226,11 +226,11 @@ class Oracle:
         arr = (OrcContact * cap)()
         if mode == "ref":
             h = self.lib.orc_ccd_sh_extended_ref(C.byref(grid), len(tri), _ptr(tri), _ptr(x),
-                                                 _ptr(p), C.c_float(thickness), arr, cap)
+                                                 _ptr(p), C.c_float(thickness), arr, C.c_int64(cap))
         else:
             h = self.lib.orc_ccd_vf_pairs(C.byref(grid), len(x), len(tri), _ptr(tri),
                                           _ptr(tri_inst), _ptr(point_inst), _ptr(x), _ptr(p),
-                                          C.c_float(thickness), arr, cap)
+                                          C.c_float(thickness), arr, C.c_int64(cap))
         return contacts_to_numpy(arr, min(h, cap)), h
 
     def _contacts_struct(self, ids, face=None):

@@ -661,34 +661,50 @@ static int table_lower(const cell_table *t, uint64_t key)
     return lo;
 }
 
+/* FindNeighbors (P/SpatialHashSystem.cpp:134-187) of one triangle into a
+ * growable list; returns the count */
+static int neighbors_of(const orc_grid *g, const cell_table *t, const int *cells, int tri,
+                        int **buf, int *cap)
+{
+    int n = 0;
+    const int *c = cells + 3 * tri;
+    if (g->bounded && outside(g, c)) return 0;
+    for (int z = -1; z <= 1; ++z)
+        for (int y = -1; y <= 1; ++y)
+            for (int x = -1; x <= 1; ++x) {
+                int nc[3] = {c[0] + x, c[1] + y, c[2] + z};
+                if (g->bounded && outside(g, nc)) continue;
+                uint64_t key = g->bounded ? (uint64_t)orc_cell_hash(g, nc) : cell_key(nc);
+                for (int i = table_lower(t, key); i < t->n && t->e[i].key == key; ++i) {
+                    if (t->e[i].id == tri) continue;
+                    if (n == *cap) {
+                        *cap *= 2;
+                        *buf = (int *)realloc(*buf, sizeof(int) * (size_t)*cap);
+                    }
+                    (*buf)[n++] = t->e[i].id;
+                }
+            }
+    return n;
+}
+
 int64_t orc_find_neighbors_all(const orc_grid *g, int n_tris, const int *tri_idx,
                                const float *pos, int *out_start_num, int *out_idx)
 {
     int *cells = (int *)malloc(sizeof(int) * 3 * (size_t)(n_tris > 0 ? n_tris : 1));
     cell_table t = build_table(g, n_tris, tri_idx, pos, cells);
+    int cap = 1024;
+    int *buf = (int *)malloc(sizeof(int) * (size_t)cap);
     int64_t total = 0;
     for (int tri = 0; tri < n_tris; ++tri) {
-        int64_t start = total;
-        const int *c = cells + 3 * tri;
-        if (!(g->bounded && outside(g, c))) {
-            for (int z = -1; z <= 1; ++z)
-                for (int y = -1; y <= 1; ++y)
-                    for (int x = -1; x <= 1; ++x) {
-                        int nc[3] = {c[0] + x, c[1] + y, c[2] + z};
-                        if (g->bounded && outside(g, nc)) continue;
-                        uint64_t key = g->bounded ? (uint64_t)orc_cell_hash(g, nc) : cell_key(nc);
-                        for (int i = table_lower(&t, key); i < t.n && t.e[i].key == key; ++i) {
-                            if (t.e[i].id == tri) continue;
-                            if (out_idx) out_idx[total] = t.e[i].id;
-                            total++;
-                        }
-                    }
-        }
+        int n = neighbors_of(g, &t, cells, tri, &buf, &cap);
+        if (out_idx) memcpy(out_idx + total, buf, sizeof(int) * (size_t)n);
         if (out_start_num) {
-            out_start_num[2 * tri] = (int)start;
-            out_start_num[2 * tri + 1] = (int)(total - start);
+            out_start_num[2 * tri] = (int)total;
+            out_start_num[2 * tri + 1] = n;
         }
+        total += n;
     }
+    free(buf);
     free(t.e);
     free(cells);
     return total;
@@ -875,20 +891,32 @@ int64_t orc_ccd_sh_extended_ref(const orc_grid *g, int n_tris, const int *tri_id
                                 const float *pos, const float *prdp,
                                 float thickness, orc_contact *out, int64_t cap)
 {
-    /* UpdateSH(prdP) then, per triangle, FindNeighbors and the
-     * point x neighbor loop (P/CCD.cpp:1530-1586) */
-    int64_t nn = orc_find_neighbors_all(g, n_tris, tri_idx, prdp, NULL, NULL);
-    int *sn = (int *)malloc(sizeof(int) * 2 * (size_t)(n_tris > 0 ? n_tris : 1));
-    int *nb = (int *)malloc(sizeof(int) * (size_t)(nn > 0 ? nn : 1));
-    orc_find_neighbors_all(g, n_tris, tri_idx, prdp, sn, nb);
+    return orc_ccd_sh_extended_ref_range(g, n_tris, tri_idx, pos, prdp, thickness, 0, n_tris,
+                                         out, cap);
+}
+
+int64_t orc_ccd_sh_extended_ref_range(const orc_grid *g, int n_tris, const int *tri_idx,
+                                      const float *pos, const float *prdp, float thickness,
+                                      int tri_begin, int tri_end, orc_contact *out, int64_t cap)
+{
+    /* UpdateSH(prdP) (binning of every triangle) then, per triangle of the
+     * range, FindNeighbors and the point x neighbor loop
+     * (P/CCD.cpp:1530-1586) */
+    int *cells = (int *)malloc(sizeof(int) * 3 * (size_t)(n_tris > 0 ? n_tris : 1));
+    cell_table tb = build_table(g, n_tris, tri_idx, prdp, cells);
+    int nbcap = 1024;
+    int *nb = (int *)malloc(sizeof(int) * (size_t)nbcap);
     int64_t h = 0;
     int64_t hcap = 1024;
     int *keys = (int *)malloc(sizeof(int) * 4 * (size_t)hcap);
-    for (int tri = 0; tri < n_tris; ++tri) {
+    if (tri_begin < 0) tri_begin = 0;
+    if (tri_end > n_tris) tri_end = n_tris;
+    for (int tri = tri_begin; tri < tri_end; ++tri) {
+        int nn = neighbors_of(g, &tb, cells, tri, &nb, &nbcap);
         for (int j = 0; j < 3; ++j) {
             int ids[4];
             ids[0] = tri_idx[3 * tri + j];
-            for (int q = sn[2 * tri]; q < sn[2 * tri] + sn[2 * tri + 1]; ++q) {
+            for (int q = 0; q < nn; ++q) {
                 int nt = nb[q];
                 ids[1] = tri_idx[3 * nt];
                 ids[2] = tri_idx[3 * nt + 1];
@@ -921,8 +949,9 @@ int64_t orc_ccd_sh_extended_ref(const orc_grid *g, int n_tris, const int *tri_id
         }
     }
     free(keys);
-    free(sn);
     free(nb);
+    free(tb.e);
+    free(cells);
     return h;
 }
 

@@ -225,6 +225,13 @@ int64_t orc_ccd_sh_extended_ref(const orc_grid *g, int n_tris, const int *tri_id
                                 const float *pos, const float *prdp,
                                 float thickness, orc_contact *out, int64_t cap);
 
+/* The same loop restricted to triangles [tri_begin, tri_end) of the outer
+ * loop (the neighbour search still bins every triangle): a slice of one
+ * CCD pass, used to time the reference path in bounded pieces. */
+int64_t orc_ccd_sh_extended_ref_range(const orc_grid *g, int n_tris, const int *tri_idx,
+                                      const float *pos, const float *prdp, float thickness,
+                                      int tri_begin, int tri_end, orc_contact *out, int64_t cap);
+
 /* Same contact set, computed once per distinct (point, triangle) pair
  * using point -> incident triangle lists (the evaluation order the CUDA
  * path uses); contacts sorted by (point, face triangle).  inst (may be

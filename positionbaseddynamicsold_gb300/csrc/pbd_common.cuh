@@ -114,6 +114,7 @@ struct pbd_object {
     // state (w of x and p = massBuffer value)
     pbd::DBuf<float4> x, p, v;
     pbd::DBuf<float> mass;
+    std::vector<float> h_mass;              // host copy of massBuffer
     // meshTopol triangles: (i0, i1, i2, instance)
     pbd::DBuf<int4> tri;
     pbd::DBuf<int> pt_tri_first, pt_tri_last, pt_tri;  // point -> incident triangles
@@ -216,6 +217,7 @@ struct pbd_solver {
     int g_sub = 0, g_it = 0;
     pbd_colli *g_colli = nullptr;
     int g_sig = 0;
+    long long g_kernels = 0;
 };
 
 // internal entry points shared between translation units

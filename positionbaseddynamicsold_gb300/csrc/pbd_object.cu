@@ -578,6 +578,7 @@ int pbd_object_create(const pbd_object_desc *d, pbd_object **out) {
     for (int k = 0; k < 3; ++k) o->gravity[k] = d->gravity[k];
     o->h_prim_count = cnt;
     o->h_ctype = ct;
+    o->h_mass.assign(d->mass, d->mass + d->n_points);
     int r;
     if (cudaStreamCreateWithFlags(&o->stream, cudaStreamNonBlocking) != cudaSuccess) {
         set_error("cudaStreamCreate failed: %s", cudaGetErrorString(cudaGetLastError()));
@@ -841,15 +842,8 @@ static int copy_out3(pbd_object *o, const float4 *src, float *dst) {
 static int copy_in3(pbd_object *o, float4 *dst, const float *src, bool keep_w) {
     PBD_CHECK(o && src, PBD_ERR_ARG, "null argument");
     std::vector<float4> h(o->n);
-    std::vector<float> m;
-    if (keep_w) {
-        m.resize(o->n);
-        PBD_CUDA(cudaMemcpyAsync(m.data(), o->mass.p, sizeof(float) * o->n, cudaMemcpyDeviceToHost,
-                                 o->stream));
-        PBD_CUDA(cudaStreamSynchronize(o->stream));
-    }
     for (int i = 0; i < o->n; ++i)
-        h[i] = make_float4(src[3 * i], src[3 * i + 1], src[3 * i + 2], keep_w ? m[i] : 0.f);
+        h[i] = make_float4(src[3 * i], src[3 * i + 1], src[3 * i + 2], keep_w ? o->h_mass[i] : 0.f);
     PBD_CUDA(cudaMemcpyAsync(dst, h.data(), sizeof(float4) * o->n, cudaMemcpyHostToDevice, o->stream));
     PBD_CUDA(cudaStreamSynchronize(o->stream));
     return PBD_OK;
@@ -1185,6 +1179,16 @@ int pbd_solver_step(pbd_solver *s, float dt, int substeps, int iterations, pbd_c
             return r;
         }
         PBD_CUDA(e);
+        size_t nn = 0;
+        cudaGraphGetNodes(g, nullptr, &nn);
+        std::vector<cudaGraphNode_t> nodes(nn);
+        cudaGraphGetNodes(g, nodes.data(), &nn);
+        long long nk = 0;
+        for (size_t i = 0; i < nn; ++i) {
+            cudaGraphNodeType t;
+            if (cudaGraphNodeGetType(nodes[i], &t) == cudaSuccess && t == cudaGraphNodeTypeKernel) ++nk;
+        }
+        s->g_kernels = nk;
         cudaError_t ei = cudaGraphInstantiate(&s->gexec, g, 0);
         cudaGraphDestroy(g);
         PBD_CUDA(ei);
@@ -1195,6 +1199,12 @@ int pbd_solver_step(pbd_solver *s, float dt, int substeps, int iterations, pbd_c
         s->g_sig = sig;
     }
     PBD_CUDA(cudaGraphLaunch(s->gexec, st));
+    return PBD_OK;
+}
+
+int pbd_solver_graph_kernels(pbd_solver *s, long long *n) {
+    PBD_CHECK(s && n, PBD_ERR_ARG, "null argument");
+    *n = s->gexec ? s->g_kernels : 0;
     return PBD_OK;
 }
 

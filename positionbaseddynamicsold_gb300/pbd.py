@@ -54,7 +54,7 @@ EXPORTS = [
     "pbd_solver_destroy", "pbd_solver_set_target", "pbd_solver_advect",
     "pbd_solver_project_constraint", "pbd_solver_project_constraint_with_colli",
     "pbd_solver_integration", "pbd_solver_set_sphere", "pbd_solver_set_ground",
-    "pbd_solver_step", "pbd_shs_create", "pbd_shs_create_hashed", "pbd_shs_destroy",
+    "pbd_solver_step", "pbd_solver_graph_kernels", "pbd_shs_create", "pbd_shs_create_hashed", "pbd_shs_destroy",
     "pbd_shs_set_grid_center", "pbd_shs_set_grid_size", "pbd_shs_set_division", "pbd_shs_init",
     "pbd_shs_update", "pbd_shs_find_neighbors", "pbd_shs_find_neighbors_all",
     "pbd_colli_create", "pbd_colli_destroy", "pbd_colli_set_target",
@@ -448,6 +448,11 @@ class SolverPBD:
 
     def set_ground(self, enable, height=0.0):
         _check(self.L.pbd_solver_set_ground(self.h, int(enable), height))
+
+    def graph_kernels(self):
+        n = C.c_longlong()
+        _check(self.L.pbd_solver_graph_kernels(self.h, C.byref(n)))
+        return n.value
 
     def step(self, dt, substeps=1, iterations=20, colli=None, use_graph=True):
         _check(self.L.pbd_solver_step(self.h, dt, substeps, iterations,
