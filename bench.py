@@ -178,6 +178,8 @@ def run_ours(args, rank, world):
     clocks = ClockSampler(torch.cuda.current_device())
     clocks.start()
     t_wall = time.perf_counter()
+    if args.profile_range:
+        torch.cuda.profiler.start()
     with torch.cuda.stream(stream):
         for k in range(args.steps):
             flush.fill_(k & 255)
@@ -185,6 +187,8 @@ def run_ours(args, rank, world):
             step()
             ev[k][1].record(stream)
     torch.cuda.synchronize()
+    if args.profile_range:
+        torch.cuda.profiler.stop()
     t_wall = time.perf_counter() - t_wall
     clk = clocks.stop()
     ms = sum(a.elapsed_time(b) for a, b in ev)
@@ -369,6 +373,9 @@ def main():
     ap.add_argument("--workload", default="drape256", choices=["drape256", "fold1024", "hanging32"])
     ap.add_argument("--preroll", type=int, default=120)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile-range", action="store_true",
+                    help="cudaProfilerStart/Stop around the timed substeps (for ncu "
+                         "--profile-from-start off)")
     ap.add_argument("--traffic", type=float, default=None,
                     help="ncu dram bytes per launch of the dominant kernel (from profiles/)")
     args = ap.parse_args()
