@@ -212,6 +212,29 @@ int pbd_colli_get_contacts(pbd_colli *c, int *ids, int *face, float *t, double *
  * the last CCD call, and the overflow flag */
 int pbd_colli_stats(pbd_colli *c, long long *candidates, long long *contacts, int *overflow);
 
+/* ---- allocation-free residual --------------------------------------------- */
+/* No counterpart in the reference.  The relative residual of
+ * pbd_constraints_residual computed from device buffers the caller owns,
+ * without allocating device memory: for callers that cannot let a library
+ * call cudaMalloc (an engine that sub-allocates everything from its own
+ * arena, code between its allocation phase and a graph capture, a process
+ * under a fixed device-memory budget).  Partial sums live in a 1 MiB
+ * file-scope device array that every GPU loading the library keeps until
+ * exit; calls whose work overlaps on the GPU race on it.  The first call on a
+ * device looks the array's address up (make it before any stream capture).
+ *   d_pos4       float4 per point (xyz used), 16-byte aligned
+ *   d_dist_idx   int2 per distance constraint, d_rest_length float each
+ *   d_bend_idx   int4 {e0, e1, wA, wB} per bending constraint, with
+ *                d_rest_angle and d_hinge_rest (rest hinge length) each
+ *   d_out        3 doubles on the device: residual, sum C^2, sum L^2
+ *   stream       cudaStream_t (NULL = legacy default stream)
+ * At most 16,777,216 constraints in total (PBD_ERR_ARG beyond).  A point id
+ * outside [0, n_points) is skipped and the residual written as NaN. */
+int pbd_residual_noalloc(const float *d_pos4, int n_points, const int *d_dist_idx,
+                         const float *d_rest_length, int n_dist, const int *d_bend_idx,
+                         const float *d_rest_angle, const float *d_hinge_rest, int n_bend,
+                         double *d_out, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

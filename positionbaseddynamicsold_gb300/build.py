@@ -23,6 +23,7 @@ SOURCES = {
     "pbd_sort.cu": [],
     "pbd_object.cu": ["-fmad=false"],
     "pbd_collision.cu": ["-fmad=false"],
+    "pbd_noalloc.cu": [],
 }
 HEADERS = ["pbd_common.cuh"]
 

@@ -61,6 +61,7 @@ EXPORTS = [
     "pbd_colli_set_acce_struct", "pbd_colli_set_thickness", "pbd_colli_set_iterations",
     "pbd_colli_set_response", "pbd_colli_set_capacity", "pbd_colli_ccd_sh_extended",
     "pbd_colli_collision_resolve_new", "pbd_colli_get_contacts", "pbd_colli_stats",
+    "pbd_residual_noalloc",
 ]
 
 
@@ -99,6 +100,9 @@ def load(build_if_missing: bool = True) -> C.CDLL:
     L.pbd_shs_find_neighbors_all.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_longlong,
                                              C.c_void_p]
     L.pbd_colli_get_contacts.argtypes = [C.c_void_p] + [C.c_void_p] * 5 + [C.c_longlong, C.c_void_p]
+    L.pbd_residual_noalloc.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_int,
+                                       C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p,
+                                       C.c_void_p]
     _LIB = L
     return L
 
@@ -457,3 +461,12 @@ class SolverPBD:
     def step(self, dt, substeps=1, iterations=20, colli=None, use_graph=True):
         _check(self.L.pbd_solver_step(self.h, dt, substeps, iterations,
                                       colli.h if colli else None, int(use_graph)))
+
+
+def residual_noalloc(d_pos4, n_points, d_dist_idx, d_rest_length, n_dist, d_bend_idx,
+                     d_rest_angle, d_hinge_rest, n_bend, d_out, stream=0):
+    """pbd_residual_noalloc on caller-owned device pointers (ints)."""
+    L = load()
+    _check(L.pbd_residual_noalloc(d_pos4, n_points, d_dist_idx or None, d_rest_length or None,
+                                  n_dist, d_bend_idx or None, d_rest_angle or None,
+                                  d_hinge_rest or None, n_bend, d_out, stream or None))
