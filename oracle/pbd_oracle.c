@@ -1169,7 +1169,11 @@ void orc_collision_resolve_jacobi(int n_points, int n_contacts,
                                   float *prdp, const float *mass, int iterations,
                                   float thickness, int mass_weighted)
 {
-    float *acc = (float *)malloc(sizeof(float) * 3 * (size_t)(n_points > 0 ? n_points : 1));
+    /* Corrections are accumulated in 2^-32 m fixed point (each float
+     * correction rounded to the nearest integer multiple, ties to even), so
+     * the sum does not depend on the order contacts are visited in; each
+     * point then moves by sum * 2^-32 / count (double), rounded to float. */
+    int64_t *acc = (int64_t *)malloc(sizeof(int64_t) * 3 * (size_t)(n_points > 0 ? n_points : 1));
     int *cnt = (int *)malloc(sizeof(int) * (size_t)(n_points > 0 ? n_points : 1));
     float *dl = (float *)malloc(sizeof(float) * 12 * (size_t)(n_contacts > 0 ? n_contacts : 1));
     int *act = (int *)malloc(sizeof(int) * (size_t)(n_contacts > 0 ? n_contacts : 1));
@@ -1182,22 +1186,22 @@ void orc_collision_resolve_jacobi(int n_points, int n_contacts,
             for (int j = 0; j < 4; ++j) wm[j] = mass ? mass[ids[j]] : 1.0f;
             act[c] = orc_vf_resolve_deltas(xs, ps, wm, thickness, mass_weighted, dl + 12 * c);
         }
-        /* each point: mean of its active corrections, summed in contact
-         * order (contacts are sorted by point, then face) */
-        memset(acc, 0, sizeof(float) * 3 * (size_t)n_points);
+        memset(acc, 0, sizeof(int64_t) * 3 * (size_t)n_points);
         memset(cnt, 0, sizeof(int) * (size_t)n_points);
         for (int c = 0; c < n_contacts; ++c) {
             if (!act[c]) continue;
             int ids[4] = {cts[c].v, cts[c].f0, cts[c].f1, cts[c].f2};
             for (int j = 0; j < 4; ++j) {
-                for (int k = 0; k < 3; ++k) acc[3 * ids[j] + k] += dl[12 * c + 3 * j + k];
+                for (int k = 0; k < 3; ++k)
+                    acc[3 * ids[j] + k] += (int64_t)llrintf(dl[12 * c + 3 * j + k] * 4294967296.0f);
                 cnt[ids[j]]++;
             }
         }
         for (int i = 0; i < n_points; ++i)
             if (cnt[i] > 0)
                 for (int k = 0; k < 3; ++k)
-                    prdp[3 * i + k] = prdp[3 * i + k] + acc[3 * i + k] / (float)cnt[i];
+                    prdp[3 * i + k] = prdp[3 * i + k] +
+                        (float)((double)acc[3 * i + k] * (1.0 / 4294967296.0) / (double)cnt[i]);
     }
     free(acc);
     free(cnt);

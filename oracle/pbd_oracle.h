@@ -257,9 +257,10 @@ void orc_collision_resolve_ref(int n_contacts, const orc_contact *cts,
 /* Contact response as the CUDA path runs it: per pass every contact
  * evaluates VFResolveTest on the pass-start positions and, if active,
  * computes its four corrections; each point then moves by the mean of the
- * corrections of its active contacts.  mass_weighted=0 uses the reference
- * split (VFResolveNew); 1 uses the inverse-mass split (see the CUDA
- * kernel for the formula). */
+ * corrections of its active contacts, summed in 2^-32 m fixed point so the
+ * result does not depend on contact order.  mass_weighted=0 uses the
+ * reference split (VFResolveNew); 1 uses the inverse-mass split (see the
+ * CUDA kernel for the formula). */
 void orc_collision_resolve_jacobi(int n_points, int n_contacts,
                                   const orc_contact *cts, const float *pos,
                                   float *prdp, const float *mass, int iterations,

@@ -6,27 +6,32 @@
 //      bucket key (bounded grid: the reference's linear cell id; hashed:
 //      Teschner et al. 2003 hash of the cell mod 2^k), swept AABB;
 //   2. stable radix sort of (bucket, triangle id) and a bucket -> [start, end)
-//      table (the reference's cellStart/cellEnd, reset each update);
-//   3. one thread per point: the union of the 27-cell neighbourhoods of the
-//      centroid cells of its incident triangles (CCD_SH_Extended,
-//      P/CCD.cpp:1541-1586, tests every (point, neighbour) pair; the union
-//      holds each distinct pair once), exact-cell check per bucket entry,
-//      then two conservative FP32 filters that cannot reject a pair the
-//      ExtendedVFTest would accept (swept-AABB overlap with margin 5.5 h and
-//      a lower bound on the point-triangle distance over the step);
-//      survivors are appended with one atomic per warp.
+//      table (the reference's cellStart/cellEnd, reset each update) plus the
+//      union of the swept AABBs of each bucket's triangles;
+//   3. one warp per point, one lane per cell of the union of the 27-cell
+//      neighbourhoods of the centroid cells of its incident triangles
+//      (CCD_SH_Extended, P/CCD.cpp:1541-1586, tests every (point, neighbour)
+//      pair; the union holds each distinct pair once); a cell whose bucket
+//      AABB misses the point's grown swept AABB is skipped; per entry an
+//      exact-cell check, then two conservative FP32 filters that cannot
+//      reject a pair the ExtendedVFTest would accept (swept-AABB overlap with
+//      margin 5.5 h and a lower bound on the point-triangle distance over the
+//      step); survivors are appended with one atomic per group of lanes.
 // Narrowphase: one thread per surviving pair runs ExtendedVFTest
 // (P/CCD.cpp:1733-1808) with the reference's arithmetic: float triple
 // products widened to double, the double cubic solve (P/CCD.cpp:48-113), the
-// float barycentric inside test.  Contacts are sorted by (point, triangle).
+// float barycentric inside test.  Contacts are kept in discovery order on the
+// device and sorted by (point, triangle) only when copied out.
 // Response: per pass every contact computes its four corrections from the
-// pass-start positions (VFResolveTest + VFResolveNew, P/CCD.cpp:1996-2090);
-// each point then moves by the mean of its active corrections, summed in
-// contact order (deterministic, no float atomics).
+// pass-start positions (VFResolveTest + VFResolveNew, P/CCD.cpp:1996-2090)
+// and adds them to per-point sums in 2^-32 m fixed point (integer atomics:
+// the sum is exact, so the result does not depend on contact order); each
+// point then moves by sum / count.
 //
 // Compiled with -fmad=false: products round separately as in the reference.
 #include <cooperative_groups.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 
@@ -266,17 +271,14 @@ __device__ __forceinline__ int agg_inc(int *counter) {
 }
 
 // ---------------------------------------------------------------------------
-__global__ void k_reset_buckets(const uint32_t *skey, const int *n_prev, uint32_t nb, int *bstart,
-                                int *bend, long long cap) {
+__global__ void k_reset_buckets(const uint32_t *skey, const int *n_prev, uint32_t nb,
+                                int2 *brange, long long cap) {
     long long n = *n_prev;
     if (n > cap) n = cap;
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
          i += (long long)gridDim.x * blockDim.x) {
         uint32_t k = skey[i];
-        if (k < nb) {
-            bstart[k] = 0;
-            bend[k] = 0;
-        }
+        if (k < nb) brange[k] = make_int2(0, 0);
     }
 }
 
@@ -322,21 +324,31 @@ __global__ void __launch_bounds__(256) k_tri_cells(int nt, GridParams g, float m
 }
 
 __global__ void k_bucket_ranges(const uint32_t *skey, const int *sid, const int *n_valid,
-                                const int4 *tcell, int *bstart, int *bend, int4 *scell) {
+                                const int4 *tcell, const float4 *tlo, const float4 *thi,
+                                int2 *brange, float4 *blo, float4 *bhi, int4 *scell) {
     int n = *n_valid;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         uint32_t k = skey[i];
-        if (i == 0 || skey[i - 1] != k) bstart[k] = i;
-        if (i == n - 1 || skey[i + 1] != k) bend[k] = i + 1;
         scell[i] = tcell[sid[i]];
+        if (i > 0 && skey[i - 1] == k) continue;
+        float4 lo = tlo[sid[i]], hi = thi[sid[i]];
+        int e = i + 1;
+        for (; e < n && skey[e] == k; ++e) {
+            float4 a = tlo[sid[e]], b = thi[sid[e]];
+            lo.x = fminf(lo.x, a.x); lo.y = fminf(lo.y, a.y); lo.z = fminf(lo.z, a.z);
+            hi.x = fmaxf(hi.x, b.x); hi.y = fmaxf(hi.y, b.y); hi.z = fmaxf(hi.z, b.z);
+        }
+        brange[k] = make_int2(i, e);
+        blo[k] = lo;
+        bhi[k] = hi;
     }
 }
 
 // FindNeighbors (P/SpatialHashSystem.cpp:134-187) for every triangle:
 // count (out == nullptr) or fill
-__global__ void k_find_neighbors(int nt, GridParams g, const int4 *tcell, const int *bstart,
-                                 const int *bend, const int4 *scell, const int *sid,
-                                 const int *off, int *cnt, int *out) {
+__global__ void k_find_neighbors(int nt, GridParams g, const int4 *tcell, const int2 *brange,
+                                 const int4 *scell, const int *sid, const int *off, int *cnt,
+                                 int *out) {
     int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= nt) return;
     int4 c = tcell[t];
@@ -347,8 +359,8 @@ __global__ void k_find_neighbors(int nt, GridParams g, const int4 *tcell, const 
                 for (int x = -1; x <= 1; ++x) {
                     int nx = c.x + x, ny = c.y + y, nz = c.z + z;
                     if (!g.hashed && outside(g, nx, ny, nz)) continue;
-                    uint32_t b = bucket_of(g, nx, ny, nz);
-                    for (int i = bstart[b]; i < bend[b]; ++i) {
+                    int2 r = brange[bucket_of(g, nx, ny, nz)];
+                    for (int i = r.x; i < r.y; ++i) {
                         int4 sc = scell[i];
                         if (sc.x != nx || sc.y != ny || sc.z != nz) continue;
                         int id = sid[i];
@@ -361,104 +373,120 @@ __global__ void k_find_neighbors(int nt, GridParams g, const int4 *tcell, const 
     if (cnt) cnt[t] = k;
 }
 
-// candidate pairs: one thread per point
-__global__ void __launch_bounds__(128) k_candidates(
+// candidate pairs: one warp per point, lanes over the candidate cells
+constexpr int kCandWarps = 4;
+__global__ void __launch_bounds__(32 * kCandWarps) k_candidates(
     int n, GridParams g, float margin, float reach, const int4 *__restrict__ tri,
     const int *__restrict__ pt_first, const int *__restrict__ pt_last,
     const int *__restrict__ pt_tri, const int *__restrict__ point_inst,
     const float4 *__restrict__ x, const float4 *__restrict__ p, const int4 *__restrict__ tcell,
     const float4 *__restrict__ tlo, const float4 *__restrict__ thi,
-    const int *__restrict__ bstart, const int *__restrict__ bend,
-    const int4 *__restrict__ scell, const int *__restrict__ sid, int2 *cand, long long cap,
-    int *counters) {
-    int v = blockIdx.x * blockDim.x + threadIdx.x;
-    bool active = v < n;
-    int cx[kMaxInc], cy[kMaxInc], cz[kMaxInc];
-    int nc = 0;
-    int lo[3] = {0, 0, 0}, hi[3] = {-1, -1, -1};
-    v3 X0 = mk3(0, 0, 0), P0 = mk3(0, 0, 0);
-    float plo[3], phi[3];
-    int inst = 0;
-    if (active) {
+    const int2 *__restrict__ brange, const float4 *__restrict__ blo,
+    const float4 *__restrict__ bhi, const int4 *__restrict__ scell, const int *__restrict__ sid,
+    int2 *cand, long long cap, int *counters) {
+    const int lane = threadIdx.x & 31;
+    const int warp0 = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int nwarps = (gridDim.x * blockDim.x) >> 5;
+    for (int v = warp0; v < n; v += nwarps) {
         int f0 = pt_first[v], f1 = pt_last[v];
-        if (f1 - f0 > kMaxInc) atomicOr(counters + 2, 4);
-        for (int q = f0; q < f1 && nc < kMaxInc; ++q) {
-            int4 c = tcell[pt_tri[q]];
-            if (!g.hashed && outside(g, c.x, c.y, c.z)) continue;
-            cx[nc] = c.x;
-            cy[nc] = c.y;
-            cz[nc] = c.z;
-            if (nc == 0) {
-                lo[0] = hi[0] = c.x;
-                lo[1] = hi[1] = c.y;
-                lo[2] = hi[2] = c.z;
-            } else {
-                lo[0] = min(lo[0], c.x); hi[0] = max(hi[0], c.x);
-                lo[1] = min(lo[1], c.y); hi[1] = max(hi[1], c.y);
-                lo[2] = min(lo[2], c.z); hi[2] = max(hi[2], c.z);
-            }
-            ++nc;
+        int ninc = f1 - f0;
+        if (ninc > kMaxInc) {
+            if (lane == 0) atomicOr(counters + 2, 4);
+            ninc = kMaxInc;
         }
-        X0 = ld3(x[v]);
-        P0 = ld3(p[v]);
-        // swept AABB of the point, grown by the per-axis reach of a hit
-        plo[0] = fminf(X0.x, P0.x) - margin; phi[0] = fmaxf(X0.x, P0.x) + margin;
-        plo[1] = fminf(X0.y, P0.y) - margin; phi[1] = fmaxf(X0.y, P0.y) + margin;
-        plo[2] = fminf(X0.z, P0.z) - margin; phi[2] = fmaxf(X0.z, P0.z) + margin;
-        if (point_inst) inst = point_inst[v];
-    }
-    if (!active || nc == 0) {
-        lo[0] = 1; hi[0] = -1;  // empty cell loop
-    }
-    v3 D0 = sub3(P0, X0);
-    for (int z = lo[2] - 1; z <= hi[2] + 1; ++z)
-        for (int y = lo[1] - 1; y <= hi[1] + 1; ++y)
-            for (int xx = lo[0] - 1; xx <= hi[0] + 1; ++xx) {
-                bool near = false;
-                for (int i = 0; i < nc && !near; ++i)
-                    near = abs(cx[i] - xx) <= 1 && abs(cy[i] - y) <= 1 && abs(cz[i] - z) <= 1;
-                if (!near) continue;
-                if (!g.hashed && outside(g, xx, y, z)) continue;
-                uint32_t b = bucket_of(g, xx, y, z);
-                int e1 = bend[b];
-                for (int e = bstart[b]; e < e1; ++e) {
-                    int4 sc = scell[e];
-                    if (sc.x != xx || sc.y != y || sc.z != z) continue;
-                    if (point_inst && sc.w != inst) continue;
-                    int f = sid[e];
-                    float4 bl = tlo[f], bh = thi[f];
-                    if (plo[0] > bh.x || phi[0] < bl.x || plo[1] > bh.y || phi[1] < bl.y ||
-                        plo[2] > bh.z || phi[2] < bl.z)
-                        continue;
-                    int4 fi = tri[f];
-                    if (fi.x == v || fi.y == v || fi.z == v) continue;
-                    if (bl.w == 0.f) {
-                        // lower bound of the point-triangle distance over the step
-                        v3 xa = ld3(x[fi.x]), xb = ld3(x[fi.y]), xc = ld3(x[fi.z]);
-                        v3 pa = ld3(p[fi.x]), pb = ld3(p[fi.y]), pc = ld3(p[fi.z]);
-                        float d0 = point_tri_dist(X0, xa, xb, xc);
-                        float d1 = point_tri_dist(P0, pa, pb, pc);
-                        v3 ua = sub3(sub3(pa, xa), D0), ub = sub3(sub3(pb, xb), D0),
-                           uc = sub3(sub3(pc, xc), D0);
-                        float U = sqrtf(fmaxf(fmaxf(dot3(ua, ua), dot3(ub, ub)), dot3(uc, uc)));
-                        if ((d0 + d1 - U) * 0.5f > reach) continue;
-                    }
-                    long long slot = agg_inc(counters);
-                    if (slot < cap)
-                        cand[slot] = make_int2(v, f);
-                    else
-                        atomicOr(counters + 2, 1);
+        int4 mc = make_int4(0, 0, 0, 0);
+        bool valid = false;
+        if (lane < ninc) {
+            mc = tcell[pt_tri[f0 + lane]];
+            valid = g.hashed || !outside(g, mc.x, mc.y, mc.z);
+        }
+        unsigned vm = __ballot_sync(0xffffffffu, valid);
+        if (!vm) continue;
+        // the incident centroid cells, broadcast to every lane
+        int cx[kMaxInc], cy[kMaxInc], cz[kMaxInc];
+        int nc = 0;
+        int lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
+#pragma unroll
+        for (int i = 0; i < kMaxInc; ++i) {
+            int src = __ffs(vm) - 1;
+            int x_ = __shfl_sync(0xffffffffu, mc.x, src < 0 ? 0 : src);
+            int y_ = __shfl_sync(0xffffffffu, mc.y, src < 0 ? 0 : src);
+            int z_ = __shfl_sync(0xffffffffu, mc.z, src < 0 ? 0 : src);
+            if (src >= 0) {
+                cx[nc] = x_; cy[nc] = y_; cz[nc] = z_;
+                if (nc == 0) {
+                    lo[0] = hi[0] = x_; lo[1] = hi[1] = y_; lo[2] = hi[2] = z_;
+                } else {
+                    lo[0] = min(lo[0], x_); hi[0] = max(hi[0], x_);
+                    lo[1] = min(lo[1], y_); hi[1] = max(hi[1], y_);
+                    lo[2] = min(lo[2], z_); hi[2] = max(hi[2], z_);
                 }
+                ++nc;
+                vm &= vm - 1;
             }
+        }
+        v3 X0 = ld3(x[v]), P0 = ld3(p[v]);
+        v3 D0 = sub3(P0, X0);
+        // swept AABB of the point, grown by the per-axis reach of a hit
+        float plx = fminf(X0.x, P0.x) - margin, phx = fmaxf(X0.x, P0.x) + margin;
+        float ply = fminf(X0.y, P0.y) - margin, phy = fmaxf(X0.y, P0.y) + margin;
+        float plz = fminf(X0.z, P0.z) - margin, phz = fmaxf(X0.z, P0.z) + margin;
+        int inst = point_inst ? point_inst[v] : 0;
+        int ex = hi[0] - lo[0] + 3, ey = hi[1] - lo[1] + 3, ez = hi[2] - lo[2] + 3;
+        int ncell = ex * ey * ez;
+        for (int ci = lane; ci < ncell; ci += 32) {
+            int xx = lo[0] - 1 + ci % ex;
+            int y = lo[1] - 1 + (ci / ex) % ey;
+            int z = lo[2] - 1 + ci / (ex * ey);
+            bool near = false;
+            for (int i = 0; i < nc; ++i)
+                near |= abs(cx[i] - xx) <= 1 && abs(cy[i] - y) <= 1 && abs(cz[i] - z) <= 1;
+            if (!near) continue;
+            if (!g.hashed && outside(g, xx, y, z)) continue;
+            uint32_t b = bucket_of(g, xx, y, z);
+            int2 r = brange[b];
+            if (r.x >= r.y) continue;
+            float4 bl = blo[b], bh = bhi[b];
+            if (plx > bh.x || phx < bl.x || ply > bh.y || phy < bl.y || plz > bh.z || phz < bl.z)
+                continue;
+            for (int e = r.x; e < r.y; ++e) {
+                int4 sc = scell[e];
+                if (sc.x != xx || sc.y != y || sc.z != z) continue;
+                if (point_inst && sc.w != inst) continue;
+                int f = sid[e];
+                float4 tl = tlo[f], th = thi[f];
+                if (plx > th.x || phx < tl.x || ply > th.y || phy < tl.y || plz > th.z ||
+                    phz < tl.z)
+                    continue;
+                int4 fi = tri[f];
+                if (fi.x == v || fi.y == v || fi.z == v) continue;
+                if (tl.w == 0.f) {
+                    // lower bound of the point-triangle distance over the step
+                    v3 xa = ld3(x[fi.x]), xb = ld3(x[fi.y]), xc = ld3(x[fi.z]);
+                    v3 pa = ld3(p[fi.x]), pb = ld3(p[fi.y]), pc = ld3(p[fi.z]);
+                    float d0 = point_tri_dist(X0, xa, xb, xc);
+                    float d1 = point_tri_dist(P0, pa, pb, pc);
+                    v3 ua = sub3(sub3(pa, xa), D0), ub = sub3(sub3(pb, xb), D0),
+                       uc = sub3(sub3(pc, xc), D0);
+                    float U = sqrtf(fmaxf(fmaxf(dot3(ua, ua), dot3(ub, ub)), dot3(uc, uc)));
+                    if ((d0 + d1 - U) * 0.5f > reach) continue;
+                }
+                long long slot = agg_inc(counters);
+                if (slot < cap)
+                    cand[slot] = make_int2(v, f);
+                else
+                    atomicOr(counters + 2, 1);
+            }
+        }
+    }
 }
 
 __global__ void __launch_bounds__(128) k_narrow(const int2 *__restrict__ cand, long long cap,
                                                 int nt, float th, const int4 *__restrict__ tri,
                                                 const float4 *__restrict__ x,
                                                 const float4 *__restrict__ p, int *counters,
-                                                long long ccap, unsigned long long *ckey,
-                                                int *cperm, int4 *cids, int *cface, float4 *ctn,
-                                                double4 *cw) {
+                                                long long ccap, int4 *cids, int *cface,
+                                                float4 *ctn, double4 *cw) {
     long long n = counters[0];
     if (n > cap) n = cap;
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
@@ -474,8 +502,6 @@ __global__ void __launch_bounds__(128) k_narrow(const int2 *__restrict__ cand, l
             atomicOr(counters + 2, 2);
             continue;
         }
-        ckey[slot] = (unsigned long long)c.x * (unsigned long long)nt + (unsigned long long)c.y;
-        cperm[slot] = slot;
         cids[slot] = make_int4(c.x, f.x, f.y, f.z);
         cface[slot] = c.y;
         ctn[slot] = make_float4(r.t, r.n.x, r.n.y, r.n.z);
@@ -486,39 +512,23 @@ __global__ void __launch_bounds__(128) k_narrow(const int2 *__restrict__ cand, l
 __global__ void k_clamp_counts(int *counters, long long cap, long long ccap) {
     if (threadIdx.x == 0 && blockIdx.x == 0) {
         if (counters[1] > ccap) counters[1] = (int)ccap;
-        counters[3] = 4 * counters[1];
         if (counters[0] > cap) counters[0] = (int)cap;
     }
 }
 
-__global__ void k_gather_contacts(const int *counters, const int *perm, const int4 *ids_raw,
-                                  const int *face_raw, const float4 *tn_raw,
-                                  const double4 *w_raw, int4 *ids, int *face, float4 *tn,
-                                  double4 *w, uint32_t *ekey, int *eval_) {
-    int n = counters[1];
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        int j = perm[i];
-        int4 a = ids_raw[j];
-        ids[i] = a;
-        face[i] = face_raw[j];
-        tn[i] = tn_raw[j];
-        w[i] = w_raw[j];
-        ekey[4 * i] = (uint32_t)a.x;
-        ekey[4 * i + 1] = (uint32_t)a.y;
-        ekey[4 * i + 2] = (uint32_t)a.z;
-        ekey[4 * i + 3] = (uint32_t)a.w;
-        eval_[4 * i] = 4 * i;
-        eval_[4 * i + 1] = 4 * i + 1;
-        eval_[4 * i + 2] = 4 * i + 2;
-        eval_[4 * i + 3] = 4 * i + 3;
-    }
+__device__ __forceinline__ void add_fixed(long long *acc, int pt, float dx, float dy, float dz) {
+    atomicAdd((unsigned long long *)(acc + 3 * (long long)pt), (unsigned long long)__float2ll_rn(dx * 4294967296.0f));
+    atomicAdd((unsigned long long *)(acc + 3 * (long long)pt + 1), (unsigned long long)__float2ll_rn(dy * 4294967296.0f));
+    atomicAdd((unsigned long long *)(acc + 3 * (long long)pt + 2), (unsigned long long)__float2ll_rn(dz * 4294967296.0f));
 }
 
 // corrections of one contact (VFResolveTest + VFResolveNew, P/CCD.cpp:1996-2090)
+// added to the per-point fixed-point sums
 __global__ void __launch_bounds__(128) k_contact_deltas(const int *counters, const int4 *ids,
                                                         const float4 *__restrict__ x,
                                                         const float4 *__restrict__ p, float th,
-                                                        int mass_weighted, float4 *delta) {
+                                                        int mass_weighted, long long *acc,
+                                                        int *acnt) {
     int n = counters[1];
     for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < n; c += gridDim.x * blockDim.x) {
         int4 id = ids[c];
@@ -526,89 +536,78 @@ __global__ void __launch_bounds__(128) k_contact_deltas(const int *counters, con
         v3 X0 = ld3(q0), X1 = ld3(q1), X2 = ld3(q2), X3 = ld3(q3);
         v3 P0 = ld3(p[id.x]), P1 = ld3(p[id.y]), P2 = ld3(p[id.z]), P3 = ld3(p[id.w]);
         float wm0 = q0.w, wm1 = q1.w, wm2 = q2.w, wm3 = q3.w;
-        float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
-        float4 out[4] = {zero, zero, zero, zero};
         v3 e1 = sub3(P2, P1), e2 = sub3(P3, P1);
         v3 pr = cross3(e1, e2);
         float pr2 = dot3(pr, pr);
         bool ok = mass_weighted ? (pr2 > 1e-12f * (dot3(e1, e1) * dot3(e2, e2)))
                                 : !((double)pr2 <= 1e-6);
-        if (ok) {
-            v3 fn = nrm3(cross3(sub3(X2, X1), sub3(X3, X1)));
-            bool dir = dot3(sub3(X0, X1), fn) >= 0;  // RelativePos
-            v3 pn = nrm3(pr);
-            float sg = dir ? 1.0f : -1.0f;
-            v3 ns = mul3(pn, sg);
-            float gap = (float)((double)dot3(sub3(P0, P1), ns) - 2.0 * (double)th);
-            if (gap < -1e-6f) {
-                v3 p1proj = add3(P1, mul3(mul3(ns, 2.0f), th));
-                float depth = (float)((double)dot3(sub3(p1proj, P0), ns) * 0.5);
-                v3 w = bary(P0, P1, P2, P3);
-                v3 dv, d1, d2, d3;
-                bool act = true;
-                if (!mass_weighted) {
-                    v3 vfix = mul3(ns, depth);
-                    v3 ffix = mul3(mul3(pn, -sg), depth);
-                    float sw = w.x * w.x + w.y * w.y + w.z * w.z;
-                    dv = vfix;
-                    d1 = div3(mul3(ffix, w.x), sw);
-                    d2 = div3(mul3(ffix, w.y), sw);
-                    d3 = div3(mul3(ffix, w.z), sw);
-                } else {
-                    float sw = w.x * w.x + w.y * w.y + w.z * w.z;
-                    float swm = w.x * w.x * wm1 + w.y * w.y * wm2 + w.z * w.z * wm3;
-                    float mf = swm / sw;
-                    float msum = wm0 + mf;
-                    if (!(msum > 0.0f) || !(sw > 0.0f)) {
-                        act = false;
-                    } else {
-                        float alpha = wm0 / msum;
-                        float sep = 2.0f * depth;
-                        dv = mul3(ns, sep * alpha);
-                        float fs = swm > 0.0f ? -sep * (1.0f - alpha) / swm : 0.0f;
-                        d1 = mul3(ns, fs * w.x * wm1);
-                        d2 = mul3(ns, fs * w.y * wm2);
-                        d3 = mul3(ns, fs * w.z * wm3);
-                    }
-                }
-                if (act) {
-                    out[0] = make_float4(dv.x, dv.y, dv.z, 1.f);
-                    out[1] = make_float4(d1.x, d1.y, d1.z, 1.f);
-                    out[2] = make_float4(d2.x, d2.y, d2.z, 1.f);
-                    out[3] = make_float4(d3.x, d3.y, d3.z, 1.f);
-                }
-            }
+        if (!ok) continue;
+        v3 fn = nrm3(cross3(sub3(X2, X1), sub3(X3, X1)));
+        bool dir = dot3(sub3(X0, X1), fn) >= 0;  // RelativePos
+        v3 pn = nrm3(pr);
+        float sg = dir ? 1.0f : -1.0f;
+        v3 ns = mul3(pn, sg);
+        float gap = (float)((double)dot3(sub3(P0, P1), ns) - 2.0 * (double)th);
+        if (!(gap < -1e-6f)) continue;
+        v3 p1proj = add3(P1, mul3(mul3(ns, 2.0f), th));
+        float depth = (float)((double)dot3(sub3(p1proj, P0), ns) * 0.5);
+        v3 w = bary(P0, P1, P2, P3);
+        v3 dv, d1, d2, d3;
+        if (!mass_weighted) {
+            v3 vfix = mul3(ns, depth);
+            v3 ffix = mul3(mul3(pn, -sg), depth);
+            float sw = w.x * w.x + w.y * w.y + w.z * w.z;
+            dv = vfix;
+            d1 = div3(mul3(ffix, w.x), sw);
+            d2 = div3(mul3(ffix, w.y), sw);
+            d3 = div3(mul3(ffix, w.z), sw);
+        } else {
+            float sw = w.x * w.x + w.y * w.y + w.z * w.z;
+            float swm = w.x * w.x * wm1 + w.y * w.y * wm2 + w.z * w.z * wm3;
+            float mf = swm / sw;
+            float msum = wm0 + mf;
+            if (!(msum > 0.0f) || !(sw > 0.0f)) continue;
+            float alpha = wm0 / msum;
+            float sep = 2.0f * depth;
+            dv = mul3(ns, sep * alpha);
+            float fs = swm > 0.0f ? -sep * (1.0f - alpha) / swm : 0.0f;
+            d1 = mul3(ns, fs * w.x * wm1);
+            d2 = mul3(ns, fs * w.y * wm2);
+            d3 = mul3(ns, fs * w.z * wm3);
         }
-        delta[4 * c] = out[0];
-        delta[4 * c + 1] = out[1];
-        delta[4 * c + 2] = out[2];
-        delta[4 * c + 3] = out[3];
+        add_fixed(acc, id.x, dv.x, dv.y, dv.z);
+        add_fixed(acc, id.y, d1.x, d1.y, d1.z);
+        add_fixed(acc, id.z, d2.x, d2.y, d2.z);
+        add_fixed(acc, id.w, d3.x, d3.y, d3.z);
+        atomicAdd(acnt + id.x, 1);
+        atomicAdd(acnt + id.y, 1);
+        atomicAdd(acnt + id.z, 1);
+        atomicAdd(acnt + id.w, 1);
     }
 }
 
-// mean of the active corrections per point, summed in contact order
-__global__ void k_apply_deltas(const int *counters, const uint32_t *sekey, const int *seval,
-                               const float4 *delta, float4 *p) {
-    int n = counters[3];
+// each point of a contact: the first thread to claim it applies sum/count
+// and clears the sums
+__global__ void k_apply_deltas(const int *counters, const int4 *ids, long long *acc, int *acnt,
+                               float4 *p) {
+    int n = 4 * counters[1];
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        uint32_t pt = sekey[i];
-        if (i > 0 && sekey[i - 1] == pt) continue;
-        float ax = 0.f, ay = 0.f, az = 0.f;
-        int cnt = 0;
-        for (int e = i; e < n && sekey[e] == pt; ++e) {
-            float4 d = delta[seval[e]];
-            if (d.w != 0.f) {
-                ax = ax + d.x;
-                ay = ay + d.y;
-                az = az + d.z;
-                ++cnt;
-            }
-        }
-        if (cnt) {
-            float4 P = p[pt];
-            float fc = (float)cnt;
-            p[pt] = make_float4(P.x + ax / fc, P.y + ay / fc, P.z + az / fc, P.w);
-        }
+        int4 id = ids[i >> 2];
+        int j = i & 3;
+        int pt = j == 0 ? id.x : j == 1 ? id.y : j == 2 ? id.z : id.w;
+        int cnt = atomicExch(acnt + pt, 0);
+        if (cnt <= 0) continue;
+        long long sx = acc[3 * (long long)pt], sy = acc[3 * (long long)pt + 1],
+                  sz = acc[3 * (long long)pt + 2];
+        acc[3 * (long long)pt] = 0;
+        acc[3 * (long long)pt + 1] = 0;
+        acc[3 * (long long)pt + 2] = 0;
+        float4 P = p[pt];
+        double dc = (double)cnt;
+        P.x = P.x + (float)((double)sx * (1.0 / 4294967296.0) / dc);
+        P.y = P.y + (float)((double)sy * (1.0 / 4294967296.0) / dc);
+        P.z = P.z + (float)((double)sz * (1.0 / 4294967296.0) / dc);
+        p[pt] = P;
     }
 }
 
@@ -641,18 +640,18 @@ int shs_update(pbd_shs *h) {
     GridParams g = params_of(h);
     if (o->nt == 0) return PBD_OK;
     // clear the ranges of the buckets the previous update filled
-    k_reset_buckets<<<kPersistentBlocks, 256, 0, s>>>(h->skey, h->n_valid.p, g.nb, h->bstart.p,
-                                                      h->bend.p, o->nt);
+    k_reset_buckets<<<kPersistentBlocks, 256, 0, s>>>(h->skey, h->n_valid.p, g.nb, h->brange.p,
+                                                      o->nt);
     PBD_CUDA(cudaMemsetAsync(h->n_valid.p, 0, sizeof(int), s));
-    float margin = 0.0f;  // AABB margin is added per collision solver (see ccd_detect)
-    k_tri_cells<<<grid_for(o->nt, 256), 256, 0, s>>>(o->nt, g, margin, o->tri.p, o->x.p, o->p.p,
+    k_tri_cells<<<grid_for(o->nt, 256), 256, 0, s>>>(o->nt, g, 0.0f, o->tri.p, o->x.p, o->p.p,
                                                      h->tcell.p, h->tlo.p, h->thi.p, h->key.p,
                                                      h->id.p, h->n_valid.p);
     PBD_LAUNCH();
     PBD_TRY(radix_sort<uint32_t>(h->key.p, h->id.p, h->key_alt.p, h->id_alt.p, o->nt, nullptr,
                                  round8(h->key_bits), h->scr, s, &h->skey, &h->sid));
     k_bucket_ranges<<<kPersistentBlocks, 256, 0, s>>>(h->skey, h->sid, h->n_valid.p, h->tcell.p,
-                                                      h->bstart.p, h->bend.p, h->scell.p);
+                                                      h->tlo.p, h->thi.p, h->brange.p, h->blo.p,
+                                                      h->bhi.p, h->scell.p);
     PBD_LAUNCH();
     return PBD_OK;
 }
@@ -662,26 +661,15 @@ static int colli_alloc(pbd_colli *c) {
     PBD_TRY(c->cand.alloc(c->cand_cap));
     PBD_TRY(c->counters.alloc(8));
     size_t H = (size_t)c->contact_cap;
-    PBD_TRY(c->ckey.alloc(H));
-    PBD_TRY(c->ckey_alt.alloc(H));
-    PBD_TRY(c->cperm.alloc(H));
-    PBD_TRY(c->cperm_alt.alloc(H));
-    PBD_TRY(c->cids_raw.alloc(H));
     PBD_TRY(c->cids.alloc(H));
-    PBD_TRY(c->cface_raw.alloc(H));
     PBD_TRY(c->cface.alloc(H));
-    PBD_TRY(c->ctn_raw.alloc(H));
     PBD_TRY(c->ctn.alloc(H));
-    PBD_TRY(c->cw_raw.alloc(H));
     PBD_TRY(c->cw.alloc(H));
-    PBD_TRY(c->delta.alloc(4 * H));
-    PBD_TRY(c->ekey.alloc(4 * H));
-    PBD_TRY(c->ekey_alt.alloc(4 * H));
-    PBD_TRY(c->eval_.alloc(4 * H));
-    PBD_TRY(c->eval_alt.alloc(4 * H));
-    PBD_TRY(c->scr.hist.alloc(radix_hist_size(4 * (long long)H)));
-    PBD_TRY(c->scr.carry.alloc(256));
-    (void)o;
+    PBD_TRY(c->acc.alloc(3 * (size_t)o->n));
+    PBD_TRY(c->acnt.alloc(o->n));
+    PBD_CUDA(cudaMemsetAsync(c->acc.p, 0, sizeof(long long) * 3 * (size_t)o->n, o->stream));
+    PBD_CUDA(cudaMemsetAsync(c->acnt.p, 0, sizeof(int) * (size_t)o->n, o->stream));
+    PBD_CUDA(cudaMemsetAsync(c->counters.p, 0, sizeof(int) * 8, o->stream));
     return PBD_OK;
 }
 
@@ -698,38 +686,22 @@ int ccd_detect(pbd_colli *c) {
     PBD_TRY(shs_update(h));
     GridParams g = params_of(h);
     float th = c->thickness;
-    // per-axis reach of a hit: 2h off the plane + 3h inside the inflated
-    // triangle (barycentric epsilon = h / mean edge), with slack
+    // per-axis reach of a hit: 2h off the plane + 3h inside the triangle grown
+    // by the barycentric epsilon h / mean edge; Euclidean reach 3.61h; both
+    // with slack
     float margin = 5.5f * th + 2e-6f;
     float reach = 4.5f * th + 2e-6f;
-    // add the margin to the triangle AABBs (those not flagged as slivers)
-    // inside k_candidates by expanding the point AABB instead
-    (void)margin;
-    k_candidates<<<grid_for(o->n, 128), 128, 0, s>>>(
+    k_candidates<<<grid_for((long long)o->n * 32, 32 * kCandWarps), 32 * kCandWarps, 0, s>>>(
         o->n, g, margin, reach, o->tri.p, o->pt_tri_first.p, o->pt_tri_last.p, o->pt_tri.p,
         o->has_inst ? o->point_inst.p : nullptr, o->x.p, o->p.p, h->tcell.p, h->tlo.p, h->thi.p,
-        h->bstart.p, h->bend.p, h->scell.p, h->sid, c->cand.p, c->cand_cap, c->counters.p);
+        h->brange.p, h->blo.p, h->bhi.p, h->scell.p, h->sid, c->cand.p, c->cand_cap,
+        c->counters.p);
     PBD_LAUNCH();
     k_narrow<<<kPersistentBlocks, 128, 0, s>>>(c->cand.p, c->cand_cap, o->nt, th, o->tri.p, o->x.p,
-                                               o->p.p, c->counters.p, c->contact_cap, c->ckey.p,
-                                               c->cperm.p, c->cids_raw.p, c->cface_raw.p,
-                                               c->ctn_raw.p, c->cw_raw.p);
+                                               o->p.p, c->counters.p, c->contact_cap, c->cids.p,
+                                               c->cface.p, c->ctn.p, c->cw.p);
     k_clamp_counts<<<1, 32, 0, s>>>(c->counters.p, c->cand_cap, c->contact_cap);
     PBD_LAUNCH();
-    unsigned long long *sk;
-    int *sp;
-    int kb = round8(bits_for((long long)o->n * (long long)o->nt));
-    PBD_TRY(radix_sort<unsigned long long>(c->ckey.p, c->cperm.p, c->ckey_alt.p, c->cperm_alt.p,
-                                           c->contact_cap, c->counters.p + 1, kb, c->scr, s, &sk,
-                                           &sp));
-    k_gather_contacts<<<kPersistentBlocks, 256, 0, s>>>(c->counters.p, sp, c->cids_raw.p,
-                                                        c->cface_raw.p, c->ctn_raw.p, c->cw_raw.p,
-                                                        c->cids.p, c->cface.p, c->ctn.p, c->cw.p,
-                                                        c->ekey.p, c->eval_.p);
-    PBD_LAUNCH();
-    PBD_TRY(radix_sort<uint32_t>(c->ekey.p, c->eval_.p, c->ekey_alt.p, c->eval_alt.p,
-                                 4 * c->contact_cap, c->counters.p + 3, round8(bits_for(o->n)),
-                                 c->scr, s, &c->sekey, &c->seval));
     return PBD_OK;
 }
 
@@ -741,9 +713,9 @@ int ccd_resolve(pbd_colli *c, int passes) {
         k_contact_deltas<<<kPersistentBlocks, 128, 0, s>>>(c->counters.p, c->cids.p, o->x.p, o->p.p,
                                                            c->thickness,
                                                            c->response == PBD_RESPONSE_MASS_WEIGHTED,
-                                                           c->delta.p);
-        k_apply_deltas<<<kPersistentBlocks, 256, 0, s>>>(c->counters.p, c->sekey, c->seval,
-                                                         c->delta.p, o->p.p);
+                                                           c->acc.p, c->acnt.p);
+        k_apply_deltas<<<kPersistentBlocks, 256, 0, s>>>(c->counters.p, c->cids.p, c->acc.p,
+                                                         c->acnt.p, o->p.p);
         PBD_LAUNCH();
     }
     return PBD_OK;
@@ -767,12 +739,12 @@ static int shs_alloc(pbd_shs *h) {
     PBD_TRY(h->id_alt.alloc(nt));
     PBD_TRY(h->scell.alloc(nt));
     PBD_TRY(h->n_valid.alloc(1));
-    PBD_TRY(h->bstart.alloc((size_t)h->n_buckets + 1));
-    PBD_TRY(h->bend.alloc((size_t)h->n_buckets + 1));
+    PBD_TRY(h->brange.alloc((size_t)h->n_buckets + 1));
+    PBD_TRY(h->blo.alloc((size_t)h->n_buckets + 1));
+    PBD_TRY(h->bhi.alloc((size_t)h->n_buckets + 1));
     PBD_TRY(h->scr.hist.alloc(radix_hist_size((long long)nt)));
     PBD_TRY(h->scr.carry.alloc(256));
-    PBD_CUDA(cudaMemsetAsync(h->bstart.p, 0, sizeof(int) * (h->n_buckets + 1), o->stream));
-    PBD_CUDA(cudaMemsetAsync(h->bend.p, 0, sizeof(int) * (h->n_buckets + 1), o->stream));
+    PBD_CUDA(cudaMemsetAsync(h->brange.p, 0, sizeof(int2) * (h->n_buckets + 1), o->stream));
     PBD_CUDA(cudaMemsetAsync(h->n_valid.p, 0, sizeof(int), o->stream));
     h->skey = h->key.p;
     h->sid = h->id.p;
@@ -839,7 +811,7 @@ int pbd_shs_set_grid_size(pbd_shs *h, const int *size) {
     h->n_buckets = (int)ncell;
     h->key_bits = bits_for(ncell);
     h->initialized = false;
-    h->bstart.release();
+    h->brange.release();
     return PBD_OK;
 }
 
@@ -857,7 +829,7 @@ int pbd_shs_init(pbd_shs *h) {
         float shift = ((float)(unsigned)h->size[k] * h->cell[k]) / 2.0f;
         h->start[k] = h->center[k] - shift;
     }
-    if (!h->bstart.p || h->bstart.n < (size_t)h->n_buckets + 1) PBD_TRY(shs_alloc(h));
+    if (!h->brange.p || h->brange.n < (size_t)h->n_buckets + 1) PBD_TRY(shs_alloc(h));
     h->initialized = true;
     return shs_update(h);
 }
@@ -881,8 +853,8 @@ int pbd_shs_find_neighbors_all(pbd_shs *h, int *start_num, int *out, long long c
     PBD_TRY(off.alloc(nt));
     PBD_TRY(tot.alloc(1));
     GridParams g = params_of(h);
-    k_find_neighbors<<<grid_for(nt, 128), 128, 0, s>>>(nt, g, h->tcell.p, h->bstart.p, h->bend.p,
-                                                       h->scell.p, h->sid, nullptr, cnt.p, nullptr);
+    k_find_neighbors<<<grid_for(nt, 128), 128, 0, s>>>(nt, g, h->tcell.p, h->brange.p, h->scell.p,
+                                                       h->sid, nullptr, cnt.p, nullptr);
     PBD_LAUNCH();
     PBD_TRY(exclusive_scan(cnt.p, off.p, nt, tot.p, s));
     int t = 0;
@@ -903,9 +875,9 @@ int pbd_shs_find_neighbors_all(pbd_shs *h, int *start_num, int *out, long long c
         PBD_CHECK(cap >= t, PBD_ERR_OVERFLOW, "neighbor output needs %d entries", t);
         DBuf<int> dout;
         PBD_TRY(dout.alloc(t));
-        k_find_neighbors<<<grid_for(nt, 128), 128, 0, s>>>(nt, g, h->tcell.p, h->bstart.p,
-                                                           h->bend.p, h->scell.p, h->sid, off.p,
-                                                           nullptr, dout.p);
+        k_find_neighbors<<<grid_for(nt, 128), 128, 0, s>>>(nt, g, h->tcell.p, h->brange.p,
+                                                           h->scell.p, h->sid, off.p, nullptr,
+                                                           dout.p);
         PBD_LAUNCH();
         PBD_CUDA(cudaMemcpyAsync(out, dout.p, sizeof(int) * t, cudaMemcpyDeviceToHost, s));
         PBD_CUDA(cudaStreamSynchronize(s));
@@ -969,6 +941,7 @@ int pbd_colli_set_capacity(pbd_colli *c, long long cand, long long contacts) {
     c->cand_cap = cand;
     c->contact_cap = contacts;
     c->cand.release();
+    c->cids.release();
     return PBD_OK;
 }
 
@@ -999,34 +972,43 @@ int pbd_colli_get_contacts(pbd_colli *c, int *ids, int *face, float *t, double *
     PBD_CUDA(cudaStreamSynchronize(s));
     long long h = hc[1];
     *count = h;
-    long long m = std::min(h, cap);
-    if (m <= 0) return PBD_OK;
-    std::vector<int4> hi(m);
-    std::vector<float4> htn(m);
-    std::vector<double4> hw(m);
-    PBD_CUDA(cudaMemcpyAsync(hi.data(), c->cids.p, sizeof(int4) * m, cudaMemcpyDeviceToHost, s));
-    PBD_CUDA(cudaMemcpyAsync(htn.data(), c->ctn.p, sizeof(float4) * m, cudaMemcpyDeviceToHost, s));
-    PBD_CUDA(cudaMemcpyAsync(hw.data(), c->cw.p, sizeof(double4) * m, cudaMemcpyDeviceToHost, s));
-    if (face) PBD_CUDA(cudaMemcpyAsync(face, c->cface.p, sizeof(int) * m, cudaMemcpyDeviceToHost, s));
+    if (h <= 0 || cap <= 0) return PBD_OK;
+    std::vector<int4> hi(h);
+    std::vector<int> hf(h);
+    std::vector<float4> htn(h);
+    std::vector<double4> hw(h);
+    PBD_CUDA(cudaMemcpyAsync(hi.data(), c->cids.p, sizeof(int4) * h, cudaMemcpyDeviceToHost, s));
+    PBD_CUDA(cudaMemcpyAsync(hf.data(), c->cface.p, sizeof(int) * h, cudaMemcpyDeviceToHost, s));
+    PBD_CUDA(cudaMemcpyAsync(htn.data(), c->ctn.p, sizeof(float4) * h, cudaMemcpyDeviceToHost, s));
+    PBD_CUDA(cudaMemcpyAsync(hw.data(), c->cw.p, sizeof(double4) * h, cudaMemcpyDeviceToHost, s));
     PBD_CUDA(cudaStreamSynchronize(s));
-    for (long long i = 0; i < m; ++i) {
+    // order by (point, face triangle)
+    std::vector<long long> order(h);
+    for (long long i = 0; i < h; ++i) order[i] = i;
+    std::sort(order.begin(), order.end(), [&](long long a, long long b) {
+        return hi[a].x != hi[b].x ? hi[a].x < hi[b].x : hf[a] < hf[b];
+    });
+    long long m = std::min(h, cap);
+    for (long long k = 0; k < m; ++k) {
+        long long i = order[k];
         if (ids) {
-            ids[4 * i] = hi[i].x;
-            ids[4 * i + 1] = hi[i].y;
-            ids[4 * i + 2] = hi[i].z;
-            ids[4 * i + 3] = hi[i].w;
+            ids[4 * k] = hi[i].x;
+            ids[4 * k + 1] = hi[i].y;
+            ids[4 * k + 2] = hi[i].z;
+            ids[4 * k + 3] = hi[i].w;
         }
-        if (t) t[i] = htn[i].x;
+        if (face) face[k] = hf[i];
+        if (t) t[k] = htn[i].x;
         if (n) {
-            n[3 * i] = htn[i].y;
-            n[3 * i + 1] = htn[i].z;
-            n[3 * i + 2] = htn[i].w;
+            n[3 * k] = htn[i].y;
+            n[3 * k + 1] = htn[i].z;
+            n[3 * k + 2] = htn[i].w;
         }
         if (w) {
-            w[4 * i] = hw[i].x;
-            w[4 * i + 1] = hw[i].y;
-            w[4 * i + 2] = hw[i].z;
-            w[4 * i + 3] = hw[i].w;
+            w[4 * k] = hw[i].x;
+            w[4 * k + 1] = hw[i].y;
+            w[4 * k + 2] = hw[i].z;
+            w[4 * k + 3] = hw[i].w;
         }
     }
     return PBD_OK;

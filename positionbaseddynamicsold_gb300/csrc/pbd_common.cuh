@@ -169,11 +169,9 @@ struct pbd_shs {
     uint32_t *skey = nullptr;    // sorted result pointers (into key/key_alt)
     int *sid = nullptr;
     pbd::DBuf<int4> scell;       // cell of sorted entry
-    pbd::DBuf<int> bstart, bend; // bucket -> [start, end) in sorted order
+    pbd::DBuf<int2> brange;      // bucket -> [start, end) in sorted order
+    pbd::DBuf<float4> blo, bhi;  // bucket -> union of its triangles' swept AABBs
     pbd::DBuf<int> n_valid;
-    bool table_clean = false;
-    pbd::DBuf<uint32_t> prev_keys;
-    pbd::DBuf<int> n_prev;
     pbd::SortScratch scr;
 };
 
@@ -187,21 +185,16 @@ struct pbd_colli {
     long long contact_cap = 1 << 20;
     // candidates (point, triangle)
     pbd::DBuf<int2> cand;
-    pbd::DBuf<int> counters;    // [0] candidates, [1] contacts, [2] overflow, [3] entries
-    // contacts (unsorted, then sorted)
-    pbd::DBuf<unsigned long long> ckey, ckey_alt;
-    pbd::DBuf<int> cperm, cperm_alt;
-    pbd::DBuf<int4> cids_raw, cids;     // i0..i3
-    pbd::DBuf<int> cface_raw, cface;
-    pbd::DBuf<float4> ctn_raw, ctn;     // t, n
-    pbd::DBuf<double4> cw_raw, cw;
-    // response
-    pbd::DBuf<float4> delta;            // 4 per contact, w = active
-    pbd::DBuf<uint32_t> ekey, ekey_alt; // point id per entry
-    pbd::DBuf<int> eval_, eval_alt;
-    uint32_t *sekey = nullptr;
-    int *seval = nullptr;
-    pbd::SortScratch scr;
+    pbd::DBuf<int> counters;    // [0] candidates, [1] contacts, [2] overflow flags
+    // contacts, in the order the narrow phase found them
+    pbd::DBuf<int4> cids;               // i0..i3
+    pbd::DBuf<int> cface;
+    pbd::DBuf<float4> ctn;              // t, n
+    pbd::DBuf<double4> cw;
+    // response: per-point 2^-32 m fixed-point sums and counts (kept zero
+    // between passes)
+    pbd::DBuf<long long> acc;
+    pbd::DBuf<int> acnt;
 };
 
 struct pbd_solver {

@@ -92,7 +92,8 @@ def test_resolve_matches_oracle(orc, golden, mw):
 
 def test_resolve_reference_split_when_contacts_disjoint(orc, golden):
     """With vertex-disjoint contacts the Jacobi response is the reference's
-    sequential CollisionResolveNew."""
+    sequential CollisionResolveNew, up to the 2^-32 m quantisation of the
+    fixed-point sums (below one float ulp of the positions here)."""
     g = golden("ccd")
     obj, cs = ccd_gpu(g, iterations=1)
     ids = cs.contacts()["ids"]
@@ -104,7 +105,8 @@ def test_resolve_reference_split_when_contacts_disjoint(orc, golden):
     sub = ids[keep]
     seq = orc.resolve_ref(sub, g["pos"], g["prdp"], 1, float(g["thickness"]))
     jac = orc.resolve_jacobi(sub, g["pos"], g["prdp"], None, 1, float(g["thickness"]), 0)
-    np.testing.assert_array_equal(seq, jac)
+    assert len(sub) > 10
+    assert np.abs(seq - jac).max() <= 1e-7
 
 
 def drape_small(seed=0):
