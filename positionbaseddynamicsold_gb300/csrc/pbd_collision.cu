@@ -8,16 +8,17 @@
 //   2. stable radix sort of (bucket, triangle id) and a bucket -> [start, end)
 //      table (the reference's cellStart/cellEnd, reset each update) plus the
 //      union of the swept AABBs of each bucket's triangles;
-//   3. one warp per point, one lane per cell of the union of the 27-cell
-//      neighbourhoods of the centroid cells of its incident triangles
+//   3. cell tasks: one warp per point, one lane per cell of the union of the
+//      27-cell neighbourhoods of the centroid cells of its incident triangles
 //      (CCD_SH_Extended, P/CCD.cpp:1541-1586, tests every (point, neighbour)
 //      pair; the union holds each distinct pair once); a cell whose bucket
-//      AABB misses the point's grown swept AABB is skipped; per entry an
-//      exact-cell check, then two conservative FP32 filters that cannot
-//      reject a pair the ExtendedVFTest would accept (swept-AABB overlap with
-//      margin 5.5 h and a lower bound on the point-triangle distance over the
-//      step); survivors are appended with one atomic per group of lanes.
-// Narrowphase: one thread per surviving pair runs ExtendedVFTest
+//      AABB misses the point's grown swept AABB yields no task;
+//   4. one thread per task scans the bucket's entries (sorted-order copies of
+//      cell and AABB): exact-cell check and swept-AABB overlap with margin
+//      5.5 h; survivors become candidate pairs (one atomic per lane group).
+// Narrowphase: one thread per candidate first applies a lower bound on the
+// point-triangle distance over the step (reject if above 4.5 h; a hit needs
+// it below 3.61 h), then runs ExtendedVFTest
 // (P/CCD.cpp:1733-1808) with the reference's arithmetic: float triple
 // products widened to double, the double cubic solve (P/CCD.cpp:48-113), the
 // float barycentric inside test.  Contacts are kept in discovery order on the
@@ -32,6 +33,7 @@
 #include <cooperative_groups.h>
 
 #include <algorithm>
+#include <climits>
 #include <cmath>
 #include <cstring>
 
@@ -325,11 +327,16 @@ __global__ void __launch_bounds__(256) k_tri_cells(int nt, GridParams g, float m
 
 __global__ void k_bucket_ranges(const uint32_t *skey, const int *sid, const int *n_valid,
                                 const int4 *tcell, const float4 *tlo, const float4 *thi,
-                                int2 *brange, float4 *blo, float4 *bhi, int4 *scell) {
+                                int2 *brange, float4 *blo, float4 *bhi, int4 *scell,
+                                float4 *slo, float4 *shi) {
     int n = *n_valid;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         uint32_t k = skey[i];
-        scell[i] = tcell[sid[i]];
+        int t = sid[i];
+        int4 c = tcell[t];
+        scell[i] = make_int4(c.x, c.y, c.z, t);  // w = triangle id
+        slo[i] = tlo[t];
+        shi[i] = thi[t];
         if (i > 0 && skey[i - 1] == k) continue;
         float4 lo = tlo[sid[i]], hi = thi[sid[i]];
         int e = i + 1;
@@ -363,7 +370,7 @@ __global__ void k_find_neighbors(int nt, GridParams g, const int4 *tcell, const 
                     for (int i = r.x; i < r.y; ++i) {
                         int4 sc = scell[i];
                         if (sc.x != nx || sc.y != ny || sc.z != nz) continue;
-                        int id = sid[i];
+                        int id = sc.w;
                         if (id == t) continue;
                         if (out) out[o + k] = id;
                         ++k;
@@ -373,17 +380,17 @@ __global__ void k_find_neighbors(int nt, GridParams g, const int4 *tcell, const 
     if (cnt) cnt[t] = k;
 }
 
-// candidate pairs: one warp per point, lanes over the candidate cells
-constexpr int kCandWarps = 4;
-__global__ void __launch_bounds__(32 * kCandWarps) k_candidates(
-    int n, GridParams g, float margin, float reach, const int4 *__restrict__ tri,
-    const int *__restrict__ pt_first, const int *__restrict__ pt_last,
-    const int *__restrict__ pt_tri, const int *__restrict__ point_inst,
+// stage 1 of the candidate search: one warp per point, one lane per cell of
+// the union of the 27-cell neighbourhoods of its incident triangles' centroid
+// cells; a task (point, bucket, cell) is emitted for every such cell whose
+// bucket is non-empty and whose bucket AABB meets the point's grown swept AABB
+constexpr int kTaskWarps = 8;
+__global__ void __launch_bounds__(32 * kTaskWarps) k_cell_tasks(
+    int n, GridParams g, float margin, const int *__restrict__ pt_first,
+    const int *__restrict__ pt_last, const int *__restrict__ pt_tri,
     const float4 *__restrict__ x, const float4 *__restrict__ p, const int4 *__restrict__ tcell,
-    const float4 *__restrict__ tlo, const float4 *__restrict__ thi,
     const int2 *__restrict__ brange, const float4 *__restrict__ blo,
-    const float4 *__restrict__ bhi, const int4 *__restrict__ scell, const int *__restrict__ sid,
-    int2 *cand, long long cap, int *counters) {
+    const float4 *__restrict__ bhi, int4 *tasks, int *tcell_z, long long cap, int *counters) {
     const int lane = threadIdx.x & 31;
     const int warp0 = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int nwarps = (gridDim.x * blockDim.x) >> 5;
@@ -402,45 +409,38 @@ __global__ void __launch_bounds__(32 * kCandWarps) k_candidates(
         }
         unsigned vm = __ballot_sync(0xffffffffu, valid);
         if (!vm) continue;
-        // the incident centroid cells, broadcast to every lane
-        int cx[kMaxInc], cy[kMaxInc], cz[kMaxInc];
-        int nc = 0;
-        int lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
+        // bbox of the valid incident cells (warp min/max)
+        int lx = valid ? mc.x : INT_MAX, ly = valid ? mc.y : INT_MAX, lz = valid ? mc.z : INT_MAX;
+        int hx = valid ? mc.x : INT_MIN, hy = valid ? mc.y : INT_MIN, hz = valid ? mc.z : INT_MIN;
 #pragma unroll
-        for (int i = 0; i < kMaxInc; ++i) {
-            int src = __ffs(vm) - 1;
-            int x_ = __shfl_sync(0xffffffffu, mc.x, src < 0 ? 0 : src);
-            int y_ = __shfl_sync(0xffffffffu, mc.y, src < 0 ? 0 : src);
-            int z_ = __shfl_sync(0xffffffffu, mc.z, src < 0 ? 0 : src);
-            if (src >= 0) {
-                cx[nc] = x_; cy[nc] = y_; cz[nc] = z_;
-                if (nc == 0) {
-                    lo[0] = hi[0] = x_; lo[1] = hi[1] = y_; lo[2] = hi[2] = z_;
-                } else {
-                    lo[0] = min(lo[0], x_); hi[0] = max(hi[0], x_);
-                    lo[1] = min(lo[1], y_); hi[1] = max(hi[1], y_);
-                    lo[2] = min(lo[2], z_); hi[2] = max(hi[2], z_);
-                }
-                ++nc;
-                vm &= vm - 1;
-            }
+        for (int o = 16; o > 0; o >>= 1) {
+            lx = min(lx, __shfl_xor_sync(0xffffffffu, lx, o));
+            ly = min(ly, __shfl_xor_sync(0xffffffffu, ly, o));
+            lz = min(lz, __shfl_xor_sync(0xffffffffu, lz, o));
+            hx = max(hx, __shfl_xor_sync(0xffffffffu, hx, o));
+            hy = max(hy, __shfl_xor_sync(0xffffffffu, hy, o));
+            hz = max(hz, __shfl_xor_sync(0xffffffffu, hz, o));
         }
         v3 X0 = ld3(x[v]), P0 = ld3(p[v]);
-        v3 D0 = sub3(P0, X0);
-        // swept AABB of the point, grown by the per-axis reach of a hit
         float plx = fminf(X0.x, P0.x) - margin, phx = fmaxf(X0.x, P0.x) + margin;
         float ply = fminf(X0.y, P0.y) - margin, phy = fmaxf(X0.y, P0.y) + margin;
         float plz = fminf(X0.z, P0.z) - margin, phz = fmaxf(X0.z, P0.z) + margin;
-        int inst = point_inst ? point_inst[v] : 0;
-        int ex = hi[0] - lo[0] + 3, ey = hi[1] - lo[1] + 3, ez = hi[2] - lo[2] + 3;
+        int ex = hx - lx + 3, ey = hy - ly + 3, ez = hz - lz + 3;
         int ncell = ex * ey * ez;
         for (int ci = lane; ci < ncell; ci += 32) {
-            int xx = lo[0] - 1 + ci % ex;
-            int y = lo[1] - 1 + (ci / ex) % ey;
-            int z = lo[2] - 1 + ci / (ex * ey);
+            int xx = lx - 1 + ci % ex;
+            int y = ly - 1 + (ci / ex) % ey;
+            int z = lz - 1 + ci / (ex * ey);
+            // near: within one cell of some valid incident cell
             bool near = false;
-            for (int i = 0; i < nc; ++i)
-                near |= abs(cx[i] - xx) <= 1 && abs(cy[i] - y) <= 1 && abs(cz[i] - z) <= 1;
+            unsigned m = vm;
+            while (m) {
+                int src = __ffs(m) - 1;
+                m &= m - 1;
+                // the incident cells are held by lanes < ninc; read them by index
+                int4 c = tcell[pt_tri[f0 + src]];
+                near |= abs(c.x - xx) <= 1 && abs(c.y - y) <= 1 && abs(c.z - z) <= 1;
+            }
             if (!near) continue;
             if (!g.hashed && outside(g, xx, y, z)) continue;
             uint32_t b = bucket_of(g, xx, y, z);
@@ -449,40 +449,58 @@ __global__ void __launch_bounds__(32 * kCandWarps) k_candidates(
             float4 bl = blo[b], bh = bhi[b];
             if (plx > bh.x || phx < bl.x || ply > bh.y || phy < bl.y || plz > bh.z || phz < bl.z)
                 continue;
-            for (int e = r.x; e < r.y; ++e) {
-                int4 sc = scell[e];
-                if (sc.x != xx || sc.y != y || sc.z != z) continue;
-                if (point_inst && sc.w != inst) continue;
-                int f = sid[e];
-                float4 tl = tlo[f], th = thi[f];
-                if (plx > th.x || phx < tl.x || ply > th.y || phy < tl.y || plz > th.z ||
-                    phz < tl.z)
-                    continue;
-                int4 fi = tri[f];
-                if (fi.x == v || fi.y == v || fi.z == v) continue;
-                if (tl.w == 0.f) {
-                    // lower bound of the point-triangle distance over the step
-                    v3 xa = ld3(x[fi.x]), xb = ld3(x[fi.y]), xc = ld3(x[fi.z]);
-                    v3 pa = ld3(p[fi.x]), pb = ld3(p[fi.y]), pc = ld3(p[fi.z]);
-                    float d0 = point_tri_dist(X0, xa, xb, xc);
-                    float d1 = point_tri_dist(P0, pa, pb, pc);
-                    v3 ua = sub3(sub3(pa, xa), D0), ub = sub3(sub3(pb, xb), D0),
-                       uc = sub3(sub3(pc, xc), D0);
-                    float U = sqrtf(fmaxf(fmaxf(dot3(ua, ua), dot3(ub, ub)), dot3(uc, uc)));
-                    if ((d0 + d1 - U) * 0.5f > reach) continue;
-                }
-                long long slot = agg_inc(counters);
-                if (slot < cap)
-                    cand[slot] = make_int2(v, f);
-                else
-                    atomicOr(counters + 2, 1);
+            int slot = agg_inc(counters + 3);
+            if (slot < cap) {
+                tasks[slot] = make_int4(v, (int)b, xx, y);
+                tcell_z[slot] = z;
+            } else {
+                atomicOr(counters + 2, 8);
             }
         }
     }
 }
 
+// stage 2: one thread per task scans the bucket's entries (sorted-order
+// copies of cell and AABB, independent loads) and emits (point, triangle)
+// pairs whose cell is the task's and whose swept AABBs meet
+__global__ void __launch_bounds__(256) k_task_entries(
+    const int4 *__restrict__ tasks, const int *__restrict__ tcell_z, long long tcap,
+    float margin, const int *__restrict__ point_inst, const int *__restrict__ tri_inst4,
+    const float4 *__restrict__ x, const float4 *__restrict__ p, const int2 *__restrict__ brange,
+    const int4 *__restrict__ scell, const float4 *__restrict__ slo,
+    const float4 *__restrict__ shi, int2 *cand, long long cap, int *counters) {
+    long long nt = counters[3];
+    if (nt > tcap) nt = tcap;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < nt;
+         i += (long long)gridDim.x * blockDim.x) {
+        int4 tk = tasks[i];
+        int z = tcell_z[i];
+        int v = tk.x;
+        v3 X0 = ld3(x[v]), P0 = ld3(p[v]);
+        float plx = fminf(X0.x, P0.x) - margin, phx = fmaxf(X0.x, P0.x) + margin;
+        float ply = fminf(X0.y, P0.y) - margin, phy = fmaxf(X0.y, P0.y) + margin;
+        float plz = fminf(X0.z, P0.z) - margin, phz = fmaxf(X0.z, P0.z) + margin;
+        int inst = point_inst ? point_inst[v] : 0;
+        int2 r = brange[tk.y];
+        for (int e = r.x; e < r.y; ++e) {
+            int4 sc = scell[e];
+            float4 tl = slo[e], th = shi[e];
+            if (sc.x != tk.z || sc.y != tk.w || sc.z != z) continue;
+            if (plx > th.x || phx < tl.x || ply > th.y || phy < tl.y || plz > th.z || phz < tl.z)
+                continue;
+            if (point_inst && tri_inst4[sc.w] != inst) continue;
+            long long slot = agg_inc(counters);
+            if (slot < cap)
+                cand[slot] = make_int2(v, sc.w);
+            else
+                atomicOr(counters + 2, 1);
+        }
+    }
+}
+
 __global__ void __launch_bounds__(128) k_narrow(const int2 *__restrict__ cand, long long cap,
-                                                int nt, float th, const int4 *__restrict__ tri,
+                                                int nt, float th, float reach,
+                                                const int4 *__restrict__ tri,
                                                 const float4 *__restrict__ x,
                                                 const float4 *__restrict__ p, int *counters,
                                                 long long ccap, int4 *cids, int *cface,
@@ -493,8 +511,19 @@ __global__ void __launch_bounds__(128) k_narrow(const int2 *__restrict__ cand, l
          i += (long long)gridDim.x * blockDim.x) {
         int2 c = cand[i];
         int4 f = tri[c.y];
+        if (f.x == c.x || f.y == c.x || f.z == c.x) continue;
         v3 X[4] = {ld3(x[c.x]), ld3(x[f.x]), ld3(x[f.y]), ld3(x[f.z])};
         v3 P[4] = {ld3(p[c.x]), ld3(p[f.x]), ld3(p[f.y]), ld3(p[f.z])};
+        if (!sliver(X[1], X[2], X[3]) && !sliver(P[1], P[2], P[3])) {
+            // lower bound of the point-triangle distance over the step
+            v3 D0 = sub3(P[0], X[0]);
+            float d0 = point_tri_dist(X[0], X[1], X[2], X[3]);
+            float d1 = point_tri_dist(P[0], P[1], P[2], P[3]);
+            v3 ua = sub3(sub3(P[1], X[1]), D0), ub = sub3(sub3(P[2], X[2]), D0),
+               uc = sub3(sub3(P[3], X[3]), D0);
+            float U = sqrtf(fmaxf(fmaxf(dot3(ua, ua), dot3(ub, ub)), dot3(uc, uc)));
+            if ((d0 + d1 - U) * 0.5f > reach) continue;
+        }
         VFResult r;
         if (!extended_vf_test(X, P, th, r)) continue;
         int slot = agg_inc(counters + 1);
@@ -651,7 +680,7 @@ int shs_update(pbd_shs *h) {
                                  round8(h->key_bits), h->scr, s, &h->skey, &h->sid));
     k_bucket_ranges<<<kPersistentBlocks, 256, 0, s>>>(h->skey, h->sid, h->n_valid.p, h->tcell.p,
                                                       h->tlo.p, h->thi.p, h->brange.p, h->blo.p,
-                                                      h->bhi.p, h->scell.p);
+                                                      h->bhi.p, h->scell.p, h->slo.p, h->shi.p);
     PBD_LAUNCH();
     return PBD_OK;
 }
@@ -659,6 +688,8 @@ int shs_update(pbd_shs *h) {
 static int colli_alloc(pbd_colli *c) {
     pbd_object *o = c->obj;
     PBD_TRY(c->cand.alloc(c->cand_cap));
+    PBD_TRY(c->tasks.alloc(c->task_cap));
+    PBD_TRY(c->tasks_z.alloc(c->task_cap));
     PBD_TRY(c->counters.alloc(8));
     size_t H = (size_t)c->contact_cap;
     PBD_TRY(c->cids.alloc(H));
@@ -691,15 +722,19 @@ int ccd_detect(pbd_colli *c) {
     // with slack
     float margin = 5.5f * th + 2e-6f;
     float reach = 4.5f * th + 2e-6f;
-    k_candidates<<<grid_for((long long)o->n * 32, 32 * kCandWarps), 32 * kCandWarps, 0, s>>>(
-        o->n, g, margin, reach, o->tri.p, o->pt_tri_first.p, o->pt_tri_last.p, o->pt_tri.p,
-        o->has_inst ? o->point_inst.p : nullptr, o->x.p, o->p.p, h->tcell.p, h->tlo.p, h->thi.p,
-        h->brange.p, h->blo.p, h->bhi.p, h->scell.p, h->sid, c->cand.p, c->cand_cap,
+    k_cell_tasks<<<grid_for((long long)o->n * 32, 32 * kTaskWarps), 32 * kTaskWarps, 0, s>>>(
+        o->n, g, margin, o->pt_tri_first.p, o->pt_tri_last.p, o->pt_tri.p, o->x.p, o->p.p,
+        h->tcell.p, h->brange.p, h->blo.p, h->bhi.p, c->tasks.p, c->tasks_z.p, c->task_cap,
         c->counters.p);
     PBD_LAUNCH();
-    k_narrow<<<kPersistentBlocks, 128, 0, s>>>(c->cand.p, c->cand_cap, o->nt, th, o->tri.p, o->x.p,
-                                               o->p.p, c->counters.p, c->contact_cap, c->cids.p,
-                                               c->cface.p, c->ctn.p, c->cw.p);
+    k_task_entries<<<kPersistentBlocks, 256, 0, s>>>(
+        c->tasks.p, c->tasks_z.p, c->task_cap, margin, o->has_inst ? o->point_inst.p : nullptr,
+        o->has_inst ? o->tri_inst.p : nullptr, o->x.p, o->p.p, h->brange.p, h->scell.p,
+        h->slo.p, h->shi.p, c->cand.p, c->cand_cap, c->counters.p);
+    PBD_LAUNCH();
+    k_narrow<<<kPersistentBlocks, 128, 0, s>>>(c->cand.p, c->cand_cap, o->nt, th, reach, o->tri.p,
+                                               o->x.p, o->p.p, c->counters.p, c->contact_cap,
+                                               c->cids.p, c->cface.p, c->ctn.p, c->cw.p);
     k_clamp_counts<<<1, 32, 0, s>>>(c->counters.p, c->cand_cap, c->contact_cap);
     PBD_LAUNCH();
     return PBD_OK;
@@ -738,6 +773,8 @@ static int shs_alloc(pbd_shs *h) {
     PBD_TRY(h->id.alloc(nt));
     PBD_TRY(h->id_alt.alloc(nt));
     PBD_TRY(h->scell.alloc(nt));
+    PBD_TRY(h->slo.alloc(nt));
+    PBD_TRY(h->shi.alloc(nt));
     PBD_TRY(h->n_valid.alloc(1));
     PBD_TRY(h->brange.alloc((size_t)h->n_buckets + 1));
     PBD_TRY(h->blo.alloc((size_t)h->n_buckets + 1));
@@ -940,6 +977,7 @@ int pbd_colli_set_capacity(pbd_colli *c, long long cand, long long contacts) {
               PBD_ERR_ARG, "bad capacity");
     c->cand_cap = cand;
     c->contact_cap = contacts;
+    c->task_cap = cand;
     c->cand.release();
     c->cids.release();
     return PBD_OK;

@@ -118,7 +118,7 @@ struct pbd_object {
     // meshTopol triangles: (i0, i1, i2, instance)
     pbd::DBuf<int4> tri;
     pbd::DBuf<int> pt_tri_first, pt_tri_last, pt_tri;  // point -> incident triangles
-    pbd::DBuf<int> point_inst;
+    pbd::DBuf<int> point_inst, tri_inst;
     // constraint buffers by prim id
     pbd::DBuf<int2> prim_list;
     pbd::DBuf<int> indices, ctype;
@@ -168,7 +168,8 @@ struct pbd_shs {
     pbd::DBuf<int> id, id_alt;
     uint32_t *skey = nullptr;    // sorted result pointers (into key/key_alt)
     int *sid = nullptr;
-    pbd::DBuf<int4> scell;       // cell of sorted entry
+    pbd::DBuf<int4> scell;       // cell of sorted entry, w = triangle id
+    pbd::DBuf<float4> slo, shi;  // swept AABB of sorted entry
     pbd::DBuf<int2> brange;      // bucket -> [start, end) in sorted order
     pbd::DBuf<float4> blo, bhi;  // bucket -> union of its triangles' swept AABBs
     pbd::DBuf<int> n_valid;
@@ -183,9 +184,12 @@ struct pbd_colli {
     int response = PBD_RESPONSE_REFERENCE;
     long long cand_cap = 1 << 22;
     long long contact_cap = 1 << 20;
-    // candidates (point, triangle)
+    long long task_cap = 1 << 22;
+    // cell tasks (point, bucket, cell) and candidates (point, triangle)
+    pbd::DBuf<int4> tasks;
+    pbd::DBuf<int> tasks_z;
     pbd::DBuf<int2> cand;
-    pbd::DBuf<int> counters;    // [0] candidates, [1] contacts, [2] overflow flags
+    pbd::DBuf<int> counters;    // [0] candidates, [1] contacts, [2] overflow flags, [3] tasks
     // contacts, in the order the narrow phase found them
     pbd::DBuf<int4> cids;               // i0..i3
     pbd::DBuf<int> cface;

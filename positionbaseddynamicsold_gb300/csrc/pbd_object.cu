@@ -615,6 +615,12 @@ int pbd_object_create(const pbd_object_desc *d, pbd_object **out) {
     }
     o->has_inst = d->point_inst != nullptr;
     if (d->point_inst && (r = o->point_inst.upload(d->point_inst, o->n, s))) return fail(r);
+    if (d->point_inst) {
+        std::vector<int> ti(o->nt, 0);
+        if (d->tri_inst) ti.assign(d->tri_inst, d->tri_inst + o->nt);
+        if ((r = o->tri_inst.upload(ti.data(), o->nt, s))) return fail(r);
+        if (cudaStreamSynchronize(s) != cudaSuccess) return fail(PBD_ERR_CUDA);
+    }
     // constraint buffers
     if (o->np) {
         if ((r = o->prim_list.upload((const int2 *)d->prim_list, o->np, s)) ||
