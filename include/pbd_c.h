@@ -158,6 +158,17 @@ int pbd_solver_set_ground(pbd_solver *s, int enable, float height);
 int pbd_solver_step(pbd_solver *s, float dt, int substeps, int iterations, pbd_colli *colli,
                     int use_graph);
 
+/* How a Gauss-Seidel sweep runs: PBD_GS_PER_COLOR launches one kernel per
+ * color (any size); PBD_GS_CLUSTER keeps every point in the distributed
+ * shared memory of one 16-block thread-block cluster (objects up to 131,072
+ * points) and separates colors by cluster barriers; PBD_GS_AUTO (default)
+ * uses the cluster form when the object fits.  Both give identical results.
+ * No reference counterpart. */
+enum { PBD_GS_AUTO = 0, PBD_GS_PER_COLOR = 1, PBD_GS_CLUSTER = 2 };
+int pbd_solver_set_gs_path(pbd_solver *s, int path);
+/* the form the next sweep will use (PBD_GS_PER_COLOR or PBD_GS_CLUSTER) */
+int pbd_solver_get_gs_path(pbd_solver *s, int *path);
+
 /* kernel launches recorded in the cached pbd_solver_step graph (no
  * reference counterpart; used to report launches per step) */
 int pbd_solver_graph_kernels(pbd_solver *s, long long *n);

@@ -14,11 +14,12 @@
 //      pair; the union holds each distinct pair once); a cell whose bucket
 //      AABB misses the point's grown swept AABB yields no task;
 //   4. one thread per task scans the bucket's entries (sorted-order copies of
-//      cell and AABB): exact-cell check and swept-AABB overlap with margin
-//      5.5 h; survivors become candidate pairs (one atomic per lane group).
-// Narrowphase: one thread per candidate first applies a lower bound on the
-// point-triangle distance over the step (reject if above 4.5 h; a hit needs
-// it below 3.61 h), then runs ExtendedVFTest
+//      cell and AABB): exact-cell check, swept-AABB overlap with margin 5.5 h,
+//      then a lower bound on the point-triangle distance over the step
+//      (reject above 4.5 h; a hit needs it below 3.61 h); survivors become
+//      candidate pairs (one atomic per lane group).  Neither filter can
+//      reject a pair ExtendedVFTest would accept.
+// Narrowphase: one thread per candidate runs ExtendedVFTest
 // (P/CCD.cpp:1733-1808) with the reference's arithmetic: float triple
 // products widened to double, the double cubic solve (P/CCD.cpp:48-113), the
 // float barycentric inside test.  Contacts are kept in discovery order on the
@@ -465,7 +466,8 @@ __global__ void __launch_bounds__(32 * kTaskWarps) k_cell_tasks(
 // pairs whose cell is the task's and whose swept AABBs meet
 __global__ void __launch_bounds__(256) k_task_entries(
     const int4 *__restrict__ tasks, const int *__restrict__ tcell_z, long long tcap,
-    float margin, const int *__restrict__ point_inst, const int *__restrict__ tri_inst4,
+    float margin, float reach, const int4 *__restrict__ tri,
+    const int *__restrict__ point_inst, const int *__restrict__ tri_inst4,
     const float4 *__restrict__ x, const float4 *__restrict__ p, const int2 *__restrict__ brange,
     const int4 *__restrict__ scell, const float4 *__restrict__ slo,
     const float4 *__restrict__ shi, int2 *cand, long long cap, int *counters) {
@@ -489,6 +491,20 @@ __global__ void __launch_bounds__(256) k_task_entries(
             if (plx > th.x || phx < tl.x || ply > th.y || phy < tl.y || plz > th.z || phz < tl.z)
                 continue;
             if (point_inst && tri_inst4[sc.w] != inst) continue;
+            int4 fi = tri[sc.w];
+            if (fi.x == v || fi.y == v || fi.z == v) continue;
+            v3 xa = ld3(x[fi.x]), xb = ld3(x[fi.y]), xc = ld3(x[fi.z]);
+            v3 pa = ld3(p[fi.x]), pb = ld3(p[fi.y]), pc = ld3(p[fi.z]);
+            if (!sliver(xa, xb, xc) && !sliver(pa, pb, pc)) {
+                // lower bound of the point-triangle distance over the step
+                v3 D0 = sub3(P0, X0);
+                float d0 = point_tri_dist(X0, xa, xb, xc);
+                float d1 = point_tri_dist(P0, pa, pb, pc);
+                v3 ua = sub3(sub3(pa, xa), D0), ub = sub3(sub3(pb, xb), D0),
+                   uc = sub3(sub3(pc, xc), D0);
+                float U = sqrtf(fmaxf(fmaxf(dot3(ua, ua), dot3(ub, ub)), dot3(uc, uc)));
+                if ((d0 + d1 - U) * 0.5f > reach) continue;
+            }
             long long slot = agg_inc(counters);
             if (slot < cap)
                 cand[slot] = make_int2(v, sc.w);
@@ -499,7 +515,7 @@ __global__ void __launch_bounds__(256) k_task_entries(
 }
 
 __global__ void __launch_bounds__(128) k_narrow(const int2 *__restrict__ cand, long long cap,
-                                                int nt, float th, float reach,
+                                                int nt, float th,
                                                 const int4 *__restrict__ tri,
                                                 const float4 *__restrict__ x,
                                                 const float4 *__restrict__ p, int *counters,
@@ -511,19 +527,8 @@ __global__ void __launch_bounds__(128) k_narrow(const int2 *__restrict__ cand, l
          i += (long long)gridDim.x * blockDim.x) {
         int2 c = cand[i];
         int4 f = tri[c.y];
-        if (f.x == c.x || f.y == c.x || f.z == c.x) continue;
         v3 X[4] = {ld3(x[c.x]), ld3(x[f.x]), ld3(x[f.y]), ld3(x[f.z])};
         v3 P[4] = {ld3(p[c.x]), ld3(p[f.x]), ld3(p[f.y]), ld3(p[f.z])};
-        if (!sliver(X[1], X[2], X[3]) && !sliver(P[1], P[2], P[3])) {
-            // lower bound of the point-triangle distance over the step
-            v3 D0 = sub3(P[0], X[0]);
-            float d0 = point_tri_dist(X[0], X[1], X[2], X[3]);
-            float d1 = point_tri_dist(P[0], P[1], P[2], P[3]);
-            v3 ua = sub3(sub3(P[1], X[1]), D0), ub = sub3(sub3(P[2], X[2]), D0),
-               uc = sub3(sub3(P[3], X[3]), D0);
-            float U = sqrtf(fmaxf(fmaxf(dot3(ua, ua), dot3(ub, ub)), dot3(uc, uc)));
-            if ((d0 + d1 - U) * 0.5f > reach) continue;
-        }
         VFResult r;
         if (!extended_vf_test(X, P, th, r)) continue;
         int slot = agg_inc(counters + 1);
@@ -728,11 +733,12 @@ int ccd_detect(pbd_colli *c) {
         c->counters.p);
     PBD_LAUNCH();
     k_task_entries<<<kPersistentBlocks, 256, 0, s>>>(
-        c->tasks.p, c->tasks_z.p, c->task_cap, margin, o->has_inst ? o->point_inst.p : nullptr,
+        c->tasks.p, c->tasks_z.p, c->task_cap, margin, reach, o->tri.p,
+        o->has_inst ? o->point_inst.p : nullptr,
         o->has_inst ? o->tri_inst.p : nullptr, o->x.p, o->p.p, h->brange.p, h->scell.p,
         h->slo.p, h->shi.p, c->cand.p, c->cand_cap, c->counters.p);
     PBD_LAUNCH();
-    k_narrow<<<kPersistentBlocks, 128, 0, s>>>(c->cand.p, c->cand_cap, o->nt, th, reach, o->tri.p,
+    k_narrow<<<kPersistentBlocks, 128, 0, s>>>(c->cand.p, c->cand_cap, o->nt, th, o->tri.p,
                                                o->x.p, o->p.p, c->counters.p, c->contact_cap,
                                                c->cids.p, c->cface.p, c->ctn.p, c->cw.p);
     k_clamp_counts<<<1, 32, 0, s>>>(c->counters.p, c->cand_cap, c->contact_cap);

@@ -143,6 +143,14 @@ struct pbd_object {
     pbd::DBuf<float2> bpar;                     // rest angle, stiffness
     pbd::DBuf<float4> arec;                     // rest xyz, point id bits
     std::vector<int> h_dseg, h_bseg, h_aseg;    // n_colors+1 starts each
+    // records re-ordered for the cluster kernel: by color, then by the block
+    // owning the record's first point; segments (color*S + block)
+    int cl_state = 0;           // 0 not built, 1 usable, -1 not applicable
+    int cl_S = 0, cl_shift = 0;
+    pbd::DBuf<int4> cdrec, cbidx;
+    pbd::DBuf<float2> cbpar;
+    pbd::DBuf<float4> carec;
+    pbd::DBuf<int> cdseg, cbseg, caseg;
     // residual
     double res_den = 0.0;
     pbd::DBuf<double> res_part;
@@ -203,6 +211,7 @@ struct pbd_colli {
 
 struct pbd_solver {
     pbd_object *obj = nullptr;
+    int gs_path = 0;  // PBD_GS_AUTO / PER_COLOR / CLUSTER
     int sphere_on = 0;
     float sphere_c[3] = {0, 0, 0};
     float sphere_r = 1.0f;
@@ -221,7 +230,7 @@ struct pbd_solver {
 namespace pbd {
 int launch_advect(pbd_object *o, float dt);
 int launch_integrate(pbd_object *o, float dt);
-int launch_sweep(pbd_object *o, int iter);
+int launch_sweeps(pbd_solver *s, int it0, int it1, bool obstacles_inside);
 int launch_obstacles(pbd_solver *s);
 int ccd_detect(pbd_colli *c);
 int ccd_resolve(pbd_colli *c, int passes);

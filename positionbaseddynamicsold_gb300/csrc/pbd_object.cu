@@ -20,7 +20,11 @@
 #include <cmath>
 #include <cstring>
 
+#include <cooperative_groups.h>
+
 #include "pbd_common.cuh"
+
+namespace cg = cooperative_groups;
 
 namespace pbd {
 
@@ -261,9 +265,30 @@ __global__ void __launch_bounds__(256) k_integrate(int n, float dt, float4 *__re
     x[i] = make_float4(P.x, P.y, P.z, X.w);
 }
 
+// Position accessors: the per-color kernel reads and writes the global
+// array; the cluster kernel reads and writes the distributed shared memory of
+// a thread-block cluster, point i living in block i >> shift at slot
+// i & (2^shift - 1).
+struct GlobalPos {
+    float4 *p;
+    __device__ __forceinline__ float4 ld(int i) const { return p[i]; }
+    __device__ __forceinline__ void st(int i, float4 v) const { p[i] = v; }
+};
+struct ClusterPos {
+    float4 *local;
+    int shift;
+    __device__ __forceinline__ float4 *at(int i) const {
+        return cg::this_cluster().map_shared_rank(local, (unsigned)(i >> shift)) +
+               (i & ((1 << shift) - 1));
+    }
+    __device__ __forceinline__ float4 ld(int i) const { return *at(i); }
+    __device__ __forceinline__ void st(int i, float4 v) const { *at(i) = v; }
+};
+
 // distance constraint of ProjectContraintsGPUKernel (P/PBD_cuda.cu:1264-1294)
-__device__ __forceinline__ void project_distance(int4 r, float4 *__restrict__ p, float expk) {
-    float4 P0 = p[r.x], P1 = p[r.y];
+template <class Pos>
+__device__ __forceinline__ void project_distance(int4 r, const Pos &p, float expk) {
+    float4 P0 = p.ld(r.x), P1 = p.ld(r.y);
     float m0 = P0.w, m1 = P1.w;
     float msum = m0 + m1;
     float dx = P0.x - P1.x, dy = P0.y - P1.y, dz = P0.z - P1.z;
@@ -273,10 +298,10 @@ __device__ __forceinline__ void project_distance(int4 r, float4 *__restrict__ p,
     float k = 1.f - powf(1.f - s, expk);
     float s0 = -m0 / msum * (d - rest);
     float s1 = m1 / msum * (d - rest);
-    p[r.x] = make_float4(P0.x + ((dx * s0) / d) * k, P0.y + ((dy * s0) / d) * k,
-                         P0.z + ((dz * s0) / d) * k, m0);
-    p[r.y] = make_float4(P1.x + ((dx * s1) / d) * k, P1.y + ((dy * s1) / d) * k,
-                         P1.z + ((dz * s1) / d) * k, m1);
+    p.st(r.x, make_float4(P0.x + ((dx * s0) / d) * k, P0.y + ((dy * s0) / d) * k,
+                          P0.z + ((dz * s0) / d) * k, m0));
+    p.st(r.y, make_float4(P1.x + ((dx * s1) / d) * k, P1.y + ((dy * s1) / d) * k,
+                          P1.z + ((dz * s1) / d) * k, m1));
 }
 
 struct v3 {
@@ -297,9 +322,9 @@ __device__ __forceinline__ v3 cross3(v3 a, v3 b) {
 // Bridson-Marino-Fedkiw (2003) gradients grad_i theta = -u_i, inside the
 // PBD projection of Mueller et al. (2007).  Same operation order as the
 // oracle's orc_bending_project_f32.
-__device__ __forceinline__ void project_bending(int4 r, float2 par, float4 *__restrict__ p,
-                                                float expk) {
-    float4 Q0 = p[r.x], Q1 = p[r.y], Q2 = p[r.z], Q3 = p[r.w];
+template <class Pos>
+__device__ __forceinline__ void project_bending(int4 r, float2 par, const Pos &p, float expk) {
+    float4 Q0 = p.ld(r.x), Q1 = p.ld(r.y), Q2 = p.ld(r.z), Q3 = p.ld(r.w);
     v3 e0 = mk3(Q0.x, Q0.y, Q0.z), e1 = mk3(Q1.x, Q1.y, Q1.z);
     v3 wa = mk3(Q2.x, Q2.y, Q2.z), wb = mk3(Q3.x, Q3.y, Q3.z);
     v3 E = sub3(e1, e0);
@@ -326,10 +351,17 @@ __device__ __forceinline__ void project_bending(int4 r, float2 par, float4 *__re
     v3 n1 = add3(e1, mul3(ue1, Q1.w * s));
     v3 n2 = add3(wa, mul3(uwa, Q2.w * s));
     v3 n3 = add3(wb, mul3(uwb, Q3.w * s));
-    p[r.x] = make_float4(n0.x, n0.y, n0.z, Q0.w);
-    p[r.y] = make_float4(n1.x, n1.y, n1.z, Q1.w);
-    p[r.z] = make_float4(n2.x, n2.y, n2.z, Q2.w);
-    p[r.w] = make_float4(n3.x, n3.y, n3.z, Q3.w);
+    p.st(r.x, make_float4(n0.x, n0.y, n0.z, Q0.w));
+    p.st(r.y, make_float4(n1.x, n1.y, n1.z, Q1.w));
+    p.st(r.z, make_float4(n2.x, n2.y, n2.z, Q2.w));
+    p.st(r.w, make_float4(n3.x, n3.y, n3.z, Q3.w));
+}
+
+// ANCHOR (P/PBD_cuda.cu:1298-1305): snap the point to its rest position
+template <class Pos>
+__device__ __forceinline__ void project_anchor(float4 a, const Pos &p) {
+    int i = __float_as_int(a.w);
+    p.st(i, make_float4(a.x, a.y, a.z, p.ld(i).w));
 }
 
 // one color phase: distance, then bending, then anchor records of the color
@@ -339,25 +371,20 @@ __global__ void __launch_bounds__(256) k_project_color(const int4 *__restrict__ 
                                                        const float4 *__restrict__ arec, int na,
                                                        float4 *__restrict__ p, float expk) {
     int t = blockIdx.x * blockDim.x + threadIdx.x;
+    GlobalPos P{p};
     if (t < nd) {
-        project_distance(drec[t], p, expk);
+        project_distance(drec[t], P, expk);
     } else if (t < nd + nb) {
         int j = t - nd;
-        project_bending(bidx[j], bpar[j], p, expk);
+        project_bending(bidx[j], bpar[j], P, expk);
     } else if (t < nd + nb + na) {
-        // ANCHOR (P/PBD_cuda.cu:1298-1305): snap the point to its rest position
-        float4 a = arec[t - nd - nb];
-        int i = __float_as_int(a.w);
-        p[i] = make_float4(a.x, a.y, a.z, p[i].w);
+        project_anchor(arec[t - nd - nb], P);
     }
 }
 
-// ColliWithShpGrd (P/PBD_cuda.cu:1519-1573): sphere push-out and ground plane
-__global__ void k_obstacles(int n, float4 *p, int sphere_on, float3 c, float r, int ground_on,
-                            float gh) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    float4 P = p[i];
+// ColliWithShpGrd (P/PBD_cuda.cu:1519-1573) on one point
+__device__ __forceinline__ float4 obstacle_point(float4 P, int sphere_on, float3 c, float r,
+                                                 int ground_on, float gh) {
     if (sphere_on) {
         float dx = P.x - c.x, dy = P.y - c.y, dz = P.z - c.z;
         float d = sqrtf(dx * dx + dy * dy + dz * dz);
@@ -372,7 +399,61 @@ __global__ void k_obstacles(int n, float4 *p, int sphere_on, float3 c, float r, 
         }
     }
     if (ground_on && P.y - gh < 0.001f) P.y = gh;
-    p[i] = P;
+    return P;
+}
+
+// Colored GS held in one thread-block cluster: the cluster's distributed
+// shared memory holds every point; block r processes the records of each
+// color whose first point it owns (segments (color*S + r) of the
+// cluster-ordered records); a cluster barrier separates color phases, so a
+// sweep costs one launch instead of one per color.  Within a color no two
+// records share a point, so the result equals the per-color launches'.
+constexpr int kClusterThreads = 512;
+__global__ void __launch_bounds__(kClusterThreads, 1) k_gs_cluster(
+    const int4 *__restrict__ drec, const int *__restrict__ dseg, const int4 *__restrict__ bidx,
+    const float2 *__restrict__ bpar, const int *__restrict__ bseg,
+    const float4 *__restrict__ arec, const int *__restrict__ aseg, int n_colors, int n,
+    int shift, float4 *__restrict__ p, int it0, int it1, int sphere_on, float3 sc, float sr,
+    int ground_on, float gh) {
+    extern __shared__ float4 sp[];
+    cg::cluster_group cl = cg::this_cluster();
+    const int r = (int)cl.block_rank();
+    const int S = (int)cl.num_blocks();
+    const int chunk = 1 << shift;
+    const int base = r << shift;
+    for (int i = threadIdx.x; i < chunk; i += blockDim.x) {
+        int g = base + i;
+        sp[i] = g < n ? p[g] : make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+    cl.sync();
+    ClusterPos P{sp, shift};
+    for (int it = it0; it < it1; ++it) {
+        float expk = (float)(1.0 / (double)(it + 1));
+        for (int c = 0; c < n_colors; ++c) {
+            int q = c * S + r;
+            for (int k = dseg[q] + threadIdx.x; k < dseg[q + 1]; k += blockDim.x)
+                project_distance(drec[k], P, expk);
+            for (int k = bseg[q] + threadIdx.x; k < bseg[q + 1]; k += blockDim.x)
+                project_bending(bidx[k], bpar[k], P, expk);
+            for (int k = aseg[q] + threadIdx.x; k < aseg[q + 1]; k += blockDim.x)
+                project_anchor(arec[k], P);
+            cl.sync();
+        }
+        if (sphere_on || ground_on) {
+            for (int i = threadIdx.x; i < chunk && base + i < n; i += blockDim.x)
+                sp[i] = obstacle_point(sp[i], sphere_on, sc, sr, ground_on, gh);
+            cl.sync();
+        }
+    }
+    for (int i = threadIdx.x; i < chunk && base + i < n; i += blockDim.x) p[base + i] = sp[i];
+}
+
+// ColliWithShpGrd (P/PBD_cuda.cu:1519-1573): sphere push-out and ground plane
+__global__ void k_obstacles(int n, float4 *p, int sphere_on, float3 c, float r, int ground_on,
+                            float gh) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    p[i] = obstacle_point(p[i], sphere_on, c, r, ground_on, gh);
 }
 
 // residual: FP64 per constraint, warp-shuffle + block reduction
@@ -444,6 +525,8 @@ constexpr int kResidualBlocks = 4 * kNumSMs;
 // ---------------------------------------------------------------------------
 // host helpers
 // ---------------------------------------------------------------------------
+int launch_obstacles(pbd_solver *s);
+
 int launch_advect(pbd_object *o, float dt) {
     float dp = powf(o->damping, dt);
     float3 gdt = make_float3(o->gravity[0] * dt, o->gravity[1] * dt, o->gravity[2] * dt);
@@ -458,9 +541,13 @@ int launch_integrate(pbd_object *o, float dt) {
     return PBD_OK;
 }
 
-int launch_sweep(pbd_object *o, int iter) {
-    PBD_CHECK(o->sorted, PBD_ERR_STATE,
-              "no color-sorted constraints: run edge coloring and SortEdgesColors first");
+static inline int __float_as_int_host(float f) {
+    int i;
+    memcpy(&i, &f, sizeof(i));
+    return i;
+}
+
+static int launch_sweep_per_color(pbd_object *o, int iter) {
     float expk = (float)(1.0 / (double)(iter + 1));
     for (int c = 0; c < o->n_colors; ++c) {
         int d0 = o->h_dseg[c], nd = o->h_dseg[c + 1] - d0;
@@ -473,6 +560,160 @@ int launch_sweep(pbd_object *o, int iter) {
             expk);
     }
     PBD_LAUNCH();
+    return PBD_OK;
+}
+
+// Builds the cluster-ordered records once per coloring; returns whether the
+// cluster form applies (the object fits one cluster's shared memory and the
+// device can co-schedule the cluster).
+static int cluster_plan(pbd_object *o) {
+    if (o->cl_state != 0) return PBD_OK;
+    o->cl_state = -1;
+    if (o->np == 0 || o->n_colors == 0) return PBD_OK;
+    const int max_chunk_shift = 13;  // 8192 points x 16 B = 128 KiB per block
+    int S = 0, shift = 0;
+    for (int cand : {16, 8}) {
+        int sh = 0;
+        while (((long long)cand << sh) < o->n) ++sh;
+        if (sh > max_chunk_shift) continue;
+        if (sh < 5) sh = 5;
+        size_t smem = (size_t)sizeof(float4) << sh;
+        if (cudaFuncSetAttribute(k_gs_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)smem) != cudaSuccess) {
+            cudaGetLastError();
+            continue;
+        }
+        if (cand > 8 &&
+            cudaFuncSetAttribute(k_gs_cluster, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) !=
+                cudaSuccess) {
+            cudaGetLastError();
+            continue;
+        }
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3(cand);
+        cfg.blockDim = dim3(kClusterThreads);
+        cfg.dynamicSmemBytes = smem;
+        cudaLaunchAttribute at[1];
+        at[0].id = cudaLaunchAttributeClusterDimension;
+        at[0].val.clusterDim.x = cand;
+        at[0].val.clusterDim.y = 1;
+        at[0].val.clusterDim.z = 1;
+        cfg.attrs = at;
+        cfg.numAttrs = 1;
+        int nclusters = 0;
+        if (cudaOccupancyMaxActiveClusters(&nclusters, k_gs_cluster, &cfg) != cudaSuccess) {
+            cudaGetLastError();
+            continue;
+        }
+        if (nclusters >= 1) {
+            S = cand;
+            shift = sh;
+            break;
+        }
+    }
+    if (!S) return PBD_OK;
+    cudaStream_t s = o->stream;
+    int nc = o->n_colors;
+    int nd = o->h_dseg[nc], nb = o->h_bseg[nc], na = o->h_aseg[nc];
+    std::vector<int4> d(nd), bi(nb);
+    std::vector<float2> bp(nb);
+    std::vector<float4> a(na);
+    if (nd) PBD_CUDA(cudaMemcpyAsync(d.data(), o->drec.p, sizeof(int4) * nd, cudaMemcpyDeviceToHost, s));
+    if (nb) {
+        PBD_CUDA(cudaMemcpyAsync(bi.data(), o->bidx.p, sizeof(int4) * nb, cudaMemcpyDeviceToHost, s));
+        PBD_CUDA(cudaMemcpyAsync(bp.data(), o->bpar.p, sizeof(float2) * nb, cudaMemcpyDeviceToHost, s));
+    }
+    if (na) PBD_CUDA(cudaMemcpyAsync(a.data(), o->arec.p, sizeof(float4) * na, cudaMemcpyDeviceToHost, s));
+    PBD_CUDA(cudaStreamSynchronize(s));
+    // stable bucketing of each color's records by owner block
+    auto order = [&](const std::vector<int> &seg, auto first_point, std::vector<int> &perm,
+                     std::vector<int> &cseg) {
+        int total = seg[nc];
+        perm.resize(total);
+        cseg.assign((size_t)nc * S + 1, 0);
+        int out = 0;
+        for (int c = 0; c < nc; ++c) {
+            std::vector<int> cnt(S + 1, 0);
+            for (int k = seg[c]; k < seg[c + 1]; ++k) cnt[(first_point(k) >> shift) + 1]++;
+            for (int r = 0; r < S; ++r) cnt[r + 1] += cnt[r];
+            for (int r = 0; r < S; ++r) cseg[(size_t)c * S + r] = out + cnt[r];
+            std::vector<int> pos(cnt.begin(), cnt.end() - 1);
+            for (int k = seg[c]; k < seg[c + 1]; ++k) perm[out + pos[first_point(k) >> shift]++] = k;
+            out += seg[c + 1] - seg[c];
+        }
+        cseg[(size_t)nc * S] = out;
+    };
+    std::vector<int> pd, pb, pa, sd, sb, sa;
+    order(o->h_dseg, [&](int k) { return d[k].x; }, pd, sd);
+    order(o->h_bseg, [&](int k) { return bi[k].x; }, pb, sb);
+    order(o->h_aseg, [&](int k) { return __float_as_int_host(a[k].w); }, pa, sa);
+    std::vector<int4> d2(nd), b2(nb);
+    std::vector<float2> p2(nb);
+    std::vector<float4> a2(na);
+    for (int k = 0; k < nd; ++k) d2[k] = d[pd[k]];
+    for (int k = 0; k < nb; ++k) {
+        b2[k] = bi[pb[k]];
+        p2[k] = bp[pb[k]];
+    }
+    for (int k = 0; k < na; ++k) a2[k] = a[pa[k]];
+    PBD_TRY(o->cdrec.upload(d2.data(), nd, s));
+    PBD_TRY(o->cbidx.upload(b2.data(), nb, s));
+    PBD_TRY(o->cbpar.upload(p2.data(), nb, s));
+    PBD_TRY(o->carec.upload(a2.data(), na, s));
+    PBD_TRY(o->cdseg.upload(sd.data(), sd.size(), s));
+    PBD_TRY(o->cbseg.upload(sb.data(), sb.size(), s));
+    PBD_TRY(o->caseg.upload(sa.data(), sa.size(), s));
+    PBD_CUDA(cudaStreamSynchronize(s));
+    o->cl_S = S;
+    o->cl_shift = shift;
+    o->cl_state = 1;
+    return PBD_OK;
+}
+
+static int resolved_path(pbd_solver *s) {
+    if (s->gs_path == PBD_GS_PER_COLOR) return PBD_GS_PER_COLOR;
+    if (cluster_plan(s->obj) != PBD_OK) return -1;
+    if (s->obj->cl_state == 1) return PBD_GS_CLUSTER;
+    return s->gs_path == PBD_GS_CLUSTER ? -2 : PBD_GS_PER_COLOR;
+}
+
+// GS sweeps it0..it1-1, each followed by the analytic obstacles when
+// obstacles_inside (otherwise the caller applies them)
+int launch_sweeps(pbd_solver *s, int it0, int it1, bool obstacles_inside) {
+    pbd_object *o = s->obj;
+    PBD_CHECK(o->sorted, PBD_ERR_STATE,
+              "no color-sorted constraints: run edge coloring and SortEdgesColors first");
+    int path = resolved_path(s);
+    PBD_CHECK(path != -1, PBD_ERR_CUDA, "cluster plan failed: %s", pbd_last_error());
+    PBD_CHECK(path != -2, PBD_ERR_STATE,
+              "the cluster Gauss-Seidel form does not apply to this object (%d points)", o->n);
+    if (path == PBD_GS_CLUSTER) {
+        int ob = obstacles_inside && (s->sphere_on || s->ground_on);
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3(o->cl_S);
+        cfg.blockDim = dim3(kClusterThreads);
+        cfg.dynamicSmemBytes = sizeof(float4) << o->cl_shift;
+        cfg.stream = o->stream;
+        cudaLaunchAttribute at[1];
+        at[0].id = cudaLaunchAttributeClusterDimension;
+        at[0].val.clusterDim.x = o->cl_S;
+        at[0].val.clusterDim.y = 1;
+        at[0].val.clusterDim.z = 1;
+        cfg.attrs = at;
+        cfg.numAttrs = 1;
+        PBD_CUDA(cudaLaunchKernelEx(
+            &cfg, k_gs_cluster, (const int4 *)o->cdrec.p, (const int *)o->cdseg.p,
+            (const int4 *)o->cbidx.p, (const float2 *)o->cbpar.p, (const int *)o->cbseg.p,
+            (const float4 *)o->carec.p, (const int *)o->caseg.p, o->n_colors, o->n, o->cl_shift,
+            o->p.p, it0, it1, ob ? s->sphere_on : 0,
+            make_float3(s->sphere_c[0], s->sphere_c[1], s->sphere_c[2]), s->sphere_r,
+            ob ? s->ground_on : 0, s->ground_h));
+        return PBD_OK;
+    }
+    for (int it = it0; it < it1; ++it) {
+        PBD_TRY(launch_sweep_per_color(o, it));
+        if (obstacles_inside) PBD_TRY(launch_obstacles(s));
+    }
     return PBD_OK;
 }
 
@@ -887,6 +1128,7 @@ static int finish_coloring(pbd_object *o) {
     o->n_colors = mx + 1;
     o->colored = true;
     o->sorted = false;
+    o->cl_state = 0;
     return PBD_OK;
 }
 
@@ -1110,11 +1352,8 @@ int pbd_solver_integration(pbd_solver *s, float dt) {
 int pbd_solver_project_constraint(pbd_solver *s, int st, int iterations) {
     PBD_CHECK(s && s->obj, PBD_ERR_STATE, "solver has no target");
     PBD_CHECK(st == PBD_GAUSSSEIDEL, PBD_ERR_ARG, "only Gauss-Seidel is implemented");
-    for (int i = 0; i < iterations; ++i) {
-        PBD_TRY(launch_sweep(s->obj, i));
-        PBD_TRY(launch_obstacles(s));
-    }
-    return PBD_OK;
+    if (iterations <= 0) return PBD_OK;
+    return launch_sweeps(s, 0, iterations, true);
 }
 
 int pbd_solver_set_sphere(pbd_solver *s, int on, const float *c, float r) {
@@ -1134,10 +1373,11 @@ int pbd_solver_set_ground(pbd_solver *s, int on, float h) {
 }
 
 static int project_with_colli(pbd_solver *s, int iterations, pbd_colli *c) {
+    if (!c) return iterations > 0 ? launch_sweeps(s, 0, iterations, true) : PBD_OK;
     for (int ii = 0; ii < iterations; ++ii) {
-        if (c && (ii % 10 == 0 || ii == iterations - 1)) PBD_TRY(ccd_detect(c));
-        PBD_TRY(launch_sweep(s->obj, ii));
-        if (c) PBD_TRY(ccd_resolve(c, c->iterations));
+        if (ii % 10 == 0 || ii == iterations - 1) PBD_TRY(ccd_detect(c));
+        PBD_TRY(launch_sweeps(s, ii, ii + 1, false));
+        PBD_TRY(ccd_resolve(c, c->iterations));
         PBD_TRY(launch_obstacles(s));
     }
     return PBD_OK;
@@ -1166,7 +1406,8 @@ int pbd_solver_step(pbd_solver *s, float dt, int substeps, int iterations, pbd_c
     PBD_CHECK(s->obj->sorted, PBD_ERR_STATE, "constraints are not color-sorted");
     PBD_CHECK(!c || c->obj == s->obj, PBD_ERR_ARG, "collision solver targets another object");
     if (!use_graph) return record_steps(s, dt, substeps, iterations, c);
-    int sig = s->sphere_on * 3 + s->ground_on * 7 + (c ? c->response * 11 + c->iterations * 13 : 0);
+    int sig = s->sphere_on * 3 + s->ground_on * 7 + (c ? c->response * 11 + c->iterations * 13 : 0) +
+              s->gs_path * 1009;
     if (s->gexec && (s->g_dt != dt || s->g_sub != substeps || s->g_it != iterations ||
                      s->g_colli != c || s->g_sig != sig)) {
         cudaGraphExecDestroy(s->gexec);
@@ -1175,6 +1416,7 @@ int pbd_solver_step(pbd_solver *s, float dt, int substeps, int iterations, pbd_c
     cudaStream_t st = s->obj->stream;
     if (!s->gexec) {
         if (c) PBD_TRY(ccd_detect(c));  // sizes every buffer before capture
+        PBD_TRY(cluster_plan(s->obj));  // host-side set-up stays out of the capture
         PBD_CUDA(cudaStreamSynchronize(st));
         cudaGraph_t g;
         PBD_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
@@ -1205,6 +1447,21 @@ int pbd_solver_step(pbd_solver *s, float dt, int substeps, int iterations, pbd_c
         s->g_sig = sig;
     }
     PBD_CUDA(cudaGraphLaunch(s->gexec, st));
+    return PBD_OK;
+}
+
+int pbd_solver_set_gs_path(pbd_solver *s, int path) {
+    PBD_CHECK(s && path >= PBD_GS_AUTO && path <= PBD_GS_CLUSTER, PBD_ERR_ARG, "bad path");
+    s->gs_path = path;
+    return PBD_OK;
+}
+
+int pbd_solver_get_gs_path(pbd_solver *s, int *path) {
+    PBD_CHECK(s && path && s->obj, PBD_ERR_STATE, "solver has no target");
+    PBD_CHECK(s->obj->sorted, PBD_ERR_STATE, "constraints are not color-sorted");
+    int p = resolved_path(s);
+    PBD_CHECK(p != -1, PBD_ERR_CUDA, "cluster plan failed");
+    *path = p == -2 ? PBD_GS_PER_COLOR : p;
     return PBD_OK;
 }
 

@@ -20,6 +20,7 @@ from . import build as _build
 DISTANCE, BENDING, ANCHOR = 0x001, 0x010, 0x100
 JACOBI, GAUSSSEIDEL = 0, 1
 RESPONSE_REFERENCE, RESPONSE_MASS_WEIGHTED = 0, 1
+GS_AUTO, GS_PER_COLOR, GS_CLUSTER = 0, 1, 2
 _ERRS = {1: "ARG", 2: "OOM", 3: "CUDA", 4: "TIMEOUT", 5: "OVERFLOW", 6: "STATE"}
 
 
@@ -54,7 +55,8 @@ EXPORTS = [
     "pbd_solver_destroy", "pbd_solver_set_target", "pbd_solver_advect",
     "pbd_solver_project_constraint", "pbd_solver_project_constraint_with_colli",
     "pbd_solver_integration", "pbd_solver_set_sphere", "pbd_solver_set_ground",
-    "pbd_solver_step", "pbd_solver_graph_kernels", "pbd_shs_create", "pbd_shs_create_hashed", "pbd_shs_destroy",
+    "pbd_solver_step", "pbd_solver_set_gs_path", "pbd_solver_get_gs_path",
+    "pbd_solver_graph_kernels", "pbd_shs_create", "pbd_shs_create_hashed", "pbd_shs_destroy",
     "pbd_shs_set_grid_center", "pbd_shs_set_grid_size", "pbd_shs_set_division", "pbd_shs_init",
     "pbd_shs_update", "pbd_shs_find_neighbors", "pbd_shs_find_neighbors_all",
     "pbd_colli_create", "pbd_colli_destroy", "pbd_colli_set_target",
@@ -452,6 +454,14 @@ class SolverPBD:
 
     def set_ground(self, enable, height=0.0):
         _check(self.L.pbd_solver_set_ground(self.h, int(enable), height))
+
+    def set_gs_path(self, path):
+        _check(self.L.pbd_solver_set_gs_path(self.h, int(path)))
+
+    def gs_path(self):
+        v = C.c_int()
+        _check(self.L.pbd_solver_get_gs_path(self.h, C.byref(v)))
+        return v.value
 
     def graph_kernels(self):
         n = C.c_longlong()

@@ -149,3 +149,33 @@ def test_sphere_and_ground_obstacles(orc):
     s.set_ground(True, 0.9)
     s.project_constraint(1)
     assert (obj.predicted()[:, 1] >= 0.9).all()
+
+
+@pytest.mark.parametrize("res", [32, 100])
+def test_cluster_path_equals_per_color(orc, res):
+    """The cluster-resident sweep (all points in distributed shared memory,
+    colors separated by cluster barriers) gives the per-color launches'
+    result bit for bit, with and without the analytic obstacles."""
+    from positionbaseddynamicsold_gb300.pbd import GS_CLUSTER, GS_PER_COLOR
+    sc = scenes.grid_cloth(res, res, 1.0, 1.0, origin=(-0.5, 0.9, -0.5), jitter=1e-3, seed=6,
+                           pins=[0, res - 1])
+    out = []
+    for path in (GS_PER_COLOR, GS_CLUSTER):
+        obj = PBDObject(sc, damping=0.9, gravity=G)
+        obj.prepare()
+        s = SolverPBD(obj)
+        s.set_gs_path(path)
+        assert s.gs_path() == path
+        s.set_sphere(True, (0.0, 0.0, 0.0), 1.0)
+        for _ in range(3):
+            s.advect(1.0 / 600)
+            s.project_constraint(20)
+            s.integration(1.0 / 600)
+        s.step(1.0 / 600, substeps=2, iterations=20, use_graph=True)
+        out.append(obj.positions())
+    np.testing.assert_array_equal(out[0], out[1])
+    # and the per-color path equals the oracle on the first substep already
+    # (test_substep_hanging_cloth_32); auto resolves to the cluster form here
+    obj = PBDObject(sc, damping=0.9, gravity=G)
+    obj.prepare()
+    assert SolverPBD(obj).gs_path() == GS_CLUSTER
