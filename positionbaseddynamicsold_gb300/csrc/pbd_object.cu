@@ -408,7 +408,8 @@ __device__ __forceinline__ float4 obstacle_point(float4 P, int sphere_on, float3
 // cluster-ordered records); a cluster barrier separates color phases, so a
 // sweep costs one launch instead of one per color.  Within a color no two
 // records share a point, so the result equals the per-color launches'.
-constexpr int kClusterThreads = 512;
+constexpr int kClusterThreads = 1024;
+constexpr int kClusterMaxColors = 256;
 __global__ void __launch_bounds__(kClusterThreads, 1) k_gs_cluster(
     const int4 *__restrict__ drec, const int *__restrict__ dseg, const int4 *__restrict__ bidx,
     const float2 *__restrict__ bpar, const int *__restrict__ bseg,
@@ -416,36 +417,72 @@ __global__ void __launch_bounds__(kClusterThreads, 1) k_gs_cluster(
     int shift, float4 *__restrict__ p, int it0, int it1, int sphere_on, float3 sc, float sr,
     int ground_on, float gh) {
     extern __shared__ float4 sp[];
+    // this block's segment of every color, per record kind: [s0, s1)
+    __shared__ int sd0[kClusterMaxColors], sd1[kClusterMaxColors];
+    __shared__ int sb0[kClusterMaxColors], sb1[kClusterMaxColors];
+    __shared__ int sa0[kClusterMaxColors], sa1[kClusterMaxColors];
     cg::cluster_group cl = cg::this_cluster();
     const int r = (int)cl.block_rank();
     const int S = (int)cl.num_blocks();
     const int chunk = 1 << shift;
     const int base = r << shift;
-    for (int i = threadIdx.x; i < chunk; i += blockDim.x) {
+    const int tid = threadIdx.x;
+    for (int c = tid; c < n_colors; c += blockDim.x) {
+        int q = c * S + r;
+        sd0[c] = dseg[q];
+        sd1[c] = dseg[q + 1];
+        sb0[c] = bseg[q];
+        sb1[c] = bseg[q + 1];
+        sa0[c] = aseg[q];
+        sa1[c] = aseg[q + 1];
+    }
+    for (int i = tid; i < chunk; i += blockDim.x) {
         int g = base + i;
         sp[i] = g < n ? p[g] : make_float4(0.f, 0.f, 0.f, 0.f);
     }
     cl.sync();
     ClusterPos P{sp, shift};
+    // the first record of each kind this thread takes in the coming phase,
+    // loaded before the barrier that precedes the phase
+    int4 dr = make_int4(0, 0, 0, 0), br = make_int4(0, 0, 0, 0);
+    float2 bp = make_float2(0.f, 0.f);
+    float4 ar = make_float4(0.f, 0.f, 0.f, 0.f);
+    bool hd = false, hb = false, ha = false;
+    auto fetch = [&](int c) {
+        int kd = sd0[c] + tid, kb = sb0[c] + tid, ka = sa0[c] + tid;
+        hd = kd < sd1[c];
+        hb = kb < sb1[c];
+        ha = ka < sa1[c];
+        if (hd) dr = drec[kd];
+        if (hb) {
+            br = bidx[kb];
+            bp = bpar[kb];
+        }
+        if (ha) ar = arec[ka];
+    };
+    fetch(0);
     for (int it = it0; it < it1; ++it) {
         float expk = (float)(1.0 / (double)(it + 1));
         for (int c = 0; c < n_colors; ++c) {
-            int q = c * S + r;
-            for (int k = dseg[q] + threadIdx.x; k < dseg[q + 1]; k += blockDim.x)
+            if (hd) project_distance(dr, P, expk);
+            for (int k = sd0[c] + tid + (int)blockDim.x; k < sd1[c]; k += blockDim.x)
                 project_distance(drec[k], P, expk);
-            for (int k = bseg[q] + threadIdx.x; k < bseg[q + 1]; k += blockDim.x)
+            if (hb) project_bending(br, bp, P, expk);
+            for (int k = sb0[c] + tid + (int)blockDim.x; k < sb1[c]; k += blockDim.x)
                 project_bending(bidx[k], bpar[k], P, expk);
-            for (int k = aseg[q] + threadIdx.x; k < aseg[q + 1]; k += blockDim.x)
+            if (ha) project_anchor(ar, P);
+            for (int k = sa0[c] + tid + (int)blockDim.x; k < sa1[c]; k += blockDim.x)
                 project_anchor(arec[k], P);
+            fetch(c + 1 < n_colors ? c + 1 : 0);
             cl.sync();
         }
         if (sphere_on || ground_on) {
-            for (int i = threadIdx.x; i < chunk && base + i < n; i += blockDim.x)
+            for (int i = tid; i < chunk && base + i < n; i += blockDim.x)
                 sp[i] = obstacle_point(sp[i], sphere_on, sc, sr, ground_on, gh);
             cl.sync();
         }
     }
-    for (int i = threadIdx.x; i < chunk && base + i < n; i += blockDim.x) p[base + i] = sp[i];
+    for (int i = tid; i < chunk && base + i < n; i += blockDim.x) p[base + i] = sp[i];
 }
 
 // ColliWithShpGrd (P/PBD_cuda.cu:1519-1573): sphere push-out and ground plane
@@ -569,7 +606,7 @@ static int launch_sweep_per_color(pbd_object *o, int iter) {
 static int cluster_plan(pbd_object *o) {
     if (o->cl_state != 0) return PBD_OK;
     o->cl_state = -1;
-    if (o->np == 0 || o->n_colors == 0) return PBD_OK;
+    if (o->np == 0 || o->n_colors == 0 || o->n_colors > kClusterMaxColors) return PBD_OK;
     const int max_chunk_shift = 13;  // 8192 points x 16 B = 128 KiB per block
     int S = 0, shift = 0;
     for (int cand : {16, 8}) {
@@ -670,11 +707,13 @@ static int cluster_plan(pbd_object *o) {
     return PBD_OK;
 }
 
+// PBD_GS_AUTO takes the per-color launches: measured on GB300 they are the
+// faster form (a 256x256 cloth: 3.4 us per color phase inside a graph
+// against 8.5 us per phase for the cluster form)
 static int resolved_path(pbd_solver *s) {
-    if (s->gs_path == PBD_GS_PER_COLOR) return PBD_GS_PER_COLOR;
+    if (s->gs_path != PBD_GS_CLUSTER) return PBD_GS_PER_COLOR;
     if (cluster_plan(s->obj) != PBD_OK) return -1;
-    if (s->obj->cl_state == 1) return PBD_GS_CLUSTER;
-    return s->gs_path == PBD_GS_CLUSTER ? -2 : PBD_GS_PER_COLOR;
+    return s->obj->cl_state == 1 ? PBD_GS_CLUSTER : -2;
 }
 
 // GS sweeps it0..it1-1, each followed by the analytic obstacles when
@@ -1416,7 +1455,7 @@ int pbd_solver_step(pbd_solver *s, float dt, int substeps, int iterations, pbd_c
     cudaStream_t st = s->obj->stream;
     if (!s->gexec) {
         if (c) PBD_TRY(ccd_detect(c));  // sizes every buffer before capture
-        PBD_TRY(cluster_plan(s->obj));  // host-side set-up stays out of the capture
+        if (s->gs_path == PBD_GS_CLUSTER) PBD_TRY(cluster_plan(s->obj));  // outside the capture
         PBD_CUDA(cudaStreamSynchronize(st));
         cudaGraph_t g;
         PBD_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));

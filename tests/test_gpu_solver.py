@@ -174,8 +174,7 @@ def test_cluster_path_equals_per_color(orc, res):
         s.step(1.0 / 600, substeps=2, iterations=20, use_graph=True)
         out.append(obj.positions())
     np.testing.assert_array_equal(out[0], out[1])
-    # and the per-color path equals the oracle on the first substep already
-    # (test_substep_hanging_cloth_32); auto resolves to the cluster form here
+    # the per-color form is checked against the oracle by the other tests
     obj = PBDObject(sc, damping=0.9, gravity=G)
     obj.prepare()
-    assert SolverPBD(obj).gs_path() == GS_CLUSTER
+    assert SolverPBD(obj).gs_path() == GS_PER_COLOR
