@@ -154,6 +154,7 @@ def run_ours(args, rank, world):
     torch.cuda.set_device(0 if world == 1 else int(os.environ.get("LOCAL_RANK", rank)))
     sc, cfg, colli_on, tl = make_workload(args.workload)
     obj, solver, shs, cs = setup(sc, colli_on, tl)
+    solver.set_gs_path({"auto": 0, "per-color": 1, "cluster": 2}[args.gs_path])
     stream = torch.cuda.ExternalStream(obj.stream())
     nd = int((sc["ctype"] == scenes.DISTANCE).sum())
     nb = int((sc["ctype"] == scenes.BENDING).sum())
@@ -373,6 +374,7 @@ def main():
     ap.add_argument("--workload", default="drape256", choices=["drape256", "fold1024", "hanging32"])
     ap.add_argument("--preroll", type=int, default=120)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--gs-path", default="auto", choices=["auto", "per-color", "cluster"])
     ap.add_argument("--profile-range", action="store_true",
                     help="cudaProfilerStart/Stop around the timed substeps (for ncu "
                          "--profile-from-start off)")
