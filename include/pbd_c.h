@@ -220,6 +220,12 @@ int pbd_colli_collision_resolve_new(pbd_colli *c);
  * face triangle, t, w (4 doubles), n (3 floats); any output may be NULL. */
 int pbd_colli_get_contacts(pbd_colli *c, int *ids, int *face, float *t, double *w, float *n,
                            long long cap, long long *count);
+/* The free ExtendedVFTest (P/CCD.cpp:1733-1808) on n independent
+ * configurations, host arrays in and out: x12/p12 = start / predicted
+ * positions of point, f0, f1, f2 (12 floats each per case), thickness per
+ * case; outputs hit (0/1), t, w (4 doubles), n (3 floats) per case. */
+int pbd_ccd_vf_test_batch(const float *x12, const float *p12, const float *thickness, int n,
+                          int *hit, float *t, double *w, float *nrm);
 /* number of broadphase candidate pairs that reached the narrow phase in
  * the last CCD call, and the overflow flag */
 int pbd_colli_stats(pbd_colli *c, long long *candidates, long long *contacts, int *overflow);

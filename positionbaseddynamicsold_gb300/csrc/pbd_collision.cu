@@ -14,11 +14,11 @@
 //      pair; the union holds each distinct pair once); a cell whose bucket
 //      AABB misses the point's grown swept AABB yields no task;
 //   4. one thread per task scans the bucket's entries (sorted-order copies of
-//      cell and AABB): exact-cell check, swept-AABB overlap with margin 5.5 h,
-//      then a lower bound on the point-triangle distance over the step
-//      (reject above 4.5 h; a hit needs it below 3.61 h); survivors become
-//      candidate pairs (one atomic per lane group).  Neither filter can
-//      reject a pair ExtendedVFTest would accept.
+//      cell and AABB): exact-cell check and swept-AABB overlap with margin
+//      5.5 h; the survivors, one thread each, then need a lower bound on the
+//      point-triangle distance over the step of at most 4.5 h (a hit needs it
+//      below 3.61 h) to become candidates.  Neither filter can reject a pair
+//      ExtendedVFTest would accept.
 // Narrowphase: one thread per candidate runs ExtendedVFTest
 // (P/CCD.cpp:1733-1808) with the reference's arithmetic: float triple
 // products widened to double, the double cubic solve (P/CCD.cpp:48-113), the
@@ -155,8 +155,52 @@ struct VFResult {
     double w[4];
 };
 
+// one evaluation of ExtendedVFTest's loop body at time t
+__device__ __forceinline__ bool vf_eval_at(const v3 *X, const v3 *P, float th, double t,
+                                           VFResult &res) {
+    v3 c0 = lerp_t(X[0], P[0], t), c1 = lerp_t(X[1], P[1], t);
+    v3 c2 = lerp_t(X[2], P[2], t), c3 = lerp_t(X[3], P[3], t);
+    v3 n = nrm3(cross3(sub3(P[2], P[1]), sub3(P[3], P[1])));
+    v3 cn = nrm3(cross3(sub3(c2, c1), sub3(c3, c1)));
+    double dist = dot3(sub3(c0, c1), cn);
+    v3 w = bary(c0, c1, c2, c3);
+    res.t = (float)t;
+    res.n = n;
+    res.w[0] = 1;
+    res.w[1] = w.x;
+    res.w[2] = w.y;
+    res.w[3] = w.z;
+    float e1 = dist3(c1, c2), e2 = dist3(c1, c3), e3 = dist3(c2, c3);
+    float eps = (float)((double)th / ((double)(e1 + e2 + e3) / 3.0));
+    bool in = (w.x <= (1 + eps)) && (w.x >= (-eps)) && (w.y <= (1 + eps)) && (w.y >= (-eps)) &&
+              (w.z <= (1 + eps)) && (w.z >= (-eps));
+    return (fabs(dist) - (double)(2.0f * th) < -1e-6) && in;
+}
+
+// true when a3 t^3 + a2 t^2 + a1 t + a0 has no root on [-d, 1+d], d = 1e-3:
+// its Bernstein coefficients on that interval share one strict sign
+__device__ __forceinline__ bool no_root_near_unit(double a0, double a1, double a2, double a3) {
+    const double u = -1e-3, L = 1.002;
+    double c0 = ((a3 * u + a2) * u + a1) * u + a0;
+    double c1 = L * ((3.0 * a3 * u + 2.0 * a2) * u + a1);
+    double c2 = L * L * (3.0 * a3 * u + a2);
+    double c3 = L * L * L * a3;
+    double b0 = c0, b1 = c0 + c1 / 3.0, b2 = c0 + 2.0 * c1 / 3.0 + c2 / 3.0, b3 = c0 + c1 + c2 + c3;
+    double tol = 1e-9 * (fabs(a0) + fabs(a1) + fabs(a2) + fabs(a3));
+    bool pos = b0 > tol && b1 > tol && b2 > tol && b3 > tol;
+    bool neg = b0 < -tol && b1 < -tol && b2 < -tol && b3 < -tol;
+    return pos || neg;
+}
+
 // ExtendedVFTest (P/CCD.cpp:1733-1808); X/P = start/predicted positions of
-// point, f0, f1, f2
+// point, f0, f1, f2.  The reference evaluates t = 0, the cubic's roots in
+// [0, 1] and t = 1 in ascending order and stops at the first hit.  Two
+// shortcuts keep that result: t = 0 is always the first time evaluated, so
+// a hit there ends the test before any root is needed; and when the
+// coplanarity cubic provably has no root within 1e-3 of [0, 1], the root
+// solver (Newton iterations converging to roots outside that range) adds no
+// time to evaluate, leaving t = 1.  Only the remaining pairs run the FP64
+// root isolation.
 __device__ bool extended_vf_test(const v3 *X, const v3 *P, float th, VFResult &res) {
     v3 x0 = X[0], v0 = sub3(P[0], x0);
     v3 x1 = sub3(X[1], x0), x2 = sub3(X[2], x0), x3 = sub3(X[3], x0);
@@ -166,6 +210,8 @@ __device__ bool extended_vf_test(const v3 *X, const v3 *P, float th, VFResult &r
     double a1 = stp(v1, x2, x3) + stp(x1, v2, x3) + stp(x1, x2, v3_);
     double a2 = stp(x1, v2, v3_) + stp(v1, x2, v3_) + stp(v1, v2, x3);
     double a3 = stp(v1, v2, v3_);
+    if (vf_eval_at(X, P, th, 0.0, res)) return true;
+    if (no_root_near_unit(a0, a1, a2, a3)) return vf_eval_at(X, P, th, 1.0, res);
     double t[5];
     int nsol = solve_cubic(a3, a2, a1, a0, t);
     t[nsol] = 1;
@@ -182,23 +228,7 @@ __device__ bool extended_vf_test(const v3 *X, const v3 *P, float th, VFResult &r
     }
     for (int i = 0; i < m; ++i) {
         if (t[i] < 0 || t[i] > 1) continue;
-        v3 c0 = lerp_t(X[0], P[0], t[i]), c1 = lerp_t(X[1], P[1], t[i]);
-        v3 c2 = lerp_t(X[2], P[2], t[i]), c3 = lerp_t(X[3], P[3], t[i]);
-        v3 n = nrm3(cross3(sub3(P[2], P[1]), sub3(P[3], P[1])));
-        v3 cn = nrm3(cross3(sub3(c2, c1), sub3(c3, c1)));
-        double dist = dot3(sub3(c0, c1), cn);
-        v3 w = bary(c0, c1, c2, c3);
-        res.t = (float)t[i];
-        res.n = n;
-        res.w[0] = 1;
-        res.w[1] = w.x;
-        res.w[2] = w.y;
-        res.w[3] = w.z;
-        float e1 = dist3(c1, c2), e2 = dist3(c1, c3), e3 = dist3(c2, c3);
-        float eps = (float)((double)th / ((double)(e1 + e2 + e3) / 3.0));
-        bool in = (w.x <= (1 + eps)) && (w.x >= (-eps)) && (w.y <= (1 + eps)) &&
-                  (w.y >= (-eps)) && (w.z <= (1 + eps)) && (w.z >= (-eps));
-        if ((fabs(dist) - (double)(2.0f * th) < -1e-6) && in) return true;
+        if (vf_eval_at(X, P, th, t[i], res)) return true;
     }
     return false;
 }
@@ -466,11 +496,10 @@ __global__ void __launch_bounds__(32 * kTaskWarps) k_cell_tasks(
 // pairs whose cell is the task's and whose swept AABBs meet
 __global__ void __launch_bounds__(256) k_task_entries(
     const int4 *__restrict__ tasks, const int *__restrict__ tcell_z, long long tcap,
-    float margin, float reach, const int4 *__restrict__ tri,
-    const int *__restrict__ point_inst, const int *__restrict__ tri_inst4,
+    float margin, const int *__restrict__ point_inst, const int *__restrict__ tri_inst4,
     const float4 *__restrict__ x, const float4 *__restrict__ p, const int2 *__restrict__ brange,
     const int4 *__restrict__ scell, const float4 *__restrict__ slo,
-    const float4 *__restrict__ shi, int2 *cand, long long cap, int *counters) {
+    const float4 *__restrict__ shi, int2 *pairs, long long cap, int *counters) {
     long long nt = counters[3];
     if (nt > tcap) nt = tcap;
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < nt;
@@ -491,26 +520,48 @@ __global__ void __launch_bounds__(256) k_task_entries(
             if (plx > th.x || phx < tl.x || ply > th.y || phy < tl.y || plz > th.z || phz < tl.z)
                 continue;
             if (point_inst && tri_inst4[sc.w] != inst) continue;
-            int4 fi = tri[sc.w];
-            if (fi.x == v || fi.y == v || fi.z == v) continue;
-            v3 xa = ld3(x[fi.x]), xb = ld3(x[fi.y]), xc = ld3(x[fi.z]);
-            v3 pa = ld3(p[fi.x]), pb = ld3(p[fi.y]), pc = ld3(p[fi.z]);
-            if (!sliver(xa, xb, xc) && !sliver(pa, pb, pc)) {
-                // lower bound of the point-triangle distance over the step
-                v3 D0 = sub3(P0, X0);
-                float d0 = point_tri_dist(X0, xa, xb, xc);
-                float d1 = point_tri_dist(P0, pa, pb, pc);
-                v3 ua = sub3(sub3(pa, xa), D0), ub = sub3(sub3(pb, xb), D0),
-                   uc = sub3(sub3(pc, xc), D0);
-                float U = sqrtf(fmaxf(fmaxf(dot3(ua, ua), dot3(ub, ub)), dot3(uc, uc)));
-                if ((d0 + d1 - U) * 0.5f > reach) continue;
-            }
-            long long slot = agg_inc(counters);
+            long long slot = agg_inc(counters + 4);
             if (slot < cap)
-                cand[slot] = make_int2(v, sc.w);
+                pairs[slot] = make_int2(v, sc.w);
             else
-                atomicOr(counters + 2, 1);
+                atomicOr(counters + 2, 16);
         }
+    }
+}
+
+// stage 3: one thread per AABB-overlapping pair: the point is not a vertex
+// of the triangle and a lower bound of the point-triangle distance over the
+// step is at most 4.5 h
+__global__ void __launch_bounds__(256) k_dist_filter(const int2 *__restrict__ pairs,
+                                                     long long pcap, float reach,
+                                                     const int4 *__restrict__ tri,
+                                                     const float4 *__restrict__ x,
+                                                     const float4 *__restrict__ p, int2 *cand,
+                                                     long long cap, int *counters) {
+    long long n = counters[4];
+    if (n > pcap) n = pcap;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x) {
+        int2 c = pairs[i];
+        int4 fi = tri[c.y];
+        if (fi.x == c.x || fi.y == c.x || fi.z == c.x) continue;
+        v3 X0 = ld3(x[c.x]), P0 = ld3(p[c.x]);
+        v3 xa = ld3(x[fi.x]), xb = ld3(x[fi.y]), xc = ld3(x[fi.z]);
+        v3 pa = ld3(p[fi.x]), pb = ld3(p[fi.y]), pc = ld3(p[fi.z]);
+        if (!sliver(xa, xb, xc) && !sliver(pa, pb, pc)) {
+            v3 D0 = sub3(P0, X0);
+            float d0 = point_tri_dist(X0, xa, xb, xc);
+            float d1 = point_tri_dist(P0, pa, pb, pc);
+            v3 ua = sub3(sub3(pa, xa), D0), ub = sub3(sub3(pb, xb), D0),
+               uc = sub3(sub3(pc, xc), D0);
+            float U = sqrtf(fmaxf(fmaxf(dot3(ua, ua), dot3(ub, ub)), dot3(uc, uc)));
+            if ((d0 + d1 - U) * 0.5f > reach) continue;
+        }
+        long long slot = agg_inc(counters);
+        if (slot < cap)
+            cand[slot] = c;
+        else
+            atomicOr(counters + 2, 1);
     }
 }
 
@@ -620,17 +671,12 @@ __global__ void __launch_bounds__(128) k_contact_deltas(const int *counters, con
     }
 }
 
-// each point of a contact: the first thread to claim it applies sum/count
-// and clears the sums
-__global__ void k_apply_deltas(const int *counters, const int4 *ids, long long *acc, int *acnt,
-                               float4 *p) {
-    int n = 4 * counters[1];
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        int4 id = ids[i >> 2];
-        int j = i & 3;
-        int pt = j == 0 ? id.x : j == 1 ? id.y : j == 2 ? id.z : id.w;
-        int cnt = atomicExch(acnt + pt, 0);
+// every point with a correction: p += sum * 2^-32 / count; sums cleared
+__global__ void k_apply_deltas(int n, long long *acc, int *acnt, float4 *p) {
+    for (int pt = blockIdx.x * blockDim.x + threadIdx.x; pt < n; pt += gridDim.x * blockDim.x) {
+        int cnt = acnt[pt];
         if (cnt <= 0) continue;
+        acnt[pt] = 0;
         long long sx = acc[3 * (long long)pt], sy = acc[3 * (long long)pt + 1],
                   sz = acc[3 * (long long)pt + 2];
         acc[3 * (long long)pt] = 0;
@@ -643,6 +689,27 @@ __global__ void k_apply_deltas(const int *counters, const int4 *ids, long long *
         P.z = P.z + (float)((double)sz * (1.0 / 4294967296.0) / dc);
         p[pt] = P;
     }
+}
+
+__global__ void k_vf_batch(int n, const float *x12, const float *p12, const float *th, int *hit,
+                           float *t, double *w, float *nrm) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    v3 X[4], P[4];
+    for (int j = 0; j < 4; ++j) {
+        X[j] = mk3(x12[12 * i + 3 * j], x12[12 * i + 3 * j + 1], x12[12 * i + 3 * j + 2]);
+        P[j] = mk3(p12[12 * i + 3 * j], p12[12 * i + 3 * j + 1], p12[12 * i + 3 * j + 2]);
+    }
+    VFResult r;
+    r.t = 0.f;
+    r.n = mk3(0.f, 0.f, 0.f);
+    r.w[0] = r.w[1] = r.w[2] = r.w[3] = 0.0;
+    hit[i] = extended_vf_test(X, P, th[i], r) ? 1 : 0;
+    t[i] = r.t;
+    for (int k = 0; k < 4; ++k) w[4 * i + k] = r.w[k];
+    nrm[3 * i] = r.n.x;
+    nrm[3 * i + 1] = r.n.y;
+    nrm[3 * i + 2] = r.n.z;
 }
 
 int bits_for(long long maxval) {
@@ -694,6 +761,7 @@ static int colli_alloc(pbd_colli *c) {
     pbd_object *o = c->obj;
     PBD_TRY(c->cand.alloc(c->cand_cap));
     PBD_TRY(c->tasks.alloc(c->task_cap));
+    PBD_TRY(c->pairs.alloc(c->task_cap));
     PBD_TRY(c->tasks_z.alloc(c->task_cap));
     PBD_TRY(c->counters.alloc(8));
     size_t H = (size_t)c->contact_cap;
@@ -733,10 +801,13 @@ int ccd_detect(pbd_colli *c) {
         c->counters.p);
     PBD_LAUNCH();
     k_task_entries<<<kPersistentBlocks, 256, 0, s>>>(
-        c->tasks.p, c->tasks_z.p, c->task_cap, margin, reach, o->tri.p,
-        o->has_inst ? o->point_inst.p : nullptr,
+        c->tasks.p, c->tasks_z.p, c->task_cap, margin, o->has_inst ? o->point_inst.p : nullptr,
         o->has_inst ? o->tri_inst.p : nullptr, o->x.p, o->p.p, h->brange.p, h->scell.p,
-        h->slo.p, h->shi.p, c->cand.p, c->cand_cap, c->counters.p);
+        h->slo.p, h->shi.p, c->pairs.p, c->task_cap, c->counters.p);
+    PBD_LAUNCH();
+    k_dist_filter<<<kPersistentBlocks, 256, 0, s>>>(c->pairs.p, c->task_cap, reach, o->tri.p,
+                                                    o->x.p, o->p.p, c->cand.p, c->cand_cap,
+                                                    c->counters.p);
     PBD_LAUNCH();
     k_narrow<<<kPersistentBlocks, 128, 0, s>>>(c->cand.p, c->cand_cap, o->nt, th, o->tri.p,
                                                o->x.p, o->p.p, c->counters.p, c->contact_cap,
@@ -755,8 +826,7 @@ int ccd_resolve(pbd_colli *c, int passes) {
                                                            c->thickness,
                                                            c->response == PBD_RESPONSE_MASS_WEIGHTED,
                                                            c->acc.p, c->acnt.p);
-        k_apply_deltas<<<kPersistentBlocks, 256, 0, s>>>(c->counters.p, c->cids.p, c->acc.p,
-                                                         c->acnt.p, o->p.p);
+        k_apply_deltas<<<grid_for(o->n, 256), 256, 0, s>>>(o->n, c->acc.p, c->acnt.p, o->p.p);
         PBD_LAUNCH();
     }
     return PBD_OK;
@@ -1055,6 +1125,35 @@ int pbd_colli_get_contacts(pbd_colli *c, int *ids, int *face, float *t, double *
             w[4 * k + 3] = hw[i].w;
         }
     }
+    return PBD_OK;
+}
+
+int pbd_ccd_vf_test_batch(const float *x12, const float *p12, const float *thickness, int n,
+                          int *hit, float *t, double *w, float *nrm) {
+    PBD_CHECK(x12 && p12 && thickness && hit && t && w && nrm && n >= 0, PBD_ERR_ARG,
+              "null argument");
+    if (n == 0) return PBD_OK;
+    cudaStream_t s = nullptr;
+    PBD_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+    DBuf<float> dx, dp, dth, dt, dn;
+    DBuf<int> dh;
+    DBuf<double> dw;
+    int r = PBD_OK;
+    if ((r = dx.upload(x12, 12 * (size_t)n, s)) || (r = dp.upload(p12, 12 * (size_t)n, s)) ||
+        (r = dth.upload(thickness, n, s)) || (r = dh.alloc(n)) || (r = dt.alloc(n)) ||
+        (r = dw.alloc(4 * (size_t)n)) || (r = dn.alloc(3 * (size_t)n))) {
+        cudaStreamDestroy(s);
+        return r;
+    }
+    k_vf_batch<<<grid_for(n, 128), 128, 0, s>>>(n, dx.p, dp.p, dth.p, dh.p, dt.p, dw.p, dn.p);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaMemcpyAsync(hit, dh.p, sizeof(int) * n, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(t, dt.p, sizeof(float) * n, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(w, dw.p, sizeof(double) * 4 * n, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(nrm, dn.p, sizeof(float) * 3 * n, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    cudaStreamDestroy(s);
+    PBD_CUDA(e);
     return PBD_OK;
 }
 

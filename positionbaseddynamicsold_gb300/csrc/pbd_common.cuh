@@ -196,8 +196,10 @@ struct pbd_colli {
     // cell tasks (point, bucket, cell) and candidates (point, triangle)
     pbd::DBuf<int4> tasks;
     pbd::DBuf<int> tasks_z;
+    pbd::DBuf<int2> pairs;      // AABB-overlapping (point, triangle)
     pbd::DBuf<int2> cand;
-    pbd::DBuf<int> counters;    // [0] candidates, [1] contacts, [2] overflow flags, [3] tasks
+    pbd::DBuf<int> counters;    // [0] candidates, [1] contacts, [2] overflow flags, [3] tasks,
+                                // [4] AABB pairs
     // contacts, in the order the narrow phase found them
     pbd::DBuf<int4> cids;               // i0..i3
     pbd::DBuf<int> cface;

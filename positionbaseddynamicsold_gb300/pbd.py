@@ -63,6 +63,7 @@ EXPORTS = [
     "pbd_colli_set_acce_struct", "pbd_colli_set_thickness", "pbd_colli_set_iterations",
     "pbd_colli_set_response", "pbd_colli_set_capacity", "pbd_colli_ccd_sh_extended",
     "pbd_colli_collision_resolve_new", "pbd_colli_get_contacts", "pbd_colli_stats",
+    "pbd_ccd_vf_test_batch",
     "pbd_residual_noalloc",
 ]
 
@@ -480,3 +481,19 @@ def residual_noalloc(d_pos4, n_points, d_dist_idx, d_rest_length, n_dist, d_bend
     _check(L.pbd_residual_noalloc(d_pos4, n_points, d_dist_idx or None, d_rest_length or None,
                                   n_dist, d_bend_idx or None, d_rest_angle or None,
                                   d_hinge_rest or None, n_bend, d_out, stream or None))
+
+
+def vf_test_batch(X, P, thickness):
+    """pbd_ccd_vf_test_batch: ExtendedVFTest on n (point, triangle) cases.
+    X, P: (n, 4, 3) start / predicted positions; thickness: (n,)."""
+    L = load()
+    X = np.ascontiguousarray(X, np.float32).reshape(-1, 12)
+    P = np.ascontiguousarray(P, np.float32).reshape(-1, 12)
+    th = np.ascontiguousarray(thickness, np.float32)
+    n = len(X)
+    hit = np.zeros(n, np.int32)
+    t = np.zeros(n, np.float32)
+    w = np.zeros((n, 4), np.float64)
+    nrm = np.zeros((n, 3), np.float32)
+    _check(L.pbd_ccd_vf_test_batch(_p(X), _p(P), _p(th), n, _p(hit), _p(t), _p(w), _p(nrm)))
+    return hit, t, w, nrm

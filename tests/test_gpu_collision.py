@@ -67,6 +67,21 @@ def test_ccd_hit_set_matches_reference(golden, hashed):
     assert (np.diff(key) > 0).all()
 
 
+def test_vf_test_batch_matches_reference(golden):
+    """ExtendedVFTest on the GPU (with its exact early exits) against the
+    reference's own outputs on 1,500 random near-contact configurations:
+    hit, time, barycentric weights and normal bit for bit (the reference's
+    powf-spelled edge lengths only enter the inside test's epsilon)."""
+    from positionbaseddynamicsold_gb300.pbd import vf_test_batch
+    g = golden("vf_cases")
+    hit, t, w, n = vf_test_batch(g["X"], g["P"], g["thickness"])
+    np.testing.assert_array_equal(hit, g["hit"])
+    h = hit.astype(bool)
+    np.testing.assert_array_equal(t[h], g["t"][h])
+    np.testing.assert_array_equal(w[h], g["w"][h])
+    np.testing.assert_array_equal(n[h], g["n"][h])
+
+
 def test_ccd_matches_oracle_pairs(orc, golden):
     g = golden("ccd")
     obj, cs = ccd_gpu(g)
