@@ -364,22 +364,41 @@ __device__ __forceinline__ void project_anchor(float4 a, const Pos &p) {
     p.st(i, make_float4(a.x, a.y, a.z, p.ld(i).w));
 }
 
-// one color phase: distance, then bending, then anchor records of the color
+// one color phase: distance, then bending, then anchor records of the color.
+// Launched with programmatic stream serialization: the records (which no
+// phase writes) are loaded first, the next phase is allowed to launch, and
+// positions are touched only after griddepcontrol.wait, i.e. after the
+// previous phase has completed and its writes are visible.
 __global__ void __launch_bounds__(256) k_project_color(const int4 *__restrict__ drec, int nd,
                                                        const int4 *__restrict__ bidx,
                                                        const float2 *__restrict__ bpar, int nb,
                                                        const float4 *__restrict__ arec, int na,
                                                        float4 *__restrict__ p, float expk) {
     int t = blockIdx.x * blockDim.x + threadIdx.x;
-    GlobalPos P{p};
+    int4 r = make_int4(0, 0, 0, 0);
+    float2 bp = make_float2(0.f, 0.f);
+    float4 ar = make_float4(0.f, 0.f, 0.f, 0.f);
+    int kind = 0;
     if (t < nd) {
-        project_distance(drec[t], P, expk);
+        r = drec[t];
+        kind = 1;
     } else if (t < nd + nb) {
-        int j = t - nd;
-        project_bending(bidx[j], bpar[j], P, expk);
+        r = bidx[t - nd];
+        bp = bpar[t - nd];
+        kind = 2;
     } else if (t < nd + nb + na) {
-        project_anchor(arec[t - nd - nb], P);
+        ar = arec[t - nd - nb];
+        kind = 3;
     }
+    asm volatile("griddepcontrol.launch_dependents;");
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    GlobalPos P{p};
+    if (kind == 1)
+        project_distance(r, P, expk);
+    else if (kind == 2)
+        project_bending(r, bp, P, expk);
+    else if (kind == 3)
+        project_anchor(ar, P);
 }
 
 // ColliWithShpGrd (P/PBD_cuda.cu:1519-1573) on one point
@@ -592,11 +611,19 @@ static int launch_sweep_per_color(pbd_object *o, int iter) {
         int a0 = o->h_aseg[c], na = o->h_aseg[c + 1] - a0;
         int tot = nd + nb + na;
         if (!tot) continue;
-        k_project_color<<<grid_for(tot, 256), 256, 0, o->stream>>>(
-            o->drec.p + d0, nd, o->bidx.p + b0, o->bpar.p + b0, nb, o->arec.p + a0, na, o->p.p,
-            expk);
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3(grid_for(tot, 256));
+        cfg.blockDim = dim3(256);
+        cfg.stream = o->stream;
+        cudaLaunchAttribute at[1];
+        at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+        at[0].val.programmaticStreamSerializationAllowed = 1;
+        cfg.attrs = at;
+        cfg.numAttrs = 1;
+        PBD_CUDA(cudaLaunchKernelEx(&cfg, k_project_color, (const int4 *)(o->drec.p + d0), nd,
+                                    (const int4 *)(o->bidx.p + b0), (const float2 *)(o->bpar.p + b0),
+                                    nb, (const float4 *)(o->arec.p + a0), na, o->p.p, expk));
     }
-    PBD_LAUNCH();
     return PBD_OK;
 }
 
