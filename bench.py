@@ -1,7 +1,7 @@
 """Throughput of the PBD cloth step on GB300.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--workload drape256|fold1024|hanging32]
+                    [--workload drape256|fold1024|batch512|hanging32]
 
 Workload (default, drape256): a 256x256 cloth (2 m x 2 m, 130,050 triangles,
 195,585 distance + 194,565 bending constraints) released flat at y = 0.5
@@ -69,6 +69,16 @@ def make_workload(name):
         sc = scenes.folding_cloth(res=1024, seed=0)
         cfg = {"workload": "fold1024: 1024x1024 cloth dropped onto a ground plane, self CCD",
                "grid": 1024, "substep_dt": DT, "gs_iterations": ITERS,
+               "ccd_passes_per_substep": 3, "hash_buckets": 2 ** 24, "thickness": 1e-3,
+               "cell": sc["colli"]["cell"]}
+        return sc, cfg, True, 24
+    if name == "batch512":
+        sc = scenes.batched_cloths(512, seed=0)
+        sc["colli"] = {"cell": 2.0 * scenes.mean_rest_edge(sc), "thickness": 1e-3,
+                       "spheres": sc["spheres"]}
+        cfg = {"workload": "batch512: 512 cloths, side U{16..128}, random pins, one sphere each, "
+                           "self CCD per instance, all in one launch per color phase",
+               "instances": 512, "substep_dt": DT, "gs_iterations": ITERS,
                "ccd_passes_per_substep": 3, "hash_buckets": 2 ** 24, "thickness": 1e-3,
                "cell": sc["colli"]["cell"]}
         return sc, cfg, True, 24
@@ -144,6 +154,8 @@ def setup(sc, colli_on, table_log2):
         cs.set_capacity(max(1 << 22, 64 * n), max(1 << 20, 4 * n))
         if "ground" in sc["colli"]:
             solver.set_ground(True, sc["colli"]["ground"])
+        if "spheres" in sc["colli"]:
+            solver.set_instance_spheres(sc["colli"]["spheres"])
     return obj, solver, shs, cs
 
 
@@ -371,7 +383,8 @@ def main():
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="drape256", choices=["drape256", "fold1024", "hanging32"])
+    ap.add_argument("--workload", default="drape256", choices=["drape256", "fold1024", "batch512",
+                                                          "hanging32"])
     ap.add_argument("--preroll", type=int, default=120)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--gs-path", default="auto", choices=["auto", "per-color", "cluster"])

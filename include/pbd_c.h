@@ -152,6 +152,11 @@ int pbd_solver_integration(pbd_solver *s, float dt);
  * fixed unit sphere, tolerance 0.001) and the ground plane CollideGround. */
 int pbd_solver_set_sphere(pbd_solver *s, int enable, const float *center, float radius);
 int pbd_solver_set_ground(pbd_solver *s, int enable, float height);
+/* one analytic sphere per instance of a batched object (n spheres, 4 floats
+ * each: centre xyz, radius), applied like the sphere above to every point of
+ * the instance after each GS iteration; n = 0 removes them.  No reference
+ * counterpart (the reference simulates one object). */
+int pbd_solver_set_instance_spheres(pbd_solver *s, int n, const float *spheres4);
 /* whole substeps: Advect, ProjectConstraint[WithColli], Integration, repeated
  * `substeps` times; recorded into a CUDA graph on first use (use_graph=1)
  * and replayed.  colli may be NULL. */

@@ -289,8 +289,11 @@ struct GridParams {
 __device__ __forceinline__ bool outside(const GridParams &g, int x, int y, int z) {
     return x < 0 || y < 0 || z < 0 || x >= g.size.x || y >= g.size.y || z >= g.size.z;
 }
-__device__ __forceinline__ uint32_t bucket_of(const GridParams &g, int x, int y, int z) {
-    if (g.hashed) return teschner(x, y, z) & (g.nb - 1u);
+// bucket of a cell; in hashed mode the instance is mixed in, so instances
+// that overlap in space (batched cloths) do not share buckets
+__device__ __forceinline__ uint32_t bucket_of(const GridParams &g, int x, int y, int z,
+                                              int inst) {
+    if (g.hashed) return (teschner(x, y, z) ^ ((uint32_t)inst * 0x9E3779B1u)) & (g.nb - 1u);
     return ((uint32_t)z * (uint32_t)g.size.y) * (uint32_t)g.size.x +
            (uint32_t)y * (uint32_t)g.size.x + (uint32_t)x;
 }
@@ -335,7 +338,7 @@ __global__ void __launch_bounds__(256) k_tri_cells(int nt, GridParams g, float m
         int iz = (int)floorf((cz - g.start.z) / g.cell.z);
         valid = g.hashed || !outside(g, ix, iy, iz);
         tcell[t] = make_int4(ix, iy, iz, f.w);
-        key[t] = valid ? bucket_of(g, ix, iy, iz) : g.nb;
+        key[t] = valid ? bucket_of(g, ix, iy, iz, f.w) : g.nb;
         id[t] = t;
         v3 xa = ld3(x[f.x]), xb = ld3(x[f.y]), xc = ld3(x[f.z]);
         if (sliver(a, b, c) || sliver(xa, xb, xc)) {
@@ -397,7 +400,7 @@ __global__ void k_find_neighbors(int nt, GridParams g, const int4 *tcell, const 
                 for (int x = -1; x <= 1; ++x) {
                     int nx = c.x + x, ny = c.y + y, nz = c.z + z;
                     if (!g.hashed && outside(g, nx, ny, nz)) continue;
-                    int2 r = brange[bucket_of(g, nx, ny, nz)];
+                    int2 r = brange[bucket_of(g, nx, ny, nz, c.w)];
                     for (int i = r.x; i < r.y; ++i) {
                         int4 sc = scell[i];
                         if (sc.x != nx || sc.y != ny || sc.z != nz) continue;
@@ -419,7 +422,8 @@ constexpr int kTaskWarps = 8;
 __global__ void __launch_bounds__(32 * kTaskWarps) k_cell_tasks(
     int n, GridParams g, float margin, const int *__restrict__ pt_first,
     const int *__restrict__ pt_last, const int *__restrict__ pt_tri,
-    const float4 *__restrict__ x, const float4 *__restrict__ p, const int4 *__restrict__ tcell,
+    const int *__restrict__ point_inst, const float4 *__restrict__ x,
+    const float4 *__restrict__ p, const int4 *__restrict__ tcell,
     const int2 *__restrict__ brange, const float4 *__restrict__ blo,
     const float4 *__restrict__ bhi, int4 *tasks, int *tcell_z, long long cap, int *counters) {
     const int lane = threadIdx.x & 31;
@@ -432,6 +436,7 @@ __global__ void __launch_bounds__(32 * kTaskWarps) k_cell_tasks(
             if (lane == 0) atomicOr(counters + 2, 4);
             ninc = kMaxInc;
         }
+        const int inst = point_inst ? point_inst[v] : 0;
         int4 mc = make_int4(0, 0, 0, 0);
         bool valid = false;
         if (lane < ninc) {
@@ -474,7 +479,7 @@ __global__ void __launch_bounds__(32 * kTaskWarps) k_cell_tasks(
             }
             if (!near) continue;
             if (!g.hashed && outside(g, xx, y, z)) continue;
-            uint32_t b = bucket_of(g, xx, y, z);
+            uint32_t b = bucket_of(g, xx, y, z, inst);
             int2 r = brange[b];
             if (r.x >= r.y) continue;
             float4 bl = blo[b], bh = bhi[b];
@@ -796,8 +801,9 @@ int ccd_detect(pbd_colli *c) {
     float margin = 5.5f * th + 2e-6f;
     float reach = 4.5f * th + 2e-6f;
     k_cell_tasks<<<grid_for((long long)o->n * 32, 32 * kTaskWarps), 32 * kTaskWarps, 0, s>>>(
-        o->n, g, margin, o->pt_tri_first.p, o->pt_tri_last.p, o->pt_tri.p, o->x.p, o->p.p,
-        h->tcell.p, h->brange.p, h->blo.p, h->bhi.p, c->tasks.p, c->tasks_z.p, c->task_cap,
+        o->n, g, margin, o->pt_tri_first.p, o->pt_tri_last.p, o->pt_tri.p,
+        o->has_inst ? o->point_inst.p : nullptr, o->x.p, o->p.p, h->tcell.p, h->brange.p,
+        h->blo.p, h->bhi.p, c->tasks.p, c->tasks_z.p, c->task_cap,
         c->counters.p);
     PBD_LAUNCH();
     k_task_entries<<<kPersistentBlocks, 256, 0, s>>>(

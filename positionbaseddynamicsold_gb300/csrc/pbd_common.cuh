@@ -219,6 +219,9 @@ struct pbd_solver {
     float sphere_r = 1.0f;
     int ground_on = 0;
     float ground_h = 0.0f;
+    // one analytic sphere per instance (cx, cy, cz, r), indexed by point_inst
+    pbd::DBuf<float4> inst_spheres;
+    int n_inst_spheres = 0;
     // cached graph of pbd_solver_step
     cudaGraphExec_t gexec = nullptr;
     float g_dt = 0;

@@ -512,6 +512,18 @@ __global__ void k_obstacles(int n, float4 *p, int sphere_on, float3 c, float r, 
     p[i] = obstacle_point(p[i], sphere_on, c, r, ground_on, gh);
 }
 
+// the sphere of each point's instance (ColliWithShpGrd's sphere push with a
+// per-instance centre and radius)
+__global__ void k_obstacles_inst(int n, float4 *p, const int *point_inst, const float4 *spheres,
+                                 int n_spheres) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    int k = point_inst[i];
+    if (k < 0 || k >= n_spheres) return;
+    float4 sp = spheres[k];
+    p[i] = obstacle_point(p[i], 1, make_float3(sp.x, sp.y, sp.z), sp.w, 0, 0.f);
+}
+
 // residual: FP64 per constraint, warp-shuffle + block reduction
 __device__ __forceinline__ double warp_sum(double v) {
 #pragma unroll
@@ -739,6 +751,7 @@ static int cluster_plan(pbd_object *o) {
 // against 8.5 us per phase for the cluster form)
 static int resolved_path(pbd_solver *s) {
     if (s->gs_path != PBD_GS_CLUSTER) return PBD_GS_PER_COLOR;
+    if (s->n_inst_spheres > 0) return -2;  // per-instance spheres: per-color form only
     if (cluster_plan(s->obj) != PBD_OK) return -1;
     return s->obj->cl_state == 1 ? PBD_GS_CLUSTER : -2;
 }
@@ -784,12 +797,19 @@ int launch_sweeps(pbd_solver *s, int it0, int it1, bool obstacles_inside) {
 }
 
 int launch_obstacles(pbd_solver *s) {
-    if (!s->sphere_on && !s->ground_on) return PBD_OK;
     pbd_object *o = s->obj;
-    k_obstacles<<<grid_for(o->n, 256), 256, 0, o->stream>>>(
-        o->n, o->p.p, s->sphere_on, make_float3(s->sphere_c[0], s->sphere_c[1], s->sphere_c[2]),
-        s->sphere_r, s->ground_on, s->ground_h);
-    PBD_LAUNCH();
+    if (s->sphere_on || s->ground_on) {
+        k_obstacles<<<grid_for(o->n, 256), 256, 0, o->stream>>>(
+            o->n, o->p.p, s->sphere_on,
+            make_float3(s->sphere_c[0], s->sphere_c[1], s->sphere_c[2]), s->sphere_r,
+            s->ground_on, s->ground_h);
+        PBD_LAUNCH();
+    }
+    if (s->n_inst_spheres > 0 && o->has_inst) {
+        k_obstacles_inst<<<grid_for(o->n, 256), 256, 0, o->stream>>>(
+            o->n, o->p.p, o->point_inst.p, s->inst_spheres.p, s->n_inst_spheres);
+        PBD_LAUNCH();
+    }
     return PBD_OK;
 }
 
@@ -1438,6 +1458,15 @@ int pbd_solver_set_ground(pbd_solver *s, int on, float h) {
     return PBD_OK;
 }
 
+int pbd_solver_set_instance_spheres(pbd_solver *s, int n, const float *spheres4) {
+    PBD_CHECK(s && s->obj && n >= 0 && (n == 0 || spheres4), PBD_ERR_ARG, "bad argument");
+    PBD_CHECK(n == 0 || s->obj->has_inst, PBD_ERR_STATE, "the target object has no instances");
+    if (n > 0) PBD_TRY(s->inst_spheres.upload((const float4 *)spheres4, n, s->obj->stream));
+    PBD_CUDA(cudaStreamSynchronize(s->obj->stream));
+    s->n_inst_spheres = n;
+    return PBD_OK;
+}
+
 static int project_with_colli(pbd_solver *s, int iterations, pbd_colli *c) {
     if (!c) return iterations > 0 ? launch_sweeps(s, 0, iterations, true) : PBD_OK;
     for (int ii = 0; ii < iterations; ++ii) {
@@ -1473,6 +1502,7 @@ int pbd_solver_step(pbd_solver *s, float dt, int substeps, int iterations, pbd_c
     PBD_CHECK(!c || c->obj == s->obj, PBD_ERR_ARG, "collision solver targets another object");
     if (!use_graph) return record_steps(s, dt, substeps, iterations, c);
     int sig = s->sphere_on * 3 + s->ground_on * 7 + (c ? c->response * 11 + c->iterations * 13 : 0) +
+              (s->n_inst_spheres > 0) * 17 +
               s->gs_path * 1009;
     if (s->gexec && (s->g_dt != dt || s->g_sub != substeps || s->g_it != iterations ||
                      s->g_colli != c || s->g_sig != sig)) {

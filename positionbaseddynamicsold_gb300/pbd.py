@@ -55,6 +55,7 @@ EXPORTS = [
     "pbd_solver_destroy", "pbd_solver_set_target", "pbd_solver_advect",
     "pbd_solver_project_constraint", "pbd_solver_project_constraint_with_colli",
     "pbd_solver_integration", "pbd_solver_set_sphere", "pbd_solver_set_ground",
+    "pbd_solver_set_instance_spheres",
     "pbd_solver_step", "pbd_solver_set_gs_path", "pbd_solver_get_gs_path",
     "pbd_solver_graph_kernels", "pbd_shs_create", "pbd_shs_create_hashed", "pbd_shs_destroy",
     "pbd_shs_set_grid_center", "pbd_shs_set_grid_size", "pbd_shs_set_division", "pbd_shs_init",
@@ -455,6 +456,14 @@ class SolverPBD:
 
     def set_ground(self, enable, height=0.0):
         _check(self.L.pbd_solver_set_ground(self.h, int(enable), height))
+
+    def set_instance_spheres(self, spheres):
+        """spheres: (n_instances, 4) centre xyz + radius, or None."""
+        if spheres is None or len(spheres) == 0:
+            _check(self.L.pbd_solver_set_instance_spheres(self.h, 0, None))
+            return
+        a = np.ascontiguousarray(spheres, np.float32).reshape(-1, 4)
+        _check(self.L.pbd_solver_set_instance_spheres(self.h, len(a), _p(a)))
 
     def set_gs_path(self, path):
         _check(self.L.pbd_solver_set_gs_path(self.h, int(path)))
