@@ -258,6 +258,86 @@ int pbd_residual_noalloc(const float *d_pos4, int n_points, const int *d_dist_id
                          const float *d_rest_angle, const float *d_hinge_rest, int n_bend,
                          double *d_out, void *stream);
 
+/* ---- substeps solved to a residual target --------------------------------- */
+/* No counterpart in the reference (its substeps run a fixed iteration count,
+ * P/PBD_cuda.cu:1308-1435).  The stopping test uses the relative stretch
+ * residual sqrt(sum C^2)/sqrt(sum l^2) over the distance constraints
+ * (C = |p_a - p_b| - l), FP64. */
+int pbd_constraints_residual_stretch(pbd_object *obj, double *residual);
+
+typedef struct pbd_solve_stats {
+    long long substeps;     /* substeps solved since the last reset            */
+    long long sweeps;       /* GS sweeps they ran                              */
+    long long reached;      /* substeps that ended at or below the target      */
+    long long reverts;      /* warm starts rejected because the residual rose  */
+    double last_residual;   /* residual at the end of the last substep's loop  */
+    int last_sweeps;        /* sweeps of the last substep                      */
+    double last_r0, last_r1;/* warm start guard of the last substep: residual
+                               of the advected positions / after prediction   */
+} pbd_solve_stats;
+
+/* `substeps` substeps, each: Advect; [warm start]; colored GS sweeps in
+ * chunks of `chunk` (1..32) until the stretch residual is <= target or
+ * another chunk would exceed max_sweeps; with colli, a CCD detection starts
+ * every chunk, every sweep is followed by the contact response and the
+ * analytic obstacles, and the loop ends with one more detection + response;
+ * the correction p - p_advected is kept (the warm start's feature);
+ * Integration.  Sweep i uses the stiffness exponent 1/(i+1)
+ * (P/PBD_cuda.cu:1282).  use_graph = 1 captures the substeps in a CUDA
+ * graph whose WHILE nodes run the loop on the device (no host round trip);
+ * use_graph = 0 runs the same kernels and reads the loop condition on the
+ * host after each chunk. */
+int pbd_solver_step_to_residual(pbd_solver *s, float dt, int substeps, pbd_colli *colli,
+                                double target, int max_sweeps, int chunk, int use_graph);
+int pbd_solver_solve_stats(pbd_solver *s, pbd_solve_stats *stats, int reset);
+/* kernel nodes of the cached pbd_solver_step_to_residual graph, each WHILE
+ * body counted once */
+int pbd_solver_residual_graph_kernels(pbd_solver *s, long long *n);
+/* the correction p_final - p_advected of the last solved substep, 3 per point */
+int pbd_object_get_correction(pbd_object *obj, float *corr3);
+
+/* ---- learned warm start ---------------------------------------------------- */
+/* No counterpart in the reference.  A per-point MLP 16 -> 64 -> 64 -> 3 (SiLU)
+ * predicts the correction the sweeps will apply to the advected positions,
+ * in units of the point's mean incident rest length, from 16 features:
+ * strains of the first six incident distance constraints, the previous
+ * substep's correction, an inverse-mass share, a pinned flag, the dihedral
+ * deviations of the first four incident bending constraints and a constant 1.
+ * BF16 operands on the tensor cores, FP32 accumulation, FP32 master
+ * parameters trained with Adam.  Parameter vector (pbd_warmstart_num_params
+ * floats): W1[64][16] (column 15 acts on the constant feature), W2[64][64],
+ * b2[64], W3[3][64], b3[3]. */
+typedef struct pbd_warmstart pbd_warmstart;
+int pbd_warmstart_num_params(void);
+int pbd_warmstart_create(pbd_warmstart **out);          /* parameters zero    */
+int pbd_warmstart_destroy(pbd_warmstart *w);
+int pbd_warmstart_set_params(pbd_warmstart *w, const float *params, int n);  /* resets Adam */
+int pbd_warmstart_get_params(pbd_warmstart *w, float *params, int n);
+/* network outputs y (3 per row) of n feature rows x (16 floats each, rounded
+ * to BF16; column 15 taken as 1) */
+int pbd_warmstart_forward(pbd_warmstart *w, const float *x, int n, float *y);
+/* gradient of L = 1/(2 m) sum_{rows with mask != 0} |y - t|^2 (m = rows with
+ * mask != 0; mask NULL = all rows) with respect to the parameter vector, and L */
+int pbd_warmstart_gradients(pbd_warmstart *w, const float *x, const float *t, const float *mask,
+                            int n, float *grad, double *loss);
+/* load a gradient (for checking the optimizer) / one Adam step on the
+ * current gradient, which is then cleared */
+int pbd_warmstart_set_gradient(pbd_warmstart *w, const float *grad, int n);
+int pbd_warmstart_adam(pbd_warmstart *w, float lr, float beta1, float beta2, float eps);
+/* training on solver trajectories: call pbd_warmstart_record right after
+ * Advect (features of the advected positions), solve the substep, then
+ * pbd_warmstart_train_step: targets = (p - p_advected)/lbar for the free
+ * points, one forward/backward pass over every point of the object and one
+ * Adam step (beta 0.9 / 0.999, eps 1e-8); loss may be NULL (no sync). */
+int pbd_warmstart_record(pbd_warmstart *w, pbd_object *obj);
+int pbd_warmstart_train_step(pbd_warmstart *w, pbd_object *obj, float lr, double *loss);
+/* features (16 floats per point, BF16 values) of the object's predicted positions */
+int pbd_warmstart_features(pbd_warmstart *w, pbd_object *obj, float *x);
+/* apply the prediction to the object's predicted positions (test hook) */
+int pbd_warmstart_predict(pbd_warmstart *w, pbd_object *obj);
+/* use the network in pbd_solver_step_to_residual (NULL = plain sweeps) */
+int pbd_solver_set_warmstart(pbd_solver *s, pbd_warmstart *w);
+
 #ifdef __cplusplus
 }
 #endif

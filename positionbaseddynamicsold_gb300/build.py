@@ -24,6 +24,8 @@ SOURCES = {
     "pbd_object.cu": ["-fmad=false"],
     "pbd_collision.cu": ["-fmad=false"],
     "pbd_noalloc.cu": [],
+    "pbd_mlp.cu": [],
+    "pbd_solve.cu": [],
 }
 HEADERS = ["pbd_common.cuh"]
 

@@ -153,9 +153,32 @@ struct pbd_object {
     pbd::DBuf<int> cdseg, cbseg, caseg;
     // residual
     double res_den = 0.0;
+    double res_den_d = 0.0;                 // distance constraints only
     pbd::DBuf<double> res_part;
     pbd::DBuf<double> res_out;
     pbd::SortScratch scr;
+    // host copies of the constraint topology (per-point stencils are built
+    // from them on first use)
+    std::vector<int> h_prim_list, h_indices;
+    std::vector<float> h_rest_length;
+    // predicted positions right after advect, and the correction the last
+    // solved substep applied to them (p_final - p_after_advect, w = 0)
+    pbd::DBuf<float4> p0, dprev;
+    // prim id of every bending record (record order)
+    pbd::DBuf<int> bend_prim;
+    // per prim: wrapped dihedral deviation theta - theta0 (bending prims)
+    pbd::DBuf<float> theta;
+    // per-point stencil of the warm-start features: other points of the
+    // first six incident distance constraints, prim ids of the first four
+    // incident bending constraints (both by prim id, -1 = none), their rest
+    // lengths, the mean incident rest length and the inverse-mass feature
+    pbd::DBuf<int4> fnb_a, fnb_b;           // (n0..n3), (n4, n5, h0, h1)
+    pbd::DBuf<int2> fnb_c;                  // (h2, h3)
+    pbd::DBuf<float4> frest_a, frest_b;     // (r0..r3), (r4, r5, lbar, wrel)
+    int n_free = 0;                         // points with nonzero inverse mass
+    bool feat_built = false;
+    // color phases launched with programmatic dependent launch
+    bool pdl = true;
 };
 
 struct pbd_shs {
@@ -211,8 +234,36 @@ struct pbd_colli {
     pbd::DBuf<int> acnt;
 };
 
+// Device state of the solve-to-residual loop (one per solver).
+namespace pbd {
+constexpr int kMaxChunk = 32;
+struct LoopState {
+    double r;             // residual after the last check
+    double r_prev;        // residual at the check before
+    double r0;            // warm start guard: residual of the advected positions
+    double r1;            // warm start guard: residual after the prediction
+    int sweeps;           // sweeps of the current substep's solve
+    int revert;           // the current substep's prediction was rejected
+    int cont;             // loop condition (also set on the graph's handle)
+    int pad;
+    long long substeps, total_sweeps, reached, reverts;
+    float expk[kMaxChunk];  // 1/(sweep+1) of the next chunk's sweeps
+};
+}  // namespace pbd
+
+struct pbd_warmstart;
+
 struct pbd_solver {
     pbd_object *obj = nullptr;
+    pbd_warmstart *ws = nullptr;
+    pbd::DBuf<pbd::LoopState> loop;
+    // cached graph of pbd_solver_step_to_residual
+    cudaGraphExec_t rexec = nullptr;
+    float r_dt = 0;
+    int r_sub = 0, r_max = 0, r_chunk = 0, r_sig = 0;
+    double r_target = 0;
+    pbd_colli *r_colli = nullptr;
+    long long r_kernels = 0;
     int gs_path = 0;  // PBD_GS_AUTO / PER_COLOR / CLUSTER
     int sphere_on = 0;
     float sphere_c[3] = {0, 0, 0};
@@ -231,11 +282,60 @@ struct pbd_solver {
     long long g_kernels = 0;
 };
 
+// Learned warm start: per-point MLP 16 -> 64 -> 64 -> 3 (SiLU), BF16
+// operands on the tensor cores, FP32 accumulate; FP32 master parameters
+// with Adam moments.
+namespace pbd {
+constexpr int kWsIn = 16, kWsHid = 64, kWsOut = 3;
+// packed FP32 parameters: W1[64][16] (column 15 multiplies the constant
+// feature, i.e. it is the first layer's bias), W2[64][64], b2[64],
+// W3[3][64], b3[3]
+constexpr int kWsOffW1 = 0;
+constexpr int kWsOffW2 = kWsOffW1 + kWsHid * kWsIn;
+constexpr int kWsOffB2 = kWsOffW2 + kWsHid * kWsHid;
+constexpr int kWsOffW3 = kWsOffB2 + kWsHid;
+constexpr int kWsOffB3 = kWsOffW3 + kWsOut * kWsHid;
+constexpr int kWsParams = kWsOffB3 + kWsOut;
+// BF16 operand tiles in the tensor cores' K-major core-matrix layout
+// (element offsets into one buffer)
+constexpr int kWtW1 = 0;                     // B [64 x 16]
+constexpr int kWtW2 = kWtW1 + 64 * 16;       // B [64 x 64]
+constexpr int kWtW3 = kWtW2 + 64 * 64;       // B [16 x 64], rows 3..15 zero
+constexpr int kWtW3T = kWtW3 + 16 * 64;      // B [64 x 16], columns 3..15 zero
+constexpr int kWtW2T = kWtW3T + 64 * 16;     // B [64 x 64]
+constexpr int kWtTotal = kWtW2T + 64 * 64;
+}  // namespace pbd
+
+struct pbd_warmstart {
+    cudaStream_t own = nullptr;          // for calls not tied to an object
+    pbd::DBuf<float> params, m, v, grad;
+    pbd::DBuf<unsigned short> wtiles;    // BF16 tiles (kWtTotal)
+    pbd::DBuf<float> bias;               // b2[64], b3[16] (3..15 zero)
+    pbd::DBuf<double> loss;              // [0] sum of squared errors, [1] count
+    pbd::DBuf<unsigned short> feat;      // recorded features, BF16 [n x 16]
+    pbd::DBuf<float4> tgt;               // training targets (xyz, mask)
+    long long feat_cap = 0;
+    long long adam_t = 0;
+    pbd::DBuf<int> err;                  // device error flag (tensor-core waits)
+};
+
 // internal entry points shared between translation units
 namespace pbd {
+int ws_prepare(pbd_warmstart *w, pbd_object *o);
+int ws_eval_hinges(pbd_object *o, const float4 *pos);
+int ws_infer(pbd_warmstart *w, pbd_object *o);
+int build_feature_stencil(pbd_object *o);
 int launch_advect(pbd_object *o, float dt);
+int launch_advect_p0(pbd_object *o, float dt);
 int launch_integrate(pbd_object *o, float dt);
 int launch_sweeps(pbd_solver *s, int it0, int it1, bool obstacles_inside);
+// one per-color sweep whose stiffness exponent 1/(iter+1) is read from
+// device memory (the solve-to-residual loop)
+int launch_sweep_dev(pbd_solver *s, const float *expk_dev, bool obstacles_inside);
+// residual partial sums of pos over the distance and/or bending records
+// into o->res_part (kResidualParts doubles)
+constexpr int kResidualParts = 4 * kNumSMs;
+int launch_residual_parts(pbd_object *o, bool dist, bool bend, const float4 *pos);
 int launch_obstacles(pbd_solver *s);
 int ccd_detect(pbd_colli *c);
 int ccd_resolve(pbd_colli *c, int passes);

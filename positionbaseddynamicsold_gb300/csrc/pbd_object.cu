@@ -239,7 +239,8 @@ __global__ void k_build_records(int n_rec, const int *sprim, const int2 *prim_li
 // p = x + v*dt.  gdt = g*dt and damp_pow = powf(damping, dt) come from the host.
 __global__ void __launch_bounds__(256) k_advect(int n, float dt, float damp_pow, float3 gdt,
                                                 const float4 *__restrict__ x,
-                                                float4 *__restrict__ v, float4 *__restrict__ p) {
+                                                float4 *__restrict__ v, float4 *__restrict__ p,
+                                                float4 *__restrict__ p0) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     float4 X = x[i], V = v[i];
@@ -251,7 +252,9 @@ __global__ void __launch_bounds__(256) k_advect(int n, float dt, float damp_pow,
     V.y = V.y * damp_pow;
     V.z = V.z * damp_pow;
     v[i] = make_float4(V.x, V.y, V.z, 0.f);
-    p[i] = make_float4(X.x + V.x * dt, X.y + V.y * dt, X.z + V.z * dt, m);
+    float4 P = make_float4(X.x + V.x * dt, X.y + V.y * dt, X.z + V.z * dt, m);
+    p[i] = P;
+    if (p0) p0[i] = P;  // kept for the warm start and the correction record
 }
 
 // IntegrationGPUKernel (P/PBD_cuda.cu:1467-1482): v = (p - x)/dt; x = p
@@ -373,7 +376,8 @@ __global__ void __launch_bounds__(256) k_project_color(const int4 *__restrict__ 
                                                        const int4 *__restrict__ bidx,
                                                        const float2 *__restrict__ bpar, int nb,
                                                        const float4 *__restrict__ arec, int na,
-                                                       float4 *__restrict__ p, float expk) {
+                                                       float4 *__restrict__ p, float expk,
+                                                       const float *__restrict__ expk_dev) {
     int t = blockIdx.x * blockDim.x + threadIdx.x;
     int4 r = make_int4(0, 0, 0, 0);
     float2 bp = make_float2(0.f, 0.f);
@@ -392,6 +396,8 @@ __global__ void __launch_bounds__(256) k_project_color(const int4 *__restrict__ 
     }
     asm volatile("griddepcontrol.launch_dependents;");
     asm volatile("griddepcontrol.wait;" ::: "memory");
+    // the solve-to-residual loop keeps the sweep's exponent on the device
+    if (expk_dev) expk = *expk_dev;
     GlobalPos P{p};
     if (kind == 1)
         project_distance(r, P, expk);
@@ -595,10 +601,24 @@ constexpr int kResidualBlocks = 4 * kNumSMs;
 // ---------------------------------------------------------------------------
 int launch_obstacles(pbd_solver *s);
 
-int launch_advect(pbd_object *o, float dt) {
+static int advect(pbd_object *o, float dt, float4 *p0) {
     float dp = powf(o->damping, dt);
     float3 gdt = make_float3(o->gravity[0] * dt, o->gravity[1] * dt, o->gravity[2] * dt);
-    k_advect<<<grid_for(o->n, 256), 256, 0, o->stream>>>(o->n, dt, dp, gdt, o->x.p, o->v.p, o->p.p);
+    k_advect<<<grid_for(o->n, 256), 256, 0, o->stream>>>(o->n, dt, dp, gdt, o->x.p, o->v.p, o->p.p,
+                                                         p0);
+    PBD_LAUNCH();
+    return PBD_OK;
+}
+int launch_advect(pbd_object *o, float dt) { return advect(o, dt, nullptr); }
+// advect and keep the advected positions in o->p0 (allocated by the caller)
+int launch_advect_p0(pbd_object *o, float dt) { return advect(o, dt, o->p0.p); }
+
+int launch_residual_parts(pbd_object *o, bool dist, bool bend, const float4 *pos) {
+    int nd = o->h_dseg.empty() ? 0 : o->h_dseg.back();
+    int nb = o->h_bseg.empty() ? 0 : o->h_bseg.back();
+    k_residual<<<kResidualBlocks, 256, 0, o->stream>>>(o->drec.p, dist ? nd : 0, o->bidx.p,
+                                                       o->bpar.p, bend ? nb : 0, pos,
+                                                       o->res_part.p);
     PBD_LAUNCH();
     return PBD_OK;
 }
@@ -615,7 +635,7 @@ static inline int __float_as_int_host(float f) {
     return i;
 }
 
-static int launch_sweep_per_color(pbd_object *o, int iter) {
+static int launch_sweep_per_color(pbd_object *o, int iter, const float *expk_dev = nullptr) {
     float expk = (float)(1.0 / (double)(iter + 1));
     for (int c = 0; c < o->n_colors; ++c) {
         int d0 = o->h_dseg[c], nd = o->h_dseg[c + 1] - d0;
@@ -631,11 +651,18 @@ static int launch_sweep_per_color(pbd_object *o, int iter) {
         at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
         at[0].val.programmaticStreamSerializationAllowed = 1;
         cfg.attrs = at;
-        cfg.numAttrs = 1;
+        cfg.numAttrs = o->pdl ? 1 : 0;
         PBD_CUDA(cudaLaunchKernelEx(&cfg, k_project_color, (const int4 *)(o->drec.p + d0), nd,
                                     (const int4 *)(o->bidx.p + b0), (const float2 *)(o->bpar.p + b0),
-                                    nb, (const float4 *)(o->arec.p + a0), na, o->p.p, expk));
+                                    nb, (const float4 *)(o->arec.p + a0), na, o->p.p, expk,
+                                    expk_dev));
     }
+    return PBD_OK;
+}
+
+int launch_sweep_dev(pbd_solver *s, const float *expk_dev, bool obstacles_inside) {
+    PBD_TRY(launch_sweep_per_color(s->obj, 0, expk_dev));
+    if (obstacles_inside) PBD_TRY(launch_obstacles(s));
     return PBD_OK;
 }
 
@@ -999,12 +1026,13 @@ int pbd_object_create(const pbd_object_desc *d, pbd_object **out) {
         }
         // residual denominator: rest lengths and hinge lengths of the
         // initial positions
-        double den = 0.0;
+        double den = 0.0, den_d = 0.0;
         for (int p = 0; p < o->np; ++p) {
             const int *ix = d->indices + d->prim_list[2 * p];
             if (ct[p] == PBD_DISTANCE) {
                 double l = d->rest_length[p];
                 den += l * l;
+                den_d += l * l;
             } else if (ct[p] == PBD_BENDING) {
                 double e2 = 0.0;
                 for (int k = 0; k < 3; ++k) {
@@ -1015,6 +1043,12 @@ int pbd_object_create(const pbd_object_desc *d, pbd_object **out) {
             }
         }
         o->res_den = den;
+        o->res_den_d = den_d;
+        o->h_prim_list.assign(d->prim_list, d->prim_list + 2 * (size_t)o->np);
+        o->h_indices.assign(d->indices, d->indices + n_idx);
+        o->h_rest_length.assign(o->np, 0.f);
+        if (d->rest_length)
+            for (int p = 0; p < o->np; ++p) o->h_rest_length[p] = d->rest_length[p];
     }
     if ((r = o->res_part.alloc(kResidualBlocks)) || (r = o->res_out.alloc(1))) return fail(r);
     *out = o;
@@ -1326,6 +1360,11 @@ int pbd_constraints_sort_edges_colors(pbd_object *o) {
     PBD_TRY(o->bidx.alloc(nrec[1]));
     PBD_TRY(o->bpar.alloc(nrec[1]));
     PBD_TRY(o->arec.alloc(nrec[2]));
+    PBD_TRY(o->bend_prim.alloc(nrec[1]));
+    if (nrec[1])
+        PBD_CUDA(cudaMemcpyAsync(o->bend_prim.p, sv + nrec[0], sizeof(int) * nrec[1],
+                                 cudaMemcpyDeviceToDevice, s));
+    o->feat_built = false;
     k_build_records<<<grid_for(np, 256), 256, 0, s>>>(
         nrec[0] + nrec[1] + nrec[2], sv, o->prim_list.p, o->indices.p, o->rest_length.p,
         o->stiffness.p, o->rest_angle.p, o->rest_pos.p, nrec[0], nrec[1], nrec[2], o->drec.p,
@@ -1413,6 +1452,7 @@ int pbd_solver_create(pbd_solver **out) {
 int pbd_solver_destroy(pbd_solver *s) {
     if (!s) return PBD_OK;
     if (s->gexec) cudaGraphExecDestroy(s->gexec);
+    if (s->rexec) cudaGraphExecDestroy(s->rexec);
     delete s;
     return PBD_OK;
 }
@@ -1422,6 +1462,8 @@ int pbd_solver_set_target(pbd_solver *s, pbd_object *o) {
     s->obj = o;
     if (s->gexec) cudaGraphExecDestroy(s->gexec);
     s->gexec = nullptr;
+    if (s->rexec) cudaGraphExecDestroy(s->rexec);
+    s->rexec = nullptr;
     return PBD_OK;
 }
 

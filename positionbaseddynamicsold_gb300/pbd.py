@@ -66,6 +66,13 @@ EXPORTS = [
     "pbd_colli_collision_resolve_new", "pbd_colli_get_contacts", "pbd_colli_stats",
     "pbd_ccd_vf_test_batch",
     "pbd_residual_noalloc",
+    "pbd_constraints_residual_stretch", "pbd_solver_step_to_residual", "pbd_solver_solve_stats",
+    "pbd_solver_residual_graph_kernels", "pbd_object_get_correction",
+    "pbd_warmstart_num_params", "pbd_warmstart_create", "pbd_warmstart_destroy",
+    "pbd_warmstart_set_params", "pbd_warmstart_get_params", "pbd_warmstart_forward",
+    "pbd_warmstart_gradients", "pbd_warmstart_set_gradient", "pbd_warmstart_adam",
+    "pbd_warmstart_record", "pbd_warmstart_train_step", "pbd_warmstart_features",
+    "pbd_warmstart_predict", "pbd_solver_set_warmstart",
 ]
 
 
@@ -107,6 +114,10 @@ def load(build_if_missing: bool = True) -> C.CDLL:
     L.pbd_residual_noalloc.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_int,
                                        C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p,
                                        C.c_void_p]
+    L.pbd_solver_step_to_residual.argtypes = [C.c_void_p, C.c_float, C.c_int, C.c_void_p,
+                                              C.c_double, C.c_int, C.c_int, C.c_int]
+    L.pbd_warmstart_adam.argtypes = [C.c_void_p, C.c_float, C.c_float, C.c_float, C.c_float]
+    L.pbd_warmstart_train_step.argtypes = [C.c_void_p, C.c_void_p, C.c_float, C.c_void_p]
     _LIB = L
     return L
 
@@ -280,6 +291,17 @@ class PBDObject:
         r = C.c_double()
         _check(self.L.pbd_constraints_residual(self.h, C.byref(r)))
         return r.value
+
+    def residual_stretch(self):
+        """relative stretch residual of the predicted positions (distance
+        constraints only), the stopping test of step_to_residual"""
+        r = C.c_double()
+        _check(self.L.pbd_constraints_residual_stretch(self.h, C.byref(r)))
+        return r.value
+
+    def correction(self):
+        """p_final - p_advected of the last substep solved to a residual"""
+        return self._get3(self.L.pbd_object_get_correction)
 
     def prepare(self, iterations=20000):
         """EdgeColoring + SortEdgesColors + EvalWorksets; returns sweeps."""
@@ -481,6 +503,109 @@ class SolverPBD:
     def step(self, dt, substeps=1, iterations=20, colli=None, use_graph=True):
         _check(self.L.pbd_solver_step(self.h, dt, substeps, iterations,
                                       colli.h if colli else None, int(use_graph)))
+
+    def set_warmstart(self, ws):
+        self.ws = ws
+        _check(self.L.pbd_solver_set_warmstart(self.h, ws.h if ws is not None else None))
+
+    def step_to_residual(self, dt, substeps=1, target=1e-4, max_sweeps=60, chunk=5, colli=None,
+                         use_graph=True):
+        """substeps solved until the stretch residual <= target (in chunks
+        of `chunk` sweeps, at most max_sweeps)"""
+        _check(self.L.pbd_solver_step_to_residual(self.h, dt, substeps,
+                                                  colli.h if colli else None, float(target),
+                                                  int(max_sweeps), int(chunk), int(use_graph)))
+
+    def solve_stats(self, reset=False):
+        st = _SolveStats()
+        _check(self.L.pbd_solver_solve_stats(self.h, C.byref(st), int(reset)))
+        return {k: getattr(st, k) for k, _ in _SolveStats._fields_}
+
+    def residual_graph_kernels(self):
+        n = C.c_longlong()
+        _check(self.L.pbd_solver_residual_graph_kernels(self.h, C.byref(n)))
+        return n.value
+
+
+class _SolveStats(C.Structure):
+    _fields_ = [("substeps", C.c_longlong), ("sweeps", C.c_longlong), ("reached", C.c_longlong),
+                ("reverts", C.c_longlong), ("last_residual", C.c_double),
+                ("last_sweeps", C.c_int), ("last_r0", C.c_double), ("last_r1", C.c_double)]
+
+
+class WarmStart:
+    """Learned warm start: per-point MLP 16 -> 64 -> 64 -> 3 on the tensor
+    cores (no reference counterpart).  Parameters: W1[64][16], W2[64][64],
+    b2[64], W3[3][64], b3[3] flattened in that order."""
+
+    def __init__(self, params=None):
+        self.L = load()
+        self.h = C.c_void_p()
+        _check(self.L.pbd_warmstart_create(C.byref(self.h)))
+        self.n_params = self.L.pbd_warmstart_num_params()
+        if params is not None:
+            self.set_params(params)
+
+    def close(self):
+        if self.h:
+            self.L.pbd_warmstart_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_params(self, params):
+        a = _f32(params).ravel()
+        _check(self.L.pbd_warmstart_set_params(self.h, _p(a), len(a)))
+
+    def params(self):
+        a = np.zeros(self.n_params, np.float32)
+        _check(self.L.pbd_warmstart_get_params(self.h, _p(a), len(a)))
+        return a
+
+    def forward(self, x):
+        x = _f32(x, (-1, 16))
+        y = np.zeros((len(x), 3), np.float32)
+        _check(self.L.pbd_warmstart_forward(self.h, _p(x), len(x), _p(y)))
+        return y
+
+    def gradients(self, x, t, mask=None):
+        x = _f32(x, (-1, 16))
+        t = _f32(t, (-1, 3))
+        m = None if mask is None else _f32(mask)
+        g = np.zeros(self.n_params, np.float32)
+        loss = C.c_double()
+        _check(self.L.pbd_warmstart_gradients(self.h, _p(x), _p(t), _p(m), len(x), _p(g),
+                                              C.byref(loss)))
+        return g, loss.value
+
+    def set_gradient(self, g):
+        g = _f32(g).ravel()
+        _check(self.L.pbd_warmstart_set_gradient(self.h, _p(g), len(g)))
+
+    def adam(self, lr=1e-3, beta1=0.9, beta2=0.999, eps=1e-8):
+        _check(self.L.pbd_warmstart_adam(self.h, lr, beta1, beta2, eps))
+
+    def record(self, obj):
+        _check(self.L.pbd_warmstart_record(self.h, obj.h))
+
+    def train_step(self, obj, lr=1e-3, want_loss=True):
+        loss = C.c_double()
+        _check(self.L.pbd_warmstart_train_step(self.h, obj.h, lr,
+                                               C.byref(loss) if want_loss else None))
+        return loss.value if want_loss else None
+
+    def features(self, obj):
+        n = obj.n_points
+        x = np.zeros((n, 16), np.float32)
+        _check(self.L.pbd_warmstart_features(self.h, obj.h, _p(x)))
+        return x
+
+    def predict(self, obj):
+        _check(self.L.pbd_warmstart_predict(self.h, obj.h))
 
 
 def residual_noalloc(d_pos4, n_points, d_dist_idx, d_rest_length, n_dist, d_bend_idx,
