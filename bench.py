@@ -23,6 +23,13 @@ oracle's restatement: sequential GS, triangle-ordered CCD with
 de-duplication by scan, sequential response) for one full substep of the
 same state on one host thread.
 
+Other modes: --solve residual runs every substep to a stretch-residual
+target (--target, at most --max-sweeps sweeps in chunks of --chunk, the loop
+on the device in a CUDA graph), --learned adds the trained warm start,
+--autotune picks the GS launch form first.  `learned_warm_start` in the line
+compares the trained network with the plain sweeps on held-out cloths of its
+training family (see learned_eval).
+
 Multi-GPU: a single cloth does not shard; N GPUs run N independent replicas
 (value = replicas x substeps / slowest replica's time).
 """
@@ -173,8 +180,23 @@ def run_ours(args, rank, world):
     n_colors = obj.eval_worksets()
     iters = cfg["gs_iterations"]
 
-    def step():
-        solver.step(DT, 1, iters, cs, True)
+    if args.autotune:
+        cfg["autotune"] = solver.autotune(iterations=iters, reps=3)
+    if args.solve == "residual":
+        cfg["solve"] = {"target_stretch_residual": args.target, "max_sweeps": args.max_sweeps,
+                        "chunk": args.chunk, "warm_start": bool(args.learned)}
+        if args.learned:
+            from positionbaseddynamicsold_gb300 import warmstart_train as wt
+            from positionbaseddynamicsold_gb300.pbd import WarmStart
+            params, scales, _ = wt.load_params()
+            ws_net = WarmStart(params, scales)
+            solver.set_warmstart(ws_net)
+
+        def step():
+            solver.step_to_residual(DT, 1, args.target, args.max_sweeps, args.chunk, cs, True)
+    else:
+        def step():
+            solver.step(DT, 1, iters, cs, True)
 
     # pre-roll so the timed substeps include contacts
     for _ in range(args.preroll):
@@ -182,6 +204,8 @@ def run_ours(args, rank, world):
     for _ in range(args.warmup):
         step()
     obj.sync()
+    if args.solve == "residual":
+        solver.solve_stats(reset=True)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
           for _ in range(args.steps)]
@@ -213,7 +237,15 @@ def run_ours(args, rank, world):
     value = world * args.steps / (ms / 1e3)
     stats = cs.stats() if cs is not None else {}
     residual = obj.residual()
-    launches = solver.graph_kernels()
+    if args.solve == "residual":
+        sst = solver.solve_stats()
+        cfg["solve"]["timed_substeps"] = sst
+        outer, body = solver.residual_graph_kernels()
+        # solve_stats was reset before the timed substeps
+        chunks = sst["sweeps"] / max(1, sst["substeps"]) / args.chunk
+        launches_total = int(round(args.steps * (outer + body * chunks)))
+    else:
+        launches_total = solver.graph_kernels() * args.steps
 
     # roofline of the dominant kernel (the per-color GS launch): one eager
     # 15-iteration projection on the same state, timed with events on the
@@ -265,7 +297,7 @@ def run_ours(args, rank, world):
                        distance_constraints=nd, bending_constraints=nb,
                        preroll_substeps=args.preroll),
         "e2e": e2e,
-        "gpu_launches": launches * args.steps,
+        "gpu_launches": launches_total,
         "roofline": {"bound": "hbm", "kernel": "k_project_color", "achieved": achieved,
                      "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "peak_source": peak_kind, "traffic": args.traffic,
@@ -278,6 +310,35 @@ def run_ours(args, rank, world):
     }
     if rank == 0 and not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(sc, cfg, colli_on, obj)
+    if rank == 0 and not args.no_learned_eval:
+        out["learned_warm_start"] = learned_eval()
+    return out
+
+
+def learned_eval(n_traj=4, substeps=40):
+    """The learned warm start against the plain sweeps on held-out cloths of
+    its training family (hanging, 64..256 points a side, 1-4 pins, wind),
+    stretch-residual target of training (1e-3), at most 200 sweeps:
+    same_state -- both solve every advected state of a plain trajectory
+    (sweeps summed where both reach the target); closed_loop -- each runs
+    its own trajectory through pbd_solver_step_to_residual (CUDA graph),
+    wall time on the host includes everything."""
+    from positionbaseddynamicsold_gb300 import warmstart_train as wt
+    try:
+        params, scales, meta = wt.load_params()
+    except FileNotFoundError:
+        return {"unavailable": "no trained weights at " + wt.DEFAULT_WEIGHTS}
+    tgt = float(meta.get("target", 1e-3))
+    same = wt.evaluate_same_state(params, scales, n_traj, substeps, tgt, 200, 5)
+    closed = wt.evaluate(params, scales, n_traj, substeps, tgt, 200, 5)
+    out = {"target_stretch_residual": tgt, "max_sweeps": 200, "trajectories": n_traj,
+           "substeps_each": substeps, "same_state": same, "closed_loop": closed}
+    if same["learned_sweeps"]:
+        out["same_state"]["sweep_ratio_plain_over_learned"] = (
+            same["plain_sweeps"] / same["learned_sweeps"])
+    for k in ("plain", "learned"):
+        c = closed[k]
+        c["substeps_per_s"] = c["substeps"] / c["seconds"] if c["seconds"] else None
     return out
 
 
@@ -393,6 +454,18 @@ def main():
                          "--profile-from-start off)")
     ap.add_argument("--traffic", type=float, default=None,
                     help="ncu dram bytes per launch of the dominant kernel (from profiles/)")
+    ap.add_argument("--solve", default="fixed", choices=["fixed", "residual"],
+                    help="fixed: gs_iterations sweeps per substep (the reference's step); "
+                         "residual: sweeps until the stretch residual <= --target")
+    ap.add_argument("--target", type=float, default=1e-3)
+    ap.add_argument("--max-sweeps", type=int, default=200)
+    ap.add_argument("--chunk", type=int, default=10)
+    ap.add_argument("--learned", action="store_true",
+                    help="with --solve residual: warm start from the trained network")
+    ap.add_argument("--autotune", action="store_true",
+                    help="pick the GS launch form with the autotuner before timing")
+    ap.add_argument("--no-learned-eval", action="store_true",
+                    help="skip the learned-vs-plain evaluation on held-out hanging cloths")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))

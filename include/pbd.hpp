@@ -152,9 +152,62 @@ public:
     void Step(float dt, int substeps, int iterations, CollisionSolver *c, bool graph = true) {
         check(pbd_solver_step(h_, dt, substeps, iterations, c ? c->handle() : nullptr, graph));
     }
+    // no reference counterparts below: substeps solved to a stretch-residual
+    // target (device-side loop in a CUDA graph), the learned warm start and
+    // the launch-form autotuner
+    void StepToResidual(float dt, int substeps, CollisionSolver *c, double target,
+                        int max_sweeps, int chunk, bool graph = true) {
+        check(pbd_solver_step_to_residual(h_, dt, substeps, c ? c->handle() : nullptr, target,
+                                          max_sweeps, chunk, graph));
+    }
+    pbd_solve_stats SolveStats(bool reset = false) {
+        pbd_solve_stats st;
+        check(pbd_solver_solve_stats(h_, &st, reset));
+        return st;
+    }
+    void SetWarmStart(pbd_warmstart *w, int min_sweeps = 0) {
+        check(pbd_solver_set_warmstart(h_, w, min_sweeps));
+    }
+    pbd_autotune_result Autotune(int iterations = 15, int reps = 5) {
+        pbd_autotune_result r;
+        check(pbd_solver_autotune(h_, iterations, reps, &r));
+        return r;
+    }
+    pbd_solver *handle() const { return h_; }
 
 private:
     pbd_solver *h_ = nullptr;
+};
+
+// learned warm start: per-point MLP on the tensor cores
+class WarmStart {
+public:
+    WarmStart() { check(pbd_warmstart_create(&h_)); }
+    ~WarmStart() { pbd_warmstart_destroy(h_); }
+    WarmStart(const WarmStart &) = delete;
+    WarmStart &operator=(const WarmStart &) = delete;
+    void SetParams(const std::vector<float> &p) {
+        check(pbd_warmstart_set_params(h_, p.data(), (int)p.size()));
+    }
+    void SetScales(const std::vector<float> &s) {
+        check(pbd_warmstart_set_scales(h_, s.data(), (int)s.size()));
+    }
+    std::vector<float> Params() {
+        std::vector<float> p(pbd_warmstart_num_params());
+        check(pbd_warmstart_get_params(h_, p.data(), (int)p.size()));
+        return p;
+    }
+    double TrainSubstep(SolverPBD &s, float dt, CollisionSolver *c, double target,
+                        int max_sweeps, int chunk, float lr, bool on_policy) {
+        double loss = 0.0;
+        check(pbd_solver_train_substep(s.handle(), h_, dt, c ? c->handle() : nullptr, target,
+                                       max_sweeps, chunk, lr, on_policy, &loss));
+        return loss;
+    }
+    pbd_warmstart *handle() const { return h_; }
+
+private:
+    pbd_warmstart *h_ = nullptr;
 };
 
 }  // namespace pbd

@@ -175,6 +175,23 @@ int pbd_solver_set_gs_path(pbd_solver *s, int path);
 /* the form the next sweep will use (PBD_GS_PER_COLOR or PBD_GS_CLUSTER) */
 int pbd_solver_get_gs_path(pbd_solver *s, int *path);
 
+/* Autotuner (no reference counterpart): times `iterations` sweeps replayed
+ * `reps` times from a CUDA graph for each launch form that applies -- the
+ * per-color launches with 64, 128, 256 and 512 threads per block, and the
+ * cluster form (all colors in one launch) when the object fits one cluster --
+ * and keeps the fastest for this solver and object.  The predicted positions
+ * are restored; all forms give identical results. */
+typedef struct pbd_autotune_result {
+    int n;                  /* candidates timed                       */
+    int best;               /* index of the one kept                  */
+    int path[8];            /* PBD_GS_PER_COLOR / PBD_GS_CLUSTER      */
+    int block[8];           /* threads per block                      */
+    double us_per_sweep[8]; /* GPU time per sweep, microseconds       */
+} pbd_autotune_result;
+int pbd_solver_autotune(pbd_solver *s, int iterations, int reps, pbd_autotune_result *result);
+/* threads per block of the per-color launches (256 until autotuned) */
+int pbd_solver_get_gs_block(pbd_solver *s, int *block);
+
 /* kernel launches recorded in the cached pbd_solver_step graph (no
  * reference counterpart; used to report launches per step) */
 int pbd_solver_graph_kernels(pbd_solver *s, long long *n);
@@ -290,11 +307,20 @@ typedef struct pbd_solve_stats {
 int pbd_solver_step_to_residual(pbd_solver *s, float dt, int substeps, pbd_colli *colli,
                                 double target, int max_sweeps, int chunk, int use_graph);
 int pbd_solver_solve_stats(pbd_solver *s, pbd_solve_stats *stats, int reset);
-/* kernel nodes of the cached pbd_solver_step_to_residual graph, each WHILE
- * body counted once */
-int pbd_solver_residual_graph_kernels(pbd_solver *s, long long *n);
+/* the solve alone on the current predicted positions (no Advect, no
+ * Integration, no warm start), host-driven: sweeps in chunks until the
+ * stretch residual <= target or max_sweeps; with colli as above.  Records
+ * the correction p - p_before; returns the sweeps run and the residual.
+ * Used to generate the warm start's training targets. */
+int pbd_solver_project_to_residual(pbd_solver *s, pbd_colli *colli, double target,
+                                   int max_sweeps, int chunk, int *sweeps, double *residual);
+/* kernel nodes of the cached pbd_solver_step_to_residual graph: outside the
+ * WHILE bodies (all substeps) and inside one body (one chunk) */
+int pbd_solver_residual_graph_kernels(pbd_solver *s, long long *n_outer, long long *n_body);
 /* the correction p_final - p_advected of the last solved substep, 3 per point */
 int pbd_object_get_correction(pbd_object *obj, float *corr3);
+/* overwrite it (e.g. to resume a run: the warm start reads it as a feature) */
+int pbd_object_set_correction(pbd_object *obj, const float *corr3);
 
 /* ---- learned warm start ---------------------------------------------------- */
 /* No counterpart in the reference.  A per-point MLP 16 -> 64 -> 64 -> 3 (SiLU)
@@ -313,6 +339,11 @@ int pbd_warmstart_create(pbd_warmstart **out);          /* parameters zero    */
 int pbd_warmstart_destroy(pbd_warmstart *w);
 int pbd_warmstart_set_params(pbd_warmstart *w, const float *params, int n);  /* resets Adam */
 int pbd_warmstart_get_params(pbd_warmstart *w, float *params, int n);
+/* 17 positive scales: features 0..14 are multiplied by scales[0..14] before
+ * the network (scales[15] is unused: feature 15 is the constant 1) and the
+ * network's output is multiplied by scales[16] * lbar; all 1 by default */
+int pbd_warmstart_set_scales(pbd_warmstart *w, const float *scales, int n);
+int pbd_warmstart_get_scales(pbd_warmstart *w, float *scales, int n);
 /* network outputs y (3 per row) of n feature rows x (16 floats each, rounded
  * to BF16; column 15 taken as 1) */
 int pbd_warmstart_forward(pbd_warmstart *w, const float *x, int n, float *y);
@@ -331,12 +362,28 @@ int pbd_warmstart_adam(pbd_warmstart *w, float lr, float beta1, float beta2, flo
  * Adam step (beta 0.9 / 0.999, eps 1e-8); loss may be NULL (no sync). */
 int pbd_warmstart_record(pbd_warmstart *w, pbd_object *obj);
 int pbd_warmstart_train_step(pbd_warmstart *w, pbd_object *obj, float lr, double *loss);
+/* One training substep on the solver's object, all on the device except the
+ * loop conditions: Advect; features of the advected state; the plain solve
+ * to the residual target (as pbd_solver_step_to_residual, collisions
+ * included); one forward/backward pass + Adam step on (features, plain
+ * correction).  on_policy = 0: the trajectory continues from the plain
+ * solve.  on_policy = 1: the advected state is solved again from the
+ * (just updated) network's prediction, guard included, and the trajectory
+ * continues from that solve, so later substeps are drawn from the states the
+ * warm-started solver visits.  Then the correction record and Integration.
+ * loss may be NULL. */
+int pbd_solver_train_substep(pbd_solver *s, pbd_warmstart *w, float dt, pbd_colli *colli,
+                             double target, int max_sweeps, int chunk, float lr, int on_policy,
+                             double *loss);
 /* features (16 floats per point, BF16 values) of the object's predicted positions */
 int pbd_warmstart_features(pbd_warmstart *w, pbd_object *obj, float *x);
 /* apply the prediction to the object's predicted positions (test hook) */
 int pbd_warmstart_predict(pbd_warmstart *w, pbd_object *obj);
-/* use the network in pbd_solver_step_to_residual (NULL = plain sweeps) */
-int pbd_solver_set_warmstart(pbd_solver *s, pbd_warmstart *w);
+/* use the network in pbd_solver_step_to_residual (NULL = plain sweeps);
+ * an accepted prediction is followed by at least min_sweeps sweeps (they
+ * remove the prediction's small-scale error before it reaches the
+ * velocities) */
+int pbd_solver_set_warmstart(pbd_solver *s, pbd_warmstart *w, int min_sweeps);
 
 #ifdef __cplusplus
 }

@@ -179,8 +179,9 @@ def dihedral_dev(scene, pos, prim):
     return c
 
 
-def features(scene, pos, dprev=None, st=None):
-    """(n, 16) features of every point at positions pos (float64)"""
+def features(scene, pos, dprev=None, st=None, scales=None):
+    """(n, 16) features of every point at positions pos (float64); scales
+    (17) multiply features 0..14 as in the network's input"""
     st = stencil(scene) if st is None else st
     pos = np.asarray(pos, np.float64)
     n = len(pos)
@@ -204,5 +205,7 @@ def features(scene, pos, dprev=None, st=None):
             if p not in cache:
                 cache[p] = dihedral_dev(scene, pos, p)
             F[i, 11 + k] = cache[p]
+    if scales is not None:
+        F[:, :15] *= np.asarray(scales, np.float64)[:15]
     F[:, 15] = 1.0
     return F

@@ -414,18 +414,28 @@ __global__ void k_find_neighbors(int nt, GridParams g, const int4 *tcell, const 
     if (cnt) cnt[t] = k;
 }
 
-// stage 1 of the candidate search: one warp per point, one lane per cell of
-// the union of the 27-cell neighbourhoods of its incident triangles' centroid
-// cells; a task (point, bucket, cell) is emitted for every such cell whose
-// bucket is non-empty and whose bucket AABB meets the point's grown swept AABB
+// Candidate search, one warp per point.  The point's candidate cells are
+// the union of the 27-cell neighbourhoods of its incident triangles'
+// centroid cells (FindNeighbors around every triangle that holds the point,
+// P/SpatialHashSystem.cpp:134-187, as CCD_SH_Extended visits them,
+// P/CCD.cpp:1522-1587).  A round takes 32 candidate cells, one per lane; a
+// lane keeps its cell when the bucket is non-empty and the bucket's AABB meets
+// the point's grown swept AABB.  The kept buckets' entries are then
+// spread over the 32 lanes by a warp prefix sum (lane j of the warp takes
+// flat entries j, j+32, ...), so a bucket of any size costs ceil(entries/32)
+// coalesced steps; an entry yields a (point, triangle) pair when its cell is
+// the lane's cell (the hash may mix cells), its swept AABB meets the point's
+// and it belongs to the point's instance.
 constexpr int kTaskWarps = 8;
-__global__ void __launch_bounds__(32 * kTaskWarps) k_cell_tasks(
+__global__ void __launch_bounds__(32 * kTaskWarps) k_point_pairs(
     int n, GridParams g, float margin, const int *__restrict__ pt_first,
     const int *__restrict__ pt_last, const int *__restrict__ pt_tri,
-    const int *__restrict__ point_inst, const float4 *__restrict__ x,
-    const float4 *__restrict__ p, const int4 *__restrict__ tcell,
+    const int *__restrict__ point_inst, const int *__restrict__ tri_inst,
+    const float4 *__restrict__ x, const float4 *__restrict__ p, const int4 *__restrict__ tcell,
     const int2 *__restrict__ brange, const float4 *__restrict__ blo,
-    const float4 *__restrict__ bhi, int4 *tasks, int *tcell_z, long long cap, int *counters) {
+    const float4 *__restrict__ bhi, const int4 *__restrict__ scell,
+    const float4 *__restrict__ slo, const float4 *__restrict__ shi, int2 *pairs, long long cap,
+    int *counters) {
     const int lane = threadIdx.x & 31;
     const int warp0 = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int nwarps = (gridDim.x * blockDim.x) >> 5;
@@ -443,9 +453,9 @@ __global__ void __launch_bounds__(32 * kTaskWarps) k_cell_tasks(
             mc = tcell[pt_tri[f0 + lane]];
             valid = g.hashed || !outside(g, mc.x, mc.y, mc.z);
         }
-        unsigned vm = __ballot_sync(0xffffffffu, valid);
+        const unsigned vm = __ballot_sync(0xffffffffu, valid);
         if (!vm) continue;
-        // bbox of the valid incident cells (warp min/max)
+        // bounding box of the valid incident cells
         int lx = valid ? mc.x : INT_MAX, ly = valid ? mc.y : INT_MAX, lz = valid ? mc.z : INT_MAX;
         int hx = valid ? mc.x : INT_MIN, hy = valid ? mc.y : INT_MIN, hz = valid ? mc.z : INT_MIN;
 #pragma unroll
@@ -458,78 +468,79 @@ __global__ void __launch_bounds__(32 * kTaskWarps) k_cell_tasks(
             hz = max(hz, __shfl_xor_sync(0xffffffffu, hz, o));
         }
         v3 X0 = ld3(x[v]), P0 = ld3(p[v]);
-        float plx = fminf(X0.x, P0.x) - margin, phx = fmaxf(X0.x, P0.x) + margin;
-        float ply = fminf(X0.y, P0.y) - margin, phy = fmaxf(X0.y, P0.y) + margin;
-        float plz = fminf(X0.z, P0.z) - margin, phz = fmaxf(X0.z, P0.z) + margin;
-        int ex = hx - lx + 3, ey = hy - ly + 3, ez = hz - lz + 3;
-        int ncell = ex * ey * ez;
-        for (int ci = lane; ci < ncell; ci += 32) {
-            int xx = lx - 1 + ci % ex;
-            int y = ly - 1 + (ci / ex) % ey;
-            int z = lz - 1 + ci / (ex * ey);
-            // near: within one cell of some valid incident cell
+        const float plx = fminf(X0.x, P0.x) - margin, phx = fmaxf(X0.x, P0.x) + margin;
+        const float ply = fminf(X0.y, P0.y) - margin, phy = fmaxf(X0.y, P0.y) + margin;
+        const float plz = fminf(X0.z, P0.z) - margin, phz = fmaxf(X0.z, P0.z) + margin;
+        const int ex = hx - lx + 3, ey = hy - ly + 3, ez = hz - lz + 3;
+        const int ncell = ex * ey * ez;
+        for (int base = 0; base < ncell; base += 32) {
+            const int ci = base + lane;
+            const int cx = lx - 1 + ci % ex;
+            const int cy = ly - 1 + (ci / ex) % ey;
+            const int cz = lz - 1 + ci / (ex * ey);
+            // within one cell of some valid incident cell (read from the lanes)
             bool near = false;
             unsigned m = vm;
             while (m) {
-                int src = __ffs(m) - 1;
+                const int src = __ffs(m) - 1;
                 m &= m - 1;
-                // the incident cells are held by lanes < ninc; read them by index
-                int4 c = tcell[pt_tri[f0 + src]];
-                near |= abs(c.x - xx) <= 1 && abs(c.y - y) <= 1 && abs(c.z - z) <= 1;
+                const int sx = __shfl_sync(0xffffffffu, mc.x, src);
+                const int sy = __shfl_sync(0xffffffffu, mc.y, src);
+                const int sz = __shfl_sync(0xffffffffu, mc.z, src);
+                near |= abs(sx - cx) <= 1 && abs(sy - cy) <= 1 && abs(sz - cz) <= 1;
             }
-            if (!near) continue;
-            if (!g.hashed && outside(g, xx, y, z)) continue;
-            uint32_t b = bucket_of(g, xx, y, z, inst);
-            int2 r = brange[b];
-            if (r.x >= r.y) continue;
-            float4 bl = blo[b], bh = bhi[b];
-            if (plx > bh.x || phx < bl.x || ply > bh.y || phy < bl.y || plz > bh.z || phz < bl.z)
-                continue;
-            int slot = agg_inc(counters + 3);
-            if (slot < cap) {
-                tasks[slot] = make_int4(v, (int)b, xx, y);
-                tcell_z[slot] = z;
-            } else {
-                atomicOr(counters + 2, 8);
+            int cnt = 0, start = 0;
+            if (ci < ncell && near && (g.hashed || !outside(g, cx, cy, cz))) {
+                const uint32_t b = bucket_of(g, cx, cy, cz, inst);
+                const int2 r = brange[b];
+                if (r.x < r.y) {
+                    const float4 bl = blo[b], bh = bhi[b];
+                    if (!(plx > bh.x || phx < bl.x || ply > bh.y || phy < bl.y || plz > bh.z ||
+                          phz < bl.z)) {
+                        cnt = r.y - r.x;
+                        start = r.x;
+                    }
+                }
             }
-        }
-    }
-}
-
-// stage 2: one thread per task scans the bucket's entries (sorted-order
-// copies of cell and AABB, independent loads) and emits (point, triangle)
-// pairs whose cell is the task's and whose swept AABBs meet
-__global__ void __launch_bounds__(256) k_task_entries(
-    const int4 *__restrict__ tasks, const int *__restrict__ tcell_z, long long tcap,
-    float margin, const int *__restrict__ point_inst, const int *__restrict__ tri_inst4,
-    const float4 *__restrict__ x, const float4 *__restrict__ p, const int2 *__restrict__ brange,
-    const int4 *__restrict__ scell, const float4 *__restrict__ slo,
-    const float4 *__restrict__ shi, int2 *pairs, long long cap, int *counters) {
-    long long nt = counters[3];
-    if (nt > tcap) nt = tcap;
-    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < nt;
-         i += (long long)gridDim.x * blockDim.x) {
-        int4 tk = tasks[i];
-        int z = tcell_z[i];
-        int v = tk.x;
-        v3 X0 = ld3(x[v]), P0 = ld3(p[v]);
-        float plx = fminf(X0.x, P0.x) - margin, phx = fmaxf(X0.x, P0.x) + margin;
-        float ply = fminf(X0.y, P0.y) - margin, phy = fmaxf(X0.y, P0.y) + margin;
-        float plz = fminf(X0.z, P0.z) - margin, phz = fmaxf(X0.z, P0.z) + margin;
-        int inst = point_inst ? point_inst[v] : 0;
-        int2 r = brange[tk.y];
-        for (int e = r.x; e < r.y; ++e) {
-            int4 sc = scell[e];
-            float4 tl = slo[e], th = shi[e];
-            if (sc.x != tk.z || sc.y != tk.w || sc.z != z) continue;
-            if (plx > th.x || phx < tl.x || ply > th.y || phy < tl.y || plz > th.z || phz < tl.z)
-                continue;
-            if (point_inst && tri_inst4[sc.w] != inst) continue;
-            long long slot = agg_inc(counters + 4);
-            if (slot < cap)
-                pairs[slot] = make_int2(v, sc.w);
-            else
-                atomicOr(counters + 2, 16);
+            // flat entry index space of this round's kept buckets
+            int incl = cnt;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int t = __shfl_up_sync(0xffffffffu, incl, o);
+                if (lane >= o) incl += t;
+            }
+            const int excl = incl - cnt;
+            const int total = __shfl_sync(0xffffffffu, incl, 31);
+            for (int f0 = 0; f0 < total; f0 += 32) {
+                const int f = f0 + lane;
+                // owner: the last lane whose range starts at or before f
+                int own = 0;
+#pragma unroll
+                for (int step = 16; step > 0; step >>= 1) {
+                    const int cand = own + step;
+                    const int e = __shfl_sync(0xffffffffu, excl, cand & 31);
+                    if (cand < 32 && e <= f) own = cand;
+                }
+                const int o_start = __shfl_sync(0xffffffffu, start, own);
+                const int o_excl = __shfl_sync(0xffffffffu, excl, own);
+                const int ox = __shfl_sync(0xffffffffu, cx, own);
+                const int oy = __shfl_sync(0xffffffffu, cy, own);
+                const int oz = __shfl_sync(0xffffffffu, cz, own);
+                if (f >= total) continue;
+                const int e = o_start + (f - o_excl);
+                const int4 sc = scell[e];
+                if (sc.x != ox || sc.y != oy || sc.z != oz) continue;
+                const float4 tl = slo[e], th = shi[e];
+                if (plx > th.x || phx < tl.x || ply > th.y || phy < tl.y || plz > th.z ||
+                    phz < tl.z)
+                    continue;
+                if (point_inst && tri_inst[sc.w] != inst) continue;
+                const long long slot = agg_inc(counters + 4);
+                if (slot < cap)
+                    pairs[slot] = make_int2(v, sc.w);
+                else
+                    atomicOr(counters + 2, 16);
+            }
         }
     }
 }
@@ -765,9 +776,7 @@ int shs_update(pbd_shs *h) {
 static int colli_alloc(pbd_colli *c) {
     pbd_object *o = c->obj;
     PBD_TRY(c->cand.alloc(c->cand_cap));
-    PBD_TRY(c->tasks.alloc(c->task_cap));
     PBD_TRY(c->pairs.alloc(c->task_cap));
-    PBD_TRY(c->tasks_z.alloc(c->task_cap));
     PBD_TRY(c->counters.alloc(8));
     size_t H = (size_t)c->contact_cap;
     PBD_TRY(c->cids.alloc(H));
@@ -800,16 +809,11 @@ int ccd_detect(pbd_colli *c) {
     // with slack
     float margin = 5.5f * th + 2e-6f;
     float reach = 4.5f * th + 2e-6f;
-    k_cell_tasks<<<grid_for((long long)o->n * 32, 32 * kTaskWarps), 32 * kTaskWarps, 0, s>>>(
+    k_point_pairs<<<grid_for((long long)o->n * 32, 32 * kTaskWarps), 32 * kTaskWarps, 0, s>>>(
         o->n, g, margin, o->pt_tri_first.p, o->pt_tri_last.p, o->pt_tri.p,
-        o->has_inst ? o->point_inst.p : nullptr, o->x.p, o->p.p, h->tcell.p, h->brange.p,
-        h->blo.p, h->bhi.p, c->tasks.p, c->tasks_z.p, c->task_cap,
-        c->counters.p);
-    PBD_LAUNCH();
-    k_task_entries<<<kPersistentBlocks, 256, 0, s>>>(
-        c->tasks.p, c->tasks_z.p, c->task_cap, margin, o->has_inst ? o->point_inst.p : nullptr,
-        o->has_inst ? o->tri_inst.p : nullptr, o->x.p, o->p.p, h->brange.p, h->scell.p,
-        h->slo.p, h->shi.p, c->pairs.p, c->task_cap, c->counters.p);
+        o->has_inst ? o->point_inst.p : nullptr, o->has_inst ? o->tri_inst.p : nullptr, o->x.p,
+        o->p.p, h->tcell.p, h->brange.p, h->blo.p, h->bhi.p, h->scell.p, h->slo.p, h->shi.p,
+        c->pairs.p, c->task_cap, c->counters.p);
     PBD_LAUNCH();
     k_dist_filter<<<kPersistentBlocks, 256, 0, s>>>(c->pairs.p, c->task_cap, reach, o->tri.p,
                                                     o->x.p, o->p.p, c->cand.p, c->cand_cap,

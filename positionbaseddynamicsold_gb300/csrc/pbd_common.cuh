@@ -179,6 +179,8 @@ struct pbd_object {
     bool feat_built = false;
     // color phases launched with programmatic dependent launch
     bool pdl = true;
+    // threads per block of the per-color launches (set by the autotuner)
+    int gs_block = 256;
 };
 
 struct pbd_shs {
@@ -216,12 +218,10 @@ struct pbd_colli {
     long long cand_cap = 1 << 22;
     long long contact_cap = 1 << 20;
     long long task_cap = 1 << 22;
-    // cell tasks (point, bucket, cell) and candidates (point, triangle)
-    pbd::DBuf<int4> tasks;
-    pbd::DBuf<int> tasks_z;
+    // candidates (point, triangle)
     pbd::DBuf<int2> pairs;      // AABB-overlapping (point, triangle)
     pbd::DBuf<int2> cand;
-    pbd::DBuf<int> counters;    // [0] candidates, [1] contacts, [2] overflow flags, [3] tasks,
+    pbd::DBuf<int> counters;    // [0] candidates, [1] contacts, [2] overflow flags, [3] unused,
                                 // [4] AABB pairs
     // contacts, in the order the narrow phase found them
     pbd::DBuf<int4> cids;               // i0..i3
@@ -245,7 +245,7 @@ struct LoopState {
     int sweeps;           // sweeps of the current substep's solve
     int revert;           // the current substep's prediction was rejected
     int cont;             // loop condition (also set on the graph's handle)
-    int pad;
+    int pred_used;        // the current substep starts from an accepted prediction
     long long substeps, total_sweeps, reached, reverts;
     float expk[kMaxChunk];  // 1/(sweep+1) of the next chunk's sweeps
 };
@@ -256,6 +256,7 @@ struct pbd_warmstart;
 struct pbd_solver {
     pbd_object *obj = nullptr;
     pbd_warmstart *ws = nullptr;
+    int min_sweeps = 0;   // sweeps that always follow an accepted prediction
     pbd::DBuf<pbd::LoopState> loop;
     // cached graph of pbd_solver_step_to_residual
     cudaGraphExec_t rexec = nullptr;
@@ -263,7 +264,7 @@ struct pbd_solver {
     int r_sub = 0, r_max = 0, r_chunk = 0, r_sig = 0;
     double r_target = 0;
     pbd_colli *r_colli = nullptr;
-    long long r_kernels = 0;
+    long long r_kernels[2] = {0, 0};     // kernels outside / inside one WHILE body
     int gs_path = 0;  // PBD_GS_AUTO / PER_COLOR / CLUSTER
     int sphere_on = 0;
     float sphere_c[3] = {0, 0, 0};
@@ -314,6 +315,7 @@ struct pbd_warmstart {
     pbd::DBuf<double> loss;              // [0] sum of squared errors, [1] count
     pbd::DBuf<unsigned short> feat;      // recorded features, BF16 [n x 16]
     pbd::DBuf<float4> tgt;               // training targets (xyz, mask)
+    pbd::DBuf<float> scale;              // 16 input scales + output scale
     long long feat_cap = 0;
     long long adam_t = 0;
     pbd::DBuf<int> err;                  // device error flag (tensor-core waits)
@@ -324,6 +326,8 @@ namespace pbd {
 int ws_prepare(pbd_warmstart *w, pbd_object *o);
 int ws_eval_hinges(pbd_object *o, const float4 *pos);
 int ws_infer(pbd_warmstart *w, pbd_object *o);
+int ws_record(pbd_warmstart *w, pbd_object *o);
+int ws_train_on(pbd_warmstart *w, pbd_object *o, float lr, double *loss);
 int build_feature_stencil(pbd_object *o);
 int launch_advect(pbd_object *o, float dt);
 int launch_advect_p0(pbd_object *o, float dt);

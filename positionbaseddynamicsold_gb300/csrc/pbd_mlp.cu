@@ -14,7 +14,9 @@
 //   11..14 dihedral deviation theta - theta0 of the first four incident
 //          bending constraints (by prim id)
 //   15     constant 1 (the first layer's bias)
-// Output y (3) is the correction / lbar; pinned points get none.
+// Features 0..14 are multiplied by per-feature scales before they enter the
+// network; its output y (3) is the correction / (lbar * output scale).
+// Pinned points get no correction.
 //
 // The three GEMMs of a tile of 128 points run on the 5th-generation tensor
 // cores: tcgen05.mma kind::f16 with BF16 operands in shared memory (K-major
@@ -186,6 +188,7 @@ struct FeatArgs {
     const int2 *fc;
     const float4 *ra, *rb;
     const float *theta;     // per prim
+    const float *scale;     // 16 input scales (15th unused) + the output scale
 };
 
 __device__ __forceinline__ float strain(float4 P, const float4 *pos, int j, float l) {
@@ -221,6 +224,8 @@ __device__ __forceinline__ float point_features(const FeatArgs &a, int i, float 
     f[12] = hinge(a.theta, nb.w);
     f[13] = hinge(a.theta, nc.x);
     f[14] = hinge(a.theta, nc.y);
+#pragma unroll
+    for (int k = 0; k < 15; ++k) f[k] *= a.scale[k];
     f[15] = 1.f;
     return lbar;
 }
@@ -432,8 +437,9 @@ __global__ void __launch_bounds__(kTile, 1) k_mlp_infer(int n, FeatArgs fa, floa
         if (RAW) {
             if (valid) yout[i] = make_float4(y[0] + S.b3[0], y[1] + S.b3[1], y[2] + S.b3[2], 0.f);
         } else if (valid && P.w != 0.f && lbar > 0.f) {
-            float dx = (y[0] + S.b3[0]) * lbar, dy = (y[1] + S.b3[1]) * lbar,
-                  dz = (y[2] + S.b3[2]) * lbar;
+            const float os = fa.scale[16] * lbar;
+            float dx = (y[0] + S.b3[0]) * os, dy = (y[1] + S.b3[1]) * os,
+                  dz = (y[2] + S.b3[2]) * os;
             p[i] = make_float4(P.x + dx, P.y + dy, P.z + dz, P.w);
         }
         fence_before_sync();
@@ -758,13 +764,14 @@ __global__ void k_adam(int n, float *__restrict__ P, float *__restrict__ m, floa
 // training targets of a solved substep: t = (p - p0)/lbar, w = 1 for free
 // points with distance constraints, 0 otherwise
 __global__ void k_targets(int n, const float4 *__restrict__ p, const float4 *__restrict__ p0,
-                          const float4 *__restrict__ rb, float4 *__restrict__ T) {
+                          const float4 *__restrict__ rb, const float *__restrict__ scale,
+                          float4 *__restrict__ T) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     float4 P = p[i], Q = p0[i];
     float lbar = rb[i].z;
     bool use = Q.w != 0.f && lbar > 0.f;
-    float inv = use ? 1.f / lbar : 0.f;
+    float inv = use ? 1.f / (lbar * scale[16]) : 0.f;
     T[i] = make_float4((P.x - Q.x) * inv, (P.y - Q.y) * inv, (P.z - Q.z) * inv, use ? 1.f : 0.f);
 }
 
@@ -856,8 +863,9 @@ int build_feature_stencil(pbd_object *o) {
     return PBD_OK;
 }
 
-static FeatArgs feat_args(pbd_object *o, const float4 *pos) {
+static FeatArgs feat_args(pbd_object *o, const float4 *pos, const pbd_warmstart *w) {
     FeatArgs a;
+    a.scale = w->scale.p;
     a.pos = pos;
     a.dprev = o->dprev.p;
     a.fa = o->fnb_a.p;
@@ -911,7 +919,8 @@ int ws_prepare(pbd_warmstart *w, pbd_object *o) {
 // must have been evaluated into o->theta
 int ws_infer(pbd_warmstart *w, pbd_object *o) {
     k_mlp_infer<false><<<infer_grid(o->n), kTile, kInferSmem, o->stream>>>(
-        o->n, feat_args(o, o->p0.p), o->p.p, nullptr, nullptr, w->wtiles.p, w->bias.p, w->err.p);
+        o->n, feat_args(o, o->p0.p, w), o->p.p, nullptr, nullptr, w->wtiles.p, w->bias.p,
+        w->err.p);
     PBD_LAUNCH();
     return PBD_OK;
 }
@@ -920,6 +929,35 @@ static int pack(pbd_warmstart *w, cudaStream_t s) {
     k_pack_weights<<<16, 256, 0, s>>>(w->params.p, w->wtiles.p, w->bias.p);
     PBD_LAUNCH();
     return PBD_OK;
+}
+
+// features of the object's advected positions o->p0 into w->feat
+int ws_record(pbd_warmstart *w, pbd_object *o) {
+    PBD_TRY(ws_prepare(w, o));
+    PBD_TRY(ws_eval_hinges(o, o->p0.p));
+    if (w->feat_cap < o->n) {
+        PBD_TRY(w->feat.alloc(16 * (size_t)o->n));
+        w->feat_cap = o->n;
+    }
+    k_features<<<grid_for(o->n, 256), 256, 0, o->stream>>>(o->n, feat_args(o, o->p0.p, w),
+                                                            w->feat.p);
+    PBD_LAUNCH();
+    return PBD_OK;
+}
+
+static int train_pass(pbd_warmstart *w, const unsigned short *dx, const float4 *dt, int n,
+                      int n_used, cudaStream_t s, double *loss_out);
+static int adam_step(pbd_warmstart *w, cudaStream_t s, float lr, float b1, float b2, float eps);
+
+// one Adam step on (w->feat, (o->p - o->p0) / lbar) over the object's points
+int ws_train_on(pbd_warmstart *w, pbd_object *o, float lr, double *loss) {
+    cudaStream_t s = o->stream;
+    PBD_TRY(w->tgt.alloc(o->n));
+    k_targets<<<grid_for(o->n, 256), 256, 0, s>>>(o->n, o->p.p, o->p0.p, o->frest_b.p,
+                                                  w->scale.p, w->tgt.p);
+    PBD_LAUNCH();
+    PBD_TRY(train_pass(w, w->feat.p, w->tgt.p, o->n, o->n_free, s, loss));
+    return adam_step(w, s, lr, 0.9f, 0.999f, 1e-8f);
 }
 
 static int check_err(pbd_warmstart *w, cudaStream_t s) {
@@ -955,8 +993,12 @@ int pbd_warmstart_create(pbd_warmstart **out) {
     if ((r = w->params.alloc(kWsParams)) || (r = w->m.alloc(kWsParams)) ||
         (r = w->v.alloc(kWsParams)) || (r = w->grad.alloc(kWsParams)) ||
         (r = w->wtiles.alloc(kWtTotal)) || (r = w->bias.alloc(80)) || (r = w->loss.alloc(2)) ||
-        (r = w->err.alloc(1)))
+        (r = w->err.alloc(1)) || (r = w->scale.alloc(17)))
         return fail(r);
+    {
+        std::vector<float> ones(17, 1.f);
+        if ((r = w->scale.upload(ones.data(), 17, w->own))) return fail(r);
+    }
     cudaStream_t s = w->own;
     if (cudaMemsetAsync(w->params.p, 0, sizeof(float) * kWsParams, s) ||
         cudaMemsetAsync(w->m.p, 0, sizeof(float) * kWsParams, s) ||
@@ -992,6 +1034,23 @@ int pbd_warmstart_set_params(pbd_warmstart *w, const float *params, int n) {
     w->adam_t = 0;
     PBD_TRY(pack(w, s));
     PBD_CUDA(cudaStreamSynchronize(s));
+    return PBD_OK;
+}
+
+int pbd_warmstart_set_scales(pbd_warmstart *w, const float *scales, int n) {
+    PBD_CHECK(w && scales && n == 17, PBD_ERR_ARG, "expected 17 scales");
+    for (int k = 0; k < 17; ++k)
+        PBD_CHECK(std::isfinite(scales[k]) && scales[k] > 0.f, PBD_ERR_ARG,
+                  "scale %d must be finite and > 0", k);
+    PBD_TRY(w->scale.upload(scales, 17, w->own));
+    PBD_CUDA(cudaStreamSynchronize(w->own));
+    return PBD_OK;
+}
+
+int pbd_warmstart_get_scales(pbd_warmstart *w, float *scales, int n) {
+    PBD_CHECK(w && scales && n == 17, PBD_ERR_ARG, "expected 17 scales");
+    PBD_CUDA(cudaStreamSynchronize(w->own));
+    PBD_CUDA(cudaMemcpy(scales, w->scale.p, sizeof(float) * 17, cudaMemcpyDeviceToHost));
     return PBD_OK;
 }
 
@@ -1032,6 +1091,9 @@ int pbd_warmstart_forward(pbd_warmstart *w, const float *x, int n, float *y) {
 
 // one training pass over n rows already on the device; gradient added to
 // w->grad, loss (1/2 * mean over used rows of |y - t|^2) to *loss_out
+}  // extern "C"
+
+namespace pbd {
 static int train_pass(pbd_warmstart *w, const unsigned short *dx, const float4 *dt, int n,
                       int n_used, cudaStream_t s, double *loss_out) {
     float inv = n_used > 0 ? 1.f / (float)n_used : 0.f;
@@ -1047,6 +1109,10 @@ static int train_pass(pbd_warmstart *w, const unsigned short *dx, const float4 *
     }
     return PBD_OK;
 }
+
+}  // namespace pbd
+
+extern "C" {
 
 int pbd_warmstart_gradients(pbd_warmstart *w, const float *x, const float *t, const float *mask,
                             int n, float *grad, double *loss) {
@@ -1073,6 +1139,9 @@ int pbd_warmstart_gradients(pbd_warmstart *w, const float *x, const float *t, co
     return PBD_OK;
 }
 
+}  // extern "C"
+
+namespace pbd {
 static int adam_step(pbd_warmstart *w, cudaStream_t s, float lr, float b1, float b2, float eps) {
     ++w->adam_t;
     float c1 = (float)(1.0 / (1.0 - pow((double)b1, (double)w->adam_t)));
@@ -1082,6 +1151,10 @@ static int adam_step(pbd_warmstart *w, cudaStream_t s, float lr, float b1, float
     PBD_LAUNCH();
     return pack(w, s);
 }
+
+}  // namespace pbd
+
+extern "C" {
 
 int pbd_warmstart_adam(pbd_warmstart *w, float lr, float beta1, float beta2, float eps) {
     PBD_CHECK(w && lr >= 0.f, PBD_ERR_ARG, "bad argument");
@@ -1107,7 +1180,7 @@ int pbd_warmstart_record(pbd_warmstart *w, pbd_object *o) {
         PBD_TRY(w->feat.alloc(16 * (size_t)o->n));
         w->feat_cap = o->n;
     }
-    k_features<<<grid_for(o->n, 256), 256, 0, s>>>(o->n, feat_args(o, o->p0.p), w->feat.p);
+    k_features<<<grid_for(o->n, 256), 256, 0, s>>>(o->n, feat_args(o, o->p0.p, w), w->feat.p);
     PBD_LAUNCH();
     return PBD_OK;
 }
@@ -1118,7 +1191,8 @@ int pbd_warmstart_train_step(pbd_warmstart *w, pbd_object *o, float lr, double *
               "pbd_warmstart_record has not run on this object");
     cudaStream_t s = o->stream;
     PBD_TRY(w->tgt.alloc(o->n));
-    k_targets<<<grid_for(o->n, 256), 256, 0, s>>>(o->n, o->p.p, o->p0.p, o->frest_b.p, w->tgt.p);
+    k_targets<<<grid_for(o->n, 256), 256, 0, s>>>(o->n, o->p.p, o->p0.p, o->frest_b.p,
+                                                  w->scale.p, w->tgt.p);
     PBD_LAUNCH();
     PBD_TRY(train_pass(w, w->feat.p, w->tgt.p, o->n, o->n_free, s, loss));
     PBD_TRY(adam_step(w, s, lr, 0.9f, 0.999f, 1e-8f));
@@ -1145,7 +1219,7 @@ int pbd_warmstart_features(pbd_warmstart *w, pbd_object *o, float *x) {
     DBuf<unsigned short> f;
     PBD_TRY(f.alloc(16 * (size_t)o->n));
     PBD_TRY(ws_eval_hinges(o, o->p.p));
-    k_features<<<grid_for(o->n, 256), 256, 0, s>>>(o->n, feat_args(o, o->p.p), f.p);
+    k_features<<<grid_for(o->n, 256), 256, 0, s>>>(o->n, feat_args(o, o->p.p, w), f.p);
     PBD_LAUNCH();
     std::vector<unsigned short> h(16 * (size_t)o->n);
     PBD_CUDA(cudaMemcpyAsync(h.data(), f.p, sizeof(unsigned short) * h.size(), cudaMemcpyDeviceToHost, s));
@@ -1154,6 +1228,16 @@ int pbd_warmstart_features(pbd_warmstart *w, pbd_object *o, float *x) {
         uint32_t u = (uint32_t)h[k] << 16;
         memcpy(&x[k], &u, 4);
     }
+    return PBD_OK;
+}
+
+int pbd_object_set_correction(pbd_object *o, const float *d) {
+    PBD_CHECK(o && d, PBD_ERR_ARG, "null argument");
+    if (!o->dprev.p) PBD_TRY(o->dprev.alloc(o->n));
+    std::vector<float4> h(o->n);
+    for (int i = 0; i < o->n; ++i) h[i] = make_float4(d[3 * i], d[3 * i + 1], d[3 * i + 2], 0.f);
+    PBD_CUDA(cudaMemcpyAsync(o->dprev.p, h.data(), sizeof(float4) * o->n, cudaMemcpyHostToDevice, o->stream));
+    PBD_CUDA(cudaStreamSynchronize(o->stream));
     return PBD_OK;
 }
 

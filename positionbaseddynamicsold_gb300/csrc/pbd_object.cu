@@ -372,7 +372,7 @@ __device__ __forceinline__ void project_anchor(float4 a, const Pos &p) {
 // phase writes) are loaded first, the next phase is allowed to launch, and
 // positions are touched only after griddepcontrol.wait, i.e. after the
 // previous phase has completed and its writes are visible.
-__global__ void __launch_bounds__(256) k_project_color(const int4 *__restrict__ drec, int nd,
+__global__ void __launch_bounds__(512) k_project_color(const int4 *__restrict__ drec, int nd,
                                                        const int4 *__restrict__ bidx,
                                                        const float2 *__restrict__ bpar, int nb,
                                                        const float4 *__restrict__ arec, int na,
@@ -644,8 +644,8 @@ static int launch_sweep_per_color(pbd_object *o, int iter, const float *expk_dev
         int tot = nd + nb + na;
         if (!tot) continue;
         cudaLaunchConfig_t cfg = {};
-        cfg.gridDim = dim3(grid_for(tot, 256));
-        cfg.blockDim = dim3(256);
+        cfg.gridDim = dim3(grid_for(tot, o->gs_block));
+        cfg.blockDim = dim3(o->gs_block);
         cfg.stream = o->stream;
         cudaLaunchAttribute at[1];
         at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
@@ -1606,6 +1606,105 @@ int pbd_solver_get_gs_path(pbd_solver *s, int *path) {
 int pbd_solver_graph_kernels(pbd_solver *s, long long *n) {
     PBD_CHECK(s && n, PBD_ERR_ARG, "null argument");
     *n = s->gexec ? s->g_kernels : 0;
+    return PBD_OK;
+}
+
+// Times `iterations` sweeps, replayed from a CUDA graph, for every launch
+// form that applies to the object (per-color launches with 64..512 threads
+// per block; the cluster form when the object fits one cluster), keeps the
+// fastest and restores the predicted positions.  Every form gives the same
+// result, so the choice only changes speed.
+int pbd_solver_autotune(pbd_solver *s, int iterations, int reps, pbd_autotune_result *res) {
+    PBD_CHECK(s && s->obj && res, PBD_ERR_ARG, "null argument");
+    PBD_CHECK(iterations >= 1 && reps >= 1, PBD_ERR_ARG, "need iterations, reps >= 1");
+    pbd_object *o = s->obj;
+    PBD_CHECK(o->sorted, PBD_ERR_STATE, "constraints are not color-sorted");
+    memset(res, 0, sizeof(*res));
+    cudaStream_t st = o->stream;
+    DBuf<float4> save;
+    PBD_TRY(save.alloc(o->n));
+    PBD_CUDA(cudaMemcpyAsync(save.p, o->p.p, sizeof(float4) * o->n, cudaMemcpyDeviceToDevice, st));
+    struct Cand {
+        int path, block;
+    };
+    std::vector<Cand> cands = {{PBD_GS_PER_COLOR, 64}, {PBD_GS_PER_COLOR, 128},
+                               {PBD_GS_PER_COLOR, 256}, {PBD_GS_PER_COLOR, 512}};
+    if (s->n_inst_spheres == 0) {
+        PBD_TRY(cluster_plan(o));
+        if (o->cl_state == 1) cands.push_back({PBD_GS_CLUSTER, kClusterThreads});
+    }
+    const int keep_path = s->gs_path, keep_block = o->gs_block;
+    cudaEvent_t e0, e1;
+    PBD_CUDA(cudaEventCreate(&e0));
+    PBD_CUDA(cudaEventCreate(&e1));
+    int best = -1;
+    double best_us = 0.0;
+    int rc = PBD_OK;
+    for (size_t k = 0; k < cands.size() && k < 8 && rc == PBD_OK; ++k) {
+        s->gs_path = cands[k].path;
+        if (cands[k].path == PBD_GS_PER_COLOR) o->gs_block = cands[k].block;
+        cudaGraph_t g = nullptr;
+        cudaGraphExec_t ge = nullptr;
+        if (cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+            rc = PBD_ERR_CUDA;
+            break;
+        }
+        int r = launch_sweeps(s, 0, iterations, true);
+        cudaError_t e = cudaStreamEndCapture(st, &g);
+        if (r != PBD_OK || e != cudaSuccess) {
+            if (g) cudaGraphDestroy(g);
+            rc = r != PBD_OK ? r : PBD_ERR_CUDA;
+            break;
+        }
+        e = cudaGraphInstantiate(&ge, g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess) {
+            rc = PBD_ERR_CUDA;
+            break;
+        }
+        float ms = 0.f;
+        if (cudaGraphLaunch(ge, st) != cudaSuccess || cudaEventRecord(e0, st) != cudaSuccess) rc = PBD_ERR_CUDA;
+        for (int i = 0; i < reps && rc == PBD_OK; ++i)
+            if (cudaGraphLaunch(ge, st) != cudaSuccess) rc = PBD_ERR_CUDA;
+        if (rc == PBD_OK && (cudaEventRecord(e1, st) != cudaSuccess ||
+                             cudaEventSynchronize(e1) != cudaSuccess ||
+                             cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess))
+            rc = PBD_ERR_CUDA;
+        cudaGraphExecDestroy(ge);
+        cudaMemcpyAsync(o->p.p, save.p, sizeof(float4) * o->n, cudaMemcpyDeviceToDevice, st);
+        if (rc != PBD_OK) break;
+        double us = 1e3 * ms / ((double)reps * iterations);
+        res->path[k] = cands[k].path;
+        res->block[k] = cands[k].block;
+        res->us_per_sweep[k] = us;
+        res->n = (int)k + 1;
+        if (best < 0 || us < best_us) {
+            best = (int)k;
+            best_us = us;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (rc != PBD_OK || best < 0) {
+        s->gs_path = keep_path;
+        o->gs_block = keep_block;
+        set_error("autotune failed: %s", cudaGetErrorString(cudaGetLastError()));
+        return rc != PBD_OK ? rc : PBD_ERR_CUDA;
+    }
+    s->gs_path = cands[best].path;
+    if (cands[best].path == PBD_GS_PER_COLOR) o->gs_block = cands[best].block;
+    res->best = best;
+    if (s->gexec) cudaGraphExecDestroy(s->gexec);
+    s->gexec = nullptr;
+    if (s->rexec) cudaGraphExecDestroy(s->rexec);
+    s->rexec = nullptr;
+    PBD_CUDA(cudaStreamSynchronize(st));
+    return PBD_OK;
+}
+
+int pbd_solver_get_gs_block(pbd_solver *s, int *block) {
+    PBD_CHECK(s && s->obj && block, PBD_ERR_ARG, "null argument");
+    *block = s->obj->gs_block;
     return PBD_OK;
 }
 

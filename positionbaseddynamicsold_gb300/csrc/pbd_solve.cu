@@ -38,7 +38,7 @@ enum LoopMode { kStartPlain = 0, kGuardR0 = 1, kGuardR1 = 2, kCheck = 3 };
 
 __global__ void k_loop_ctl(int mode, const double *__restrict__ part, int nparts, double sqrt_den,
                            LoopState *__restrict__ L, cudaGraphConditionalHandle h, double target,
-                           int max_sweeps, int chunk) {
+                           int max_sweeps, int chunk, int min_sweeps) {
     double s = 0.0;
     for (int k = threadIdx.x; k < nparts; k += 32) s += part[k];
 #pragma unroll
@@ -66,7 +66,10 @@ __global__ void k_loop_ctl(int mode, const double *__restrict__ part, int nparts
         }
         L->r = r;
     }
-    int cont = L->r > target && L->sweeps + chunk <= max_sweeps;
+    // an accepted prediction is followed by at least min_sweeps sweeps
+    if (mode != kCheck) L->pred_used = mode == kGuardR1 && !L->revert;
+    const int need = L->pred_used ? min_sweeps : 0;
+    int cont = (L->r > target || L->sweeps < need) && L->sweeps + chunk <= max_sweeps;
     for (int j = 0; j < chunk; ++j) L->expk[j] = (float)(1.0 / (double)(L->sweeps + j + 1));
     if (!cont) {
         L->substeps += 1;
@@ -98,14 +101,15 @@ __global__ void __launch_bounds__(256) k_store_correction(int n, const float4 *_
 
 struct ResArgs {
     double target;
-    int max_sweeps, chunk;
+    int max_sweeps, chunk, min_sweeps;
 };
 
 static int loop_ctl(pbd_solver *s, int mode, cudaGraphConditionalHandle h, const ResArgs &a) {
     pbd_object *o = s->obj;
     PBD_TRY(launch_residual_parts(o, true, false, o->p.p));
     k_loop_ctl<<<1, 32, 0, o->stream>>>(mode, o->res_part.p, kResidualParts, sqrt(o->res_den_d),
-                                        s->loop.p, h, a.target, a.max_sweeps, a.chunk);
+                                        s->loop.p, h, a.target, a.max_sweeps, a.chunk,
+                                        a.min_sweeps);
     PBD_LAUNCH();
     return PBD_OK;
 }
@@ -124,43 +128,46 @@ static int record_chunk(pbd_solver *s, pbd_colli *c, cudaGraphConditionalHandle 
     return loop_ctl(s, kCheck, h, a);
 }
 
+// warm start of the advected positions o->p0 (= o->p): prediction, guard,
+// loop start
+static int warm_start(pbd_solver *s, cudaGraphConditionalHandle h, const ResArgs &a) {
+    pbd_object *o = s->obj;
+    PBD_TRY(ws_eval_hinges(o, o->p0.p));
+    PBD_TRY(launch_residual_parts(o, true, false, o->p0.p));
+    k_loop_ctl<<<1, 32, 0, o->stream>>>(kGuardR0, o->res_part.p, kResidualParts,
+                                        sqrt(o->res_den_d), s->loop.p, h, a.target,
+                                        a.max_sweeps, a.chunk, a.min_sweeps);
+    PBD_LAUNCH();
+    PBD_TRY(ws_infer(s->ws, o));
+    PBD_TRY(loop_ctl(s, kGuardR1, h, a));
+    k_revert<<<grid_for(o->n, 256), 256, 0, o->stream>>>(o->n, s->loop.p, o->p0.p, o->p.p);
+    PBD_LAUNCH();
+    return PBD_OK;
+}
+
 // advect, warm start or plain start; the loop follows (graph or host)
 static int record_prologue(pbd_solver *s, float dt, cudaGraphConditionalHandle h,
                            const ResArgs &a) {
     pbd_object *o = s->obj;
     PBD_TRY(launch_advect_p0(o, dt));
-    if (s->ws) {
-        PBD_TRY(ws_eval_hinges(o, o->p0.p));
-        PBD_TRY(launch_residual_parts(o, true, false, o->p0.p));
-        k_loop_ctl<<<1, 32, 0, o->stream>>>(kGuardR0, o->res_part.p, kResidualParts,
-                                            sqrt(o->res_den_d), s->loop.p, h, a.target,
-                                            a.max_sweeps, a.chunk);
-        PBD_LAUNCH();
-        PBD_TRY(ws_infer(s->ws, o));
-        PBD_TRY(loop_ctl(s, kGuardR1, h, a));
-        k_revert<<<grid_for(o->n, 256), 256, 0, o->stream>>>(o->n, s->loop.p, o->p0.p, o->p.p);
-        PBD_LAUNCH();
-        return PBD_OK;
-    }
+    if (s->ws) return warm_start(s, h, a);
     return loop_ctl(s, kStartPlain, h, a);
 }
 
+static int final_contacts(pbd_solver *s, pbd_colli *c);
+
 static int record_epilogue(pbd_solver *s, float dt, pbd_colli *c) {
     pbd_object *o = s->obj;
-    if (c) {
-        PBD_TRY(ccd_detect(c));
-        PBD_TRY(ccd_resolve(c, c->iterations));
-        PBD_TRY(launch_obstacles(s));
-    }
+    PBD_TRY(final_contacts(s, c));
     k_store_correction<<<grid_for(o->n, 256), 256, 0, o->stream>>>(o->n, o->p.p, o->p0.p,
                                                                    o->dprev.p);
     PBD_LAUNCH();
     return launch_integrate(o, dt);
 }
 
-static int eager_substep(pbd_solver *s, float dt, pbd_colli *c, const ResArgs &a) {
+// the loop driven from the host: a chunk while the device says so
+static int eager_loop(pbd_solver *s, pbd_colli *c, const ResArgs &a) {
     pbd_object *o = s->obj;
-    PBD_TRY(record_prologue(s, dt, 0, a));
     for (;;) {
         int cont = 0;
         PBD_CUDA(cudaMemcpyAsync(&cont, &s->loop.p->cont, sizeof(int), cudaMemcpyDeviceToHost,
@@ -169,7 +176,20 @@ static int eager_substep(pbd_solver *s, float dt, pbd_colli *c, const ResArgs &a
         if (!cont) break;
         PBD_TRY(record_chunk(s, c, 0, a));
     }
+    return PBD_OK;
+}
+
+static int eager_substep(pbd_solver *s, float dt, pbd_colli *c, const ResArgs &a) {
+    PBD_TRY(record_prologue(s, dt, 0, a));
+    PBD_TRY(eager_loop(s, c, a));
     return record_epilogue(s, dt, c);
+}
+
+static int final_contacts(pbd_solver *s, pbd_colli *c) {
+    if (!c) return PBD_OK;
+    PBD_TRY(ccd_detect(c));
+    PBD_TRY(ccd_resolve(c, c->iterations));
+    return launch_obstacles(s);
 }
 
 // Captures `substeps` substeps on o->stream (which is capturing); the body of
@@ -234,7 +254,7 @@ static int build_graph(pbd_solver *s, float dt, int substeps, pbd_colli *c, cons
     }
     PBD_CUDA(e);
     // kernel nodes per pass (the WHILE bodies counted once)
-    long long nk = 0;
+    long long nk = 0, nbody = 0;
     todo.push_back(g);
     for (cudaGraph_t cur : todo) {
         size_t nn = 0;
@@ -244,10 +264,11 @@ static int build_graph(pbd_solver *s, float dt, int substeps, pbd_colli *c, cons
         for (size_t i = 0; i < nn; ++i) {
             cudaGraphNodeType t;
             if (cudaGraphNodeGetType(nodes[i], &t) == cudaSuccess && t == cudaGraphNodeTypeKernel)
-                ++nk;
+                ++(cur == g ? nk : nbody);
         }
     }
-    *n_kernels = nk;
+    n_kernels[0] = nk;
+    n_kernels[1] = todo.size() > 1 ? nbody / (long long)(todo.size() - 1) : 0;
     e = cudaGraphInstantiate(exec, g, 0);
     cudaGraphDestroy(g);
     PBD_CUDA(e);
@@ -273,9 +294,10 @@ using namespace pbd;
 
 extern "C" {
 
-int pbd_solver_set_warmstart(pbd_solver *s, pbd_warmstart *w) {
-    PBD_CHECK(s, PBD_ERR_ARG, "null solver");
+int pbd_solver_set_warmstart(pbd_solver *s, pbd_warmstart *w, int min_sweeps) {
+    PBD_CHECK(s && min_sweeps >= 0, PBD_ERR_ARG, "bad argument");
     s->ws = w;
+    s->min_sweeps = min_sweeps;
     if (s->rexec) cudaGraphExecDestroy(s->rexec);
     s->rexec = nullptr;
     return PBD_OK;
@@ -287,7 +309,7 @@ int pbd_solver_step_to_residual(pbd_solver *s, float dt, int substeps, pbd_colli
     PBD_CHECK(substeps >= 0 && chunk >= 1 && chunk <= kMaxChunk && max_sweeps >= 0, PBD_ERR_ARG,
               "need substeps >= 0, 1 <= chunk <= %d, max_sweeps >= 0", kMaxChunk);
     PBD_TRY(ensure_ready(s, c));
-    ResArgs a{target, max_sweeps, chunk};
+    ResArgs a{target, max_sweeps, chunk, s->min_sweeps};
     pbd_object *o = s->obj;
     if (!use_graph) {
         for (int k = 0; k < substeps; ++k) PBD_TRY(eager_substep(s, dt, c, a));
@@ -295,7 +317,7 @@ int pbd_solver_step_to_residual(pbd_solver *s, float dt, int substeps, pbd_colli
     }
     int sig = s->sphere_on * 3 + s->ground_on * 7 +
               (c ? c->response * 11 + c->iterations * 13 : 0) + (s->n_inst_spheres > 0) * 17 +
-              (s->ws != nullptr) * 19 + (o->pdl ? 23 : 0);
+              (s->ws != nullptr) * 19 + s->min_sweeps * 29 + (o->pdl ? 23 : 0);
     if (s->rexec && (s->r_dt != dt || s->r_sub != substeps || s->r_colli != c ||
                      s->r_sig != sig || s->r_target != target || s->r_max != max_sweeps ||
                      s->r_chunk != chunk)) {
@@ -305,12 +327,12 @@ int pbd_solver_step_to_residual(pbd_solver *s, float dt, int substeps, pbd_colli
     if (!s->rexec) {
         if (c) PBD_TRY(ccd_detect(c));  // sizes every buffer before capture
         PBD_CUDA(cudaStreamSynchronize(o->stream));
-        int r = build_graph(s, dt, substeps, c, a, &s->rexec, &s->r_kernels);
+        int r = build_graph(s, dt, substeps, c, a, &s->rexec, s->r_kernels);
         if (r != PBD_OK && o->pdl) {
             // retry with plain stream ordering between the color phases
             cudaGetLastError();
             o->pdl = false;
-            r = build_graph(s, dt, substeps, c, a, &s->rexec, &s->r_kernels);
+            r = build_graph(s, dt, substeps, c, a, &s->rexec, s->r_kernels);
         }
         PBD_TRY(r);
         s->r_dt = dt;
@@ -322,6 +344,78 @@ int pbd_solver_step_to_residual(pbd_solver *s, float dt, int substeps, pbd_colli
         s->r_chunk = chunk;
     }
     PBD_CUDA(cudaGraphLaunch(s->rexec, o->stream));
+    return PBD_OK;
+}
+
+int pbd_solver_project_to_residual(pbd_solver *s, pbd_colli *c, double target, int max_sweeps,
+                                  int chunk, int *sweeps, double *residual) {
+    PBD_CHECK(s && s->obj, PBD_ERR_STATE, "solver has no target");
+    PBD_CHECK(chunk >= 1 && chunk <= kMaxChunk && max_sweeps >= 0, PBD_ERR_ARG,
+              "need 1 <= chunk <= %d, max_sweeps >= 0", kMaxChunk);
+    PBD_TRY(ensure_ready(s, c));
+    pbd_object *o = s->obj;
+    ResArgs a{target, max_sweeps, chunk, s->min_sweeps};
+    PBD_CUDA(cudaMemcpyAsync(o->p0.p, o->p.p, sizeof(float4) * o->n, cudaMemcpyDeviceToDevice,
+                             o->stream));
+    PBD_TRY(loop_ctl(s, kStartPlain, 0, a));
+    for (;;) {
+        int cont = 0;
+        PBD_CUDA(cudaMemcpyAsync(&cont, &s->loop.p->cont, sizeof(int), cudaMemcpyDeviceToHost,
+                                 o->stream));
+        PBD_CUDA(cudaStreamSynchronize(o->stream));
+        if (!cont) break;
+        PBD_TRY(record_chunk(s, c, 0, a));
+    }
+    if (c) {
+        PBD_TRY(ccd_detect(c));
+        PBD_TRY(ccd_resolve(c, c->iterations));
+        PBD_TRY(launch_obstacles(s));
+    }
+    k_store_correction<<<grid_for(o->n, 256), 256, 0, o->stream>>>(o->n, o->p.p, o->p0.p,
+                                                                   o->dprev.p);
+    PBD_LAUNCH();
+    LoopState L;
+    PBD_CUDA(cudaMemcpyAsync(&L, s->loop.p, sizeof(L), cudaMemcpyDeviceToHost, o->stream));
+    PBD_CUDA(cudaStreamSynchronize(o->stream));
+    if (sweeps) *sweeps = L.sweeps;
+    if (residual) *residual = L.r;
+    return PBD_OK;
+}
+
+int pbd_solver_train_substep(pbd_solver *s, pbd_warmstart *w, float dt, pbd_colli *c,
+                             double target, int max_sweeps, int chunk, float lr, int on_policy,
+                             double *loss) {
+    PBD_CHECK(s && s->obj && w, PBD_ERR_ARG, "null argument");
+    PBD_CHECK(chunk >= 1 && chunk <= kMaxChunk && max_sweeps >= 0, PBD_ERR_ARG,
+              "need 1 <= chunk <= %d, max_sweeps >= 0", kMaxChunk);
+    PBD_TRY(ensure_ready(s, c));
+    PBD_TRY(ws_prepare(w, s->obj));
+    pbd_object *o = s->obj;
+    ResArgs a{target, max_sweeps, chunk, s->min_sweeps};
+    // the plain solve of the advected state gives the target
+    PBD_TRY(launch_advect_p0(o, dt));
+    PBD_TRY(ws_record(w, o));
+    PBD_TRY(loop_ctl(s, kStartPlain, 0, a));
+    PBD_TRY(eager_loop(s, c, a));
+    PBD_TRY(final_contacts(s, c));
+    PBD_TRY(ws_train_on(w, o, lr, loss));
+    if (on_policy) {
+        // the trajectory continues from the warm-started solve of the same state
+        PBD_CUDA(cudaMemcpyAsync(o->p.p, o->p0.p, sizeof(float4) * o->n, cudaMemcpyDeviceToDevice,
+                                 o->stream));
+        pbd_warmstart *keep = s->ws;
+        s->ws = w;
+        int r = warm_start(s, 0, a);
+        s->ws = keep;
+        PBD_TRY(r);
+        PBD_TRY(eager_loop(s, c, a));
+        PBD_TRY(final_contacts(s, c));
+    }
+    k_store_correction<<<grid_for(o->n, 256), 256, 0, o->stream>>>(o->n, o->p.p, o->p0.p,
+                                                                   o->dprev.p);
+    PBD_LAUNCH();
+    PBD_TRY(launch_integrate(o, dt));
+    PBD_CUDA(cudaStreamSynchronize(o->stream));
     return PBD_OK;
 }
 
@@ -349,9 +443,10 @@ int pbd_solver_solve_stats(pbd_solver *s, pbd_solve_stats *st, int reset) {
     return PBD_OK;
 }
 
-int pbd_solver_residual_graph_kernels(pbd_solver *s, long long *n) {
-    PBD_CHECK(s && n, PBD_ERR_ARG, "null argument");
-    *n = s->rexec ? s->r_kernels : 0;
+int pbd_solver_residual_graph_kernels(pbd_solver *s, long long *n_outer, long long *n_body) {
+    PBD_CHECK(s && n_outer && n_body, PBD_ERR_ARG, "null argument");
+    *n_outer = s->rexec ? s->r_kernels[0] : 0;
+    *n_body = s->rexec ? s->r_kernels[1] : 0;
     return PBD_OK;
 }
 

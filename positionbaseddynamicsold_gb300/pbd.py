@@ -68,11 +68,14 @@ EXPORTS = [
     "pbd_residual_noalloc",
     "pbd_constraints_residual_stretch", "pbd_solver_step_to_residual", "pbd_solver_solve_stats",
     "pbd_solver_residual_graph_kernels", "pbd_object_get_correction",
+    "pbd_object_set_correction",
     "pbd_warmstart_num_params", "pbd_warmstart_create", "pbd_warmstart_destroy",
     "pbd_warmstart_set_params", "pbd_warmstart_get_params", "pbd_warmstart_forward",
+    "pbd_warmstart_set_scales", "pbd_warmstart_get_scales",
     "pbd_warmstart_gradients", "pbd_warmstart_set_gradient", "pbd_warmstart_adam",
     "pbd_warmstart_record", "pbd_warmstart_train_step", "pbd_warmstart_features",
-    "pbd_warmstart_predict", "pbd_solver_set_warmstart",
+    "pbd_warmstart_predict", "pbd_solver_set_warmstart", "pbd_solver_project_to_residual",
+    "pbd_solver_autotune", "pbd_solver_get_gs_block", "pbd_solver_train_substep",
 ]
 
 
@@ -116,6 +119,11 @@ def load(build_if_missing: bool = True) -> C.CDLL:
                                        C.c_void_p]
     L.pbd_solver_step_to_residual.argtypes = [C.c_void_p, C.c_float, C.c_int, C.c_void_p,
                                               C.c_double, C.c_int, C.c_int, C.c_int]
+    L.pbd_solver_project_to_residual.argtypes = [C.c_void_p, C.c_void_p, C.c_double, C.c_int,
+                                                 C.c_int, C.c_void_p, C.c_void_p]
+    L.pbd_solver_train_substep.argtypes = [C.c_void_p, C.c_void_p, C.c_float, C.c_void_p,
+                                           C.c_double, C.c_int, C.c_int, C.c_float, C.c_int,
+                                           C.c_void_p]
     L.pbd_warmstart_adam.argtypes = [C.c_void_p, C.c_float, C.c_float, C.c_float, C.c_float]
     L.pbd_warmstart_train_step.argtypes = [C.c_void_p, C.c_void_p, C.c_float, C.c_void_p]
     _LIB = L
@@ -302,6 +310,10 @@ class PBDObject:
     def correction(self):
         """p_final - p_advected of the last substep solved to a residual"""
         return self._get3(self.L.pbd_object_get_correction)
+
+    def set_correction(self, d):
+        d = _f32(d).reshape(-1)
+        _check(self.L.pbd_object_set_correction(self.h, _p(d)))
 
     def prepare(self, iterations=20000):
         """EdgeColoring + SortEdgesColors + EvalWorksets; returns sweeps."""
@@ -504,9 +516,10 @@ class SolverPBD:
         _check(self.L.pbd_solver_step(self.h, dt, substeps, iterations,
                                       colli.h if colli else None, int(use_graph)))
 
-    def set_warmstart(self, ws):
+    def set_warmstart(self, ws, min_sweeps=0):
         self.ws = ws
-        _check(self.L.pbd_solver_set_warmstart(self.h, ws.h if ws is not None else None))
+        _check(self.L.pbd_solver_set_warmstart(self.h, ws.h if ws is not None else None,
+                                               int(min_sweeps)))
 
     def step_to_residual(self, dt, substeps=1, target=1e-4, max_sweeps=60, chunk=5, colli=None,
                          use_graph=True):
@@ -516,15 +529,48 @@ class SolverPBD:
                                                   colli.h if colli else None, float(target),
                                                   int(max_sweeps), int(chunk), int(use_graph)))
 
+    def project_to_residual(self, target=1e-4, max_sweeps=60, chunk=5, colli=None):
+        """the solve alone (no advect / integration); returns (sweeps, residual)"""
+        sw = C.c_int()
+        r = C.c_double()
+        _check(self.L.pbd_solver_project_to_residual(self.h, colli.h if colli else None,
+                                                     float(target), int(max_sweeps), int(chunk),
+                                                     C.byref(sw), C.byref(r)))
+        return sw.value, r.value
+
+    def autotune(self, iterations=15, reps=5):
+        """time the GS launch forms and keep the fastest; returns the table"""
+        r = _AutotuneResult()
+        _check(self.L.pbd_solver_autotune(self.h, int(iterations), int(reps), C.byref(r)))
+        rows = [{"path": r.path[k], "block": r.block[k], "us_per_sweep": r.us_per_sweep[k]}
+                for k in range(r.n)]
+        return {"candidates": rows, "best": r.best}
+
+    def gs_block(self):
+        v = C.c_int()
+        _check(self.L.pbd_solver_get_gs_block(self.h, C.byref(v)))
+        return v.value
+
+    def train_substep(self, ws, dt, target=1e-3, max_sweeps=200, chunk=5, lr=1e-3,
+                      on_policy=True, colli=None, want_loss=False):
+        """one training substep of the warm start (see pbd_solver_train_substep)"""
+        loss = C.c_double()
+        _check(self.L.pbd_solver_train_substep(self.h, ws.h, dt, colli.h if colli else None,
+                                               float(target), int(max_sweeps), int(chunk),
+                                               float(lr), int(on_policy),
+                                               C.byref(loss) if want_loss else None))
+        return loss.value if want_loss else None
+
     def solve_stats(self, reset=False):
         st = _SolveStats()
         _check(self.L.pbd_solver_solve_stats(self.h, C.byref(st), int(reset)))
         return {k: getattr(st, k) for k, _ in _SolveStats._fields_}
 
     def residual_graph_kernels(self):
-        n = C.c_longlong()
-        _check(self.L.pbd_solver_residual_graph_kernels(self.h, C.byref(n)))
-        return n.value
+        """(kernels outside the WHILE bodies, kernels in one body)"""
+        a, b = C.c_longlong(), C.c_longlong()
+        _check(self.L.pbd_solver_residual_graph_kernels(self.h, C.byref(a), C.byref(b)))
+        return a.value, b.value
 
 
 class _SolveStats(C.Structure):
@@ -533,18 +579,25 @@ class _SolveStats(C.Structure):
                 ("last_sweeps", C.c_int), ("last_r0", C.c_double), ("last_r1", C.c_double)]
 
 
+class _AutotuneResult(C.Structure):
+    _fields_ = [("n", C.c_int), ("best", C.c_int), ("path", C.c_int * 8), ("block", C.c_int * 8),
+                ("us_per_sweep", C.c_double * 8)]
+
+
 class WarmStart:
     """Learned warm start: per-point MLP 16 -> 64 -> 64 -> 3 on the tensor
     cores (no reference counterpart).  Parameters: W1[64][16], W2[64][64],
     b2[64], W3[3][64], b3[3] flattened in that order."""
 
-    def __init__(self, params=None):
+    def __init__(self, params=None, scales=None):
         self.L = load()
         self.h = C.c_void_p()
         _check(self.L.pbd_warmstart_create(C.byref(self.h)))
         self.n_params = self.L.pbd_warmstart_num_params()
         if params is not None:
             self.set_params(params)
+        if scales is not None:
+            self.set_scales(scales)
 
     def close(self):
         if self.h:
@@ -560,6 +613,16 @@ class WarmStart:
     def set_params(self, params):
         a = _f32(params).ravel()
         _check(self.L.pbd_warmstart_set_params(self.h, _p(a), len(a)))
+
+    def set_scales(self, scales):
+        """17 scales: features 0..14 (15 unused), then the output"""
+        a = _f32(scales).ravel()
+        _check(self.L.pbd_warmstart_set_scales(self.h, _p(a), len(a)))
+
+    def scales(self):
+        a = np.zeros(17, np.float32)
+        _check(self.L.pbd_warmstart_get_scales(self.h, _p(a), 17))
+        return a
 
     def params(self):
         a = np.zeros(self.n_params, np.float32)
