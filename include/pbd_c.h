@@ -167,10 +167,12 @@ int pbd_solver_step(pbd_solver *s, float dt, int substeps, int iterations, pbd_c
  * color (any size); PBD_GS_CLUSTER keeps every point in the distributed
  * shared memory of one 16-block thread-block cluster (objects up to 131,072
  * points) and separates colors by cluster barriers; PBD_GS_AUTO (default)
- * takes the per-color form, the faster one on GB300 as measured so far.
- * Both give identical results.
+ * takes the per-color form; PBD_GS_GRID runs every color of a sweep in one
+ * cooperative launch (one block per SM, a bounded grid barrier between the
+ * color phases).  All forms give identical results; pbd_solver_autotune
+ * picks the fastest for an object.
  * No reference counterpart. */
-enum { PBD_GS_AUTO = 0, PBD_GS_PER_COLOR = 1, PBD_GS_CLUSTER = 2 };
+enum { PBD_GS_AUTO = 0, PBD_GS_PER_COLOR = 1, PBD_GS_CLUSTER = 2, PBD_GS_GRID = 3 };
 int pbd_solver_set_gs_path(pbd_solver *s, int path);
 /* the form the next sweep will use (PBD_GS_PER_COLOR or PBD_GS_CLUSTER) */
 int pbd_solver_get_gs_path(pbd_solver *s, int *path);

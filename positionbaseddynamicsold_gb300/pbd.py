@@ -20,7 +20,7 @@ from . import build as _build
 DISTANCE, BENDING, ANCHOR = 0x001, 0x010, 0x100
 JACOBI, GAUSSSEIDEL = 0, 1
 RESPONSE_REFERENCE, RESPONSE_MASS_WEIGHTED = 0, 1
-GS_AUTO, GS_PER_COLOR, GS_CLUSTER = 0, 1, 2
+GS_AUTO, GS_PER_COLOR, GS_CLUSTER, GS_GRID = 0, 1, 2, 3
 _ERRS = {1: "ARG", 2: "OOM", 3: "CUDA", 4: "TIMEOUT", 5: "OVERFLOW", 6: "STATE"}
 
 
