@@ -341,6 +341,7 @@ int launch_sweeps(pbd_solver *s, int it0, int it1, bool obstacles_inside);
 // one per-color sweep whose stiffness exponent 1/(iter+1) is read from
 // device memory (the solve-to-residual loop)
 int launch_sweep_dev(pbd_solver *s, const float *expk_dev, bool obstacles_inside);
+int prepare_gs_path(pbd_solver *s);
 // residual partial sums of pos over the distance and/or bending records
 // into o->res_part (kResidualParts doubles)
 constexpr int kResidualParts = 4 * kNumSMs;

@@ -926,12 +926,24 @@ static int resolved_path(pbd_solver *s) {
     return s->obj->cl_state == 1 ? PBD_GS_CLUSTER : -2;
 }
 
+// Everything a launch form needs before a stream capture (plans, uploads,
+// barrier state); capture forbids allocation and synchronisation.
+int prepare_gs_path(pbd_solver *s) {
+    pbd_object *o = s->obj;
+    if (s->gs_path == PBD_GS_CLUSTER) PBD_TRY(cluster_plan(o));
+    if (s->gs_path == PBD_GS_GRID) {
+        PBD_TRY(grid_plan(o));
+        if (!s->gbar.p) PBD_TRY(s->gbar.alloc(1));
+    }
+    return PBD_OK;
+}
+
 // sweeps it0..it1-1 of the cooperative form; expk_dev (device) overrides the
 // exponent 1/(it+1) of a single sweep
 static int launch_sweeps_grid(pbd_solver *s, int it0, int it1, bool obstacles_inside,
                               const float *expk_dev) {
     pbd_object *o = s->obj;
-    if (!s->gbar.p) PBD_TRY(s->gbar.alloc(1));
+    PBD_CHECK(s->gbar.p, PBD_ERR_STATE, "cooperative GS form used before it was prepared");
     PBD_CUDA(cudaMemsetAsync(s->gbar.p, 0, sizeof(int4), o->stream));
     const bool inst = obstacles_inside && s->n_inst_spheres > 0 && o->has_inst;
     cudaLaunchConfig_t cfg = {};
@@ -962,6 +974,9 @@ int launch_sweeps(pbd_solver *s, int it0, int it1, bool obstacles_inside) {
     pbd_object *o = s->obj;
     PBD_CHECK(o->sorted, PBD_ERR_STATE,
               "no color-sorted constraints: run edge coloring and SortEdgesColors first");
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    PBD_CUDA(cudaStreamIsCapturing(o->stream, &cap));
+    if (cap == cudaStreamCaptureStatusNone) PBD_TRY(prepare_gs_path(s));
     int path = resolved_path(s);
     PBD_CHECK(path != -1, PBD_ERR_CUDA, "cluster plan failed: %s", pbd_last_error());
     PBD_CHECK(path != -2, PBD_ERR_STATE,
@@ -1729,7 +1744,7 @@ int pbd_solver_step(pbd_solver *s, float dt, int substeps, int iterations, pbd_c
     cudaStream_t st = s->obj->stream;
     if (!s->gexec) {
         if (c) PBD_TRY(ccd_detect(c));  // sizes every buffer before capture
-        if (s->gs_path == PBD_GS_CLUSTER) PBD_TRY(cluster_plan(s->obj));  // outside the capture
+        PBD_TRY(prepare_gs_path(s));    // plans and uploads outside the capture
         PBD_CUDA(cudaStreamSynchronize(st));
         cudaGraph_t g;
         PBD_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
@@ -1809,7 +1824,10 @@ int pbd_solver_autotune(pbd_solver *s, int iterations, int reps, pbd_autotune_re
         if (o->cl_state == 1) cands.push_back({PBD_GS_CLUSTER, kClusterThreads});
     }
     PBD_TRY(grid_plan(o));
-    if (o->gr_state == 1) cands.push_back({PBD_GS_GRID, kGridThreads});
+    if (o->gr_state == 1) {
+        cands.push_back({PBD_GS_GRID, kGridThreads});
+        if (!s->gbar.p) PBD_TRY(s->gbar.alloc(1));
+    }
     const int keep_path = s->gs_path, keep_block = o->gs_block;
     cudaEvent_t e0, e1;
     PBD_CUDA(cudaEventCreate(&e0));

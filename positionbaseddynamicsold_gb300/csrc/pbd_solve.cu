@@ -285,6 +285,7 @@ static int ensure_ready(pbd_solver *s, pbd_colli *c) {
     }
     PBD_TRY(build_feature_stencil(o));  // p0 / dprev buffers and stencils
     if (s->ws) PBD_TRY(ws_prepare(s->ws, o));
+    PBD_TRY(prepare_gs_path(s));
     return PBD_OK;
 }
 
