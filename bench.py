@@ -26,7 +26,8 @@ same state on one host thread.
 Other modes: --solve residual runs every substep to a stretch-residual
 target (--target, at most --max-sweeps sweeps in chunks of --chunk, the loop
 on the device in a CUDA graph), --learned adds the trained warm start,
---autotune picks the GS launch form first.  `learned_warm_start` in the line
+the autotuner picks the GS launch form after the pre-roll (--no-autotune
+keeps the default form).  `learned_warm_start` in the line
 compares the trained network with the plain sweeps on held-out cloths of its
 training family (see learned_eval).
 
@@ -173,15 +174,13 @@ def run_ours(args, rank, world):
     torch.cuda.set_device(0 if world == 1 else int(os.environ.get("LOCAL_RANK", rank)))
     sc, cfg, colli_on, tl = make_workload(args.workload)
     obj, solver, shs, cs = setup(sc, colli_on, tl)
-    solver.set_gs_path({"auto": 0, "per-color": 1, "cluster": 2}[args.gs_path])
+    solver.set_gs_path({"auto": 0, "per-color": 1, "cluster": 2, "grid": 3}[args.gs_path])
     stream = torch.cuda.ExternalStream(obj.stream())
     nd = int((sc["ctype"] == scenes.DISTANCE).sum())
     nb = int((sc["ctype"] == scenes.BENDING).sum())
     n_colors = obj.eval_worksets()
     iters = cfg["gs_iterations"]
 
-    if args.autotune:
-        cfg["autotune"] = solver.autotune(iterations=iters, reps=3)
     if args.solve == "residual":
         cfg["solve"] = {"target_stretch_residual": args.target, "max_sweeps": args.max_sweeps,
                         "chunk": args.chunk, "warm_start": bool(args.learned)}
@@ -201,6 +200,10 @@ def run_ours(args, rank, world):
     # pre-roll so the timed substeps include contacts
     for _ in range(args.preroll):
         step()
+    if not args.no_autotune and args.gs_path == "auto":
+        # the GS launch form picked on the workload's own state; the choice
+        # changes speed, never results
+        cfg["autotune"] = solver.autotune(iterations=iters, reps=3)
     for _ in range(args.warmup):
         step()
     obj.sync()
@@ -264,7 +267,10 @@ def run_ours(args, rank, world):
         e1.record(stream)
     torch.cuda.synchronize()
     gs_ms = e0.elapsed_time(e1)
-    n_launch = reps * iters * n_colors
+    gs_form = solver.gs_path()
+    gs_kernel = {1: "k_project_color", 2: "k_gs_cluster", 3: "k_gs_grid"}[gs_form]
+    # per-color form: one launch per color phase; the others one per sweep
+    n_launch = reps * iters * (n_colors if gs_form == 1 else 1)
     achieved = reps * iters * bytes_sweep / (gs_ms / 1e3) / 1e9
     obj.set_positions(pos_save)
     obj.set_predicted(prd_save)
@@ -298,7 +304,7 @@ def run_ours(args, rank, world):
                        preroll_substeps=args.preroll),
         "e2e": e2e,
         "gpu_launches": launches_total,
-        "roofline": {"bound": "hbm", "kernel": "k_project_color", "achieved": achieved,
+        "roofline": {"bound": "hbm", "kernel": gs_kernel, "achieved": achieved,
                      "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "peak_source": peak_kind, "traffic": args.traffic,
                      "launches_timed": n_launch, "avg_launch_us": gs_ms * 1e3 / n_launch,
@@ -448,7 +454,7 @@ def main():
                                                           "hanging32"])
     ap.add_argument("--preroll", type=int, default=120)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--gs-path", default="auto", choices=["auto", "per-color", "cluster"])
+    ap.add_argument("--gs-path", default="auto", choices=["auto", "per-color", "cluster", "grid"])
     ap.add_argument("--profile-range", action="store_true",
                     help="cudaProfilerStart/Stop around the timed substeps (for ncu "
                          "--profile-from-start off)")
@@ -462,8 +468,9 @@ def main():
     ap.add_argument("--chunk", type=int, default=10)
     ap.add_argument("--learned", action="store_true",
                     help="with --solve residual: warm start from the trained network")
-    ap.add_argument("--autotune", action="store_true",
-                    help="pick the GS launch form with the autotuner before timing")
+    ap.add_argument("--no-autotune", action="store_true",
+                    help="keep the default GS launch form (per-color, 256 threads) instead of "
+                         "the autotuner's pick")
     ap.add_argument("--no-learned-eval", action="store_true",
                     help="skip the learned-vs-plain evaluation on held-out hanging cloths")
     args = ap.parse_args()
