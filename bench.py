@@ -227,6 +227,7 @@ def run_ours(args, rank, world):
             step()
             ev[k][1].record(stream)
     torch.cuda.synchronize()
+    solver.check()   # raises if a sweep of the cooperative form ended early
     if args.profile_range:
         torch.cuda.profiler.stop()
     t_wall = time.perf_counter() - t_wall

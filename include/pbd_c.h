@@ -186,11 +186,18 @@ int pbd_solver_get_gs_path(pbd_solver *s, int *path);
 typedef struct pbd_autotune_result {
     int n;                  /* candidates timed                       */
     int best;               /* index of the one kept                  */
-    int path[8];            /* PBD_GS_PER_COLOR / PBD_GS_CLUSTER      */
+    int path[8];            /* PBD_GS_PER_COLOR / _CLUSTER / _GRID    */
     int block[8];           /* threads per block                      */
-    double us_per_sweep[8]; /* GPU time per sweep, microseconds       */
+    double us_per_sweep[8]; /* GPU time per sweep, microseconds; -1:
+                               the form's grid barrier gave up (never
+                               chosen)                                 */
 } pbd_autotune_result;
 int pbd_solver_autotune(pbd_solver *s, int iterations, int reps, pbd_autotune_result *result);
+/* Synchronise the solver's stream and report whether any sweep of the
+ * cooperative form (PBD_GS_GRID) since the last check ended early because a
+ * grid barrier gave up waiting (its waits are bounded): PBD_ERR_TIMEOUT then,
+ * and the flag is cleared.  No reference counterpart. */
+int pbd_solver_check(pbd_solver *s);
 /* threads per block of the per-color launches (256 until autotuned) */
 int pbd_solver_get_gs_block(pbd_solver *s, int *block);
 

@@ -521,8 +521,8 @@ __global__ void __launch_bounds__(kClusterThreads, 1) k_gs_cluster(
 struct GridBar {
     unsigned count;
     unsigned gen;
-    int abort;
-    int pad;
+    int abort;     // this launch gave up (cleared before every launch)
+    int sticky;    // some launch gave up since the host last looked
 };
 constexpr int kGridThreads = 512;
 constexpr int kGridSpinLimit = 1 << 22;
@@ -546,6 +546,7 @@ __device__ bool grid_sync(GridBar *bar, unsigned nblocks) {
                 if (*vabort || ++spins > kGridSpinLimit) {
                     ok = 0;
                     atomicExch(&bar->abort, 1);
+                    atomicExch(&bar->sticky, 1);
                     break;
                 }
                 __nanosleep(32);
@@ -944,7 +945,8 @@ static int launch_sweeps_grid(pbd_solver *s, int it0, int it1, bool obstacles_in
                               const float *expk_dev) {
     pbd_object *o = s->obj;
     PBD_CHECK(s->gbar.p, PBD_ERR_STATE, "cooperative GS form used before it was prepared");
-    PBD_CUDA(cudaMemsetAsync(s->gbar.p, 0, sizeof(int4), o->stream));
+    // count, gen and abort start at zero; the sticky flag is left alone
+    PBD_CUDA(cudaMemsetAsync(s->gbar.p, 0, 3 * sizeof(int), o->stream));
     const bool inst = obstacles_inside && s->n_inst_spheres > 0 && o->has_inst;
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(o->gr_blocks);
@@ -1869,11 +1871,27 @@ int pbd_solver_autotune(pbd_solver *s, int iterations, int reps, pbd_autotune_re
         cudaMemcpyAsync(o->p.p, save.p, sizeof(float4) * o->n, cudaMemcpyDeviceToDevice, st);
         if (rc != PBD_OK) break;
         double us = 1e3 * ms / ((double)reps * iterations);
+        if (cands[k].path == PBD_GS_GRID) {
+            // a grid barrier that gave up (bounded wait) disqualifies the form
+            int4 gb = make_int4(0, 0, 0, 0);
+            if (cudaMemcpyAsync(&gb, s->gbar.p, sizeof(int4), cudaMemcpyDeviceToHost, st) !=
+                    cudaSuccess ||
+                cudaStreamSynchronize(st) != cudaSuccess) {
+                rc = PBD_ERR_CUDA;
+                break;
+            }
+            if (gb.w) {
+                int4 z = make_int4(0, 0, 0, 0);
+                cudaMemcpyAsync(s->gbar.p, &z, sizeof(int4), cudaMemcpyHostToDevice, st);
+                cudaStreamSynchronize(st);
+                us = -1.0;  // reported as failed, never chosen
+            }
+        }
         res->path[k] = cands[k].path;
         res->block[k] = cands[k].block;
         res->us_per_sweep[k] = us;
         res->n = (int)k + 1;
-        if (best < 0 || us < best_us) {
+        if (us > 0.0 && (best < 0 || us < best_us)) {
             best = (int)k;
             best_us = us;
         }
@@ -1894,6 +1912,25 @@ int pbd_solver_autotune(pbd_solver *s, int iterations, int reps, pbd_autotune_re
     if (s->rexec) cudaGraphExecDestroy(s->rexec);
     s->rexec = nullptr;
     PBD_CUDA(cudaStreamSynchronize(st));
+    return PBD_OK;
+}
+
+int pbd_solver_check(pbd_solver *s) {
+    PBD_CHECK(s && s->obj, PBD_ERR_ARG, "null argument");
+    cudaStream_t st = s->obj->stream;
+    PBD_CUDA(cudaStreamSynchronize(st));
+    if (!s->gbar.p) return PBD_OK;
+    int4 gb = make_int4(0, 0, 0, 0);
+    PBD_CUDA(cudaMemcpyAsync(&gb, s->gbar.p, sizeof(int4), cudaMemcpyDeviceToHost, st));
+    PBD_CUDA(cudaStreamSynchronize(st));
+    if (gb.w) {
+        int4 z = make_int4(0, 0, 0, 0);
+        PBD_CUDA(cudaMemcpyAsync(s->gbar.p, &z, sizeof(int4), cudaMemcpyHostToDevice, st));
+        PBD_CUDA(cudaStreamSynchronize(st));
+    }
+    PBD_CHECK(!gb.w, PBD_ERR_TIMEOUT,
+              "a grid barrier of the cooperative GS form gave up waiting; the sweeps it ended "
+              "early left the positions unconverged");
     return PBD_OK;
 }
 

@@ -75,7 +75,7 @@ EXPORTS = [
     "pbd_warmstart_gradients", "pbd_warmstart_set_gradient", "pbd_warmstart_adam",
     "pbd_warmstart_record", "pbd_warmstart_train_step", "pbd_warmstart_features",
     "pbd_warmstart_predict", "pbd_solver_set_warmstart", "pbd_solver_project_to_residual",
-    "pbd_solver_autotune", "pbd_solver_get_gs_block", "pbd_solver_train_substep",
+    "pbd_solver_autotune", "pbd_solver_get_gs_block", "pbd_solver_check", "pbd_solver_train_substep",
 ]
 
 
@@ -545,6 +545,10 @@ class SolverPBD:
         rows = [{"path": r.path[k], "block": r.block[k], "us_per_sweep": r.us_per_sweep[k]}
                 for k in range(r.n)]
         return {"candidates": rows, "best": r.best}
+
+    def check(self):
+        """synchronise; raises if a cooperative-form sweep ended early"""
+        _check(self.L.pbd_solver_check(self.h))
 
     def gs_block(self):
         v = C.c_int()
