@@ -175,6 +175,8 @@ def run_ours(args, rank, world):
     sc, cfg, colli_on, tl = make_workload(args.workload)
     obj, solver, shs, cs = setup(sc, colli_on, tl)
     solver.set_gs_path({"auto": 0, "per-color": 1, "cluster": 2, "grid": 3}[args.gs_path])
+    if args.gs_block:
+        solver.set_gs_block(args.gs_block)
     stream = torch.cuda.ExternalStream(obj.stream())
     nd = int((sc["ctype"] == scenes.DISTANCE).sum())
     nb = int((sc["ctype"] == scenes.BENDING).sum())
@@ -456,6 +458,11 @@ def main():
     ap.add_argument("--preroll", type=int, default=120)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--gs-path", default="auto", choices=["auto", "per-color", "cluster", "grid"])
+    ap.add_argument("--gs-block", type=int, default=0,
+                    help="threads per block of the per-color launches (with --gs-path "
+                         "per-color; profiles pin the autotuned form this way: under ncu "
+                         "every launch is serialised and the autotuner's timings are not "
+                         "representative)")
     ap.add_argument("--profile-range", action="store_true",
                     help="cudaProfilerStart/Stop around the timed substeps (for ncu "
                          "--profile-from-start off)")

@@ -198,7 +198,9 @@ int pbd_solver_autotune(pbd_solver *s, int iterations, int reps, pbd_autotune_re
  * grid barrier gave up waiting (its waits are bounded): PBD_ERR_TIMEOUT then,
  * and the flag is cleared.  No reference counterpart. */
 int pbd_solver_check(pbd_solver *s);
-/* threads per block of the per-color launches (256 until autotuned) */
+/* threads per block of the per-color launches (256 until autotuned or set;
+ * a multiple of 32 in [32, 512]) */
+int pbd_solver_set_gs_block(pbd_solver *s, int block);
 int pbd_solver_get_gs_block(pbd_solver *s, int *block);
 
 /* kernel launches recorded in the cached pbd_solver_step graph (no

@@ -1934,6 +1934,18 @@ int pbd_solver_check(pbd_solver *s) {
     return PBD_OK;
 }
 
+int pbd_solver_set_gs_block(pbd_solver *s, int block) {
+    PBD_CHECK(s && s->obj, PBD_ERR_STATE, "solver has no target");
+    PBD_CHECK(block >= 32 && block <= 512 && block % 32 == 0, PBD_ERR_ARG,
+              "block must be a multiple of 32 in [32, 512], got %d", block);
+    s->obj->gs_block = block;
+    if (s->gexec) cudaGraphExecDestroy(s->gexec);
+    s->gexec = nullptr;
+    if (s->rexec) cudaGraphExecDestroy(s->rexec);
+    s->rexec = nullptr;
+    return PBD_OK;
+}
+
 int pbd_solver_get_gs_block(pbd_solver *s, int *block) {
     PBD_CHECK(s && s->obj && block, PBD_ERR_ARG, "null argument");
     *block = s->obj->gs_block;

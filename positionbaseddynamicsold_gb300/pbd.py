@@ -75,7 +75,8 @@ EXPORTS = [
     "pbd_warmstart_gradients", "pbd_warmstart_set_gradient", "pbd_warmstart_adam",
     "pbd_warmstart_record", "pbd_warmstart_train_step", "pbd_warmstart_features",
     "pbd_warmstart_predict", "pbd_solver_set_warmstart", "pbd_solver_project_to_residual",
-    "pbd_solver_autotune", "pbd_solver_get_gs_block", "pbd_solver_check", "pbd_solver_train_substep",
+    "pbd_solver_autotune", "pbd_solver_get_gs_block", "pbd_solver_check",
+    "pbd_solver_set_gs_block", "pbd_solver_train_substep",
 ]
 
 
@@ -549,6 +550,9 @@ class SolverPBD:
     def check(self):
         """synchronise; raises if a cooperative-form sweep ended early"""
         _check(self.L.pbd_solver_check(self.h))
+
+    def set_gs_block(self, block):
+        _check(self.L.pbd_solver_set_gs_block(self.h, int(block)))
 
     def gs_block(self):
         v = C.c_int()
