@@ -289,17 +289,18 @@ struct InferSmem {
     unsigned short w2[64 * 64];
     unsigned short w3[16 * 64];
     unsigned short x[kTile * 16];   // A tiles
-    unsigned short h1[kTile * 64];
-    unsigned short h2[kTile * 64];
+    unsigned short h[kTile * 64];   // H1, then (after layer 2 has read it) H2
     float b2[64], b3[16];
     unsigned long long mbar;
     uint32_t tslot;
 };
-// TMEM columns: Z1 [0,64), Z2 [64,128), Y [128,144)
-constexpr int kInferCols = 256;
-// dynamic shared memory requested per block: at most two blocks per SM, so
-// their 2 x 256 TMEM columns always fit
-constexpr int kInferSmem = 100 * 1024;
+// TMEM columns [0,64) hold Z1, then Z2, then Y: each is read out completely
+// before the next GEMM writes there
+constexpr int kInferCols = 64;
+// dynamic shared memory requested per block: at most six blocks per SM (228
+// KB of shared memory), whose 6 x 64 TMEM columns always fit in 512
+constexpr int kInferSmem = 36 * 1024;
+constexpr int kInferBlocksPerSM = 6;
 static_assert(sizeof(InferSmem) + 1024 <= kInferSmem, "inference smem");
 
 __device__ __forceinline__ void copy_u4(void *dst, const void *src, int bytes, int tid, int nthr) {
@@ -394,8 +395,8 @@ __global__ void __launch_bounds__(kTile, 1) k_mlp_infer(int n, FeatArgs fa, floa
             tmem_ld16(lane + 16 * c, z);
 #pragma unroll
             for (int k = 0; k < 16; ++k) z[k] = silu(z[k]);
-            st_row8(S.h1, tid, 16 * c, 64, z);
-            st_row8(S.h1, tid, 16 * c + 8, 64, z + 8);
+            st_row8(S.h, tid, 16 * c, 64, z);
+            st_row8(S.h, tid, 16 * c + 8, 64, z + 8);
         }
         fence_proxy_async();
         fence_before_sync();
@@ -403,7 +404,7 @@ __global__ void __launch_bounds__(kTile, 1) k_mlp_infer(int n, FeatArgs fa, floa
         // layer 2
         if (tid == 0) {
             fence_after_sync();
-            issue_gemm(tb, 64, S.h1, 64, S.w2, 64, 4, id64, false);
+            issue_gemm(tb, 0, S.h, 64, S.w2, 64, 4, id64, false);
             mma_commit(mbar);
         }
         ok = mbar_wait(mbar, phase);
@@ -413,11 +414,11 @@ __global__ void __launch_bounds__(kTile, 1) k_mlp_infer(int n, FeatArgs fa, floa
 #pragma unroll
         for (int c = 0; c < 4; ++c) {
             float z[16];
-            tmem_ld16(lane + 64 + 16 * c, z);
+            tmem_ld16(lane + 16 * c, z);
 #pragma unroll
             for (int k = 0; k < 16; ++k) z[k] = silu(z[k] + S.b2[16 * c + k]);
-            st_row8(S.h2, tid, 16 * c, 64, z);
-            st_row8(S.h2, tid, 16 * c + 8, 64, z + 8);
+            st_row8(S.h, tid, 16 * c, 64, z);
+            st_row8(S.h, tid, 16 * c + 8, 64, z + 8);
         }
         fence_proxy_async();
         fence_before_sync();
@@ -425,7 +426,7 @@ __global__ void __launch_bounds__(kTile, 1) k_mlp_infer(int n, FeatArgs fa, floa
         // layer 3
         if (tid == 0) {
             fence_after_sync();
-            issue_gemm(tb, 128, S.h2, 64, S.w3, 64, 4, id16, false);
+            issue_gemm(tb, 0, S.h, 64, S.w3, 64, 4, id16, false);
             mma_commit(mbar);
         }
         ok = mbar_wait(mbar, phase);
@@ -433,7 +434,7 @@ __global__ void __launch_bounds__(kTile, 1) k_mlp_infer(int n, FeatArgs fa, floa
         if (!__syncthreads_and(ok)) break;
         fence_after_sync();
         float y[16];
-        tmem_ld16(lane + 128, y);
+        tmem_ld16(lane, y);
         if (RAW) {
             if (valid) yout[i] = make_float4(y[0] + S.b3[0], y[1] + S.b3[1], y[2] + S.b3[2], 0.f);
         } else if (valid && P.w != 0.f && lbar > 0.f) {
@@ -888,7 +889,7 @@ int ws_eval_hinges(pbd_object *o, const float4 *pos) {
 
 static int infer_grid(long long n) {
     long long tiles = (n + kTile - 1) / kTile;
-    return (int)std::max(1LL, std::min(tiles, 2LL * kNumSMs));
+    return (int)std::max(1LL, std::min(tiles, (long long)kInferBlocksPerSM * kNumSMs));
 }
 static int train_grid(long long n) {
     long long tiles = (n + kTile - 1) / kTile;

@@ -1,0 +1,67 @@
+"""Small, self-contained GPU cases for kernel profiling (ncu captures).
+
+    python -m positionbaseddynamicsold_gb300.profile_cases mlp
+    python -m positionbaseddynamicsold_gb300.profile_cases ccd
+
+mlp: a 1024 x 1024 hanging cloth (1,048,576 points, inputs far larger than
+     L2), the trained warm start applied once to the advected positions
+     (k_eval_hinges, k_mlp_infer) and one training pass over the same points'
+     features (k_mlp_train).
+ccd: the drape256 scene after 60 substeps, one CCD pass (k_point_pairs,
+     k_dist_filter, k_narrow).
+Each case runs its kernels once after one warm-up call, so `-c` small
+captures the steady-state launch.
+"""
+from __future__ import annotations
+
+import sys
+
+import numpy as np
+
+from . import scenes
+from .pbd import (RESPONSE_MASS_WEIGHTED, CollisionSolver, PBDObject, SolverPBD,
+                  SpatialHashSystem, WarmStart)
+
+DT = 1.0 / 600
+G = np.array([0.0, -9.8, 0.0], np.float32)
+
+
+def case_mlp():
+    from . import warmstart_train as wt
+    params, scales, _ = wt.load_params()
+    sc = scenes.grid_cloth(1024, 1024, 4.0, 4.0, jitter=1e-4, seed=1, pins=[0, 1023])
+    obj = PBDObject(sc, damping=1.0, gravity=G)
+    obj.prepare()
+    s = SolverPBD(obj)
+    ws = WarmStart(params, scales)
+    for _ in range(2):           # warm-up + profiled
+        s.advect(DT)
+        ws.predict(obj)
+    x = ws.features(obj)
+    rng = np.random.default_rng(0)
+    t = rng.normal(0, 1, (len(x), 3)).astype(np.float32)
+    for _ in range(2):
+        ws.gradients(x, t)
+    obj.sync()
+    print("mlp case done: %d points" % obj.n_points)
+
+
+def case_ccd():
+    sc = scenes.drape_over_sphere(res=256, seed=0)
+    obj = PBDObject(sc, damping=1.0, gravity=G)
+    obj.prepare()
+    shs = SpatialHashSystem(obj, cell_size=sc["colli"]["cell"], log2_table=20)
+    shs.init()
+    cs = CollisionSolver(obj, shs, thickness=sc["colli"]["thickness"], iterations=1,
+                         response=RESPONSE_MASS_WEIGHTED)
+    s = SolverPBD(obj)
+    s.step(DT, substeps=60, iterations=15, colli=cs, use_graph=True)
+    s.advect(DT)
+    for _ in range(2):           # warm-up + profiled
+        cs.ccd_sh_extended()
+    obj.sync()
+    print("ccd case done: %s" % cs.stats())
+
+
+if __name__ == "__main__":
+    {"mlp": case_mlp, "ccd": case_ccd}[sys.argv[1]]()
