@@ -50,6 +50,9 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "cloth substeps/s"
+# DRAM bytes per launch of the dominant kernel (the per-color GS launch),
+# from the ncu capture in profiles/drape256_kernels.md (mean of 58 launches)
+TRAFFIC_BYTES = {"drape256": 1398705.0}
 G = np.array([0.0, -9.8, 0.0], np.float32)
 DT = 1.0 / 600.0
 ITERS = 15
@@ -309,7 +312,9 @@ def run_ours(args, rank, world):
         "gpu_launches": launches_total,
         "roofline": {"bound": "hbm", "kernel": gs_kernel, "achieved": achieved,
                      "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "peak_source": peak_kind, "traffic": args.traffic,
+                     "peak_source": peak_kind,
+                     "traffic": args.traffic if args.traffic is not None else
+                     (TRAFFIC_BYTES.get(args.workload) if gs_form == 1 else None),
                      "launches_timed": n_launch, "avg_launch_us": gs_ms * 1e3 / n_launch,
                      "bytes_per_sweep": bytes_sweep},
         "clocks": clk,
