@@ -50,8 +50,9 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "cloth substeps/s"
-# DRAM bytes per launch of the dominant kernel (the per-color GS launch),
-# from the ncu capture in profiles/drape256_kernels.md (mean of 58 launches)
+# DRAM bytes per launch of the dominant kernel (the per-color GS launch,
+# 64 threads per block), measured with ncu on this workload: dram__bytes_read
+# + dram__bytes_write, mean of 58 launches of the default drape256 substep
 TRAFFIC_BYTES = {"drape256": 1398705.0}
 G = np.array([0.0, -9.8, 0.0], np.float32)
 DT = 1.0 / 600.0
@@ -472,7 +473,8 @@ def main():
                     help="cudaProfilerStart/Stop around the timed substeps (for ncu "
                          "--profile-from-start off)")
     ap.add_argument("--traffic", type=float, default=None,
-                    help="ncu dram bytes per launch of the dominant kernel (from profiles/)")
+                    help="ncu dram bytes per launch of the dominant kernel (overrides the "
+                         "measured default)")
     ap.add_argument("--solve", default="fixed", choices=["fixed", "residual"],
                     help="fixed: gs_iterations sweeps per substep (the reference's step); "
                          "residual: sweeps until the stretch residual <= --target")
