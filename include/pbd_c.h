@@ -263,6 +263,50 @@ int pbd_ccd_vf_test_batch(const float *x12, const float *p12, const float *thick
  * the last CCD call, and the overflow flag */
 int pbd_colli_stats(pbd_colli *c, long long *candidates, long long *contacts, int *overflow);
 
+/* ---- the reference's text caches and text scene files ----------------------- */
+/* Host-side scene read from the reference's files (no GPU needed). */
+typedef struct pbd_scene pbd_scene;
+/* IO::ReadTopolFromCache + IO::ReadConstraintFromCache, i.e. what
+ * PBDObject::ContinueSimInit reads (P/PBD_Basic.cuh:326-530,
+ * P/PBD_cuda.cu:660-667).  Either path may be NULL.  Lines split at '|' with
+ * exactly three fields are read by name (Indices, P, primList, velBuffer,
+ * massBuffer, dampingRate, gravity; Indices, P, primList, prdPBuffer,
+ * restPosBuffer, restLengthBuffer, stiffnessBuffer, constraintType), values
+ * converted like stoi / stof; other lines are skipped.  Differences: a
+ * trailing '\r' is removed (files written on Windows); a field that does not
+ * convert returns PBD_ERR_ARG naming the file and line (the reference
+ * throws); a mesh primList entry must be a triangle; a topology without
+ * massBuffer gets 1 per point. */
+int pbd_scene_read_cache(const char *topol_path, const char *constr_path, pbd_scene **out);
+/* IO::ReadTopolFromTxt + IO::ReadDistConstrFromTxt (P/PBD_Basic.cuh:532-660):
+ * positions and triangles from the topology file (massBuffer 1, zero
+ * velocity), distance constraints with `stiffness` and the reference's powf
+ * rest lengths from the constraint file (dist_constr_path may be NULL).
+ * Constraints of a second data line follow those of the first (the
+ * reference restarts their primList offsets at 0 on every line). */
+int pbd_scene_read_txt(const char *topol_path, const char *dist_constr_path, float stiffness,
+                       pbd_scene **out);
+/* the scene as a pbd_object_desc (pointers into the scene, valid until
+ * pbd_scene_destroy); *predicted = the cache's prdPBuffer or NULL; whether
+ * the cache held dampingRate / gravity */
+int pbd_scene_desc(pbd_scene *s, pbd_object_desc *desc, const float **predicted,
+                   int *has_damping, int *has_gravity);
+int pbd_scene_destroy(pbd_scene *s);
+/* PBDObject::SaveMeshTopol / SaveConstraint (P/PBD_cuda.cu:907-938): the
+ * reference's line format, values with 6 significant digits as its output
+ * streams print them; predicted may be NULL (positions written); either
+ * path may be NULL.  The type field is written as the reference's Windows
+ * builds spell it; no reader uses it. */
+int pbd_scene_write_cache(const pbd_object_desc *desc, const float *predicted,
+                          const char *topol_path, const char *constr_path);
+/* PBDObject::ContinueSimInit (P/PBD_cuda.cu:660-667): an object from the two
+ * caches, predicted positions from prdPBuffer when present */
+int pbd_object_create_from_cache(const char *topol_path, const char *constr_path,
+                                 pbd_object **out);
+/* the object's current state written as the two caches (SaveMeshTopol and
+ * SaveConstraint), so the reference can continue from it */
+int pbd_object_save_cache(pbd_object *obj, const char *topol_path, const char *constr_path);
+
 /* ---- allocation-free residual --------------------------------------------- */
 /* No counterpart in the reference.  The relative residual of
  * pbd_constraints_residual computed from device buffers the caller owns,

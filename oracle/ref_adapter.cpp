@@ -328,4 +328,105 @@ void ref_vf_resolve_new(const float *x, float *p, float thickness) {
     }
 }
 
+
+// ---- text caches (P/PBD_cuda.cu:627-640, 660-667, 907-938; P/PBD_Basic.cuh:326-660)
+
+// PBDObject::SaveMeshTopol + SaveConstraint of a scene given as arrays
+// (meshTopol triangles as (3t, 3) prims; the buffer names the readers expect)
+int ref_save_caches(const char *topol, const char *constr, int n, const float *pos,
+                    const float *vel, const float *mass, int nt, const int *tri, float damping,
+                    const float *g, int np, const int *prim_list, const int *indices,
+                    const int *ctype, const float *rest, const float *stiff, const float *prdp) {
+    Quiet q;
+    PBDObject obj(damping, make_float3(g[0], g[1], g[2]), CPU);
+    fill_f3(obj.meshTopol.posBuffer, pos, n);
+    obj.meshTopol.indices.m_Data.assign(tri, tri + 3 * nt);
+    obj.meshTopol.primList.m_Data.resize(nt);
+    for (int t = 0; t < nt; ++t) obj.meshTopol.primList.m_Data[t] = make_int2(3 * t, 3);
+    obj.meshTopol.indices.SetName("Indices");
+    obj.meshTopol.posBuffer.SetName("P");
+    obj.meshTopol.primList.SetName("primList");
+    fill_f3(obj.velBuffer, vel, n);
+    obj.massBuffer.m_Data.assign(mass, mass + n);
+    fill_topol(obj.constrPBDBuffer.topol, np, prim_list, indices);
+    fill_f3(obj.constrPBDBuffer.topol.posBuffer, pos, n);
+    obj.constrPBDBuffer.topol.indices.SetName("Indices");
+    obj.constrPBDBuffer.topol.posBuffer.SetName("P");
+    obj.constrPBDBuffer.topol.primList.SetName("primList");
+    fill_f3(obj.constrPBDBuffer.prdPBuffer, prdp, n);
+    obj.constrPBDBuffer.restLengthBuffer.m_Data.assign(rest, rest + np);
+    obj.constrPBDBuffer.stiffnessBuffer.m_Data.assign(stiff, stiff + np);
+    obj.constrPBDBuffer.constraintType.m_Data.assign(ctype, ctype + np);
+    obj.SaveMeshTopol(topol);
+    obj.SaveConstraint(constr);
+    return 0;
+}
+
+namespace {
+// outs: 0 mesh pos, 1 mesh indices, 2 mesh primList, 3 vel, 4 mass,
+// 5 constr indices, 6 constr pos, 7 constr primList, 8 prdP, 9 rest length,
+// 10 stiffness, 11 constraint type, 12 damping (1), 13 gravity (3);
+// sizes: scalars written per array; returns -1 when an array exceeds cap
+int export_obj(PBDObject &o, void **outs, long long cap, long long *sizes) {
+    auto f3 = [&](BufferVector3f &b, int k) {
+        sizes[k] = 3 * (long long)b.m_Data.size();
+        if (sizes[k] > cap) return false;
+        read_f3(b, (float *)outs[k]);
+        return true;
+    };
+    auto i1 = [&](BufferInt &b, int k) {
+        sizes[k] = (long long)b.m_Data.size();
+        if (sizes[k] > cap) return false;
+        for (size_t i = 0; i < b.m_Data.size(); ++i) ((int *)outs[k])[i] = b.m_Data[i];
+        return true;
+    };
+    auto i2 = [&](BufferInt2 &b, int k) {
+        sizes[k] = 2 * (long long)b.m_Data.size();
+        if (sizes[k] > cap) return false;
+        for (size_t i = 0; i < b.m_Data.size(); ++i) {
+            ((int *)outs[k])[2 * i] = b.m_Data[i].x;
+            ((int *)outs[k])[2 * i + 1] = b.m_Data[i].y;
+        }
+        return true;
+    };
+    auto f1 = [&](BufferFloat &b, int k) {
+        sizes[k] = (long long)b.m_Data.size();
+        if (sizes[k] > cap) return false;
+        for (size_t i = 0; i < b.m_Data.size(); ++i) ((float *)outs[k])[i] = b.m_Data[i];
+        return true;
+    };
+    bool ok = f3(o.meshTopol.posBuffer, 0) && i1(o.meshTopol.indices, 1) &&
+              i2(o.meshTopol.primList, 2) && f3(o.velBuffer, 3) && f1(o.massBuffer, 4) &&
+              i1(o.constrPBDBuffer.topol.indices, 5) && f3(o.constrPBDBuffer.topol.posBuffer, 6) &&
+              i2(o.constrPBDBuffer.topol.primList, 7) && f3(o.constrPBDBuffer.prdPBuffer, 8) &&
+              f1(o.constrPBDBuffer.restLengthBuffer, 9) &&
+              f1(o.constrPBDBuffer.stiffnessBuffer, 10) && i1(o.constrPBDBuffer.constraintType, 11);
+    ((float *)outs[12])[0] = o.dampingRate;
+    ((float *)outs[13])[0] = o.gravity.x;
+    ((float *)outs[13])[1] = o.gravity.y;
+    ((float *)outs[13])[2] = o.gravity.z;
+    return ok ? 0 : -1;
+}
+}  // namespace
+
+// PBDObject::ContinueSimInit (IO::ReadTopolFromCache + ReadConstraintFromCache)
+int ref_read_caches(const char *topol, const char *constr, void **outs, long long cap,
+                    long long *sizes) {
+    Quiet q;
+    PBDObject obj(1.0f, make_float3(0.f, 0.f, 0.f), CPU);
+    obj.ContinueSimInit(topol, constr, CPU);
+    return export_obj(obj, outs, cap, sizes);
+}
+
+// PBDObject::Init(topolFile, distConstrFile) (IO::ReadTopolFromTxt +
+// ReadDistConstrFromTxt) on the CPU
+int ref_read_txt(const char *topol, const char *dist, float stiffness, void **outs,
+                 long long cap, long long *sizes) {
+    Quiet q;
+    float st[3] = {stiffness, stiffness, stiffness};
+    PBDObject obj(1.0f, make_float3(0.f, 0.f, 0.f), CPU);
+    obj.SetConstrOption(DISTANCE, st);
+    obj.Init(topol, dist);
+    return export_obj(obj, outs, cap, sizes);
+}
 }  // extern "C"

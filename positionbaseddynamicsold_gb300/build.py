@@ -26,6 +26,7 @@ SOURCES = {
     "pbd_noalloc.cu": [],
     "pbd_mlp.cu": [],
     "pbd_solve.cu": [],
+    "pbd_io.cpp": [],
 }
 HEADERS = ["pbd_common.cuh"]
 

@@ -66,6 +66,8 @@ EXPORTS = [
     "pbd_colli_collision_resolve_new", "pbd_colli_get_contacts", "pbd_colli_stats",
     "pbd_ccd_vf_test_batch",
     "pbd_residual_noalloc",
+    "pbd_scene_read_cache", "pbd_scene_read_txt", "pbd_scene_desc", "pbd_scene_destroy",
+    "pbd_scene_write_cache", "pbd_object_create_from_cache", "pbd_object_save_cache",
     "pbd_constraints_residual_stretch", "pbd_solver_step_to_residual", "pbd_solver_solve_stats",
     "pbd_solver_residual_graph_kernels", "pbd_object_get_correction",
     "pbd_object_set_correction",
@@ -125,6 +127,11 @@ def load(build_if_missing: bool = True) -> C.CDLL:
     L.pbd_solver_train_substep.argtypes = [C.c_void_p, C.c_void_p, C.c_float, C.c_void_p,
                                            C.c_double, C.c_int, C.c_int, C.c_float, C.c_int,
                                            C.c_void_p]
+    L.pbd_scene_read_txt.argtypes = [C.c_char_p, C.c_char_p, C.c_float, C.c_void_p]
+    L.pbd_scene_read_cache.argtypes = [C.c_char_p, C.c_char_p, C.c_void_p]
+    L.pbd_scene_write_cache.argtypes = [C.c_void_p, C.c_void_p, C.c_char_p, C.c_char_p]
+    L.pbd_object_create_from_cache.argtypes = [C.c_char_p, C.c_char_p, C.c_void_p]
+    L.pbd_object_save_cache.argtypes = [C.c_void_p, C.c_char_p, C.c_char_p]
     L.pbd_warmstart_adam.argtypes = [C.c_void_p, C.c_float, C.c_float, C.c_float, C.c_float]
     L.pbd_warmstart_train_step.argtypes = [C.c_void_p, C.c_void_p, C.c_float, C.c_void_p]
     _LIB = L
@@ -198,6 +205,18 @@ class PBDObject:
         for i in range(3):
             d.gravity[i] = gravity[i]
         _check(self.L.pbd_object_create(C.byref(d), C.byref(self.h)))
+
+    @classmethod
+    def from_cache(cls, topol_path, constr_path):
+        """PBDObject::ContinueSimInit: an object from the reference's two caches"""
+        L = load()
+        h = C.c_void_p()
+        _check(L.pbd_object_create_from_cache(_enc(topol_path), _enc(constr_path), C.byref(h)))
+        return cls(_handle=h)
+
+    def save_cache(self, topol_path, constr_path):
+        """the current state as the reference's two caches"""
+        _check(self.L.pbd_object_save_cache(self.h, _enc(topol_path), _enc(constr_path)))
 
     @classmethod
     def grid(cls, res_x, res_y, size_x, size_y, ct=DISTANCE, stiffness=(1.0, 0.1, -1.0),
@@ -677,6 +696,97 @@ class WarmStart:
 
     def predict(self, obj):
         _check(self.L.pbd_warmstart_predict(self.h, obj.h))
+
+
+def _enc(path):
+    return None if path is None else os.fsencode(path)
+
+
+def _scene_dict(h):
+    """copy a pbd_scene's arrays out (scene dict as scenes.py builds them)"""
+    L = load()
+    d = _Desc()
+    prd = C.c_void_p()
+    hd, hg = C.c_int(), C.c_int()
+    _check(L.pbd_scene_desc(h, C.byref(d), C.byref(prd), C.byref(hd), C.byref(hg)))
+
+    def arr(ptr, n, ct, dt):
+        if not ptr or n == 0:
+            return np.zeros(0, dt)
+        return np.ctypeslib.as_array(C.cast(ptr, C.POINTER(ct)), shape=(n,)).astype(dt).copy()
+
+    n, nt, np_ = d.n_points, d.n_tris, d.n_prims
+    pl = arr(d.prim_list, 2 * np_, C.c_int, np.int32).reshape(-1, 2)
+    n_idx = int((pl[:, 0] + pl[:, 1]).max()) if np_ else 0
+    sc = {
+        "pos": arr(d.pos, 3 * n, C.c_float, np.float32).reshape(-1, 3),
+        "vel": (arr(d.vel, 3 * n, C.c_float, np.float32).reshape(-1, 3) if d.vel
+                else np.zeros((n, 3), np.float32)),
+        "mass": arr(d.mass, n, C.c_float, np.float32),
+        "tri_idx": arr(d.tri_idx, 3 * nt, C.c_int, np.int32).reshape(-1, 3),
+        "prim_list": pl,
+        "indices": arr(d.indices, n_idx, C.c_int, np.int32),
+        "ctype": arr(d.constraint_type, np_, C.c_int, np.int32),
+        "rest_length": arr(d.rest_length, np_, C.c_float, np.float32),
+        "stiffness": arr(d.stiffness, np_, C.c_float, np.float32),
+        "predicted": (arr(prd.value, 3 * n, C.c_float, np.float32).reshape(-1, 3)
+                      if prd.value else None),
+        "damping": float(d.damping_rate) if hd.value else None,
+        "gravity": np.array(list(d.gravity), np.float32) if hg.value else None,
+    }
+    L.pbd_scene_destroy(h)
+    return sc
+
+
+def read_cache(topol_path, constr_path):
+    """the reference's topology / constraint caches (either may be None)"""
+    L = load()
+    h = C.c_void_p()
+    _check(L.pbd_scene_read_cache(_enc(topol_path), _enc(constr_path), C.byref(h)))
+    return _scene_dict(h)
+
+
+def read_txt(topol_path, dist_constr_path, stiffness):
+    """the reference's text scene files (topology; distance constraints)"""
+    L = load()
+    h = C.c_void_p()
+    _check(L.pbd_scene_read_txt(_enc(topol_path), _enc(dist_constr_path), float(stiffness),
+                                C.byref(h)))
+    return _scene_dict(h)
+
+
+def write_cache(scene, topol_path, constr_path, predicted=None, damping=1.0,
+                gravity=(0.0, 0.0, 0.0)):
+    """a scene dict written as the reference's two caches"""
+    L = load()
+    keep = []
+
+    def k(a):
+        keep.append(a)
+        return _p(a)
+
+    d = _Desc()
+    pos = _f32(scene["pos"]).reshape(-1)
+    d.n_points = len(pos) // 3
+    d.pos = k(pos)
+    d.vel = k(_f32(scene["vel"]).reshape(-1)) if scene.get("vel") is not None else None
+    d.mass = k(_f32(scene["mass"]))
+    tri = _i32(scene.get("tri_idx", np.zeros((0, 3), np.int32))).reshape(-1)
+    d.n_tris = len(tri) // 3
+    d.tri_idx = k(tri) if len(tri) else None
+    ct = _i32(scene.get("ctype", np.zeros(0, np.int32)))
+    d.n_prims = len(ct)
+    if len(ct):
+        d.prim_list = k(_i32(scene["prim_list"]).reshape(-1))
+        d.indices = k(_i32(scene["indices"]))
+        d.constraint_type = k(ct)
+        d.rest_length = k(_f32(scene["rest_length"]))
+        d.stiffness = k(_f32(scene["stiffness"]))
+    d.damping_rate = damping
+    for i in range(3):
+        d.gravity[i] = gravity[i]
+    prd = None if predicted is None else _f32(predicted).reshape(-1)
+    _check(L.pbd_scene_write_cache(C.byref(d), _p(prd), _enc(topol_path), _enc(constr_path)))
 
 
 def residual_noalloc(d_pos4, n_points, d_dist_idx, d_rest_length, n_dist, d_bend_idx,

@@ -3,7 +3,8 @@ compiled code (oracle/_ref/libpbdref.so, built from the reference sources by
 oracle/build_oracle.py).  Needs the reference checkout (default
 /root/reference, or PBD_REFERENCE_ROOT); run on the development machine:
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py        # all fixtures
+    python tests/golden/make_golden.py io     # the text-cache fixtures only
 
 Every fixture is a small .npz of seeded synthetic inputs and the reference's
 outputs for them.  tests/test_oracle_golden.py checks the oracle against them.
@@ -235,8 +236,76 @@ def vf_cases(ref, n=1500, seed=17):
                         resolve_new=rnew, coef=coef, roots=roots, nroot=nroot)
 
 
+def _ref_read(ref, fn, args, cap=1 << 16):
+    """run a reference reader; its 14 output arrays trimmed to their sizes"""
+    kinds = ["f", "i", "i", "f", "f", "i", "f", "i", "f", "f", "f", "i", "f", "f"]
+    outs = [np.zeros(cap, np.float32 if k == "f" else np.int32) for k in kinds]
+    ptrs = (C.c_void_p * 14)(*[o.ctypes.data for o in outs])
+    sizes = np.zeros(14, np.int64)
+    r = fn(*args, ptrs, C.c_longlong(cap), _ptr(sizes))
+    assert r == 0
+    names = ["mesh_pos", "mesh_indices", "mesh_prims", "vel", "mass", "c_indices", "c_pos",
+             "c_prims", "prdp", "rest", "stiff", "ctype", "damping", "gravity"]
+    res = {}
+    for k, nm in enumerate(names):
+        m = 1 if nm == "damping" else 3 if nm == "gravity" else int(sizes[k])
+        res[nm] = outs[k][:m].copy()
+    return res
+
+
+def io_files(ref):
+    """The reference's text caches (PBDObject::SaveMeshTopol / SaveConstraint
+    of a small pinned, jittered grid with bending prims, random velocities,
+    masses and predicted positions) and what its readers
+    (PBDObject::ContinueSimInit) read back; text scene files in the format
+    IO::ReadTopolFromTxt / ReadDistConstrFromTxt read, and what they read."""
+    d = os.path.join(OUT, "io")
+    os.makedirs(d, exist_ok=True)
+    rng = np.random.default_rng(21)
+    sc = scenes.grid_cloth(6, 5, 0.5, 0.4, jitter=1e-3, seed=4, pins=[0, 5])
+    n = len(sc["pos"])
+    pos = np.ascontiguousarray(sc["pos"], np.float32)
+    vel = rng.normal(0, 0.3, (n, 3)).astype(np.float32)
+    mass = rng.uniform(0.5, 2.0, n).astype(np.float32)
+    mass[[0, 5]] = 0.0
+    prdp = (pos + rng.normal(0, 1e-3, (n, 3))).astype(np.float32)
+    tri = np.ascontiguousarray(sc["tri_idx"], np.int32)
+    g = np.array([0.25, -9.8, -0.125], np.float32)
+    pl = np.ascontiguousarray(sc["prim_list"], np.int32)
+    ix = np.ascontiguousarray(sc["indices"], np.int32)
+    ct = np.ascontiguousarray(sc["ctype"], np.int32)
+    rl = np.ascontiguousarray(sc["rest_length"], np.float32)
+    st = np.ascontiguousarray(sc["stiffness"], np.float32)
+    tpath, cpath = os.path.join(d, "topol.cache"), os.path.join(d, "constr.cache")
+    L = ref.lib
+    L.ref_save_caches(tpath.encode(), cpath.encode(), n, _ptr(pos), _ptr(vel), _ptr(mass),
+                      len(tri), _ptr(tri), C.c_float(0.9), _ptr(g), len(pl), _ptr(pl), _ptr(ix),
+                      _ptr(ct), _ptr(rl), _ptr(st), _ptr(prdp))
+    got = _ref_read(ref, L.ref_read_caches, (tpath.encode(), cpath.encode()))
+    # text scene files: positions with six decimals, one line of triangles,
+    # one header line then one line of distance pairs
+    pairs = ix[: 2 * int((ct == scenes.DISTANCE).sum())]
+    with open(os.path.join(d, "topol.txt"), "w") as f:
+        f.write("P:" + ",".join("%.6f" % v for v in pos.ravel()) + "\n")
+        f.write("Tri:" + ",".join(str(v) for v in tri.ravel()) + "\n")
+    with open(os.path.join(d, "dist.txt"), "w") as f:
+        f.write("NumConstr:%d\n" % (len(pairs) // 2))
+        f.write("Dist:" + ",".join(str(v) for v in pairs) + "\n")
+    txt = _ref_read(ref, L.ref_read_txt, (os.path.join(d, "topol.txt").encode(),
+                                          os.path.join(d, "dist.txt").encode(), C.c_float(0.75)))
+    out = {"in_pos": pos, "in_vel": vel, "in_mass": mass, "in_prdp": prdp, "in_tri": tri,
+           "in_gravity": g, "in_prim_list": pl, "in_indices": ix, "in_ctype": ct,
+           "in_rest": rl, "in_stiff": st}
+    out.update({"cache_" + k: v for k, v in got.items()})
+    out.update({"txt_" + k: v for k, v in txt.items()})
+    np.savez_compressed(os.path.join(OUT, "io.npz"), **out)
+
+
 def main():
     ref = RefLib()
+    if sys.argv[1:] == ["io"]:
+        io_files(ref)
+        return
     orc = Oracle()
     coloring(ref, orc)
     substep_cpu(ref)
@@ -244,6 +313,7 @@ def main():
     neighbors(ref)
     ccd(ref)
     vf_cases(ref)
+    io_files(ref)
     for f in sorted(os.listdir(OUT)):
         if f.endswith(".npz"):
             print(f, os.path.getsize(os.path.join(OUT, f)))
