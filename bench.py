@@ -178,7 +178,7 @@ def run_ours(args, rank, world):
     torch.cuda.set_device(0 if world == 1 else int(os.environ.get("LOCAL_RANK", rank)))
     sc, cfg, colli_on, tl = make_workload(args.workload)
     obj, solver, shs, cs = setup(sc, colli_on, tl)
-    solver.set_gs_path({"auto": 0, "per-color": 1, "cluster": 2, "grid": 3}[args.gs_path])
+    solver.set_gs_path({"auto": 0, "per-color": 1, "cluster": 2}[args.gs_path])
     if args.gs_block:
         solver.set_gs_block(args.gs_block)
     stream = torch.cuda.ExternalStream(obj.stream())
@@ -233,7 +233,6 @@ def run_ours(args, rank, world):
             step()
             ev[k][1].record(stream)
     torch.cuda.synchronize()
-    solver.check()   # raises if a sweep of the cooperative form ended early
     if args.profile_range:
         torch.cuda.profiler.stop()
     t_wall = time.perf_counter() - t_wall
@@ -275,7 +274,7 @@ def run_ours(args, rank, world):
     torch.cuda.synchronize()
     gs_ms = e0.elapsed_time(e1)
     gs_form = solver.gs_path()
-    gs_kernel = {1: "k_project_color", 2: "k_gs_cluster", 3: "k_gs_grid"}[gs_form]
+    gs_kernel = {1: "k_project_color", 2: "k_gs_cluster"}[gs_form]
     # per-color form: one launch per color phase; the others one per sweep
     n_launch = reps * iters * (n_colors if gs_form == 1 else 1)
     achieved = reps * iters * bytes_sweep / (gs_ms / 1e3) / 1e9
@@ -463,7 +462,7 @@ def main():
                                                           "hanging32"])
     ap.add_argument("--preroll", type=int, default=120)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--gs-path", default="auto", choices=["auto", "per-color", "cluster", "grid"])
+    ap.add_argument("--gs-path", default="auto", choices=["auto", "per-color", "cluster"])
     ap.add_argument("--gs-block", type=int, default=0,
                     help="threads per block of the per-color launches (with --gs-path "
                          "per-color; profiles pin the autotuned form this way: under ncu "

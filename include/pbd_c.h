@@ -167,12 +167,10 @@ int pbd_solver_step(pbd_solver *s, float dt, int substeps, int iterations, pbd_c
  * color (any size); PBD_GS_CLUSTER keeps every point in the distributed
  * shared memory of one 16-block thread-block cluster (objects up to 131,072
  * points) and separates colors by cluster barriers; PBD_GS_AUTO (default)
- * takes the per-color form; PBD_GS_GRID runs every color of a sweep in one
- * cooperative launch (one block per SM, a bounded grid barrier between the
- * color phases).  All forms give identical results; pbd_solver_autotune
- * picks the fastest for an object.
+ * takes the per-color form.  Both give identical results;
+ * pbd_solver_autotune picks the fastest for an object.
  * No reference counterpart. */
-enum { PBD_GS_AUTO = 0, PBD_GS_PER_COLOR = 1, PBD_GS_CLUSTER = 2, PBD_GS_GRID = 3 };
+enum { PBD_GS_AUTO = 0, PBD_GS_PER_COLOR = 1, PBD_GS_CLUSTER = 2 };
 int pbd_solver_set_gs_path(pbd_solver *s, int path);
 /* the form the next sweep will use (PBD_GS_PER_COLOR or PBD_GS_CLUSTER) */
 int pbd_solver_get_gs_path(pbd_solver *s, int *path);
@@ -186,18 +184,11 @@ int pbd_solver_get_gs_path(pbd_solver *s, int *path);
 typedef struct pbd_autotune_result {
     int n;                  /* candidates timed                       */
     int best;               /* index of the one kept                  */
-    int path[8];            /* PBD_GS_PER_COLOR / _CLUSTER / _GRID    */
+    int path[8];            /* PBD_GS_PER_COLOR / PBD_GS_CLUSTER      */
     int block[8];           /* threads per block                      */
-    double us_per_sweep[8]; /* GPU time per sweep, microseconds; -1:
-                               the form's grid barrier gave up (never
-                               chosen)                                 */
+    double us_per_sweep[8]; /* GPU time per sweep, microseconds       */
 } pbd_autotune_result;
 int pbd_solver_autotune(pbd_solver *s, int iterations, int reps, pbd_autotune_result *result);
-/* Synchronise the solver's stream and report whether any sweep of the
- * cooperative form (PBD_GS_GRID) since the last check ended early because a
- * grid barrier gave up waiting (its waits are bounded): PBD_ERR_TIMEOUT then,
- * and the flag is cleared.  No reference counterpart. */
-int pbd_solver_check(pbd_solver *s);
 /* threads per block of the per-color launches (256 until autotuned or set;
  * a multiple of 32 in [32, 512]) */
 int pbd_solver_set_gs_block(pbd_solver *s, int block);

@@ -912,8 +912,9 @@ int pbd_shs_create_hashed(pbd_object *obj, const float *cell, int log2_table, pb
     return PBD_OK;
 }
 
+// The target object is not touched: it may already be gone (a caller's
+// finaliser order is not guaranteed); freeing device memory synchronises.
 int pbd_shs_destroy(pbd_shs *h) {
-    if (h && h->obj && h->obj->stream) cudaStreamSynchronize(h->obj->stream);
     delete h;
     return PBD_OK;
 }
@@ -1026,8 +1027,8 @@ int pbd_colli_create(pbd_colli **out) {
     return PBD_OK;
 }
 
+// The target object is not touched (see pbd_shs_destroy).
 int pbd_colli_destroy(pbd_colli *c) {
-    if (c && c->obj && c->obj->stream) cudaStreamSynchronize(c->obj->stream);
     delete c;
     return PBD_OK;
 }

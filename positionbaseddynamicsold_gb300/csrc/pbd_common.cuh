@@ -181,10 +181,6 @@ struct pbd_object {
     bool pdl = true;
     // threads per block of the per-color launches (set by the autotuner)
     int gs_block = 256;
-    // cooperative form: device copies of the record segments, grid size
-    int gr_state = 0;           // 0 not planned, 1 usable, -1 not applicable
-    int gr_blocks = 0;
-    pbd::DBuf<int> gdseg, gbseg, gaseg;
 };
 
 struct pbd_shs {
@@ -261,7 +257,6 @@ struct pbd_solver {
     pbd_object *obj = nullptr;
     pbd_warmstart *ws = nullptr;
     int min_sweeps = 0;   // sweeps that always follow an accepted prediction
-    pbd::DBuf<int4> gbar; // grid barrier state of the cooperative GS form
     pbd::DBuf<pbd::LoopState> loop;
     // cached graph of pbd_solver_step_to_residual
     cudaGraphExec_t rexec = nullptr;

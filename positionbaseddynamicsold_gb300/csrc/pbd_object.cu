@@ -510,118 +510,6 @@ __global__ void __launch_bounds__(kClusterThreads, 1) k_gs_cluster(
     for (int i = tid; i < chunk && base + i < n; i += blockDim.x) p[base + i] = sp[i];
 }
 
-// Colored GS in one cooperative launch: one 512-thread block per SM stays
-// resident for the whole sweep, each color's records are spread over the
-// whole grid, and a grid barrier separates the color phases instead of a
-// kernel boundary.  Same records, same per-constraint arithmetic and (within
-// a color no two records share a point) the same result as the per-color
-// launches.  The barrier's waits are bounded: a block that gives up raises
-// the abort flag, every other block then leaves its wait and the kernel ends
-// (the flag stays set for the host).
-struct GridBar {
-    unsigned count;
-    unsigned gen;
-    int abort;     // this launch gave up (cleared before every launch)
-    int sticky;    // some launch gave up since the host last looked
-};
-constexpr int kGridThreads = 512;
-constexpr int kGridSpinLimit = 1 << 22;
-
-__device__ bool grid_sync(GridBar *bar, unsigned nblocks) {
-    __shared__ int ok_s;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        int ok = 1;
-        volatile unsigned *vgen = &bar->gen;
-        volatile int *vabort = &bar->abort;
-        const unsigned g = *vgen;
-        __threadfence();
-        if (atomicAdd(&bar->count, 1u) == nblocks - 1) {
-            atomicExch(&bar->count, 0u);
-            __threadfence();
-            atomicAdd(&bar->gen, 1u);
-        } else {
-            int spins = 0;
-            while (*vgen == g) {
-                if (*vabort || ++spins > kGridSpinLimit) {
-                    ok = 0;
-                    atomicExch(&bar->abort, 1);
-                    atomicExch(&bar->sticky, 1);
-                    break;
-                }
-                __nanosleep(32);
-            }
-        }
-        __threadfence();
-        ok_s = ok;
-    }
-    __syncthreads();
-    return ok_s != 0;
-}
-
-__global__ void __launch_bounds__(kGridThreads, 1) k_gs_grid(
-    const int4 *__restrict__ drec, const int *__restrict__ dseg, const int4 *__restrict__ bidx,
-    const float2 *__restrict__ bpar, const int *__restrict__ bseg,
-    const float4 *__restrict__ arec, const int *__restrict__ aseg, int n_colors, int n,
-    float4 *__restrict__ p, int it0, int it1, const float *__restrict__ expk_dev,
-    int sphere_on, float3 sc, float sr, int ground_on, float gh,
-    const int *__restrict__ point_inst, const float4 *__restrict__ inst_spheres, int n_inst,
-    GridBar *bar) {
-    const unsigned nb = gridDim.x;
-    const int gt = blockIdx.x * blockDim.x + threadIdx.x;
-    const int gs = gridDim.x * blockDim.x;
-    GlobalPos P{p};
-    // the first record of each kind this thread takes in the coming phase,
-    // loaded before the barrier that precedes the phase
-    int4 dr = make_int4(0, 0, 0, 0), br = make_int4(0, 0, 0, 0);
-    float2 bp = make_float2(0.f, 0.f);
-    float4 ar = make_float4(0.f, 0.f, 0.f, 0.f);
-    bool hd = false, hb = false, ha = false;
-    auto fetch = [&](int c) {
-        int kd = dseg[c] + gt, kb = bseg[c] + gt, ka = aseg[c] + gt;
-        hd = kd < dseg[c + 1];
-        hb = kb < bseg[c + 1];
-        ha = ka < aseg[c + 1];
-        if (hd) dr = drec[kd];
-        if (hb) {
-            br = bidx[kb];
-            bp = bpar[kb];
-        }
-        if (ha) ar = arec[ka];
-    };
-    const bool obst = sphere_on || ground_on || n_inst > 0;
-    fetch(0);
-    for (int it = it0; it < it1; ++it) {
-        const float expk = expk_dev ? *expk_dev : (float)(1.0 / (double)(it + 1));
-        for (int c = 0; c < n_colors; ++c) {
-            if (hd) project_distance(dr, P, expk);
-            for (int k = dseg[c] + gt + gs; k < dseg[c + 1]; k += gs)
-                project_distance(drec[k], P, expk);
-            if (hb) project_bending(br, bp, P, expk);
-            for (int k = bseg[c] + gt + gs; k < bseg[c + 1]; k += gs)
-                project_bending(bidx[k], bpar[k], P, expk);
-            if (ha) project_anchor(ar, P);
-            for (int k = aseg[c] + gt + gs; k < aseg[c + 1]; k += gs) project_anchor(arec[k], P);
-            fetch(c + 1 < n_colors ? c + 1 : 0);
-            if (!grid_sync(bar, nb)) return;
-        }
-        if (obst) {
-            for (int i = gt; i < n; i += gs) {
-                float4 q = obstacle_point(p[i], sphere_on, sc, sr, ground_on, gh);
-                if (n_inst > 0) {
-                    int k = point_inst[i];
-                    if (k >= 0 && k < n_inst) {
-                        float4 sp = inst_spheres[k];
-                        q = obstacle_point(q, 1, make_float3(sp.x, sp.y, sp.z), sp.w, 0, 0.f);
-                    }
-                }
-                p[i] = q;
-            }
-            if (!grid_sync(bar, nb)) return;
-        }
-    }
-}
-
 // ColliWithShpGrd (P/PBD_cuda.cu:1519-1573): sphere push-out and ground plane
 __global__ void k_obstacles(int n, float4 *p, int sphere_on, float3 c, float r, int ground_on,
                             float gh) {
@@ -772,13 +660,7 @@ static int launch_sweep_per_color(pbd_object *o, int iter, const float *expk_dev
     return PBD_OK;
 }
 
-static int resolved_path(pbd_solver *s);
-static int launch_sweeps_grid(pbd_solver *s, int it0, int it1, bool obstacles_inside,
-                              const float *expk_dev);
-
 int launch_sweep_dev(pbd_solver *s, const float *expk_dev, bool obstacles_inside) {
-    if (s->gs_path == PBD_GS_GRID && resolved_path(s) == PBD_GS_GRID)
-        return launch_sweeps_grid(s, 0, 1, obstacles_inside, expk_dev);
     PBD_TRY(launch_sweep_per_color(s->obj, 0, expk_dev));
     if (obstacles_inside) PBD_TRY(launch_obstacles(s));
     return PBD_OK;
@@ -891,82 +773,22 @@ static int cluster_plan(pbd_object *o) {
     return PBD_OK;
 }
 
-// Device copies of the per-color record segments and the co-resident grid
-// size for the cooperative form (once per coloring).
-static int grid_plan(pbd_object *o) {
-    if (o->gr_state != 0) return PBD_OK;
-    o->gr_state = -1;
-    if (o->np == 0 || o->n_colors == 0) return PBD_OK;
-    int dev = 0, sms = 0, per_sm = 0;
-    PBD_CUDA(cudaGetDevice(&dev));
-    PBD_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-    PBD_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_gs_grid, kGridThreads, 0));
-    if (per_sm < 1 || sms < 1) return PBD_OK;
-    cudaStream_t st = o->stream;
-    PBD_TRY(o->gdseg.upload(o->h_dseg.data(), o->h_dseg.size(), st));
-    PBD_TRY(o->gbseg.upload(o->h_bseg.data(), o->h_bseg.size(), st));
-    PBD_TRY(o->gaseg.upload(o->h_aseg.data(), o->h_aseg.size(), st));
-    PBD_CUDA(cudaStreamSynchronize(st));
-    o->gr_blocks = sms;  // one block per SM
-    o->gr_state = 1;
-    return PBD_OK;
-}
-
 // PBD_GS_AUTO takes the per-color launches: measured on GB300 they are the
 // faster form (a 256x256 cloth: 3.4 us per color phase inside a graph
-// against 8.5 us per phase for the cluster form); the autotuner picks among
-// all forms per object.
+// against 8.5 us per phase for the cluster form); the autotuner picks the
+// block size (and the cluster form where it applies) per object.
 static int resolved_path(pbd_solver *s) {
-    if (s->gs_path == PBD_GS_GRID) {
-        if (grid_plan(s->obj) != PBD_OK) return -1;
-        return s->obj->gr_state == 1 ? PBD_GS_GRID : -2;
-    }
     if (s->gs_path != PBD_GS_CLUSTER) return PBD_GS_PER_COLOR;
     if (s->n_inst_spheres > 0) return -2;  // per-instance spheres: per-color form only
     if (cluster_plan(s->obj) != PBD_OK) return -1;
     return s->obj->cl_state == 1 ? PBD_GS_CLUSTER : -2;
 }
 
-// Everything a launch form needs before a stream capture (plans, uploads,
-// barrier state); capture forbids allocation and synchronisation.
+// Everything a launch form needs before a stream capture (plans and
+// uploads); capture forbids allocation and synchronisation.
 int prepare_gs_path(pbd_solver *s) {
     pbd_object *o = s->obj;
     if (s->gs_path == PBD_GS_CLUSTER) PBD_TRY(cluster_plan(o));
-    if (s->gs_path == PBD_GS_GRID) {
-        PBD_TRY(grid_plan(o));
-        if (!s->gbar.p) PBD_TRY(s->gbar.alloc(1));
-    }
-    return PBD_OK;
-}
-
-// sweeps it0..it1-1 of the cooperative form; expk_dev (device) overrides the
-// exponent 1/(it+1) of a single sweep
-static int launch_sweeps_grid(pbd_solver *s, int it0, int it1, bool obstacles_inside,
-                              const float *expk_dev) {
-    pbd_object *o = s->obj;
-    PBD_CHECK(s->gbar.p, PBD_ERR_STATE, "cooperative GS form used before it was prepared");
-    // count, gen and abort start at zero; the sticky flag is left alone
-    PBD_CUDA(cudaMemsetAsync(s->gbar.p, 0, 3 * sizeof(int), o->stream));
-    const bool inst = obstacles_inside && s->n_inst_spheres > 0 && o->has_inst;
-    cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3(o->gr_blocks);
-    cfg.blockDim = dim3(kGridThreads);
-    cfg.stream = o->stream;
-    cudaLaunchAttribute at[1];
-    at[0].id = cudaLaunchAttributeCooperative;
-    at[0].val.cooperative = 1;
-    cfg.attrs = at;
-    cfg.numAttrs = 1;
-    PBD_CUDA(cudaLaunchKernelEx(
-        &cfg, k_gs_grid, (const int4 *)o->drec.p, (const int *)o->gdseg.p,
-        (const int4 *)o->bidx.p, (const float2 *)o->bpar.p, (const int *)o->gbseg.p,
-        (const float4 *)o->arec.p, (const int *)o->gaseg.p, o->n_colors, o->n, o->p.p, it0, it1,
-        expk_dev, obstacles_inside ? s->sphere_on : 0,
-        make_float3(s->sphere_c[0], s->sphere_c[1], s->sphere_c[2]), s->sphere_r,
-        obstacles_inside ? s->ground_on : 0, s->ground_h,
-        inst ? (const int *)o->point_inst.p : nullptr,
-        inst ? (const float4 *)s->inst_spheres.p : nullptr, inst ? s->n_inst_spheres : 0,
-        reinterpret_cast<GridBar *>(s->gbar.p)));
     return PBD_OK;
 }
 
@@ -983,7 +805,6 @@ int launch_sweeps(pbd_solver *s, int it0, int it1, bool obstacles_inside) {
     PBD_CHECK(path != -1, PBD_ERR_CUDA, "cluster plan failed: %s", pbd_last_error());
     PBD_CHECK(path != -2, PBD_ERR_STATE,
               "the requested Gauss-Seidel form does not apply to this object (%d points)", o->n);
-    if (path == PBD_GS_GRID) return launch_sweeps_grid(s, it0, it1, obstacles_inside, nullptr);
     if (path == PBD_GS_CLUSTER) {
         int ob = obstacles_inside && (s->sphere_on || s->ground_on);
         cudaLaunchConfig_t cfg = {};
@@ -1556,7 +1377,6 @@ int pbd_constraints_sort_edges_colors(pbd_object *o) {
         PBD_CUDA(cudaMemcpyAsync(o->bend_prim.p, sv + nrec[0], sizeof(int) * nrec[1],
                                  cudaMemcpyDeviceToDevice, s));
     o->feat_built = false;
-    o->gr_state = 0;
     k_build_records<<<grid_for(np, 256), 256, 0, s>>>(
         nrec[0] + nrec[1] + nrec[2], sv, o->prim_list.p, o->indices.p, o->rest_length.p,
         o->stiffness.p, o->rest_angle.p, o->rest_pos.p, nrec[0], nrec[1], nrec[2], o->drec.p,
@@ -1781,7 +1601,7 @@ int pbd_solver_step(pbd_solver *s, float dt, int substeps, int iterations, pbd_c
 }
 
 int pbd_solver_set_gs_path(pbd_solver *s, int path) {
-    PBD_CHECK(s && path >= PBD_GS_AUTO && path <= PBD_GS_GRID, PBD_ERR_ARG, "bad path");
+    PBD_CHECK(s && path >= PBD_GS_AUTO && path <= PBD_GS_CLUSTER, PBD_ERR_ARG, "bad path");
     s->gs_path = path;
     return PBD_OK;
 }
@@ -1825,11 +1645,6 @@ int pbd_solver_autotune(pbd_solver *s, int iterations, int reps, pbd_autotune_re
         PBD_TRY(cluster_plan(o));
         if (o->cl_state == 1) cands.push_back({PBD_GS_CLUSTER, kClusterThreads});
     }
-    PBD_TRY(grid_plan(o));
-    if (o->gr_state == 1) {
-        cands.push_back({PBD_GS_GRID, kGridThreads});
-        if (!s->gbar.p) PBD_TRY(s->gbar.alloc(1));
-    }
     const int keep_path = s->gs_path, keep_block = o->gs_block;
     cudaEvent_t e0, e1;
     PBD_CUDA(cudaEventCreate(&e0));
@@ -1871,27 +1686,11 @@ int pbd_solver_autotune(pbd_solver *s, int iterations, int reps, pbd_autotune_re
         cudaMemcpyAsync(o->p.p, save.p, sizeof(float4) * o->n, cudaMemcpyDeviceToDevice, st);
         if (rc != PBD_OK) break;
         double us = 1e3 * ms / ((double)reps * iterations);
-        if (cands[k].path == PBD_GS_GRID) {
-            // a grid barrier that gave up (bounded wait) disqualifies the form
-            int4 gb = make_int4(0, 0, 0, 0);
-            if (cudaMemcpyAsync(&gb, s->gbar.p, sizeof(int4), cudaMemcpyDeviceToHost, st) !=
-                    cudaSuccess ||
-                cudaStreamSynchronize(st) != cudaSuccess) {
-                rc = PBD_ERR_CUDA;
-                break;
-            }
-            if (gb.w) {
-                int4 z = make_int4(0, 0, 0, 0);
-                cudaMemcpyAsync(s->gbar.p, &z, sizeof(int4), cudaMemcpyHostToDevice, st);
-                cudaStreamSynchronize(st);
-                us = -1.0;  // reported as failed, never chosen
-            }
-        }
         res->path[k] = cands[k].path;
         res->block[k] = cands[k].block;
         res->us_per_sweep[k] = us;
         res->n = (int)k + 1;
-        if (us > 0.0 && (best < 0 || us < best_us)) {
+        if (best < 0 || us < best_us) {
             best = (int)k;
             best_us = us;
         }
@@ -1912,25 +1711,6 @@ int pbd_solver_autotune(pbd_solver *s, int iterations, int reps, pbd_autotune_re
     if (s->rexec) cudaGraphExecDestroy(s->rexec);
     s->rexec = nullptr;
     PBD_CUDA(cudaStreamSynchronize(st));
-    return PBD_OK;
-}
-
-int pbd_solver_check(pbd_solver *s) {
-    PBD_CHECK(s && s->obj, PBD_ERR_ARG, "null argument");
-    cudaStream_t st = s->obj->stream;
-    PBD_CUDA(cudaStreamSynchronize(st));
-    if (!s->gbar.p) return PBD_OK;
-    int4 gb = make_int4(0, 0, 0, 0);
-    PBD_CUDA(cudaMemcpyAsync(&gb, s->gbar.p, sizeof(int4), cudaMemcpyDeviceToHost, st));
-    PBD_CUDA(cudaStreamSynchronize(st));
-    if (gb.w) {
-        int4 z = make_int4(0, 0, 0, 0);
-        PBD_CUDA(cudaMemcpyAsync(s->gbar.p, &z, sizeof(int4), cudaMemcpyHostToDevice, st));
-        PBD_CUDA(cudaStreamSynchronize(st));
-    }
-    PBD_CHECK(!gb.w, PBD_ERR_TIMEOUT,
-              "a grid barrier of the cooperative GS form gave up waiting; the sweeps it ended "
-              "early left the positions unconverged");
     return PBD_OK;
 }
 

@@ -20,7 +20,7 @@ from . import build as _build
 DISTANCE, BENDING, ANCHOR = 0x001, 0x010, 0x100
 JACOBI, GAUSSSEIDEL = 0, 1
 RESPONSE_REFERENCE, RESPONSE_MASS_WEIGHTED = 0, 1
-GS_AUTO, GS_PER_COLOR, GS_CLUSTER, GS_GRID = 0, 1, 2, 3
+GS_AUTO, GS_PER_COLOR, GS_CLUSTER = 0, 1, 2
 _ERRS = {1: "ARG", 2: "OOM", 3: "CUDA", 4: "TIMEOUT", 5: "OVERFLOW", 6: "STATE"}
 
 
@@ -77,7 +77,7 @@ EXPORTS = [
     "pbd_warmstart_gradients", "pbd_warmstart_set_gradient", "pbd_warmstart_adam",
     "pbd_warmstart_record", "pbd_warmstart_train_step", "pbd_warmstart_features",
     "pbd_warmstart_predict", "pbd_solver_set_warmstart", "pbd_solver_project_to_residual",
-    "pbd_solver_autotune", "pbd_solver_get_gs_block", "pbd_solver_check",
+    "pbd_solver_autotune", "pbd_solver_get_gs_block",
     "pbd_solver_set_gs_block", "pbd_solver_train_substep",
 ]
 
@@ -565,10 +565,6 @@ class SolverPBD:
         rows = [{"path": r.path[k], "block": r.block[k], "us_per_sweep": r.us_per_sweep[k]}
                 for k in range(r.n)]
         return {"candidates": rows, "best": r.best}
-
-    def check(self):
-        """synchronise; raises if a cooperative-form sweep ended early"""
-        _check(self.L.pbd_solver_check(self.h))
 
     def set_gs_block(self, block):
         _check(self.L.pbd_solver_set_gs_block(self.h, int(block)))

@@ -178,37 +178,3 @@ def test_cluster_path_equals_per_color(orc, res):
     obj = PBDObject(sc, damping=0.9, gravity=G)
     obj.prepare()
     assert SolverPBD(obj).gs_path() == GS_PER_COLOR
-
-
-@pytest.mark.parametrize("res", [32, 300])
-def test_grid_path_equals_per_color(res):
-    """The cooperative form (every color of a sweep in one launch, grid
-    barriers between the phases) gives the per-color launches' result bit for
-    bit: eager, from a graph, with the analytic obstacles, with collisions and
-    in the solve-to-residual loop."""
-    from positionbaseddynamicsold_gb300.pbd import (GS_GRID, GS_PER_COLOR, RESPONSE_MASS_WEIGHTED,
-                                                    CollisionSolver, SpatialHashSystem)
-    sc = scenes.grid_cloth(res, res, 1.0, 1.0, origin=(-0.5, 0.9, -0.5), jitter=1e-3, seed=6,
-                           pins=[0, res - 1])
-    out = []
-    for path in (GS_PER_COLOR, GS_GRID):
-        obj = PBDObject(sc, damping=0.9, gravity=G)
-        obj.prepare()
-        s = SolverPBD(obj)
-        s.set_gs_path(path)
-        assert s.gs_path() == path
-        s.set_sphere(True, (0.0, 0.0, 0.0), 1.0)
-        for _ in range(2):
-            s.advect(1.0 / 600)
-            s.project_constraint(20)
-            s.integration(1.0 / 600)
-        s.step(1.0 / 600, substeps=2, iterations=20, use_graph=True)
-        shs = SpatialHashSystem(obj, cell_size=2.0 / res, log2_table=16)
-        shs.init()
-        cs = CollisionSolver(obj, shs, thickness=1e-3, iterations=1,
-                             response=RESPONSE_MASS_WEIGHTED)
-        s.step(1.0 / 600, substeps=2, iterations=15, colli=cs, use_graph=True)
-        s.step_to_residual(1.0 / 600, 2, target=1e-5, max_sweeps=20, chunk=5, colli=cs)
-        s.check()   # no grid barrier gave up
-        out.append(obj.positions())
-    np.testing.assert_array_equal(out[0], out[1])
