@@ -545,11 +545,30 @@ __global__ void __launch_bounds__(32 * kTaskWarps) k_point_pairs(
     }
 }
 
-// stage 3: one thread per AABB-overlapping pair: the point is not a vertex
-// of the triangle and a lower bound of the point-triangle distance over the
-// step is at most 4.5 h
+// distance from the origin to the segment [a, b]
+__device__ __forceinline__ float seg_origin_dist(v3 a, v3 b) {
+    v3 d = sub3(b, a);
+    float dd = dot3(d, d);
+    float t = dd > 0.f ? fminf(fmaxf(-dot3(a, d) / dd, 0.f), 1.f) : 0.f;
+    v3 q = add3(a, mul3(d, t));
+    return sqrtf(dot3(q, q));
+}
+
+// stage 3: one thread per AABB-overlapping pair.  The pair goes on to the
+// narrow phase unless the point is a vertex of the triangle or no time of
+// the step can pass ExtendedVFTest's two conditions: plane distance < 2h and
+// every barycentric coordinate >= -eps, eps = h / mean edge length, at one
+// time t.  Those put the point within sqrt((2h)^2 + r^2) of the triangle,
+// r = 2h * (longest edge / mean edge) at t (the farthest point of the
+// eps-grown triangle from the triangle is a grown corner, eps |2 v_i - v_j -
+// v_k| from v_i); that ratio is at most 1.5 at any t, and over the step at
+// most the largest end length of an edge (edge vectors move linearly) over
+// the mean of the edges' smallest lengths (the distance of the segment
+// between an edge's end vectors from 0).  The point-triangle distance is at
+// least (d0 + d1 - U) / 2 over the step (d0, d1 at the ends, U the largest
+// motion of a triangle corner relative to the point).
 __global__ void __launch_bounds__(256) k_dist_filter(const int2 *__restrict__ pairs,
-                                                     long long pcap, float reach,
+                                                     long long pcap, float th,
                                                      const int4 *__restrict__ tri,
                                                      const float4 *__restrict__ x,
                                                      const float4 *__restrict__ p, int2 *cand,
@@ -571,6 +590,17 @@ __global__ void __launch_bounds__(256) k_dist_filter(const int2 *__restrict__ pa
             v3 ua = sub3(sub3(pa, xa), D0), ub = sub3(sub3(pb, xb), D0),
                uc = sub3(sub3(pc, xc), D0);
             float U = sqrtf(fmaxf(fmaxf(dot3(ua, ua), dot3(ub, ub)), dot3(uc, uc)));
+            v3 e0[3] = {sub3(xb, xa), sub3(xc, xb), sub3(xa, xc)};
+            v3 e1[3] = {sub3(pb, pa), sub3(pc, pb), sub3(pa, pc)};
+            float lmax = 0.f, lsum = 0.f;
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                lmax = fmaxf(lmax, fmaxf(sqrtf(dot3(e0[k], e0[k])), sqrtf(dot3(e1[k], e1[k]))));
+                lsum += seg_origin_dist(e0[k], e1[k]);
+            }
+            float ratio = lsum > 0.f ? fminf(1.5f, lmax / (lsum / 3.f)) : 1.5f;
+            float r = 2.f * th * ratio;
+            float reach = sqrtf(4.f * th * th + r * r) * 1.001f + 2e-6f;
             if ((d0 + d1 - U) * 0.5f > reach) continue;
         }
         long long slot = agg_inc(counters);
@@ -805,17 +835,17 @@ int ccd_detect(pbd_colli *c) {
     GridParams g = params_of(h);
     float th = c->thickness;
     // per-axis reach of a hit: 2h off the plane + 3h inside the triangle grown
-    // by the barycentric epsilon h / mean edge; Euclidean reach 3.61h; both
-    // with slack
+    // by the barycentric epsilon h / mean edge, with slack (the distance
+    // filter then applies each pair's own Euclidean reach, at most 3.61h)
     float margin = 5.5f * th + 2e-6f;
-    float reach = 4.5f * th + 2e-6f;
+
     k_point_pairs<<<grid_for((long long)o->n * 32, 32 * kTaskWarps), 32 * kTaskWarps, 0, s>>>(
         o->n, g, margin, o->pt_tri_first.p, o->pt_tri_last.p, o->pt_tri.p,
         o->has_inst ? o->point_inst.p : nullptr, o->has_inst ? o->tri_inst.p : nullptr, o->x.p,
         o->p.p, h->tcell.p, h->brange.p, h->blo.p, h->bhi.p, h->scell.p, h->slo.p, h->shi.p,
         c->pairs.p, c->task_cap, c->counters.p);
     PBD_LAUNCH();
-    k_dist_filter<<<kPersistentBlocks, 256, 0, s>>>(c->pairs.p, c->task_cap, reach, o->tri.p,
+    k_dist_filter<<<kPersistentBlocks, 256, 0, s>>>(c->pairs.p, c->task_cap, th, o->tri.p,
                                                     o->x.p, o->p.p, c->cand.p, c->cand_cap,
                                                     c->counters.p);
     PBD_LAUNCH();
