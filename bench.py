@@ -256,27 +256,32 @@ def run_ours(args, rank, world):
     else:
         launches_total = solver.graph_kernels() * args.steps
 
-    # roofline of the dominant kernel (the per-color GS launch): one eager
-    # 15-iteration projection on the same state, timed with events on the
-    # object's stream; algorithmic bytes per sweep = 84*nd + 164*nb
+    # roofline of the dominant kernel (the GS sweep): eager projections on
+    # the same state, timed with events on the object's stream, launched as
+    # the timed substeps launch them (per-color: one launch per color phase;
+    # cluster: one launch for all sweeps); algorithmic bytes per sweep =
+    # 84*nd + 164*nb
     pos_save = obj.positions()
     prd_save = obj.predicted()
     bytes_sweep = 84.0 * nd + 164.0 * nb
+    gs_form = solver.gs_path()
+    gs_kernel = {1: "k_project_color", 2: "k_gs_cluster"}[gs_form]
+
+    def sweeps():
+        solver.project_constraint(iters)
+
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    solver.project_constraint(iters)
+    sweeps()
     obj.sync()
     reps = 3
     with torch.cuda.stream(stream):
         e0.record(stream)
         for _ in range(reps):
-            solver.project_constraint(iters)
+            sweeps()
         e1.record(stream)
     torch.cuda.synchronize()
     gs_ms = e0.elapsed_time(e1)
-    gs_form = solver.gs_path()
-    gs_kernel = {1: "k_project_color", 2: "k_gs_cluster"}[gs_form]
-    # per-color form: one launch per color phase; the others one per sweep
-    n_launch = reps * iters * (n_colors if gs_form == 1 else 1)
+    n_launch = reps * (iters * n_colors if gs_form == 1 else 1)
     achieved = reps * iters * bytes_sweep / (gs_ms / 1e3) / 1e9
     obj.set_positions(pos_save)
     obj.set_predicted(prd_save)

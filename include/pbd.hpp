@@ -173,6 +173,7 @@ public:
         check(pbd_solver_autotune(h_, iterations, reps, &r));
         return r;
     }
+    void SetGSPath(int path) { check(pbd_solver_set_gs_path(h_, path)); }
     pbd_solver *handle() const { return h_; }
 
 private:

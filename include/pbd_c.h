@@ -91,7 +91,10 @@ int pbd_object_create_grid(float damping, const float *gravity, int res_x, int r
 int pbd_object_destroy(pbd_object *obj);
 int pbd_object_sizes(const pbd_object *obj, int *n_points, int *n_tris, int *n_prims);
 /* meshTopol.posBuffer / velBuffer / constrPBDBuffer.prdPBuffer copy-out and
- * copy-in (Buffer::LoadToHost / LoadToDevice, P/Buffer.cuh:123-165) */
+ * copy-in (Buffer::LoadToHost / LoadToDevice, P/Buffer.cuh:123-165), 3 floats
+ * per point, through page-locked staging.  get_* blocks until the values are
+ * in the caller's array; set_* returns once the caller's array has been read,
+ * and the copy is ordered before later work on the object's stream. */
 int pbd_object_get_positions(pbd_object *obj, float *pos3);
 int pbd_object_get_velocities(pbd_object *obj, float *vel3);
 int pbd_object_get_predicted(pbd_object *obj, float *prdp3);
@@ -169,18 +172,19 @@ int pbd_solver_step(pbd_solver *s, float dt, int substeps, int iterations, pbd_c
  * points) and separates colors by cluster barriers; PBD_GS_AUTO (default)
  * takes the per-color form.  Both give identical results;
  * pbd_solver_autotune picks the fastest for an object.
- * No reference counterpart. */
+ * No reference counterpart (the reference launches one kernel per color). */
 enum { PBD_GS_AUTO = 0, PBD_GS_PER_COLOR = 1, PBD_GS_CLUSTER = 2 };
 int pbd_solver_set_gs_path(pbd_solver *s, int path);
 /* the form the next sweep will use (PBD_GS_PER_COLOR or PBD_GS_CLUSTER) */
 int pbd_solver_get_gs_path(pbd_solver *s, int *path);
 
-/* Autotuner (no reference counterpart): times `iterations` sweeps replayed
- * `reps` times from a CUDA graph for each launch form that applies -- the
- * per-color launches with 64, 128, 256 and 512 threads per block, and the
- * cluster form (all colors in one launch) when the object fits one cluster --
- * and keeps the fastest for this solver and object.  The predicted positions
- * are restored; all forms give identical results. */
+/* Autotuner (no reference counterpart): times `iterations` sweeps (one
+ * launch sequence per sweep) replayed `reps` times from a CUDA graph for each
+ * launch form that applies -- the per-color launches with 64, 128, 256 and
+ * 512 threads per block, and the cluster form when the object fits one
+ * cluster -- and keeps the
+ * fastest for this solver and object.  The predicted positions are restored;
+ * all forms give identical results. */
 typedef struct pbd_autotune_result {
     int n;                  /* candidates timed                       */
     int best;               /* index of the one kept                  */

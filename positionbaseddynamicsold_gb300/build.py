@@ -28,7 +28,7 @@ SOURCES = {
     "pbd_solve.cu": [],
     "pbd_io.cpp": [],
 }
-HEADERS = ["pbd_common.cuh"]
+HEADERS = ["pbd_common.cuh", "pbd_project.cuh"]
 
 
 def _nvcc():

@@ -86,6 +86,36 @@ struct DBuf {
     }
 };
 
+// Owning page-locked host allocation (staging of host transfers); sizes in
+// elements.
+template <class T>
+struct HBuf {
+    T *p = nullptr;
+    size_t n = 0;
+    HBuf() = default;
+    HBuf(const HBuf &) = delete;
+    HBuf &operator=(const HBuf &) = delete;
+    ~HBuf() { release(); }
+    void release() {
+        if (p) cudaFreeHost(p);
+        p = nullptr;
+        n = 0;
+    }
+    int alloc(size_t count) {
+        if (count <= n && p) return PBD_OK;
+        release();
+        size_t bytes = (count ? count : 1) * sizeof(T);
+        cudaError_t e = cudaHostAlloc((void **)&p, bytes, cudaHostAllocDefault);
+        if (e != cudaSuccess) {
+            p = nullptr;
+            set_error("cudaHostAlloc(%zu bytes) failed: %s", bytes, cudaGetErrorString(e));
+            return e == cudaErrorMemoryAllocation ? PBD_ERR_OOM : PBD_ERR_CUDA;
+        }
+        n = count;
+        return PBD_OK;
+    }
+};
+
 // ---- stable LSD radix sort (8-bit digits) of (key, int value) pairs --------
 // Sorts n elements (n read from d_count when non-null, capped by n_cap),
 // `bits` low key bits.  Buffers: keys/vals in and alt (same capacity), hist
@@ -115,6 +145,12 @@ struct pbd_object {
     pbd::DBuf<float4> x, p, v;
     pbd::DBuf<float> mass;
     std::vector<float> h_mass;              // host copy of massBuffer
+    // host transfers of float3 arrays: page-locked staging each way, the
+    // device float3 image that the pack / unpack kernels read and write, and
+    // an event marking the end of the last upload out of h_in
+    pbd::HBuf<float> h_in, h_out;
+    pbd::DBuf<float> d3;
+    cudaEvent_t in_done = nullptr;
     // meshTopol triangles: (i0, i1, i2, instance)
     pbd::DBuf<int4> tri;
     pbd::DBuf<int> pt_tri_first, pt_tri_last, pt_tri;  // point -> incident triangles
@@ -333,8 +369,8 @@ int launch_advect(pbd_object *o, float dt);
 int launch_advect_p0(pbd_object *o, float dt);
 int launch_integrate(pbd_object *o, float dt);
 int launch_sweeps(pbd_solver *s, int it0, int it1, bool obstacles_inside);
-// one per-color sweep whose stiffness exponent 1/(iter+1) is read from
-// device memory (the solve-to-residual loop)
+// one sweep whose stiffness exponent 1/(iter+1) is read from device memory
+// (the solve-to-residual loop)
 int launch_sweep_dev(pbd_solver *s, const float *expk_dev, bool obstacles_inside);
 int prepare_gs_path(pbd_solver *s);
 // residual partial sums of pos over the distance and/or bending records

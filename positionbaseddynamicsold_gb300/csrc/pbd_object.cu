@@ -23,6 +23,7 @@
 #include <cooperative_groups.h>
 
 #include "pbd_common.cuh"
+#include "pbd_project.cuh"
 
 namespace cg = cooperative_groups;
 
@@ -268,15 +269,9 @@ __global__ void __launch_bounds__(256) k_integrate(int n, float dt, float4 *__re
     x[i] = make_float4(P.x, P.y, P.z, X.w);
 }
 
-// Position accessors: the per-color kernel reads and writes the global
-// array; the cluster kernel reads and writes the distributed shared memory of
+// Position accessor of the cluster kernel: the distributed shared memory of
 // a thread-block cluster, point i living in block i >> shift at slot
 // i & (2^shift - 1).
-struct GlobalPos {
-    float4 *p;
-    __device__ __forceinline__ float4 ld(int i) const { return p[i]; }
-    __device__ __forceinline__ void st(int i, float4 v) const { p[i] = v; }
-};
 struct ClusterPos {
     float4 *local;
     int shift;
@@ -287,85 +282,6 @@ struct ClusterPos {
     __device__ __forceinline__ float4 ld(int i) const { return *at(i); }
     __device__ __forceinline__ void st(int i, float4 v) const { *at(i) = v; }
 };
-
-// distance constraint of ProjectContraintsGPUKernel (P/PBD_cuda.cu:1264-1294)
-template <class Pos>
-__device__ __forceinline__ void project_distance(int4 r, const Pos &p, float expk) {
-    float4 P0 = p.ld(r.x), P1 = p.ld(r.y);
-    float m0 = P0.w, m1 = P1.w;
-    float msum = m0 + m1;
-    float dx = P0.x - P1.x, dy = P0.y - P1.y, dz = P0.z - P1.z;
-    float d = sqrtf(dx * dx + dy * dy + dz * dz);
-    if (msum == 0.f || d == 0.f) return;
-    float rest = __int_as_float(r.z), s = __int_as_float(r.w);
-    float k = 1.f - powf(1.f - s, expk);
-    float s0 = -m0 / msum * (d - rest);
-    float s1 = m1 / msum * (d - rest);
-    p.st(r.x, make_float4(P0.x + ((dx * s0) / d) * k, P0.y + ((dy * s0) / d) * k,
-                          P0.z + ((dz * s0) / d) * k, m0));
-    p.st(r.y, make_float4(P1.x + ((dx * s1) / d) * k, P1.y + ((dy * s1) / d) * k,
-                          P1.z + ((dz * s1) / d) * k, m1));
-}
-
-struct v3 {
-    float x, y, z;
-};
-__device__ __forceinline__ v3 mk3(float x, float y, float z) { return {x, y, z}; }
-__device__ __forceinline__ v3 sub3(v3 a, v3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
-__device__ __forceinline__ v3 add3(v3 a, v3 b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
-__device__ __forceinline__ v3 mul3(v3 a, float s) { return {a.x * s, a.y * s, a.z * s}; }
-__device__ __forceinline__ v3 div3(v3 a, float s) { return {a.x / s, a.y / s, a.z / s}; }
-__device__ __forceinline__ float dot3(v3 a, v3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
-__device__ __forceinline__ v3 cross3(v3 a, v3 b) {
-    return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
-}
-
-// dihedral bending: signed angle theta = atan2((nA x nB).E/|E|, nA.nB),
-// C = theta - theta0, dp_i = w_i * k*C/sum_j w_j|u_j|^2 * u_i with the
-// Bridson-Marino-Fedkiw (2003) gradients grad_i theta = -u_i, inside the
-// PBD projection of Mueller et al. (2007).  Same operation order as the
-// oracle's orc_bending_project_f32.
-template <class Pos>
-__device__ __forceinline__ void project_bending(int4 r, float2 par, const Pos &p, float expk) {
-    float4 Q0 = p.ld(r.x), Q1 = p.ld(r.y), Q2 = p.ld(r.z), Q3 = p.ld(r.w);
-    v3 e0 = mk3(Q0.x, Q0.y, Q0.z), e1 = mk3(Q1.x, Q1.y, Q1.z);
-    v3 wa = mk3(Q2.x, Q2.y, Q2.z), wb = mk3(Q3.x, Q3.y, Q3.z);
-    v3 E = sub3(e1, e0);
-    v3 na = cross3(sub3(wa, e0), sub3(wa, e1));
-    v3 nb = cross3(sub3(wb, e1), sub3(wb, e0));
-    float na2 = dot3(na, na), nb2 = dot3(nb, nb), el2 = dot3(E, E);
-    if (na2 == 0.f || nb2 == 0.f || el2 == 0.f) return;
-    float el = sqrtf(el2);
-    float sn = dot3(cross3(na, nb), E) / el;
-    float cs = dot3(na, nb);
-    float c = atan2f(sn, cs) - par.x;
-    if (c > 3.14159265f) c -= 6.28318531f;
-    if (c < -3.14159265f) c += 6.28318531f;
-    v3 a = div3(na, na2), b = div3(nb, nb2);
-    v3 uwa = mul3(a, el), uwb = mul3(b, el);
-    v3 ue0 = add3(mul3(a, dot3(sub3(wa, e1), E) / el), mul3(b, dot3(sub3(wb, e1), E) / el));
-    v3 ue1 = sub3(mul3(a, -dot3(sub3(wa, e0), E) / el), mul3(b, dot3(sub3(wb, e0), E) / el));
-    float den = Q0.w * dot3(ue0, ue0) + Q1.w * dot3(ue1, ue1) + Q2.w * dot3(uwa, uwa) +
-                Q3.w * dot3(uwb, uwb);
-    if (!(den > 0.f)) return;
-    float k = 1.f - powf(1.f - par.y, expk);
-    float s = k * c / den;
-    v3 n0 = add3(e0, mul3(ue0, Q0.w * s));
-    v3 n1 = add3(e1, mul3(ue1, Q1.w * s));
-    v3 n2 = add3(wa, mul3(uwa, Q2.w * s));
-    v3 n3 = add3(wb, mul3(uwb, Q3.w * s));
-    p.st(r.x, make_float4(n0.x, n0.y, n0.z, Q0.w));
-    p.st(r.y, make_float4(n1.x, n1.y, n1.z, Q1.w));
-    p.st(r.z, make_float4(n2.x, n2.y, n2.z, Q2.w));
-    p.st(r.w, make_float4(n3.x, n3.y, n3.z, Q3.w));
-}
-
-// ANCHOR (P/PBD_cuda.cu:1298-1305): snap the point to its rest position
-template <class Pos>
-__device__ __forceinline__ void project_anchor(float4 a, const Pos &p) {
-    int i = __float_as_int(a.w);
-    p.st(i, make_float4(a.x, a.y, a.z, p.ld(i).w));
-}
 
 // one color phase: distance, then bending, then anchor records of the color.
 // Launched with programmatic stream serialization: the records (which no
@@ -802,7 +718,7 @@ int launch_sweeps(pbd_solver *s, int it0, int it1, bool obstacles_inside) {
     PBD_CUDA(cudaStreamIsCapturing(o->stream, &cap));
     if (cap == cudaStreamCaptureStatusNone) PBD_TRY(prepare_gs_path(s));
     int path = resolved_path(s);
-    PBD_CHECK(path != -1, PBD_ERR_CUDA, "cluster plan failed: %s", pbd_last_error());
+    PBD_CHECK(path != -1, PBD_ERR_CUDA, "launch plan failed: %s", pbd_last_error());
     PBD_CHECK(path != -2, PBD_ERR_STATE,
               "the requested Gauss-Seidel form does not apply to this object (%d points)", o->n);
     if (path == PBD_GS_CLUSTER) {
@@ -1192,7 +1108,8 @@ int pbd_object_destroy(pbd_object *o) {
     if (!o) return PBD_OK;
     if (o->stream) cudaStreamSynchronize(o->stream);
     cudaStream_t s = o->stream;
-    delete o;  // DBuf members free their memory
+    if (o->in_done) cudaEventDestroy(o->in_done);
+    delete o;  // DBuf / HBuf members free their memory
     if (s) cudaStreamDestroy(s);
     return PBD_OK;
 }
@@ -1205,26 +1122,63 @@ int pbd_object_sizes(const pbd_object *o, int *n, int *nt, int *np) {
     return PBD_OK;
 }
 
-static int copy_out3(pbd_object *o, const float4 *src, float *dst) {
-    PBD_CHECK(o && dst, PBD_ERR_ARG, "null argument");
-    std::vector<float4> h(o->n);
-    PBD_CUDA(cudaMemcpyAsync(h.data(), src, sizeof(float4) * o->n, cudaMemcpyDeviceToHost, o->stream));
-    PBD_CUDA(cudaStreamSynchronize(o->stream));
-    for (int i = 0; i < o->n; ++i) {
-        dst[3 * i] = h[i].x;
-        dst[3 * i + 1] = h[i].y;
-        dst[3 * i + 2] = h[i].z;
-    }
+// float3 <-> float4 (w = massBuffer value, or 0) on the device, so that host
+// transfers move 12 bytes per point through page-locked staging
+__global__ void k_pack3(int n, const float *__restrict__ src, const float *__restrict__ mass,
+                        float4 *__restrict__ dst) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    dst[i] = make_float4(src[3 * i], src[3 * i + 1], src[3 * i + 2], mass ? mass[i] : 0.f);
+}
+
+__global__ void k_unpack3(int n, const float4 *__restrict__ src, float *__restrict__ dst) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float4 v = src[i];
+    dst[3 * i] = v.x;
+    dst[3 * i + 1] = v.y;
+    dst[3 * i + 2] = v.z;
+}
+
+static int staging(pbd_object *o) {
+    size_t m = 3 * (size_t)o->n;
+    PBD_TRY(o->h_in.alloc(m));
+    PBD_TRY(o->h_out.alloc(m));
+    PBD_TRY(o->d3.alloc(m));
+    if (!o->in_done) PBD_CUDA(cudaEventCreateWithFlags(&o->in_done, cudaEventDisableTiming));
     return PBD_OK;
 }
 
+// blocking: dst holds the values when this returns
+static int copy_out3(pbd_object *o, const float4 *src, float *dst) {
+    PBD_CHECK(o && dst, PBD_ERR_ARG, "null argument");
+    if (o->n == 0) return PBD_OK;
+    PBD_TRY(staging(o));
+    size_t bytes = sizeof(float) * 3 * (size_t)o->n;
+    k_unpack3<<<grid_for(o->n, 256), 256, 0, o->stream>>>(o->n, src, o->d3.p);
+    PBD_LAUNCH();
+    PBD_CUDA(cudaMemcpyAsync(o->h_out.p, o->d3.p, bytes, cudaMemcpyDeviceToHost, o->stream));
+    PBD_CUDA(cudaStreamSynchronize(o->stream));
+    std::memcpy(dst, o->h_out.p, bytes);
+    return PBD_OK;
+}
+
+// stream-ordered: src is copied into the staging before this returns, and
+// work queued on the object's stream afterwards sees the new values
 static int copy_in3(pbd_object *o, float4 *dst, const float *src, bool keep_w) {
     PBD_CHECK(o && src, PBD_ERR_ARG, "null argument");
-    std::vector<float4> h(o->n);
-    for (int i = 0; i < o->n; ++i)
-        h[i] = make_float4(src[3 * i], src[3 * i + 1], src[3 * i + 2], keep_w ? o->h_mass[i] : 0.f);
-    PBD_CUDA(cudaMemcpyAsync(dst, h.data(), sizeof(float4) * o->n, cudaMemcpyHostToDevice, o->stream));
-    PBD_CUDA(cudaStreamSynchronize(o->stream));
+    if (o->n == 0) return PBD_OK;
+    PBD_TRY(staging(o));
+    size_t bytes = sizeof(float) * 3 * (size_t)o->n;
+    // the previous upload out of the staging has to be done before it is
+    // overwritten
+    PBD_CUDA(cudaEventSynchronize(o->in_done));
+    std::memcpy(o->h_in.p, src, bytes);
+    PBD_CUDA(cudaMemcpyAsync(o->d3.p, o->h_in.p, bytes, cudaMemcpyHostToDevice, o->stream));
+    PBD_CUDA(cudaEventRecord(o->in_done, o->stream));
+    k_pack3<<<grid_for(o->n, 256), 256, 0, o->stream>>>(o->n, o->d3.p,
+                                                         keep_w ? o->mass.p : nullptr, dst);
+    PBD_LAUNCH();
     return PBD_OK;
 }
 
@@ -1320,6 +1274,7 @@ int pbd_constraints_sort_edges_colors(pbd_object *o) {
     int np = o->np;
     cudaStream_t s = o->stream;
     o->h_worksets.assign(2 * (size_t)o->n_colors, 0);
+    o->cl_state = 0;  // the cluster plan follows the records
     o->h_dseg.assign(o->n_colors + 1, 0);
     o->h_bseg.assign(o->n_colors + 1, 0);
     o->h_aseg.assign(o->n_colors + 1, 0);
@@ -1602,6 +1557,12 @@ int pbd_solver_step(pbd_solver *s, float dt, int substeps, int iterations, pbd_c
 
 int pbd_solver_set_gs_path(pbd_solver *s, int path) {
     PBD_CHECK(s && path >= PBD_GS_AUTO && path <= PBD_GS_CLUSTER, PBD_ERR_ARG, "bad path");
+    if (s->gs_path != path) {  // cached graphs hold the old form's launches
+        if (s->gexec) cudaGraphExecDestroy(s->gexec);
+        s->gexec = nullptr;
+        if (s->rexec) cudaGraphExecDestroy(s->rexec);
+        s->rexec = nullptr;
+    }
     s->gs_path = path;
     return PBD_OK;
 }
@@ -1610,7 +1571,7 @@ int pbd_solver_get_gs_path(pbd_solver *s, int *path) {
     PBD_CHECK(s && path && s->obj, PBD_ERR_STATE, "solver has no target");
     PBD_CHECK(s->obj->sorted, PBD_ERR_STATE, "constraints are not color-sorted");
     int p = resolved_path(s);
-    PBD_CHECK(p != -1, PBD_ERR_CUDA, "cluster plan failed");
+    PBD_CHECK(p != -1, PBD_ERR_CUDA, "launch plan failed");
     *path = p == -2 ? PBD_GS_PER_COLOR : p;
     return PBD_OK;
 }
@@ -1621,9 +1582,10 @@ int pbd_solver_graph_kernels(pbd_solver *s, long long *n) {
     return PBD_OK;
 }
 
-// Times `iterations` sweeps, replayed from a CUDA graph, for every launch
-// form that applies to the object (per-color launches with 64..512 threads
-// per block; the cluster form when the object fits one cluster), keeps the
+// Times `iterations` sweeps, one launch sequence per sweep as a substep with
+// collisions issues them, replayed from a CUDA graph, for every launch form
+// that applies to the object (per-color launches with 64..512 threads per
+// block; the cluster form when the object fits one cluster), keeps the
 // fastest and restores the predicted positions.  Every form gives the same
 // result, so the choice only changes speed.
 int pbd_solver_autotune(pbd_solver *s, int iterations, int reps, pbd_autotune_result *res) {
@@ -1654,14 +1616,18 @@ int pbd_solver_autotune(pbd_solver *s, int iterations, int reps, pbd_autotune_re
     int rc = PBD_OK;
     for (size_t k = 0; k < cands.size() && k < 8 && rc == PBD_OK; ++k) {
         s->gs_path = cands[k].path;
-        if (cands[k].path == PBD_GS_PER_COLOR) o->gs_block = cands[k].block;
+        if (cands[k].path != PBD_GS_CLUSTER) o->gs_block = cands[k].block;
         cudaGraph_t g = nullptr;
         cudaGraphExec_t ge = nullptr;
+        rc = prepare_gs_path(s);  // plans outside the capture
+        if (rc != PBD_OK) break;
+        if (resolved_path(s) != cands[k].path) continue;  // does not apply to this object
         if (cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
             rc = PBD_ERR_CUDA;
             break;
         }
-        int r = launch_sweeps(s, 0, iterations, true);
+        int r = PBD_OK;
+        for (int it = 0; it < iterations && r == PBD_OK; ++it) r = launch_sweeps(s, it, it + 1, true);
         cudaError_t e = cudaStreamEndCapture(st, &g);
         if (r != PBD_OK || e != cudaSuccess) {
             if (g) cudaGraphDestroy(g);
@@ -1686,12 +1652,13 @@ int pbd_solver_autotune(pbd_solver *s, int iterations, int reps, pbd_autotune_re
         cudaMemcpyAsync(o->p.p, save.p, sizeof(float4) * o->n, cudaMemcpyDeviceToDevice, st);
         if (rc != PBD_OK) break;
         double us = 1e3 * ms / ((double)reps * iterations);
-        res->path[k] = cands[k].path;
-        res->block[k] = cands[k].block;
-        res->us_per_sweep[k] = us;
-        res->n = (int)k + 1;
+        const int m = res->n;
+        res->path[m] = cands[k].path;
+        res->block[m] = cands[k].block;
+        res->us_per_sweep[m] = us;
+        res->n = m + 1;
         if (best < 0 || us < best_us) {
-            best = (int)k;
+            best = m;
             best_us = us;
         }
     }
@@ -1703,9 +1670,10 @@ int pbd_solver_autotune(pbd_solver *s, int iterations, int reps, pbd_autotune_re
         set_error("autotune failed: %s", cudaGetErrorString(cudaGetLastError()));
         return rc != PBD_OK ? rc : PBD_ERR_CUDA;
     }
-    s->gs_path = cands[best].path;
-    if (cands[best].path == PBD_GS_PER_COLOR) o->gs_block = cands[best].block;
+    s->gs_path = res->path[best];
+    if (res->path[best] != PBD_GS_CLUSTER) o->gs_block = res->block[best];
     res->best = best;
+    PBD_TRY(prepare_gs_path(s));
     if (s->gexec) cudaGraphExecDestroy(s->gexec);
     s->gexec = nullptr;
     if (s->rexec) cudaGraphExecDestroy(s->rexec);

@@ -78,7 +78,7 @@ EXPORTS = [
     "pbd_warmstart_record", "pbd_warmstart_train_step", "pbd_warmstart_features",
     "pbd_warmstart_predict", "pbd_solver_set_warmstart", "pbd_solver_project_to_residual",
     "pbd_solver_autotune", "pbd_solver_get_gs_block",
-    "pbd_solver_set_gs_block", "pbd_solver_train_substep",
+    "pbd_solver_set_gs_block", "pbd_solver_train_substep"
 ]
 
 
