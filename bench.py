@@ -181,6 +181,8 @@ def run_ours(args, rank, world):
     solver.set_gs_path({"auto": 0, "per-color": 1, "cluster": 2}[args.gs_path])
     if args.gs_block:
         solver.set_gs_block(args.gs_block)
+    if args.gs_cluster:
+        solver.set_gs_cluster(args.gs_cluster)
     stream = torch.cuda.ExternalStream(obj.stream())
     nd = int((sc["ctype"] == scenes.DISTANCE).sum())
     nb = int((sc["ctype"] == scenes.BENDING).sum())
@@ -259,16 +261,22 @@ def run_ours(args, rank, world):
     # roofline of the dominant kernel (the GS sweep): eager projections on
     # the same state, timed with events on the object's stream, launched as
     # the timed substeps launch them (per-color: one launch per color phase;
-    # cluster: one launch for all sweeps); algorithmic bytes per sweep =
+    # resident form: one launch per sweep between collision passes, one for
+    # all sweeps without collisions); algorithmic bytes per sweep =
     # 84*nd + 164*nb
     pos_save = obj.positions()
     prd_save = obj.predicted()
     bytes_sweep = 84.0 * nd + 164.0 * nb
     gs_form = solver.gs_path()
-    gs_kernel = {1: "k_project_color", 2: "k_gs_cluster"}[gs_form]
+    gs_kernel = {1: "k_project_color", 2: "k_gs_resident"}[gs_form]
+    per_sweep = gs_form == 2 and colli_on
 
     def sweeps():
-        solver.project_constraint(iters)
+        if per_sweep:
+            for _ in range(iters):
+                solver.project_constraint(1)
+        else:
+            solver.project_constraint(iters)
 
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     sweeps()
@@ -281,7 +289,7 @@ def run_ours(args, rank, world):
         e1.record(stream)
     torch.cuda.synchronize()
     gs_ms = e0.elapsed_time(e1)
-    n_launch = reps * (iters * n_colors if gs_form == 1 else 1)
+    n_launch = reps * (iters * n_colors if gs_form == 1 else iters if per_sweep else 1)
     achieved = reps * iters * bytes_sweep / (gs_ms / 1e3) / 1e9
     obj.set_positions(pos_save)
     obj.set_predicted(prd_save)
@@ -292,16 +300,27 @@ def run_ours(args, rank, world):
     v_h = obj.velocities()
     e2e_steps = max(10, min(args.steps, 100))
     obj.sync()
+    ph = [0.0, 0.0, 0.0]   # host clock: uploads, step (launch + wait), downloads
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
+        ta = time.perf_counter()
         obj.set_positions(x_h)
         obj.set_velocities(v_h)
+        tb = time.perf_counter()
         step()
+        obj.sync()
+        tc = time.perf_counter()
         x_h = obj.positions()
         v_h = obj.velocities()
+        td = time.perf_counter()
+        ph[0] += tb - ta
+        ph[1] += tc - tb
+        ph[2] += td - tc
     e2e_s = time.perf_counter() - t0
     e2e = {"value": world * e2e_steps / e2e_s, "unit": "substeps/s",
-           "h2d_bytes_per_step": 2 * 12 * obj.n_points, "d2h_bytes_per_step": 2 * 12 * obj.n_points}
+           "h2d_bytes_per_step": 2 * 12 * obj.n_points, "d2h_bytes_per_step": 2 * 12 * obj.n_points,
+           "phases_us": {"upload": 1e6 * ph[0] / e2e_steps, "step": 1e6 * ph[1] / e2e_steps,
+                         "download": 1e6 * ph[2] / e2e_steps}}
 
     out = {
         "metric": METRIC, "value": value, "unit": "substeps/s", "n_gpus": world,
@@ -321,7 +340,8 @@ def run_ours(args, rank, world):
                      "traffic": args.traffic if args.traffic is not None else
                      (TRAFFIC_BYTES.get(args.workload) if gs_form == 1 else None),
                      "launches_timed": n_launch, "avg_launch_us": gs_ms * 1e3 / n_launch,
-                     "bytes_per_sweep": bytes_sweep},
+                     "bytes_per_sweep": bytes_sweep,
+                     "cluster_size": solver.gs_cluster() if gs_form == 2 else None},
         "clocks": clk,
         "wall_s_timed_region": t_wall,
         "last_step": {"candidates": stats.get("candidates"), "contacts": stats.get("contacts"),
@@ -468,6 +488,8 @@ def main():
     ap.add_argument("--preroll", type=int, default=120)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--gs-path", default="auto", choices=["auto", "per-color", "cluster"])
+    ap.add_argument("--gs-cluster", type=int, default=0,
+                    help="cluster size of the resident form (with --gs-path cluster)")
     ap.add_argument("--gs-block", type=int, default=0,
                     help="threads per block of the per-color launches (with --gs-path "
                          "per-color; profiles pin the autotuned form this way: under ncu "

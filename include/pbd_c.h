@@ -167,11 +167,12 @@ int pbd_solver_step(pbd_solver *s, float dt, int substeps, int iterations, pbd_c
                     int use_graph);
 
 /* How a Gauss-Seidel sweep runs: PBD_GS_PER_COLOR launches one kernel per
- * color (any size); PBD_GS_CLUSTER keeps every point in the distributed
- * shared memory of one 16-block thread-block cluster (objects up to 131,072
- * points) and separates colors by cluster barriers; PBD_GS_AUTO (default)
- * takes the per-color form.  Both give identical results;
- * pbd_solver_autotune picks the fastest for an object.
+ * color (any size); PBD_GS_CLUSTER (the resident form) keeps every point in
+ * the shared memory of one thread-block cluster of S = 1, 2, 4, 8 or 16
+ * blocks (about 14,000 points per block on GB300) for whole sweeps, color
+ * phases separated by cluster barriers; PBD_GS_AUTO (default) takes the
+ * per-color form.  All give identical results; pbd_solver_autotune picks the
+ * fastest form, block size and cluster size for an object.
  * No reference counterpart (the reference launches one kernel per color). */
 enum { PBD_GS_AUTO = 0, PBD_GS_PER_COLOR = 1, PBD_GS_CLUSTER = 2 };
 int pbd_solver_set_gs_path(pbd_solver *s, int path);
@@ -181,22 +182,27 @@ int pbd_solver_get_gs_path(pbd_solver *s, int *path);
 /* Autotuner (no reference counterpart): times `iterations` sweeps (one
  * launch sequence per sweep) replayed `reps` times from a CUDA graph for each
  * launch form that applies -- the per-color launches with 64, 128, 256 and
- * 512 threads per block, and the cluster form when the object fits one
- * cluster -- and keeps the
+ * 512 threads per block, and the resident form with every cluster size that
+ * holds the object (block = S in the result) -- and keeps the
  * fastest for this solver and object.  The predicted positions are restored;
  * all forms give identical results. */
 typedef struct pbd_autotune_result {
     int n;                  /* candidates timed                       */
     int best;               /* index of the one kept                  */
-    int path[8];            /* PBD_GS_PER_COLOR / PBD_GS_CLUSTER      */
-    int block[8];           /* threads per block                      */
-    double us_per_sweep[8]; /* GPU time per sweep, microseconds       */
+    int path[12];            /* PBD_GS_PER_COLOR / PBD_GS_CLUSTER     */
+    int block[12];           /* threads per block; cluster size S     */
+    double us_per_sweep[12]; /* GPU time per sweep, microseconds      */
 } pbd_autotune_result;
 int pbd_solver_autotune(pbd_solver *s, int iterations, int reps, pbd_autotune_result *result);
 /* threads per block of the per-color launches (256 until autotuned or set;
  * a multiple of 32 in [32, 512]) */
 int pbd_solver_set_gs_block(pbd_solver *s, int block);
 int pbd_solver_get_gs_block(pbd_solver *s, int *block);
+/* cluster size S of the resident form (0: the largest that holds the object;
+ * else 1, 2, 4, 8 or 16); get reports the size a sweep would use, 0 when
+ * none holds the object */
+int pbd_solver_set_gs_cluster(pbd_solver *s, int size);
+int pbd_solver_get_gs_cluster(pbd_solver *s, int *size);
 
 /* kernel launches recorded in the cached pbd_solver_step graph (no
  * reference counterpart; used to report launches per step) */

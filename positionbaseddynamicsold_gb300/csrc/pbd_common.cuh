@@ -179,14 +179,15 @@ struct pbd_object {
     pbd::DBuf<float2> bpar;                     // rest angle, stiffness
     pbd::DBuf<float4> arec;                     // rest xyz, point id bits
     std::vector<int> h_dseg, h_bseg, h_aseg;    // n_colors+1 starts each
-    // records re-ordered for the cluster kernel: by color, then by the block
-    // owning the record's first point; segments (color*S + block)
+    // resident (cluster) form of the sweep: per-color record starts
+    // (dseg | bseg | aseg), the distinct stiffness values of the records (at
+    // most 8), the cluster sizes whose shared memory holds every point (bit
+    // S set for S in 1, 2, 4, 8, 16) and the size in use (0: the largest
+    // that fits)
     int cl_state = 0;           // 0 not built, 1 usable, -1 not applicable
-    int cl_S = 0, cl_shift = 0;
-    pbd::DBuf<int4> cdrec, cbidx;
-    pbd::DBuf<float2> cbpar;
-    pbd::DBuf<float4> carec;
-    pbd::DBuf<int> cdseg, cbseg, caseg;
+    int cl_fit = 0, cl_S = 0, cl_ntab = 0;
+    pbd::DBuf<int> cl_seg;
+    pbd::DBuf<float> cl_tab;
     // residual
     double res_den = 0.0;
     double res_den_d = 0.0;                 // distance constraints only

@@ -269,20 +269,6 @@ __global__ void __launch_bounds__(256) k_integrate(int n, float dt, float4 *__re
     x[i] = make_float4(P.x, P.y, P.z, X.w);
 }
 
-// Position accessor of the cluster kernel: the distributed shared memory of
-// a thread-block cluster, point i living in block i >> shift at slot
-// i & (2^shift - 1).
-struct ClusterPos {
-    float4 *local;
-    int shift;
-    __device__ __forceinline__ float4 *at(int i) const {
-        return cg::this_cluster().map_shared_rank(local, (unsigned)(i >> shift)) +
-               (i & ((1 << shift) - 1));
-    }
-    __device__ __forceinline__ float4 ld(int i) const { return *at(i); }
-    __device__ __forceinline__ void st(int i, float4 v) const { *at(i) = v; }
-};
-
 // one color phase: distance, then bending, then anchor records of the color.
 // Launched with programmatic stream serialization: the records (which no
 // phase writes) are loaded first, the next phase is allowed to launch, and
@@ -343,87 +329,162 @@ __device__ __forceinline__ float4 obstacle_point(float4 P, int sphere_on, float3
     return P;
 }
 
-// Colored GS held in one thread-block cluster: the cluster's distributed
-// shared memory holds every point; block r processes the records of each
-// color whose first point it owns (segments (color*S + r) of the
-// cluster-ordered records); a cluster barrier separates color phases, so a
-// sweep costs one launch instead of one per color.  Within a color no two
-// records share a point, so the result equals the per-color launches'.
-constexpr int kClusterThreads = 1024;
-constexpr int kClusterMaxColors = 256;
-__global__ void __launch_bounds__(kClusterThreads, 1) k_gs_cluster(
-    const int4 *__restrict__ drec, const int *__restrict__ dseg, const int4 *__restrict__ bidx,
-    const float2 *__restrict__ bpar, const int *__restrict__ bseg,
-    const float4 *__restrict__ arec, const int *__restrict__ aseg, int n_colors, int n,
-    int shift, float4 *__restrict__ p, int it0, int it1, int sphere_on, float3 sc, float sr,
-    int ground_on, float gh) {
-    extern __shared__ float4 sp[];
-    // this block's segment of every color, per record kind: [s0, s1)
-    __shared__ int sd0[kClusterMaxColors], sd1[kClusterMaxColors];
-    __shared__ int sb0[kClusterMaxColors], sb1[kClusterMaxColors];
-    __shared__ int sa0[kClusterMaxColors], sa1[kClusterMaxColors];
-    cg::cluster_group cl = cg::this_cluster();
-    const int r = (int)cl.block_rank();
-    const int S = (int)cl.num_blocks();
-    const int chunk = 1 << shift;
-    const int base = r << shift;
-    const int tid = threadIdx.x;
-    for (int c = tid; c < n_colors; c += blockDim.x) {
-        int q = c * S + r;
-        sd0[c] = dseg[q];
-        sd1[c] = dseg[q + 1];
-        sb0[c] = bseg[q];
-        sb1[c] = bseg[q + 1];
-        sa0[c] = aseg[q];
-        sa1[c] = aseg[q + 1];
+// Resident form of the colored GS: every point lives in shared memory for a
+// whole launch of one or more sweeps.  A thread-block cluster of S blocks
+// (S = 1: a single block, no cluster) keeps point i in block i % S at slot
+// i / S (distributed shared memory for S > 1), so a color phase costs one
+// cluster barrier instead of a kernel launch.  Block r takes the r-th of S
+// even shares of every color's flat record list (distance | bending |
+// anchor, the per-color kernel's order; no two records of
+// a color share a point), one record per thread and round.  The first
+// record of each thread in the next phase is fetched before the barrier.  The
+// stiffness factors 1 - (1 - s)^(1/(it+1)) of the object's distinct
+// stiffness values are computed once per sweep into a table; a record whose
+// value is not in the table computes its own.  Same records, same arithmetic
+// per record, so the same result as the per-color launches.
+constexpr int kResThreads = 1024;
+constexpr int kResMaxColors = 256;
+constexpr int kResTab = 8;
+
+template <int S>
+struct ResPos {
+    float4 *local;
+    __device__ __forceinline__ float4 *at(int i) const {
+        if constexpr (S == 1)
+            return local + i;
+        else
+            return cg::this_cluster().map_shared_rank(local + (unsigned)i / S,
+                                                      (unsigned)i % S);
     }
-    for (int i = tid; i < chunk; i += blockDim.x) {
-        int g = base + i;
-        sp[i] = g < n ? p[g] : make_float4(0.f, 0.f, 0.f, 0.f);
-    }
-    cl.sync();
-    ClusterPos P{sp, shift};
-    // the first record of each kind this thread takes in the coming phase,
-    // loaded before the barrier that precedes the phase
-    int4 dr = make_int4(0, 0, 0, 0), br = make_int4(0, 0, 0, 0);
-    float2 bp = make_float2(0.f, 0.f);
-    float4 ar = make_float4(0.f, 0.f, 0.f, 0.f);
-    bool hd = false, hb = false, ha = false;
-    auto fetch = [&](int c) {
-        int kd = sd0[c] + tid, kb = sb0[c] + tid, ka = sa0[c] + tid;
-        hd = kd < sd1[c];
-        hb = kb < sb1[c];
-        ha = ka < sa1[c];
-        if (hd) dr = drec[kd];
-        if (hb) {
-            br = bidx[kb];
-            bp = bpar[kb];
+    __device__ __forceinline__ float4 ld(int i) const { return *at(i); }
+    __device__ __forceinline__ void st(int i, float4 v) const { *at(i) = v; }
+};
+
+template <int S>
+__device__ __forceinline__ void res_sync() {
+    if constexpr (S == 1)
+        __syncthreads();
+    else
+        cg::this_cluster().sync();
+}
+
+struct ResRec {
+    int kind;  // 0 none, 1 distance, 2 bending, 3 anchor
+    int4 r;    // distance {i0, i1, rest, s}; bending {e0, e1, wA, wB}
+    float4 f;  // bending {rest angle, s}; anchor {rest xyz, point id}
+};
+
+// the object's factor for stiffness s (table hit) or s's own
+__device__ __forceinline__ float res_factor(float s, float expk, const float *ts, const float *tk,
+                                            int ntab) {
+    for (int j = 0; j < ntab; ++j)
+        if (ts[j] == s) return tk[j];
+    return stiffness_factor(s, expk);
+}
+
+template <int S>
+__device__ __forceinline__ void res_project(const ResRec &A, const ResPos<S> &P, float expk,
+                                            const float *ts, const float *tk, int ntab) {
+    if (A.kind == 1) {
+        float4 N0, N1;
+        if (distance_update(P.ld(A.r.x), P.ld(A.r.y), __int_as_float(A.r.z),
+                            res_factor(__int_as_float(A.r.w), expk, ts, tk, ntab), N0, N1)) {
+            P.st(A.r.x, N0);
+            P.st(A.r.y, N1);
         }
-        if (ha) ar = arec[ka];
+    } else if (A.kind == 2) {
+        float4 Q[4] = {P.ld(A.r.x), P.ld(A.r.y), P.ld(A.r.z), P.ld(A.r.w)}, N[4];
+        if (bending_update(Q, A.f.x, res_factor(A.f.y, expk, ts, tk, ntab), N)) {
+            P.st(A.r.x, N[0]);
+            P.st(A.r.y, N[1]);
+            P.st(A.r.z, N[2]);
+            P.st(A.r.w, N[3]);
+        }
+    } else if (A.kind == 3) {
+        int i = __float_as_int(A.f.w);
+        P.st(i, make_float4(A.f.x, A.f.y, A.f.z, P.ld(i).w));
+    }
+}
+
+// seg = dseg | bseg | aseg (n_colors + 1 starts each); tab = the distinct
+// stiffness values; sweeps it0..it1-1, the analytic obstacles after each
+// sweep when sphere_on / ground_on.
+template <int S>
+__global__ void __launch_bounds__(kResThreads, 1) k_gs_resident(
+    const int *__restrict__ seg, const int4 *__restrict__ drec, const int4 *__restrict__ bidx,
+    const float2 *__restrict__ bpar, const float4 *__restrict__ arec,
+    const float *__restrict__ tab, int ntab, int n_colors, int n, float4 *__restrict__ p,
+    int it0, int it1, int sphere_on, float3 sc, float sr, int ground_on, float gh) {
+    extern __shared__ float4 sp[];
+    __shared__ int sg[3 * (kResMaxColors + 1)];
+    __shared__ float tab_s[kResTab], tab_k[kResTab];
+    int r = 0;
+    if constexpr (S > 1) r = (int)cg::this_cluster().block_rank();
+    const int tid = threadIdx.x;
+    const int nc1 = n_colors + 1;
+    const int nloc = (n - r + S - 1) / S;  // this block's points: r, r + S, r + 2S, ...
+    for (int c = tid; c < 3 * nc1; c += kResThreads) sg[c] = seg[c];
+    if (tid < ntab) tab_s[tid] = tab[tid];
+    for (int j = tid; j < nloc; j += kResThreads) sp[j] = p[j * S + r];
+    __syncthreads();
+    const ResPos<S> P{sp};
+    // block r's share [lo, hi) of color c's flat record list
+    auto share = [&](int c, int &lo, int &hi, int &dn, int &bn) {
+        dn = sg[c + 1] - sg[c];
+        bn = sg[nc1 + c + 1] - sg[nc1 + c];
+        int an = sg[2 * nc1 + c + 1] - sg[2 * nc1 + c];
+        long long tot = dn + bn + an;
+        lo = (int)(tot * r / S);
+        hi = (int)(tot * (r + 1) / S);
     };
-    fetch(0);
+    auto fetch = [&](int c, int f, int hi, int dn, int bn) {
+        ResRec q;
+        q.kind = 0;
+        q.r = make_int4(0, 0, 0, 0);
+        q.f = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (f >= hi) return q;
+        if (f < dn) {
+            q.kind = 1;
+            q.r = drec[sg[c] + f];
+        } else if (f < dn + bn) {
+            q.kind = 2;
+            int k = sg[nc1 + c] + (f - dn);
+            q.r = bidx[k];
+            float2 bp = bpar[k];
+            q.f = make_float4(bp.x, bp.y, 0.f, 0.f);
+        } else {
+            q.kind = 3;
+            q.f = arec[sg[2 * nc1 + c] + (f - dn - bn)];
+        }
+        return q;
+    };
+    int lo, hi, dn, bn;
+    share(0, lo, hi, dn, bn);
+    ResRec A = fetch(0, lo + tid, hi, dn, bn);
+    res_sync<S>();  // every block's points are in place before any remote access
     for (int it = it0; it < it1; ++it) {
-        float expk = (float)(1.0 / (double)(it + 1));
+        const float expk = (float)(1.0 / (double)(it + 1));
+        if (tid < ntab) tab_k[tid] = stiffness_factor(tab_s[tid], expk);
+        __syncthreads();
         for (int c = 0; c < n_colors; ++c) {
-            if (hd) project_distance(dr, P, expk);
-            for (int k = sd0[c] + tid + (int)blockDim.x; k < sd1[c]; k += blockDim.x)
-                project_distance(drec[k], P, expk);
-            if (hb) project_bending(br, bp, P, expk);
-            for (int k = sb0[c] + tid + (int)blockDim.x; k < sb1[c]; k += blockDim.x)
-                project_bending(bidx[k], bpar[k], P, expk);
-            if (ha) project_anchor(ar, P);
-            for (int k = sa0[c] + tid + (int)blockDim.x; k < sa1[c]; k += blockDim.x)
-                project_anchor(arec[k], P);
-            fetch(c + 1 < n_colors ? c + 1 : 0);
-            cl.sync();
+            share(c, lo, hi, dn, bn);
+            res_project<S>(A, P, expk, tab_s, tab_k, ntab);
+            for (int f = lo + tid + kResThreads; f < hi; f += kResThreads)
+                res_project<S>(fetch(c, f, hi, dn, bn), P, expk, tab_s, tab_k, ntab);
+            // the next phase's first record, before the barrier
+            const int cn = c + 1 < n_colors ? c + 1 : 0;
+            int lo2, hi2, dn2, bn2;
+            share(cn, lo2, hi2, dn2, bn2);
+            A = fetch(cn, lo2 + tid, hi2, dn2, bn2);
+            res_sync<S>();
         }
         if (sphere_on || ground_on) {
-            for (int i = tid; i < chunk && base + i < n; i += blockDim.x)
-                sp[i] = obstacle_point(sp[i], sphere_on, sc, sr, ground_on, gh);
-            cl.sync();
+            for (int j = tid; j < nloc; j += kResThreads)
+                sp[j] = obstacle_point(sp[j], sphere_on, sc, sr, ground_on, gh);
+            res_sync<S>();
         }
     }
-    for (int i = tid; i < chunk && base + i < n; i += blockDim.x) p[base + i] = sp[i];
+    for (int j = tid; j < nloc; j += kResThreads) p[j * S + r] = sp[j];
 }
 
 // ColliWithShpGrd (P/PBD_cuda.cu:1519-1573): sphere push-out and ground plane
@@ -582,129 +643,151 @@ int launch_sweep_dev(pbd_solver *s, const float *expk_dev, bool obstacles_inside
     return PBD_OK;
 }
 
-// Builds the cluster-ordered records once per coloring; returns whether the
-// cluster form applies (the object fits one cluster's shared memory and the
-// device can co-schedule the cluster).
-static int cluster_plan(pbd_object *o) {
+template <int S>
+static bool resident_fits(int n, int smem_optin) {
+    size_t smem = sizeof(float4) * (size_t)((n + S - 1) / S);
+    if (smem < 16) smem = 16;
+    if ((long long)smem > smem_optin) return false;
+    if (cudaFuncSetAttribute(k_gs_resident<S>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)smem) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    if (S > 8 && cudaFuncSetAttribute(k_gs_resident<S>,
+                                      cudaFuncAttributeNonPortableClusterSizeAllowed, 1) !=
+                     cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(S);
+    cfg.blockDim = dim3(kResThreads);
+    cfg.dynamicSmemBytes = smem;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = S;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    int nclusters = 0;
+    if (cudaOccupancyMaxActiveClusters(&nclusters, k_gs_resident<S>, &cfg) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return nclusters >= 1;
+}
+
+// Once per coloring: which cluster sizes hold every point in shared memory,
+// the device copy of the per-color record starts and the table of distinct
+// stiffness values.  The records themselves are the per-color ones.
+static int resident_plan(pbd_object *o) {
     if (o->cl_state != 0) return PBD_OK;
     o->cl_state = -1;
-    if (o->np == 0 || o->n_colors == 0 || o->n_colors > kClusterMaxColors) return PBD_OK;
-    const int max_chunk_shift = 13;  // 8192 points x 16 B = 128 KiB per block
-    int S = 0, shift = 0;
-    for (int cand : {16, 8}) {
-        int sh = 0;
-        while (((long long)cand << sh) < o->n) ++sh;
-        if (sh > max_chunk_shift) continue;
-        if (sh < 5) sh = 5;
-        size_t smem = (size_t)sizeof(float4) << sh;
-        if (cudaFuncSetAttribute(k_gs_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)smem) != cudaSuccess) {
-            cudaGetLastError();
-            continue;
-        }
-        if (cand > 8 &&
-            cudaFuncSetAttribute(k_gs_cluster, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) !=
-                cudaSuccess) {
-            cudaGetLastError();
-            continue;
-        }
-        cudaLaunchConfig_t cfg = {};
-        cfg.gridDim = dim3(cand);
-        cfg.blockDim = dim3(kClusterThreads);
-        cfg.dynamicSmemBytes = smem;
-        cudaLaunchAttribute at[1];
-        at[0].id = cudaLaunchAttributeClusterDimension;
-        at[0].val.clusterDim.x = cand;
-        at[0].val.clusterDim.y = 1;
-        at[0].val.clusterDim.z = 1;
-        cfg.attrs = at;
-        cfg.numAttrs = 1;
-        int nclusters = 0;
-        if (cudaOccupancyMaxActiveClusters(&nclusters, k_gs_cluster, &cfg) != cudaSuccess) {
-            cudaGetLastError();
-            continue;
-        }
-        if (nclusters >= 1) {
-            S = cand;
-            shift = sh;
-            break;
-        }
-    }
-    if (!S) return PBD_OK;
+    o->cl_fit = 0;
+    const int nc = o->n_colors;
+    if (o->np == 0 || nc == 0 || nc > kResMaxColors) return PBD_OK;
+    int dev = 0, optin = 0;
+    PBD_CUDA(cudaGetDevice(&dev));
+    PBD_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+    optin -= (int)(sizeof(int) * 3 * (kResMaxColors + 1) + 2 * sizeof(float) * kResTab) + 1024;
+    if (resident_fits<1>(o->n, optin)) o->cl_fit |= 1;
+    if (resident_fits<2>(o->n, optin)) o->cl_fit |= 2;
+    if (resident_fits<4>(o->n, optin)) o->cl_fit |= 4;
+    if (resident_fits<8>(o->n, optin)) o->cl_fit |= 8;
+    if (resident_fits<16>(o->n, optin)) o->cl_fit |= 16;
+    if (!o->cl_fit) return PBD_OK;
     cudaStream_t s = o->stream;
-    int nc = o->n_colors;
-    int nd = o->h_dseg[nc], nb = o->h_bseg[nc], na = o->h_aseg[nc];
-    std::vector<int4> d(nd), bi(nb);
+    const int nd = o->h_dseg[nc], nb = o->h_bseg[nc];
+    std::vector<int4> d(nd);
     std::vector<float2> bp(nb);
-    std::vector<float4> a(na);
     if (nd) PBD_CUDA(cudaMemcpyAsync(d.data(), o->drec.p, sizeof(int4) * nd, cudaMemcpyDeviceToHost, s));
-    if (nb) {
-        PBD_CUDA(cudaMemcpyAsync(bi.data(), o->bidx.p, sizeof(int4) * nb, cudaMemcpyDeviceToHost, s));
-        PBD_CUDA(cudaMemcpyAsync(bp.data(), o->bpar.p, sizeof(float2) * nb, cudaMemcpyDeviceToHost, s));
-    }
-    if (na) PBD_CUDA(cudaMemcpyAsync(a.data(), o->arec.p, sizeof(float4) * na, cudaMemcpyDeviceToHost, s));
+    if (nb) PBD_CUDA(cudaMemcpyAsync(bp.data(), o->bpar.p, sizeof(float2) * nb, cudaMemcpyDeviceToHost, s));
     PBD_CUDA(cudaStreamSynchronize(s));
-    // stable bucketing of each color's records by owner block
-    auto order = [&](const std::vector<int> &seg, auto first_point, std::vector<int> &perm,
-                     std::vector<int> &cseg) {
-        int total = seg[nc];
-        perm.resize(total);
-        cseg.assign((size_t)nc * S + 1, 0);
-        int out = 0;
-        for (int c = 0; c < nc; ++c) {
-            std::vector<int> cnt(S + 1, 0);
-            for (int k = seg[c]; k < seg[c + 1]; ++k) cnt[(first_point(k) >> shift) + 1]++;
-            for (int r = 0; r < S; ++r) cnt[r + 1] += cnt[r];
-            for (int r = 0; r < S; ++r) cseg[(size_t)c * S + r] = out + cnt[r];
-            std::vector<int> pos(cnt.begin(), cnt.end() - 1);
-            for (int k = seg[c]; k < seg[c + 1]; ++k) perm[out + pos[first_point(k) >> shift]++] = k;
-            out += seg[c + 1] - seg[c];
-        }
-        cseg[(size_t)nc * S] = out;
+    // the first kResTab distinct stiffness values, in record order
+    std::vector<float> tab;
+    auto add = [&](float v) {
+        if (v != v || (int)tab.size() >= kResTab) return;
+        for (float t : tab)
+            if (t == v) return;
+        tab.push_back(v);
     };
-    std::vector<int> pd, pb, pa, sd, sb, sa;
-    order(o->h_dseg, [&](int k) { return d[k].x; }, pd, sd);
-    order(o->h_bseg, [&](int k) { return bi[k].x; }, pb, sb);
-    order(o->h_aseg, [&](int k) { return __float_as_int_host(a[k].w); }, pa, sa);
-    std::vector<int4> d2(nd), b2(nb);
-    std::vector<float2> p2(nb);
-    std::vector<float4> a2(na);
-    for (int k = 0; k < nd; ++k) d2[k] = d[pd[k]];
-    for (int k = 0; k < nb; ++k) {
-        b2[k] = bi[pb[k]];
-        p2[k] = bp[pb[k]];
+    for (int k = 0; k < nd; ++k) {
+        float v;
+        std::memcpy(&v, &d[k].w, sizeof(float));
+        add(v);
     }
-    for (int k = 0; k < na; ++k) a2[k] = a[pa[k]];
-    PBD_TRY(o->cdrec.upload(d2.data(), nd, s));
-    PBD_TRY(o->cbidx.upload(b2.data(), nb, s));
-    PBD_TRY(o->cbpar.upload(p2.data(), nb, s));
-    PBD_TRY(o->carec.upload(a2.data(), na, s));
-    PBD_TRY(o->cdseg.upload(sd.data(), sd.size(), s));
-    PBD_TRY(o->cbseg.upload(sb.data(), sb.size(), s));
-    PBD_TRY(o->caseg.upload(sa.data(), sa.size(), s));
+    for (int k = 0; k < nb; ++k) add(bp[k].y);
+    std::vector<int> seg;
+    seg.insert(seg.end(), o->h_dseg.begin(), o->h_dseg.end());
+    seg.insert(seg.end(), o->h_bseg.begin(), o->h_bseg.end());
+    seg.insert(seg.end(), o->h_aseg.begin(), o->h_aseg.end());
+    PBD_TRY(o->cl_seg.upload(seg.data(), seg.size(), s));
+    PBD_TRY(o->cl_tab.upload(tab.data(), std::max<size_t>(tab.size(), 1), s));
     PBD_CUDA(cudaStreamSynchronize(s));
-    o->cl_S = S;
-    o->cl_shift = shift;
+    o->cl_ntab = (int)tab.size();
     o->cl_state = 1;
     return PBD_OK;
 }
 
-// PBD_GS_AUTO takes the per-color launches: measured on GB300 they are the
-// faster form (a 256x256 cloth: 3.4 us per color phase inside a graph
-// against 8.5 us per phase for the cluster form); the autotuner picks the
-// block size (and the cluster form where it applies) per object.
+// cluster size in use: the one set, else the largest that fits
+static int resident_size(const pbd_object *o) {
+    if (o->cl_S) return (o->cl_fit & o->cl_S) ? o->cl_S : 0;
+    for (int S = 16; S >= 1; S >>= 1)
+        if (o->cl_fit & S) return S;
+    return 0;
+}
+
+template <int S>
+static int launch_resident_s(pbd_solver *s, int it0, int it1, bool ob) {
+    pbd_object *o = s->obj;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(S);
+    cfg.blockDim = dim3(kResThreads);
+    cfg.dynamicSmemBytes = std::max<size_t>(16, sizeof(float4) * (size_t)((o->n + S - 1) / S));
+    cfg.stream = o->stream;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = S;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = S > 1 ? 1 : 0;
+    PBD_CUDA(cudaLaunchKernelEx(
+        &cfg, k_gs_resident<S>, (const int *)o->cl_seg.p, (const int4 *)o->drec.p,
+        (const int4 *)o->bidx.p, (const float2 *)o->bpar.p, (const float4 *)o->arec.p,
+        (const float *)o->cl_tab.p, o->cl_ntab, o->n_colors, o->n, o->p.p, it0, it1,
+        ob ? s->sphere_on : 0, make_float3(s->sphere_c[0], s->sphere_c[1], s->sphere_c[2]),
+        s->sphere_r, ob ? s->ground_on : 0, s->ground_h));
+    return PBD_OK;
+}
+
+static int launch_resident(pbd_solver *s, int it0, int it1, bool ob) {
+    switch (resident_size(s->obj)) {
+        case 1: return launch_resident_s<1>(s, it0, it1, ob);
+        case 2: return launch_resident_s<2>(s, it0, it1, ob);
+        case 4: return launch_resident_s<4>(s, it0, it1, ob);
+        case 8: return launch_resident_s<8>(s, it0, it1, ob);
+        case 16: return launch_resident_s<16>(s, it0, it1, ob);
+    }
+    PBD_CHECK(false, PBD_ERR_STATE, "no cluster size holds this object's points");
+}
+
+// PBD_GS_AUTO takes the per-color launches, which apply to every object; the
+// autotuner picks the block size, or the resident form and its cluster size
+// where that is faster, per object.
 static int resolved_path(pbd_solver *s) {
     if (s->gs_path != PBD_GS_CLUSTER) return PBD_GS_PER_COLOR;
     if (s->n_inst_spheres > 0) return -2;  // per-instance spheres: per-color form only
-    if (cluster_plan(s->obj) != PBD_OK) return -1;
-    return s->obj->cl_state == 1 ? PBD_GS_CLUSTER : -2;
+    if (resident_plan(s->obj) != PBD_OK) return -1;
+    return s->obj->cl_state == 1 && resident_size(s->obj) ? PBD_GS_CLUSTER : -2;
 }
 
 // Everything a launch form needs before a stream capture (plans and
 // uploads); capture forbids allocation and synchronisation.
 int prepare_gs_path(pbd_solver *s) {
     pbd_object *o = s->obj;
-    if (s->gs_path == PBD_GS_CLUSTER) PBD_TRY(cluster_plan(o));
+    if (s->gs_path == PBD_GS_CLUSTER) PBD_TRY(resident_plan(o));
     return PBD_OK;
 }
 
@@ -721,29 +804,8 @@ int launch_sweeps(pbd_solver *s, int it0, int it1, bool obstacles_inside) {
     PBD_CHECK(path != -1, PBD_ERR_CUDA, "launch plan failed: %s", pbd_last_error());
     PBD_CHECK(path != -2, PBD_ERR_STATE,
               "the requested Gauss-Seidel form does not apply to this object (%d points)", o->n);
-    if (path == PBD_GS_CLUSTER) {
-        int ob = obstacles_inside && (s->sphere_on || s->ground_on);
-        cudaLaunchConfig_t cfg = {};
-        cfg.gridDim = dim3(o->cl_S);
-        cfg.blockDim = dim3(kClusterThreads);
-        cfg.dynamicSmemBytes = sizeof(float4) << o->cl_shift;
-        cfg.stream = o->stream;
-        cudaLaunchAttribute at[1];
-        at[0].id = cudaLaunchAttributeClusterDimension;
-        at[0].val.clusterDim.x = o->cl_S;
-        at[0].val.clusterDim.y = 1;
-        at[0].val.clusterDim.z = 1;
-        cfg.attrs = at;
-        cfg.numAttrs = 1;
-        PBD_CUDA(cudaLaunchKernelEx(
-            &cfg, k_gs_cluster, (const int4 *)o->cdrec.p, (const int *)o->cdseg.p,
-            (const int4 *)o->cbidx.p, (const float2 *)o->cbpar.p, (const int *)o->cbseg.p,
-            (const float4 *)o->carec.p, (const int *)o->caseg.p, o->n_colors, o->n, o->cl_shift,
-            o->p.p, it0, it1, ob ? s->sphere_on : 0,
-            make_float3(s->sphere_c[0], s->sphere_c[1], s->sphere_c[2]), s->sphere_r,
-            ob ? s->ground_on : 0, s->ground_h));
-        return PBD_OK;
-    }
+    if (path == PBD_GS_CLUSTER)
+        return launch_resident(s, it0, it1, obstacles_inside && (s->sphere_on || s->ground_on));
     for (int it = it0; it < it1; ++it) {
         PBD_TRY(launch_sweep_per_color(o, it));
         if (obstacles_inside) PBD_TRY(launch_obstacles(s));
@@ -1604,19 +1666,24 @@ int pbd_solver_autotune(pbd_solver *s, int iterations, int reps, pbd_autotune_re
     std::vector<Cand> cands = {{PBD_GS_PER_COLOR, 64}, {PBD_GS_PER_COLOR, 128},
                                {PBD_GS_PER_COLOR, 256}, {PBD_GS_PER_COLOR, 512}};
     if (s->n_inst_spheres == 0) {
-        PBD_TRY(cluster_plan(o));
-        if (o->cl_state == 1) cands.push_back({PBD_GS_CLUSTER, kClusterThreads});
+        PBD_TRY(resident_plan(o));
+        if (o->cl_state == 1)
+            for (int S = 1; S <= 16; S <<= 1)
+                if (o->cl_fit & S) cands.push_back({PBD_GS_CLUSTER, S});
     }
-    const int keep_path = s->gs_path, keep_block = o->gs_block;
+    const int keep_path = s->gs_path, keep_block = o->gs_block, keep_cl = o->cl_S;
     cudaEvent_t e0, e1;
     PBD_CUDA(cudaEventCreate(&e0));
     PBD_CUDA(cudaEventCreate(&e1));
     int best = -1;
     double best_us = 0.0;
     int rc = PBD_OK;
-    for (size_t k = 0; k < cands.size() && k < 8 && rc == PBD_OK; ++k) {
+    for (size_t k = 0; k < cands.size() && k < 12 && rc == PBD_OK; ++k) {
         s->gs_path = cands[k].path;
-        if (cands[k].path != PBD_GS_CLUSTER) o->gs_block = cands[k].block;
+        if (cands[k].path == PBD_GS_CLUSTER)
+            o->cl_S = cands[k].block;
+        else
+            o->gs_block = cands[k].block;
         cudaGraph_t g = nullptr;
         cudaGraphExec_t ge = nullptr;
         rc = prepare_gs_path(s);  // plans outside the capture
@@ -1667,11 +1734,16 @@ int pbd_solver_autotune(pbd_solver *s, int iterations, int reps, pbd_autotune_re
     if (rc != PBD_OK || best < 0) {
         s->gs_path = keep_path;
         o->gs_block = keep_block;
+        o->cl_S = keep_cl;
         set_error("autotune failed: %s", cudaGetErrorString(cudaGetLastError()));
         return rc != PBD_OK ? rc : PBD_ERR_CUDA;
     }
     s->gs_path = res->path[best];
-    if (res->path[best] != PBD_GS_CLUSTER) o->gs_block = res->block[best];
+    if (res->path[best] == PBD_GS_CLUSTER)
+        o->cl_S = res->block[best];
+    else
+        o->gs_block = res->block[best];
+    if (res->path[best] != PBD_GS_CLUSTER) o->cl_S = keep_cl;
     res->best = best;
     PBD_TRY(prepare_gs_path(s));
     if (s->gexec) cudaGraphExecDestroy(s->gexec);
@@ -1697,6 +1769,26 @@ int pbd_solver_set_gs_block(pbd_solver *s, int block) {
 int pbd_solver_get_gs_block(pbd_solver *s, int *block) {
     PBD_CHECK(s && s->obj && block, PBD_ERR_ARG, "null argument");
     *block = s->obj->gs_block;
+    return PBD_OK;
+}
+
+int pbd_solver_set_gs_cluster(pbd_solver *s, int size) {
+    PBD_CHECK(s && s->obj, PBD_ERR_STATE, "solver has no target");
+    PBD_CHECK(size == 0 || size == 1 || size == 2 || size == 4 || size == 8 || size == 16,
+              PBD_ERR_ARG, "cluster size must be 0, 1, 2, 4, 8 or 16, got %d", size);
+    s->obj->cl_S = size;
+    if (s->gexec) cudaGraphExecDestroy(s->gexec);
+    s->gexec = nullptr;
+    if (s->rexec) cudaGraphExecDestroy(s->rexec);
+    s->rexec = nullptr;
+    return PBD_OK;
+}
+
+int pbd_solver_get_gs_cluster(pbd_solver *s, int *size) {
+    PBD_CHECK(s && s->obj && size, PBD_ERR_ARG, "null argument");
+    PBD_CHECK(s->obj->sorted, PBD_ERR_STATE, "constraints are not color-sorted");
+    PBD_TRY(resident_plan(s->obj));
+    *size = s->obj->cl_state == 1 ? resident_size(s->obj) : 0;
     return PBD_OK;
 }
 

@@ -78,7 +78,8 @@ EXPORTS = [
     "pbd_warmstart_record", "pbd_warmstart_train_step", "pbd_warmstart_features",
     "pbd_warmstart_predict", "pbd_solver_set_warmstart", "pbd_solver_project_to_residual",
     "pbd_solver_autotune", "pbd_solver_get_gs_block",
-    "pbd_solver_set_gs_block", "pbd_solver_train_substep"
+    "pbd_solver_set_gs_block", "pbd_solver_train_substep", "pbd_solver_set_gs_cluster",
+    "pbd_solver_get_gs_cluster",
 ]
 
 
@@ -574,6 +575,15 @@ class SolverPBD:
         _check(self.L.pbd_solver_get_gs_block(self.h, C.byref(v)))
         return v.value
 
+    def set_gs_cluster(self, size):
+        """cluster size of the resident form (0: the largest that fits)"""
+        _check(self.L.pbd_solver_set_gs_cluster(self.h, int(size)))
+
+    def gs_cluster(self):
+        v = C.c_int()
+        _check(self.L.pbd_solver_get_gs_cluster(self.h, C.byref(v)))
+        return v.value
+
     def train_substep(self, ws, dt, target=1e-3, max_sweeps=200, chunk=5, lr=1e-3,
                       on_policy=True, colli=None, want_loss=False):
         """one training substep of the warm start (see pbd_solver_train_substep)"""
@@ -603,8 +613,8 @@ class _SolveStats(C.Structure):
 
 
 class _AutotuneResult(C.Structure):
-    _fields_ = [("n", C.c_int), ("best", C.c_int), ("path", C.c_int * 8), ("block", C.c_int * 8),
-                ("us_per_sweep", C.c_double * 8)]
+    _fields_ = [("n", C.c_int), ("best", C.c_int), ("path", C.c_int * 12),
+                ("block", C.c_int * 12), ("us_per_sweep", C.c_double * 12)]
 
 
 class WarmStart:
