@@ -87,6 +87,41 @@ int pbd_object_create(const pbd_object_desc *desc, pbd_object **out);
 int pbd_object_create_grid(float damping, const float *gravity, int res_x, int res_y,
                            float size_x, float size_y, unsigned ct_mask,
                            const float *stiffness, pbd_object **out);
+/* A triangle mesh whose constraints are derived on the device (no reference
+ * counterpart: the reference builds its grid stencil on the host,
+ * P/PBD_cuda.cu:19-123, or reads Houdini caches). */
+typedef struct pbd_mesh_desc {
+    int n_points;
+    const float *pos;             /* 3*n_points                                  */
+    const float *vel;             /* 3*n_points (NULL = zero)                    */
+    const float *mass;            /* massBuffer, n_points                        */
+    const float *rest_pos;        /* rest shape, 3*n_points (NULL = pos)         */
+    int n_tris;
+    const int *tri_idx;           /* 3*n_tris                                    */
+    unsigned ct_mask;             /* PBD_DISTANCE and/or PBD_BENDING             */
+    float stiffness[2];           /* {distance, bending}                         */
+    const int *point_inst;        /* instance id per point (NULL = one cloth)    */
+    const int *tri_inst;          /* instance id per triangle (NULL)             */
+    float damping_rate;
+    float gravity[3];
+} pbd_mesh_desc;
+/* Constraint set of a triangle mesh, derived on the device: a distance
+ * constraint on every edge (rest length |p_a - p_b| in float32 from
+ * rest_pos) and a dihedral bending constraint (e0, e1, wA, wB) on every edge
+ * shared by exactly two triangles (rest angle: the signed dihedral angle of
+ * rest_pos in float64, stored as float32).  Edges (a < b) and hinges come
+ * out in the order of the key a * n_points + b; a hinge's wA / wB are the
+ * vertices opposite the edge in the first / second of its triangles in
+ * (slot, triangle) order, e0 -> e1 following wing A's triangle.  With all
+ * output pointers NULL only the counts are written; otherwise every
+ * non-NULL output gets its values (edges 2 ints, hinges 4 ints each) and
+ * both counts must be <= capacity. */
+int pbd_mesh_constraints(int n_points, const float *rest_pos, int n_tris, const int *tri_idx,
+                         long long capacity, int *n_edges, int *n_hinges, int *edges,
+                         float *edge_rest, int *hinges, float *hinge_angle);
+/* pbd_mesh_constraints + pbd_object_create: distance prims first (edge
+ * order), then bending prims (hinge order), stiffness per type. */
+int pbd_object_create_mesh(const pbd_mesh_desc *desc, pbd_object **out);
 /* ~PBDObject / freeGPUBuffers (P/PBD_cuda.cu:752-794) */
 int pbd_object_destroy(pbd_object *obj);
 int pbd_object_sizes(const pbd_object *obj, int *n_points, int *n_tris, int *n_prims);

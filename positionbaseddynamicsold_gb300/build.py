@@ -23,6 +23,7 @@ SOURCES = {
     "pbd_sort.cu": [],
     "pbd_object.cu": ["-fmad=false"],
     "pbd_collision.cu": ["-fmad=false"],
+    "pbd_mesh.cu": ["-fmad=false"],
     "pbd_noalloc.cu": [],
     "pbd_mlp.cu": [],
     "pbd_solve.cu": [],

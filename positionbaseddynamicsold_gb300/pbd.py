@@ -30,6 +30,14 @@ class PBDError(RuntimeError):
         self.code = code
 
 
+class _MeshDesc(C.Structure):
+    _fields_ = [("n_points", C.c_int), ("pos", C.c_void_p), ("vel", C.c_void_p),
+                ("mass", C.c_void_p), ("rest_pos", C.c_void_p), ("n_tris", C.c_int),
+                ("tri_idx", C.c_void_p), ("ct_mask", C.c_uint), ("stiffness", C.c_float * 2),
+                ("point_inst", C.c_void_p), ("tri_inst", C.c_void_p),
+                ("damping_rate", C.c_float), ("gravity", C.c_float * 3)]
+
+
 class _Desc(C.Structure):
     _fields_ = [("n_points", C.c_int), ("pos", C.c_void_p), ("vel", C.c_void_p),
                 ("mass", C.c_void_p), ("n_tris", C.c_int), ("tri_idx", C.c_void_p),
@@ -79,7 +87,7 @@ EXPORTS = [
     "pbd_warmstart_predict", "pbd_solver_set_warmstart", "pbd_solver_project_to_residual",
     "pbd_solver_autotune", "pbd_solver_get_gs_block",
     "pbd_solver_set_gs_block", "pbd_solver_train_substep", "pbd_solver_set_gs_cluster",
-    "pbd_solver_get_gs_cluster",
+    "pbd_solver_get_gs_cluster", "pbd_mesh_constraints", "pbd_object_create_mesh",
 ]
 
 
@@ -133,6 +141,9 @@ def load(build_if_missing: bool = True) -> C.CDLL:
     L.pbd_scene_write_cache.argtypes = [C.c_void_p, C.c_void_p, C.c_char_p, C.c_char_p]
     L.pbd_object_create_from_cache.argtypes = [C.c_char_p, C.c_char_p, C.c_void_p]
     L.pbd_object_save_cache.argtypes = [C.c_void_p, C.c_char_p, C.c_char_p]
+    L.pbd_mesh_constraints.argtypes = [C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_longlong,
+                                       C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                       C.c_void_p, C.c_void_p]
     L.pbd_warmstart_adam.argtypes = [C.c_void_p, C.c_float, C.c_float, C.c_float, C.c_float]
     L.pbd_warmstart_train_step.argtypes = [C.c_void_p, C.c_void_p, C.c_float, C.c_void_p]
     _LIB = L
@@ -206,6 +217,42 @@ class PBDObject:
         for i in range(3):
             d.gravity[i] = gravity[i]
         _check(self.L.pbd_object_create(C.byref(d), C.byref(self.h)))
+
+    @classmethod
+    def from_mesh(cls, pos, tris, mass, vel=None, rest_pos=None, stiffness=(1.0, 0.1),
+                  bending=True, point_inst=None, tri_inst=None, damping=1.0,
+                  gravity=(0.0, -9.8, 0.0)):
+        """an object whose constraints the device derives from the triangle
+        mesh (pbd_object_create_mesh): distance on every edge, bending on
+        every interior edge"""
+        L = load()
+        keep = []
+
+        def k(a):
+            keep.append(a)
+            return _p(a)
+
+        d = _MeshDesc()
+        p = _f32(pos).reshape(-1)
+        t = _i32(tris).reshape(-1)
+        d.n_points = len(p) // 3
+        d.pos = k(p)
+        d.vel = k(_f32(vel).reshape(-1)) if vel is not None else None
+        d.mass = k(_f32(mass))
+        d.rest_pos = k(_f32(rest_pos).reshape(-1)) if rest_pos is not None else None
+        d.n_tris = len(t) // 3
+        d.tri_idx = k(t)
+        d.ct_mask = DISTANCE | (BENDING if bending else 0)
+        d.stiffness[0], d.stiffness[1] = float(stiffness[0]), float(stiffness[1])
+        if point_inst is not None:
+            d.point_inst = k(_i32(point_inst))
+            d.tri_inst = k(_i32(tri_inst))
+        d.damping_rate = damping
+        for i in range(3):
+            d.gravity[i] = gravity[i]
+        h = C.c_void_p()
+        _check(L.pbd_object_create_mesh(C.byref(d), C.byref(h)))
+        return cls(_handle=h)
 
     @classmethod
     def from_cache(cls, topol_path, constr_path):
@@ -342,6 +389,45 @@ class PBDObject:
         self.sort_edges_colors()
         self.eval_worksets()
         return sw
+
+
+def mesh_constraints(rest_pos, tris, dist_stiffness=1.0, bend_stiffness=0.1, bending=True):
+    """The constraint set of a triangle mesh derived on the device
+    (pbd_mesh_constraints), in the layout of scenes.constraints_from_mesh:
+    distance prims on the edges, then bending prims on the interior edges."""
+    L = load()
+    rp = _f32(rest_pos).reshape(-1)
+    t = _i32(tris).reshape(-1)
+    n, nt = len(rp) // 3, len(t) // 3
+    ne, nh = C.c_int(), C.c_int()
+    _check(L.pbd_mesh_constraints(n, _p(rp), nt, _p(t), 0, C.byref(ne), C.byref(nh),
+                                  None, None, None, None))
+    cap = max(ne.value, nh.value, 1)
+    e = np.zeros((cap, 2), np.int32)
+    el = np.zeros(cap, np.float32)
+    h = np.zeros((cap, 4), np.int32)
+    ha = np.zeros(cap, np.float32)
+    _check(L.pbd_mesh_constraints(n, _p(rp), nt, _p(t), cap, C.byref(ne), C.byref(nh),
+                                  _p(e), _p(el), _p(h), _p(ha)))
+    nd, nb = ne.value, (nh.value if bending else 0)
+    e, el, h, ha = e[:nd], el[:nd], h[:nb], ha[:nb]
+    prim_list = np.concatenate([
+        np.stack([np.arange(nd) * 2, np.full(nd, 2)], 1),
+        np.stack([2 * nd + np.arange(nb) * 4, np.full(nb, 4)], 1)], 0).astype(np.int32)
+    rest_length = np.zeros(nd + nb, np.float32)
+    rest_length[:nd] = el
+    rest_angle = np.zeros(nd + nb, np.float32)
+    rest_angle[nd:] = ha
+    return {
+        "prim_list": prim_list,
+        "indices": np.concatenate([e.ravel(), h.ravel()]).astype(np.int32),
+        "ctype": np.concatenate([np.full(nd, DISTANCE), np.full(nb, BENDING)]).astype(np.int32),
+        "rest_length": rest_length,
+        "stiffness": np.concatenate([np.full(nd, dist_stiffness),
+                                     np.full(nb, bend_stiffness)]).astype(np.float32),
+        "rest_angle": rest_angle, "rest_pos": np.zeros((nd + nb, 3), np.float32),
+        "n_distance": nd, "n_bending": nb,
+    }
 
 
 class SpatialHashSystem:
