@@ -136,6 +136,26 @@ int pbd_object_get_predicted(pbd_object *obj, float *prdp3);
 int pbd_object_set_positions(pbd_object *obj, const float *pos3);
 int pbd_object_set_velocities(pbd_object *obj, const float *vel3);
 int pbd_object_set_predicted(pbd_object *obj, const float *prdp3);
+
+/* Stiffness schedule: the factor k a projection applies for stiffness s in
+ * sweep iter (0-based) of a projection call.  PBD_SCHEDULE_REFERENCE (the
+ * default): k = 1 - (1 - s)^(1/(iter+1)), ProjectContraintsGPUKernel
+ * (P/PBD_cuda.cu:1282); PBD_SCHEDULE_UNIT: k = 1, projectConstraintCPU
+ * (P/PBD_cuda.cu:1119); PBD_SCHEDULE_DIRECT: k = s.  Solver graphs are
+ * recaptured when it changes. */
+enum { PBD_SCHEDULE_REFERENCE = 0, PBD_SCHEDULE_UNIT = 1, PBD_SCHEDULE_DIRECT = 2 };
+int pbd_object_set_stiffness_schedule(pbd_object *obj, int schedule);
+int pbd_object_get_stiffness_schedule(pbd_object *obj, int *schedule);
+/* stiffnessBuffer of every prim whose constraintType is in ct_mask set to
+ * value (PBDObject::SetConstrOption's per-type stiffness, P/PBD_cuda.cu:
+ * 669-673, changed after Init); stream-ordered. */
+int pbd_object_set_stiffness(pbd_object *obj, unsigned ct_mask, float value);
+/* Attachments: the rest positions of the ANCHOR prims `prims` (the points
+ * InitAnchorConstr pins, P/PBD_cuda.cu:125-153, snapped to by the ANCHOR
+ * branch, :1298-1305) moved to targets (3 floats each), e.g. every substep
+ * for an animated attachment; stream-ordered, the caller's arrays are read
+ * before the call returns. */
+int pbd_object_set_anchor_targets(pbd_object *obj, int n, const int *prims, const float *targets);
 /* the object's CUDA stream (cudaStream_t) */
 int pbd_object_stream(pbd_object *obj, void **stream);
 int pbd_object_sync(pbd_object *obj);

@@ -130,6 +130,10 @@ class Oracle:
         return c, sid, ws[:nw].copy()
 
     # -- solver ----------------------------------------------------------
+    def set_stiffness_schedule(self, mode):
+        """0: k = 1-(1-s)^(1/(iter+1)); 1: k = 1; 2: k = s (process-wide)"""
+        self.lib.orc_set_stiffness_schedule(int(mode))
+
     def substep_gpu(self, scene, state, sorted_prim_id, worksets, iterations, dt, damping,
                     gravity, bending_fp64=False, colli=None):
         """state: dict pos, vel (float32 (N,3)); modified in place."""

@@ -308,10 +308,21 @@ void orc_integrate(int n, float dt, float *vel, const float *prdp, float *pos)
     }
 }
 
-/* k = 1 - (1-s)^(1/(iter+1)) (P/PBD_cuda.cu:1282); the exponent is computed
- * in double and narrowed to float by powf's parameter. */
+/* Stiffness schedule (orc_set_stiffness_schedule): 0 = k = 1 - (1-s)^(1/(iter+1))
+ * (P/PBD_cuda.cu:1282; the exponent is computed in double and narrowed to
+ * float by powf's parameter), 1 = k = 1 (projectConstraintCPU,
+ * P/PBD_cuda.cu:1119), 2 = k = s. */
+static int g_schedule = 0;
+
+void orc_set_stiffness_schedule(int mode)
+{
+    g_schedule = mode;
+}
+
 static inline float stiff_k(float s, int iter)
 {
+    if (g_schedule == 1) return 1.0f;
+    if (g_schedule == 2) return s;
     return 1.0f - powf(1.0f - s, (float)(1.0 / (double)(iter + 1)));
 }
 

@@ -125,8 +125,13 @@ void orc_project_colored(const orc_constraints *c, const int *sorted_prim_id,
                          int iter_end, const float *mass, float *prdp,
                          int bending_fp64);
 
+/* Stiffness schedule of the colored GS: 0 = k = 1 - (1-s)^(1/(iter+1))
+ * (P/PBD_cuda.cu:1282, the default), 1 = k = 1 (P/PBD_cuda.cu:1119),
+ * 2 = k = s.  Process-wide. */
+void orc_set_stiffness_schedule(int mode);
+
 /* One constraint of the colored GS, iteration `iter` (stiffness schedule
- * k = 1 - (1-s)^(1/(iter+1)), P/PBD_cuda.cu:1282). */
+ * above). */
 void orc_project_one(const orc_constraints *c, int prim, int iter,
                      const float *mass, float *prdp, int bending_fp64);
 

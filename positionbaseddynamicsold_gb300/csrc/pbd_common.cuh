@@ -179,6 +179,13 @@ struct pbd_object {
     pbd::DBuf<float2> bpar;                     // rest angle, stiffness
     pbd::DBuf<float4> arec;                     // rest xyz, point id bits
     std::vector<int> h_dseg, h_bseg, h_aseg;    // n_colors+1 starts each
+    pbd::DBuf<int> rec_prim;                    // prim of every record, record order
+    int n_rec[3] = {0, 0, 0};                   // distance, bending, anchor records
+    // stiffness schedule of the projections (PBD_SCHEDULE_*)
+    int sched = 0;
+    // staging of pbd_object_set_anchor_targets
+    pbd::DBuf<int> anc_prim;
+    pbd::DBuf<float> anc_t;
     // resident (cluster) form of the sweep: per-color record starts
     // (dseg | bseg | aseg), the distinct stiffness values of the records (at
     // most 8), the cluster sizes whose shared memory holds every point (bit

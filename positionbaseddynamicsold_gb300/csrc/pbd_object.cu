@@ -209,12 +209,14 @@ __global__ void k_class_keys(int np, const int *color, const int *ctype, int nc,
     val[i] = i;
 }
 
-__global__ void k_build_records(int n_rec, const int *sprim, const int2 *prim_list,
+// records i0 .. n_rec-1 from the per-prim buffers (sprim = the prim of each
+// record, in record order)
+__global__ void k_build_records(int i0, int n_rec, const int *sprim, const int2 *prim_list,
                                 const int *indices, const float *rest_length,
                                 const float *stiffness, const float *rest_angle,
                                 const float4 *rest_pos, int nd, int nb, int na, int4 *drec,
                                 int4 *bidx, float2 *bpar, float4 *arec) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    int i = i0 + blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n_rec) return;
     int p = sprim[i];
     int s = prim_list[p].x;
@@ -230,6 +232,18 @@ __global__ void k_build_records(int n_rec, const int *sprim, const int2 *prim_li
         float4 r = rest_pos ? rest_pos[p] : make_float4(0.f, 0.f, 0.f, 0.f);
         arec[j] = make_float4(r.x, r.y, r.z, __int_as_float(indices[s]));
     }
+}
+
+__global__ void k_set_type_stiffness(int np, const int *__restrict__ ctype, unsigned mask,
+                                     float v, float *stiffness) {
+    int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p < np && ((unsigned)ctype[p] & mask)) stiffness[p] = v;
+}
+
+__global__ void k_set_rest_pos(int n, const int *__restrict__ prims, const float *__restrict__ t3,
+                               float4 *rest_pos) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) rest_pos[prims[i]] = make_float4(t3[3 * i], t3[3 * i + 1], t3[3 * i + 2], 0.f);
 }
 
 // ---------------------------------------------------------------------------
@@ -279,7 +293,8 @@ __global__ void __launch_bounds__(512) k_project_color(const int4 *__restrict__ 
                                                        const float2 *__restrict__ bpar, int nb,
                                                        const float4 *__restrict__ arec, int na,
                                                        float4 *__restrict__ p, float expk,
-                                                       const float *__restrict__ expk_dev) {
+                                                       const float *__restrict__ expk_dev,
+                                                       int sched) {
     int t = blockIdx.x * blockDim.x + threadIdx.x;
     int4 r = make_int4(0, 0, 0, 0);
     float2 bp = make_float2(0.f, 0.f);
@@ -302,9 +317,9 @@ __global__ void __launch_bounds__(512) k_project_color(const int4 *__restrict__ 
     if (expk_dev) expk = *expk_dev;
     GlobalPos P{p};
     if (kind == 1)
-        project_distance(r, P, expk);
+        project_distance(r, P, expk, sched);
     else if (kind == 2)
-        project_bending(r, bp, P, expk);
+        project_bending(r, bp, P, expk, sched);
     else if (kind == 3)
         project_anchor(ar, P);
 }
@@ -375,26 +390,28 @@ struct ResRec {
 };
 
 // the object's factor for stiffness s (table hit) or s's own
-__device__ __forceinline__ float res_factor(float s, float expk, const float *ts, const float *tk,
-                                            int ntab) {
+__device__ __forceinline__ float res_factor(float s, float expk, int sched, const float *ts,
+                                            const float *tk, int ntab) {
     for (int j = 0; j < ntab; ++j)
         if (ts[j] == s) return tk[j];
-    return stiffness_factor(s, expk);
+    return stiffness_factor(s, expk, sched);
 }
 
 template <int S>
 __device__ __forceinline__ void res_project(const ResRec &A, const ResPos<S> &P, float expk,
-                                            const float *ts, const float *tk, int ntab) {
+                                            int sched, const float *ts, const float *tk,
+                                            int ntab) {
     if (A.kind == 1) {
         float4 N0, N1;
         if (distance_update(P.ld(A.r.x), P.ld(A.r.y), __int_as_float(A.r.z),
-                            res_factor(__int_as_float(A.r.w), expk, ts, tk, ntab), N0, N1)) {
+                            res_factor(__int_as_float(A.r.w), expk, sched, ts, tk, ntab), N0,
+                            N1)) {
             P.st(A.r.x, N0);
             P.st(A.r.y, N1);
         }
     } else if (A.kind == 2) {
         float4 Q[4] = {P.ld(A.r.x), P.ld(A.r.y), P.ld(A.r.z), P.ld(A.r.w)}, N[4];
-        if (bending_update(Q, A.f.x, res_factor(A.f.y, expk, ts, tk, ntab), N)) {
+        if (bending_update(Q, A.f.x, res_factor(A.f.y, expk, sched, ts, tk, ntab), N)) {
             P.st(A.r.x, N[0]);
             P.st(A.r.y, N[1]);
             P.st(A.r.z, N[2]);
@@ -414,7 +431,7 @@ __global__ void __launch_bounds__(kResThreads, 1) k_gs_resident(
     const int *__restrict__ seg, const int4 *__restrict__ drec, const int4 *__restrict__ bidx,
     const float2 *__restrict__ bpar, const float4 *__restrict__ arec,
     const float *__restrict__ tab, int ntab, int n_colors, int n, float4 *__restrict__ p,
-    int it0, int it1, int sphere_on, float3 sc, float sr, int ground_on, float gh) {
+    int it0, int it1, int sched, int sphere_on, float3 sc, float sr, int ground_on, float gh) {
     extern __shared__ float4 sp[];
     __shared__ int sg[3 * (kResMaxColors + 1)];
     __shared__ float tab_s[kResTab], tab_k[kResTab];
@@ -464,13 +481,13 @@ __global__ void __launch_bounds__(kResThreads, 1) k_gs_resident(
     res_sync<S>();  // every block's points are in place before any remote access
     for (int it = it0; it < it1; ++it) {
         const float expk = (float)(1.0 / (double)(it + 1));
-        if (tid < ntab) tab_k[tid] = stiffness_factor(tab_s[tid], expk);
+        if (tid < ntab) tab_k[tid] = stiffness_factor(tab_s[tid], expk, sched);
         __syncthreads();
         for (int c = 0; c < n_colors; ++c) {
             share(c, lo, hi, dn, bn);
-            res_project<S>(A, P, expk, tab_s, tab_k, ntab);
+            res_project<S>(A, P, expk, sched, tab_s, tab_k, ntab);
             for (int f = lo + tid + kResThreads; f < hi; f += kResThreads)
-                res_project<S>(fetch(c, f, hi, dn, bn), P, expk, tab_s, tab_k, ntab);
+                res_project<S>(fetch(c, f, hi, dn, bn), P, expk, sched, tab_s, tab_k, ntab);
             // the next phase's first record, before the barrier
             const int cn = c + 1 < n_colors ? c + 1 : 0;
             int lo2, hi2, dn2, bn2;
@@ -632,7 +649,7 @@ static int launch_sweep_per_color(pbd_object *o, int iter, const float *expk_dev
         PBD_CUDA(cudaLaunchKernelEx(&cfg, k_project_color, (const int4 *)(o->drec.p + d0), nd,
                                     (const int4 *)(o->bidx.p + b0), (const float2 *)(o->bpar.p + b0),
                                     nb, (const float4 *)(o->arec.p + a0), na, o->p.p, expk,
-                                    expk_dev));
+                                    expk_dev, o->sched));
     }
     return PBD_OK;
 }
@@ -723,7 +740,9 @@ static int resident_plan(pbd_object *o) {
     seg.insert(seg.end(), o->h_bseg.begin(), o->h_bseg.end());
     seg.insert(seg.end(), o->h_aseg.begin(), o->h_aseg.end());
     PBD_TRY(o->cl_seg.upload(seg.data(), seg.size(), s));
-    PBD_TRY(o->cl_tab.upload(tab.data(), std::max<size_t>(tab.size(), 1), s));
+    // full capacity once: graphs captured earlier keep the table's address
+    PBD_TRY(o->cl_tab.alloc(kResTab));
+    if (!tab.empty()) PBD_TRY(o->cl_tab.upload(tab.data(), tab.size(), s));
     PBD_CUDA(cudaStreamSynchronize(s));
     o->cl_ntab = (int)tab.size();
     o->cl_state = 1;
@@ -756,7 +775,7 @@ static int launch_resident_s(pbd_solver *s, int it0, int it1, bool ob) {
     PBD_CUDA(cudaLaunchKernelEx(
         &cfg, k_gs_resident<S>, (const int *)o->cl_seg.p, (const int4 *)o->drec.p,
         (const int4 *)o->bidx.p, (const float2 *)o->bpar.p, (const float4 *)o->arec.p,
-        (const float *)o->cl_tab.p, o->cl_ntab, o->n_colors, o->n, o->p.p, it0, it1,
+        (const float *)o->cl_tab.p, o->cl_ntab, o->n_colors, o->n, o->p.p, it0, it1, o->sched,
         ob ? s->sphere_on : 0, make_float3(s->sphere_c[0], s->sphere_c[1], s->sphere_c[2]),
         s->sphere_r, ob ? s->ground_on : 0, s->ground_h));
     return PBD_OK;
@@ -1251,6 +1270,64 @@ int pbd_object_set_positions(pbd_object *o, const float *v) { return copy_in3(o,
 int pbd_object_set_velocities(pbd_object *o, const float *v) { return copy_in3(o, o ? o->v.p : nullptr, v, false); }
 int pbd_object_set_predicted(pbd_object *o, const float *v) { return copy_in3(o, o ? o->p.p : nullptr, v, true); }
 
+// records i0.. from the per-prim buffers, after a per-prim change
+static int rebuild_records(pbd_object *o, int i0) {
+    const int n_rec = o->n_rec[0] + o->n_rec[1] + o->n_rec[2];
+    if (!o->sorted || i0 >= n_rec) return PBD_OK;
+    k_build_records<<<grid_for(n_rec - i0, 256), 256, 0, o->stream>>>(
+        i0, n_rec, o->rec_prim.p, o->prim_list.p, o->indices.p, o->rest_length.p,
+        o->stiffness.p, o->rest_angle.p, o->rest_pos.p, o->n_rec[0], o->n_rec[1], o->n_rec[2],
+        o->drec.p, o->bidx.p, o->bpar.p, o->arec.p);
+    PBD_LAUNCH();
+    return PBD_OK;
+}
+
+int pbd_object_set_stiffness_schedule(pbd_object *o, int schedule) {
+    PBD_CHECK(o, PBD_ERR_ARG, "null object");
+    PBD_CHECK(schedule >= PBD_SCHEDULE_REFERENCE && schedule <= PBD_SCHEDULE_DIRECT, PBD_ERR_ARG,
+              "unknown stiffness schedule %d", schedule);
+    o->sched = schedule;
+    return PBD_OK;
+}
+
+int pbd_object_get_stiffness_schedule(pbd_object *o, int *schedule) {
+    PBD_CHECK(o && schedule, PBD_ERR_ARG, "null argument");
+    *schedule = o->sched;
+    return PBD_OK;
+}
+
+int pbd_object_set_stiffness(pbd_object *o, unsigned ct_mask, float value) {
+    PBD_CHECK(o, PBD_ERR_ARG, "null object");
+    PBD_CHECK(value == value, PBD_ERR_ARG, "stiffness is NaN");
+    if (!o->np || !ct_mask) return PBD_OK;
+    k_set_type_stiffness<<<grid_for(o->np, 256), 256, 0, o->stream>>>(o->np, o->ctype.p, ct_mask,
+                                                                       value, o->stiffness.p);
+    PBD_LAUNCH();
+    PBD_TRY(rebuild_records(o, 0));
+    o->cl_state = 0;  // the resident form's table of distinct values
+    return PBD_OK;
+}
+
+int pbd_object_set_anchor_targets(pbd_object *o, int n, const int *prims, const float *targets) {
+    PBD_CHECK(o && n >= 0 && (n == 0 || (prims && targets)), PBD_ERR_ARG, "bad argument");
+    for (int i = 0; i < n; ++i) {
+        PBD_CHECK(prims[i] >= 0 && prims[i] < o->np, PBD_ERR_ARG, "prim %d out of range", prims[i]);
+        PBD_CHECK(o->h_ctype[prims[i]] == PBD_ANCHOR, PBD_ERR_ARG, "prim %d is not an ANCHOR",
+                  prims[i]);
+        PBD_CHECK(targets[3 * i] == targets[3 * i] && targets[3 * i + 1] == targets[3 * i + 1] &&
+                      targets[3 * i + 2] == targets[3 * i + 2],
+                  PBD_ERR_ARG, "target %d is NaN", i);
+    }
+    if (!n) return PBD_OK;
+    // both uploads read the caller's arrays before returning
+    PBD_TRY(o->anc_prim.upload(prims, n, o->stream));
+    PBD_TRY(o->anc_t.upload(targets, 3 * (size_t)n, o->stream));
+    k_set_rest_pos<<<grid_for(n, 256), 256, 0, o->stream>>>(n, o->anc_prim.p, o->anc_t.p,
+                                                             o->rest_pos.p);
+    PBD_LAUNCH();
+    return rebuild_records(o, o->n_rec[0] + o->n_rec[1]);
+}
+
 int pbd_object_stream(pbd_object *o, void **s) {
     PBD_CHECK(o && s, PBD_ERR_ARG, "null argument");
     *s = (void *)o->stream;
@@ -1394,10 +1471,19 @@ int pbd_constraints_sort_edges_colors(pbd_object *o) {
         PBD_CUDA(cudaMemcpyAsync(o->bend_prim.p, sv + nrec[0], sizeof(int) * nrec[1],
                                  cudaMemcpyDeviceToDevice, s));
     o->feat_built = false;
+    // the prim of every record, for rebuilding records after the per-prim
+    // stiffness or anchor targets change
+    const int n_rec = nrec[0] + nrec[1] + nrec[2];
+    PBD_TRY(o->rec_prim.alloc(std::max(n_rec, 1)));
+    if (n_rec)
+        PBD_CUDA(cudaMemcpyAsync(o->rec_prim.p, sv, sizeof(int) * n_rec, cudaMemcpyDeviceToDevice, s));
+    o->n_rec[0] = nrec[0];
+    o->n_rec[1] = nrec[1];
+    o->n_rec[2] = nrec[2];
     k_build_records<<<grid_for(np, 256), 256, 0, s>>>(
-        nrec[0] + nrec[1] + nrec[2], sv, o->prim_list.p, o->indices.p, o->rest_length.p,
-        o->stiffness.p, o->rest_angle.p, o->rest_pos.p, nrec[0], nrec[1], nrec[2], o->drec.p,
-        o->bidx.p, o->bpar.p, o->arec.p);
+        0, n_rec, sv, o->prim_list.p, o->indices.p, o->rest_length.p, o->stiffness.p,
+        o->rest_angle.p, o->rest_pos.p, nrec[0], nrec[1], nrec[2], o->drec.p, o->bidx.p,
+        o->bpar.p, o->arec.p);
     PBD_LAUNCH();
     PBD_CUDA(cudaStreamSynchronize(s));
     // worksets over the color-sorted prim list
@@ -1574,7 +1660,7 @@ int pbd_solver_step(pbd_solver *s, float dt, int substeps, int iterations, pbd_c
     if (!use_graph) return record_steps(s, dt, substeps, iterations, c);
     int sig = s->sphere_on * 3 + s->ground_on * 7 + (c ? c->response * 11 + c->iterations * 13 : 0) +
               (s->n_inst_spheres > 0) * 17 +
-              s->gs_path * 1009;
+              s->gs_path * 1009 + s->obj->sched * 7919;
     if (s->gexec && (s->g_dt != dt || s->g_sub != substeps || s->g_it != iterations ||
                      s->g_colli != c || s->g_sig != sig)) {
         cudaGraphExecDestroy(s->gexec);

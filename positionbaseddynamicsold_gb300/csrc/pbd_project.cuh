@@ -23,8 +23,14 @@ struct GlobalPos {
     __device__ __forceinline__ void st(int i, float4 v) const { p[i] = v; }
 };
 
-// stiffness factor of ProjectContraintsGPUKernel (P/PBD_cuda.cu:1282)
-__device__ __forceinline__ float stiffness_factor(float s, float expk) {
+// Stiffness factor k of a constraint with stiffness s in the sweep whose
+// exponent is expk = 1/(iter+1), by schedule (PBD_SCHEDULE_*):
+//   0  1 - (1 - s)^expk   ProjectContraintsGPUKernel (P/PBD_cuda.cu:1282)
+//   1  1                  projectConstraintCPU (P/PBD_cuda.cu:1119, k = 1)
+//   2  s                  the stiffness itself, every sweep
+__device__ __forceinline__ float stiffness_factor(float s, float expk, int sched) {
+    if (sched == 1) return 1.f;
+    if (sched == 2) return s;
     return 1.f - powf(1.f - s, expk);
 }
 
@@ -47,9 +53,9 @@ __device__ __forceinline__ bool distance_update(float4 P0, float4 P1, float rest
 }
 
 template <class Pos>
-__device__ __forceinline__ void project_distance(int4 r, const Pos &p, float expk) {
+__device__ __forceinline__ void project_distance(int4 r, const Pos &p, float expk, int sched) {
     float4 P0 = p.ld(r.x), P1 = p.ld(r.y), N0, N1;
-    float k = stiffness_factor(__int_as_float(r.w), expk);
+    float k = stiffness_factor(__int_as_float(r.w), expk, sched);
     if (!distance_update(P0, P1, __int_as_float(r.z), k, N0, N1)) return;
     p.st(r.x, N0);
     p.st(r.y, N1);
@@ -109,9 +115,10 @@ __device__ __forceinline__ bool bending_update(const float4 Q[4], float theta0, 
 }
 
 template <class Pos>
-__device__ __forceinline__ void project_bending(int4 r, float2 par, const Pos &p, float expk) {
+__device__ __forceinline__ void project_bending(int4 r, float2 par, const Pos &p, float expk,
+                                                int sched) {
     float4 Q[4] = {p.ld(r.x), p.ld(r.y), p.ld(r.z), p.ld(r.w)}, N[4];
-    if (!bending_update(Q, par.x, stiffness_factor(par.y, expk), N)) return;
+    if (!bending_update(Q, par.x, stiffness_factor(par.y, expk, sched), N)) return;
     p.st(r.x, N[0]);
     p.st(r.y, N[1]);
     p.st(r.z, N[2]);

@@ -21,6 +21,7 @@ DISTANCE, BENDING, ANCHOR = 0x001, 0x010, 0x100
 JACOBI, GAUSSSEIDEL = 0, 1
 RESPONSE_REFERENCE, RESPONSE_MASS_WEIGHTED = 0, 1
 GS_AUTO, GS_PER_COLOR, GS_CLUSTER = 0, 1, 2
+SCHEDULE_REFERENCE, SCHEDULE_UNIT, SCHEDULE_DIRECT = 0, 1, 2
 _ERRS = {1: "ARG", 2: "OOM", 3: "CUDA", 4: "TIMEOUT", 5: "OVERFLOW", 6: "STATE"}
 
 
@@ -88,6 +89,8 @@ EXPORTS = [
     "pbd_solver_autotune", "pbd_solver_get_gs_block",
     "pbd_solver_set_gs_block", "pbd_solver_train_substep", "pbd_solver_set_gs_cluster",
     "pbd_solver_get_gs_cluster", "pbd_mesh_constraints", "pbd_object_create_mesh",
+    "pbd_object_set_stiffness_schedule", "pbd_object_get_stiffness_schedule",
+    "pbd_object_set_stiffness", "pbd_object_set_anchor_targets",
 ]
 
 
@@ -144,6 +147,7 @@ def load(build_if_missing: bool = True) -> C.CDLL:
     L.pbd_mesh_constraints.argtypes = [C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_longlong,
                                        C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                        C.c_void_p, C.c_void_p]
+    L.pbd_object_set_stiffness.argtypes = [C.c_void_p, C.c_uint, C.c_float]
     L.pbd_warmstart_adam.argtypes = [C.c_void_p, C.c_float, C.c_float, C.c_float, C.c_float]
     L.pbd_warmstart_train_step.argtypes = [C.c_void_p, C.c_void_p, C.c_float, C.c_void_p]
     _LIB = L
@@ -261,6 +265,27 @@ class PBDObject:
         h = C.c_void_p()
         _check(L.pbd_object_create_from_cache(_enc(topol_path), _enc(constr_path), C.byref(h)))
         return cls(_handle=h)
+
+    def set_stiffness_schedule(self, mode):
+        """SCHEDULE_REFERENCE (k = 1-(1-s)^(1/(iter+1))), SCHEDULE_UNIT (k = 1)
+        or SCHEDULE_DIRECT (k = s)"""
+        _check(self.L.pbd_object_set_stiffness_schedule(self.h, int(mode)))
+
+    def stiffness_schedule(self):
+        v = C.c_int()
+        _check(self.L.pbd_object_get_stiffness_schedule(self.h, C.byref(v)))
+        return v.value
+
+    def set_stiffness(self, ct_mask, value):
+        """stiffness of every constraint of the types in ct_mask"""
+        _check(self.L.pbd_object_set_stiffness(self.h, int(ct_mask), float(value)))
+
+    def set_anchor_targets(self, prims, targets):
+        """move the rest positions (targets, (n, 3)) of the ANCHOR prims"""
+        p = _i32(prims).reshape(-1)
+        t = _f32(targets).reshape(-1)
+        assert len(t) == 3 * len(p)
+        _check(self.L.pbd_object_set_anchor_targets(self.h, len(p), _p(p), _p(t)))
 
     def save_cache(self, topol_path, constr_path):
         """the current state as the reference's two caches"""
