@@ -17,8 +17,9 @@ write) before every timed substep; each substep is timed with CUDA events on
 the object's stream.
 
 Metric: cloth substeps/s.  `e2e` is the same step through the C ABI with
-the state in host memory: upload positions and velocities, step, read them
-back, every step.  `cpu_baseline` times the reference's CPU path (the
+the state in page-locked host memory: upload positions and velocities, step,
+read them back, every step, replaying the first min(K, 100) timed substeps
+from the state they started from.  `cpu_baseline` times the reference's CPU path (the
 oracle's restatement: sequential GS, triangle-ordered CCD with
 de-duplication by scan, sequential response) for one full substep of the
 same state on one host thread.
@@ -183,6 +184,11 @@ def run_ours(args, rank, world):
         solver.set_gs_block(args.gs_block)
     if args.gs_cluster:
         solver.set_gs_cluster(args.gs_cluster)
+    if args.edge_edge:
+        if cs is None:
+            raise SystemExit("--edge-edge needs a workload with collisions")
+        cs.set_edge_edge(True)
+        cfg["edge_edge_ccd"] = True
     stream = torch.cuda.ExternalStream(obj.stream())
     nd = int((sc["ctype"] == scenes.DISTANCE).sum())
     nb = int((sc["ctype"] == scenes.BENDING).sum())
@@ -217,6 +223,9 @@ def run_ours(args, rank, world):
     obj.sync()
     if args.solve == "residual":
         solver.solve_stats(reset=True)
+    # the state the timed substeps start from; the e2e loop replays the same
+    # substeps from it
+    state0 = obj.get_state()
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
           for _ in range(args.steps)]
@@ -295,23 +304,24 @@ def run_ours(args, rank, world):
     obj.set_predicted(prd_save)
     peak, peak_kind = load_peaks()
 
-    # end to end through the C ABI with host buffers
-    x_h = obj.positions()
-    v_h = obj.velocities()
-    e2e_steps = max(10, min(args.steps, 100))
+    # end to end through the C ABI with host buffers: the state lives in
+    # page-locked host arrays, uploaded before and read back after every step
+    n_pts = obj.n_points
+    x_h = torch.empty((n_pts, 3), dtype=torch.float32, pin_memory=True).numpy()
+    v_h = torch.empty((n_pts, 3), dtype=torch.float32, pin_memory=True).numpy()
+    x_h[:], v_h[:] = state0
+    e2e_steps = max(1, min(args.steps, 100))
     obj.sync()
     ph = [0.0, 0.0, 0.0]   # host clock: uploads, step (launch + wait), downloads
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
         ta = time.perf_counter()
-        obj.set_positions(x_h)
-        obj.set_velocities(v_h)
+        obj.set_state(x_h, v_h)
         tb = time.perf_counter()
         step()
         obj.sync()
         tc = time.perf_counter()
-        x_h = obj.positions()
-        v_h = obj.velocities()
+        obj.get_state(x_h, v_h)
         td = time.perf_counter()
         ph[0] += tb - ta
         ph[1] += tc - tb
@@ -345,6 +355,7 @@ def run_ours(args, rank, world):
         "clocks": clk,
         "wall_s_timed_region": t_wall,
         "last_step": {"candidates": stats.get("candidates"), "contacts": stats.get("contacts"),
+                      "edge_edge": cs.ee_stats() if args.edge_edge else None,
                       "overflow": stats.get("overflow"), "relative_residual": residual},
     }
     if rank == 0 and not args.no_cpu_baseline:
@@ -512,6 +523,8 @@ def main():
     ap.add_argument("--no-autotune", action="store_true",
                     help="keep the default GS launch form (per-color, 256 threads) instead of "
                          "the autotuner's pick")
+    ap.add_argument("--edge-edge", action="store_true",
+                    help="also run edge-edge CCD (not in the reference's step; off by default)")
     ap.add_argument("--no-learned-eval", action="store_true",
                     help="skip the learned-vs-plain evaluation on held-out hanging cloths")
     args = ap.parse_args()

@@ -127,15 +127,21 @@ int pbd_object_destroy(pbd_object *obj);
 int pbd_object_sizes(const pbd_object *obj, int *n_points, int *n_tris, int *n_prims);
 /* meshTopol.posBuffer / velBuffer / constrPBDBuffer.prdPBuffer copy-out and
  * copy-in (Buffer::LoadToHost / LoadToDevice, P/Buffer.cuh:123-165), 3 floats
- * per point, through page-locked staging.  get_* blocks until the values are
- * in the caller's array; set_* returns once the caller's array has been read,
- * and the copy is ordered before later work on the object's stream. */
+ * per point.  Page-locked caller arrays (cudaHostAlloc / cudaHostRegister)
+ * are copied directly, others through the object's page-locked staging.
+ * get_* blocks until the values are in the caller's array; set_* returns
+ * once the caller's array has been read, and the copy is ordered before
+ * later work on the object's stream. */
 int pbd_object_get_positions(pbd_object *obj, float *pos3);
 int pbd_object_get_velocities(pbd_object *obj, float *vel3);
 int pbd_object_get_predicted(pbd_object *obj, float *prdp3);
 int pbd_object_set_positions(pbd_object *obj, const float *pos3);
 int pbd_object_set_velocities(pbd_object *obj, const float *vel3);
 int pbd_object_set_predicted(pbd_object *obj, const float *prdp3);
+/* positions and velocities together, one synchronisation (the per-frame
+ * LoadToHost / LoadToDevice of posBuffer and velBuffer) */
+int pbd_object_get_state(pbd_object *obj, float *pos3, float *vel3);
+int pbd_object_set_state(pbd_object *obj, const float *pos3, const float *vel3);
 
 /* Stiffness schedule: the factor k a projection applies for stiffness s in
  * sweep iter (0-based) of a projection call.  PBD_SCHEDULE_REFERENCE (the
@@ -318,6 +324,37 @@ int pbd_ccd_vf_test_batch(const float *x12, const float *p12, const float *thick
 /* number of broadphase candidate pairs that reached the narrow phase in
  * the last CCD call, and the overflow flag */
 int pbd_colli_stats(pbd_colli *c, long long *candidates, long long *contacts, int *overflow);
+
+/* ---- edge-edge CCD (declared only by the reference: Contact::EE,
+ * P/CCD_Basic.h:14; EEResolve commented out, P/CCD.cpp:925-928) -------------- */
+/* Off by default (the reference's step).  On: every CCD pass also finds
+ * edge-edge contacts among the target's unique mesh edges -- the coplanarity
+ * cubic of ExtendedVFTest in FP64, times 0, its roots in [0, 1] and 1 in
+ * ascending order, a hit at the first time the lines of the two edges meet
+ * strictly inside both edges closer than 2 * thickness -- and every response
+ * pass separates them along their common normal to 2 * thickness on the
+ * side they started on, in the same Jacobi sums as the vertex-face
+ * contacts.  Solver graphs are recaptured when this changes. */
+int pbd_colli_set_edge_edge(pbd_colli *c, int on);
+/* the target's unique edges (a < b, 2 ints each) the edge-edge pass uses;
+ * edges NULL: count only */
+int pbd_colli_ee_edges(pbd_colli *c, int *edges, long long cap, int *n);
+/* edge-edge contacts of the last CCD pass, sorted by edge pair: pairs (edge
+ * ids, 2 per), ids (a0 a1 b0 b1), tsu (t and the closest-point parameters
+ * s on edge a, u on edge b), m0 (unit common normal at t = 0 and the side
+ * +1/-1 edge a starts on); any output may be NULL; PBD_ERR_OVERFLOW when a
+ * buffer of the pass overflowed. */
+int pbd_colli_get_ee_contacts(pbd_colli *c, int *pairs, int *ids, float *tsu, float *m0,
+                              long long cap, long long *count);
+/* counts of the last edge-edge pass: edge-cell entries, box-overlapping
+ * pairs, candidates after the distance bound, contacts */
+int pbd_colli_ee_stats(pbd_colli *c, long long *entries, long long *pairs, long long *candidates,
+                       long long *contacts);
+/* the edge-edge test on n independent configurations (x12 / p12: start /
+ * predicted a0, a1, b0, b1, 12 floats per case): hit, tsu (3 floats), m0 (4
+ * floats) per case */
+int pbd_ee_test_batch(const float *x12, const float *p12, const float *thickness, int n,
+                      int *hit, float *tsu, float *m0);
 
 /* ---- the reference's text caches and text scene files ----------------------- */
 /* Host-side scene read from the reference's files (no GPU needed). */

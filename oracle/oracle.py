@@ -38,6 +38,10 @@ class OrcContact(C.Structure):
                 ("face", C.c_int), ("t", C.c_float), ("w", C.c_double * 4), ("n", C.c_float * 3)]
 
 
+class OrcEEHit(C.Structure):
+    _fields_ = [("t", C.c_float), ("s", C.c_float), ("u", C.c_float), ("m0", C.c_float * 4)]
+
+
 class OrcColliParams(C.Structure):
     _fields_ = [("enabled", C.c_int), ("grid", OrcGrid), ("thickness", C.c_float),
                 ("resolve_passes", C.c_int), ("mass_weighted", C.c_int), ("ccd_every", C.c_int),
@@ -72,6 +76,7 @@ class Oracle:
         L.orc_edge_coloring_cpu.restype = C.c_int
         L.orc_eval_worksets.restype = C.c_int
         L.orc_residual.restype = C.c_double
+        L.orc_ccd_ee_brute.restype = C.c_int64
         L.orc_solve_cubic.restype = C.c_int
         L.orc_solve_cubic.argtypes = [C.c_double] * 4 + [_f64p]
         L.orc_extended_vf_test.restype = C.c_int
@@ -260,6 +265,45 @@ class Oracle:
         arr = self._contacts_struct(ids)
         self.lib.orc_collision_resolve_jacobi(len(x), len(ids), arr, _ptr(x), _ptr(p), _ptr(m),
                                               iterations, C.c_float(thickness), int(mass_weighted))
+        return p
+
+    # -- edge-edge CCD (no reference arithmetic; see pbd_oracle.h) ----------
+    def ee_test(self, x, p, thickness):
+        """x, p: (4, 3) start / predicted a0, a1, b0, b1 -> (hit, t, s, u, m0[4])"""
+        xs = np.ascontiguousarray(x, dtype=np.float32).reshape(12)
+        ps = np.ascontiguousarray(p, dtype=np.float32).reshape(12)
+        h = OrcEEHit()
+        hit = self.lib.orc_ee_test(_ptr(xs), _ptr(ps), C.c_float(thickness), C.byref(h))
+        return bool(hit), h.t, h.s, h.u, np.array(h.m0[:], np.float32)
+
+    def ccd_ee_brute(self, edges, point_inst, x, p, thickness, cap=1 << 20):
+        """all edge pairs tested: (pairs (n, 2), tsu (n, 3), m0 (n, 4))"""
+        e = np.ascontiguousarray(edges, dtype=np.int32).reshape(-1, 2)
+        xs = np.ascontiguousarray(x, dtype=np.float32)
+        ps = np.ascontiguousarray(p, dtype=np.float32)
+        pi = None if point_inst is None else np.ascontiguousarray(point_inst, dtype=np.int32)
+        pairs = np.zeros((cap, 2), np.int32)
+        hits = (OrcEEHit * cap)()
+        n = self.lib.orc_ccd_ee_brute(len(e), _ptr(e), _ptr(pi), _ptr(xs), _ptr(ps),
+                                      C.c_float(thickness), _ptr(pairs), hits, C.c_int64(cap))
+        assert n <= cap
+        tsu = np.array([[hits[i].t, hits[i].s, hits[i].u] for i in range(n)], np.float32).reshape(-1, 3)
+        m0 = np.array([hits[i].m0[:] for i in range(n)], np.float32).reshape(-1, 4)
+        return pairs[:n].copy(), tsu, m0
+
+    def resolve_jacobi_ee(self, vf_ids, ee_ids, ee_m0, pos, prdp, mass, iterations, thickness,
+                          mass_weighted):
+        """one Jacobi scheme over vertex-face (v, f0, f1, f2) and edge-edge
+        (a0, a1, b0, b1; side info m0) contacts together"""
+        p = np.ascontiguousarray(prdp, dtype=np.float32).copy()
+        x = np.ascontiguousarray(pos, dtype=np.float32)
+        m = None if mass is None else np.ascontiguousarray(mass, dtype=np.float32)
+        vf = self._contacts_struct(vf_ids)
+        ee = np.ascontiguousarray(ee_ids, dtype=np.int32).reshape(-1, 4)
+        m0 = np.ascontiguousarray(ee_m0, dtype=np.float32).reshape(-1, 4)
+        self.lib.orc_collision_resolve_jacobi_ee(len(x), len(vf_ids), vf, len(ee), _ptr(ee),
+                                                 _ptr(m0), _ptr(x), _ptr(p), _ptr(m), iterations,
+                                                 C.c_float(thickness), int(mass_weighted))
         return p
 
     def vf_resolve_test(self, x, p, thickness):

@@ -1221,6 +1221,224 @@ void orc_collision_resolve_jacobi(int n_points, int n_contacts,
 }
 
 /* ------------------------------------------------------------------ */
+/* edge-edge CCD.  The reference declares the contact kind only          */
+/* (Contact::EE, P/CCD_Basic.h:14; EEResolve is commented out,           */
+/* P/CCD.cpp:925-928), so this follows ExtendedVFTest's structure         */
+/* (P/CCD.cpp:1733-1808): the coplanarity cubic of the four points, the   */
+/* times 0, its roots in [0, 1] and 1 in ascending order, and a hit at    */
+/* the first time the two edges' lines meet inside both edges closer      */
+/* than 2 * thickness.                                                    */
+/* ------------------------------------------------------------------ */
+
+static inline float clamp01(float v) { return fminf(fmaxf(v, 0.0f), 1.0f); }
+
+/* closest points of the lines through a0a1 and b0b1 (Ericson, Real-Time
+ * Collision Detection, 5.1.8): 1 when the lines are not near-parallel and
+ * both parameters lie strictly inside (0, 1); *d = A(s) - B(u) */
+static int ee_interior(f3 a0, f3 a1, f3 b0, f3 b1, float *s, float *u, f3 *d)
+{
+    f3 d1 = sub(a1, a0), d2 = sub(b1, b0), r = sub(a0, b0);
+    float a = dot(d1, d1), e = dot(d2, d2), b = dot(d1, d2);
+    float c = dot(d1, r), f = dot(d2, r);
+    float den = a * e - b * b;
+    if (!(den > 1e-8f * (a * e))) return 0;
+    float ss = (b * f - c * e) / den;
+    float uu = (a * f - b * c) / den;
+    if (!(ss > 0.0f && ss < 1.0f && uu > 0.0f && uu < 1.0f)) return 0;
+    *s = ss;
+    *u = uu;
+    *d = sub(add(a0, mul(d1, ss)), add(b0, mul(d2, uu)));
+    return 1;
+}
+
+/* closest points of the segments a0a1 and b0b1 (Ericson 5.1.9) */
+static void seg_closest(f3 p1, f3 q1, f3 p2, f3 q2, float *s, float *t)
+{
+    f3 d1 = sub(q1, p1), d2 = sub(q2, p2), r = sub(p1, p2);
+    float a = dot(d1, d1), e = dot(d2, d2), f = dot(d2, r);
+    float ss, tt;
+    if (a <= 1e-20f && e <= 1e-20f) {
+        ss = 0.0f;
+        tt = 0.0f;
+    } else if (a <= 1e-20f) {
+        ss = 0.0f;
+        tt = clamp01(f / e);
+    } else {
+        float c = dot(d1, r);
+        if (e <= 1e-20f) {
+            tt = 0.0f;
+            ss = clamp01(-c / a);
+        } else {
+            float b = dot(d1, d2), den = a * e - b * b;
+            ss = den != 0.0f ? clamp01((b * f - c * e) / den) : 0.0f;
+            tt = (b * ss + f) / e;
+            if (tt < 0.0f) {
+                tt = 0.0f;
+                ss = clamp01(-c / a);
+            } else if (tt > 1.0f) {
+                tt = 1.0f;
+                ss = clamp01((b - c) / a);
+            }
+        }
+    }
+    *s = ss;
+    *t = tt;
+}
+
+int orc_ee_test(const float *x, const float *p, float thickness, orc_ee_hit *hit)
+{
+    f3 X0 = ld3(x), X1 = ld3(x + 3), X2 = ld3(x + 6), X3 = ld3(x + 9);
+    f3 P0 = ld3(p), P1 = ld3(p + 3), P2 = ld3(p + 6), P3 = ld3(p + 9);
+    /* the side the edges start on: the common normal at t = 0 */
+    f3 da = sub(X1, X0), db = sub(X3, X2);
+    f3 m0 = cross(da, db);
+    if (!(dot(m0, m0) > 1e-12f * (dot(da, da) * dot(db, db)))) return 0;
+    m0 = nrm(m0);
+    float sg = dot(sub(X0, X2), m0) >= 0.0f ? 1.0f : -1.0f;
+    double a[4];
+    vf_cubic(x, p, a);
+    double t[5];
+    int nsol = orc_solve_cubic(a[3], a[2], a[1], a[0], t);
+    t[nsol] = 1;
+    t[nsol + 1] = 0;
+    sort_small(t, nsol + 2);
+    for (int i = 0; i < nsol + 2; ++i) {
+        if (t[i] < 0 || t[i] > 1) continue;
+        f3 c0 = lerp_t(X0, P0, t[i]), c1 = lerp_t(X1, P1, t[i]);
+        f3 c2 = lerp_t(X2, P2, t[i]), c3 = lerp_t(X3, P3, t[i]);
+        float s, u;
+        f3 d;
+        if (!ee_interior(c0, c1, c2, c3, &s, &u, &d)) continue;
+        float dist = sqrtf(dot(d, d));
+        if ((double)dist - (double)(2.0f * thickness) < -1e-6) {
+            if (hit) {
+                hit->t = (float)t[i];
+                hit->s = s;
+                hit->u = u;
+                hit->m0[0] = m0.x;
+                hit->m0[1] = m0.y;
+                hit->m0[2] = m0.z;
+                hit->m0[3] = sg;
+            }
+            return 1;
+        }
+    }
+    return 0;
+}
+
+int64_t orc_ccd_ee_brute(int n_edges, const int *edges, const int *point_inst, const float *x,
+                         const float *p, float thickness, int *pairs, orc_ee_hit *hits,
+                         int64_t cap)
+{
+    int64_t n = 0;
+    for (int i = 0; i < n_edges; ++i)
+        for (int j = i + 1; j < n_edges; ++j) {
+            int ids[4] = {edges[2 * i], edges[2 * i + 1], edges[2 * j], edges[2 * j + 1]};
+            if (ids[0] == ids[2] || ids[0] == ids[3] || ids[1] == ids[2] || ids[1] == ids[3])
+                continue;
+            if (point_inst && point_inst[ids[0]] != point_inst[ids[2]]) continue;
+            float xs[12], ps[12];
+            gather4(ids, x, xs);
+            gather4(ids, p, ps);
+            orc_ee_hit h;
+            if (!orc_ee_test(xs, ps, thickness, &h)) continue;
+            if (n < cap) {
+                if (pairs) {
+                    pairs[2 * n] = i;
+                    pairs[2 * n + 1] = j;
+                }
+                if (hits) hits[n] = h;
+            }
+            ++n;
+        }
+    return n;
+}
+
+int orc_ee_resolve_deltas(const float *p, const float *wm, const float *m0s, float thickness,
+                          float *delta)
+{
+    f3 A0 = ld3(p), A1 = ld3(p + 3), B0 = ld3(p + 6), B1 = ld3(p + 9);
+    f3 d1 = sub(A1, A0), d2 = sub(B1, B0);
+    f3 mp = cross(d1, d2);
+    if (!(dot(mp, mp) > 1e-12f * (dot(d1, d1) * dot(d2, d2)))) return 0;
+    mp = nrm(mp);
+    if (dot(mp, ld3(m0s)) < 0.0f) mp = mul(mp, -1.0f);
+    float sg = m0s[3];
+    float s, u;
+    seg_closest(A0, A1, B0, B1, &s, &u);
+    f3 d = sub(add(A0, mul(d1, s)), add(B0, mul(d2, u)));
+    float g = (float)((double)(sg * dot(d, mp)) - 2.0 * (double)thickness);
+    if (!(g < -1e-6f)) return 0;
+    float depth = -g;
+    float c[4] = {1.0f - s, s, 1.0f - u, u};
+    float den = wm[0] * c[0] * c[0] + wm[1] * c[1] * c[1] + wm[2] * c[2] * c[2] +
+                wm[3] * c[3] * c[3];
+    if (!(den > 0.0f)) return 0;
+    float imp = depth / den;
+    st3(delta, mul(mp, sg * c[0] * wm[0] * imp));
+    st3(delta + 3, mul(mp, sg * c[1] * wm[1] * imp));
+    st3(delta + 6, mul(mp, -sg * c[2] * wm[2] * imp));
+    st3(delta + 9, mul(mp, -sg * c[3] * wm[3] * imp));
+    return 1;
+}
+
+void orc_collision_resolve_jacobi_ee(int n_points, int n_vf, const orc_contact *vf,
+                                     int n_ee, const int *ee_ids, const float *ee_m0,
+                                     const float *pos, float *prdp, const float *mass,
+                                     int iterations, float thickness, int mass_weighted)
+{
+    /* one Jacobi pass over both contact kinds: every correction in 2^-32 m
+     * fixed point into per-point sums, then sum * 2^-32 / count per point
+     * (orc_collision_resolve_jacobi's scheme) */
+    int64_t *acc = (int64_t *)malloc(sizeof(int64_t) * 3 * (size_t)(n_points > 0 ? n_points : 1));
+    int *cnt = (int *)malloc(sizeof(int) * (size_t)(n_points > 0 ? n_points : 1));
+    int nc = n_vf + n_ee;
+    float *dl = (float *)malloc(sizeof(float) * 12 * (size_t)(nc > 0 ? nc : 1));
+    int *act = (int *)malloc(sizeof(int) * (size_t)(nc > 0 ? nc : 1));
+    int *ids = (int *)malloc(sizeof(int) * 4 * (size_t)(nc > 0 ? nc : 1));
+    for (int c = 0; c < n_vf; ++c) {
+        ids[4 * c] = vf[c].v;
+        ids[4 * c + 1] = vf[c].f0;
+        ids[4 * c + 2] = vf[c].f1;
+        ids[4 * c + 3] = vf[c].f2;
+    }
+    for (int c = 0; c < n_ee; ++c)
+        for (int j = 0; j < 4; ++j) ids[4 * (n_vf + c) + j] = ee_ids[4 * c + j];
+    for (int it = 0; it < iterations; ++it) {
+        for (int c = 0; c < nc; ++c) {
+            float xs[12], ps[12], wm[4];
+            gather4(ids + 4 * c, pos, xs);
+            gather4(ids + 4 * c, prdp, ps);
+            for (int j = 0; j < 4; ++j) wm[j] = mass ? mass[ids[4 * c + j]] : 1.0f;
+            act[c] = c < n_vf ? orc_vf_resolve_deltas(xs, ps, wm, thickness, mass_weighted, dl + 12 * c)
+                              : orc_ee_resolve_deltas(ps, wm, ee_m0 + 4 * (c - n_vf), thickness,
+                                                      dl + 12 * c);
+        }
+        memset(acc, 0, sizeof(int64_t) * 3 * (size_t)n_points);
+        memset(cnt, 0, sizeof(int) * (size_t)n_points);
+        for (int c = 0; c < nc; ++c) {
+            if (!act[c]) continue;
+            for (int j = 0; j < 4; ++j) {
+                for (int k = 0; k < 3; ++k)
+                    acc[3 * ids[4 * c + j] + k] +=
+                        (int64_t)llrintf(dl[12 * c + 3 * j + k] * 4294967296.0f);
+                cnt[ids[4 * c + j]]++;
+            }
+        }
+        for (int i = 0; i < n_points; ++i)
+            if (cnt[i] > 0)
+                for (int k = 0; k < 3; ++k)
+                    prdp[3 * i + k] = prdp[3 * i + k] +
+                        (float)((double)acc[3 * i + k] * (1.0 / 4294967296.0) / (double)cnt[i]);
+    }
+    free(acc);
+    free(cnt);
+    free(dl);
+    free(act);
+    free(ids);
+}
+
+/* ------------------------------------------------------------------ */
 /* substeps                                                             */
 /* ------------------------------------------------------------------ */
 

@@ -293,6 +293,39 @@ typedef struct orc_colli_params {
     int64_t contact_cap;
 } orc_colli_params;
 
+/* Edge-edge CCD (no reference arithmetic: Contact::EE is declared in
+ * P/CCD_Basic.h:14, EEResolve is commented out in P/CCD.cpp:925-928).
+ * x, p: start / predicted positions of a0, a1, b0, b1.  Times 0, the
+ * coplanarity cubic's roots in [0, 1] and 1 in ascending order (as
+ * ExtendedVFTest); a hit is the first time the lines of the two edges meet
+ * strictly inside both edges closer than 2 * thickness.  m0 = the unit
+ * common normal of the edges at t = 0, m0[3] = the side (+1/-1) edge A
+ * starts on along it.  Edges parallel at t = 0 give no hit. */
+typedef struct orc_ee_hit {
+    float t, s, u;
+    float m0[4];
+} orc_ee_hit;
+int orc_ee_test(const float *x, const float *p, float thickness, orc_ee_hit *hit);
+/* every pair i < j of edges (2 point ids each) that share no point and lie
+ * in one instance, tested with orc_ee_test; returns the number of hits
+ * (stored up to cap, in (i, j) order) */
+int64_t orc_ccd_ee_brute(int n_edges, const int *edges, const int *point_inst, const float *x,
+                         const float *p, float thickness, int *pairs, orc_ee_hit *hits,
+                         int64_t cap);
+/* corrections of one edge-edge contact at the predicted positions p (a0,
+ * a1, b0, b1), inverse masses wm: the segments' closest points are pushed
+ * apart along the predicted common normal (oriented like m0) until they
+ * are 2 * thickness apart on the m0[3] side, split by wm and the closest-
+ * point weights.  Returns 0 when the pair needs no correction. */
+int orc_ee_resolve_deltas(const float *p, const float *wm, const float *m0s, float thickness,
+                          float *delta);
+/* orc_collision_resolve_jacobi over vertex-face and edge-edge contacts
+ * together (one set of fixed-point sums per pass) */
+void orc_collision_resolve_jacobi_ee(int n_points, int n_vf, const orc_contact *vf,
+                                     int n_ee, const int *ee_ids, const float *ee_m0,
+                                     const float *pos, float *prdp, const float *mass,
+                                     int iterations, float thickness, int mass_weighted);
+
 /* GPU-semantics substep: advect, iterations x (optional CCD, colored GS
  * sweep, optional response), integrate.  Returns contacts found in the
  * last CCD pass (or 0). */

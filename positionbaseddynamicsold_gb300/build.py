@@ -24,12 +24,13 @@ SOURCES = {
     "pbd_object.cu": ["-fmad=false"],
     "pbd_collision.cu": ["-fmad=false"],
     "pbd_mesh.cu": ["-fmad=false"],
+    "pbd_edge.cu": ["-fmad=false"],
     "pbd_noalloc.cu": [],
     "pbd_mlp.cu": [],
     "pbd_solve.cu": [],
     "pbd_io.cpp": [],
 }
-HEADERS = ["pbd_common.cuh", "pbd_project.cuh"]
+HEADERS = ["pbd_common.cuh", "pbd_project.cuh", "pbd_ccd.cuh"]
 
 
 def _nvcc():

@@ -1,0 +1,295 @@
+// pbd_ccd.cuh -- arithmetic shared by the vertex-face and edge-edge
+// continuous collision paths: float3 helpers, barycentric coordinates, the
+// FP64 cubic root isolation of P/CCD.cpp:48-113, ExtendedVFTest's evaluation
+// (P/CCD.cpp:1733-1808), point-triangle distance, the spatial-hash cell and
+// bucket functions, warp-aggregated counters and the fixed-point response
+// sums.  Include only from translation units compiled with -fmad=false.
+#pragma once
+
+#include <cooperative_groups.h>
+
+#include "pbd_common.cuh"
+
+namespace pbd {
+namespace {
+
+namespace cg = cooperative_groups;
+
+struct v3 {
+    float x, y, z;
+};
+__device__ __forceinline__ v3 mk3(float x, float y, float z) { return {x, y, z}; }
+__device__ __forceinline__ v3 ld3(float4 a) { return {a.x, a.y, a.z}; }
+__device__ __forceinline__ v3 sub3(v3 a, v3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+__device__ __forceinline__ v3 add3(v3 a, v3 b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
+__device__ __forceinline__ v3 mul3(v3 a, float s) { return {a.x * s, a.y * s, a.z * s}; }
+__device__ __forceinline__ v3 div3(v3 a, float s) { return {a.x / s, a.y / s, a.z / s}; }
+__device__ __forceinline__ float dot3(v3 a, v3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+__device__ __forceinline__ v3 cross3(v3 a, v3 b) {
+    return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
+}
+// normalize with a correctly rounded reciprocal square root, as the
+// reference's host build computes it (1.0f / sqrtf)
+__device__ __forceinline__ v3 nrm3(v3 v) {
+    float inv = 1.0f / sqrtf(dot3(v, v));
+    return mul3(v, inv);
+}
+__device__ __forceinline__ float dist3(v3 a, v3 b) {
+    float dx = a.x - b.x, dy = a.y - b.y, dz = a.z - b.z;
+    return sqrtf(dx * dx + dy * dy + dz * dz);
+}
+__device__ __forceinline__ float stp(v3 u, v3 v, v3 w) { return dot3(u, cross3(v, w)); }
+__device__ __forceinline__ v3 lerp_t(v3 a, v3 b, double t) {
+    float tf = (float)t;
+    v3 d = sub3(b, a);
+    return add3(a, mk3(tf * d.x, tf * d.y, tf * d.z));
+}
+// BarycentricCoord (P/CCD.cpp:115-130)
+__device__ __forceinline__ v3 bary(v3 pos, v3 p0, v3 p1, v3 p2) {
+    v3 ab = sub3(p0, p2), ac = sub3(p1, p2), ap = sub3(pos, p2);
+    float d00 = dot3(ac, ac), d01 = dot3(ac, ab), d02 = dot3(ac, ap);
+    float d11 = dot3(ab, ab), d12 = dot3(ab, ap);
+    float inv = 1.0f / (d00 * d11 - d01 * d01);
+    float v = (d11 * d02 - d01 * d12) * inv;
+    float u = (d00 * d12 - d01 * d02) * inv;
+    float w = 1.0f - u - v;
+    return mk3(u, v, w);
+}
+
+// ---- cubic root isolation (P/CCD.cpp:48-113), double precision ----------
+__device__ __forceinline__ double sgnd(double x) { return x < 0 ? -1.0 : 1.0; }
+
+__device__ int solve_quadratic(double a, double b, double c, double x[2]) {
+    double d = b * b - 4 * a * c;
+    if (d < 0) {
+        x[0] = -b / (2 * a);
+        return 0;
+    }
+    double q = -(b + sgnd(b) * sqrt(d)) / 2;
+    int i = 0;
+    if (fabs(a) > 1e-12 * fabs(q)) x[i++] = q / a;
+    if (fabs(q) > 1e-12 * fabs(c)) x[i++] = c / q;
+    if (i == 2 && x[0] > x[1]) {
+        double s = x[0];
+        x[0] = x[1];
+        x[1] = s;
+    }
+    return i;
+}
+
+__device__ double newtons_method(double a, double b, double c, double d, double x0, int dir) {
+    if (dir != 0) {
+        double y0 = d + x0 * (c + x0 * (b + x0 * a));
+        double ddy0 = 2 * b + x0 * (6 * a);
+        x0 += dir * sqrt(fabs(2 * y0 / ddy0));
+    }
+    for (int iter = 0; iter < 100; iter++) {
+        double y = d + x0 * (c + x0 * (b + x0 * a));
+        double dy = c + x0 * (2 * b + x0 * 3 * a);
+        if (dy == 0) return x0;
+        double x1 = x0 - y / dy;
+        if (fabs(x0 - x1) < 1e-6) return x0;
+        x0 = x1;
+    }
+    return x0;
+}
+
+// when the derivative has no critical point and none was written, Newton
+// starts from 0 (the reference reads an uninitialised value there)
+__device__ int solve_cubic(double a, double b, double c, double d, double x[3]) {
+    double xc[2] = {0.0, 0.0};
+    int ncrit = solve_quadratic(3 * a, 2 * b, c, xc);
+    if (ncrit == 0) {
+        x[0] = newtons_method(a, b, c, d, xc[0], 0);
+        return 1;
+    } else if (ncrit == 1) {
+        return solve_quadratic(b, c, d, x);
+    }
+    double yc[2] = {d + xc[0] * (c + xc[0] * (b + xc[0] * a)),
+                    d + xc[1] * (c + xc[1] * (b + xc[1] * a))};
+    int i = 0;
+    if (yc[0] * a >= 0) x[i++] = newtons_method(a, b, c, d, xc[0], -1);
+    if (yc[0] * yc[1] <= 0) {
+        int closer = fabs(yc[0]) < fabs(yc[1]) ? 0 : 1;
+        x[i++] = newtons_method(a, b, c, d, xc[closer], closer == 0 ? 1 : -1);
+    }
+    if (yc[1] * a <= 0) x[i++] = newtons_method(a, b, c, d, xc[1], 1);
+    return i;
+}
+
+struct VFResult {
+    float t;
+    v3 n;
+    double w[4];
+};
+
+// one evaluation of ExtendedVFTest's loop body at time t
+__device__ __forceinline__ bool vf_eval_at(const v3 *X, const v3 *P, float th, double t,
+                                           VFResult &res) {
+    v3 c0 = lerp_t(X[0], P[0], t), c1 = lerp_t(X[1], P[1], t);
+    v3 c2 = lerp_t(X[2], P[2], t), c3 = lerp_t(X[3], P[3], t);
+    v3 n = nrm3(cross3(sub3(P[2], P[1]), sub3(P[3], P[1])));
+    v3 cn = nrm3(cross3(sub3(c2, c1), sub3(c3, c1)));
+    double dist = dot3(sub3(c0, c1), cn);
+    v3 w = bary(c0, c1, c2, c3);
+    res.t = (float)t;
+    res.n = n;
+    res.w[0] = 1;
+    res.w[1] = w.x;
+    res.w[2] = w.y;
+    res.w[3] = w.z;
+    float e1 = dist3(c1, c2), e2 = dist3(c1, c3), e3 = dist3(c2, c3);
+    float eps = (float)((double)th / ((double)(e1 + e2 + e3) / 3.0));
+    bool in = (w.x <= (1 + eps)) && (w.x >= (-eps)) && (w.y <= (1 + eps)) && (w.y >= (-eps)) &&
+              (w.z <= (1 + eps)) && (w.z >= (-eps));
+    return (fabs(dist) - (double)(2.0f * th) < -1e-6) && in;
+}
+
+// true when a3 t^3 + a2 t^2 + a1 t + a0 has no root on [-d, 1+d], d = 1e-3:
+// its Bernstein coefficients on that interval share one strict sign
+__device__ __forceinline__ bool no_root_near_unit(double a0, double a1, double a2, double a3) {
+    const double u = -1e-3, L = 1.002;
+    double c0 = ((a3 * u + a2) * u + a1) * u + a0;
+    double c1 = L * ((3.0 * a3 * u + 2.0 * a2) * u + a1);
+    double c2 = L * L * (3.0 * a3 * u + a2);
+    double c3 = L * L * L * a3;
+    double b0 = c0, b1 = c0 + c1 / 3.0, b2 = c0 + 2.0 * c1 / 3.0 + c2 / 3.0, b3 = c0 + c1 + c2 + c3;
+    double tol = 1e-9 * (fabs(a0) + fabs(a1) + fabs(a2) + fabs(a3));
+    bool pos = b0 > tol && b1 > tol && b2 > tol && b3 > tol;
+    bool neg = b0 < -tol && b1 < -tol && b2 < -tol && b3 < -tol;
+    return pos || neg;
+}
+
+// ExtendedVFTest (P/CCD.cpp:1733-1808); X/P = start/predicted positions of
+// point, f0, f1, f2.  The reference evaluates t = 0, the cubic's roots in
+// [0, 1] and t = 1 in ascending order and stops at the first hit.  Two
+// shortcuts keep that result: t = 0 is always the first time evaluated, so
+// a hit there ends the test before any root is needed; and when the
+// coplanarity cubic provably has no root within 1e-3 of [0, 1], the root
+// solver (Newton iterations converging to roots outside that range) adds no
+// time to evaluate, leaving t = 1.  Only the remaining pairs run the FP64
+// root isolation.
+__device__ bool extended_vf_test(const v3 *X, const v3 *P, float th, VFResult &res) {
+    v3 x0 = X[0], v0 = sub3(P[0], x0);
+    v3 x1 = sub3(X[1], x0), x2 = sub3(X[2], x0), x3 = sub3(X[3], x0);
+    v3 v1 = sub3(sub3(P[1], X[1]), v0), v2 = sub3(sub3(P[2], X[2]), v0),
+       v3_ = sub3(sub3(P[3], X[3]), v0);
+    double a0 = stp(x1, x2, x3);
+    double a1 = stp(v1, x2, x3) + stp(x1, v2, x3) + stp(x1, x2, v3_);
+    double a2 = stp(x1, v2, v3_) + stp(v1, x2, v3_) + stp(v1, v2, x3);
+    double a3 = stp(v1, v2, v3_);
+    if (vf_eval_at(X, P, th, 0.0, res)) return true;
+    if (no_root_near_unit(a0, a1, a2, a3)) return vf_eval_at(X, P, th, 1.0, res);
+    double t[5];
+    int nsol = solve_cubic(a3, a2, a1, a0, t);
+    t[nsol] = 1;
+    t[nsol + 1] = 0;
+    int m = nsol + 2;
+    for (int i = 1; i < m; ++i) {
+        double v = t[i];
+        int j = i - 1;
+        while (j >= 0 && t[j] > v) {
+            t[j + 1] = t[j];
+            --j;
+        }
+        t[j + 1] = v;
+    }
+    for (int i = 0; i < m; ++i) {
+        if (t[i] < 0 || t[i] > 1) continue;
+        if (vf_eval_at(X, P, th, t[i], res)) return true;
+    }
+    return false;
+}
+
+// closest distance from point p to triangle abc (Ericson, Real-Time
+// Collision Detection, 5.1.5), float
+__device__ float point_tri_dist(v3 p, v3 a, v3 b, v3 c) {
+    v3 ab = sub3(b, a), ac = sub3(c, a), ap = sub3(p, a);
+    float d1 = dot3(ab, ap), d2 = dot3(ac, ap);
+    if (d1 <= 0.f && d2 <= 0.f) return sqrtf(dot3(ap, ap));
+    v3 bp = sub3(p, b);
+    float d3 = dot3(ab, bp), d4 = dot3(ac, bp);
+    if (d3 >= 0.f && d4 <= d3) return sqrtf(dot3(bp, bp));
+    float vc = d1 * d4 - d3 * d2;
+    if (vc <= 0.f && d1 >= 0.f && d3 <= 0.f) {
+        float v = d1 / (d1 - d3);
+        v3 q = sub3(p, add3(a, mul3(ab, v)));
+        return sqrtf(dot3(q, q));
+    }
+    v3 cp = sub3(p, c);
+    float d5 = dot3(ab, cp), d6 = dot3(ac, cp);
+    if (d6 >= 0.f && d5 <= d6) return sqrtf(dot3(cp, cp));
+    float vb = d5 * d2 - d1 * d6;
+    if (vb <= 0.f && d2 >= 0.f && d6 <= 0.f) {
+        float w = d2 / (d2 - d6);
+        v3 q = sub3(p, add3(a, mul3(ac, w)));
+        return sqrtf(dot3(q, q));
+    }
+    float va = d3 * d6 - d5 * d4;
+    if (va <= 0.f && (d4 - d3) >= 0.f && (d5 - d6) >= 0.f) {
+        float w = (d4 - d3) / ((d4 - d3) + (d5 - d6));
+        v3 q = sub3(p, add3(b, mul3(sub3(c, b), w)));
+        return sqrtf(dot3(q, q));
+    }
+    float den = 1.f / (va + vb + vc);
+    float v = vb * den, w = vc * den;
+    v3 q = sub3(p, add3(a, add3(mul3(ab, v), mul3(ac, w))));
+    return sqrtf(dot3(q, q));
+}
+
+__device__ __forceinline__ bool sliver(v3 a, v3 b, v3 c) {
+    v3 e1 = sub3(b, a), e2 = sub3(c, a);
+    v3 n = cross3(e1, e2);
+    return !(dot3(n, n) > 1e-10f * (dot3(e1, e1) * dot3(e2, e2)));
+}
+
+__device__ __forceinline__ uint32_t teschner(int x, int y, int z) {
+    return ((uint32_t)x * 73856093u) ^ ((uint32_t)y * 19349663u) ^ ((uint32_t)z * 83492791u);
+}
+
+struct GridParams {
+    float3 start, cell;
+    int3 size;
+    int hashed;
+    uint32_t nb;  // buckets (bounded: cells; sentinel key = nb)
+};
+
+__device__ __forceinline__ bool outside(const GridParams &g, int x, int y, int z) {
+    return x < 0 || y < 0 || z < 0 || x >= g.size.x || y >= g.size.y || z >= g.size.z;
+}
+// bucket of a cell; in hashed mode the instance is mixed in, so instances
+// that overlap in space (batched cloths) do not share buckets
+__device__ __forceinline__ uint32_t bucket_of(const GridParams &g, int x, int y, int z,
+                                              int inst) {
+    if (g.hashed) return (teschner(x, y, z) ^ ((uint32_t)inst * 0x9E3779B1u)) & (g.nb - 1u);
+    return ((uint32_t)z * (uint32_t)g.size.y) * (uint32_t)g.size.x +
+           (uint32_t)y * (uint32_t)g.size.x + (uint32_t)x;
+}
+
+// one atomic per group of lanes that reach this call together
+__device__ __forceinline__ int agg_inc(int *counter) {
+    cg::coalesced_group g = cg::coalesced_threads();
+    int base = 0;
+    if (g.thread_rank() == 0) base = atomicAdd(counter, (int)g.size());
+    return g.shfl(base, 0) + (int)g.thread_rank();
+}
+
+__device__ __forceinline__ void add_fixed(long long *acc, int pt, float dx, float dy, float dz) {
+    atomicAdd((unsigned long long *)(acc + 3 * (long long)pt), (unsigned long long)__float2ll_rn(dx * 4294967296.0f));
+    atomicAdd((unsigned long long *)(acc + 3 * (long long)pt + 1), (unsigned long long)__float2ll_rn(dy * 4294967296.0f));
+    atomicAdd((unsigned long long *)(acc + 3 * (long long)pt + 2), (unsigned long long)__float2ll_rn(dz * 4294967296.0f));
+}
+
+
+GridParams params_of(const pbd_shs *h) {
+    GridParams g;
+    g.start = make_float3(h->start[0], h->start[1], h->start[2]);
+    g.cell = make_float3(h->cell[0], h->cell[1], h->cell[2]);
+    g.size = make_int3(h->size[0], h->size[1], h->size[2]);
+    g.hashed = h->hashed;
+    g.nb = (uint32_t)h->n_buckets;
+    return g;
+}
+
+}  // namespace
+}  // namespace pbd

@@ -276,6 +276,24 @@ struct pbd_colli {
     // between passes)
     pbd::DBuf<long long> acc;
     pbd::DBuf<int> acnt;
+    // edge-edge CCD (off unless enabled): the object's unique edges (built
+    // on first use; -1 = not yet), their grown swept boxes, the edge-cell
+    // entries of the edge hash and their sort buffers, the edge pairs,
+    // candidates and contacts (ids a0 a1 b0 b1, side m0 + sign, t s u, the
+    // edge pair).  counters[8..11]: entries, pairs, candidates, contacts.
+    int ee_on = 0;
+    int ee_n = -1;
+    int ee_log2 = 0;
+    long long ee_entry_cap = 0;
+    pbd::DBuf<int2> ee_edges;
+    pbd::DBuf<float4> ee_lo, ee_hi;
+    pbd::DBuf<int4> ee_cell;
+    pbd::DBuf<uint32_t> ee_key, ee_key2;
+    pbd::DBuf<int> ee_val, ee_val2;
+    pbd::DBuf<int2> ee_pairs, ee_cand, ee_hpair;
+    pbd::DBuf<int4> ee_ids;
+    pbd::DBuf<float4> ee_m0, ee_tsu;
+    pbd::SortScratch ee_scr;
 };
 
 // Device state of the solve-to-residual loop (one per solver).
@@ -388,5 +406,10 @@ int launch_residual_parts(pbd_object *o, bool dist, bool bend, const float4 *pos
 int launch_obstacles(pbd_solver *s);
 int ccd_detect(pbd_colli *c);
 int ccd_resolve(pbd_colli *c, int passes);
+// edge-edge CCD (pbd_edge.cu): buffers and edge list, one detection pass,
+// the response's corrections into the shared fixed-point sums
+int ee_prepare(pbd_colli *c);
+int ee_detect(pbd_colli *c);
+int ee_deltas_launch(pbd_colli *c);
 int shs_update(pbd_shs *h);
 }  // namespace pbd

@@ -183,6 +183,16 @@ int build(int n_points, const float *rest_pos, int n_tris, const int *tris, Mesh
 }
 
 }  // namespace
+
+// the unique edges (a < b, key order) of a triangle mesh
+int mesh_unique_edges(int n_points, int n_tris, const int *tris, std::vector<int2> &edges) {
+    std::vector<float> zero(3 * (size_t)n_points, 0.f);
+    MeshResult r;
+    PBD_TRY(build(n_points, zero.data(), n_tris, tris, r));
+    edges.swap(r.edges);
+    return PBD_OK;
+}
+
 }  // namespace pbd
 
 using namespace pbd;

@@ -1223,44 +1223,84 @@ __global__ void k_unpack3(int n, const float4 *__restrict__ src, float *__restri
 
 static int staging(pbd_object *o) {
     size_t m = 3 * (size_t)o->n;
-    PBD_TRY(o->h_in.alloc(m));
-    PBD_TRY(o->h_out.alloc(m));
-    PBD_TRY(o->d3.alloc(m));
+    PBD_TRY(o->h_in.alloc(2 * m));
+    PBD_TRY(o->h_out.alloc(2 * m));
+    PBD_TRY(o->d3.alloc(2 * m));
     if (!o->in_done) PBD_CUDA(cudaEventCreateWithFlags(&o->in_done, cudaEventDisableTiming));
     return PBD_OK;
 }
 
-// blocking: dst holds the values when this returns
-static int copy_out3(pbd_object *o, const float4 *src, float *dst) {
-    PBD_CHECK(o && dst, PBD_ERR_ARG, "null argument");
+// page-locked (cudaHostAlloc / cudaHostRegister) host memory is copied
+// directly; anything else goes through the object's staging
+static bool page_locked(const void *h) {
+    cudaPointerAttributes at;
+    if (cudaPointerGetAttributes(&at, h) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return at.type == cudaMemoryTypeHost;
+}
+
+// Device float4 arrays src[k] -> host float3 arrays dst[k] (k < cnt); blocks
+// until every dst holds its values.
+static int copy_out3n(pbd_object *o, int cnt, const float4 *const *src, float *const *dst) {
+    for (int k = 0; k < cnt; ++k) PBD_CHECK(dst[k], PBD_ERR_ARG, "null argument");
     if (o->n == 0) return PBD_OK;
     PBD_TRY(staging(o));
-    size_t bytes = sizeof(float) * 3 * (size_t)o->n;
-    k_unpack3<<<grid_for(o->n, 256), 256, 0, o->stream>>>(o->n, src, o->d3.p);
-    PBD_LAUNCH();
-    PBD_CUDA(cudaMemcpyAsync(o->h_out.p, o->d3.p, bytes, cudaMemcpyDeviceToHost, o->stream));
+    const size_t m = 3 * (size_t)o->n, bytes = sizeof(float) * m;
+    bool direct[2];
+    for (int k = 0; k < cnt; ++k) {
+        direct[k] = page_locked(dst[k]);
+        float *d3 = o->d3.p + k * m;
+        k_unpack3<<<grid_for(o->n, 256), 256, 0, o->stream>>>(o->n, src[k], d3);
+        PBD_LAUNCH();
+        PBD_CUDA(cudaMemcpyAsync(direct[k] ? dst[k] : o->h_out.p + k * m, d3, bytes,
+                                 cudaMemcpyDeviceToHost, o->stream));
+    }
     PBD_CUDA(cudaStreamSynchronize(o->stream));
-    std::memcpy(dst, o->h_out.p, bytes);
+    for (int k = 0; k < cnt; ++k)
+        if (!direct[k]) std::memcpy(dst[k], o->h_out.p + k * m, bytes);
     return PBD_OK;
 }
 
-// stream-ordered: src is copied into the staging before this returns, and
-// work queued on the object's stream afterwards sees the new values
-static int copy_in3(pbd_object *o, float4 *dst, const float *src, bool keep_w) {
-    PBD_CHECK(o && src, PBD_ERR_ARG, "null argument");
+// Host float3 arrays src[k] -> device float4 arrays dst[k] (w = massBuffer
+// value when keep_w[k], else 0).  Returns once every src has been read; the
+// copies are ordered before later work on the object's stream.
+static int copy_in3n(pbd_object *o, int cnt, float4 *const *dst, const float *const *src,
+                     const bool *keep_w) {
+    for (int k = 0; k < cnt; ++k) PBD_CHECK(src[k], PBD_ERR_ARG, "null argument");
     if (o->n == 0) return PBD_OK;
     PBD_TRY(staging(o));
-    size_t bytes = sizeof(float) * 3 * (size_t)o->n;
-    // the previous upload out of the staging has to be done before it is
-    // overwritten
+    const size_t m = 3 * (size_t)o->n, bytes = sizeof(float) * m;
+    // the previous upload out of the staging (or a caller's page-locked
+    // array) has to be done before the staging is overwritten
     PBD_CUDA(cudaEventSynchronize(o->in_done));
-    std::memcpy(o->h_in.p, src, bytes);
-    PBD_CUDA(cudaMemcpyAsync(o->d3.p, o->h_in.p, bytes, cudaMemcpyHostToDevice, o->stream));
+    bool any_direct = false;
+    for (int k = 0; k < cnt; ++k) {
+        const bool direct = page_locked(src[k]);
+        any_direct |= direct;
+        if (!direct) std::memcpy(o->h_in.p + k * m, src[k], bytes);
+        float *d3 = o->d3.p + k * m;
+        PBD_CUDA(cudaMemcpyAsync(d3, direct ? src[k] : o->h_in.p + k * m, bytes,
+                                 cudaMemcpyHostToDevice, o->stream));
+        k_pack3<<<grid_for(o->n, 256), 256, 0, o->stream>>>(
+            o->n, d3, keep_w[k] ? o->mass.p : nullptr, dst[k]);
+        PBD_LAUNCH();
+    }
     PBD_CUDA(cudaEventRecord(o->in_done, o->stream));
-    k_pack3<<<grid_for(o->n, 256), 256, 0, o->stream>>>(o->n, o->d3.p,
-                                                         keep_w ? o->mass.p : nullptr, dst);
-    PBD_LAUNCH();
+    // a caller's page-locked array is read by the copy itself: wait for it
+    if (any_direct) PBD_CUDA(cudaEventSynchronize(o->in_done));
     return PBD_OK;
+}
+
+static int copy_out3(pbd_object *o, const float4 *src, float *dst) {
+    PBD_CHECK(o, PBD_ERR_ARG, "null argument");
+    return copy_out3n(o, 1, &src, &dst);
+}
+
+static int copy_in3(pbd_object *o, float4 *dst, const float *src, bool keep_w) {
+    PBD_CHECK(o, PBD_ERR_ARG, "null argument");
+    return copy_in3n(o, 1, &dst, &src, &keep_w);
 }
 
 int pbd_object_get_positions(pbd_object *o, float *v) { return copy_out3(o, o ? o->x.p : nullptr, v); }
@@ -1269,6 +1309,21 @@ int pbd_object_get_predicted(pbd_object *o, float *v) { return copy_out3(o, o ? 
 int pbd_object_set_positions(pbd_object *o, const float *v) { return copy_in3(o, o ? o->x.p : nullptr, v, true); }
 int pbd_object_set_velocities(pbd_object *o, const float *v) { return copy_in3(o, o ? o->v.p : nullptr, v, false); }
 int pbd_object_set_predicted(pbd_object *o, const float *v) { return copy_in3(o, o ? o->p.p : nullptr, v, true); }
+
+int pbd_object_get_state(pbd_object *o, float *pos3, float *vel3) {
+    PBD_CHECK(o, PBD_ERR_ARG, "null object");
+    const float4 *src[2] = {o->x.p, o->v.p};
+    float *dst[2] = {pos3, vel3};
+    return copy_out3n(o, 2, src, dst);
+}
+
+int pbd_object_set_state(pbd_object *o, const float *pos3, const float *vel3) {
+    PBD_CHECK(o, PBD_ERR_ARG, "null object");
+    float4 *dst[2] = {o->x.p, o->v.p};
+    const float *src[2] = {pos3, vel3};
+    const bool keep[2] = {true, false};
+    return copy_in3n(o, 2, dst, src, keep);
+}
 
 // records i0.. from the per-prim buffers, after a per-prim change
 static int rebuild_records(pbd_object *o, int i0) {
@@ -1658,7 +1713,8 @@ int pbd_solver_step(pbd_solver *s, float dt, int substeps, int iterations, pbd_c
     PBD_CHECK(s->obj->sorted, PBD_ERR_STATE, "constraints are not color-sorted");
     PBD_CHECK(!c || c->obj == s->obj, PBD_ERR_ARG, "collision solver targets another object");
     if (!use_graph) return record_steps(s, dt, substeps, iterations, c);
-    int sig = s->sphere_on * 3 + s->ground_on * 7 + (c ? c->response * 11 + c->iterations * 13 : 0) +
+    int sig = s->sphere_on * 3 + s->ground_on * 7 +
+              (c ? c->response * 11 + c->iterations * 13 + c->ee_on * 101 : 0) +
               (s->n_inst_spheres > 0) * 17 +
               s->gs_path * 1009 + s->obj->sched * 7919;
     if (s->gexec && (s->g_dt != dt || s->g_sub != substeps || s->g_it != iterations ||

@@ -317,7 +317,8 @@ int pbd_solver_step_to_residual(pbd_solver *s, float dt, int substeps, pbd_colli
         return PBD_OK;
     }
     int sig = s->sphere_on * 3 + s->ground_on * 7 +
-              (c ? c->response * 11 + c->iterations * 13 : 0) + (s->n_inst_spheres > 0) * 17 +
+              (c ? c->response * 11 + c->iterations * 13 + c->ee_on * 101 : 0) +
+              (s->n_inst_spheres > 0) * 17 +
               (s->ws != nullptr) * 19 + s->min_sweeps * 29 + (o->pdl ? 23 : 0) +
               s->gs_path * 1009 + o->sched * 7919;
     if (s->rexec && (s->r_dt != dt || s->r_sub != substeps || s->r_colli != c ||

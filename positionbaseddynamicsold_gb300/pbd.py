@@ -91,6 +91,8 @@ EXPORTS = [
     "pbd_solver_get_gs_cluster", "pbd_mesh_constraints", "pbd_object_create_mesh",
     "pbd_object_set_stiffness_schedule", "pbd_object_get_stiffness_schedule",
     "pbd_object_set_stiffness", "pbd_object_set_anchor_targets",
+    "pbd_colli_set_edge_edge", "pbd_colli_ee_edges", "pbd_colli_get_ee_contacts",
+    "pbd_colli_ee_stats", "pbd_ee_test_batch", "pbd_object_get_state", "pbd_object_set_state",
 ]
 
 
@@ -148,6 +150,9 @@ def load(build_if_missing: bool = True) -> C.CDLL:
                                        C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                        C.c_void_p, C.c_void_p]
     L.pbd_object_set_stiffness.argtypes = [C.c_void_p, C.c_uint, C.c_float]
+    L.pbd_colli_ee_edges.argtypes = [C.c_void_p, C.c_void_p, C.c_longlong, C.c_void_p]
+    L.pbd_colli_get_ee_contacts.argtypes = [C.c_void_p] + [C.c_void_p] * 4 + [C.c_longlong,
+                                                                              C.c_void_p]
     L.pbd_warmstart_adam.argtypes = [C.c_void_p, C.c_float, C.c_float, C.c_float, C.c_float]
     L.pbd_warmstart_train_step.argtypes = [C.c_void_p, C.c_void_p, C.c_float, C.c_void_p]
     _LIB = L
@@ -327,6 +332,19 @@ class PBDObject:
 
     def predicted(self):
         return self._get3(self.L.pbd_object_get_predicted)
+
+    def get_state(self, pos=None, vel=None):
+        """positions and velocities in one call; pos / vel: optional (n, 3)
+        float32 arrays to fill (page-locked ones are copied directly)"""
+        pos = np.empty((self.n_points, 3), np.float32) if pos is None else pos
+        vel = np.empty((self.n_points, 3), np.float32) if vel is None else vel
+        assert pos.dtype == np.float32 and vel.dtype == np.float32
+        assert pos.flags.c_contiguous and vel.flags.c_contiguous
+        _check(self.L.pbd_object_get_state(self.h, _p(pos), _p(vel)))
+        return pos, vel
+
+    def set_state(self, pos, vel):
+        _check(self.L.pbd_object_set_state(self.h, _p(_f32(pos, (-1,))), _p(_f32(vel, (-1,)))))
 
     def set_positions(self, a):
         _check(self.L.pbd_object_set_positions(self.h, _p(_f32(a, (-1,)))))
@@ -576,6 +594,36 @@ class CollisionSolver:
         a, b, c = C.c_longlong(), C.c_longlong(), C.c_int()
         _check(self.L.pbd_colli_stats(self.h, C.byref(a), C.byref(b), C.byref(c)))
         return {"candidates": a.value, "contacts": b.value, "overflow": c.value}
+
+    # edge-edge CCD (no reference arithmetic; off by default)
+    def set_edge_edge(self, on=True):
+        _check(self.L.pbd_colli_set_edge_edge(self.h, int(bool(on))))
+
+    def ee_edges(self):
+        n = C.c_int()
+        _check(self.L.pbd_colli_ee_edges(self.h, None, 0, C.byref(n)))
+        e = np.zeros((max(n.value, 1), 2), np.int32)
+        _check(self.L.pbd_colli_ee_edges(self.h, _p(e), len(e), C.byref(n)))
+        return e[:n.value]
+
+    def ee_contacts(self):
+        """(pairs (n, 2), ids (n, 4), tsu (n, 3), m0 (n, 4)) sorted by edge pair"""
+        n = C.c_longlong()
+        _check(self.L.pbd_colli_get_ee_contacts(self.h, None, None, None, None, 0, C.byref(n)))
+        k = max(n.value, 1)
+        pairs = np.zeros((k, 2), np.int32)
+        ids = np.zeros((k, 4), np.int32)
+        tsu = np.zeros((k, 3), np.float32)
+        m0 = np.zeros((k, 4), np.float32)
+        _check(self.L.pbd_colli_get_ee_contacts(self.h, _p(pairs), _p(ids), _p(tsu), _p(m0), k,
+                                                C.byref(n)))
+        m = n.value
+        return pairs[:m], ids[:m], tsu[:m], m0[:m]
+
+    def ee_stats(self):
+        v = [C.c_longlong() for _ in range(4)]
+        _check(self.L.pbd_colli_ee_stats(self.h, *[C.byref(x) for x in v]))
+        return dict(zip(("entries", "pairs", "candidates", "contacts"), [x.value for x in v]))
 
 
 class SolverPBD:
@@ -913,6 +961,21 @@ def residual_noalloc(d_pos4, n_points, d_dist_idx, d_rest_length, n_dist, d_bend
     _check(L.pbd_residual_noalloc(d_pos4, n_points, d_dist_idx or None, d_rest_length or None,
                                   n_dist, d_bend_idx or None, d_rest_angle or None,
                                   d_hinge_rest or None, n_bend, d_out, stream or None))
+
+
+def ee_test_batch(X, P, thickness):
+    """pbd_ee_test_batch: the edge-edge test on n (edge a, edge b) cases.
+    X, P: (n, 4, 3) start / predicted a0, a1, b0, b1; thickness: (n,)."""
+    L = load()
+    X = np.ascontiguousarray(X, np.float32).reshape(-1, 12)
+    P = np.ascontiguousarray(P, np.float32).reshape(-1, 12)
+    th = np.ascontiguousarray(thickness, np.float32)
+    n = len(X)
+    hit = np.zeros(n, np.int32)
+    tsu = np.zeros((n, 3), np.float32)
+    m0 = np.zeros((n, 4), np.float32)
+    _check(L.pbd_ee_test_batch(_p(X), _p(P), _p(th), n, _p(hit), _p(tsu), _p(m0)))
+    return hit, tsu, m0
 
 
 def vf_test_batch(X, P, thickness):
