@@ -153,7 +153,12 @@ __device__ __forceinline__ bool no_root_near_unit(double a0, double a1, double a
     double c1 = L * ((3.0 * a3 * u + 2.0 * a2) * u + a1);
     double c2 = L * L * (3.0 * a3 * u + a2);
     double c3 = L * L * L * a3;
-    double b0 = c0, b1 = c0 + c1 / 3.0, b2 = c0 + 2.0 * c1 / 3.0 + c2 / 3.0, b3 = c0 + c1 + c2 + c3;
+    // the Bernstein coefficients only decide a sign with a relative margin
+    // of 1e-9, so multiplying by the rounded 1/3 instead of dividing by 3
+    // (an FP64 division is a long sequence on this GPU) changes nothing
+    const double third = 1.0 / 3.0;
+    double b0 = c0, b1 = c0 + c1 * third, b2 = c0 + 2.0 * c1 * third + c2 * third,
+           b3 = c0 + c1 + c2 + c3;
     double tol = 1e-9 * (fabs(a0) + fabs(a1) + fabs(a2) + fabs(a3));
     bool pos = b0 > tol && b1 > tol && b2 > tol && b3 > tol;
     bool neg = b0 < -tol && b1 < -tol && b2 < -tol && b3 < -tol;
@@ -169,17 +174,36 @@ __device__ __forceinline__ bool no_root_near_unit(double a0, double a1, double a
 // solver (Newton iterations converging to roots outside that range) adds no
 // time to evaluate, leaving t = 1.  Only the remaining pairs run the FP64
 // root isolation.
-__device__ bool extended_vf_test(const v3 *X, const v3 *P, float th, VFResult &res) {
+//
+// Split in two so a kernel can keep the root isolation off its common path:
+// extended_vf_first answers for t = 0 and, when the cubic has no root near
+// [0, 1], for t = 1 (returns 1 hit, 0 no hit, 2 roots needed);
+// extended_vf_roots finishes a pair that needs roots (t = 0 is known not to
+// hit).  extended_vf_test is the composition.
+__device__ __forceinline__ void vf_coeffs(const v3 *X, const v3 *P, double a[4]) {
     v3 x0 = X[0], v0 = sub3(P[0], x0);
     v3 x1 = sub3(X[1], x0), x2 = sub3(X[2], x0), x3 = sub3(X[3], x0);
     v3 v1 = sub3(sub3(P[1], X[1]), v0), v2 = sub3(sub3(P[2], X[2]), v0),
        v3_ = sub3(sub3(P[3], X[3]), v0);
-    double a0 = stp(x1, x2, x3);
-    double a1 = stp(v1, x2, x3) + stp(x1, v2, x3) + stp(x1, x2, v3_);
-    double a2 = stp(x1, v2, v3_) + stp(v1, x2, v3_) + stp(v1, v2, x3);
-    double a3 = stp(v1, v2, v3_);
-    if (vf_eval_at(X, P, th, 0.0, res)) return true;
-    if (no_root_near_unit(a0, a1, a2, a3)) return vf_eval_at(X, P, th, 1.0, res);
+    a[0] = stp(x1, x2, x3);
+    a[1] = stp(v1, x2, x3) + stp(x1, v2, x3) + stp(x1, x2, v3_);
+    a[2] = stp(x1, v2, v3_) + stp(v1, x2, v3_) + stp(v1, v2, x3);
+    a[3] = stp(v1, v2, v3_);
+}
+
+__device__ __forceinline__ int extended_vf_first(const v3 *X, const v3 *P, float th,
+                                                 VFResult &res) {
+    double a[4];
+    vf_coeffs(X, P, a);
+    if (vf_eval_at(X, P, th, 0.0, res)) return 1;
+    if (no_root_near_unit(a[0], a[1], a[2], a[3])) return vf_eval_at(X, P, th, 1.0, res) ? 1 : 0;
+    return 2;
+}
+
+__device__ bool extended_vf_roots(const v3 *X, const v3 *P, float th, VFResult &res) {
+    double a[4];
+    vf_coeffs(X, P, a);
+    const double a0 = a[0], a1 = a[1], a2 = a[2], a3 = a[3];
     double t[5];
     int nsol = solve_cubic(a3, a2, a1, a0, t);
     t[nsol] = 1;
@@ -199,6 +223,12 @@ __device__ bool extended_vf_test(const v3 *X, const v3 *P, float th, VFResult &r
         if (vf_eval_at(X, P, th, t[i], res)) return true;
     }
     return false;
+}
+
+__device__ bool extended_vf_test(const v3 *X, const v3 *P, float th, VFResult &res) {
+    int r = extended_vf_first(X, P, th, res);
+    if (r != 2) return r == 1;
+    return extended_vf_roots(X, P, th, res);
 }
 
 // closest distance from point p to triangle abc (Ericson, Real-Time

@@ -8,22 +8,27 @@
 //   2. stable radix sort of (bucket, triangle id) and a bucket -> [start, end)
 //      table (the reference's cellStart/cellEnd, reset each update) plus the
 //      union of the swept AABBs of each bucket's triangles;
-//   3. cell tasks: one warp per point, one lane per cell of the union of the
-//      27-cell neighbourhoods of the centroid cells of its incident triangles
-//      (CCD_SH_Extended, P/CCD.cpp:1541-1586, tests every (point, neighbour)
-//      pair; the union holds each distinct pair once); a cell whose bucket
-//      AABB misses the point's grown swept AABB yields no task;
-//   4. one thread per task scans the bucket's entries (sorted-order copies of
-//      cell and AABB): exact-cell check and swept-AABB overlap with margin
-//      5.5 h; the survivors, one thread each, then need a lower bound on the
-//      point-triangle distance over the step of at most 4.5 h (a hit needs it
-//      below 3.61 h) to become candidates.  Neither filter can reject a pair
-//      ExtendedVFTest would accept.
-// Narrowphase: one thread per candidate runs ExtendedVFTest
-// (P/CCD.cpp:1733-1808) with the reference's arithmetic: float triple
-// products widened to double, the double cubic solve (P/CCD.cpp:48-113), the
-// float barycentric inside test.  Contacts are kept in discovery order on the
-// device and sorted by (point, triangle) only when copied out.
+//   3. candidate search (k_point_pairs): one warp per point, one lane per
+//      cell of the union of the 27-cell neighbourhoods of the centroid cells
+//      of its incident triangles (CCD_SH_Extended, P/CCD.cpp:1541-1586,
+//      tests every (point, neighbour) pair; the union holds each distinct
+//      pair once); a cell whose bucket AABB misses the point's swept AABB
+//      grown by 3.61 h yields nothing; the kept buckets' entries are spread
+//      over the lanes (warp prefix sum), each entry checked for its exact
+//      cell and swept-AABB overlap;
+//   4. distance filter: a pair survives when a lower bound of the
+//      point-triangle distance over the step is within the pair's own reach
+//      sqrt((2h)^2 + r^2), r = 2h * longest / mean edge (at most 3.61 h).
+//      Neither filter can reject a pair ExtendedVFTest would accept.
+// Narrowphase: ExtendedVFTest (P/CCD.cpp:1733-1808) with the reference's
+// arithmetic: float triple products widened to double, the double cubic
+// solve (P/CCD.cpp:48-113), the float barycentric inside test.  One thread
+// per candidate evaluates t = 0 and, when the cubic has no root near [0, 1],
+// t = 1; the few pairs that need the roots are compacted into a list that a
+// second kernel solves on full warps (the FP64 root isolation is slow on
+// this GPU and would otherwise stall nearly every warp).  Contacts are kept
+// in discovery order on the device and sorted by (point, triangle) only
+// when copied out.
 // Response: per pass every contact computes its four corrections from the
 // pass-start positions (VFResolveTest + VFResolveNew, P/CCD.cpp:1996-2090)
 // and adds them to per-point sums in 2^-32 m fixed point (integer atomics:
@@ -353,13 +358,31 @@ __global__ void __launch_bounds__(256) k_dist_filter(const int2 *__restrict__ pa
     }
 }
 
+__device__ __forceinline__ void store_contact(int *counters, long long ccap, int2 c, int4 f,
+                                              const VFResult &r, int4 *cids, int *cface,
+                                              float4 *ctn, double4 *cw) {
+    int slot = agg_inc(counters + 1);
+    if (slot >= ccap) {
+        atomicOr(counters + 2, 2);
+        return;
+    }
+    cids[slot] = make_int4(c.x, f.x, f.y, f.z);
+    cface[slot] = c.y;
+    ctn[slot] = make_float4(r.t, r.n.x, r.n.y, r.n.z);
+    cw[slot] = make_double4(r.w[0], r.w[1], r.w[2], r.w[3]);
+}
+
+// narrow phase, common path: t = 0, and t = 1 when the coplanarity cubic has
+// no root near [0, 1]; a pair that needs the cubic's roots goes to the hard
+// list (counters[3]) so that the FP64 root isolation runs on full warps in
+// k_narrow_roots instead of stalling the warps of the common path
 __global__ void __launch_bounds__(128) k_narrow(const int2 *__restrict__ cand, long long cap,
                                                 int nt, float th,
                                                 const int4 *__restrict__ tri,
                                                 const float4 *__restrict__ x,
                                                 const float4 *__restrict__ p, int *counters,
                                                 long long ccap, int4 *cids, int *cface,
-                                                float4 *ctn, double4 *cw) {
+                                                float4 *ctn, double4 *cw, int *hard) {
     long long n = counters[0];
     if (n > cap) n = cap;
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
@@ -369,16 +392,28 @@ __global__ void __launch_bounds__(128) k_narrow(const int2 *__restrict__ cand, l
         v3 X[4] = {ld3(x[c.x]), ld3(x[f.x]), ld3(x[f.y]), ld3(x[f.z])};
         v3 P[4] = {ld3(p[c.x]), ld3(p[f.x]), ld3(p[f.y]), ld3(p[f.z])};
         VFResult r;
-        if (!extended_vf_test(X, P, th, r)) continue;
-        int slot = agg_inc(counters + 1);
-        if (slot >= ccap) {
-            atomicOr(counters + 2, 2);
-            continue;
-        }
-        cids[slot] = make_int4(c.x, f.x, f.y, f.z);
-        cface[slot] = c.y;
-        ctn[slot] = make_float4(r.t, r.n.x, r.n.y, r.n.z);
-        cw[slot] = make_double4(r.w[0], r.w[1], r.w[2], r.w[3]);
+        int q = extended_vf_first(X, P, th, r);
+        if (q == 1) store_contact(counters, ccap, c, f, r, cids, cface, ctn, cw);
+        if (q == 2) hard[agg_inc(counters + 3)] = (int)i;  // at most one entry per candidate
+    }
+}
+
+// narrow phase, hard pairs: the cubic's roots in [0, 1] and t = 1
+__global__ void __launch_bounds__(128) k_narrow_roots(const int2 *__restrict__ cand, float th,
+                                                      const int4 *__restrict__ tri,
+                                                      const float4 *__restrict__ x,
+                                                      const float4 *__restrict__ p,
+                                                      int *counters, long long ccap, int4 *cids,
+                                                      int *cface, float4 *ctn, double4 *cw,
+                                                      const int *__restrict__ hard) {
+    const int n = counters[3];
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+        int2 c = cand[hard[k]];
+        int4 f = tri[c.y];
+        v3 X[4] = {ld3(x[c.x]), ld3(x[f.x]), ld3(x[f.y]), ld3(x[f.z])};
+        v3 P[4] = {ld3(p[c.x]), ld3(p[f.x]), ld3(p[f.y]), ld3(p[f.z])};
+        VFResult r;
+        if (extended_vf_roots(X, P, th, r)) store_contact(counters, ccap, c, f, r, cids, cface, ctn, cw);
     }
 }
 
@@ -533,6 +568,7 @@ int shs_update(pbd_shs *h) {
 static int colli_alloc(pbd_colli *c) {
     pbd_object *o = c->obj;
     PBD_TRY(c->cand.alloc(c->cand_cap));
+    PBD_TRY(c->hard.alloc(c->cand_cap));
     PBD_TRY(c->pairs.alloc(c->task_cap));
     PBD_TRY(c->counters.alloc(16));
     size_t H = (size_t)c->contact_cap;
@@ -562,10 +598,11 @@ int ccd_detect(pbd_colli *c) {
     PBD_TRY(shs_update(h));
     GridParams g = params_of(h);
     float th = c->thickness;
-    // per-axis reach of a hit: 2h off the plane + 3h inside the triangle grown
-    // by the barycentric epsilon h / mean edge, with slack (the distance
-    // filter then applies each pair's own Euclidean reach, at most 3.61h)
-    float margin = 5.5f * th + 2e-6f;
+    // a hit needs the point within sqrt((2h)^2 + r^2) of the triangle, r =
+    // 2h * (longest edge / mean edge) <= 3h (the distance filter's bound),
+    // so within 3.606h on every axis: the point's swept box is grown by that
+    // with slack (the filter then applies each pair's own reach)
+    float margin = 3.61f * th * 1.001f + 2e-6f;
 
     k_point_pairs<<<grid_for((long long)o->n * 32, 32 * kTaskWarps), 32 * kTaskWarps, 0, s>>>(
         o->n, g, margin, o->pt_tri_first.p, o->pt_tri_last.p, o->pt_tri.p,
@@ -579,7 +616,11 @@ int ccd_detect(pbd_colli *c) {
     PBD_LAUNCH();
     k_narrow<<<kPersistentBlocks, 128, 0, s>>>(c->cand.p, c->cand_cap, o->nt, th, o->tri.p,
                                                o->x.p, o->p.p, c->counters.p, c->contact_cap,
-                                               c->cids.p, c->cface.p, c->ctn.p, c->cw.p);
+                                               c->cids.p, c->cface.p, c->ctn.p, c->cw.p,
+                                               c->hard.p);
+    k_narrow_roots<<<kPersistentBlocks, 128, 0, s>>>(c->cand.p, th, o->tri.p, o->x.p, o->p.p,
+                                                     c->counters.p, c->contact_cap, c->cids.p,
+                                                     c->cface.p, c->ctn.p, c->cw.p, c->hard.p);
     k_clamp_counts<<<1, 32, 0, s>>>(c->counters.p, c->cand_cap, c->contact_cap);
     PBD_LAUNCH();
     if (c->ee_on) PBD_TRY(ee_detect(c));

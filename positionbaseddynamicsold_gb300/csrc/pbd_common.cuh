@@ -265,8 +265,9 @@ struct pbd_colli {
     // candidates (point, triangle)
     pbd::DBuf<int2> pairs;      // AABB-overlapping (point, triangle)
     pbd::DBuf<int2> cand;
-    pbd::DBuf<int> counters;    // [0] candidates, [1] contacts, [2] overflow flags, [3] unused,
-                                // [4] AABB pairs
+    pbd::DBuf<int> counters;    // [0] candidates, [1] contacts, [2] overflow flags, [3] hard
+                                // candidates (cubic roots needed), [4] AABB pairs
+    pbd::DBuf<int> hard;        // candidate indices that need the cubic's roots
     // contacts, in the order the narrow phase found them
     pbd::DBuf<int4> cids;               // i0..i3
     pbd::DBuf<int> cface;

@@ -7,8 +7,10 @@ mlp: a 1024 x 1024 hanging cloth (1,048,576 points, inputs far larger than
      L2), the trained warm start applied once to the advected positions
      (k_eval_hinges, k_mlp_infer) and one training pass over the same points'
      features (k_mlp_train).
-ccd: the drape256 scene after 60 substeps, one CCD pass (k_point_pairs,
-     k_dist_filter, k_narrow).
+ccd: the drape256 scene after 160 substeps (the cloth lies on the sphere),
+     one CCD pass (k_point_pairs, k_dist_filter, k_narrow).
+ccd_fold: the fold1024 scene (1,048,576 points, ground plane) after 120
+     substeps, one CCD pass.
 Each case runs its kernels once after one warm-up call, so `-c` small
 captures the steady-state launch.
 """
@@ -46,16 +48,19 @@ def case_mlp():
     print("mlp case done: %d points" % obj.n_points)
 
 
-def case_ccd():
-    sc = scenes.drape_over_sphere(res=256, seed=0)
+def _ccd(sc, log2, substeps):
     obj = PBDObject(sc, damping=1.0, gravity=G)
     obj.prepare()
-    shs = SpatialHashSystem(obj, cell_size=sc["colli"]["cell"], log2_table=20)
+    shs = SpatialHashSystem(obj, cell_size=sc["colli"]["cell"], log2_table=log2)
     shs.init()
     cs = CollisionSolver(obj, shs, thickness=sc["colli"]["thickness"], iterations=1,
                          response=RESPONSE_MASS_WEIGHTED)
+    n = obj.n_points
+    cs.set_capacity(max(1 << 22, 64 * n), max(1 << 20, 4 * n))
     s = SolverPBD(obj)
-    s.step(DT, substeps=60, iterations=15, colli=cs, use_graph=True)
+    if "ground" in sc["colli"]:
+        s.set_ground(True, sc["colli"]["ground"])
+    s.step(DT, substeps=substeps, iterations=15, colli=cs, use_graph=True)
     s.advect(DT)
     for _ in range(2):           # warm-up + profiled
         cs.ccd_sh_extended()
@@ -63,5 +68,13 @@ def case_ccd():
     print("ccd case done: %s" % cs.stats())
 
 
+def case_ccd():
+    _ccd(scenes.drape_over_sphere(res=256, seed=0), 20, 160)
+
+
+def case_ccd_fold():
+    _ccd(scenes.folding_cloth(res=1024, seed=0), 24, 120)
+
+
 if __name__ == "__main__":
-    {"mlp": case_mlp, "ccd": case_ccd}[sys.argv[1]]()
+    {"mlp": case_mlp, "ccd": case_ccd, "ccd_fold": case_ccd_fold}[sys.argv[1]]()
