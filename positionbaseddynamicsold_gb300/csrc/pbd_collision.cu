@@ -187,6 +187,9 @@ __global__ void __launch_bounds__(32 * kTaskWarps) k_point_pairs(
     const int warp0 = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int nwarps = (gridDim.x * blockDim.x) >> 5;
     for (int v = warp0; v < n; v += nwarps) {
+        // the point's own positions first: their loads overlap the chain
+        // point -> incident triangles -> their cells
+        const float4 xv = x[v], pv = p[v];
         int f0 = pt_first[v], f1 = pt_last[v];
         int ninc = f1 - f0;
         if (ninc > kMaxInc) {
@@ -202,6 +205,14 @@ __global__ void __launch_bounds__(32 * kTaskWarps) k_point_pairs(
         }
         const unsigned vm = __ballot_sync(0xffffffffu, valid);
         if (!vm) continue;
+        // distinct valid incident cells: the lowest lane of each group of
+        // lanes holding the same cell
+        const unsigned same = __match_any_sync(0xffffffffu, valid ? mc.x : INT_MIN) &
+                              __match_any_sync(0xffffffffu, valid ? mc.y : INT_MIN) &
+                              __match_any_sync(0xffffffffu, valid ? mc.z : INT_MIN);
+        const unsigned dm =
+            __ballot_sync(0xffffffffu, valid && (same & vm & ((1u << lane) - 1u)) == 0u);
+        const bool single = __popc(dm) == 1;
         // bounding box of the valid incident cells
         int lx = valid ? mc.x : INT_MAX, ly = valid ? mc.y : INT_MAX, lz = valid ? mc.z : INT_MAX;
         int hx = valid ? mc.x : INT_MIN, hy = valid ? mc.y : INT_MIN, hz = valid ? mc.z : INT_MIN;
@@ -214,20 +225,30 @@ __global__ void __launch_bounds__(32 * kTaskWarps) k_point_pairs(
             hy = max(hy, __shfl_xor_sync(0xffffffffu, hy, o));
             hz = max(hz, __shfl_xor_sync(0xffffffffu, hz, o));
         }
-        v3 X0 = ld3(x[v]), P0 = ld3(p[v]);
+        v3 X0 = ld3(xv), P0 = ld3(pv);
         const float plx = fminf(X0.x, P0.x) - margin, phx = fmaxf(X0.x, P0.x) + margin;
         const float ply = fminf(X0.y, P0.y) - margin, phy = fmaxf(X0.y, P0.y) + margin;
         const float plz = fminf(X0.z, P0.z) - margin, phz = fmaxf(X0.z, P0.z) + margin;
         const int ex = hx - lx + 3, ey = hy - ly + 3, ez = hz - lz + 3;
-        const int ncell = ex * ey * ez;
+        const int exy = ex * ey, ncell = exy * ez;
+        // ci -> (x, y, z) in the box by multiplying with ceil(2^32 / d),
+        // exact for ci * d < 2^32 (ex, exy >= 3; ci < ncell); boxes too large
+        // for that divide
+        const bool magic = (unsigned long long)ncell * (unsigned long long)exy < (1ull << 32);
+        const unsigned mex = 0xffffffffu / (unsigned)ex + 1u;
+        const unsigned mexy = 0xffffffffu / (unsigned)exy + 1u;
         for (int base = 0; base < ncell; base += 32) {
             const int ci = base + lane;
-            const int cx = lx - 1 + ci % ex;
-            const int cy = ly - 1 + (ci / ex) % ey;
-            const int cz = lz - 1 + ci / (ex * ey);
-            // within one cell of some valid incident cell (read from the lanes)
-            bool near = false;
-            unsigned m = vm;
+            const int qz = magic ? (int)__umulhi((unsigned)ci, mexy) : ci / exy;
+            const int rz = ci - qz * exy;
+            const int qy = magic ? (int)__umulhi((unsigned)rz, mex) : rz / ex;
+            const int cx = lx - 1 + (rz - qy * ex);
+            const int cy = ly - 1 + qy;
+            const int cz = lz - 1 + qz;
+            // within one cell of some valid incident cell (read from the lanes
+            // holding the distinct cells; with one cell every box cell is)
+            bool near = single;
+            unsigned m = single ? 0u : dm;
             while (m) {
                 const int src = __ffs(m) - 1;
                 m &= m - 1;
@@ -431,6 +452,11 @@ __global__ void __launch_bounds__(128) k_contact_deltas(const int *counters, con
                                                         const float4 *__restrict__ p, float th,
                                                         int mass_weighted, long long *acc,
                                                         int *acnt) {
+    // launched as a programmatic dependent of the sweep's last color phase:
+    // nothing is read before that phase has completed; the apply kernel may
+    // then launch while the corrections are summed
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    asm volatile("griddepcontrol.launch_dependents;");
     int n = counters[1];
     for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < n; c += gridDim.x * blockDim.x) {
         int4 id = ids[c];
@@ -490,6 +516,7 @@ __global__ void __launch_bounds__(128) k_contact_deltas(const int *counters, con
 
 // every point with a correction: p += sum * 2^-32 / count; sums cleared
 __global__ void k_apply_deltas(int n, long long *acc, int *acnt, float4 *p) {
+    asm volatile("griddepcontrol.wait;" ::: "memory");  // every sum is complete
     for (int pt = blockIdx.x * blockDim.x + threadIdx.x; pt < n; pt += gridDim.x * blockDim.x) {
         int cnt = acnt[pt];
         if (cnt <= 0) continue;
@@ -631,14 +658,27 @@ int ccd_resolve(pbd_colli *c, int passes) {
     pbd_object *o = c->obj;
     cudaStream_t s = o->stream;
     if (!c->cand.p || o->nt == 0) return PBD_OK;
+    // both kernels are programmatic dependents of the kernel before them
+    // (their first instruction waits for it), so their launch overlaps it
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cudaLaunchConfig_t cd = {}, ca = {};
+    cd.gridDim = dim3(kPersistentBlocks);
+    cd.blockDim = dim3(128);
+    ca.gridDim = dim3(grid_for(o->n, 256));
+    ca.blockDim = dim3(256);
+    cd.stream = ca.stream = s;
+    cd.attrs = ca.attrs = at;
+    cd.numAttrs = ca.numAttrs = o->pdl ? 1 : 0;
     for (int k = 0; k < passes; ++k) {
-        k_contact_deltas<<<kPersistentBlocks, 128, 0, s>>>(c->counters.p, c->cids.p, o->x.p, o->p.p,
-                                                           c->thickness,
-                                                           c->response == PBD_RESPONSE_MASS_WEIGHTED,
-                                                           c->acc.p, c->acnt.p);
+        PBD_CUDA(cudaLaunchKernelEx(&cd, k_contact_deltas, (const int *)c->counters.p,
+                                    (const int4 *)c->cids.p, (const float4 *)o->x.p,
+                                    (const float4 *)o->p.p, c->thickness,
+                                    (int)(c->response == PBD_RESPONSE_MASS_WEIGHTED), c->acc.p,
+                                    c->acnt.p));
         if (c->ee_on) PBD_TRY(ee_deltas_launch(c));
-        k_apply_deltas<<<grid_for(o->n, 256), 256, 0, s>>>(o->n, c->acc.p, c->acnt.p, o->p.p);
-        PBD_LAUNCH();
+        PBD_CUDA(cudaLaunchKernelEx(&ca, k_apply_deltas, o->n, c->acc.p, c->acnt.p, o->p.p));
     }
     return PBD_OK;
 }
