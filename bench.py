@@ -88,12 +88,14 @@ def make_workload(name):
     if name == "batch512":
         sc = scenes.batched_cloths(512, seed=0)
         sc["colli"] = {"cell": 2.0 * scenes.mean_rest_edge(sc), "thickness": 1e-3,
-                       "spheres": sc["spheres"]}
+                       "spheres": sc["spheres"], "instance_cells": scenes.instance_cells(sc)}
         cfg = {"workload": "batch512: 512 cloths, side U{16..128}, random pins, one sphere each, "
-                           "self CCD per instance, all in one launch per color phase",
+                           "self CCD per instance (hash cell 2 x each cloth's mean rest edge), "
+                           "all in one launch per color phase",
                "instances": 512, "substep_dt": DT, "gs_iterations": ITERS,
                "ccd_passes_per_substep": 3, "hash_buckets": 2 ** 24, "thickness": 1e-3,
-               "cell": sc["colli"]["cell"]}
+               "cell_per_instance": [float(sc["colli"]["instance_cells"].min()),
+                                     float(sc["colli"]["instance_cells"].max())]}
         return sc, cfg, True, 24
     if name == "hanging32":
         sc = scenes.hanging_cloth(32, seed=0)
@@ -169,6 +171,8 @@ def setup(sc, colli_on, table_log2):
             solver.set_ground(True, sc["colli"]["ground"])
         if "spheres" in sc["colli"]:
             solver.set_instance_spheres(sc["colli"]["spheres"])
+        if "instance_cells" in sc["colli"]:
+            shs.set_instance_cells(sc["colli"]["instance_cells"])
     return obj, solver, shs, cs
 
 

@@ -279,6 +279,12 @@ int pbd_shs_create(pbd_object *obj, const float *grid_center, const int *grid_si
 int pbd_shs_create_hashed(pbd_object *obj, const float *cell_size, int log2_table,
                           pbd_shs **out);
 int pbd_shs_destroy(pbd_shs *shs);
+/* Hashed grid only (no reference counterpart; the reference hashes one
+ * object): a cell size per instance (3 floats each, n = number of
+ * instances), so every batched cloth is binned with the cells it would get
+ * alone -- the per-instance hash tables of a batch; n = 0 returns to the one
+ * cell size. */
+int pbd_shs_set_instance_cells(pbd_shs *shs, int n, const float *cells3);
 int pbd_shs_set_grid_center(pbd_shs *shs, const float *center);
 int pbd_shs_set_grid_size(pbd_shs *shs, const int *size);
 int pbd_shs_set_division(pbd_shs *shs, const float *cell_size);

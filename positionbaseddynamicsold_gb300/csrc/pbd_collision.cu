@@ -55,17 +55,19 @@ constexpr int kMaxInc = 16;  // incident triangles considered per point
 
 // ---------------------------------------------------------------------------
 __global__ void k_reset_buckets(const uint32_t *skey, const int *n_prev, uint32_t nb,
-                                int2 *brange, long long cap) {
+                                float4 *btab, long long cap) {
     long long n = *n_prev;
     if (n > cap) n = cap;
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
          i += (long long)gridDim.x * blockDim.x) {
         uint32_t k = skey[i];
-        if (k < nb) brange[k] = make_int2(0, 0);
+        if (k < nb) btab[2 * (size_t)k] = make_float4(0.f, 0.f, 0.f, 0.f);  // empty range
     }
 }
 
 __global__ void __launch_bounds__(256) k_tri_cells(int nt, GridParams g, float margin,
+                                                   const float4 *__restrict__ inst_cell,
+                                                   int n_inst_cell,
                                                    const int4 *__restrict__ tri,
                                                    const float4 *__restrict__ x,
                                                    const float4 *__restrict__ p, int4 *tcell,
@@ -80,9 +82,14 @@ __global__ void __launch_bounds__(256) k_tri_cells(int nt, GridParams g, float m
         float cx = (a.x + b.x + c.x) / 3.0f;
         float cy = (a.y + b.y + c.y) / 3.0f;
         float cz = (a.z + b.z + c.z) / 3.0f;
-        int ix = (int)floorf((cx - g.start.x) / g.cell.x);
-        int iy = (int)floorf((cy - g.start.y) / g.cell.y);
-        int iz = (int)floorf((cz - g.start.z) / g.cell.z);
+        float3 cell = g.cell;
+        if (f.w >= 0 && f.w < n_inst_cell) {
+            float4 ic = inst_cell[f.w];
+            cell = make_float3(ic.x, ic.y, ic.z);
+        }
+        int ix = (int)floorf((cx - g.start.x) / cell.x);
+        int iy = (int)floorf((cy - g.start.y) / cell.y);
+        int iz = (int)floorf((cz - g.start.z) / cell.z);
         valid = g.hashed || !outside(g, ix, iy, iz);
         tcell[t] = make_int4(ix, iy, iz, f.w);
         key[t] = valid ? bucket_of(g, ix, iy, iz, f.w) : g.nb;
@@ -108,16 +115,16 @@ __global__ void __launch_bounds__(256) k_tri_cells(int nt, GridParams g, float m
 
 __global__ void k_bucket_ranges(const uint32_t *skey, const int *sid, const int *n_valid,
                                 const int4 *tcell, const float4 *tlo, const float4 *thi,
-                                int2 *brange, float4 *blo, float4 *bhi, int4 *scell,
-                                float4 *slo, float4 *shi) {
+                                float4 *btab, float4 *etab) {
     int n = *n_valid;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         uint32_t k = skey[i];
         int t = sid[i];
         int4 c = tcell[t];
-        scell[i] = make_int4(c.x, c.y, c.z, t);  // w = triangle id
-        slo[i] = tlo[t];
-        shi[i] = thi[t];
+        etab[3 * (size_t)i] = make_float4(__int_as_float(c.x), __int_as_float(c.y),
+                                          __int_as_float(c.z), __int_as_float(t));
+        etab[3 * (size_t)i + 1] = tlo[t];
+        etab[3 * (size_t)i + 2] = thi[t];
         if (i > 0 && skey[i - 1] == k) continue;
         float4 lo = tlo[sid[i]], hi = thi[sid[i]];
         int e = i + 1;
@@ -126,16 +133,15 @@ __global__ void k_bucket_ranges(const uint32_t *skey, const int *sid, const int 
             lo.x = fminf(lo.x, a.x); lo.y = fminf(lo.y, a.y); lo.z = fminf(lo.z, a.z);
             hi.x = fmaxf(hi.x, b.x); hi.y = fmaxf(hi.y, b.y); hi.z = fmaxf(hi.z, b.z);
         }
-        brange[k] = make_int2(i, e);
-        blo[k] = lo;
-        bhi[k] = hi;
+        btab[2 * (size_t)k] = make_float4(__int_as_float(i), __int_as_float(e), lo.x, lo.y);
+        btab[2 * (size_t)k + 1] = make_float4(lo.z, hi.x, hi.y, hi.z);
     }
 }
 
 // FindNeighbors (P/SpatialHashSystem.cpp:134-187) for every triangle:
 // count (out == nullptr) or fill
-__global__ void k_find_neighbors(int nt, GridParams g, const int4 *tcell, const int2 *brange,
-                                 const int4 *scell, const int *sid, const int *off, int *cnt,
+__global__ void k_find_neighbors(int nt, GridParams g, const int4 *tcell, const float4 *btab,
+                                 const float4 *etab, const int *sid, const int *off, int *cnt,
                                  int *out) {
     int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= nt) return;
@@ -147,9 +153,12 @@ __global__ void k_find_neighbors(int nt, GridParams g, const int4 *tcell, const 
                 for (int x = -1; x <= 1; ++x) {
                     int nx = c.x + x, ny = c.y + y, nz = c.z + z;
                     if (!g.hashed && outside(g, nx, ny, nz)) continue;
-                    int2 r = brange[bucket_of(g, nx, ny, nz, c.w)];
+                    float4 b0 = btab[2 * (size_t)bucket_of(g, nx, ny, nz, c.w)];
+                    int2 r = make_int2(__float_as_int(b0.x), __float_as_int(b0.y));
                     for (int i = r.x; i < r.y; ++i) {
-                        int4 sc = scell[i];
+                        float4 e0 = etab[3 * (size_t)i];
+                        int4 sc = make_int4(__float_as_int(e0.x), __float_as_int(e0.y),
+                                            __float_as_int(e0.z), __float_as_int(e0.w));
                         if (sc.x != nx || sc.y != ny || sc.z != nz) continue;
                         int id = sc.w;
                         if (id == t) continue;
@@ -179,9 +188,7 @@ __global__ void __launch_bounds__(32 * kTaskWarps) k_point_pairs(
     const int *__restrict__ pt_last, const int *__restrict__ pt_tri,
     const int *__restrict__ point_inst, const int *__restrict__ tri_inst,
     const float4 *__restrict__ x, const float4 *__restrict__ p, const int4 *__restrict__ tcell,
-    const int2 *__restrict__ brange, const float4 *__restrict__ blo,
-    const float4 *__restrict__ bhi, const int4 *__restrict__ scell,
-    const float4 *__restrict__ slo, const float4 *__restrict__ shi, int2 *pairs, long long cap,
+    const float4 *__restrict__ btab, const float4 *__restrict__ etab, int2 *pairs, long long cap,
     int *counters) {
     const int lane = threadIdx.x & 31;
     const int warp0 = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -260,14 +267,13 @@ __global__ void __launch_bounds__(32 * kTaskWarps) k_point_pairs(
             int cnt = 0, start = 0;
             if (ci < ncell && near && (g.hashed || !outside(g, cx, cy, cz))) {
                 const uint32_t b = bucket_of(g, cx, cy, cz, inst);
-                const int2 r = brange[b];
-                if (r.x < r.y) {
-                    const float4 bl = blo[b], bh = bhi[b];
-                    if (!(plx > bh.x || phx < bl.x || ply > bh.y || phy < bl.y || plz > bh.z ||
-                          phz < bl.z)) {
-                        cnt = r.y - r.x;
-                        start = r.x;
-                    }
+                // range and box in one sector, loaded together
+                const float4 b0 = btab[2 * (size_t)b], b1 = btab[2 * (size_t)b + 1];
+                const int rs = __float_as_int(b0.x), re = __float_as_int(b0.y);
+                if (rs < re && !(plx > b1.y || phx < b0.z || ply > b1.z || phy < b0.w ||
+                                 plz > b1.w || phz < b1.x)) {
+                    cnt = re - rs;
+                    start = rs;
                 }
             }
             // flat entry index space of this round's kept buckets
@@ -296,9 +302,12 @@ __global__ void __launch_bounds__(32 * kTaskWarps) k_point_pairs(
                 const int oz = __shfl_sync(0xffffffffu, cz, own);
                 if (f >= total) continue;
                 const int e = o_start + (f - o_excl);
-                const int4 sc = scell[e];
+                // the entry's cell, id and box: 48 contiguous bytes, loaded together
+                const float4 e0 = etab[3 * (size_t)e], tl = etab[3 * (size_t)e + 1],
+                             th = etab[3 * (size_t)e + 2];
+                const int4 sc = make_int4(__float_as_int(e0.x), __float_as_int(e0.y),
+                                          __float_as_int(e0.z), __float_as_int(e0.w));
                 if (sc.x != ox || sc.y != oy || sc.z != oz) continue;
-                const float4 tl = slo[e], th = shi[e];
                 if (plx > th.x || phx < tl.x || ply > th.y || phy < tl.y || plz > th.z ||
                     phz < tl.z)
                     continue;
@@ -576,18 +585,18 @@ int shs_update(pbd_shs *h) {
     GridParams g = params_of(h);
     if (o->nt == 0) return PBD_OK;
     // clear the ranges of the buckets the previous update filled
-    k_reset_buckets<<<kPersistentBlocks, 256, 0, s>>>(h->skey, h->n_valid.p, g.nb, h->brange.p,
+    k_reset_buckets<<<kPersistentBlocks, 256, 0, s>>>(h->skey, h->n_valid.p, g.nb, h->btab.p,
                                                       o->nt);
     PBD_CUDA(cudaMemsetAsync(h->n_valid.p, 0, sizeof(int), s));
-    k_tri_cells<<<grid_for(o->nt, 256), 256, 0, s>>>(o->nt, g, 0.0f, o->tri.p, o->x.p, o->p.p,
+    k_tri_cells<<<grid_for(o->nt, 256), 256, 0, s>>>(o->nt, g, 0.0f, h->inst_cell.p,
+                                                     h->n_inst_cell, o->tri.p, o->x.p, o->p.p,
                                                      h->tcell.p, h->tlo.p, h->thi.p, h->key.p,
                                                      h->id.p, h->n_valid.p);
     PBD_LAUNCH();
     PBD_TRY(radix_sort<uint32_t>(h->key.p, h->id.p, h->key_alt.p, h->id_alt.p, o->nt, nullptr,
                                  round8(h->key_bits), h->scr, s, &h->skey, &h->sid));
     k_bucket_ranges<<<kPersistentBlocks, 256, 0, s>>>(h->skey, h->sid, h->n_valid.p, h->tcell.p,
-                                                      h->tlo.p, h->thi.p, h->brange.p, h->blo.p,
-                                                      h->bhi.p, h->scell.p, h->slo.p, h->shi.p);
+                                                      h->tlo.p, h->thi.p, h->btab.p, h->etab.p);
     PBD_LAUNCH();
     return PBD_OK;
 }
@@ -634,8 +643,7 @@ int ccd_detect(pbd_colli *c) {
     k_point_pairs<<<grid_for((long long)o->n * 32, 32 * kTaskWarps), 32 * kTaskWarps, 0, s>>>(
         o->n, g, margin, o->pt_tri_first.p, o->pt_tri_last.p, o->pt_tri.p,
         o->has_inst ? o->point_inst.p : nullptr, o->has_inst ? o->tri_inst.p : nullptr, o->x.p,
-        o->p.p, h->tcell.p, h->brange.p, h->blo.p, h->bhi.p, h->scell.p, h->slo.p, h->shi.p,
-        c->pairs.p, c->task_cap, c->counters.p);
+        o->p.p, h->tcell.p, h->btab.p, h->etab.p, c->pairs.p, c->task_cap, c->counters.p);
     PBD_LAUNCH();
     k_dist_filter<<<kPersistentBlocks, 256, 0, s>>>(c->pairs.p, c->task_cap, th, o->tri.p,
                                                     o->x.p, o->p.p, c->cand.p, c->cand_cap,
@@ -699,16 +707,12 @@ static int shs_alloc(pbd_shs *h) {
     PBD_TRY(h->key_alt.alloc(nt));
     PBD_TRY(h->id.alloc(nt));
     PBD_TRY(h->id_alt.alloc(nt));
-    PBD_TRY(h->scell.alloc(nt));
-    PBD_TRY(h->slo.alloc(nt));
-    PBD_TRY(h->shi.alloc(nt));
+    PBD_TRY(h->etab.alloc(3 * nt));
     PBD_TRY(h->n_valid.alloc(1));
-    PBD_TRY(h->brange.alloc((size_t)h->n_buckets + 1));
-    PBD_TRY(h->blo.alloc((size_t)h->n_buckets + 1));
-    PBD_TRY(h->bhi.alloc((size_t)h->n_buckets + 1));
+    PBD_TRY(h->btab.alloc(2 * ((size_t)h->n_buckets + 1)));
     PBD_TRY(h->scr.hist.alloc(radix_hist_size((long long)nt)));
     PBD_TRY(h->scr.carry.alloc(256));
-    PBD_CUDA(cudaMemsetAsync(h->brange.p, 0, sizeof(int2) * (h->n_buckets + 1), o->stream));
+    PBD_CUDA(cudaMemsetAsync(h->btab.p, 0, sizeof(float4) * 2 * (h->n_buckets + 1), o->stream));
     PBD_CUDA(cudaMemsetAsync(h->n_valid.p, 0, sizeof(int), o->stream));
     h->skey = h->key.p;
     h->sid = h->id.p;
@@ -776,7 +780,7 @@ int pbd_shs_set_grid_size(pbd_shs *h, const int *size) {
     h->n_buckets = (int)ncell;
     h->key_bits = bits_for(ncell);
     h->initialized = false;
-    h->brange.release();
+    h->btab.release();
     return PBD_OK;
 }
 
@@ -787,6 +791,22 @@ int pbd_shs_set_division(pbd_shs *h, const float *cell) {
     return PBD_OK;
 }
 
+int pbd_shs_set_instance_cells(pbd_shs *h, int n, const float *cells3) {
+    PBD_CHECK(h && n >= 0 && (n == 0 || cells3), PBD_ERR_ARG, "bad argument");
+    PBD_CHECK(n == 0 || h->hashed, PBD_ERR_STATE,
+              "per-instance cells need the hashed grid (pbd_shs_create_hashed)");
+    std::vector<float4> c(n);
+    for (int i = 0; i < n; ++i) {
+        PBD_CHECK(cells3[3 * i] > 0 && cells3[3 * i + 1] > 0 && cells3[3 * i + 2] > 0,
+                  PBD_ERR_ARG, "cell of instance %d is not positive", i);
+        c[i] = make_float4(cells3[3 * i], cells3[3 * i + 1], cells3[3 * i + 2], 0.f);
+    }
+    if (n) PBD_TRY(h->inst_cell.upload(c.data(), n, h->obj->stream));
+    PBD_CUDA(cudaStreamSynchronize(h->obj->stream));
+    h->n_inst_cell = n;
+    return PBD_OK;
+}
+
 int pbd_shs_init(pbd_shs *h) {
     PBD_CHECK(h, PBD_ERR_ARG, "null argument");
     // m_girdStartPos = center - (gridSize * cellSize) / 2 (P/SpatialHashSystem.cpp:91-94)
@@ -794,7 +814,7 @@ int pbd_shs_init(pbd_shs *h) {
         float shift = ((float)(unsigned)h->size[k] * h->cell[k]) / 2.0f;
         h->start[k] = h->center[k] - shift;
     }
-    if (!h->brange.p || h->brange.n < (size_t)h->n_buckets + 1) PBD_TRY(shs_alloc(h));
+    if (!h->btab.p || h->btab.n < 2 * ((size_t)h->n_buckets + 1)) PBD_TRY(shs_alloc(h));
     h->initialized = true;
     return shs_update(h);
 }
@@ -818,7 +838,7 @@ int pbd_shs_find_neighbors_all(pbd_shs *h, int *start_num, int *out, long long c
     PBD_TRY(off.alloc(nt));
     PBD_TRY(tot.alloc(1));
     GridParams g = params_of(h);
-    k_find_neighbors<<<grid_for(nt, 128), 128, 0, s>>>(nt, g, h->tcell.p, h->brange.p, h->scell.p,
+    k_find_neighbors<<<grid_for(nt, 128), 128, 0, s>>>(nt, g, h->tcell.p, h->btab.p, h->etab.p,
                                                        h->sid, nullptr, cnt.p, nullptr);
     PBD_LAUNCH();
     PBD_TRY(exclusive_scan(cnt.p, off.p, nt, tot.p, s));
@@ -840,8 +860,8 @@ int pbd_shs_find_neighbors_all(pbd_shs *h, int *start_num, int *out, long long c
         PBD_CHECK(cap >= t, PBD_ERR_OVERFLOW, "neighbor output needs %d entries", t);
         DBuf<int> dout;
         PBD_TRY(dout.alloc(t));
-        k_find_neighbors<<<grid_for(nt, 128), 128, 0, s>>>(nt, g, h->tcell.p, h->brange.p,
-                                                           h->scell.p, h->sid, off.p, nullptr,
+        k_find_neighbors<<<grid_for(nt, 128), 128, 0, s>>>(nt, g, h->tcell.p, h->btab.p,
+                                                           h->etab.p, h->sid, off.p, nullptr,
                                                            dout.p);
         PBD_LAUNCH();
         PBD_CUDA(cudaMemcpyAsync(out, dout.p, sizeof(int) * t, cudaMemcpyDeviceToHost, s));

@@ -245,12 +245,19 @@ struct pbd_shs {
     pbd::DBuf<int> id, id_alt;
     uint32_t *skey = nullptr;    // sorted result pointers (into key/key_alt)
     int *sid = nullptr;
-    pbd::DBuf<int4> scell;       // cell of sorted entry, w = triangle id
-    pbd::DBuf<float4> slo, shi;  // swept AABB of sorted entry
-    pbd::DBuf<int2> brange;      // bucket -> [start, end) in sorted order
-    pbd::DBuf<float4> blo, bhi;  // bucket -> union of its triangles' swept AABBs
+    // sorted entries, 3 float4 each (48 contiguous bytes): cell xyz and
+    // triangle id as int bits; the swept AABB's low corner; its high corner
+    pbd::DBuf<float4> etab;
+    // buckets, 2 float4 each (one 32-byte sector): [start, end) in sorted
+    // order as int bits, then the union of its triangles' swept AABBs
+    // (start, end, lo.x, lo.y), (lo.z, hi.x, hi.y, hi.z)
+    pbd::DBuf<float4> btab;
     pbd::DBuf<int> n_valid;
     pbd::SortScratch scr;
+    // hashed grid only: a cell size per instance (xyz, w unused), so each
+    // batched cloth gets the cells it would get alone; 0 instances = one cell
+    pbd::DBuf<float4> inst_cell;
+    int n_inst_cell = 0;
 };
 
 struct pbd_colli {

@@ -207,7 +207,19 @@ __device__ __forceinline__ int cell_of(float v, float start, float cell) {
 }
 
 // step 1: boxes and entries
+// the cell size of an instance (the spatial hash's per-instance cells, or
+// its one cell)
+__device__ __forceinline__ float3 inst_cell_of(const GridParams &g, const float4 *ic, int n_ic,
+                                               int inst) {
+    if (inst >= 0 && inst < n_ic) {
+        float4 c = ic[inst];
+        return make_float3(c.x, c.y, c.z);
+    }
+    return g.cell;
+}
+
 __global__ void __launch_bounds__(256) k_ee_entries(int ne, GridParams g, float grow,
+                                                    const float4 *__restrict__ icell, int n_icell,
                                                     const int2 *__restrict__ edges,
                                                     const int *__restrict__ point_inst,
                                                     const float4 *__restrict__ x,
@@ -226,24 +238,25 @@ __global__ void __launch_bounds__(256) k_ee_entries(int ne, GridParams g, float 
                             fmaxf(fmaxf(xa.z, xb.z), fmaxf(pa.z, pb.z)) + grow, 0.f);
     elo[e] = lo;
     ehi[e] = hi;
-    float ext[6] = {(lo.x - g.start.x) / g.cell.x, (lo.y - g.start.y) / g.cell.y,
-                    (lo.z - g.start.z) / g.cell.z, (hi.x - g.start.x) / g.cell.x,
-                    (hi.y - g.start.y) / g.cell.y, (hi.z - g.start.z) / g.cell.z};
+    const int inst = point_inst ? point_inst[ed.x] : 0;
+    const float3 cl = inst_cell_of(g, icell, n_icell, inst);
+    float ext[6] = {(lo.x - g.start.x) / cl.x, (lo.y - g.start.y) / cl.y,
+                    (lo.z - g.start.z) / cl.z, (hi.x - g.start.x) / cl.x,
+                    (hi.y - g.start.y) / cl.y, (hi.z - g.start.z) / cl.z};
     for (int k = 0; k < 6; ++k)
         if (!(fabsf(ext[k]) < 1e9f)) {  // non-finite or far outside any grid
             atomicOr(counters + 2, 32);
             return;
         }
-    int x0 = cell_of(lo.x, g.start.x, g.cell.x), x1 = cell_of(hi.x, g.start.x, g.cell.x);
-    int y0 = cell_of(lo.y, g.start.y, g.cell.y), y1 = cell_of(hi.y, g.start.y, g.cell.y);
-    int z0 = cell_of(lo.z, g.start.z, g.cell.z), z1 = cell_of(hi.z, g.start.z, g.cell.z);
+    int x0 = cell_of(lo.x, g.start.x, cl.x), x1 = cell_of(hi.x, g.start.x, cl.x);
+    int y0 = cell_of(lo.y, g.start.y, cl.y), y1 = cell_of(hi.y, g.start.y, cl.y);
+    int z0 = cell_of(lo.z, g.start.z, cl.z), z1 = cell_of(hi.z, g.start.z, cl.z);
     long long nx = x1 - x0 + 1, ny = y1 - y0 + 1, nz = z1 - z0 + 1;
     long long nc = nx * ny * nz;
     if (nc <= 0 || nc > kEEMaxCells) {
         atomicOr(counters + 2, 32);
         return;
     }
-    int inst = point_inst ? point_inst[ed.x] : 0;
     // every slot below cap that the counter hands out is written, so the
     // first min(count, cap) entries are always valid
     long long base = atomicAdd(counters + kEntries, (int)nc);
@@ -268,6 +281,7 @@ __global__ void __launch_bounds__(256) k_ee_pairs(long long cap, const uint32_t 
                                                   const float4 *__restrict__ ehi,
                                                   const int2 *__restrict__ edges,
                                                   const int *__restrict__ point_inst, GridParams g,
+                                                  const float4 *__restrict__ icell, int n_icell,
                                                   int2 *pairs, long long pcap, int *counters) {
     long long n = counters[kEntries];
     if (n > cap) n = cap;
@@ -279,6 +293,7 @@ __global__ void __launch_bounds__(256) k_ee_pairs(long long cap, const uint32_t 
         const int2 E1 = edges[e1];
         const float4 lo1 = elo[e1], hi1 = ehi[e1];
         const int inst1 = point_inst ? point_inst[E1.x] : 0;
+        const float3 cl = inst_cell_of(g, icell, n_icell, inst1);
         for (long long j = i + 1; j < n && skey[j] == k; ++j) {
             const int4 cj = ecell[sval[j]];
             if (cj.x != ci.x || cj.y != ci.y || cj.z != ci.z) continue;
@@ -291,9 +306,9 @@ __global__ void __launch_bounds__(256) k_ee_pairs(long long cap, const uint32_t 
                 lo1.z > hi2.z || lo2.z > hi1.z)
                 continue;
             // the cell of the intersection's low corner reports the pair
-            if (cell_of(fmaxf(lo1.x, lo2.x), g.start.x, g.cell.x) != ci.x ||
-                cell_of(fmaxf(lo1.y, lo2.y), g.start.y, g.cell.y) != ci.y ||
-                cell_of(fmaxf(lo1.z, lo2.z), g.start.z, g.cell.z) != ci.z)
+            if (cell_of(fmaxf(lo1.x, lo2.x), g.start.x, cl.x) != ci.x ||
+                cell_of(fmaxf(lo1.y, lo2.y), g.start.y, cl.y) != ci.y ||
+                cell_of(fmaxf(lo1.z, lo2.z), g.start.z, cl.z) != ci.z)
                 continue;
             const long long slot = agg_inc(counters + kPairs);
             if (slot < pcap)
@@ -479,7 +494,8 @@ int ee_detect(pbd_colli *c) {
     const float th = c->thickness;
     const int *pinst = o->has_inst ? o->point_inst.p : nullptr;
     k_ee_entries<<<grid_for(c->ee_n, 256), 256, 0, s>>>(
-        c->ee_n, g, 2.f * th * 1.001f + 4e-6f, c->ee_edges.p, pinst, o->x.p, o->p.p, c->ee_lo.p,
+        c->ee_n, g, 2.f * th * 1.001f + 4e-6f, c->shs->inst_cell.p, c->shs->n_inst_cell,
+        c->ee_edges.p, pinst, o->x.p, o->p.p, c->ee_lo.p,
         c->ee_hi.p, c->ee_cell.p, c->ee_key.p, c->ee_val.p, c->ee_entry_cap, c->counters.p);
     PBD_LAUNCH();
     uint32_t *sk;
@@ -488,7 +504,8 @@ int ee_detect(pbd_colli *c) {
                                  c->ee_entry_cap, c->counters.p + kEntries,
                                  (c->ee_log2 + 7) / 8 * 8, c->ee_scr, s, &sk, &sv));
     k_ee_pairs<<<kEEBlocks, 256, 0, s>>>(c->ee_entry_cap, sk, sv, c->ee_cell.p, c->ee_lo.p,
-                                         c->ee_hi.p, c->ee_edges.p, pinst, g, c->ee_pairs.p,
+                                         c->ee_hi.p, c->ee_edges.p, pinst, g,
+                                         c->shs->inst_cell.p, c->shs->n_inst_cell, c->ee_pairs.p,
                                          c->cand_cap, c->counters.p);
     PBD_LAUNCH();
     k_ee_filter<<<kEEBlocks, 256, 0, s>>>(c->cand_cap, th, c->ee_edges.p, c->ee_pairs.p, o->x.p,

@@ -93,6 +93,7 @@ EXPORTS = [
     "pbd_object_set_stiffness", "pbd_object_set_anchor_targets",
     "pbd_colli_set_edge_edge", "pbd_colli_ee_edges", "pbd_colli_get_ee_contacts",
     "pbd_colli_ee_stats", "pbd_ee_test_batch", "pbd_object_get_state", "pbd_object_set_state",
+    "pbd_shs_set_instance_cells",
 ]
 
 
@@ -490,6 +491,18 @@ class SpatialHashSystem:
             _check(self.L.pbd_shs_create(obj.h, _p(np.asarray(grid_center, np.float32)),
                                          _p(np.asarray(grid_size, np.int32)), _p(cell),
                                          C.byref(self.h)))
+
+    def set_instance_cells(self, cells):
+        """cell size per instance ((n_instances, 3) or (n_instances,)); None
+        or empty: one cell size for all"""
+        if cells is None or len(cells) == 0:
+            _check(self.L.pbd_shs_set_instance_cells(self.h, 0, None))
+            return
+        c = np.asarray(cells, np.float32)
+        if c.ndim == 1:
+            c = np.repeat(c[:, None], 3, 1)
+        c = np.ascontiguousarray(c.reshape(-1, 3))
+        _check(self.L.pbd_shs_set_instance_cells(self.h, len(c), _p(c)))
 
     def close(self):
         if self.h:

@@ -197,6 +197,18 @@ def mean_rest_edge(scene):
 # the measured workloads
 # ---------------------------------------------------------------------------
 
+def instance_cells(scene, factor=2.0):
+    """per-instance hash cell sizes: factor x each instance's mean rest edge
+    (its distance constraints' rest lengths), float32 (n_instances,)"""
+    inst = np.asarray(scene["point_inst"])
+    d = np.nonzero(scene["ctype"] == DISTANCE)[0]
+    k = inst[scene["indices"][scene["prim_list"][d, 0]]]
+    n = int(inst.max()) + 1
+    total = np.bincount(k, weights=scene["rest_length"][d].astype(np.float64), minlength=n)
+    count = np.bincount(k, minlength=n)
+    return (factor * total / np.maximum(count, 1)).astype(np.float32)
+
+
 def hanging_cloth(res=32, seed=0):
     """32x32 grid over 1 m x 1 m in the xz-plane, distance (s=1) on every
     triangle edge, bending (s=0.1) on interior edges, corners 0 and res-1

@@ -34,11 +34,13 @@ def make_batch(sides, seed=0):
     return parts, np.asarray(spheres, np.float32)
 
 
-def run(sc, substeps, spheres=None, single_sphere=None, cell=None):
+def run(sc, substeps, spheres=None, single_sphere=None, cell=None, inst_cells=None):
     obj = PBDObject(sc, damping=0.95, gravity=G)
     obj.prepare()
     shs = SpatialHashSystem(obj, cell_size=cell, log2_table=14)
     shs.init()
+    if inst_cells is not None:
+        shs.set_instance_cells(inst_cells)
     cs = CollisionSolver(obj, shs, thickness=2e-3, iterations=1, response=RESPONSE_MASS_WEIGHTED)
     s = SolverPBD(obj)
     if spheres is not None:
@@ -68,6 +70,24 @@ def test_batch_equals_instances_alone():
     # the spheres acted: some points were pushed out to the sphere surface
     d = np.linalg.norm(got[:len(parts[0]["pos"])] - spheres[0, :3], axis=1)
     assert d.min() >= spheres[0, 3] - 1e-4
+
+
+def test_batch_with_per_instance_cells_equals_instances_alone():
+    """Each instance hashed with its own cell size (2 x its mean rest edge)
+    gives exactly what simulating it alone with that cell gives."""
+    sides = [6, 15, 9, 20]
+    parts, spheres = make_batch(sides, seed=5)
+    batch = scenes.concat_scenes(parts)
+    cells = scenes.instance_cells(batch)
+    assert len(np.unique(cells)) == len(sides)
+    got, st = run(batch, 40, spheres=spheres, cell=float(cells.mean()), inst_cells=cells)
+    assert st["overflow"] == 0
+    off = 0
+    for k, c in enumerate(parts):
+        alone, _ = run(c, 40, single_sphere=spheres[k], cell=float(cells[k]))
+        n = len(c["pos"])
+        np.testing.assert_array_equal(got[off:off + n], alone)
+        off += n
 
 
 def test_batch_collision_substep_matches_oracle(orc):
