@@ -627,7 +627,12 @@ int ccd_detect(pbd_colli *c) {
     pbd_object *o = c->obj;
     pbd_shs *h = c->shs;
     cudaStream_t s = o->stream;
-    if (!c->cand.p) PBD_TRY(colli_alloc(c));
+    // (re)size everything for the current target: a first call, a capacity
+    // change, or a target with another point count
+    if (!c->cand.p || c->sized_n != o->n) {
+        PBD_TRY(colli_alloc(c));
+        c->sized_n = o->n;
+    }
     if (c->ee_on) PBD_TRY(ee_prepare(c));
     PBD_CUDA(cudaMemsetAsync(c->counters.p, 0, sizeof(int) * 16, s));
     if (o->nt == 0) return PBD_OK;
@@ -666,6 +671,8 @@ int ccd_resolve(pbd_colli *c, int passes) {
     pbd_object *o = c->obj;
     cudaStream_t s = o->stream;
     if (!c->cand.p || o->nt == 0) return PBD_OK;
+    PBD_CHECK(c->sized_n == o->n, PBD_ERR_STATE,
+              "the target changed since the last CCD pass: detect before resolving");
     // both kernels are programmatic dependents of the kernel before them
     // (their first instruction waits for it), so their launch overlaps it
     cudaLaunchAttribute at[1];

@@ -275,6 +275,7 @@ struct pbd_colli {
     pbd::DBuf<int> counters;    // [0] candidates, [1] contacts, [2] overflow flags, [3] hard
                                 // candidates (cubic roots needed), [4] AABB pairs
     pbd::DBuf<int> hard;        // candidate indices that need the cubic's roots
+    int sized_n = -1;           // point count the per-point buffers were sized for
     // contacts, in the order the narrow phase found them
     pbd::DBuf<int4> cids;               // i0..i3
     pbd::DBuf<int> cface;

@@ -11,7 +11,7 @@ import pytest
 
 from positionbaseddynamicsold_gb300 import scenes
 from positionbaseddynamicsold_gb300.pbd import (RESPONSE_MASS_WEIGHTED, RESPONSE_REFERENCE,
-                                                CollisionSolver, PBDObject, SolverPBD,
+                                                CollisionSolver, PBDError, PBDObject, SolverPBD,
                                                 SpatialHashSystem)
 
 pytestmark = pytest.mark.gpu
@@ -218,3 +218,40 @@ def test_filters_keep_every_hit_under_deformation(orc, seed, h_rel):
     ka = set(zip(got["ids"][:, 0].tolist(), got["face"].tolist()))
     kb = set(zip(want["ids"][:, 0].tolist(), want["face"].tolist()))
     assert ka == kb
+
+
+def test_solver_retargeted_to_a_larger_object():
+    """A collision solver moved to another object (other point count) sizes
+    its per-point buffers for it: same contacts and response as a fresh
+    solver; a response before the first detection on the new target is
+    refused instead of touching stale buffers."""
+    def obj_of(res, seed):
+        sc = scenes.drape_over_sphere(res=res, seed=seed, sphere_level=2)
+        o = PBDObject(sc, damping=1.0, gravity=np.array([0.0, -9.8, 0.0], np.float32))
+        o.prepare()
+        prd = sc["pos"].copy()
+        prd[: sc["n_cloth_points"], 1] -= np.float32(0.12)   # through the sphere's top
+        o.set_predicted(prd)
+        shs = SpatialHashSystem(o, cell_size=sc["colli"]["cell"], log2_table=14)
+        shs.init()
+        return o, shs
+
+    a, sa = obj_of(12, 1)
+    b, sb = obj_of(40, 2)
+    cs = CollisionSolver(a, sa, thickness=1e-3, iterations=1, response=RESPONSE_MASS_WEIGHTED)
+    cs.ccd_sh_extended()
+    cs.set_target(b)
+    cs.set_acce_struct(sb)
+    with pytest.raises(PBDError):
+        cs.collision_resolve_new()
+    cs.ccd_sh_extended()
+    cs.collision_resolve_new()
+    got = b.predicted()
+    b2, sb2 = obj_of(40, 2)
+    fresh = CollisionSolver(b2, sb2, thickness=1e-3, iterations=1,
+                            response=RESPONSE_MASS_WEIGHTED)
+    fresh.ccd_sh_extended()
+    assert fresh.stats()["contacts"] > 0
+    assert cs.stats()["contacts"] == fresh.stats()["contacts"]
+    fresh.collision_resolve_new()
+    np.testing.assert_array_equal(got, b2.predicted())
