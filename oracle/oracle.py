@@ -219,11 +219,13 @@ class Oracle:
         n = self.lib.orc_solve_cubic(a, b, c, d, x)
         return x[:n]
 
-    def extended_vf_test(self, x, p, thickness, ids=(0, 1, 2, 3), narrow=False):
+    def extended_vf_test(self, x, p, thickness, ids=(0, 1, 2, 3), narrow=False, fp64=False):
+        """fp64: the all-double yardstick (orc_extended_vf_test_f64)"""
         xs = np.ascontiguousarray(x, dtype=np.float32).reshape(12)
         ps = np.ascontiguousarray(p, dtype=np.float32).reshape(12)
         ct = OrcContact()
-        fn = self.lib.orc_narrow_vf_ccd_test if narrow else self.lib.orc_extended_vf_test
+        fn = (self.lib.orc_extended_vf_test_f64 if fp64 else
+              self.lib.orc_narrow_vf_ccd_test if narrow else self.lib.orc_extended_vf_test)
         hit = fn(_ptr(xs), _ptr(ps), C.c_float(thickness), *[int(i) for i in ids], C.byref(ct))
         return hit, ct.t, np.array(ct.w), np.array(ct.n, dtype=np.float32)
 

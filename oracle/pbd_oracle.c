@@ -892,6 +892,91 @@ int orc_narrow_vf_ccd_test(const float *x, const float *p, float thickness,
     return 0;
 }
 
+/* ExtendedVFTest restated entirely in FP64, the accuracy yardstick of the
+ * reference-arithmetic test above (which mixes float geometry with double
+ * cubic coefficients and stops Newton at |dx| < 1e-6): the same times 0,
+ * roots in [0, 1] and 1, but every quantity in double and every root
+ * polished by Newton steps to |dx| < 1e-14.  Returns the same hit
+ * decision rule with the double quantities. */
+static double polish_root(const double *a, double t)
+{
+    for (int k = 0; k < 50; ++k) {
+        double y = a[0] + t * (a[1] + t * (a[2] + t * a[3]));
+        double dy = a[1] + t * (2 * a[2] + t * 3 * a[3]);
+        if (dy == 0) break;
+        double t1 = t - y / dy;
+        if (fabs(t1 - t) < 1e-14) return t1;
+        t = t1;
+    }
+    return t;
+}
+
+int orc_extended_vf_test_f64(const float *x, const float *p, float thickness, int i0, int i1,
+                             int i2, int i3, orc_contact *ct)
+{
+    if (i0 == i1 || i0 == i2 || i0 == i3) return 0;
+    d3 X[4], P[4];
+    for (int j = 0; j < 4; ++j) {
+        X[j] = dmk(x[3 * j], x[3 * j + 1], x[3 * j + 2]);
+        P[j] = dmk(p[3 * j], p[3 * j + 1], p[3 * j + 2]);
+    }
+    d3 x0 = X[0], v0 = dsub(P[0], x0);
+    d3 x1 = dsub(X[1], x0), x2 = dsub(X[2], x0), x3 = dsub(X[3], x0);
+    d3 v1 = dsub(dsub(P[1], X[1]), v0), v2 = dsub(dsub(P[2], X[2]), v0),
+       v3 = dsub(dsub(P[3], X[3]), v0);
+    double a[4];
+    a[0] = ddot(x1, dcross(x2, x3));
+    a[1] = ddot(v1, dcross(x2, x3)) + ddot(x1, dcross(v2, x3)) + ddot(x1, dcross(x2, v3));
+    a[2] = ddot(x1, dcross(v2, v3)) + ddot(v1, dcross(x2, v3)) + ddot(v1, dcross(v2, x3));
+    a[3] = ddot(v1, dcross(v2, v3));
+    double t[5];
+    int nsol = orc_solve_cubic(a[3], a[2], a[1], a[0], t);
+    for (int i = 0; i < nsol; ++i) t[i] = polish_root(a, t[i]);
+    t[nsol] = 1;
+    t[nsol + 1] = 0;
+    sort_small(t, nsol + 2);
+    double h = (double)thickness;
+    for (int i = 0; i < nsol + 2; ++i) {
+        if (t[i] < 0 || t[i] > 1) continue;
+        d3 c[4];
+        for (int j = 0; j < 4; ++j) c[j] = dadd(X[j], dmul(dsub(P[j], X[j]), t[i]));
+        d3 cn = dcross(dsub(c[2], c[1]), dsub(c[3], c[1]));
+        double ln = sqrt(ddot(cn, cn));
+        if (!(ln > 0)) continue;
+        cn = dmul(cn, 1.0 / ln);
+        double dist = ddot(dsub(c[0], c[1]), cn);
+        /* barycentric weights of c0 in (c1, c2, c3) (Ericson 3.4) */
+        d3 ab = dsub(c[1], c[3]), ac = dsub(c[2], c[3]), ap = dsub(c[0], c[3]);
+        double d00 = ddot(ac, ac), d01 = ddot(ac, ab), d02 = ddot(ac, ap);
+        double d11 = ddot(ab, ab), d12 = ddot(ab, ap);
+        double inv = 1.0 / (d00 * d11 - d01 * d01);
+        double wv = (d11 * d02 - d01 * d12) * inv;
+        double wu = (d00 * d12 - d01 * d02) * inv;
+        double ww = 1.0 - wu - wv;
+        double e1 = sqrt(ddot(dsub(c[1], c[2]), dsub(c[1], c[2])));
+        double e2 = sqrt(ddot(dsub(c[1], c[3]), dsub(c[1], c[3])));
+        double e3 = sqrt(ddot(dsub(c[2], c[3]), dsub(c[2], c[3])));
+        double eps = h / ((e1 + e2 + e3) / 3.0);
+        int in = wu <= 1 + eps && wu >= -eps && wv <= 1 + eps && wv >= -eps && ww <= 1 + eps &&
+                 ww >= -eps;
+        if (ct) {
+            ct->t = (float)t[i];
+            ct->w[0] = 1;
+            ct->w[1] = wu;
+            ct->w[2] = wv;
+            ct->w[3] = ww;
+            ct->n[0] = (float)cn.x;
+            ct->n[1] = (float)cn.y;
+            ct->n[2] = (float)cn.z;
+        }
+        if (fabs(dist) - 2.0 * h < -1e-6 && in) {
+            if (ct) ct->t = (float)t[i];
+            return 1;
+        }
+    }
+    return 0;
+}
+
 static void gather4(const int *ids, const float *src, float *dst)
 {
     for (int j = 0; j < 4; ++j)

@@ -293,6 +293,12 @@ typedef struct orc_colli_params {
     int64_t contact_cap;
 } orc_colli_params;
 
+/* ExtendedVFTest entirely in FP64 with roots polished to 1e-14: the
+ * accuracy yardstick the reference-arithmetic results are measured
+ * against (t, w and the hit decision). */
+int orc_extended_vf_test_f64(const float *x, const float *p, float thickness, int i0, int i1,
+                             int i2, int i3, orc_contact *ct);
+
 /* Edge-edge CCD (no reference arithmetic: Contact::EE is declared in
  * P/CCD_Basic.h:14, EEResolve is commented out in P/CCD.cpp:925-928).
  * x, p: start / predicted positions of a0, a1, b0, b1.  Times 0, the
