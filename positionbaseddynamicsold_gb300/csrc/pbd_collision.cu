@@ -361,12 +361,24 @@ __global__ void __launch_bounds__(256) k_dist_filter(const int2 *__restrict__ pa
         v3 xa = ld3(x[fi.x]), xb = ld3(x[fi.y]), xc = ld3(x[fi.z]);
         v3 pa = ld3(p[fi.x]), pb = ld3(p[fi.y]), pc = ld3(p[fi.z]);
         if (!sliver(xa, xb, xc) && !sliver(pa, pb, pc)) {
+            // the pair's reach lies between its values at edge ratio 1 and
+            // 1.5 (the ratio computed below is at least 1 and at most 1.5),
+            // so only bounds in between need the ratio; rejecting above the
+            // largest reach is exactly as safe, and accepting more is always
+            // safe (the narrow phase decides)
+            const float r15 = 2.f * th * 1.5f, r10 = 2.f * th;
+            const float reach_max = sqrtf(4.f * th * th + r15 * r15) * 1.001f + 2e-6f;
+            const float reach_min = sqrtf(4.f * th * th + r10 * r10) * 1.001f + 2e-6f;
             v3 D0 = sub3(P0, X0);
-            float d0 = point_tri_dist(X0, xa, xb, xc);
-            float d1 = point_tri_dist(P0, pa, pb, pc);
             v3 ua = sub3(sub3(pa, xa), D0), ub = sub3(sub3(pb, xb), D0),
                uc = sub3(sub3(pc, xc), D0);
             float U = sqrtf(fmaxf(fmaxf(dot3(ua, ua), dot3(ub, ub)), dot3(uc, uc)));
+            float d0 = point_tri_dist(X0, xa, xb, xc);
+            if ((d0 - U) * 0.5f > reach_max) continue;  // d1 >= 0 only raises the bound
+            float d1 = point_tri_dist(P0, pa, pb, pc);
+            const float bound = (d0 + d1 - U) * 0.5f;
+            if (bound > reach_max) continue;
+            if (bound > reach_min) {
             v3 e0[3] = {sub3(xb, xa), sub3(xc, xb), sub3(xa, xc)};
             v3 e1[3] = {sub3(pb, pa), sub3(pc, pb), sub3(pa, pc)};
             float lmax = 0.f, lsum = 0.f;
@@ -378,7 +390,8 @@ __global__ void __launch_bounds__(256) k_dist_filter(const int2 *__restrict__ pa
             float ratio = lsum > 0.f ? fminf(1.5f, lmax / (lsum / 3.f)) : 1.5f;
             float r = 2.f * th * ratio;
             float reach = sqrtf(4.f * th * th + r * r) * 1.001f + 2e-6f;
-            if ((d0 + d1 - U) * 0.5f > reach) continue;
+            if (bound > reach) continue;
+            }
         }
         long long slot = agg_inc(counters);
         if (slot < cap)
