@@ -249,24 +249,42 @@ def folding_cloth(res=1024, seed=0):
     return cloth
 
 
-def batched_cloths(n=512, seed=0, side_lo=16, side_hi=128):
-    """n independent cloths, side U{side_lo..side_hi}, random pins (1-4
-    corners) and one analytic sphere each (radius U(0.2, 0.6), centre below
-    the cloth).  Instances are concatenated; point_inst/tri_inst tag them."""
+def _batched_params(n, seed, side_lo, side_hi):
+    """the per-instance draws of batched_cloths, in draw order"""
     rng = np.random.default_rng(seed)
-    parts = []
-    spheres = []
+    out = []
     for k in range(n):
         side = int(rng.integers(side_lo, side_hi + 1))
-        size = 1.0
         corners = np.array([0, side - 1, side * (side - 1), side * side - 1])
         npin = int(rng.integers(1, 5))
         pins = rng.choice(corners, npin, replace=False)
-        c = grid_cloth(side, side, size, size, origin=(-0.5, 0.0, -0.5), jitter=1e-4,
-                       seed=seed * 100003 + k, pins=pins)
         r = float(rng.uniform(0.2, 0.6))
-        spheres.append((float(rng.uniform(-0.2, 0.2)), -r - float(rng.uniform(0.01, 0.3)),
-                        float(rng.uniform(-0.2, 0.2)), r))
+        sphere = (float(rng.uniform(-0.2, 0.2)), -r - float(rng.uniform(0.01, 0.3)),
+                  float(rng.uniform(-0.2, 0.2)), r)
+        out.append((side, pins, sphere))
+    return out
+
+
+def batched_cloth_points(n=512, seed=0, side_lo=16, side_hi=128):
+    """points of every instance of batched_cloths(n, seed, ...)"""
+    return [side * side for side, _, _ in _batched_params(n, seed, side_lo, side_hi)]
+
+
+def batched_cloths(n=512, seed=0, side_lo=16, side_hi=128, subset=None):
+    """n independent cloths, side U{side_lo..side_hi}, random pins (1-4
+    corners) and one analytic sphere each (radius U(0.2, 0.6), centre below
+    the cloth).  Instances are concatenated; point_inst/tri_inst tag them.
+    subset: the instance indices to build (all by default); each instance is
+    the same whichever others are built."""
+    parts = []
+    spheres = []
+    keep = range(n) if subset is None else sorted(subset)
+    params = _batched_params(n, seed, side_lo, side_hi)
+    for k in keep:
+        side, pins, sphere = params[k]
+        c = grid_cloth(side, side, 1.0, 1.0, origin=(-0.5, 0.0, -0.5), jitter=1e-4,
+                       seed=seed * 100003 + k, pins=pins)
+        spheres.append(sphere)
         parts.append(c)
     return concat_scenes(parts, spheres)
 
