@@ -11,7 +11,11 @@
 //   arec           float4 {rest xyz, point id} per anchor, grouped by color.
 // One kernel launch per color applies every constraint of that color; no
 // two constraints of a color share a point, so the launch has no races and
-// its result does not depend on thread order.
+// its result does not depend on thread order.  The resident form
+// (k_gs_resident) runs whole sweeps in one launch with the points in the
+// shared memory of a thread-block cluster and a cluster barrier per color.
+// Per-point host transfers go through page-locked staging (or directly from
+// a page-locked caller array) and float3 <-> float4 pack kernels.
 //
 // Arithmetic mirrors the reference kernels operation by operation; this
 // translation unit is compiled with -fmad=false so no multiply-add is fused
@@ -1789,9 +1793,9 @@ int pbd_solver_graph_kernels(pbd_solver *s, long long *n) {
 // Times `iterations` sweeps, one launch sequence per sweep as a substep with
 // collisions issues them, replayed from a CUDA graph, for every launch form
 // that applies to the object (per-color launches with 64..512 threads per
-// block; the cluster form when the object fits one cluster), keeps the
-// fastest and restores the predicted positions.  Every form gives the same
-// result, so the choice only changes speed.
+// block; the resident form with every cluster size whose shared memory holds
+// the object), keeps the fastest and restores the predicted positions.
+// Every form gives the same result, so the choice only changes speed.
 int pbd_solver_autotune(pbd_solver *s, int iterations, int reps, pbd_autotune_result *res) {
     PBD_CHECK(s && s->obj && res, PBD_ERR_ARG, "null argument");
     PBD_CHECK(iterations >= 1 && reps >= 1, PBD_ERR_ARG, "need iterations, reps >= 1");
