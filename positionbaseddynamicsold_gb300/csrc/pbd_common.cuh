@@ -299,6 +299,9 @@ struct pbd_colli {
     pbd::DBuf<int4> ee_cell;
     pbd::DBuf<uint32_t> ee_key, ee_key2;
     pbd::DBuf<int> ee_val, ee_val2;
+    pbd::DBuf<int4> ee_r0;               // sorted entry records (cell, edge)
+    pbd::DBuf<float4> ee_r1, ee_r2;      // (box lo, end 0), (box hi, end 1)
+    pbd::DBuf<int> ee_rinst;             // instance of a sorted entry (batches)
     pbd::DBuf<int2> ee_pairs, ee_cand, ee_hpair;
     pbd::DBuf<int4> ee_ids;
     pbd::DBuf<float4> ee_m0, ee_tsu;

@@ -12,8 +12,9 @@
 //      overlaps (cell = the spatial hash's); one (bucket, entry) pair per
 //      cell, the instance mixed into the bucket like the triangle hash;
 //   2. radix sort of the entries by bucket;
-//   3. one thread per sorted entry pairs it with the later entries of its
-//      bucket: same cell (the hash may mix cells), no shared point, same
+//   3. the sorted entries gathered into contiguous records (cell, edge, end
+//      points, box); one thread per record pairs it with the later records
+//      of its bucket: same cell (the hash may mix cells), no shared point, same
 //      instance, overlapping boxes, and the pair is reported only by the cell
 //      holding the low corner of the boxes' intersection -- so every pair of
 //      edges whose boxes overlap is reported exactly once;
@@ -48,6 +49,7 @@ namespace pbd {
 namespace {
 
 constexpr int kEEMaxCells = 256;      // cells per edge box; more sets overflow bit 32
+constexpr int kEEEdgeMask = (1 << 28) - 1;  // entry word: edge | first-cell bits << 28
 constexpr int kEEBlocks = 8 * kNumSMs;
 
 // counters slots (pbd_colli::counters) of this path
@@ -269,54 +271,163 @@ __global__ void __launch_bounds__(256) k_ee_entries(int ne, GridParams g, float 
                 if (q >= cap) return;
                 key[q] = bucket_of(g, cx, cy, cz, inst);
                 val[q] = (int)q;
-                ecell[q] = make_int4(cx, cy, cz, e);
+                // bits 28-30: the cell is the box's first along x, y, z
+                const int first = (cx == x0) | (cy == y0) << 1 | (cz == z0) << 2;
+                ecell[q] = make_int4(cx, cy, cz, e | first << 28);
             }
 }
 
-// step 3: pairs within a bucket run
-__global__ void __launch_bounds__(256) k_ee_pairs(long long cap, const uint32_t *__restrict__ skey,
-                                                  const int *__restrict__ sval,
-                                                  const int4 *__restrict__ ecell,
-                                                  const float4 *__restrict__ elo,
-                                                  const float4 *__restrict__ ehi,
-                                                  const int2 *__restrict__ edges,
-                                                  const int *__restrict__ point_inst, GridParams g,
-                                                  const float4 *__restrict__ icell, int n_icell,
-                                                  int2 *pairs, long long pcap, int *counters) {
+// step 3a: the sorted entries as contiguous records, so that the pairing
+// below reads neighbouring words (shared by the lanes of a warp through L1)
+// instead of three levels of dependent gathers per pair:
+//   r0 = (cell x, cell y, cell z, edge), r1 = (box lo, end point 0),
+//   r2 = (box hi, end point 1), rinst = the edge's instance (batches only)
+__global__ void __launch_bounds__(256) k_ee_gather(long long cap, const int *__restrict__ sval,
+                                                   const int4 *__restrict__ ecell,
+                                                   const float4 *__restrict__ elo,
+                                                   const float4 *__restrict__ ehi,
+                                                   const int2 *__restrict__ edges,
+                                                   const int *__restrict__ point_inst, int4 *r0,
+                                                   float4 *r1, float4 *r2, int *rinst,
+                                                   const int *counters) {
     long long n = counters[kEntries];
     if (n > cap) n = cap;
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
          i += (long long)gridDim.x * blockDim.x) {
-        const uint32_t k = skey[i];
-        const int4 ci = ecell[sval[i]];
-        const int e1 = ci.w;
-        const int2 E1 = edges[e1];
-        const float4 lo1 = elo[e1], hi1 = ehi[e1];
-        const int inst1 = point_inst ? point_inst[E1.x] : 0;
-        const float3 cl = inst_cell_of(g, icell, n_icell, inst1);
-        for (long long j = i + 1; j < n && skey[j] == k; ++j) {
-            const int4 cj = ecell[sval[j]];
-            if (cj.x != ci.x || cj.y != ci.y || cj.z != ci.z) continue;
-            const int e2 = cj.w;
-            const int2 E2 = edges[e2];
-            if (E1.x == E2.x || E1.x == E2.y || E1.y == E2.x || E1.y == E2.y) continue;
-            if (point_inst && point_inst[E2.x] != inst1) continue;
-            const float4 lo2 = elo[e2], hi2 = ehi[e2];
-            if (lo1.x > hi2.x || lo2.x > hi1.x || lo1.y > hi2.y || lo2.y > hi1.y ||
-                lo1.z > hi2.z || lo2.z > hi1.z)
-                continue;
-            // the cell of the intersection's low corner reports the pair
-            if (cell_of(fmaxf(lo1.x, lo2.x), g.start.x, cl.x) != ci.x ||
-                cell_of(fmaxf(lo1.y, lo2.y), g.start.y, cl.y) != ci.y ||
-                cell_of(fmaxf(lo1.z, lo2.z), g.start.z, cl.z) != ci.z)
-                continue;
-            const long long slot = agg_inc(counters + kPairs);
-            if (slot < pcap)
-                pairs[slot] = make_int2(min(e1, e2), max(e1, e2));
-            else
-                atomicOr(counters + 2, 64);
+        const int4 c = ecell[sval[i]];
+        const int e = c.w & kEEEdgeMask;
+        const int2 E = edges[e];
+        const float4 lo = elo[e], hi = ehi[e];
+        r0[i] = c;
+        r1[i] = make_float4(lo.x, lo.y, lo.z, __int_as_float(E.x));
+        r2[i] = make_float4(hi.x, hi.y, hi.z, __int_as_float(E.y));
+        if (point_inst) rinst[i] = point_inst[E.x];
+    }
+}
+
+// step 3b: pairs within a bucket run.  Work is balanced over a run of m
+// records: record a pairs with records (a + d) mod m, d = 1 .. (m - 1) / 2,
+// and also d = m / 2 when m is even and a < m / 2 -- every unordered pair
+// once, about m / 2 steps per record (the round-robin of a complete graph).
+// A warp finds its records' run bounds from ballots of the run heads over
+// its 32 records and, for runs crossing its window, over 32-record chunks
+// before and after it.  Reported pairs are staged per warp in shared memory
+// and appended with one atomic per kEEPairStage pairs (one counter takes
+// every pair of the pass).  Reporting rule: the cell of the boxes'
+// intersection's low corner is, per axis, the larger of the two boxes' first
+// cells (floor((v - start) / cell) is monotone in v), so with both records
+// in this cell it is this cell exactly when, on every axis, one of the two
+// is its box's first cell there -- the record's three "first" bits.
+constexpr int kEEPairStage = 256;
+constexpr int kEEPairWarps = 8;
+
+__device__ __forceinline__ void ee_flush(const int2 *stage, int cnt, int lane, int2 *pairs,
+                                         long long pcap, int *counters) {
+    int base = 0;
+    if (lane == 0) base = atomicAdd(counters + kPairs, cnt);
+    base = __shfl_sync(0xffffffffu, base, 0);
+    bool over = false;
+    for (int l = lane; l < cnt; l += 32) {
+        const long long slot = (long long)base + l;
+        if (slot < pcap)
+            pairs[slot] = stage[l];
+        else
+            over = true;
+    }
+    if (__any_sync(0xffffffffu, over) && lane == 0) atomicOr(counters + 2, 64);
+    __syncwarp();
+}
+
+__global__ void __launch_bounds__(32 * kEEPairWarps) k_ee_pairs(
+    int cap, const uint32_t *__restrict__ skey, const int4 *__restrict__ r0,
+    const float4 *__restrict__ r1, const float4 *__restrict__ r2, const int *__restrict__ rinst,
+    int2 *pairs, long long pcap, int *counters) {
+    constexpr unsigned kAll = 0xffffffffu;
+    __shared__ int2 stage_all[kEEPairWarps][kEEPairStage];
+    const int lane = threadIdx.x & 31;
+    int2 *stage = stage_all[threadIdx.x >> 5];
+    int cnt = 0;
+    const int n = min(counters[kEntries], cap);
+    const int stride = gridDim.x * blockDim.x;
+    for (int w = blockIdx.x * blockDim.x + (threadIdx.x & ~31); w < n; w += stride) {
+        const int i = w + lane;
+        const bool valid = i < n;
+        const unsigned heads =
+            __ballot_sync(kAll, valid && (i == 0 || skey[i - 1] != skey[i]));
+        // start of the run holding the window's first record
+        int s0 = w;
+        if (!(heads & 1u)) {
+            for (int b = w;; b -= 32) {
+                const int q = b - 32 + lane;
+                const unsigned hb =
+                    __ballot_sync(kAll, q >= 0 && (q == 0 || skey[q - 1] != skey[q]));
+                if (hb) {
+                    s0 = b - 32 + 31 - __clz(hb);
+                    break;
+                }
+            }
+        }
+        // end of the run holding the window's last record
+        int e31 = n;
+        for (int b = w + 32; b < n; b += 32) {
+            const int q = b + lane;
+            const unsigned hb = __ballot_sync(kAll, q < n && skey[q - 1] != skey[q]);
+            if (hb) {
+                e31 = b + __ffs(hb) - 1;
+                break;
+            }
+        }
+        const unsigned below = heads & (kAll >> (31 - lane));
+        const unsigned above = lane == 31 ? 0u : heads & (kAll << (lane + 1));
+        const int s = below ? w + 31 - __clz(below) : s0;
+        const int e = above ? w + __ffs(above) - 1 : e31;
+        const int m = e - s, a = i - s;
+        const int steps = valid ? (m - 1) / 2 + ((m & 1) == 0 && a < m / 2) : 0;
+        const int max_steps = __reduce_max_sync(kAll, steps);
+        if (max_steps == 0) continue;
+        int4 ci = make_int4(0, 0, 0, 0);
+        float4 lo1 = make_float4(0.f, 0.f, 0.f, 0.f), hi1 = lo1;
+        int inst1 = 0;
+        if (steps) {
+            ci = r0[i];
+            lo1 = r1[i];
+            hi1 = r2[i];
+            if (rinst) inst1 = rinst[i];
+        }
+        const int e1 = ci.w & kEEEdgeMask, f1 = ci.w >> 28;
+        const int a0 = __float_as_int(lo1.w), a1 = __float_as_int(hi1.w);
+        int j = i;
+        for (int d = 1; d <= max_steps; ++d) {
+            bool hit = false;
+            int e2 = 0;
+            if (d <= steps) {
+                if (++j == e) j = s;
+                const int4 cj = r0[j];
+                if (cj.x == ci.x && cj.y == ci.y && cj.z == ci.z && (f1 | cj.w >> 28) == 7) {
+                    const float4 lo2 = r1[j], hi2 = r2[j];
+                    const int b0 = __float_as_int(lo2.w), b1 = __float_as_int(hi2.w);
+                    hit = !(a0 == b0 || a0 == b1 || a1 == b0 || a1 == b1) &&
+                          !(lo1.x > hi2.x || lo2.x > hi1.x || lo1.y > hi2.y || lo2.y > hi1.y ||
+                            lo1.z > hi2.z || lo2.z > hi1.z) &&
+                          (!rinst || rinst[j] == inst1);
+                    e2 = cj.w & kEEEdgeMask;
+                }
+            }
+            const unsigned hm = __ballot_sync(kAll, hit);
+            if (hm) {
+                if (cnt + 32 > kEEPairStage) {
+                    ee_flush(stage, cnt, lane, pairs, pcap, counters);
+                    cnt = 0;
+                }
+                if (hit)
+                    stage[cnt + __popc(hm & ((1u << lane) - 1u))] =
+                        make_int2(min(e1, e2), max(e1, e2));
+                cnt += __popc(hm);
+                __syncwarp();
+            }
         }
     }
+    if (cnt) ee_flush(stage, cnt, lane, pairs, pcap, counters);
 }
 
 // step 4: distance bound over the step
@@ -461,11 +572,14 @@ int ee_prepare(pbd_colli *c) {
         }
         std::vector<int2> e;
         if (o->nt) PBD_TRY(mesh_unique_edges(o->n, o->nt, tri.data(), e));
+        PBD_CHECK(e.size() <= (size_t)kEEEdgeMask, PBD_ERR_ARG,
+                  "edge-edge CCD: %zu edges, at most %d", e.size(), kEEEdgeMask);
         c->ee_n = (int)e.size();
         PBD_TRY(c->ee_edges.upload(e.data(), std::max<size_t>(e.size(), 1), s));
     }
     const long long ne = std::max(c->ee_n, 1);
-    if (!c->ee_entry_cap) c->ee_entry_cap = std::max(1LL << 20, 16 * ne);
+    // entries are indexed with 32-bit ints on the device
+    if (!c->ee_entry_cap) c->ee_entry_cap = std::min(1LL << 30, std::max(1LL << 20, 16 * ne));
     const long long ecap = c->ee_entry_cap;
     PBD_TRY(c->ee_lo.alloc(ne));
     PBD_TRY(c->ee_hi.alloc(ne));
@@ -474,6 +588,10 @@ int ee_prepare(pbd_colli *c) {
     PBD_TRY(c->ee_key2.alloc(ecap));
     PBD_TRY(c->ee_val.alloc(ecap));
     PBD_TRY(c->ee_val2.alloc(ecap));
+    PBD_TRY(c->ee_r0.alloc(ecap));
+    PBD_TRY(c->ee_r1.alloc(ecap));
+    PBD_TRY(c->ee_r2.alloc(ecap));
+    if (o->has_inst) PBD_TRY(c->ee_rinst.alloc(ecap));
     PBD_TRY(c->ee_pairs.alloc(c->cand_cap));
     PBD_TRY(c->ee_cand.alloc(c->cand_cap));
     PBD_TRY(c->ee_ids.alloc(c->contact_cap));
@@ -503,10 +621,14 @@ int ee_detect(pbd_colli *c) {
     PBD_TRY(radix_sort<uint32_t>(c->ee_key.p, c->ee_val.p, c->ee_key2.p, c->ee_val2.p,
                                  c->ee_entry_cap, c->counters.p + kEntries,
                                  (c->ee_log2 + 7) / 8 * 8, c->ee_scr, s, &sk, &sv));
-    k_ee_pairs<<<kEEBlocks, 256, 0, s>>>(c->ee_entry_cap, sk, sv, c->ee_cell.p, c->ee_lo.p,
-                                         c->ee_hi.p, c->ee_edges.p, pinst, g,
-                                         c->shs->inst_cell.p, c->shs->n_inst_cell, c->ee_pairs.p,
-                                         c->cand_cap, c->counters.p);
+    k_ee_gather<<<kEEBlocks, 256, 0, s>>>(c->ee_entry_cap, sv, c->ee_cell.p, c->ee_lo.p,
+                                          c->ee_hi.p, c->ee_edges.p, pinst, c->ee_r0.p,
+                                          c->ee_r1.p, c->ee_r2.p, pinst ? c->ee_rinst.p : nullptr,
+                                          c->counters.p);
+    PBD_LAUNCH();
+    k_ee_pairs<<<kEEBlocks, 32 * kEEPairWarps, 0, s>>>(
+        (int)c->ee_entry_cap, sk, c->ee_r0.p, c->ee_r1.p, c->ee_r2.p, pinst ? c->ee_rinst.p : nullptr,
+        c->ee_pairs.p, c->cand_cap, c->counters.p);
     PBD_LAUNCH();
     k_ee_filter<<<kEEBlocks, 256, 0, s>>>(c->cand_cap, th, c->ee_edges.p, c->ee_pairs.p, o->x.p,
                                           o->p.p, c->ee_cand.p, c->cand_cap, c->counters.p);

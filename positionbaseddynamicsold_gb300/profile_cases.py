@@ -11,6 +11,9 @@ ccd: the drape256 scene after 160 substeps (the cloth lies on the sphere),
      one CCD pass (k_point_pairs, k_dist_filter, k_narrow).
 ccd_fold: the fold1024 scene (1,048,576 points, ground plane) after 120
      substeps, one CCD pass.
+ccd_fold_ee: the fold scene at 512 x 512 over 2 m x 2 m (262,144 points,
+     fold1024's spacing) after 120 substeps, one CCD pass with edge-edge CCD on (k_ee_entries, k_ee_gather,
+     k_ee_pairs, k_ee_filter, k_ee_narrow: about 4.6 M edge-cell entries).
 Each case runs its kernels once after one warm-up call, so `-c` small
 captures the steady-state launch.
 """
@@ -48,7 +51,7 @@ def case_mlp():
     print("mlp case done: %d points" % obj.n_points)
 
 
-def _ccd(sc, log2, substeps):
+def _ccd(sc, log2, substeps, edge_edge=False):
     obj = PBDObject(sc, damping=1.0, gravity=G)
     obj.prepare()
     shs = SpatialHashSystem(obj, cell_size=sc["colli"]["cell"], log2_table=log2)
@@ -62,10 +65,11 @@ def _ccd(sc, log2, substeps):
         s.set_ground(True, sc["colli"]["ground"])
     s.step(DT, substeps=substeps, iterations=15, colli=cs, use_graph=True)
     s.advect(DT)
+    cs.set_edge_edge(edge_edge)
     for _ in range(2):           # warm-up + profiled
         cs.ccd_sh_extended()
     obj.sync()
-    print("ccd case done: %s" % cs.stats())
+    print("ccd case done: %s%s" % (cs.stats(), " ee %s" % cs.ee_stats() if edge_edge else ""))
 
 
 def case_ccd():
@@ -76,5 +80,10 @@ def case_ccd_fold():
     _ccd(scenes.folding_cloth(res=1024, seed=0), 24, 120)
 
 
+def case_ccd_fold_ee():
+    _ccd(scenes.folding_cloth(res=512, seed=0, size=2.0), 22, 120, edge_edge=True)
+
+
 if __name__ == "__main__":
-    {"mlp": case_mlp, "ccd": case_ccd, "ccd_fold": case_ccd_fold}[sys.argv[1]]()
+    {"mlp": case_mlp, "ccd": case_ccd, "ccd_fold": case_ccd_fold,
+     "ccd_fold_ee": case_ccd_fold_ee}[sys.argv[1]]()

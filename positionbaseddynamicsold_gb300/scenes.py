@@ -229,12 +229,13 @@ def drape_over_sphere(res=256, seed=0, sphere_level=5):
     return scene
 
 
-def folding_cloth(res=1024, seed=0):
-    """res^2 grid over 4 m x 4 m, rotated 45 degrees about the vertical axis
-    and tilted 30 degrees about x, lowest point 0.05 m above the ground plane
-    y = 0, jitter U(+-1e-4).  Collision: self CCD, cell = 2 x mean rest edge,
-    table 2^24, thickness 1e-3, ground plane."""
-    cloth = grid_cloth(res, res, 4.0, 4.0, origin=(-2.0, 0.0, -2.0), jitter=1e-4, seed=seed)
+def folding_cloth(res=1024, seed=0, size=4.0):
+    """res^2 grid over size x size (4 m), rotated 45 degrees about the
+    vertical axis and tilted 30 degrees about x, lowest point 0.05 m above the
+    ground plane y = 0, jitter U(+-1e-4).  Collision: self CCD, cell = 2 x
+    mean rest edge, table 2^24, thickness 1e-3, ground plane."""
+    cloth = grid_cloth(res, res, size, size, origin=(-size / 2, 0.0, -size / 2), jitter=1e-4,
+                       seed=seed)
     p = cloth["pos"].astype(np.float64)
     c, s = np.cos(np.pi / 4), np.sin(np.pi / 4)
     ry = np.array([[c, 0, s], [0, 1, 0], [-s, 0, c]])

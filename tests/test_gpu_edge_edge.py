@@ -8,6 +8,8 @@ test_ee_oracle.py pin the arithmetic):
 * detection over two cloth patches passing through each other: the same
   contacts as testing every edge pair (so the edge hash, the low-corner
   reporting rule and the distance bound lose nothing);
+* the pair count: exactly the overlapping edge boxes, within an instance
+  in batches;
 * one response pass over the vertex-face and edge-edge contacts together:
   bit for bit;
 * two crossing strips that vertex-face CCD cannot see pass through each
@@ -125,6 +127,53 @@ def test_detection_equals_every_pair_tested(orc):
     np.testing.assert_array_equal(ids, np.concatenate([edges[opairs[:, 0]], edges[opairs[:, 1]]], 1))
     st = cs.ee_stats()
     assert st["contacts"] == len(opairs) and st["candidates"] >= st["contacts"]
+
+
+def box_pairs_brute(edges, x, p, h, point_inst=None):
+    """every pair of edges without a shared point (of one instance) whose
+    swept boxes, grown by 2 h * 1.001 + 4e-6 like the edge hash's, overlap"""
+    f = np.float32
+    grow = f(2) * f(h) * f(1.001) + f(4e-6)
+    pts = np.stack([x[edges[:, 0]], x[edges[:, 1]], p[edges[:, 0]], p[edges[:, 1]]], 0)
+    lo, hi = pts.min(0) - grow, pts.max(0) + grow
+    i, j = np.triu_indices(len(edges), 1)
+    ok = np.all((lo[i] <= hi[j]) & (lo[j] <= hi[i]), 1)
+    ok &= ~((edges[i, 0] == edges[j, 0]) | (edges[i, 0] == edges[j, 1]) |
+            (edges[i, 1] == edges[j, 0]) | (edges[i, 1] == edges[j, 1]))
+    if point_inst is not None:
+        ok &= point_inst[edges[i, 0]] == point_inst[edges[j, 0]]
+    return int(ok.sum())
+
+
+def test_every_overlapping_box_pair_reported_once():
+    """the hash's pair count is exactly the number of overlapping edge boxes:
+    nothing lost, nothing reported twice (same cell, low-corner rule)"""
+    sc, prd = crossing_patches(seed=1)
+    obj, shs, cs = detect(sc, prd)
+    st = cs.ee_stats()
+    assert st["pairs"] == box_pairs_brute(cs.ee_edges(), sc["pos"], prd, H) > 1000
+
+
+def test_batch_pairs_stay_within_instances(orc):
+    """two instances of crossing patches in the same place: the pairs are
+    each instance's own, and the contacts those of testing every pair of one
+    instance"""
+    parts = [crossing_patches(seed=s) for s in (0, 5)]
+    batch = scenes.concat_scenes([sc for sc, _ in parts])
+    prd = np.concatenate([q for _, q in parts]).astype(np.float32)
+    obj, shs, cs = detect(batch, prd)
+    edges = cs.ee_edges()
+    inst = batch["point_inst"]
+    st = cs.ee_stats()
+    assert st["pairs"] == box_pairs_brute(edges, batch["pos"], prd, H, inst)
+    assert st["pairs"] < box_pairs_brute(edges, batch["pos"], prd, H)
+    pairs, ids, tsu, m0 = cs.ee_contacts()
+    opairs, otsu, om0 = orc.ccd_ee_brute(edges, inst, batch["pos"], prd, H)
+    assert len(opairs) > 100
+    assert np.all(inst[edges[opairs[:, 0], 0]] == inst[edges[opairs[:, 1], 0]])
+    np.testing.assert_array_equal(pairs, opairs)
+    np.testing.assert_array_equal(tsu, otsu)
+    np.testing.assert_array_equal(m0, om0)
 
 
 def test_response_matches_oracle(orc):
