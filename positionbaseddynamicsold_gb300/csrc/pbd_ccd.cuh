@@ -296,6 +296,44 @@ __device__ __forceinline__ uint32_t bucket_of(const GridParams &g, int x, int y,
            (uint32_t)y * (uint32_t)g.size.x + (uint32_t)x;
 }
 
+// Append a warp's staged pairs (stage[0, cnt), filled by the whole warp) to
+// out with one atomic on *counter; slots at or past cap are dropped and set
+// flag_bit in *flags.  Called by all 32 lanes.
+__device__ __forceinline__ void warp_flush_pairs(const int2 *stage, int cnt, int lane, int2 *out,
+                                                 long long cap, int *counter, int *flags,
+                                                 int flag_bit) {
+    int base = 0;
+    if (lane == 0) base = atomicAdd(counter, cnt);
+    base = __shfl_sync(0xffffffffu, base, 0);
+    bool over = false;
+    for (int l = lane; l < cnt; l += 32) {
+        const long long slot = (long long)base + l;
+        if (slot < cap)
+            out[slot] = stage[l];
+        else
+            over = true;
+    }
+    if (__any_sync(0xffffffffu, over) && lane == 0) atomicOr(flags, flag_bit);
+    __syncwarp();
+}
+
+// Stage this lane's pair (when hit) in the warp's buffer of `size` pairs,
+// flushing it first when the 32 new ones might not fit.  Called by all 32
+// lanes with the warp's running count cnt.
+__device__ __forceinline__ void warp_stage_pair(bool hit, int2 pr, int2 *stage, int size,
+                                                int &cnt, int lane, int2 *out, long long cap,
+                                                int *counter, int *flags, int flag_bit) {
+    const unsigned hm = __ballot_sync(0xffffffffu, hit);
+    if (!hm) return;
+    if (cnt + 32 > size) {
+        warp_flush_pairs(stage, cnt, lane, out, cap, counter, flags, flag_bit);
+        cnt = 0;
+    }
+    if (hit) stage[cnt + __popc(hm & ((1u << lane) - 1u))] = pr;
+    cnt += __popc(hm);
+    __syncwarp();
+}
+
 // one atomic per group of lanes that reach this call together
 __device__ __forceinline__ int agg_inc(int *counter) {
     cg::coalesced_group g = cg::coalesced_threads();

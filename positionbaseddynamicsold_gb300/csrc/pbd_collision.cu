@@ -15,7 +15,9 @@
 //      pair once); a cell whose bucket AABB misses the point's swept AABB
 //      grown by 3.61 h yields nothing; the kept buckets' entries are spread
 //      over the lanes (warp prefix sum), each entry checked for its exact
-//      cell and swept-AABB overlap;
+//      cell and swept-AABB overlap; found pairs are staged per warp in
+//      shared memory and appended with one atomic per batch (warps loop
+//      over points, so a batch spans many points);
 //   4. distance filter: a pair survives when a lower bound of the
 //      point-triangle distance over the step is within the pair's own reach
 //      sqrt((2h)^2 + r^2), r = 2h * longest / mean edge (at most 3.61 h).
@@ -183,6 +185,7 @@ __global__ void k_find_neighbors(int nt, GridParams g, const int4 *tcell, const 
 // the lane's cell (the hash may mix cells), its swept AABB meets the point's
 // and it belongs to the point's instance.
 constexpr int kTaskWarps = 8;
+constexpr int kPointPairStage = 256;  // pairs staged per warp, appended with one atomic
 __global__ void __launch_bounds__(32 * kTaskWarps) k_point_pairs(
     int n, GridParams g, float margin, const int *__restrict__ pt_first,
     const int *__restrict__ pt_last, const int *__restrict__ pt_tri,
@@ -190,9 +193,12 @@ __global__ void __launch_bounds__(32 * kTaskWarps) k_point_pairs(
     const float4 *__restrict__ x, const float4 *__restrict__ p, const int4 *__restrict__ tcell,
     const float4 *__restrict__ btab, const float4 *__restrict__ etab, int2 *pairs, long long cap,
     int *counters) {
+    __shared__ int2 stage_all[kTaskWarps][kPointPairStage];
     const int lane = threadIdx.x & 31;
     const int warp0 = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int nwarps = (gridDim.x * blockDim.x) >> 5;
+    int2 *stage = stage_all[threadIdx.x >> 5];
+    int scnt = 0;  // pairs staged by this warp
     for (int v = warp0; v < n; v += nwarps) {
         // the point's own positions first: their loads overlap the chain
         // point -> incident triangles -> their cells
@@ -300,26 +306,26 @@ __global__ void __launch_bounds__(32 * kTaskWarps) k_point_pairs(
                 const int ox = __shfl_sync(0xffffffffu, cx, own);
                 const int oy = __shfl_sync(0xffffffffu, cy, own);
                 const int oz = __shfl_sync(0xffffffffu, cz, own);
-                if (f >= total) continue;
-                const int e = o_start + (f - o_excl);
-                // the entry's cell, id and box: 48 contiguous bytes, loaded together
-                const float4 e0 = etab[3 * (size_t)e], tl = etab[3 * (size_t)e + 1],
-                             th = etab[3 * (size_t)e + 2];
-                const int4 sc = make_int4(__float_as_int(e0.x), __float_as_int(e0.y),
-                                          __float_as_int(e0.z), __float_as_int(e0.w));
-                if (sc.x != ox || sc.y != oy || sc.z != oz) continue;
-                if (plx > th.x || phx < tl.x || ply > th.y || phy < tl.y || plz > th.z ||
-                    phz < tl.z)
-                    continue;
-                if (point_inst && tri_inst[sc.w] != inst) continue;
-                const long long slot = agg_inc(counters + 4);
-                if (slot < cap)
-                    pairs[slot] = make_int2(v, sc.w);
-                else
-                    atomicOr(counters + 2, 16);
+                bool hit = false;
+                int tri = 0;
+                if (f < total) {
+                    const int e = o_start + (f - o_excl);
+                    // the entry's cell, id and box: 48 contiguous bytes, loaded together
+                    const float4 e0 = etab[3 * (size_t)e], tl = etab[3 * (size_t)e + 1],
+                                 th = etab[3 * (size_t)e + 2];
+                    tri = __float_as_int(e0.w);
+                    hit = __float_as_int(e0.x) == ox && __float_as_int(e0.y) == oy &&
+                          __float_as_int(e0.z) == oz &&
+                          !(plx > th.x || phx < tl.x || ply > th.y || phy < tl.y ||
+                            plz > th.z || phz < tl.z) &&
+                          (!point_inst || tri_inst[tri] == inst);
+                }
+                warp_stage_pair(hit, make_int2(v, tri), stage, kPointPairStage, scnt, lane, pairs,
+                                cap, counters + 4, counters + 2, 16);
             }
         }
     }
+    if (scnt) warp_flush_pairs(stage, scnt, lane, pairs, cap, counters + 4, counters + 2, 16);
 }
 
 // distance from the origin to the segment [a, b]
@@ -658,7 +664,10 @@ int ccd_detect(pbd_colli *c) {
     // with slack (the filter then applies each pair's own reach)
     float margin = 3.61f * th * 1.001f + 2e-6f;
 
-    k_point_pairs<<<grid_for((long long)o->n * 32, 32 * kTaskWarps), 32 * kTaskWarps, 0, s>>>(
+    // warps loop over points, so each warp's staged pairs span many points
+    const int pp_blocks = (int)std::min<long long>(grid_for((long long)o->n * 32, 32 * kTaskWarps),
+                                                   8 * kNumSMs);
+    k_point_pairs<<<pp_blocks, 32 * kTaskWarps, 0, s>>>(
         o->n, g, margin, o->pt_tri_first.p, o->pt_tri_last.p, o->pt_tri.p,
         o->has_inst ? o->point_inst.p : nullptr, o->has_inst ? o->tri_inst.p : nullptr, o->x.p,
         o->p.p, h->tcell.p, h->btab.p, h->etab.p, c->pairs.p, c->task_cap, c->counters.p);

@@ -321,23 +321,6 @@ __global__ void __launch_bounds__(256) k_ee_gather(long long cap, const int *__r
 constexpr int kEEPairStage = 256;
 constexpr int kEEPairWarps = 8;
 
-__device__ __forceinline__ void ee_flush(const int2 *stage, int cnt, int lane, int2 *pairs,
-                                         long long pcap, int *counters) {
-    int base = 0;
-    if (lane == 0) base = atomicAdd(counters + kPairs, cnt);
-    base = __shfl_sync(0xffffffffu, base, 0);
-    bool over = false;
-    for (int l = lane; l < cnt; l += 32) {
-        const long long slot = (long long)base + l;
-        if (slot < pcap)
-            pairs[slot] = stage[l];
-        else
-            over = true;
-    }
-    if (__any_sync(0xffffffffu, over) && lane == 0) atomicOr(counters + 2, 64);
-    __syncwarp();
-}
-
 __global__ void __launch_bounds__(32 * kEEPairWarps) k_ee_pairs(
     int cap, const uint32_t *__restrict__ skey, const int4 *__restrict__ r0,
     const float4 *__restrict__ r1, const float4 *__restrict__ r2, const int *__restrict__ rinst,
@@ -413,21 +396,11 @@ __global__ void __launch_bounds__(32 * kEEPairWarps) k_ee_pairs(
                     e2 = cj.w & kEEEdgeMask;
                 }
             }
-            const unsigned hm = __ballot_sync(kAll, hit);
-            if (hm) {
-                if (cnt + 32 > kEEPairStage) {
-                    ee_flush(stage, cnt, lane, pairs, pcap, counters);
-                    cnt = 0;
-                }
-                if (hit)
-                    stage[cnt + __popc(hm & ((1u << lane) - 1u))] =
-                        make_int2(min(e1, e2), max(e1, e2));
-                cnt += __popc(hm);
-                __syncwarp();
-            }
+            warp_stage_pair(hit, make_int2(min(e1, e2), max(e1, e2)), stage, kEEPairStage, cnt,
+                            lane, pairs, pcap, counters + kPairs, counters + 2, 64);
         }
     }
-    if (cnt) ee_flush(stage, cnt, lane, pairs, pcap, counters);
+    if (cnt) warp_flush_pairs(stage, cnt, lane, pairs, pcap, counters + kPairs, counters + 2, 64);
 }
 
 // step 4: distance bound over the step
