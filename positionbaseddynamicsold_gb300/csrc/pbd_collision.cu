@@ -15,9 +15,10 @@
 //      pair once); a cell whose bucket AABB misses the point's swept AABB
 //      grown by 3.61 h yields nothing; the kept buckets' entries are spread
 //      over the lanes (warp prefix sum), each entry checked for its exact
-//      cell and swept-AABB overlap; found pairs are staged per warp in
-//      shared memory and appended with one atomic per batch (warps loop
-//      over points, so a batch spans many points);
+//      cell and swept-AABB overlap, the point's own triangles dropped;
+//      found pairs are staged per warp in shared memory and appended with
+//      one atomic per batch (warps loop over points, so a batch spans many
+//      points);
 //   4. distance filter: a pair survives when a lower bound of the
 //      point-triangle distance over the step is within the pair's own reach
 //      sqrt((2h)^2 + r^2), r = 2h * longest / mean edge (at most 3.61 h).
@@ -212,8 +213,10 @@ __global__ void __launch_bounds__(32 * kTaskWarps) k_point_pairs(
         const int inst = point_inst ? point_inst[v] : 0;
         int4 mc = make_int4(0, 0, 0, 0);
         bool valid = false;
+        int inc_tri = -1;  // this lane's incident triangle
         if (lane < ninc) {
-            mc = tcell[pt_tri[f0 + lane]];
+            inc_tri = pt_tri[f0 + lane];
+            mc = tcell[inc_tri];
             valid = g.hashed || !outside(g, mc.x, mc.y, mc.z);
         }
         const unsigned vm = __ballot_sync(0xffffffffu, valid);
@@ -320,6 +323,11 @@ __global__ void __launch_bounds__(32 * kTaskWarps) k_point_pairs(
                             plz > th.z || phz < tl.z) &&
                           (!point_inst || tri_inst[tri] == inst);
                 }
+                // a triangle of the point itself is no candidate (the point is
+                // one of its vertices): matched against the incident list
+                if (__any_sync(0xffffffffu, hit))
+                    for (int q = 0; q < ninc; ++q)
+                        hit &= __shfl_sync(0xffffffffu, inc_tri, q) != tri;
                 warp_stage_pair(hit, make_int2(v, tri), stage, kPointPairStage, scnt, lane, pairs,
                                 cap, counters + 4, counters + 2, 16);
             }
