@@ -330,6 +330,12 @@ int pbd_ccd_vf_test_batch(const float *x12, const float *p12, const float *thick
 /* number of broadphase candidate pairs that reached the narrow phase in
  * the last CCD call, and the overflow flag */
 int pbd_colli_stats(pbd_colli *c, long long *candidates, long long *contacts, int *overflow);
+/* The (point, triangle) pairs the last CCD call's hash search handed to
+ * the distance filter, in device order: pairs of the reference's candidate
+ * set (CCD_SH_Extended, P/CCD.cpp:1541-1586) whose swept boxes meet, the
+ * point's own triangles left out.  *n = their count; min(*n, cap) pairs
+ * (point, triangle) are written to pairs when it is not NULL. */
+int pbd_colli_get_pairs(pbd_colli *c, int *pairs, long long cap, long long *n);
 
 /* ---- edge-edge CCD (declared only by the reference: Contact::EE,
  * P/CCD_Basic.h:14; EEResolve commented out, P/CCD.cpp:925-928) -------------- */

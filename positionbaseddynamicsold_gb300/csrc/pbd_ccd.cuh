@@ -296,6 +296,17 @@ __device__ __forceinline__ uint32_t bucket_of(const GridParams &g, int x, int y,
            (uint32_t)y * (uint32_t)g.size.x + (uint32_t)x;
 }
 
+// the cell size of an instance (the spatial hash's per-instance cells, or
+// its one cell)
+__device__ __forceinline__ float3 inst_cell_of(const GridParams &g, const float4 *ic, int n_ic,
+                                               int inst) {
+    if (inst >= 0 && inst < n_ic) {
+        float4 c = ic[inst];
+        return make_float3(c.x, c.y, c.z);
+    }
+    return g.cell;
+}
+
 // Append a warp's staged pairs (stage[0, cnt), filled by the whole warp) to
 // out with one atomic on *counter; slots at or past cap are dropped and set
 // flag_bit in *flags.  Called by all 32 lanes.

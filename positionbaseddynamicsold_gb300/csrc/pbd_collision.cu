@@ -187,6 +187,7 @@ __global__ void k_find_neighbors(int nt, GridParams g, const int4 *tcell, const 
 // and it belongs to the point's instance.
 constexpr int kTaskWarps = 8;
 constexpr int kPointPairStage = 256;  // pairs staged per warp, appended with one atomic
+constexpr unsigned long long kNear3 = 0x0000077707770777ull;  // 3x3x3 corner of a 4x4x4 block
 __global__ void __launch_bounds__(32 * kTaskWarps) k_point_pairs(
     int n, GridParams g, float margin, const int *__restrict__ pt_first,
     const int *__restrict__ pt_last, const int *__restrict__ pt_tri,
@@ -221,57 +222,82 @@ __global__ void __launch_bounds__(32 * kTaskWarps) k_point_pairs(
         }
         const unsigned vm = __ballot_sync(0xffffffffu, valid);
         if (!vm) continue;
-        // distinct valid incident cells: the lowest lane of each group of
-        // lanes holding the same cell
-        const unsigned same = __match_any_sync(0xffffffffu, valid ? mc.x : INT_MIN) &
-                              __match_any_sync(0xffffffffu, valid ? mc.y : INT_MIN) &
-                              __match_any_sync(0xffffffffu, valid ? mc.z : INT_MIN);
-        const unsigned dm =
-            __ballot_sync(0xffffffffu, valid && (same & vm & ((1u << lane) - 1u)) == 0u);
-        const bool single = __popc(dm) == 1;
-        // bounding box of the valid incident cells
-        int lx = valid ? mc.x : INT_MAX, ly = valid ? mc.y : INT_MAX, lz = valid ? mc.z : INT_MAX;
-        int hx = valid ? mc.x : INT_MIN, hy = valid ? mc.y : INT_MIN, hz = valid ? mc.z : INT_MIN;
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            lx = min(lx, __shfl_xor_sync(0xffffffffu, lx, o));
-            ly = min(ly, __shfl_xor_sync(0xffffffffu, ly, o));
-            lz = min(lz, __shfl_xor_sync(0xffffffffu, lz, o));
-            hx = max(hx, __shfl_xor_sync(0xffffffffu, hx, o));
-            hy = max(hy, __shfl_xor_sync(0xffffffffu, hy, o));
-            hz = max(hz, __shfl_xor_sync(0xffffffffu, hz, o));
-        }
+        // box of the valid incident cells
+        const int lx = __reduce_min_sync(0xffffffffu, valid ? mc.x : INT_MAX);
+        const int ly = __reduce_min_sync(0xffffffffu, valid ? mc.y : INT_MAX);
+        const int lz = __reduce_min_sync(0xffffffffu, valid ? mc.z : INT_MAX);
+        const int hx = __reduce_max_sync(0xffffffffu, valid ? mc.x : INT_MIN);
+        const int hy = __reduce_max_sync(0xffffffffu, valid ? mc.y : INT_MIN);
+        const int hz = __reduce_max_sync(0xffffffffu, valid ? mc.z : INT_MIN);
         v3 X0 = ld3(xv), P0 = ld3(pv);
         const float plx = fminf(X0.x, P0.x) - margin, phx = fmaxf(X0.x, P0.x) + margin;
         const float ply = fminf(X0.y, P0.y) - margin, phy = fmaxf(X0.y, P0.y) + margin;
         const float plz = fminf(X0.z, P0.z) - margin, phz = fmaxf(X0.z, P0.z) + margin;
-        const int ex = hx - lx + 3, ey = hy - ly + 3, ez = hz - lz + 3;
-        const int exy = ex * ey, ncell = exy * ez;
-        // ci -> (x, y, z) in the box by multiplying with ceil(2^32 / d),
-        // exact for ci * d < 2^32 (ex, exy >= 3; ci < ncell); boxes too large
-        // for that divide
-        const bool magic = (unsigned long long)ncell * (unsigned long long)exy < (1ull << 32);
-        const unsigned mex = 0xffffffffu / (unsigned)ex + 1u;
-        const unsigned mexy = 0xffffffffu / (unsigned)exy + 1u;
+        // Incident cells within a 2 x 2 x 2 block (nearly always): the union
+        // of their 27-neighbourhoods is a mask over the 4 x 4 x 4 block at
+        // (lx - 1, ly - 1, lz - 1), bit x + 4 y + 16 z, OR-reduced over the
+        // lanes.  Otherwise each cell of the box is checked against the
+        // distinct incident cells.
+        const bool compact = hx - lx <= 1 && hy - ly <= 1 && hz - lz <= 1;
+        unsigned long long nmask = 0;
+        unsigned dm = 0;
+        bool single = false;
+        int ex = 4, exy = 16, ncell = 64;
+        unsigned mex = 0, mexy = 0;
+        bool magic = false;
+        if (compact) {
+            const unsigned long long mine =
+                valid ? kNear3 << ((mc.x - lx) + 4 * (mc.y - ly) + 16 * (mc.z - lz)) : 0ull;
+            nmask = (unsigned long long)__reduce_or_sync(0xffffffffu, (unsigned)(mine >> 32))
+                        << 32 |
+                    __reduce_or_sync(0xffffffffu, (unsigned)mine);
+        } else {
+            // distinct valid incident cells: the lowest lane of each group of
+            // lanes holding the same cell
+            const unsigned same = __match_any_sync(0xffffffffu, valid ? mc.x : INT_MIN) &
+                                  __match_any_sync(0xffffffffu, valid ? mc.y : INT_MIN) &
+                                  __match_any_sync(0xffffffffu, valid ? mc.z : INT_MIN);
+            dm = __ballot_sync(0xffffffffu, valid && (same & vm & ((1u << lane) - 1u)) == 0u);
+            single = __popc(dm) == 1;
+            ex = hx - lx + 3;
+            exy = ex * (hy - ly + 3);
+            ncell = exy * (hz - lz + 3);
+            // ci -> (x, y, z) in the box by multiplying with ceil(2^32 / d),
+            // exact for ci * d < 2^32 (ex, exy >= 3; ci < ncell); boxes too
+            // large for that divide
+            magic = (unsigned long long)ncell * (unsigned long long)exy < (1ull << 32);
+            mex = 0xffffffffu / (unsigned)ex + 1u;
+            mexy = 0xffffffffu / (unsigned)exy + 1u;
+        }
         for (int base = 0; base < ncell; base += 32) {
             const int ci = base + lane;
-            const int qz = magic ? (int)__umulhi((unsigned)ci, mexy) : ci / exy;
-            const int rz = ci - qz * exy;
-            const int qy = magic ? (int)__umulhi((unsigned)rz, mex) : rz / ex;
-            const int cx = lx - 1 + (rz - qy * ex);
-            const int cy = ly - 1 + qy;
-            const int cz = lz - 1 + qz;
-            // within one cell of some valid incident cell (read from the lanes
-            // holding the distinct cells; with one cell every box cell is)
-            bool near = single;
-            unsigned m = single ? 0u : dm;
-            while (m) {
-                const int src = __ffs(m) - 1;
-                m &= m - 1;
-                const int sx = __shfl_sync(0xffffffffu, mc.x, src);
-                const int sy = __shfl_sync(0xffffffffu, mc.y, src);
-                const int sz = __shfl_sync(0xffffffffu, mc.z, src);
-                near |= abs(sx - cx) <= 1 && abs(sy - cy) <= 1 && abs(sz - cz) <= 1;
+            int cx, cy, cz;
+            bool near;
+            if (compact) {
+                cx = lx - 1 + (ci & 3);
+                cy = ly - 1 + ((ci >> 2) & 3);
+                cz = lz - 1 + (ci >> 4);
+                near = ((nmask >> ci) & 1ull) != 0;
+            } else {
+                const int qz = magic ? (int)__umulhi((unsigned)ci, mexy) : ci / exy;
+                const int rz = ci - qz * exy;
+                const int qy = magic ? (int)__umulhi((unsigned)rz, mex) : rz / ex;
+                cx = lx - 1 + (rz - qy * ex);
+                cy = ly - 1 + qy;
+                cz = lz - 1 + qz;
+                // within one cell of some valid incident cell (read from the
+                // lanes holding the distinct cells; with one cell every box
+                // cell is)
+                near = single;
+                unsigned m = single ? 0u : dm;
+                while (m) {
+                    const int src = __ffs(m) - 1;
+                    m &= m - 1;
+                    const int sx = __shfl_sync(0xffffffffu, mc.x, src);
+                    const int sy = __shfl_sync(0xffffffffu, mc.y, src);
+                    const int sz = __shfl_sync(0xffffffffu, mc.z, src);
+                    near |= abs(sx - cx) <= 1 && abs(sy - cy) <= 1 && abs(sz - cz) <= 1;
+                }
             }
             int cnt = 0, start = 0;
             if (ci < ncell && near && (g.hashed || !outside(g, cx, cy, cz))) {
@@ -1064,6 +1090,25 @@ int pbd_ccd_vf_test_batch(const float *x12, const float *p12, const float *thick
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     cudaStreamDestroy(s);
     PBD_CUDA(e);
+    return PBD_OK;
+}
+
+int pbd_colli_get_pairs(pbd_colli *c, int *pairs, long long cap, long long *n) {
+    PBD_CHECK(c && n && cap >= 0, PBD_ERR_ARG, "bad argument");
+    int cnt = 0;
+    if (c->counters.p) {
+        PBD_CUDA(cudaMemcpyAsync(&cnt, c->counters.p + 4, sizeof(int), cudaMemcpyDeviceToHost,
+                                 c->obj->stream));
+        PBD_CUDA(cudaStreamSynchronize(c->obj->stream));
+    }
+    const long long m = std::min<long long>(cnt, c->task_cap);
+    *n = m;
+    const long long k = std::min(m, cap);
+    if (pairs && k > 0) {
+        PBD_CUDA(cudaMemcpyAsync(pairs, c->pairs.p, sizeof(int2) * k, cudaMemcpyDeviceToHost,
+                                 c->obj->stream));
+        PBD_CUDA(cudaStreamSynchronize(c->obj->stream));
+    }
     return PBD_OK;
 }
 

@@ -209,17 +209,6 @@ __device__ __forceinline__ int cell_of(float v, float start, float cell) {
 }
 
 // step 1: boxes and entries
-// the cell size of an instance (the spatial hash's per-instance cells, or
-// its one cell)
-__device__ __forceinline__ float3 inst_cell_of(const GridParams &g, const float4 *ic, int n_ic,
-                                               int inst) {
-    if (inst >= 0 && inst < n_ic) {
-        float4 c = ic[inst];
-        return make_float3(c.x, c.y, c.z);
-    }
-    return g.cell;
-}
-
 __global__ void __launch_bounds__(256) k_ee_entries(int ne, GridParams g, float grow,
                                                     const float4 *__restrict__ icell, int n_icell,
                                                     const int2 *__restrict__ edges,

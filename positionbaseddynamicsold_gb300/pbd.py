@@ -73,6 +73,7 @@ EXPORTS = [
     "pbd_colli_set_acce_struct", "pbd_colli_set_thickness", "pbd_colli_set_iterations",
     "pbd_colli_set_response", "pbd_colli_set_capacity", "pbd_colli_ccd_sh_extended",
     "pbd_colli_collision_resolve_new", "pbd_colli_get_contacts", "pbd_colli_stats",
+    "pbd_colli_get_pairs",
     "pbd_ccd_vf_test_batch",
     "pbd_residual_noalloc",
     "pbd_scene_read_cache", "pbd_scene_read_txt", "pbd_scene_desc", "pbd_scene_destroy",
@@ -602,6 +603,16 @@ class CollisionSolver:
         _check(self.L.pbd_colli_get_contacts(self.h, _p(ids), _p(face), _p(t), _p(w), _p(n), h,
                                              C.byref(cnt)))
         return {"ids": ids[:h], "face": face[:h], "t": t[:h], "w": w[:h], "n": n[:h]}
+
+    def pairs(self):
+        """the hash search's (point, triangle) pairs of the last CCD call,
+        sorted"""
+        n = C.c_longlong()
+        _check(self.L.pbd_colli_get_pairs(self.h, None, 0, C.byref(n)))
+        out = np.zeros((max(n.value, 1), 2), np.int32)
+        _check(self.L.pbd_colli_get_pairs(self.h, _p(out), n.value, C.byref(n)))
+        out = out[: n.value]
+        return out[np.lexsort((out[:, 1], out[:, 0]))]
 
     def stats(self):
         a, b, c = C.c_longlong(), C.c_longlong(), C.c_int()
