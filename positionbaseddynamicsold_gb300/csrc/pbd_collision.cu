@@ -773,8 +773,7 @@ static int shs_alloc(pbd_shs *h) {
     PBD_TRY(h->etab.alloc(3 * nt));
     PBD_TRY(h->n_valid.alloc(1));
     PBD_TRY(h->btab.alloc(2 * ((size_t)h->n_buckets + 1)));
-    PBD_TRY(h->scr.hist.alloc(radix_hist_size((long long)nt)));
-    PBD_TRY(h->scr.carry.alloc(256));
+    PBD_TRY(radix_reserve(h->scr, (long long)nt, round8(h->key_bits)));
     PBD_CUDA(cudaMemsetAsync(h->btab.p, 0, sizeof(float4) * 2 * (h->n_buckets + 1), o->stream));
     PBD_CUDA(cudaMemsetAsync(h->n_valid.p, 0, sizeof(int), o->stream));
     h->skey = h->key.p;
@@ -1119,6 +1118,11 @@ int pbd_colli_stats(pbd_colli *c, long long *cand, long long *contacts, int *ove
         PBD_CUDA(cudaMemcpyAsync(hc, c->counters.p, sizeof(hc), cudaMemcpyDeviceToHost, c->obj->stream));
         PBD_CUDA(cudaStreamSynchronize(c->obj->stream));
     }
+    // a radix-sort look-back wait that ran out (never expected) shows as 256
+    int st = 0, st_ee = 0;
+    if (c->shs) PBD_TRY(radix_status(c->shs->scr, c->obj->stream, &st));
+    PBD_TRY(radix_status(c->ee_scr, c->obj->stream, &st_ee));
+    if (st || st_ee) hc[2] |= 256;
     if (cand) *cand = hc[0];
     if (contacts) *contacts = hc[1];
     if (overflow) *overflow = hc[2];

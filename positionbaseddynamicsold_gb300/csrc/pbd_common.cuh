@@ -118,13 +118,17 @@ struct HBuf {
 
 // ---- stable LSD radix sort (8-bit digits) of (key, int value) pairs --------
 // Sorts n elements (n read from d_count when non-null, capped by n_cap),
-// `bits` low key bits.  Buffers: keys/vals in and alt (same capacity), hist
-// of hist_size(n_cap) ints.  Returns the pointers holding the result.
+// `bits` low key bits.  Buffers: keys/vals in and alt (same capacity) and a
+// scratch (radix_reserve sizes it; radix_sort does when needed, which a
+// caller that captures the sort in a graph must have done before).  Returns
+// the pointers holding the result.
 struct SortScratch {
-    DBuf<int> hist;
-    DBuf<int> carry;
+    DBuf<unsigned> flags;   // look-back words, pass x tile x digit
+    DBuf<int> aux;          // digit counts per pass, tile counters, status
 };
-int radix_hist_size(long long n_cap);
+int radix_reserve(SortScratch &scr, long long n_cap, int bits);
+// nonzero when a look-back wait of some earlier sort ran out (never expected)
+int radix_status(const SortScratch &scr, cudaStream_t s, int *status);
 template <class K>
 int radix_sort(K *keys, int *vals, K *keys_alt, int *vals_alt, long long n_cap,
                const int *d_count, int bits, SortScratch &scr, cudaStream_t s,

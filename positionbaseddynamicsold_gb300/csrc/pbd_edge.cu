@@ -561,6 +561,7 @@ int ee_prepare(pbd_colli *c) {
     PBD_TRY(c->ee_tsu.alloc(c->contact_cap));
     PBD_TRY(c->ee_hpair.alloc(c->contact_cap));
     c->ee_log2 = pow2_at_least(2 * ecap, 24);
+    PBD_TRY(radix_reserve(c->ee_scr, ecap, (c->ee_log2 + 7) / 8 * 8));
     return PBD_OK;
 }
 
