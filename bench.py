@@ -374,7 +374,7 @@ def run_ours(args, rank, world):
                       "overflow": stats.get("overflow"), "relative_residual": residual},
     }
     if rank == 0 and not args.no_cpu_baseline:
-        out["cpu_baseline"] = cpu_baseline(sc, cfg, colli_on, obj)
+        out["cpu_baseline"] = cpu_baseline(sc, cfg, colli_on, obj, args.workload)
     if rank == 0 and not args.no_learned_eval:
         out["learned_warm_start"] = learned_eval()
     return out
@@ -407,91 +407,214 @@ def learned_eval(n_traj=4, substeps=40):
     return out
 
 
-def oracle_state(sc, obj):
-    st = {"pos": obj.positions(), "vel": obj.velocities()}
-    return st
-
-
 def cpu_colli(sc):
     return {"center": (0.0, 0.0, 0.0), "cell": sc["colli"]["cell"], "bounded": False,
             "thickness": sc["colli"]["thickness"], "tri_idx": sc["tri_idx"], "mass_weighted": 0,
             "resolve_passes": 1, "contact_cap": 1 << 21}
 
 
-def cpu_baseline(sc, cfg, colli_on, obj):
-    """The reference CPU path (oracle restatement) on one thread, one full
-    substep of the current state."""
-    from oracle.oracle import Oracle
-    orc = Oracle()
-    st = oracle_state(sc, obj)
-    t0 = time.perf_counter()
-    orc.substep_cpu_ref(sc, st, cfg["gs_iterations"], DT, G,
-                        colli=cpu_colli(sc) if colli_on else None)
+class RefSampler:
+    """The reference's CPU path (the oracle's restatement of it) in bounded
+    steps, each a fraction phi = 1 / (iterations * m) of a substep, in the
+    reference's order:
+
+    * GS: the next phi * iterations * n_prims prims of projectConstraintCPU's
+      sequential loop (one full iteration per step when m = 1);
+    * CCD: the next phi * 3 * n_tris triangles of CCD_SH_Extended's loop
+      (three detection passes per substep), against the table UpdateSH
+      built at the pass's first slice;
+    * response: the contacts that slice found, resolved five times (fifteen
+      response passes per substep over one pass's contacts);
+    * advection at the first step of a substep, integration at the last;
+      with a sphere, ColliWithShpGrd after each full GS iteration.
+
+    m keeps a step near 2,000 triangle queries so a step stays a bounded
+    sample on every workload; the substep rate is phi * steps / time."""
+
+    def __init__(self, sc, cfg, colli_on, pos, vel, sphere=None):
+        import ctypes as C
+        from oracle.oracle import Oracle, OrcContact, _ptr
+        self.C, self.ptr = C, _ptr
+        self.orc = Oracle()
+        self.L = self.orc.lib
+        self.L.orc_ccd_sh_extended_ref_range_tab.restype = C.c_int64
+        self.L.orc_sh_build.restype = C.c_void_p
+        self.L.orc_sh_build.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]
+        self.L.orc_sh_free.argtypes = [C.c_void_p]
+        self.table = None
+        self.c = self.orc.constraints(sc)
+        self.colli_on = colli_on
+        self.pos = np.ascontiguousarray(pos, np.float32).copy()
+        self.vel = np.ascontiguousarray(vel, np.float32).copy()
+        self.prdp = self.pos.copy()
+        self.n = len(self.pos)
+        self.nt = len(sc["tri_idx"])
+        self.n_prims = int(self.c.n_prims)
+        self.iters = cfg["gs_iterations"]
+        self.m = max(1, -(-3 * self.nt // (self.iters * 2000))) if colli_on else 1
+        self.phi = 1.0 / (self.iters * self.m)
+        self.gs_chunk = max(1, round(self.phi * self.iters * self.n_prims))
+        self.ccd_chunk = max(1, round(self.phi * 3 * self.nt))
+        self.gp = self.tp = 0
+        self.colli = self.orc._colli(cpu_colli(sc)) if colli_on else None
+        self.cap = 1 << 21
+        self.arr = (OrcContact * self.cap)()
+        self.tri = np.ascontiguousarray(sc["tri_idx"], np.int32)
+        self.g = np.ascontiguousarray(G)
+        self.mass = np.ascontiguousarray(sc["mass"])
+        self.sphere = None if sphere is None else np.ascontiguousarray(sphere[:3], np.float32)
+        self.radius = 0.0 if sphere is None else float(sphere[3])
+        self.k = 0
+
+    def step(self):
+        C, P, L = self.C, self.ptr, self.L
+        per = self.iters * self.m
+        s = self.k % per
+        if s == 0:
+            L.orc_advect_cpu(self.n, C.c_float(DT), P(self.g), P(self.vel), P(self.prdp),
+                             P(self.pos))
+        left = self.gs_chunk
+        while left:
+            a = self.gp
+            b = min(self.n_prims, a + left)
+            L.orc_project_cpu_range(C.byref(self.c), P(self.mass), P(self.prdp), a, b)
+            left -= b - a
+            self.gp = b % self.n_prims
+            if b == self.n_prims and self.sphere is not None:  # ColliWithShpGrd per iteration
+                L.orc_colli_sphere(self.n, P(self.prdp), P(self.sphere), C.c_float(self.radius))
+        if self.colli_on:
+            t0 = self.tp
+            t1 = min(self.nt, t0 + self.ccd_chunk)
+            if t0 == 0:  # a detection pass starts: UpdateSH bins every triangle once
+                if self.table:
+                    L.orc_sh_free(self.table)
+                self.table = L.orc_sh_build(C.byref(self.colli.grid), self.nt, P(self.tri),
+                                            P(self.prdp))
+            h = L.orc_ccd_sh_extended_ref_range_tab(
+                C.byref(self.colli.grid), C.c_void_p(self.table), self.nt, P(self.tri),
+                P(self.pos), P(self.prdp), C.c_float(self.colli.thickness), t0, t1, self.arr,
+                C.c_int64(self.cap))
+            self.tp = t1 % self.nt
+            L.orc_collision_resolve_ref(int(min(h, self.cap)), self.arr, P(self.pos),
+                                        P(self.prdp), 5, C.c_float(self.colli.thickness))
+        if s == per - 1:
+            L.orc_integrate(self.n, C.c_float(DT), P(self.vel), P(self.prdp), P(self.pos))
+        self.k += 1
+
+    def sample(self):
+        return ("each step = 1/%d substep: %d of %d prims of one sequential GS iteration%s; "
+                "1 host thread" % (self.iters * self.m, self.gs_chunk, self.n_prims,
+                                   ", %d of %d triangles of a CCD pass, its contacts resolved 5 "
+                                   "times" % (self.ccd_chunk, self.nt) if self.colli_on else ""))
+
+
+class BatchRefSampler:
+    """batch512 on the reference, which has no batches: each cloth is its own
+    simulation with its own spatial hash (cell 2 x its mean rest edge) and
+    sphere, run one after another.  A sample of every `every`-th instance,
+    each built exactly as in the batch, advances in RefSampler steps taken
+    round-robin; the batch's substep time is the sampled instances' substep
+    times summed and scaled by the points of all instances over theirs."""
+
+    def __init__(self, cfg, n_inst=512, seed=0, every=32):
+        from positionbaseddynamicsold_gb300 import scenes
+        sizes = scenes.batched_cloth_points(n_inst, seed=seed)
+        self.ids = list(range(0, n_inst, every))
+        self.points = [sizes[i] for i in self.ids]
+        self.total_points = int(sum(sizes))
+        self.samplers = []
+        for i in self.ids:
+            sc = scenes.batched_cloths(n_inst, seed=seed, subset=[i])
+            sc["colli"] = {"cell": 2.0 * scenes.mean_rest_edge(sc), "thickness": 1e-3}
+            self.samplers.append(RefSampler(sc, cfg, True, sc["pos"], sc["vel"],
+                                            sphere=sc["spheres"][0]))
+        self.reset()
+
+    def reset(self):
+        self.t = [0.0] * len(self.samplers)
+        self.n = [0] * len(self.samplers)
+        self.k = 0
+
+    def step(self):
+        j = self.k % len(self.samplers)
+        t0 = time.perf_counter()
+        self.samplers[j].step()
+        self.t[j] += time.perf_counter() - t0
+        self.n[j] += 1
+        self.k += 1
+
+    def value(self):
+        done = [j for j in range(len(self.samplers)) if self.n[j]]
+        tsub = sum(self.t[j] / (self.n[j] * self.samplers[j].phi) for j in done)
+        pts = sum(self.points[j] for j in done)
+        return pts / (tsub * self.total_points)
+
+    def sample(self):
+        return ("instances %s of 512 (%d of %d points) simulated separately, round-robin "
+                "RefSampler steps (1/15 to 1/%d substep each: a GS iteration share, a CCD "
+                "pass share, its contacts resolved 5 times, the sphere per iteration), "
+                "scaled to all instances by points; 1 host thread"
+                % (",".join(map(str, self.ids)), sum(self.points), self.total_points,
+                   max(s.iters * s.m for s in self.samplers)))
+
+
+def cpu_baseline(sc, cfg, colli_on, obj, workload, budget_s=10.0):
+    """The reference CPU path (oracle restatement) on one thread: RefSampler
+    steps from the timed state for about budget_s seconds (batch512: the
+    instances' own simulations from their start states)."""
+    if workload == "batch512":
+        rs = BatchRefSampler(cfg)
+        for _ in range(len(rs.samplers)):
+            rs.step()  # warm-up
+        rs.reset()
+        t0 = time.perf_counter()
+        while rs.k < 2 * len(rs.samplers) or time.perf_counter() - t0 < budget_s:
+            rs.step()
+        dt = time.perf_counter() - t0
+        return {"value": rs.value(), "unit": "substeps/s", "cores": 1, "kind": "port",
+                "sample": "%d steps in %.1f s; %s" % (rs.k, dt, rs.sample()),
+                "host_cores_available": os.cpu_count()}
+    rs = RefSampler(sc, cfg, colli_on, obj.positions(), obj.velocities())
+    rs.step()  # warm-up
+    steps, t0 = 0, time.perf_counter()
+    while steps < 3 or time.perf_counter() - t0 < budget_s:
+        rs.step()
+        steps += 1
     dt = time.perf_counter() - t0
-    return {"value": 1.0 / dt, "unit": "substeps/s", "cores": 1, "kind": "port",
-            "sample": "1 full substep (%d GS iterations%s) of the timed state, 1 host thread"
-                      % (cfg["gs_iterations"], ", 3 CCD passes" if colli_on else ""),
+    return {"value": steps * rs.phi / dt, "unit": "substeps/s", "cores": 1, "kind": "port",
+            "sample": "%d steps in %.1f s; %s" % (steps, dt, rs.sample()),
             "host_cores_available": os.cpu_count()}
 
 
 def run_reference(args):
     """The reference's CPU implementation of the path (the oracle's
     restatement of it: the reference sources are not present on the GPU
-    host).  One step = one fifteenth of a substep: one sequential GS
-    iteration, one response pass and a fifth of a CCD pass (triangle slice
-    in the reference's loop order); 15 steps hold one substep's work."""
-    import ctypes as C
-    from oracle.oracle import Oracle, OrcContact, _ptr
+    host), in RefSampler steps from the workload's start state."""
     sc, cfg, colli_on, tl = make_workload(args.workload)
-    orc = Oracle()
-    L = orc.lib
-    c = orc.constraints(sc)
-    pos = sc["pos"].copy()
-    # start from a contact state like the timed arm: drop the cloth onto the sphere
-    if args.workload == "drape256":
-        pos[:sc["n_cloth_points"], 1] -= np.float32(0.099)
-    vel = sc["vel"].copy()
-    prdp = pos.copy()
-    n = len(pos)
-    iters = cfg["gs_iterations"]
-    slices = iters
-    ccd_slices = 5
-    colli = orc._colli(cpu_colli(sc)) if colli_on else None
-    cap = 1 << 21
-    arr = (OrcContact * cap)()
-    nt = len(sc["tri_idx"])
-    tri = np.ascontiguousarray(sc["tri_idx"], np.int32)
-    g = np.ascontiguousarray(G)
-    mass = np.ascontiguousarray(sc["mass"])
-
-    def ref_step(k):
-        s = k % slices
-        if s == 0:
-            L.orc_advect_cpu(n, C.c_float(DT), _ptr(g), _ptr(vel), _ptr(prdp), _ptr(pos))
-        h = 0
-        if colli_on:
-            q = s % ccd_slices
-            t0, t1 = q * nt // ccd_slices, (q + 1) * nt // ccd_slices
-            h = L.orc_ccd_sh_extended_ref_range(C.byref(colli.grid), nt, _ptr(tri), _ptr(pos),
-                                                _ptr(prdp), C.c_float(colli.thickness), t0, t1,
-                                                arr, C.c_int64(cap))
-        L.orc_project_cpu(C.byref(c), 1, _ptr(mass), _ptr(prdp), n, None, C.c_float(0.0))
-        if colli_on:
-            L.orc_collision_resolve_ref(int(min(h, cap)), arr, _ptr(pos), _ptr(prdp), 1,
-                                        C.c_float(colli.thickness))
-        if s == slices - 1:
-            L.orc_integrate(n, C.c_float(DT), _ptr(vel), _ptr(prdp), _ptr(pos))
-
-    L.orc_ccd_sh_extended_ref_range.restype = C.c_int64
-    for k in range(args.warmup):
-        ref_step(k)
-    t0 = time.perf_counter()
-    for k in range(args.steps):
-        ref_step(args.warmup + k)
-    dt = time.perf_counter() - t0
-    value = args.steps / dt / slices
-    sample = ("each step = 1/%d substep: one sequential GS iteration, one response pass%s; "
-              "1 host thread" % (slices, ", 1/5 of a CCD pass" if colli_on else ""))
+    if args.workload == "batch512":
+        rs = BatchRefSampler(cfg)
+        for _ in range(args.warmup):
+            rs.step()
+        rs.reset()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            rs.step()
+        dt = time.perf_counter() - t0
+        value = rs.value()
+    else:
+        pos = sc["pos"].copy()
+        # start from a contact state like the timed arm: drop the cloth onto the sphere
+        if args.workload == "drape256":
+            pos[:sc["n_cloth_points"], 1] -= np.float32(0.099)
+        rs = RefSampler(sc, cfg, colli_on, pos, sc["vel"])
+        for _ in range(args.warmup):
+            rs.step()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            rs.step()
+        dt = time.perf_counter() - t0
+        value = args.steps * rs.phi / dt
+    sample = rs.sample()
     return {"impl": "reference", "metric": METRIC, "value": value, "unit": "substeps/s",
             "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": dt * 1e3 / args.steps, "higher_is_better": True, "scaling": "weak",

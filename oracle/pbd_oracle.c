@@ -509,33 +509,39 @@ void orc_colli_sphere(int n, float *prdp, const float *center, float radius)
     }
 }
 
+void orc_project_cpu_range(const orc_constraints *c, const float *mass, float *prdp,
+                           int p0, int p1)
+{
+    for (int i = p0; i < p1; ++i) {
+        if (c->prim_list[2 * i + 1] != 2) continue;
+        int i0 = c->indices[c->prim_list[2 * i]];
+        int i1 = c->indices[c->prim_list[2 * i] + 1];
+        f3 p0v = ld3(prdp + 3 * i0), p1v = ld3(prdp + 3 * i1);
+        float d = dist3(p0v, p1v);
+        /* normalize as compiled in the reference's .cu translation unit:
+         * the host rsqrtf there evaluates 1/sqrt in double */
+        f3 r0 = sub(p0v, p1v);
+        f3 r = mul(r0, (float)(1.0 / sqrt((double)dot(r0, r0))));
+        float m0 = mass[i0], m1 = mass[i1];
+        float rest = c->rest_length[i];
+        /* P/PBD_cuda.cu:1113-1123, k = 1 */
+        f3 dp1 = mk(-m0 / (m0 + m1) * (d - rest) * r.x, -m0 / (m0 + m1) * (d - rest) * r.y,
+                    -m0 / (m0 + m1) * (d - rest) * r.z);
+        f3 dp2 = mk(m1 / (m0 + m1) * (d - rest) * r.x, m1 / (m0 + m1) * (d - rest) * r.y,
+                    m1 / (m0 + m1) * (d - rest) * r.z);
+        dp1 = mul(dp1, 1.0f);
+        dp2 = mul(dp2, 1.0f);
+        st3(prdp + 3 * i0, add(p0v, dp1));
+        st3(prdp + 3 * i1, add(ld3(prdp + 3 * i1), dp2));
+    }
+}
+
 void orc_project_cpu(const orc_constraints *c, int iterations,
                      const float *mass, float *prdp, int n_points,
                      const float *sphere_center, float sphere_radius)
 {
     for (int ii = 0; ii < iterations; ++ii) {
-        for (int i = 0; i < c->n_prims; ++i) {
-            if (c->prim_list[2 * i + 1] != 2) continue;
-            int i0 = c->indices[c->prim_list[2 * i]];
-            int i1 = c->indices[c->prim_list[2 * i] + 1];
-            f3 p0 = ld3(prdp + 3 * i0), p1 = ld3(prdp + 3 * i1);
-            float d = dist3(p0, p1);
-            /* normalize as compiled in the reference's .cu translation unit:
-             * the host rsqrtf there evaluates 1/sqrt in double */
-            f3 r0 = sub(p0, p1);
-            f3 r = mul(r0, (float)(1.0 / sqrt((double)dot(r0, r0))));
-            float m0 = mass[i0], m1 = mass[i1];
-            float rest = c->rest_length[i];
-            /* P/PBD_cuda.cu:1113-1123, k = 1 */
-            f3 dp1 = mk(-m0 / (m0 + m1) * (d - rest) * r.x, -m0 / (m0 + m1) * (d - rest) * r.y,
-                        -m0 / (m0 + m1) * (d - rest) * r.z);
-            f3 dp2 = mk(m1 / (m0 + m1) * (d - rest) * r.x, m1 / (m0 + m1) * (d - rest) * r.y,
-                        m1 / (m0 + m1) * (d - rest) * r.z);
-            dp1 = mul(dp1, 1.0f);
-            dp2 = mul(dp2, 1.0f);
-            st3(prdp + 3 * i0, add(p0, dp1));
-            st3(prdp + 3 * i1, add(ld3(prdp + 3 * i1), dp2));
-        }
+        orc_project_cpu_range(c, mass, prdp, 0, c->n_prims);
         if (sphere_center) orc_colli_sphere(n_points, prdp, sphere_center, sphere_radius);
     }
 }
@@ -991,15 +997,36 @@ int64_t orc_ccd_sh_extended_ref(const orc_grid *g, int n_tris, const int *tri_id
                                          out, cap);
 }
 
-int64_t orc_ccd_sh_extended_ref_range(const orc_grid *g, int n_tris, const int *tri_idx,
-                                      const float *pos, const float *prdp, float thickness,
-                                      int tri_begin, int tri_end, orc_contact *out, int64_t cap)
+struct orc_sh_table {
+    int *cells;
+    cell_table tb;
+};
+
+orc_sh_table *orc_sh_build(const orc_grid *g, int n_tris, const int *tri_idx, const float *prdp)
 {
-    /* UpdateSH(prdP) (binning of every triangle) then, per triangle of the
-     * range, FindNeighbors and the point x neighbor loop
-     * (P/CCD.cpp:1530-1586) */
-    int *cells = (int *)malloc(sizeof(int) * 3 * (size_t)(n_tris > 0 ? n_tris : 1));
-    cell_table tb = build_table(g, n_tris, tri_idx, prdp, cells);
+    orc_sh_table *t = (orc_sh_table *)malloc(sizeof(orc_sh_table));
+    t->cells = (int *)malloc(sizeof(int) * 3 * (size_t)(n_tris > 0 ? n_tris : 1));
+    t->tb = build_table(g, n_tris, tri_idx, prdp, t->cells);
+    return t;
+}
+
+void orc_sh_free(orc_sh_table *t)
+{
+    if (!t) return;
+    free(t->tb.e);
+    free(t->cells);
+    free(t);
+}
+
+int64_t orc_ccd_sh_extended_ref_range_tab(const orc_grid *g, const orc_sh_table *t, int n_tris,
+                                          const int *tri_idx, const float *pos,
+                                          const float *prdp, float thickness, int tri_begin,
+                                          int tri_end, orc_contact *out, int64_t cap)
+{
+    /* per triangle of the range, FindNeighbors and the point x neighbor
+     * loop (P/CCD.cpp:1541-1586) over a table UpdateSH built */
+    const int *cells = t->cells;
+    const cell_table tb = t->tb;
     int nbcap = 1024;
     int *nb = (int *)malloc(sizeof(int) * (size_t)nbcap);
     int64_t h = 0;
@@ -1046,8 +1073,19 @@ int64_t orc_ccd_sh_extended_ref_range(const orc_grid *g, int n_tris, const int *
     }
     free(keys);
     free(nb);
-    free(tb.e);
-    free(cells);
+    return h;
+}
+
+int64_t orc_ccd_sh_extended_ref_range(const orc_grid *g, int n_tris, const int *tri_idx,
+                                      const float *pos, const float *prdp, float thickness,
+                                      int tri_begin, int tri_end, orc_contact *out, int64_t cap)
+{
+    /* UpdateSH(prdP) (binning of every triangle, P/CCD.cpp:1530-1540), then
+     * the range */
+    orc_sh_table *t = orc_sh_build(g, n_tris, tri_idx, prdp);
+    int64_t h = orc_ccd_sh_extended_ref_range_tab(g, t, n_tris, tri_idx, pos, prdp, thickness,
+                                                  tri_begin, tri_end, out, cap);
+    orc_sh_free(t);
     return h;
 }
 

@@ -140,6 +140,9 @@ void orc_project_one(const orc_constraints *c, int prim, int iter,
 void orc_project_cpu(const orc_constraints *c, int iterations,
                      const float *mass, float *prdp, int n_points,
                      const float *sphere_center, float sphere_radius);
+/* one sequential pass of projectConstraintCPU's loop over prims [p0, p1) */
+void orc_project_cpu_range(const orc_constraints *c, const float *mass, float *prdp,
+                           int p0, int p1);
 
 /* ColliWithShpGrd (P/PBD_cuda.cu:1519-1573). */
 void orc_colli_sphere(int n, float *prdp, const float *center, float radius);
@@ -233,6 +236,16 @@ int64_t orc_ccd_sh_extended_ref(const orc_grid *g, int n_tris, const int *tri_id
 /* The same loop restricted to triangles [tri_begin, tri_end) of the outer
  * loop (the neighbour search still bins every triangle): a slice of one
  * CCD pass, used to time the reference path in bounded pieces. */
+/* UpdateSH's table over every triangle (binned by prdp), and the ranged
+ * detection below run against it (a detection pass = one build, then its
+ * triangle ranges). */
+typedef struct orc_sh_table orc_sh_table;
+orc_sh_table *orc_sh_build(const orc_grid *g, int n_tris, const int *tri_idx, const float *prdp);
+void orc_sh_free(orc_sh_table *t);
+int64_t orc_ccd_sh_extended_ref_range_tab(const orc_grid *g, const orc_sh_table *t, int n_tris,
+                                          const int *tri_idx, const float *pos,
+                                          const float *prdp, float thickness, int tri_begin,
+                                          int tri_end, orc_contact *out, int64_t cap);
 int64_t orc_ccd_sh_extended_ref_range(const orc_grid *g, int n_tris, const int *tri_idx,
                                       const float *pos, const float *prdp, float thickness,
                                       int tri_begin, int tri_end, orc_contact *out, int64_t cap);
