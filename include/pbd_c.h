@@ -328,7 +328,10 @@ int pbd_colli_get_contacts(pbd_colli *c, int *ids, int *face, float *t, double *
 int pbd_ccd_vf_test_batch(const float *x12, const float *p12, const float *thickness, int n,
                           int *hit, float *t, double *w, float *nrm);
 /* number of broadphase candidate pairs that reached the narrow phase in
- * the last CCD call, and the overflow flag */
+ * the last CCD call, and the overflow word: 1 candidates, 2 contacts, 4 a
+ * point with more than 16 incident triangles, 16 hash-search pairs,
+ * 32/64/128/256 edge-edge entries / pairs / candidates / contacts, 512 a
+ * radix-sort wait that ran out (never expected) */
 int pbd_colli_stats(pbd_colli *c, long long *candidates, long long *contacts, int *overflow);
 /* The (point, triangle) pairs the last CCD call's hash search handed to
  * the distance filter, in device order: pairs of the reference's candidate

@@ -1118,11 +1118,11 @@ int pbd_colli_stats(pbd_colli *c, long long *cand, long long *contacts, int *ove
         PBD_CUDA(cudaMemcpyAsync(hc, c->counters.p, sizeof(hc), cudaMemcpyDeviceToHost, c->obj->stream));
         PBD_CUDA(cudaStreamSynchronize(c->obj->stream));
     }
-    // a radix-sort look-back wait that ran out (never expected) shows as 256
+    // a radix-sort look-back wait that ran out (never expected) shows as 512
     int st = 0, st_ee = 0;
     if (c->shs) PBD_TRY(radix_status(c->shs->scr, c->obj->stream, &st));
     PBD_TRY(radix_status(c->ee_scr, c->obj->stream, &st_ee));
-    if (st || st_ee) hc[2] |= 256;
+    if (st || st_ee) hc[2] |= 512;
     if (cand) *cand = hc[0];
     if (contacts) *contacts = hc[1];
     if (overflow) *overflow = hc[2];
