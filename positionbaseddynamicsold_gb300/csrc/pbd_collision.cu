@@ -311,7 +311,7 @@ __global__ void __launch_bounds__(32 * kTaskWarps) k_point_pairs(
                     start = rs;
                 }
             }
-            // flat entry index space of this round's kept buckets
+            // flat entry index space of these 32 cells' kept buckets
             int incl = cnt;
 #pragma unroll
             for (int o = 1; o < 32; o <<= 1) {
