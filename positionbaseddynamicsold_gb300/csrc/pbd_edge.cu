@@ -540,8 +540,10 @@ int ee_prepare(pbd_colli *c) {
         PBD_TRY(c->ee_edges.upload(e.data(), std::max<size_t>(e.size(), 1), s));
     }
     const long long ne = std::max(c->ee_n, 1);
-    // entries are indexed with 32-bit ints on the device
-    if (!c->ee_entry_cap) c->ee_entry_cap = std::min(1LL << 30, std::max(1LL << 20, 16 * ne));
+    // entries are indexed with 32-bit ints on the device, and the radix sort
+    // counts them in 30 bits
+    if (!c->ee_entry_cap)
+        c->ee_entry_cap = std::min((1LL << 30) - 1, std::max(1LL << 20, 16 * ne));
     const long long ecap = c->ee_entry_cap;
     PBD_TRY(c->ee_lo.alloc(ne));
     PBD_TRY(c->ee_hi.alloc(ne));
