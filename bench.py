@@ -420,9 +420,10 @@ class RefSampler:
 
     * GS: the next phi * iterations * n_prims prims of projectConstraintCPU's
       sequential loop (one full iteration per step when m = 1);
-    * CCD: the next phi * 3 * n_tris triangles of CCD_SH_Extended's loop
-      (three detection passes per substep), against the table UpdateSH
-      built at the pass's first slice;
+    * CCD: a slice of phi * 3 * n_tris consecutive triangles of
+      CCD_SH_Extended's loop (three detection passes per substep), against
+      the table UpdateSH built at the pass's first slice; a pass's slices
+      are taken in a stride order that spreads a short run over the mesh;
     * response: the contacts that slice found, resolved five times (fifteen
       response passes per substep over one pass's contacts);
     * advection at the first step of a substep, integration at the last;
@@ -455,7 +456,14 @@ class RefSampler:
         self.phi = 1.0 / (self.iters * self.m)
         self.gs_chunk = max(1, round(self.phi * self.iters * self.n_prims))
         self.ccd_chunk = max(1, round(self.phi * 3 * self.nt))
-        self.gp = self.tp = 0
+        # a pass's triangle slices, visited in a stride order coprime to
+        # their count so that a short run samples the whole mesh
+        self.n_slices = max(1, -(-self.nt // self.ccd_chunk))
+        stride = max(1, int(self.n_slices * 0.618))
+        while np.gcd(stride, self.n_slices) != 1:
+            stride += 1
+        self.slice_order = [(j * stride) % self.n_slices for j in range(self.n_slices)]
+        self.gp = self.sk = 0
         self.colli = self.orc._colli(cpu_colli(sc)) if colli_on else None
         self.cap = 1 << 21
         self.arr = (OrcContact * self.cap)()
@@ -483,9 +491,9 @@ class RefSampler:
             if b == self.n_prims and self.sphere is not None:  # ColliWithShpGrd per iteration
                 L.orc_colli_sphere(self.n, P(self.prdp), P(self.sphere), C.c_float(self.radius))
         if self.colli_on:
-            t0 = self.tp
+            t0 = self.slice_order[self.sk] * self.ccd_chunk
             t1 = min(self.nt, t0 + self.ccd_chunk)
-            if t0 == 0:  # a detection pass starts: UpdateSH bins every triangle once
+            if self.sk == 0:  # a detection pass starts: UpdateSH bins every triangle once
                 if self.table:
                     L.orc_sh_free(self.table)
                 self.table = L.orc_sh_build(C.byref(self.colli.grid), self.nt, P(self.tri),
@@ -494,7 +502,7 @@ class RefSampler:
                 C.byref(self.colli.grid), C.c_void_p(self.table), self.nt, P(self.tri),
                 P(self.pos), P(self.prdp), C.c_float(self.colli.thickness), t0, t1, self.arr,
                 C.c_int64(self.cap))
-            self.tp = t1 % self.nt
+            self.sk = (self.sk + 1) % self.n_slices
             L.orc_collision_resolve_ref(int(min(h, self.cap)), self.arr, P(self.pos),
                                         P(self.prdp), 5, C.c_float(self.colli.thickness))
         if s == per - 1:

@@ -97,6 +97,11 @@ def test_one_substep_of_steps_covers_one_substep_of_work(workload):
     assert abs(rs.gs_chunk * per - rs.iters * rs.n_prims) <= per
     assert abs(rs.ccd_chunk * per - 3 * rs.nt) <= per
     assert rs.ccd_chunk <= 2100
+    # a pass visits every slice once, consecutive steps far apart
+    assert sorted(rs.slice_order) == list(range(rs.n_slices))
+    assert rs.n_slices * rs.ccd_chunk >= rs.nt > (rs.n_slices - 1) * rs.ccd_chunk
+    if rs.n_slices > 10:
+        assert abs(rs.slice_order[1] - rs.slice_order[0]) > rs.n_slices // 4
 
 
 def test_batch_scaling_by_points():
