@@ -19,10 +19,11 @@ the object's stream.
 Metric: cloth substeps/s.  `e2e` is the same step through the C ABI with
 the state in page-locked host memory: upload positions and velocities, step,
 read them back, every step, replaying the first min(K, 100) timed substeps
-from the state they started from.  `cpu_baseline` times the reference's CPU path (the
-oracle's restatement: sequential GS, triangle-ordered CCD with
-de-duplication by scan, sequential response) for one full substep of the
-same state on one host thread.
+from the state they started from.  `cpu_baseline` times the reference's CPU
+path (the oracle's restatement: sequential GS, triangle-ordered CCD with
+de-duplication by scan, sequential response) on one host thread from the
+timed state, in bounded RefSampler steps for about 10 s; `--impl reference`
+times the same steps from the workload's start state.
 
 Other modes: --solve residual runs every substep to a stretch-residual
 target (--target, at most --max-sweeps sweeps in chunks of --chunk, the loop
@@ -33,7 +34,9 @@ compares the trained network with the plain sweeps on held-out cloths of its
 training family (see learned_eval).
 
 Multi-GPU: a single cloth does not shard; N GPUs run N independent replicas
-(value = replicas x substeps / slowest replica's time).
+(value = replicas x substeps / slowest replica's time).  batch512 shards its
+instances over the ranks, balanced by points, with no exchange on the data
+path.
 """
 from __future__ import annotations
 
