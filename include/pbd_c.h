@@ -424,12 +424,16 @@ int pbd_object_save_cache(pbd_object *obj, const char *topol_path, const char *c
  * under a fixed device-memory budget).  Partial sums live in a 1 MiB
  * file-scope device array that every GPU loading the library keeps until
  * exit; calls whose work overlaps on the GPU race on it.  The first call on a
- * device looks the array's address up (make it before any stream capture).
+ * device looks the array's address up (make it before any stream capture);
+ * a later call looks it up again when the device's context changed (after
+ * cudaDeviceReset the library's module, and the array, can be reloaded at
+ * another address).
  *   d_pos4       float4 per point (xyz used), 16-byte aligned
  *   d_dist_idx   int2 per distance constraint, d_rest_length float each
  *   d_bend_idx   int4 {e0, e1, wA, wB} per bending constraint, with
  *                d_rest_angle and d_hinge_rest (rest hinge length) each
- *   d_out        3 doubles on the device: residual, sum C^2, sum L^2
+ *   d_out        3 doubles on the device, 8-byte aligned: residual, sum C^2,
+ *                sum L^2
  *   stream       cudaStream_t (NULL = legacy default stream)
  * At most 16,777,216 constraints in total (PBD_ERR_ARG beyond).  A point id
  * outside [0, n_points) is skipped and the residual written as NaN. */

@@ -54,6 +54,10 @@ def build_oracle(force: bool = False) -> str:
 
 
 def find_reference(ref_root: str | None = None) -> str | None:
+    """The reference's source folder: the argument, else PBD_REFERENCE_ROOT,
+    else the read-only checkout's mount point on the development machine
+    (this recipe is the one place that reads the sources there; the GPU
+    host has no checkout and uses the oracle alone)."""
     cands = [ref_root, os.environ.get("PBD_REFERENCE_ROOT"), "/root/reference"]
     for c in cands:
         if c and os.path.isdir(os.path.join(c, REF_SUBDIR)):

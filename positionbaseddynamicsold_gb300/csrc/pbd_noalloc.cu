@@ -135,20 +135,64 @@ __global__ void __launch_bounds__(1024) k_residual_final(const double *parts, in
 
 std::mutex g_setup_mu;
 constexpr int kMaxDevices = 64;
-double *g_scratch_dev[kMaxDevices] = {nullptr};
 
-// device address of the scratch array on the current device, looked up once
+// The array's address belongs to the module loaded in one CUDA context.
+// After cudaDeviceReset (or with another context current) the module is
+// loaded again, possibly elsewhere, so the cached address is keyed by the
+// context's unique id and looked up again when that id changes.
+struct ScratchSlot {
+    unsigned long long ctx_id;
+    double *ptr;
+};
+ScratchSlot g_slot[kMaxDevices] = {};
+
+typedef int (*CtxGetCurrentFn)(void **);
+typedef int (*CtxGetIdFn)(void *, unsigned long long *);
+CtxGetCurrentFn g_ctx_current = nullptr;
+CtxGetIdFn g_ctx_id = nullptr;
+bool g_ctx_fns_tried = false;
+
+// id of the current context (0 when it cannot be read: then the address is
+// looked up on every call)
+unsigned long long current_context_id() {
+    if (!g_ctx_fns_tried) {
+        g_ctx_fns_tried = true;
+        cudaDriverEntryPointQueryResult q;
+        void *f = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault,
+                                             &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            g_ctx_current = (CtxGetCurrentFn)f;
+        f = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            g_ctx_id = (CtxGetIdFn)f;
+        cudaGetLastError();
+    }
+    if (!g_ctx_current || !g_ctx_id) return 0;
+    void *ctx = nullptr;
+    unsigned long long id = 0;
+    if (g_ctx_current(&ctx) != 0 || !ctx || g_ctx_id(ctx, &id) != 0) return 0;
+    return id;
+}
+
+// device address of the scratch array in the current device's context
 int scratch_address(double **out) {
     int dev = 0;
     PBD_CUDA(cudaGetDevice(&dev));
     PBD_CHECK(dev >= 0 && dev < kMaxDevices, PBD_ERR_ARG, "device %d out of range", dev);
     std::lock_guard<std::mutex> lk(g_setup_mu);
-    if (!g_scratch_dev[dev]) {
+    unsigned long long id = current_context_id();
+    if (!g_slot[dev].ptr || id == 0 || g_slot[dev].ctx_id != id) {
         void *p = nullptr;
         PBD_CUDA(cudaGetSymbolAddress(&p, g_residual_scratch));
-        g_scratch_dev[dev] = (double *)p;
+        // the lookup made the device's context current if it was not yet
+        if (id == 0) id = current_context_id();
+        g_slot[dev].ptr = (double *)p;
+        g_slot[dev].ctx_id = id;
     }
-    *out = g_scratch_dev[dev];
+    *out = g_slot[dev].ptr;
     return PBD_OK;
 }
 
@@ -166,9 +210,9 @@ extern "C" int pbd_residual_noalloc(const float *d_pos4, int n_points, const int
     PBD_CHECK(n_bend == 0 || (d_bend_idx && d_rest_angle && d_hinge_rest), PBD_ERR_ARG,
               "pbd_residual_noalloc: bending buffers missing");
     PBD_CHECK(((uintptr_t)d_pos4 & 15) == 0 && ((uintptr_t)d_dist_idx & 7) == 0 &&
-                  ((uintptr_t)d_bend_idx & 15) == 0,
+                  ((uintptr_t)d_bend_idx & 15) == 0 && ((uintptr_t)d_out & 7) == 0,
               PBD_ERR_ARG, "pbd_residual_noalloc: positions and bending ids need 16-byte, "
-                           "distance ids 8-byte alignment");
+                           "distance ids and the output 8-byte alignment");
     long long total = (long long)n_dist + n_bend;
     PBD_CHECK(total <= (long long)kMaxBlocks * kBlock, PBD_ERR_ARG,
               "pbd_residual_noalloc: %lld constraints exceed the maximum of %d",

@@ -664,13 +664,17 @@ int launch_sweep_dev(pbd_solver *s, const float *expk_dev, bool obstacles_inside
     return PBD_OK;
 }
 
+// The kernel attribute is process-wide, so it is set to the device's opt-in
+// limit (net of the static shared memory), the same value for every object:
+// a small object planned after a large one must not lower the limit that
+// the large object's launches need.
 template <int S>
 static bool resident_fits(int n, int smem_optin) {
     size_t smem = sizeof(float4) * (size_t)((n + S - 1) / S);
     if (smem < 16) smem = 16;
     if ((long long)smem > smem_optin) return false;
     if (cudaFuncSetAttribute(k_gs_resident<S>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)smem) != cudaSuccess) {
+                             smem_optin) != cudaSuccess) {
         cudaGetLastError();
         return false;
     }

@@ -1,7 +1,8 @@
 """Regenerate the golden fixtures in this directory from the reference's own
 compiled code (oracle/_ref/libpbdref.so, built from the reference sources by
-oracle/build_oracle.py).  Needs the reference checkout (default
-/root/reference, or PBD_REFERENCE_ROOT); run on the development machine:
+oracle/build_oracle.py, which finds the reference checkout: PBD_REFERENCE_ROOT
+first, then the checkout's mount point on the development machine).  Run it
+on the development machine:
 
     python tests/golden/make_golden.py        # all fixtures
     python tests/golden/make_golden.py io     # the text-cache fixtures only

@@ -104,3 +104,22 @@ def test_resident_sizes_that_do_not_hold_the_object_are_refused():
     s.set_gs_cluster(0)          # the largest size that fits
     assert s.gs_cluster() in (4, 8, 16)
     s.step(DT, 1, 5, None, True)
+
+
+def test_small_object_planned_after_a_large_one_keeps_the_large_ones_launch():
+    # the resident kernel's shared-memory limit is a process-wide attribute:
+    # planning a small object after a large one must leave the large
+    # object's launches (more shared memory per block) valid
+    big = scenes.grid_cloth(120, 120, 1.0, 1.0, jitter=1e-3, seed=11, pins=[0, 119])
+    small = scenes.grid_cloth(20, 20, 1.0, 1.0, jitter=1e-3, seed=12, pins=[0, 19])
+    ref = run(big, None, 2, 10)
+    obj_a, s_a, _ = make(big)
+    s_a.set_gs_path(GS_CLUSTER)
+    s_a.set_gs_cluster(4)
+    s_a.step(DT, 1, 10, None, False)        # plans A: 14,400 points over 4 blocks
+    obj_b, s_b, _ = make(small)
+    s_b.set_gs_path(GS_CLUSTER)
+    s_b.set_gs_cluster(4)
+    s_b.step(DT, 1, 10, None, False)        # plans B: 400 points over 4 blocks
+    s_a.step(DT, 1, 10, None, False)        # A launches again with its larger share
+    np.testing.assert_array_equal(obj_a.positions(), ref[0])
