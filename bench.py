@@ -2,28 +2,39 @@
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
                     [--workload drape256|fold1024|batch512|hanging32]
+                    [--sub-workloads fold1024,batch512]
 
-Workload (default, drape256): a 256x256 cloth (2 m x 2 m, 130,050 triangles,
-195,585 distance + 194,565 bending constraints) released flat at y = 0.5
-above a fixed icosphere (r = 0.4, 20,480 triangles); spatial hash with cell =
-2 x mean rest edge and 2^20 buckets, vertex-face CCD with thickness 1e-3
-(cloth-sphere and self collision), FP32 positions, FP64 cubic; dt = 1/600
-(10 substeps per 1/60 frame), 15 colored Gauss-Seidel iterations, CCD at
-iterations 0, 10 and 14.  One step = one substep: advect, 15 x (CCD when
-due, one sweep over all colors, one response pass), integrate.  Before the
-warm-up the cloth is simulated 120 substeps (untimed) so it touches the
-sphere and the timed substeps include contacts.  L2 is flushed (a 256 MiB
-write) before every timed substep; each substep is timed with CUDA events on
-the object's stream.
+Headline workload (drape256): a 256x256 cloth (2 m x 2 m, 130,050 triangles,
+195,585 distance + 194,565 bending constraints) over a fixed icosphere
+(r = 0.4, 20,480 triangles); spatial hash with cell = 2 x mean rest edge and
+2^20 buckets, vertex-face CCD with thickness 1e-3 (cloth-sphere and self
+collision), FP32 positions, FP64 cubic; dt = 1/600 (10 substeps per 1/60
+frame), 15 colored Gauss-Seidel iterations, CCD at iterations 0, 10 and 14.
+One step = one substep: advect, 15 x (CCD when due, one sweep over all
+colors, one response pass), integrate.  The cloth is released flat at
+y = 0.5; its free fall (a rigid translation) is fast-forwarded to 1.5 mm
+above the sphere's top, so contacts start at the first substep, and both
+bench arms start from that state and run the same W warm-up and K timed
+substeps.  L2 is flushed (a 256 MiB write) before every timed substep; each
+substep is timed with CUDA events on the object's stream.
+
+After the headline, the other workloads of --sub-workloads (default
+fold1024: the 1024x1024 self-colliding fold, and batch512: 512 cloths in
+one launch per color phase) are measured the same way, after their
+120-substep pre-roll, and reported under "workloads".
 
 Metric: cloth substeps/s.  `e2e` is the same step through the C ABI with
 the state in page-locked host memory: upload positions and velocities, step,
 read them back, every step, replaying the first min(K, 100) timed substeps
 from the state they started from.  `cpu_baseline` times the reference's CPU
 path (the oracle's restatement: sequential GS, triangle-ordered CCD with
-de-duplication by scan, sequential response) on one host thread from the
-timed state, in bounded RefSampler steps for about 10 s; `--impl reference`
-times the same steps from the workload's start state.
+de-duplication by scan, sequential response) from the timed start state:
+whole substeps with the CCD detection on every host core for drape256,
+bounded RefSampler steps on one thread for fold1024 and batch512.
+`--impl reference` times the reference CPU path on the headline's start
+state and substeps (whole substeps, every host core for the CCD detection),
+with the GPU arm's response, and the reference's own response as a second
+number.
 
 Other modes: --solve residual runs every substep to a stretch-residual
 target (--target, at most --max-sweeps sweeps in chunks of --chunk, the loop
@@ -54,10 +65,11 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "cloth substeps/s"
-# DRAM bytes per launch of the dominant kernel (the per-color GS launch,
-# 64 threads per block), measured with ncu on this workload: dram__bytes_read
-# + dram__bytes_write, mean of 58 launches of the default drape256 substep
+# DRAM bytes per launch of the dominant kernel (the per-color GS launch),
+# dram__bytes_read.sum + dram__bytes_write.sum from one ncu capture of the
+# workload on the current kernels (the profile named beside each)
 TRAFFIC_BYTES = {"drape256": 1398705.0}
+TRAFFIC_SOURCE = {"drape256": "profiles/drape256_kernels.md"}
 G = np.array([0.0, -9.8, 0.0], np.float32)
 DT = 1.0 / 600.0
 ITERS = 15
@@ -72,26 +84,38 @@ def load_peaks():
         return 6800.0, "fallback"
 
 
+RESPONSE_NOTE = ("mass-weighted: CollisionResolveNew's separation split by inverse mass with a "
+                 "scale-free degeneracy guard (the reference's |n|^2 <= 1e-6 guard rejects every "
+                 "triangle of this cloth and sphere, so its own response moves nothing here)")
+
+
 def make_workload(name, rank=0, world=1):
-    """The workload's scene and config.  batch512 with world > 1: this
-    rank's share of the instances (balanced by points, no exchange); every
-    other workload is one object per rank (replicas)."""
+    """(scene, config, collisions on, log2 hash buckets, pre-roll substeps).
+    The config describes the workload only and is the same in both bench
+    arms.  batch512 with world > 1: this rank's share of the instances
+    (balanced by points, no exchange); every other workload is one object
+    per rank (replicas)."""
     from positionbaseddynamicsold_gb300 import scenes
     from positionbaseddynamicsold_gb300.dist import shard_instances
+    l2 = "flushed (256 MiB write) before every timed GPU substep"
     if name == "drape256":
-        sc = scenes.drape_over_sphere(res=256, seed=0)
+        sc = scenes.drape_over_sphere(res=256, seed=0, start="contact")
         cfg = {"workload": "drape256: 256x256 cloth over a fixed icosphere (20,480 tris), "
                            "vertex-face CCD + self collision",
                "grid": 256, "substep_dt": DT, "gs_iterations": ITERS, "ccd_passes_per_substep": 3,
-               "hash_buckets": 2 ** 20, "thickness": 1e-3, "cell": sc["colli"]["cell"]}
-        return sc, cfg, True, 20
+               "hash_buckets": 2 ** 20, "thickness": 1e-3, "cell": sc["colli"]["cell"],
+               "start": "released flat at y = 0.5, free fall fast-forwarded to 1.5 mm above the "
+                        "sphere's top (every point moving down at 1.389 m/s)",
+               "preroll_substeps": 0, "response": RESPONSE_NOTE, "l2": l2}
+        return sc, cfg, True, 20, 0
     if name == "fold1024":
         sc = scenes.folding_cloth(res=1024, seed=0)
         cfg = {"workload": "fold1024: 1024x1024 cloth dropped onto a ground plane, self CCD",
                "grid": 1024, "substep_dt": DT, "gs_iterations": ITERS,
                "ccd_passes_per_substep": 3, "hash_buckets": 2 ** 24, "thickness": 1e-3,
-               "cell": sc["colli"]["cell"]}
-        return sc, cfg, True, 24
+               "cell": sc["colli"]["cell"], "preroll_substeps": 120, "response": RESPONSE_NOTE,
+               "l2": l2}
+        return sc, cfg, True, 24, 120
     if name == "batch512":
         subset = None
         if world > 1:
@@ -106,13 +130,14 @@ def make_workload(name, rank=0, world=1):
                "substep_dt": DT, "gs_iterations": ITERS,
                "ccd_passes_per_substep": 3, "hash_buckets": 2 ** 24, "thickness": 1e-3,
                "cell_per_instance": [float(sc["colli"]["instance_cells"].min()),
-                                     float(sc["colli"]["instance_cells"].max())]}
-        return sc, cfg, True, 24
+                                     float(sc["colli"]["instance_cells"].max())],
+               "preroll_substeps": 120, "response": RESPONSE_NOTE, "l2": l2}
+        return sc, cfg, True, 24, 120
     if name == "hanging32":
         sc = scenes.hanging_cloth(32, seed=0)
         cfg = {"workload": "hanging32: 32x32 hanging cloth, no collisions", "grid": 32,
-               "substep_dt": DT, "gs_iterations": 20}
-        return sc, cfg, False, 0
+               "substep_dt": DT, "gs_iterations": 20, "preroll_substeps": 0, "l2": l2}
+        return sc, cfg, False, 0, 0
     raise SystemExit("unknown workload " + name)
 
 
@@ -187,16 +212,23 @@ def setup(sc, colli_on, table_log2):
     return obj, solver, shs, cs
 
 
-def run_ours(args, rank, world):
+def measure(name, args, rank, world, headline=True):
+    """One workload on the GPU: pre-roll, autotune, W warm-up and K timed
+    substeps (CUDA events on the object's stream, L2 flushed before each),
+    the GS kernel's roofline, e2e through the C ABI and the CPU baseline.
+    Returns the workload's record (the full contract line for the
+    headline)."""
     import torch
     from positionbaseddynamicsold_gb300 import scenes
     from positionbaseddynamicsold_gb300.dist import max_over_ranks
 
-    torch.cuda.set_device(0 if world == 1 else int(os.environ.get("LOCAL_RANK", rank)))
-    sc, cfg, colli_on, tl = make_workload(args.workload, rank, world)
+    sc, cfg, colli_on, tl, preroll = make_workload(name, rank, world)
+    if args.preroll is not None:
+        preroll = args.preroll
+        cfg["preroll_substeps"] = preroll
     # batch512 shards its instances over the ranks (the job's substeps are
     # done when the slowest rank is); the other workloads run replicas
-    sharded = args.workload == "batch512" and world > 1
+    sharded = name == "batch512" and world > 1
     units = 1 if sharded else world
     obj, solver, shs, cs = setup(sc, colli_on, tl)
     solver.set_gs_path({"auto": 0, "per-color": 1, "cluster": 2}[args.gs_path])
@@ -214,6 +246,8 @@ def run_ours(args, rank, world):
     nb = int((sc["ctype"] == scenes.BENDING).sum())
     n_colors = obj.eval_worksets()
     iters = cfg["gs_iterations"]
+    plan = {"colors": n_colors, "points": obj.n_points, "triangles": obj.n_tris,
+            "distance_constraints": nd, "bending_constraints": nb}
 
     if args.solve == "residual":
         cfg["solve"] = {"target_stretch_residual": args.target, "max_sweeps": args.max_sweeps,
@@ -231,13 +265,13 @@ def run_ours(args, rank, world):
         def step():
             solver.step(DT, 1, iters, cs, True)
 
-    # pre-roll so the timed substeps include contacts
-    for _ in range(args.preroll):
+    for _ in range(preroll):
         step()
     if not args.no_autotune and args.gs_path == "auto":
         # the GS launch form picked on the workload's own state; the choice
-        # changes speed, never results
-        cfg["autotune"] = solver.autotune(iterations=iters, reps=3)
+        # changes speed, never results (the autotuner puts the predicted
+        # positions it sweeps back afterwards)
+        plan["autotune"] = solver.autotune(iterations=iters, reps=3)
     for _ in range(args.warmup):
         step()
     obj.sync()
@@ -255,7 +289,7 @@ def run_ours(args, rank, world):
     clocks = ClockSampler(torch.cuda.current_device())
     clocks.start()
     t_wall = time.perf_counter()
-    if args.profile_range:
+    if args.profile_range and headline:
         torch.cuda.profiler.start()
     with torch.cuda.stream(stream):
         for k in range(args.steps):
@@ -264,7 +298,7 @@ def run_ours(args, rank, world):
             step()
             ev[k][1].record(stream)
     torch.cuda.synchronize()
-    if args.profile_range:
+    if args.profile_range and headline:
         torch.cuda.profiler.stop()
     t_wall = time.perf_counter() - t_wall
     clk = clocks.stop()
@@ -272,6 +306,7 @@ def run_ours(args, rank, world):
     value = units * args.steps / (ms / 1e3)
     stats = cs.stats() if cs is not None else {}
     residual = obj.residual()
+    state_end = obj.get_state()
     if args.solve == "residual":
         sst = solver.solve_stats()
         cfg["solve"]["timed_substeps"] = sst
@@ -347,26 +382,24 @@ def run_ours(args, rank, world):
            "h2d_bytes_per_step": 2 * 12 * obj.n_points, "d2h_bytes_per_step": 2 * 12 * obj.n_points,
            "phases_us": {"upload": 1e6 * ph[0] / e2e_steps, "step": 1e6 * ph[1] / e2e_steps,
                          "download": 1e6 * ph[2] / e2e_steps}}
-
+    traffic = args.traffic if (args.traffic is not None and headline) else (
+        TRAFFIC_BYTES.get(name) if gs_form == 1 else None)
     out = {
         "metric": METRIC, "value": value, "unit": "substeps/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
         "higher_is_better": True, "scaling": "strong" if sharded else "weak", "vs_baseline": None,
         "dtype": "f32+f64(ccd cubic)",
         "data": "synthetic (seeded scene generators)",
-        "config": dict(cfg, l2="flushed (256 MiB write) before every timed substep",
-                       parallelism=("instances sharded over %d ranks" % world if sharded else
-                                    "replicas only" if world > 1 else "single GPU"),
-                       colors=n_colors, points=obj.n_points, triangles=obj.n_tris,
-                       distance_constraints=nd, bending_constraints=nb,
-                       preroll_substeps=args.preroll),
+        "config": cfg,
+        "parallelism": ("instances sharded over %d ranks" % world if sharded else
+                        "replicas only" if world > 1 else "single GPU"),
+        "plan": plan,
         "e2e": e2e,
         "gpu_launches": launches_total,
         "roofline": {"bound": "hbm", "kernel": gs_kernel, "achieved": achieved,
                      "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "peak_source": peak_kind,
-                     "traffic": args.traffic if args.traffic is not None else
-                     (TRAFFIC_BYTES.get(args.workload) if gs_form == 1 else None),
+                     "peak_source": peak_kind, "traffic": traffic,
+                     "traffic_source": TRAFFIC_SOURCE.get(name) if traffic is not None else None,
                      "launches_timed": n_launch, "avg_launch_us": gs_ms * 1e3 / n_launch,
                      "bytes_per_sweep": bytes_sweep,
                      "cluster_size": solver.gs_cluster() if gs_form == 2 else None},
@@ -377,7 +410,29 @@ def run_ours(args, rank, world):
                       "overflow": stats.get("overflow"), "relative_residual": residual},
     }
     if rank == 0 and not args.no_cpu_baseline:
-        out["cpu_baseline"] = cpu_baseline(sc, cfg, colli_on, obj, args.workload)
+        out["cpu_baseline"] = cpu_baseline(name, sc, cfg, colli_on, state0, args)
+    del state_end
+    for h in (cs, shs, solver, obj):
+        if h is not None:
+            h.close()
+    del flush
+    torch.cuda.empty_cache()
+    return out
+
+
+def run_ours(args, rank, world):
+    import torch
+    torch.cuda.set_device(0 if world == 1 else int(os.environ.get("LOCAL_RANK", rank)))
+    out = measure(args.workload, args, rank, world, headline=True)
+    subs = [w for w in args.sub_workloads.split(",") if w and w != args.workload]
+    if subs:
+        out["workloads"] = {}
+        for w in subs:
+            rec = measure(w, args, rank, world, headline=False)
+            out["workloads"][w] = {k: rec[k] for k in
+                                   ("value", "unit", "ms_per_step", "steps", "warmup", "config",
+                                    "plan", "e2e", "gpu_launches", "roofline", "clocks",
+                                    "last_step", "cpu_baseline") if k in rec}
     if rank == 0 and not args.no_learned_eval:
         out["learned_warm_start"] = learned_eval()
     return out
@@ -569,11 +624,50 @@ class BatchRefSampler:
                    max(s.iters * s.m for s in self.samplers)))
 
 
-def cpu_baseline(sc, cfg, colli_on, obj, workload, budget_s=10.0):
-    """The reference CPU path (oracle restatement) on one thread: RefSampler
-    steps from the timed state for about budget_s seconds (batch512: the
-    instances' own simulations from their start states)."""
-    if workload == "batch512":
+class RefSubsteps:
+    """The reference's CPU path in whole substeps (advectCPU,
+    projectConstraintWithColliCPU, integrationCPU: P/PBD_cuda.cu:997-1210,
+    the oracle's restatement): per iteration [UpdateSH + CCD_SH_Extended at
+    iterations 0, 10 and 14], one sequential GS pass over every prim in id
+    order, one CollisionResolveNew pass over the stored contacts in order.
+    CCD_SH_Extended's triangle loop runs on `threads` host threads over
+    consecutive triangle slices whose hits are stored in loop order with the
+    reference's duplicate scan, so the contact list, and with it the whole
+    step, is the one-thread result; everything else is sequential as in the
+    reference.  mass_weighted = 1 gives the response the GPU arm runs
+    (inverse-mass split, scale-free guard); 0 the reference's own."""
+
+    def __init__(self, sc, cfg, pos, vel, threads, mass_weighted=1):
+        from oracle.oracle import Oracle
+        self.orc = Oracle()
+        self.threads = threads
+        self.sc = sc
+        self.iters = cfg["gs_iterations"]
+        self.colli = None
+        if "colli" in sc:
+            self.colli = dict(cpu_colli(sc), mass_weighted=int(mass_weighted))
+        self.state = {"pos": np.ascontiguousarray(pos, np.float32).copy(),
+                      "vel": np.ascontiguousarray(vel, np.float32).copy()}
+        self.contacts = 0
+
+    def step(self):
+        self.orc.set_threads(self.threads)
+        self.contacts = self.orc.substep_cpu_ref(self.sc, self.state, self.iters, DT, G,
+                                                 colli=self.colli)
+
+    def sample(self, n):
+        return ("%d whole substeps (advect, %d iterations of sequential GS + CCD at 0/10/14 + "
+                "sequential response, integrate); CCD detection on %d host threads, "
+                "everything else on one" % (n, self.iters, self.threads))
+
+
+def cpu_baseline(name, sc, cfg, colli_on, state0, args, budget_s=10.0):
+    """The reference CPU path (oracle restatement) from the timed start
+    state.  drape256 / hanging32: whole substeps on every host core for
+    about budget_s seconds (RefSubsteps).  fold1024 (a whole substep takes
+    about half a minute there) and batch512 (512 separate simulations):
+    RefSampler steps on one thread."""
+    if name == "batch512":
         rs = BatchRefSampler(cfg)
         for _ in range(len(rs.samplers)):
             rs.step()  # warm-up
@@ -585,56 +679,100 @@ def cpu_baseline(sc, cfg, colli_on, obj, workload, budget_s=10.0):
         return {"value": rs.value(), "unit": "substeps/s", "cores": 1, "kind": "port",
                 "sample": "%d steps in %.1f s; %s" % (rs.k, dt, rs.sample()),
                 "host_cores_available": os.cpu_count()}
-    rs = RefSampler(sc, cfg, colli_on, obj.positions(), obj.velocities())
-    rs.step()  # warm-up
-    steps, t0 = 0, time.perf_counter()
-    while steps < 3 or time.perf_counter() - t0 < budget_s:
+    if name == "fold1024":
+        rs = RefSampler(sc, cfg, colli_on, state0[0], state0[1])
+        rs.step()  # warm-up
+        steps, t0 = 0, time.perf_counter()
+        while steps < 3 or time.perf_counter() - t0 < budget_s:
+            rs.step()
+            steps += 1
+        dt = time.perf_counter() - t0
+        return {"value": steps * rs.phi / dt, "unit": "substeps/s", "cores": 1, "kind": "port",
+                "sample": "%d steps in %.1f s; %s" % (steps, dt, rs.sample()),
+                "host_cores_available": os.cpu_count()}
+    threads = os.cpu_count() or 1
+    rs = RefSubsteps(sc, cfg, state0[0], state0[1], threads)
+    n, t0 = 0, time.perf_counter()
+    while n < 2 or time.perf_counter() - t0 < budget_s:
         rs.step()
-        steps += 1
+        n += 1
     dt = time.perf_counter() - t0
-    return {"value": steps * rs.phi / dt, "unit": "substeps/s", "cores": 1, "kind": "port",
-            "sample": "%d steps in %.1f s; %s" % (steps, dt, rs.sample()),
+    return {"value": n / dt, "unit": "substeps/s", "cores": threads, "kind": "port",
+            "sample": "from the timed start state: " + rs.sample(n),
             "host_cores_available": os.cpu_count()}
 
 
 def run_reference(args):
     """The reference's CPU implementation of the path (the oracle's
     restatement of it: the reference sources are not present on the GPU
-    host), in RefSampler steps from the workload's start state."""
-    sc, cfg, colli_on, tl = make_workload(args.workload)
-    if args.workload == "batch512":
-        rs = BatchRefSampler(cfg)
+    host) on the GPU arm's workload, config and start state.  drape256 /
+    hanging32: the same W warm-up and K timed whole substeps as the GPU arm
+    (RefSubsteps, every host core), with the GPU arm's response; then
+    min(K, 5) substeps from the same state with the reference's own response
+    as a second number.  fold1024 / batch512: bounded RefSampler steps from
+    the workload's start state."""
+    sc, cfg, colli_on, tl, preroll = make_workload(args.workload)
+    if args.workload in ("drape256", "hanging32"):
+        threads = os.cpu_count() or 1
+        rs = RefSubsteps(sc, cfg, sc["pos"], sc["vel"], threads)
         for _ in range(args.warmup):
             rs.step()
-        rs.reset()
+        start = (rs.state["pos"].copy(), rs.state["vel"].copy())
         t0 = time.perf_counter()
         for _ in range(args.steps):
             rs.step()
         dt = time.perf_counter() - t0
-        value = rs.value()
+        value = args.steps / dt
+        sample = ("the GPU arm's start state and substeps: %d warm-up + %s"
+                  % (args.warmup, rs.sample(args.steps)))
+        cores = threads
+        extra = {"last_step": {"contacts": int(rs.contacts)}}
+        if colli_on:
+            n2 = max(1, min(args.steps, 5))
+            r2 = RefSubsteps(sc, cfg, start[0], start[1], threads, mass_weighted=0)
+            t1 = time.perf_counter()
+            for _ in range(n2):
+                r2.step()
+            d2 = time.perf_counter() - t1
+            extra["reference_response"] = {
+                "value": n2 / d2, "unit": "substeps/s", "substeps": n2,
+                "note": "the same start state with the reference's own response "
+                        "(|n|^2 <= 1e-6 guard: no corrections on this cloth)",
+                "last_step_contacts": int(r2.contacts)}
     else:
-        pos = sc["pos"].copy()
-        # start from a contact state like the timed arm: drop the cloth onto the sphere
-        if args.workload == "drape256":
-            pos[:sc["n_cloth_points"], 1] -= np.float32(0.099)
-        rs = RefSampler(sc, cfg, colli_on, pos, sc["vel"])
-        for _ in range(args.warmup):
-            rs.step()
-        t0 = time.perf_counter()
-        for _ in range(args.steps):
-            rs.step()
-        dt = time.perf_counter() - t0
-        value = args.steps * rs.phi / dt
-    sample = rs.sample()
-    return {"impl": "reference", "metric": METRIC, "value": value, "unit": "substeps/s",
-            "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": dt * 1e3 / args.steps, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32+f64(ccd cubic)", "data": "synthetic",
-            "config": cfg,
-            "cpu_baseline": {"value": value, "unit": "substeps/s", "cores": 1, "kind": "port",
-                             "sample": sample, "host_cores_available": os.cpu_count()},
-            "e2e": {"value": value, "unit": "substeps/s", "h2d_bytes_per_step": 0,
-                    "d2h_bytes_per_step": 0}}
+        extra = {}
+        cores = 1
+        if args.workload == "batch512":
+            rs = BatchRefSampler(cfg)
+            for _ in range(args.warmup):
+                rs.step()
+            rs.reset()
+            t0 = time.perf_counter()
+            for _ in range(args.steps):
+                rs.step()
+            dt = time.perf_counter() - t0
+            value = rs.value()
+        else:
+            rs = RefSampler(sc, cfg, colli_on, sc["pos"], sc["vel"])
+            for _ in range(args.warmup):
+                rs.step()
+            t0 = time.perf_counter()
+            for _ in range(args.steps):
+                rs.step()
+            dt = time.perf_counter() - t0
+            value = args.steps * rs.phi / dt
+        sample = rs.sample()
+    out = {"impl": "reference", "metric": METRIC, "value": value, "unit": "substeps/s",
+           "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+           "ms_per_step": dt * 1e3 / args.steps, "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f32+f64(ccd cubic)",
+           "data": "synthetic (seeded scene generators)", "config": cfg,
+           "cpu_baseline": {"value": value, "unit": "substeps/s", "cores": cores, "kind": "port",
+                            "sample": sample, "host_cores_available": os.cpu_count()},
+           "e2e": {"value": value, "unit": "substeps/s", "h2d_bytes_per_step": 0,
+                   "d2h_bytes_per_step": 0}}
+    out.update(extra)
+    return out
 
 
 def main():
@@ -645,7 +783,11 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="drape256", choices=["drape256", "fold1024", "batch512",
                                                           "hanging32"])
-    ap.add_argument("--preroll", type=int, default=120)
+    ap.add_argument("--preroll", type=int, default=None,
+                    help="untimed substeps before the warm-up (default: the workload's own)")
+    ap.add_argument("--sub-workloads", default="fold1024,batch512",
+                    help="comma-separated workloads measured after the headline one and "
+                         "reported under 'workloads' (empty: none)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--gs-path", default="auto", choices=["auto", "per-color", "cluster"])
     ap.add_argument("--gs-cluster", type=int, default=0,

@@ -83,14 +83,22 @@ class Oracle:
         L.orc_narrow_vf_ccd_test.restype = C.c_int
         L.orc_find_neighbors_all.restype = C.c_int64
         L.orc_ccd_sh_extended_ref.restype = C.c_int64
+        L.orc_get_threads.restype = C.c_int
         L.orc_ccd_vf_pairs.restype = C.c_int64
         L.orc_vf_resolve_test.restype = C.c_int
         L.orc_vf_resolve_deltas.restype = C.c_int
         L.orc_substep_gpu.restype = C.c_int64
+        L.orc_substep_gpu_obst.restype = C.c_int64
         L.orc_substep_cpu_ref.restype = C.c_int64
         L.orc_dihedral_angle.restype = C.c_double
         L.orc_bending_project_f64.restype = C.c_int
         L.orc_bending_project_f32.restype = C.c_int
+
+    def set_threads(self, n=None):
+        """host threads for the oracle's independent loops (process-wide;
+        None: every core); results do not depend on the count"""
+        self.lib.orc_set_threads(int(n if n is not None else (os.cpu_count() or 1)))
+        return self.lib.orc_get_threads()
 
     # -- constraints -----------------------------------------------------
     @staticmethod
@@ -140,8 +148,9 @@ class Oracle:
         self.lib.orc_set_stiffness_schedule(int(mode))
 
     def substep_gpu(self, scene, state, sorted_prim_id, worksets, iterations, dt, damping,
-                    gravity, bending_fp64=False, colli=None):
-        """state: dict pos, vel (float32 (N,3)); modified in place."""
+                    gravity, bending_fp64=False, colli=None, sphere=None, ground=None):
+        """state: dict pos, vel (float32 (N,3)); modified in place.  sphere:
+        (cx, cy, cz, r) pushed out after every sweep; ground: plane height."""
         c = self.constraints(scene)
         n = state["pos"].shape[0]
         prdp = state["pos"].copy()
@@ -149,11 +158,13 @@ class Oracle:
         sid = np.ascontiguousarray(sorted_prim_id, dtype=np.int32)
         ws = np.ascontiguousarray(worksets, dtype=np.int32)
         cp = self._colli(colli)
-        nct = self.lib.orc_substep_gpu(
+        sp4 = None if sphere is None else np.ascontiguousarray(sphere, dtype=np.float32)
+        nct = self.lib.orc_substep_gpu_obst(
             n, C.byref(c), _ptr(sid), len(ws), _ptr(ws), iterations, C.c_float(dt),
             C.c_float(damping), _ptr(g), _ptr(scene["mass"]), _ptr(state["pos"]),
             _ptr(state["vel"]), _ptr(prdp), int(bending_fp64),
-            C.byref(cp) if cp is not None else None)
+            C.byref(cp) if cp is not None else None, _ptr(sp4), int(ground is not None),
+            C.c_float(0.0 if ground is None else ground))
         state["prdp"] = prdp
         return nct
 

@@ -17,6 +17,25 @@
 #include <math.h>
 #include <stdlib.h>
 #include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+/* Host threads for the loops whose iterations are independent (CCD
+ * detection per triangle or point, projections within one color, the
+ * response's per-contact corrections).  Every merge that the reference does
+ * in order (contact storage with its duplicate scan, the sequential GS and
+ * response) stays sequential, so results do not depend on the count. */
+static int g_threads = 1;
+void orc_set_threads(int n) { g_threads = n > 0 ? n : 1; }
+int orc_get_threads(void)
+{
+#ifdef _OPENMP
+    return g_threads;
+#else
+    return 1;
+#endif
+}
 
 /* ------------------------------------------------------------------ */
 /* float3 arithmetic in the operation order of the reference's host code */
@@ -489,10 +508,17 @@ void orc_project_colored(const orc_constraints *c, const int *sorted_prim_id,
                          int iter_end, const float *mass, float *prdp,
                          int bending_fp64)
 {
+    /* constraints of one color share no point: any order gives the same
+     * positions */
     for (int it = iter_begin; it < iter_end; ++it)
-        for (int w = 0; w < n_worksets; ++w)
-            for (int i = worksets[2 * w]; i < worksets[2 * w] + worksets[2 * w + 1]; ++i)
+        for (int w = 0; w < n_worksets; ++w) {
+            const int a = worksets[2 * w], b = worksets[2 * w] + worksets[2 * w + 1];
+#ifdef _OPENMP
+#pragma omp parallel for num_threads(g_threads) schedule(static) if (g_threads > 1 && b - a > 4096)
+#endif
+            for (int i = a; i < b; ++i)
                 orc_project_one(c, sorted_prim_id[i], it, mass, prdp, bending_fp64);
+        }
 }
 
 void orc_colli_sphere(int n, float *prdp, const float *center, float radius)
@@ -1076,6 +1102,105 @@ int64_t orc_ccd_sh_extended_ref_range_tab(const orc_grid *g, const orc_sh_table 
     return h;
 }
 
+/* Hits of one slice of triangles in the loop order of
+ * orc_ccd_sh_extended_ref_range_tab, before the duplicate scan. */
+typedef struct {
+    int64_t n, cap;
+    orc_contact *c;
+} raw_hits;
+
+static void detect_slice(const orc_grid *g, const orc_sh_table *t, const int *tri_idx,
+                         const float *pos, const float *prdp, float thickness, int tri_begin,
+                         int tri_end, raw_hits *out)
+{
+    int nbcap = 1024;
+    int *nb = (int *)malloc(sizeof(int) * (size_t)nbcap);
+    out->n = 0;
+    out->cap = 256;
+    out->c = (orc_contact *)malloc(sizeof(orc_contact) * (size_t)out->cap);
+    for (int tri = tri_begin; tri < tri_end; ++tri) {
+        int nn = neighbors_of(g, &t->tb, t->cells, tri, &nb, &nbcap);
+        for (int j = 0; j < 3; ++j) {
+            int ids[4];
+            ids[0] = tri_idx[3 * tri + j];
+            for (int q = 0; q < nn; ++q) {
+                int nt = nb[q];
+                ids[1] = tri_idx[3 * nt];
+                ids[2] = tri_idx[3 * nt + 1];
+                ids[3] = tri_idx[3 * nt + 2];
+                float xs[12], ps[12];
+                gather4(ids, pos, xs);
+                gather4(ids, prdp, ps);
+                orc_contact ct;
+                if (!orc_extended_vf_test(xs, ps, thickness, ids[0], ids[1], ids[2], ids[3], &ct))
+                    continue;
+                ct.v = ids[0]; ct.f0 = ids[1]; ct.f1 = ids[2]; ct.f2 = ids[3];
+                ct.face = nt;
+                if (out->n == out->cap) {
+                    out->cap *= 2;
+                    out->c = (orc_contact *)realloc(out->c, sizeof(orc_contact) * (size_t)out->cap);
+                }
+                out->c[out->n++] = ct;
+            }
+        }
+    }
+    free(nb);
+}
+
+int64_t orc_ccd_sh_extended_ref_range_tab_mt(const orc_grid *g, const orc_sh_table *t,
+                                             int n_tris, const int *tri_idx, const float *pos,
+                                             const float *prdp, float thickness, int tri_begin,
+                                             int tri_end, orc_contact *out, int64_t cap)
+{
+    /* The triangle loop of CCD_SH_Extended (P/CCD.cpp:1541-1586) split into
+     * consecutive slices detected on g_threads threads; the slices' hits
+     * are then stored in loop order with the reference's IsDuplicated
+     * linear scan (P/CCD.cpp:132-147), so the contact list equals the
+     * sequential one. */
+    if (tri_begin < 0) tri_begin = 0;
+    if (tri_end > n_tris) tri_end = n_tris;
+    int n = tri_end - tri_begin;
+    if (n <= 0) return 0;
+    int nsl = orc_get_threads() * 16;
+    if (nsl > n) nsl = n;
+    raw_hits *rh = (raw_hits *)calloc((size_t)nsl, sizeof(raw_hits));
+#ifdef _OPENMP
+#pragma omp parallel for num_threads(g_threads) schedule(dynamic, 1)
+#endif
+    for (int k = 0; k < nsl; ++k) {
+        int a = tri_begin + (int)((int64_t)n * k / nsl);
+        int b = tri_begin + (int)((int64_t)n * (k + 1) / nsl);
+        detect_slice(g, t, tri_idx, pos, prdp, thickness, a, b, rh + k);
+    }
+    int64_t h = 0, hcap = 1024;
+    int *keys = (int *)malloc(sizeof(int) * 4 * (size_t)hcap);
+    for (int k = 0; k < nsl; ++k) {
+        for (int64_t i = 0; i < rh[k].n; ++i) {
+            const orc_contact *ct = rh[k].c + i;
+            int ids[4] = {ct->v, ct->f0, ct->f1, ct->f2};
+            int dup = 0;
+            for (int64_t q = 0; q < h; ++q)
+                if (keys[4 * q] == ids[0] && keys[4 * q + 1] == ids[1] &&
+                    keys[4 * q + 2] == ids[2] && keys[4 * q + 3] == ids[3]) {
+                    dup = 1;
+                    break;
+                }
+            if (dup) continue;
+            if (h == hcap) {
+                hcap *= 2;
+                keys = (int *)realloc(keys, sizeof(int) * 4 * (size_t)hcap);
+            }
+            memcpy(keys + 4 * h, ids, sizeof(ids));
+            if (out && h < cap) out[h] = *ct;
+            h++;
+        }
+        free(rh[k].c);
+    }
+    free(rh);
+    free(keys);
+    return h;
+}
+
 int64_t orc_ccd_sh_extended_ref_range(const orc_grid *g, int n_tris, const int *tri_idx,
                                       const float *pos, const float *prdp, float thickness,
                                       int tri_begin, int tri_end, orc_contact *out, int64_t cap)
@@ -1083,8 +1208,11 @@ int64_t orc_ccd_sh_extended_ref_range(const orc_grid *g, int n_tris, const int *
     /* UpdateSH(prdP) (binning of every triangle, P/CCD.cpp:1530-1540), then
      * the range */
     orc_sh_table *t = orc_sh_build(g, n_tris, tri_idx, prdp);
-    int64_t h = orc_ccd_sh_extended_ref_range_tab(g, t, n_tris, tri_idx, pos, prdp, thickness,
-                                                  tri_begin, tri_end, out, cap);
+    int64_t h = orc_get_threads() > 1
+                    ? orc_ccd_sh_extended_ref_range_tab_mt(g, t, n_tris, tri_idx, pos, prdp,
+                                                           thickness, tri_begin, tri_end, out, cap)
+                    : orc_ccd_sh_extended_ref_range_tab(g, t, n_tris, tri_idx, pos, prdp,
+                                                        thickness, tri_begin, tri_end, out, cap);
     orc_sh_free(t);
     return h;
 }
@@ -1093,6 +1221,68 @@ typedef struct { int face; orc_contact c; } hit_rec;
 static int cmp_hit(const void *a, const void *b)
 {
     return ((const hit_rec *)a)->face - ((const hit_rec *)b)->face;
+}
+
+/* The hits of point v in face order (orc_ccd_vf_pairs' loop body); hits
+ * and cc are the caller's scratch. */
+static int vf_pairs_point(const orc_grid *g, const cell_table *t, const int *cells,
+                          const int *pc, const int *pt, int v, const int *tri_idx,
+                          const int *tri_inst, const int *point_inst, const float *pos,
+                          const float *prdp, float thickness, hit_rec **hits, int *hcap,
+                          int *cc)
+{
+    /* centroid cells of the incident triangles (those in the grid) */
+    int nc = 0;
+    for (int q = pc[v]; q < pc[v + 1] && nc < 64; ++q) {
+        const int *c = cells + 3 * pt[q];
+        if (g->bounded && outside(g, c)) continue;
+        cc[3 * nc] = c[0]; cc[3 * nc + 1] = c[1]; cc[3 * nc + 2] = c[2];
+        nc++;
+    }
+    if (nc == 0) return 0;
+    int lo[3], hi[3];
+    for (int k = 0; k < 3; ++k) { lo[k] = cc[k]; hi[k] = cc[k]; }
+    for (int i = 1; i < nc; ++i)
+        for (int k = 0; k < 3; ++k) {
+            if (cc[3 * i + k] < lo[k]) lo[k] = cc[3 * i + k];
+            if (cc[3 * i + k] > hi[k]) hi[k] = cc[3 * i + k];
+        }
+    int nh = 0;
+    for (int z = lo[2] - 1; z <= hi[2] + 1; ++z)
+        for (int y = lo[1] - 1; y <= hi[1] + 1; ++y)
+            for (int x = lo[0] - 1; x <= hi[0] + 1; ++x) {
+                int cell[3] = {x, y, z};
+                int near = 0;
+                for (int i = 0; i < nc && !near; ++i)
+                    near = abs(cc[3 * i] - x) <= 1 && abs(cc[3 * i + 1] - y) <= 1 &&
+                           abs(cc[3 * i + 2] - z) <= 1;
+                if (!near) continue;
+                if (g->bounded && outside(g, cell)) continue;
+                uint64_t key = g->bounded ? (uint64_t)orc_cell_hash(g, cell) : cell_key(cell);
+                for (int e = table_lower(t, key); e < t->n && t->e[e].key == key; ++e) {
+                    int f = t->e[e].id;
+                    if (tri_inst && point_inst && tri_inst[f] != point_inst[v]) continue;
+                    int ids[4] = {v, tri_idx[3 * f], tri_idx[3 * f + 1], tri_idx[3 * f + 2]};
+                    float xs[12], ps[12];
+                    gather4(ids, pos, xs);
+                    gather4(ids, prdp, ps);
+                    orc_contact ct;
+                    if (!orc_extended_vf_test(xs, ps, thickness, ids[0], ids[1], ids[2], ids[3],
+                                              &ct))
+                        continue;
+                    ct.v = ids[0]; ct.f0 = ids[1]; ct.f1 = ids[2]; ct.f2 = ids[3];
+                    ct.face = f;
+                    if (nh == *hcap) {
+                        *hcap *= 2;
+                        *hits = (hit_rec *)realloc(*hits, sizeof(hit_rec) * (size_t)*hcap);
+                    }
+                    (*hits)[nh].face = f;
+                    (*hits)[nh].c = ct;
+                    nh++;
+                }
+            }
+    qsort(*hits, (size_t)nh, sizeof(hit_rec), cmp_hit);
+    return nh;
 }
 
 int64_t orc_ccd_vf_pairs(const orc_grid *g, int n_points, int n_tris,
@@ -1111,69 +1301,50 @@ int64_t orc_ccd_vf_pairs(const orc_grid *g, int n_points, int n_tris,
     int *fill = (int *)malloc(sizeof(int) * ((size_t)n_points + 1));
     memcpy(fill, pc, sizeof(int) * ((size_t)n_points + 1));
     for (int i = 0; i < 3 * n_tris; ++i) pt[fill[tri_idx[i]]++] = i / 3;
-    int64_t h = 0;
-    int hcap = 256;
-    hit_rec *hits = (hit_rec *)malloc(sizeof(hit_rec) * (size_t)hcap);
-    int *cc = (int *)malloc(sizeof(int) * 3 * 64);
-    for (int v = 0; v < n_points; ++v) {
-        /* centroid cells of the incident triangles (those in the grid) */
-        int nc = 0;
-        for (int q = pc[v]; q < pc[v + 1] && nc < 64; ++q) {
-            const int *c = cells + 3 * pt[q];
-            if (g->bounded && outside(g, c)) continue;
-            cc[3 * nc] = c[0]; cc[3 * nc + 1] = c[1]; cc[3 * nc + 2] = c[2];
-            nc++;
-        }
-        if (nc == 0) continue;
-        int lo[3], hi[3];
-        for (int k = 0; k < 3; ++k) { lo[k] = cc[k]; hi[k] = cc[k]; }
-        for (int i = 1; i < nc; ++i)
-            for (int k = 0; k < 3; ++k) {
-                if (cc[3 * i + k] < lo[k]) lo[k] = cc[3 * i + k];
-                if (cc[3 * i + k] > hi[k]) hi[k] = cc[3 * i + k];
-            }
-        int nh = 0;
-        for (int z = lo[2] - 1; z <= hi[2] + 1; ++z)
-            for (int y = lo[1] - 1; y <= hi[1] + 1; ++y)
-                for (int x = lo[0] - 1; x <= hi[0] + 1; ++x) {
-                    int cell[3] = {x, y, z};
-                    int near = 0;
-                    for (int i = 0; i < nc && !near; ++i)
-                        near = abs(cc[3 * i] - x) <= 1 && abs(cc[3 * i + 1] - y) <= 1 &&
-                               abs(cc[3 * i + 2] - z) <= 1;
-                    if (!near) continue;
-                    if (g->bounded && outside(g, cell)) continue;
-                    uint64_t key = g->bounded ? (uint64_t)orc_cell_hash(g, cell) : cell_key(cell);
-                    for (int e = table_lower(&t, key); e < t.n && t.e[e].key == key; ++e) {
-                        int f = t.e[e].id;
-                        if (tri_inst && point_inst && tri_inst[f] != point_inst[v]) continue;
-                        int ids[4] = {v, tri_idx[3 * f], tri_idx[3 * f + 1], tri_idx[3 * f + 2]};
-                        float xs[12], ps[12];
-                        gather4(ids, pos, xs);
-                        gather4(ids, prdp, ps);
-                        orc_contact ct;
-                        if (!orc_extended_vf_test(xs, ps, thickness, ids[0], ids[1], ids[2],
-                                                  ids[3], &ct))
-                            continue;
-                        ct.v = ids[0]; ct.f0 = ids[1]; ct.f1 = ids[2]; ct.f2 = ids[3];
-                        ct.face = f;
-                        if (nh == hcap) {
-                            hcap *= 2;
-                            hits = (hit_rec *)realloc(hits, sizeof(hit_rec) * (size_t)hcap);
-                        }
-                        hits[nh].face = f;
-                        hits[nh].c = ct;
-                        nh++;
-                    }
+    /* points in blocks, each block's hits kept in point order; blocks are
+     * independent and joined in order */
+    const int B = 256;
+    int nblk = (n_points + B - 1) / B;
+    raw_hits *rh = (raw_hits *)calloc((size_t)(nblk > 0 ? nblk : 1), sizeof(raw_hits));
+#ifdef _OPENMP
+#pragma omp parallel num_threads(g_threads) if (g_threads > 1)
+#endif
+    {
+        int hcap = 256;
+        hit_rec *hits = (hit_rec *)malloc(sizeof(hit_rec) * (size_t)hcap);
+        int *cc = (int *)malloc(sizeof(int) * 3 * 64);
+#ifdef _OPENMP
+#pragma omp for schedule(dynamic, 4)
+#endif
+        for (int k = 0; k < nblk; ++k) {
+            raw_hits *o = rh + k;
+            o->n = 0;
+            o->cap = 0;
+            o->c = NULL;
+            int v1 = (k + 1) * B < n_points ? (k + 1) * B : n_points;
+            for (int v = k * B; v < v1; ++v) {
+                int nh = vf_pairs_point(g, &t, cells, pc, pt, v, tri_idx, tri_inst, point_inst,
+                                        pos, prdp, thickness, &hits, &hcap, cc);
+                if (!nh) continue;
+                if (o->n + nh > o->cap) {
+                    o->cap = 2 * (o->n + nh);
+                    o->c = (orc_contact *)realloc(o->c, sizeof(orc_contact) * (size_t)o->cap);
                 }
-        qsort(hits, (size_t)nh, sizeof(hit_rec), cmp_hit);
-        for (int i = 0; i < nh; ++i) {
-            if (out && h < cap) out[h] = hits[i].c;
+                for (int i = 0; i < nh; ++i) o->c[o->n++] = hits[i].c;
+            }
+        }
+        free(cc);
+        free(hits);
+    }
+    int64_t h = 0;
+    for (int k = 0; k < nblk; ++k) {
+        for (int64_t i = 0; i < rh[k].n; ++i) {
+            if (out && h < cap) out[h] = rh[k].c[i];
             h++;
         }
+        free(rh[k].c);
     }
-    free(cc);
-    free(hits);
+    free(rh);
     free(pc);
     free(pt);
     free(fill);
@@ -1298,6 +1469,28 @@ int orc_vf_resolve_deltas(const float *x, const float *p, const float *wm,
     return 1;
 }
 
+void orc_collision_resolve_seq(int n_contacts, const orc_contact *cts, const float *pos,
+                               float *prdp, const float *mass, int iterations,
+                               float thickness, int mass_weighted)
+{
+    /* CollisionResolveNew's sequential pass (P/CCD.cpp:1874-1994): contacts
+     * in stored order, each applied in place before the next is tested;
+     * the correction of orc_vf_resolve_deltas (mass_weighted 0: the
+     * reference's split and guard, as orc_collision_resolve_ref; 1: the
+     * inverse-mass split with the scale-free guard) */
+    for (int it = 0; it < iterations; ++it)
+        for (int c = 0; c < n_contacts; ++c) {
+            int ids[4] = {cts[c].v, cts[c].f0, cts[c].f1, cts[c].f2};
+            float xs[12], ps[12], wm[4], dl[12];
+            gather4(ids, pos, xs);
+            gather4(ids, prdp, ps);
+            for (int j = 0; j < 4; ++j) wm[j] = mass ? mass[ids[j]] : 1.0f;
+            if (!orc_vf_resolve_deltas(xs, ps, wm, thickness, mass_weighted, dl)) continue;
+            for (int j = 0; j < 4; ++j)
+                for (int k = 0; k < 3; ++k) prdp[3 * ids[j] + k] = ps[3 * j + k] + dl[3 * j + k];
+        }
+}
+
 void orc_collision_resolve_jacobi(int n_points, int n_contacts,
                                   const orc_contact *cts, const float *pos,
                                   float *prdp, const float *mass, int iterations,
@@ -1312,6 +1505,9 @@ void orc_collision_resolve_jacobi(int n_points, int n_contacts,
     float *dl = (float *)malloc(sizeof(float) * 12 * (size_t)(n_contacts > 0 ? n_contacts : 1));
     int *act = (int *)malloc(sizeof(int) * (size_t)(n_contacts > 0 ? n_contacts : 1));
     for (int it = 0; it < iterations; ++it) {
+#ifdef _OPENMP
+#pragma omp parallel for num_threads(g_threads) schedule(static) if (g_threads > 1 && n_contacts > 1024)
+#endif
         for (int c = 0; c < n_contacts; ++c) {
             int ids[4] = {cts[c].v, cts[c].f0, cts[c].f1, cts[c].f2};
             float xs[12], ps[12], wm[4];
@@ -1565,13 +1761,25 @@ void orc_collision_resolve_jacobi_ee(int n_points, int n_vf, const orc_contact *
 /* substeps                                                             */
 /* ------------------------------------------------------------------ */
 
-int64_t orc_substep_gpu(int n_points, const orc_constraints *c,
-                        const int *sorted_prim_id, int n_worksets,
-                        const int *worksets, int iterations, float dt,
-                        float damping, const float *gravity, const float *mass,
-                        float *pos, float *vel, float *prdp, int bending_fp64,
-                        const orc_colli_params *colli)
+/* The analytic ground of the GPU path: a point closer than 1 mm above the
+ * plane y = h (or below it) is put on it. */
+void orc_ground(int n, float *prdp, float h)
 {
+    for (int i = 0; i < n; ++i)
+        if (prdp[3 * i + 1] - h < 0.001f) prdp[3 * i + 1] = h;
+}
+
+int64_t orc_substep_gpu_obst(int n_points, const orc_constraints *c,
+                             const int *sorted_prim_id, int n_worksets,
+                             const int *worksets, int iterations, float dt,
+                             float damping, const float *gravity, const float *mass,
+                             float *pos, float *vel, float *prdp, int bending_fp64,
+                             const orc_colli_params *colli, const float *sphere4,
+                             int ground_on, float ground_h)
+{
+    /* the GPU step's order: per iteration [detection when due], one colored
+     * sweep, [one response pass], then the analytic obstacles (the sphere
+     * push of ColliWithShpGrd, P/PBD_cuda.cu:1519-1573, and the ground) */
     float damp_pow = powf(damping, dt);
     orc_advect_gpu(n_points, dt, damp_pow, gravity, mass, vel, prdp, pos);
     int64_t nct = 0;
@@ -1591,10 +1799,24 @@ int64_t orc_substep_gpu(int n_points, const orc_constraints *c,
             orc_collision_resolve_jacobi(n_points, (int)nct, cts, pos, prdp, mass,
                                          colli->resolve_passes, colli->thickness,
                                          colli->mass_weighted);
+        if (sphere4) orc_colli_sphere(n_points, prdp, sphere4, sphere4[3]);
+        if (ground_on) orc_ground(n_points, prdp, ground_h);
     }
     orc_integrate(n_points, dt, vel, prdp, pos);
     free(cts);
     return nct;
+}
+
+int64_t orc_substep_gpu(int n_points, const orc_constraints *c,
+                        const int *sorted_prim_id, int n_worksets,
+                        const int *worksets, int iterations, float dt,
+                        float damping, const float *gravity, const float *mass,
+                        float *pos, float *vel, float *prdp, int bending_fp64,
+                        const orc_colli_params *colli)
+{
+    return orc_substep_gpu_obst(n_points, c, sorted_prim_id, n_worksets, worksets, iterations,
+                                dt, damping, gravity, mass, pos, vel, prdp, bending_fp64, colli,
+                                NULL, 0, 0.0f);
 }
 
 int64_t orc_substep_cpu_ref(int n_points, const orc_constraints *c, int iterations,
@@ -1616,7 +1838,10 @@ int64_t orc_substep_cpu_ref(int n_points, const orc_constraints *c, int iteratio
                 if (nct > colli->contact_cap) nct = colli->contact_cap;
             }
             orc_project_cpu(c, 1, mass, prdp, n_points, NULL, 0.0f);
-            orc_collision_resolve_ref((int)nct, cts, pos, prdp, 1, colli->thickness);
+            if (colli->mass_weighted)
+                orc_collision_resolve_seq((int)nct, cts, pos, prdp, mass, 1, colli->thickness, 1);
+            else
+                orc_collision_resolve_ref((int)nct, cts, pos, prdp, 1, colli->thickness);
             if (sphere_center) orc_colli_sphere(n_points, prdp, sphere_center, sphere_radius);
         }
         free(cts);

@@ -32,6 +32,11 @@ extern "C" {
 /* Distance() spelled as powf like the reference (1) or as sqrtf of the
  * squared sum like the CUDA kernels (0, default). */
 void orc_set_pow_distance(int on);
+/* host threads for the loops whose iterations are independent (default 1;
+ * results do not depend on the count); orc_get_threads returns 1 when the
+ * library was built without OpenMP */
+void orc_set_threads(int n);
+int orc_get_threads(void);
 
 /* constraint type bits, P/PBD_Basic.cuh:38-43 */
 #define ORC_DISTANCE 0x001
@@ -246,6 +251,13 @@ int64_t orc_ccd_sh_extended_ref_range_tab(const orc_grid *g, const orc_sh_table 
                                           const int *tri_idx, const float *pos,
                                           const float *prdp, float thickness, int tri_begin,
                                           int tri_end, orc_contact *out, int64_t cap);
+/* the same on orc_get_threads() threads: consecutive triangle slices
+ * detected in parallel, then stored in loop order with the duplicate scan
+ * (the contact list equals the sequential one) */
+int64_t orc_ccd_sh_extended_ref_range_tab_mt(const orc_grid *g, const orc_sh_table *t,
+                                             int n_tris, const int *tri_idx, const float *pos,
+                                             const float *prdp, float thickness, int tri_begin,
+                                             int tri_end, orc_contact *out, int64_t cap);
 int64_t orc_ccd_sh_extended_ref_range(const orc_grid *g, int n_tris, const int *tri_idx,
                                       const float *pos, const float *prdp, float thickness,
                                       int tri_begin, int tri_end, orc_contact *out, int64_t cap);
@@ -279,6 +291,12 @@ void orc_collision_resolve_ref(int n_contacts, const orc_contact *cts,
  * result does not depend on contact order.  mass_weighted=0 uses the
  * reference split (VFResolveNew); 1 uses the inverse-mass split (see the
  * CUDA kernel for the formula). */
+/* CollisionResolveNew's sequential in-place pass with the correction of
+ * orc_vf_resolve_deltas (mass_weighted 0: the reference's; 1: inverse-mass
+ * split, scale-free guard) */
+void orc_collision_resolve_seq(int n_contacts, const orc_contact *cts, const float *pos,
+                               float *prdp, const float *mass, int iterations,
+                               float thickness, int mass_weighted);
 void orc_collision_resolve_jacobi(int n_points, int n_contacts,
                                   const orc_contact *cts, const float *pos,
                                   float *prdp, const float *mass, int iterations,
@@ -354,6 +372,17 @@ int64_t orc_substep_gpu(int n_points, const orc_constraints *c,
                         float damping, const float *gravity, const float *mass,
                         float *pos, float *vel, float *prdp, int bending_fp64,
                         const orc_colli_params *colli);
+/* orc_substep_gpu with the GPU path's analytic obstacles after every sweep
+ * (and its response): sphere4 = {centre xyz, radius} or NULL (the sphere
+ * push of ColliWithShpGrd), the ground plane y = ground_h when ground_on */
+int64_t orc_substep_gpu_obst(int n_points, const orc_constraints *c,
+                             const int *sorted_prim_id, int n_worksets,
+                             const int *worksets, int iterations, float dt,
+                             float damping, const float *gravity, const float *mass,
+                             float *pos, float *vel, float *prdp, int bending_fp64,
+                             const orc_colli_params *colli, const float *sphere4,
+                             int ground_on, float ground_h);
+void orc_ground(int n, float *prdp, float h);
 
 /* Reference CPU substep (P/PBD_cuda.cu:997-1009 advectCPU,
  * 1130-1210 projectConstraintWithColliCPU or 1090-1127 projectConstraintCPU,

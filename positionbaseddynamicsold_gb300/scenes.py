@@ -216,12 +216,25 @@ def hanging_cloth(res=32, seed=0):
     return grid_cloth(res, res, 1.0, 1.0, jitter=1e-3, seed=seed, pins=[0, res - 1])
 
 
-def drape_over_sphere(res=256, seed=0, sphere_level=5):
+def drape_over_sphere(res=256, seed=0, sphere_level=5, start="release", gap=1.5e-3):
     """res^2 grid over 2 m x 2 m, flat at y = 0.5 above a fixed sphere of
     radius 0.4 at the origin (icosphere, 20*4^level triangles), jitter
-    U(+-1e-4).  Collision: cell = 2 x mean rest edge, thickness 1e-3."""
+    U(+-1e-4).  Collision: cell = 2 x mean rest edge, thickness 1e-3.
+
+    start="contact": the released cloth fast-forwarded through its free fall
+    (a rigid translation: nothing else acts on it before it touches) until
+    its lowest point is `gap` above the sphere's top, every cloth point
+    moved down by that fall height d and moving at sqrt(2 g d) downward
+    (g = 9.8).  With the default gap of 1.5 thicknesses the sphere's top
+    triangles are within the contact band from the first substep."""
     cloth = grid_cloth(res, res, 2.0, 2.0, origin=(-1.0, 0.5, -1.0), jitter=1e-4, seed=seed)
     sp, st = icosphere(sphere_level, 0.4)
+    if start == "contact":
+        d = float(cloth["pos"][:, 1].min()) - (float(sp[:, 1].max()) + gap)
+        cloth["pos"][:, 1] -= np.float32(d)
+        cloth["vel"][:, 1] = -np.float32(np.sqrt(2.0 * 9.8 * d))
+    elif start != "release":
+        raise ValueError("start must be 'release' or 'contact'")
     scene = add_static_mesh(cloth, sp, st)
     cell = 2.0 * mean_rest_edge(cloth)
     scene["colli"] = {"cell": cell, "thickness": 1e-3, "center": (0.0, 0.0, 0.0),

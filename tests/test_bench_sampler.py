@@ -88,7 +88,7 @@ def test_ranges_against_one_table_find_the_pass_contacts(orc):
 
 @pytest.mark.parametrize("workload", ["drape256", "fold1024"])
 def test_one_substep_of_steps_covers_one_substep_of_work(workload):
-    sc, cfg, colli_on, _ = bench.make_workload(workload)
+    sc, cfg, colli_on, _, _ = bench.make_workload(workload)
     rs = bench.RefSampler(sc, cfg, colli_on, sc["pos"], sc["vel"])
     per = rs.iters * rs.m
     assert rs.phi == pytest.approx(1.0 / per)
@@ -118,3 +118,51 @@ def test_batch_scaling_by_points():
     # substep times 1.5 s and 3.0 s for 1,280 points; 100,000 points in all
     want = 1280 / ((0.3 / (3 / 15) + 0.6 / (6 / 30)) * 100000)
     assert b.value() == pytest.approx(want)
+
+
+def test_threaded_reference_substeps_equal_one_thread():
+    """RefSubsteps with the CCD detection spread over host threads gives the
+    one-thread result exactly: contact lists (stored in loop order with the
+    duplicate scan) and positions, with either response; and the threaded
+    contact list equals the sequential CCD_SH_Extended's."""
+    from oracle.oracle import Oracle
+    from positionbaseddynamicsold_gb300 import scenes
+    sc = scenes.drape_over_sphere(res=40, seed=3, sphere_level=2, start="contact")
+    cfg = {"gs_iterations": 15}
+    for mw in (1, 0):
+        out = []
+        for th in (1, 4):
+            rs = bench.RefSubsteps(sc, cfg, sc["pos"], sc["vel"], th, mass_weighted=mw)
+            nc = []
+            for _ in range(4):
+                rs.step()
+                nc.append(int(rs.contacts))
+            out.append((rs.state["pos"].copy(), nc))
+        np.testing.assert_array_equal(out[0][0], out[1][0])
+        assert out[0][1] == out[1][1] and max(out[0][1]) > 0
+    orc = Oracle()
+    n = sc["n_cloth_points"]
+    pos = sc["pos"].copy()
+    prd = pos.copy()
+    prd[:n, 1] -= np.float32(0.03)
+    grid = orc.grid((0.0, 0.0, 0.0), None, sc["colli"]["cell"], False)
+    res = []
+    for th in (1, 4):
+        orc.set_threads(th)
+        res.append(orc.ccd(grid, sc["tri_idx"], pos, prd, 1e-3, mode="ref"))
+    orc.set_threads(1)
+    assert res[0][1] == res[1][1] > 20
+    for k in res[0][0]:
+        np.testing.assert_array_equal(res[0][0][k], res[1][0][k])
+
+
+def test_reference_arm_and_gpu_arm_share_the_workload_config():
+    """Both arms take the workload's config from make_workload; it holds
+    only what describes the workload (no GPU-derived plan)."""
+    for w in ("drape256", "hanging32"):
+        sc, cfg, colli_on, tl, preroll = bench.make_workload(w)
+        for k in ("colors", "autotune", "points", "parallelism"):
+            assert k not in cfg
+        assert cfg["preroll_substeps"] == preroll
+    sc, cfg, _, _, preroll = bench.make_workload("drape256")
+    assert preroll == 0 and "start" in cfg and "response" in cfg
