@@ -189,7 +189,7 @@ class ClockSampler:
                 "samples": len(self.samples)}
 
 
-def setup(sc, colli_on, table_log2):
+def setup(sc, colli_on, table_log2, overlap=True):
     from positionbaseddynamicsold_gb300.pbd import (RESPONSE_MASS_WEIGHTED, CollisionSolver,
                                                     PBDObject, SolverPBD, SpatialHashSystem)
     obj = PBDObject(sc, damping=1.0, gravity=G)
@@ -203,6 +203,7 @@ def setup(sc, colli_on, table_log2):
                              response=RESPONSE_MASS_WEIGHTED)
         n = obj.n_points
         cs.set_capacity(max(1 << 22, 64 * n), max(1 << 20, 4 * n))
+        cs.set_overlap(overlap)
         if "ground" in sc["colli"]:
             solver.set_ground(True, sc["colli"]["ground"])
         if "spheres" in sc["colli"]:
@@ -230,7 +231,10 @@ def measure(name, args, rank, world, headline=True):
     # done when the slowest rank is); the other workloads run replicas
     sharded = name == "batch512" and world > 1
     units = 1 if sharded else world
-    obj, solver, shs, cs = setup(sc, colli_on, tl)
+    obj, solver, shs, cs = setup(sc, colli_on, tl, overlap=not args.no_overlap)
+    plan = {}
+    if colli_on:
+        plan["detection_overlaps_sweep"] = not args.no_overlap
     solver.set_gs_path({"auto": 0, "per-color": 1, "cluster": 2}[args.gs_path])
     if args.gs_block:
         solver.set_gs_block(args.gs_block)
@@ -246,8 +250,8 @@ def measure(name, args, rank, world, headline=True):
     nb = int((sc["ctype"] == scenes.BENDING).sum())
     n_colors = obj.eval_worksets()
     iters = cfg["gs_iterations"]
-    plan = {"colors": n_colors, "points": obj.n_points, "triangles": obj.n_tris,
-            "distance_constraints": nd, "bending_constraints": nb}
+    plan.update({"colors": n_colors, "points": obj.n_points, "triangles": obj.n_tris,
+            "distance_constraints": nd, "bending_constraints": nb})
 
     if args.solve == "residual":
         cfg["solve"] = {"target_stretch_residual": args.target, "max_sweeps": args.max_sweeps,
@@ -814,6 +818,9 @@ def main():
     ap.add_argument("--no-autotune", action="store_true",
                     help="keep the default GS launch form (per-color, 256 threads) instead of "
                          "the autotuner's pick")
+    ap.add_argument("--no-overlap", action="store_true",
+                    help="run each CCD detection before its sweep on the object's stream "
+                         "instead of beside it (same results)")
     ap.add_argument("--edge-edge", action="store_true",
                     help="also run edge-edge CCD (not in the reference's step; off by default)")
     ap.add_argument("--no-learned-eval", action="store_true",

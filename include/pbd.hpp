@@ -120,6 +120,7 @@ public:
     void SetThickness(float t) { check(pbd_colli_set_thickness(h_, t)); }
     void SetIterations(int i) { check(pbd_colli_set_iterations(h_, i)); }
     void SetResponse(int mode) { check(pbd_colli_set_response(h_, mode)); }
+    void SetOverlap(bool on) { check(pbd_colli_set_overlap(h_, on ? 1 : 0)); }
     void CCD_SH_Extended() { check(pbd_colli_ccd_sh_extended(h_)); }
     void CollisionResolveNew() { check(pbd_colli_collision_resolve_new(h_)); }
     long long ContactCount() {

@@ -307,6 +307,14 @@ int pbd_colli_set_thickness(pbd_colli *c, float thickness);    /* SetThickness  
 int pbd_colli_set_iterations(pbd_colli *c, int iterations);    /* SetIterations: response passes */
 int pbd_colli_set_response(pbd_colli *c, int mode);            /* PBD_RESPONSE_* */
 int pbd_colli_set_capacity(pbd_colli *c, long long candidates, long long contacts);
+/* No counterpart in the reference (its detection and projection share one
+ * host thread).  on = 1 (default): inside pbd_solver_step and
+ * pbd_solver_project_constraint_with_colli, a due detection runs on a
+ * low-priority side stream from a copy of the iteration's starting
+ * positions, beside that iteration's sweep; the response waits for it.
+ * The contacts, and every result, are those of on = 0 (detection, then
+ * sweep, on the object's stream). */
+int pbd_colli_set_overlap(pbd_colli *c, int on);
 /* CCD_SH_Extended (P/CCD.cpp:210-274, 1522-1587): UpdateSH on the predicted
  * positions, then the vertex-face ExtendedVFTest over every distinct
  * (point, neighbour triangle) pair; contacts kept on the device, sorted by

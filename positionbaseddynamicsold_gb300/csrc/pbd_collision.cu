@@ -57,14 +57,27 @@ namespace {
 constexpr int kMaxInc = 16;  // incident triangles considered per point
 
 // ---------------------------------------------------------------------------
-__global__ void k_reset_buckets(const uint32_t *skey, const int *n_prev, uint32_t nb,
-                                float4 *btab, long long cap) {
-    long long n = *n_prev;
+// Clears the buckets the previous update filled.  n_valid = {valid keys of
+// that update, blocks done}: the last block to finish (every block has read
+// the count by then) zeroes both for the update that follows, and zeroes
+// `zero` (n_zero ints, the detection's counters) when given.
+__global__ void k_reset_buckets(const uint32_t *skey, int *n_valid, uint32_t nb, float4 *btab,
+                                long long cap, int *zero, int n_zero) {
+    long long n = n_valid[0];
     if (n > cap) n = cap;
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
          i += (long long)gridDim.x * blockDim.x) {
         uint32_t k = skey[i];
         if (k < nb) btab[2 * (size_t)k] = make_float4(0.f, 0.f, 0.f, 0.f);  // empty range
+    }
+    if (zero && blockIdx.x == 0 && (int)threadIdx.x < n_zero) zero[threadIdx.x] = 0;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        if (atomicAdd(n_valid + 1, 1) == (int)gridDim.x - 1) {
+            n_valid[0] = 0;
+            n_valid[1] = 0;
+        }
     }
 }
 
@@ -500,6 +513,13 @@ __global__ void __launch_bounds__(128) k_narrow_roots(const int2 *__restrict__ c
     }
 }
 
+// the predicted positions an overlapped detection reads
+__global__ void __launch_bounds__(256) k_copy_points(int n, const float4 *__restrict__ p,
+                                                     float4 *__restrict__ q) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) q[i] = p[i];
+}
+
 __global__ void k_clamp_counts(int *counters, long long cap, long long ccap) {
     if (threadIdx.x == 0 && blockIdx.x == 0) {
         if (counters[1] > ccap) counters[1] = (int)ccap;
@@ -509,11 +529,11 @@ __global__ void k_clamp_counts(int *counters, long long cap, long long ccap) {
 
 // corrections of one contact (VFResolveTest + VFResolveNew, P/CCD.cpp:1996-2090)
 // added to the per-point fixed-point sums
-__global__ void __launch_bounds__(128) k_contact_deltas(const int *counters, const int4 *ids,
+__global__ void __launch_bounds__(128) k_contact_deltas(int *counters, const int4 *ids,
                                                         const float4 *__restrict__ x,
                                                         const float4 *__restrict__ p, float th,
                                                         int mass_weighted, long long *acc,
-                                                        int *acnt) {
+                                                        int *acnt, int *touched) {
     // launched as a programmatic dependent of the sweep's last color phase:
     // nothing is read before that phase has completed; the apply kernel may
     // then launch while the corrections are summed
@@ -569,19 +589,23 @@ __global__ void __launch_bounds__(128) k_contact_deltas(const int *counters, con
         add_fixed(acc, id.y, d1.x, d1.y, d1.z);
         add_fixed(acc, id.z, d2.x, d2.y, d2.z);
         add_fixed(acc, id.w, d3.x, d3.y, d3.z);
-        atomicAdd(acnt + id.x, 1);
-        atomicAdd(acnt + id.y, 1);
-        atomicAdd(acnt + id.z, 1);
-        atomicAdd(acnt + id.w, 1);
+        touch_point(acnt, id.x, touched, counters);
+        touch_point(acnt, id.y, touched, counters);
+        touch_point(acnt, id.z, touched, counters);
+        touch_point(acnt, id.w, touched, counters);
     }
 }
 
-// every point with a correction: p += sum * 2^-32 / count; sums cleared
-__global__ void k_apply_deltas(int n, long long *acc, int *acnt, float4 *p) {
+// every point with a correction (the touched list): p += sum * 2^-32 /
+// count; sums and counts cleared.  The last block to finish empties the
+// list (every block has read its length by then).
+__global__ void __launch_bounds__(256) k_apply_touched(int *counters, const int *touched,
+                                                       long long *acc, int *acnt, float4 *p) {
     asm volatile("griddepcontrol.wait;" ::: "memory");  // every sum is complete
-    for (int pt = blockIdx.x * blockDim.x + threadIdx.x; pt < n; pt += gridDim.x * blockDim.x) {
+    const int n = counters[kTouched];
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+        const int pt = touched[k];
         int cnt = acnt[pt];
-        if (cnt <= 0) continue;
         acnt[pt] = 0;
         long long sx = acc[3 * (long long)pt], sy = acc[3 * (long long)pt + 1],
                   sz = acc[3 * (long long)pt + 2];
@@ -594,6 +618,14 @@ __global__ void k_apply_deltas(int n, long long *acc, int *acnt, float4 *p) {
         P.y = P.y + (float)((double)sy * (1.0 / 4294967296.0) / dc);
         P.z = P.z + (float)((double)sz * (1.0 / 4294967296.0) / dc);
         p[pt] = P;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        if (atomicAdd(counters + kApplyDone, 1) == (int)gridDim.x - 1) {
+            counters[kTouched] = 0;
+            counters[kApplyDone] = 0;
+        }
     }
 }
 
@@ -627,22 +659,26 @@ int round8(int b) { return (b + 7) / 8 * 8; }
 
 
 constexpr int kPersistentBlocks = 8 * kNumSMs;
+// the response's two kernels: grid-stride over the contacts / touched points
+constexpr int kResponseBlocks = 2 * kNumSMs;
+// bucket reset: grid-stride over the previous update's keys
+constexpr int kResetBlocks = 2 * kNumSMs;
 
 }  // namespace
 
-// UpdateSH on the object's predicted positions
-int shs_update(pbd_shs *h) {
+// UpdateSH on predicted positions psrc (the object's, or a copy of them),
+// enqueued on stream s
+static int shs_update_on(pbd_shs *h, cudaStream_t s, const float4 *psrc, int *zero = nullptr,
+                         int n_zero = 0) {
     PBD_CHECK(h->initialized, PBD_ERR_STATE, "spatial hash used before InitSH");
     pbd_object *o = h->obj;
-    cudaStream_t s = o->stream;
     GridParams g = params_of(h);
     if (o->nt == 0) return PBD_OK;
     // clear the ranges of the buckets the previous update filled
-    k_reset_buckets<<<kPersistentBlocks, 256, 0, s>>>(h->skey, h->n_valid.p, g.nb, h->btab.p,
-                                                      o->nt);
-    PBD_CUDA(cudaMemsetAsync(h->n_valid.p, 0, sizeof(int), s));
+    k_reset_buckets<<<kResetBlocks, 256, 0, s>>>(h->skey, h->n_valid.p, g.nb, h->btab.p, o->nt,
+                                                 zero, n_zero);
     k_tri_cells<<<grid_for(o->nt, 256), 256, 0, s>>>(o->nt, g, 0.0f, h->inst_cell.p,
-                                                     h->n_inst_cell, o->tri.p, o->x.p, o->p.p,
+                                                     h->n_inst_cell, o->tri.p, o->x.p, psrc,
                                                      h->tcell.p, h->tlo.p, h->thi.p, h->key.p,
                                                      h->id.p, h->n_valid.p);
     PBD_LAUNCH();
@@ -653,6 +689,9 @@ int shs_update(pbd_shs *h) {
     PBD_LAUNCH();
     return PBD_OK;
 }
+
+// UpdateSH on the object's predicted positions
+int shs_update(pbd_shs *h) { return shs_update_on(h, h->obj->stream, h->obj->p.p); }
 
 static int colli_alloc(pbd_colli *c) {
     pbd_object *o = c->obj;
@@ -667,29 +706,33 @@ static int colli_alloc(pbd_colli *c) {
     PBD_TRY(c->cw.alloc(H));
     PBD_TRY(c->acc.alloc(3 * (size_t)o->n));
     PBD_TRY(c->acnt.alloc(o->n));
+    PBD_TRY(c->touched.alloc(o->n));
     PBD_CUDA(cudaMemsetAsync(c->acc.p, 0, sizeof(long long) * 3 * (size_t)o->n, o->stream));
     PBD_CUDA(cudaMemsetAsync(c->acnt.p, 0, sizeof(int) * (size_t)o->n, o->stream));
     PBD_CUDA(cudaMemsetAsync(c->counters.p, 0, sizeof(int) * 16, o->stream));
+    // overlapped detections (made here, outside any stream capture)
+    PBD_TRY(c->psnap.alloc(o->n));
+    if (!c->side) {
+        int least = 0, greatest = 0;
+        PBD_CUDA(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+        PBD_CUDA(cudaStreamCreateWithPriority(&c->side, cudaStreamNonBlocking, least));
+    }
+    if (!c->ev_fork) PBD_CUDA(cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming));
+    if (!c->ev_join) PBD_CUDA(cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming));
     return PBD_OK;
 }
 
-// CCD_SH_Extended on the device; no host synchronisation
-int ccd_detect(pbd_colli *c) {
-    PBD_CHECK(c && c->obj && c->shs, PBD_ERR_STATE, "collision solver needs a target and a hash");
-    PBD_CHECK(c->shs->obj == c->obj, PBD_ERR_ARG, "hash and collision solver target differ");
+// CCD_SH_Extended on the device from predicted positions psrc, enqueued on
+// stream s (buffers already sized); no host synchronisation
+static int ccd_detect_on(pbd_colli *c, cudaStream_t s, const float4 *psrc) {
     pbd_object *o = c->obj;
     pbd_shs *h = c->shs;
-    cudaStream_t s = o->stream;
-    // (re)size everything for the current target: a first call, a capacity
-    // change, or a target with another point count
-    if (!c->cand.p || c->sized_n != o->n) {
-        PBD_TRY(colli_alloc(c));
-        c->sized_n = o->n;
+    if (o->nt == 0) {
+        PBD_CUDA(cudaMemsetAsync(c->counters.p, 0, sizeof(int) * 16, s));
+        return PBD_OK;
     }
-    if (c->ee_on) PBD_TRY(ee_prepare(c));
-    PBD_CUDA(cudaMemsetAsync(c->counters.p, 0, sizeof(int) * 16, s));
-    if (o->nt == 0) return PBD_OK;
-    PBD_TRY(shs_update(h));
+    // the hash update's first kernel also zeroes the 16 counters
+    PBD_TRY(shs_update_on(h, s, psrc, c->counters.p, 16));
     GridParams g = params_of(h);
     float th = c->thickness;
     // a hit needs the point within sqrt((2h)^2 + r^2) of the triangle, r =
@@ -704,22 +747,66 @@ int ccd_detect(pbd_colli *c) {
     k_point_pairs<<<pp_blocks, 32 * kTaskWarps, 0, s>>>(
         o->n, g, margin, o->pt_tri_first.p, o->pt_tri_last.p, o->pt_tri.p,
         o->has_inst ? o->point_inst.p : nullptr, o->has_inst ? o->tri_inst.p : nullptr, o->x.p,
-        o->p.p, h->tcell.p, h->btab.p, h->etab.p, c->pairs.p, c->task_cap, c->counters.p);
+        psrc, h->tcell.p, h->btab.p, h->etab.p, c->pairs.p, c->task_cap, c->counters.p);
     PBD_LAUNCH();
     k_dist_filter<<<kPersistentBlocks, 256, 0, s>>>(c->pairs.p, c->task_cap, th, o->tri.p,
-                                                    o->x.p, o->p.p, c->cand.p, c->cand_cap,
+                                                    o->x.p, psrc, c->cand.p, c->cand_cap,
                                                     c->counters.p);
     PBD_LAUNCH();
     k_narrow<<<kPersistentBlocks, 128, 0, s>>>(c->cand.p, c->cand_cap, o->nt, th, o->tri.p,
-                                               o->x.p, o->p.p, c->counters.p, c->contact_cap,
+                                               o->x.p, psrc, c->counters.p, c->contact_cap,
                                                c->cids.p, c->cface.p, c->ctn.p, c->cw.p,
                                                c->hard.p);
-    k_narrow_roots<<<kPersistentBlocks, 128, 0, s>>>(c->cand.p, th, o->tri.p, o->x.p, o->p.p,
+    k_narrow_roots<<<kPersistentBlocks, 128, 0, s>>>(c->cand.p, th, o->tri.p, o->x.p, psrc,
                                                      c->counters.p, c->contact_cap, c->cids.p,
                                                      c->cface.p, c->ctn.p, c->cw.p, c->hard.p);
     k_clamp_counts<<<1, 32, 0, s>>>(c->counters.p, c->cand_cap, c->contact_cap);
     PBD_LAUNCH();
+    return PBD_OK;
+}
+
+static int ccd_prepare(pbd_colli *c) {
+    PBD_CHECK(c && c->obj && c->shs, PBD_ERR_STATE, "collision solver needs a target and a hash");
+    PBD_CHECK(c->shs->obj == c->obj, PBD_ERR_ARG, "hash and collision solver target differ");
+    pbd_object *o = c->obj;
+    // (re)size everything for the current target: a first call, a capacity
+    // change, or a target with another point count
+    if (!c->cand.p || c->sized_n != o->n) {
+        PBD_TRY(colli_alloc(c));
+        c->sized_n = o->n;
+    }
+    if (c->ee_on) PBD_TRY(ee_prepare(c));
+    return PBD_OK;
+}
+
+// CCD_SH_Extended on the device; no host synchronisation
+int ccd_detect(pbd_colli *c) {
+    PBD_TRY(ccd_prepare(c));
+    PBD_TRY(ccd_detect_on(c, c->obj->stream, c->obj->p.p));
     if (c->ee_on) PBD_TRY(ee_detect(c));
+    return PBD_OK;
+}
+
+int ccd_detect_fork(pbd_colli *c, bool *forked) {
+    *forked = false;
+    PBD_CHECK(c && c->obj && c->shs, PBD_ERR_STATE, "collision solver needs a target and a hash");
+    pbd_object *o = c->obj;
+    if (!c->overlap || c->ee_on || !c->cand.p || c->sized_n != o->n || !c->side ||
+        o->nt == 0 || c->shs->obj != o)
+        return ccd_detect(c);
+    cudaStream_t s = o->stream;
+    k_copy_points<<<grid_for(o->n, 256), 256, 0, s>>>(o->n, o->p.p, c->psnap.p);
+    PBD_LAUNCH();
+    PBD_CUDA(cudaEventRecord(c->ev_fork, s));
+    PBD_CUDA(cudaStreamWaitEvent(c->side, c->ev_fork, 0));
+    PBD_TRY(ccd_detect_on(c, c->side, c->psnap.p));
+    PBD_CUDA(cudaEventRecord(c->ev_join, c->side));
+    *forked = true;
+    return PBD_OK;
+}
+
+int ccd_join(pbd_colli *c) {
+    PBD_CUDA(cudaStreamWaitEvent(c->obj->stream, c->ev_join, 0));
     return PBD_OK;
 }
 
@@ -735,21 +822,22 @@ int ccd_resolve(pbd_colli *c, int passes) {
     at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
     at[0].val.programmaticStreamSerializationAllowed = 1;
     cudaLaunchConfig_t cd = {}, ca = {};
-    cd.gridDim = dim3(kPersistentBlocks);
+    cd.gridDim = dim3(kResponseBlocks);
     cd.blockDim = dim3(128);
-    ca.gridDim = dim3(grid_for(o->n, 256));
+    ca.gridDim = dim3(kResponseBlocks);
     ca.blockDim = dim3(256);
     cd.stream = ca.stream = s;
     cd.attrs = ca.attrs = at;
     cd.numAttrs = ca.numAttrs = o->pdl ? 1 : 0;
     for (int k = 0; k < passes; ++k) {
-        PBD_CUDA(cudaLaunchKernelEx(&cd, k_contact_deltas, (const int *)c->counters.p,
+        PBD_CUDA(cudaLaunchKernelEx(&cd, k_contact_deltas, c->counters.p,
                                     (const int4 *)c->cids.p, (const float4 *)o->x.p,
                                     (const float4 *)o->p.p, c->thickness,
                                     (int)(c->response == PBD_RESPONSE_MASS_WEIGHTED), c->acc.p,
-                                    c->acnt.p));
+                                    c->acnt.p, c->touched.p));
         if (c->ee_on) PBD_TRY(ee_deltas_launch(c));
-        PBD_CUDA(cudaLaunchKernelEx(&ca, k_apply_deltas, o->n, c->acc.p, c->acnt.p, o->p.p));
+        PBD_CUDA(cudaLaunchKernelEx(&ca, k_apply_touched, c->counters.p,
+                                    (const int *)c->touched.p, c->acc.p, c->acnt.p, o->p.p));
     }
     return PBD_OK;
 }
@@ -771,11 +859,11 @@ static int shs_alloc(pbd_shs *h) {
     PBD_TRY(h->id.alloc(nt));
     PBD_TRY(h->id_alt.alloc(nt));
     PBD_TRY(h->etab.alloc(3 * nt));
-    PBD_TRY(h->n_valid.alloc(1));
+    PBD_TRY(h->n_valid.alloc(2));
     PBD_TRY(h->btab.alloc(2 * ((size_t)h->n_buckets + 1)));
     PBD_TRY(radix_reserve(h->scr, (long long)nt, round8(h->key_bits)));
     PBD_CUDA(cudaMemsetAsync(h->btab.p, 0, sizeof(float4) * 2 * (h->n_buckets + 1), o->stream));
-    PBD_CUDA(cudaMemsetAsync(h->n_valid.p, 0, sizeof(int), o->stream));
+    PBD_CUDA(cudaMemsetAsync(h->n_valid.p, 0, 2 * sizeof(int), o->stream));
     h->skey = h->key.p;
     h->sid = h->id.p;
     return PBD_OK;
@@ -991,6 +1079,12 @@ int pbd_colli_set_capacity(pbd_colli *c, long long cand, long long contacts) {
     c->task_cap = cand;
     c->cand.release();
     c->cids.release();
+    return PBD_OK;
+}
+
+int pbd_colli_set_overlap(pbd_colli *c, int on) {
+    PBD_CHECK(c, PBD_ERR_ARG, "null argument");
+    c->overlap = on ? 1 : 0;
     return PBD_OK;
 }
 

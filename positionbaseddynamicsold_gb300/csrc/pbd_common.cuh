@@ -116,6 +116,9 @@ struct HBuf {
     }
 };
 
+// response bookkeeping in pbd_colli::counters
+constexpr int kTouched = 5, kApplyDone = 6;
+
 // ---- stable LSD radix sort (8-bit digits) of (key, int value) pairs --------
 // Sorts n elements (n read from d_count when non-null, capped by n_cap),
 // `bits` low key bits.  Buffers: keys/vals in and alt (same capacity) and a
@@ -277,7 +280,9 @@ struct pbd_colli {
     pbd::DBuf<int2> pairs;      // AABB-overlapping (point, triangle)
     pbd::DBuf<int2> cand;
     pbd::DBuf<int> counters;    // [0] candidates, [1] contacts, [2] overflow flags, [3] hard
-                                // candidates (cubic roots needed), [4] AABB pairs
+                                // candidates (cubic roots needed), [4] AABB pairs,
+                                // [5] touched points of the response pass, [6] apply
+                                // blocks done
     pbd::DBuf<int> hard;        // candidate indices that need the cubic's roots
     int sized_n = -1;           // point count the per-point buffers were sized for
     // contacts, in the order the narrow phase found them
@@ -289,6 +294,9 @@ struct pbd_colli {
     // between passes)
     pbd::DBuf<long long> acc;
     pbd::DBuf<int> acnt;
+    // points whose count went from 0 to 1 in the current response pass
+    // (counters[kTouched] of them); the apply kernel visits only these
+    pbd::DBuf<int> touched;
     // edge-edge CCD (off unless enabled): the object's unique edges (built
     // on first use; -1 = not yet), their grown swept boxes, the edge-cell
     // entries of the edge hash and their sort buffers, the edge pairs,
@@ -310,6 +318,21 @@ struct pbd_colli {
     pbd::DBuf<int4> ee_ids;
     pbd::DBuf<float4> ee_m0, ee_tsu;
     pbd::SortScratch ee_scr;
+    // Detection overlapped with the sweep that follows it (the substeps of
+    // pbd_solver_step / project_constraint_with_colli): a copy of the
+    // predicted positions at the iteration's start, a low-priority side
+    // stream the detection runs on, and the fork / join events.  The
+    // response after the sweep waits for the join, so the contacts are the
+    // ones a detection before the sweep finds.
+    int overlap = 1;
+    pbd::DBuf<float4> psnap;
+    cudaStream_t side = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+    ~pbd_colli() {
+        if (ev_fork) cudaEventDestroy(ev_fork);
+        if (ev_join) cudaEventDestroy(ev_join);
+        if (side) cudaStreamDestroy(side);
+    }
 };
 
 // Device state of the solve-to-residual loop (one per solver).
@@ -421,7 +444,17 @@ constexpr int kResidualParts = 4 * kNumSMs;
 int launch_residual_parts(pbd_object *o, bool dist, bool bend, const float4 *pos);
 int launch_obstacles(pbd_solver *s);
 int ccd_detect(pbd_colli *c);
+// the detection of one iteration started on the side stream from a copy of
+// the predicted positions (overlapping the sweep the caller launches next);
+// returns PBD_OK with *forked = false when it ran on the object's stream
+// instead (overlap off, edge-edge CCD on, or buffers not yet sized)
+int ccd_detect_fork(pbd_colli *c, bool *forked);
+// the object's stream waits for a forked detection
+int ccd_join(pbd_colli *c);
 int ccd_resolve(pbd_colli *c, int passes);
+// priority of the color-phase launches (the greatest the device offers),
+// so pending sweep blocks are scheduled before an overlapped detection's
+int gs_priority();
 // edge-edge CCD (pbd_edge.cu): buffers and edge list, one detection pass,
 // the response's corrections into the shared fixed-point sums
 int ee_prepare(pbd_colli *c);

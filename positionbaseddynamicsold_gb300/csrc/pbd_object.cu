@@ -645,17 +645,32 @@ static int launch_sweep_per_color(pbd_object *o, int iter, const float *expk_dev
         cfg.gridDim = dim3(grid_for(tot, o->gs_block));
         cfg.blockDim = dim3(o->gs_block);
         cfg.stream = o->stream;
-        cudaLaunchAttribute at[1];
-        at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-        at[0].val.programmaticStreamSerializationAllowed = 1;
+        cudaLaunchAttribute at[2];
+        at[0].id = cudaLaunchAttributePriority;
+        at[0].val.priority = gs_priority();
+        at[1].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+        at[1].val.programmaticStreamSerializationAllowed = 1;
         cfg.attrs = at;
-        cfg.numAttrs = o->pdl ? 1 : 0;
+        cfg.numAttrs = o->pdl ? 2 : 1;
         PBD_CUDA(cudaLaunchKernelEx(&cfg, k_project_color, (const int4 *)(o->drec.p + d0), nd,
                                     (const int4 *)(o->bidx.p + b0), (const float2 *)(o->bpar.p + b0),
                                     nb, (const float4 *)(o->arec.p + a0), na, o->p.p, expk,
                                     expk_dev, o->sched));
     }
     return PBD_OK;
+}
+
+int gs_priority() {
+    static int prio = 1;
+    if (prio == 1) {
+        int least = 0, greatest = 0;
+        if (cudaDeviceGetStreamPriorityRange(&least, &greatest) != cudaSuccess) {
+            cudaGetLastError();
+            greatest = 0;
+        }
+        prio = greatest;
+    }
+    return prio;
 }
 
 int launch_sweep_dev(pbd_solver *s, const float *expk_dev, bool obstacles_inside) {
@@ -1687,11 +1702,20 @@ int pbd_solver_set_instance_spheres(pbd_solver *s, int n, const float *spheres4)
     return PBD_OK;
 }
 
+// projectConstraintWithColli's iteration (P/PBD_cuda.cu:1130-1210): CCD when
+// due, one sweep, the response, the analytic obstacles.  A due detection
+// reads the positions at the iteration's start and its contacts are first
+// used by the response after the sweep, so it runs beside the sweep on the
+// collision solver's side stream (from a copy of those positions) and the
+// response waits for it: the same contacts as a detection before the
+// sweep.
 static int project_with_colli(pbd_solver *s, int iterations, pbd_colli *c) {
     if (!c) return iterations > 0 ? launch_sweeps(s, 0, iterations, true) : PBD_OK;
     for (int ii = 0; ii < iterations; ++ii) {
-        if (ii % 10 == 0 || ii == iterations - 1) PBD_TRY(ccd_detect(c));
+        bool forked = false;
+        if (ii % 10 == 0 || ii == iterations - 1) PBD_TRY(ccd_detect_fork(c, &forked));
         PBD_TRY(launch_sweeps(s, ii, ii + 1, false));
+        if (forked) PBD_TRY(ccd_join(c));
         PBD_TRY(ccd_resolve(c, c->iterations));
         PBD_TRY(launch_obstacles(s));
     }
@@ -1754,7 +1778,8 @@ int pbd_solver_step(pbd_solver *s, float dt, int substeps, int iterations, pbd_c
             if (cudaGraphNodeGetType(nodes[i], &t) == cudaSuccess && t == cudaGraphNodeTypeKernel) ++nk;
         }
         s->g_kernels = nk;
-        cudaError_t ei = cudaGraphInstantiate(&s->gexec, g, 0);
+        // node priorities: the color phases before an overlapped detection
+        cudaError_t ei = cudaGraphInstantiate(&s->gexec, g, cudaGraphInstantiateFlagUseNodePriority);
         cudaGraphDestroy(g);
         PBD_CUDA(ei);
         s->g_dt = dt;

@@ -71,7 +71,8 @@ EXPORTS = [
     "pbd_shs_update", "pbd_shs_find_neighbors", "pbd_shs_find_neighbors_all",
     "pbd_colli_create", "pbd_colli_destroy", "pbd_colli_set_target",
     "pbd_colli_set_acce_struct", "pbd_colli_set_thickness", "pbd_colli_set_iterations",
-    "pbd_colli_set_response", "pbd_colli_set_capacity", "pbd_colli_ccd_sh_extended",
+    "pbd_colli_set_response", "pbd_colli_set_capacity", "pbd_colli_set_overlap",
+    "pbd_colli_ccd_sh_extended",
     "pbd_colli_collision_resolve_new", "pbd_colli_get_contacts", "pbd_colli_stats",
     "pbd_colli_get_pairs",
     "pbd_ccd_vf_test_batch",
@@ -584,6 +585,11 @@ class CollisionSolver:
 
     def set_capacity(self, candidates, contacts):
         _check(self.L.pbd_colli_set_capacity(self.h, int(candidates), int(contacts)))
+
+    def set_overlap(self, on=True):
+        """detections inside step / project_constraint_with_colli run beside
+        the following sweep on a side stream (same results either way)"""
+        _check(self.L.pbd_colli_set_overlap(self.h, int(bool(on))))
 
     def ccd_sh_extended(self):
         _check(self.L.pbd_colli_ccd_sh_extended(self.h))

@@ -255,3 +255,32 @@ def test_solver_retargeted_to_a_larger_object():
     assert cs.stats()["contacts"] == fresh.stats()["contacts"]
     fresh.collision_resolve_new()
     np.testing.assert_array_equal(got, b2.predicted())
+
+
+@pytest.mark.parametrize("graph", [False, True])
+def test_overlapped_detection_equals_sequential(graph):
+    """A detection run beside the following sweep (side stream, copy of the
+    iteration's starting positions; the response waits for it) gives the
+    sequential substeps' results bit for bit: drape with self contacts and
+    a fold onto the ground plane."""
+    for sc, log2 in ((scenes.drape_over_sphere(res=64, seed=4, sphere_level=3,
+                                               start="contact"), 16),
+                     (scenes.folding_cloth(res=64, seed=4, size=0.5), 16)):
+        G = np.array([0, -9.8, 0], np.float32)
+        res = []
+        for overlap in (False, True):
+            obj = PBDObject(sc, damping=1.0, gravity=G)
+            obj.prepare()
+            shs = SpatialHashSystem(obj, cell_size=sc["colli"]["cell"], log2_table=log2)
+            shs.init()
+            cs = CollisionSolver(obj, shs, thickness=1e-3, iterations=1,
+                                 response=RESPONSE_MASS_WEIGHTED)
+            cs.set_overlap(overlap)
+            s = SolverPBD(obj)
+            if "ground" in sc["colli"]:
+                s.set_ground(True, sc["colli"]["ground"])
+            s.step(1.0 / 600, substeps=30, iterations=15, colli=cs, use_graph=graph)
+            res.append((obj.positions(), obj.velocities(), cs.stats()["contacts"]))
+        np.testing.assert_array_equal(res[0][0], res[1][0])
+        np.testing.assert_array_equal(res[0][1], res[1][1])
+        assert res[0][2] == res[1][2]
