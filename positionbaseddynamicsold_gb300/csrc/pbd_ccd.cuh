@@ -353,12 +353,6 @@ __device__ __forceinline__ int agg_inc(int *counter) {
     return g.shfl(base, 0) + (int)g.thread_rank();
 }
 
-// one more correction for point `id`; the first one of a pass lists the
-// point for the apply kernel (one list atomic per warp)
-__device__ __forceinline__ void touch_point(int *acnt, int id, int *touched, int *counters) {
-    if (atomicAdd(acnt + id, 1) == 0) touched[agg_inc(counters + kTouched)] = id;
-}
-
 __device__ __forceinline__ void add_fixed(long long *acc, int pt, float dx, float dy, float dz) {
     atomicAdd((unsigned long long *)(acc + 3 * (long long)pt), (unsigned long long)__float2ll_rn(dx * 4294967296.0f));
     atomicAdd((unsigned long long *)(acc + 3 * (long long)pt + 1), (unsigned long long)__float2ll_rn(dy * 4294967296.0f));

@@ -57,27 +57,19 @@ namespace {
 constexpr int kMaxInc = 16;  // incident triangles considered per point
 
 // ---------------------------------------------------------------------------
-// Clears the buckets the previous update filled.  n_valid = {valid keys of
-// that update, blocks done}: the last block to finish (every block has read
-// the count by then) zeroes both for the update that follows, and zeroes
-// `zero` (n_zero ints, the detection's counters) when given.
-__global__ void k_reset_buckets(const uint32_t *skey, int *n_valid, uint32_t nb, float4 *btab,
-                                long long cap, int *zero, int n_zero) {
-    long long n = n_valid[0];
-    if (n > cap) n = cap;
-    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
-         i += (long long)gridDim.x * blockDim.x) {
+// Clears the buckets the previous update filled: its sorted keys (all nt
+// triangles; keys >= nb are the out-of-grid ones) name them.  Also zeroes
+// the valid-key count for the update that follows and, when given, `zero`
+// (n_zero ints: the detection's counters).
+__global__ void k_reset_buckets(const uint32_t *skey, int nt, uint32_t nb, float4 *btab,
+                                int *n_valid, int *zero, int n_zero) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nt; i += gridDim.x * blockDim.x) {
         uint32_t k = skey[i];
         if (k < nb) btab[2 * (size_t)k] = make_float4(0.f, 0.f, 0.f, 0.f);  // empty range
     }
-    if (zero && blockIdx.x == 0 && (int)threadIdx.x < n_zero) zero[threadIdx.x] = 0;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        __threadfence();
-        if (atomicAdd(n_valid + 1, 1) == (int)gridDim.x - 1) {
-            n_valid[0] = 0;
-            n_valid[1] = 0;
-        }
+    if (blockIdx.x == 0) {
+        if (threadIdx.x == 0) *n_valid = 0;
+        if (zero && (int)threadIdx.x < n_zero) zero[threadIdx.x] = 0;
     }
 }
 
@@ -529,11 +521,11 @@ __global__ void k_clamp_counts(int *counters, long long cap, long long ccap) {
 
 // corrections of one contact (VFResolveTest + VFResolveNew, P/CCD.cpp:1996-2090)
 // added to the per-point fixed-point sums
-__global__ void __launch_bounds__(128) k_contact_deltas(int *counters, const int4 *ids,
+__global__ void __launch_bounds__(128) k_contact_deltas(const int *counters, const int4 *ids,
                                                         const float4 *__restrict__ x,
                                                         const float4 *__restrict__ p, float th,
                                                         int mass_weighted, long long *acc,
-                                                        int *acnt, int *touched) {
+                                                        int *acnt) {
     // launched as a programmatic dependent of the sweep's last color phase:
     // nothing is read before that phase has completed; the apply kernel may
     // then launch while the corrections are summed
@@ -589,23 +581,20 @@ __global__ void __launch_bounds__(128) k_contact_deltas(int *counters, const int
         add_fixed(acc, id.y, d1.x, d1.y, d1.z);
         add_fixed(acc, id.z, d2.x, d2.y, d2.z);
         add_fixed(acc, id.w, d3.x, d3.y, d3.z);
-        touch_point(acnt, id.x, touched, counters);
-        touch_point(acnt, id.y, touched, counters);
-        touch_point(acnt, id.z, touched, counters);
-        touch_point(acnt, id.w, touched, counters);
+        atomicAdd(acnt + id.x, 1);
+        atomicAdd(acnt + id.y, 1);
+        atomicAdd(acnt + id.z, 1);
+        atomicAdd(acnt + id.w, 1);
     }
 }
 
-// every point with a correction (the touched list): p += sum * 2^-32 /
-// count; sums and counts cleared.  The last block to finish empties the
-// list (every block has read its length by then).
-__global__ void __launch_bounds__(256) k_apply_touched(int *counters, const int *touched,
-                                                       long long *acc, int *acnt, float4 *p) {
+// every point with a correction: p += sum * 2^-32 / count; sums cleared
+__global__ void __launch_bounds__(256) k_apply_deltas(int n, long long *acc, int *acnt,
+                                                      float4 *p) {
     asm volatile("griddepcontrol.wait;" ::: "memory");  // every sum is complete
-    const int n = counters[kTouched];
-    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
-        const int pt = touched[k];
+    for (int pt = blockIdx.x * blockDim.x + threadIdx.x; pt < n; pt += gridDim.x * blockDim.x) {
         int cnt = acnt[pt];
+        if (cnt <= 0) continue;
         acnt[pt] = 0;
         long long sx = acc[3 * (long long)pt], sy = acc[3 * (long long)pt + 1],
                   sz = acc[3 * (long long)pt + 2];
@@ -618,14 +607,6 @@ __global__ void __launch_bounds__(256) k_apply_touched(int *counters, const int 
         P.y = P.y + (float)((double)sy * (1.0 / 4294967296.0) / dc);
         P.z = P.z + (float)((double)sz * (1.0 / 4294967296.0) / dc);
         p[pt] = P;
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        __threadfence();
-        if (atomicAdd(counters + kApplyDone, 1) == (int)gridDim.x - 1) {
-            counters[kTouched] = 0;
-            counters[kApplyDone] = 0;
-        }
     }
 }
 
@@ -659,7 +640,7 @@ int round8(int b) { return (b + 7) / 8 * 8; }
 
 
 constexpr int kPersistentBlocks = 8 * kNumSMs;
-// the response's two kernels: grid-stride over the contacts / touched points
+// the response's contact kernel: grid-stride over the contacts
 constexpr int kResponseBlocks = 2 * kNumSMs;
 // bucket reset: grid-stride over the previous update's keys
 constexpr int kResetBlocks = 2 * kNumSMs;
@@ -675,7 +656,7 @@ static int shs_update_on(pbd_shs *h, cudaStream_t s, const float4 *psrc, int *ze
     GridParams g = params_of(h);
     if (o->nt == 0) return PBD_OK;
     // clear the ranges of the buckets the previous update filled
-    k_reset_buckets<<<kResetBlocks, 256, 0, s>>>(h->skey, h->n_valid.p, g.nb, h->btab.p, o->nt,
+    k_reset_buckets<<<kResetBlocks, 256, 0, s>>>(h->skey, o->nt, g.nb, h->btab.p, h->n_valid.p,
                                                  zero, n_zero);
     k_tri_cells<<<grid_for(o->nt, 256), 256, 0, s>>>(o->nt, g, 0.0f, h->inst_cell.p,
                                                      h->n_inst_cell, o->tri.p, o->x.p, psrc,
@@ -706,7 +687,6 @@ static int colli_alloc(pbd_colli *c) {
     PBD_TRY(c->cw.alloc(H));
     PBD_TRY(c->acc.alloc(3 * (size_t)o->n));
     PBD_TRY(c->acnt.alloc(o->n));
-    PBD_TRY(c->touched.alloc(o->n));
     PBD_CUDA(cudaMemsetAsync(c->acc.p, 0, sizeof(long long) * 3 * (size_t)o->n, o->stream));
     PBD_CUDA(cudaMemsetAsync(c->acnt.p, 0, sizeof(int) * (size_t)o->n, o->stream));
     PBD_CUDA(cudaMemsetAsync(c->counters.p, 0, sizeof(int) * 16, o->stream));
@@ -824,20 +804,19 @@ int ccd_resolve(pbd_colli *c, int passes) {
     cudaLaunchConfig_t cd = {}, ca = {};
     cd.gridDim = dim3(kResponseBlocks);
     cd.blockDim = dim3(128);
-    ca.gridDim = dim3(kResponseBlocks);
+    ca.gridDim = dim3(grid_for(o->n, 256));
     ca.blockDim = dim3(256);
     cd.stream = ca.stream = s;
     cd.attrs = ca.attrs = at;
     cd.numAttrs = ca.numAttrs = o->pdl ? 1 : 0;
     for (int k = 0; k < passes; ++k) {
-        PBD_CUDA(cudaLaunchKernelEx(&cd, k_contact_deltas, c->counters.p,
+        PBD_CUDA(cudaLaunchKernelEx(&cd, k_contact_deltas, (const int *)c->counters.p,
                                     (const int4 *)c->cids.p, (const float4 *)o->x.p,
                                     (const float4 *)o->p.p, c->thickness,
                                     (int)(c->response == PBD_RESPONSE_MASS_WEIGHTED), c->acc.p,
-                                    c->acnt.p, c->touched.p));
+                                    c->acnt.p));
         if (c->ee_on) PBD_TRY(ee_deltas_launch(c));
-        PBD_CUDA(cudaLaunchKernelEx(&ca, k_apply_touched, c->counters.p,
-                                    (const int *)c->touched.p, c->acc.p, c->acnt.p, o->p.p));
+        PBD_CUDA(cudaLaunchKernelEx(&ca, k_apply_deltas, o->n, c->acc.p, c->acnt.p, o->p.p));
     }
     return PBD_OK;
 }
@@ -859,11 +838,13 @@ static int shs_alloc(pbd_shs *h) {
     PBD_TRY(h->id.alloc(nt));
     PBD_TRY(h->id_alt.alloc(nt));
     PBD_TRY(h->etab.alloc(3 * nt));
-    PBD_TRY(h->n_valid.alloc(2));
+    PBD_TRY(h->n_valid.alloc(1));
     PBD_TRY(h->btab.alloc(2 * ((size_t)h->n_buckets + 1)));
     PBD_TRY(radix_reserve(h->scr, (long long)nt, round8(h->key_bits)));
     PBD_CUDA(cudaMemsetAsync(h->btab.p, 0, sizeof(float4) * 2 * (h->n_buckets + 1), o->stream));
-    PBD_CUDA(cudaMemsetAsync(h->n_valid.p, 0, 2 * sizeof(int), o->stream));
+    PBD_CUDA(cudaMemsetAsync(h->n_valid.p, 0, sizeof(int), o->stream));
+    // no bucket filled yet: the first reset reads keys beyond every bucket
+    PBD_CUDA(cudaMemsetAsync(h->key.p, 0xff, sizeof(uint32_t) * nt, o->stream));
     h->skey = h->key.p;
     h->sid = h->id.p;
     return PBD_OK;

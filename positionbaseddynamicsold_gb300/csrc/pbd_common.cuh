@@ -116,8 +116,6 @@ struct HBuf {
     }
 };
 
-// response bookkeeping in pbd_colli::counters
-constexpr int kTouched = 5, kApplyDone = 6;
 
 // ---- stable LSD radix sort (8-bit digits) of (key, int value) pairs --------
 // Sorts n elements (n read from d_count when non-null, capped by n_cap),
@@ -280,9 +278,7 @@ struct pbd_colli {
     pbd::DBuf<int2> pairs;      // AABB-overlapping (point, triangle)
     pbd::DBuf<int2> cand;
     pbd::DBuf<int> counters;    // [0] candidates, [1] contacts, [2] overflow flags, [3] hard
-                                // candidates (cubic roots needed), [4] AABB pairs,
-                                // [5] touched points of the response pass, [6] apply
-                                // blocks done
+                                // candidates (cubic roots needed), [4] AABB pairs
     pbd::DBuf<int> hard;        // candidate indices that need the cubic's roots
     int sized_n = -1;           // point count the per-point buffers were sized for
     // contacts, in the order the narrow phase found them
@@ -294,9 +290,6 @@ struct pbd_colli {
     // between passes)
     pbd::DBuf<long long> acc;
     pbd::DBuf<int> acnt;
-    // points whose count went from 0 to 1 in the current response pass
-    // (counters[kTouched] of them); the apply kernel visits only these
-    pbd::DBuf<int> touched;
     // edge-edge CCD (off unless enabled): the object's unique edges (built
     // on first use; -1 = not yet), their grown swept boxes, the edge-cell
     // entries of the edge hash and their sort buffers, the edge pairs,

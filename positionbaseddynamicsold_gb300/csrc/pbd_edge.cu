@@ -462,7 +462,7 @@ __global__ void __launch_bounds__(128) k_ee_deltas(long long hcap, const int4 *_
                                                    const float4 *__restrict__ m0,
                                                    const float4 *__restrict__ p, float th,
                                                    long long *acc, int *acnt,
-                                                   int *touched, int *counters) {
+                                                   const int *counters) {
     long long n = counters[kHits];
     if (n > hcap) n = hcap;
     for (long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x; c < n;
@@ -477,10 +477,10 @@ __global__ void __launch_bounds__(128) k_ee_deltas(long long hcap, const int4 *_
         add_fixed(acc, id.y, dl[1].x, dl[1].y, dl[1].z);
         add_fixed(acc, id.z, dl[2].x, dl[2].y, dl[2].z);
         add_fixed(acc, id.w, dl[3].x, dl[3].y, dl[3].z);
-        touch_point(acnt, id.x, touched, counters);
-        touch_point(acnt, id.y, touched, counters);
-        touch_point(acnt, id.z, touched, counters);
-        touch_point(acnt, id.w, touched, counters);
+        atomicAdd(acnt + id.x, 1);
+        atomicAdd(acnt + id.y, 1);
+        atomicAdd(acnt + id.z, 1);
+        atomicAdd(acnt + id.w, 1);
     }
 }
 
@@ -610,7 +610,7 @@ int ee_deltas_launch(pbd_colli *c) {
     if (c->ee_n <= 0) return PBD_OK;
     k_ee_deltas<<<kEEBlocks, 128, 0, o->stream>>>(c->contact_cap, c->ee_ids.p, c->ee_m0.p, o->p.p,
                                                   c->thickness, c->acc.p, c->acnt.p,
-                                                  c->touched.p, c->counters.p);
+                                                  c->counters.p);
     PBD_LAUNCH();
     return PBD_OK;
 }
