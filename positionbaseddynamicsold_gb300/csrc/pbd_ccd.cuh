@@ -138,16 +138,30 @@ __device__ __forceinline__ bool vf_eval_at(const v3 *X, const v3 *P, float th, d
     res.w[1] = w.x;
     res.w[2] = w.y;
     res.w[3] = w.z;
+    // the plane test first: the inside test only matters when it passes
+    if (!(fabs(dist) - (double)(2.0f * th) < -1e-6)) return false;
     float e1 = dist3(c1, c2), e2 = dist3(c1, c3), e3 = dist3(c2, c3);
-    float eps = (float)((double)th / ((double)(e1 + e2 + e3) / 3.0));
-    bool in = (w.x <= (1 + eps)) && (w.x >= (-eps)) && (w.y <= (1 + eps)) && (w.y >= (-eps)) &&
-              (w.z <= (1 + eps)) && (w.z >= (-eps));
-    return (fabs(dist) - (double)(2.0f * th) < -1e-6) && in;
+    float es = e1 + e2 + e3;
+    // epsilon = thickness / (edge sum / 3.0), a double division rounded to
+    // float in the reference.  A float quotient is within a few ulps of it
+    // (relative error < 1e-6), so the six inside comparisons come out the
+    // same whenever every weight is more than 2^-20 max(1, epsilon) from its
+    // bound; otherwise the FP64 division (a long instruction sequence on
+    // this GPU) decides.
+    float ea = __fdividef(3.0f * th, es);
+    const float m = 9.5367431640625e-07f * fmaxf(1.f, ea);  // 2^-20 max(1, eps)
+    bool clear = fabsf(w.x - (1 + ea)) > m && fabsf(w.x + ea) > m &&
+                 fabsf(w.y - (1 + ea)) > m && fabsf(w.y + ea) > m &&
+                 fabsf(w.z - (1 + ea)) > m && fabsf(w.z + ea) > m && isfinite(ea);
+    float eps = clear ? ea : (float)((double)th / ((double)es / 3.0));
+    return (w.x <= (1 + eps)) && (w.x >= (-eps)) && (w.y <= (1 + eps)) && (w.y >= (-eps)) &&
+           (w.z <= (1 + eps)) && (w.z >= (-eps));
 }
 
 // true when a3 t^3 + a2 t^2 + a1 t + a0 has no root on [-d, 1+d], d = 1e-3:
 // its Bernstein coefficients on that interval share one strict sign
-__device__ __forceinline__ bool no_root_near_unit(double a0, double a1, double a2, double a3) {
+__device__ __forceinline__ bool no_root_near_unit_f64(double a0, double a1, double a2,
+                                                      double a3) {
     const double u = -1e-3, L = 1.002;
     double c0 = ((a3 * u + a2) * u + a1) * u + a0;
     double c1 = L * ((3.0 * a3 * u + 2.0 * a2) * u + a1);
@@ -163,6 +177,29 @@ __device__ __forceinline__ bool no_root_near_unit(double a0, double a1, double a
     bool pos = b0 > tol && b1 > tol && b2 > tol && b3 > tol;
     bool neg = b0 < -tol && b1 < -tol && b2 < -tol && b3 < -tol;
     return pos || neg;
+}
+
+// The same decision, computed in float first.  The coefficients are float
+// values (the triple products are float); the float Bernstein coefficients
+// are within ~10 ulps of sum |a| of the double ones, so when all four
+// clear 1e-5 sum |a| with one sign, the double ones clear the 1e-9 sum |a|
+// tolerance with that sign too.  Otherwise the double evaluation decides.
+__device__ __forceinline__ bool no_root_near_unit(double a0, double a1, double a2, double a3) {
+    const float f0 = (float)a0, f1 = (float)a1, f2 = (float)a2, f3 = (float)a3;
+    const float u = -1e-3f, L = 1.002f;
+    float c0 = ((f3 * u + f2) * u + f1) * u + f0;
+    float c1 = L * ((3.0f * f3 * u + 2.0f * f2) * u + f1);
+    float c2 = L * L * (3.0f * f3 * u + f2);
+    float c3 = L * L * L * f3;
+    const float third = 1.0f / 3.0f;
+    float b0 = c0, b1 = c0 + c1 * third, b2 = c0 + 2.0f * c1 * third + c2 * third,
+          b3 = c0 + c1 + c2 + c3;
+    float tol = 1e-5f * (fabsf(f0) + fabsf(f1) + fabsf(f2) + fabsf(f3));
+    if (tol > 0.f && isfinite(tol)) {
+        if (b0 > tol && b1 > tol && b2 > tol && b3 > tol) return true;
+        if (b0 < -tol && b1 < -tol && b2 < -tol && b3 < -tol) return true;
+    }
+    return no_root_near_unit_f64(a0, a1, a2, a3);
 }
 
 // ExtendedVFTest (P/CCD.cpp:1733-1808); X/P = start/predicted positions of
