@@ -785,6 +785,22 @@ int ccd_detect_fork(pbd_colli *c, bool *forked) {
     return PBD_OK;
 }
 
+int ccd_snapshot(pbd_colli *c, const float4 *src) {
+    pbd_object *o = c->obj;
+    k_copy_points<<<grid_for(o->n, 256), 256, 0, o->stream>>>(o->n, src, c->psnap.p);
+    PBD_LAUNCH();
+    return PBD_OK;
+}
+
+int ccd_detect_snapshot(pbd_colli *c) {
+    PBD_TRY(ccd_prepare(c));
+    PBD_TRY(ccd_detect_on(c, c->obj->stream, c->psnap.p));
+    if (c->ee_on) PBD_TRY(ee_detect(c));
+    return PBD_OK;
+}
+
+int ccd_prepare_all(pbd_colli *c) { return ccd_prepare(c); }
+
 int ccd_join(pbd_colli *c) {
     PBD_CUDA(cudaStreamWaitEvent(c->obj->stream, c->ev_join, 0));
     return PBD_OK;

@@ -444,6 +444,13 @@ int ccd_detect(pbd_colli *c);
 int ccd_detect_fork(pbd_colli *c, bool *forked);
 // the object's stream waits for a forked detection
 int ccd_join(pbd_colli *c);
+// sizes the collision solver's buffers for its target (outside captures)
+int ccd_prepare_all(pbd_colli *c);
+// copies positions src into the detection snapshot (c->psnap) on the
+// object's stream; ccd_detect_snapshot detects from that snapshot (the
+// vertex-face pass; edge-edge CCD, when on, reads the object's positions)
+int ccd_snapshot(pbd_colli *c, const float4 *src);
+int ccd_detect_snapshot(pbd_colli *c);
 int ccd_resolve(pbd_colli *c, int passes);
 // priority of the color-phase launches (the greatest the device offers),
 // so pending sweep blocks are scheduled before an overlapped detection's

@@ -11,7 +11,9 @@
 //
 // A substep is: advect; [warm start]; sweeps in chunks of `chunk` until the
 // residual is at or below the target or `max_sweeps` would be exceeded;
-// [a last CCD detection + response]; record the correction; integrate.
+// [a last CCD detection + response]; record the correction; integrate.  A
+// chunk's detection reads the positions its chunk starts from, the first
+// one the advected positions (taken before the warm start).
 // Sweep i uses the reference's exponent 1/(i+1).  With collisions each chunk
 // starts with a CCD detection (the reference detects every 10th iteration,
 // P/PBD_cuda.cu:1139-1145: chunk = 10 keeps that cadence) and every sweep is
@@ -114,10 +116,15 @@ static int loop_ctl(pbd_solver *s, int mode, cudaGraphConditionalHandle h, const
     return PBD_OK;
 }
 
-// one chunk of sweeps followed by the residual check
+// one chunk of sweeps followed by the residual check.  With collisions the
+// chunk starts with a detection from the snapshot of the positions the
+// chunk starts from (the prologue takes the first one from the advected
+// positions, before any warm start; each chunk takes the next one), so a
+// warm-started and a plain solve of one state detect the same contacts
+// first.
 static int record_chunk(pbd_solver *s, pbd_colli *c, cudaGraphConditionalHandle h,
                         const ResArgs &a) {
-    if (c) PBD_TRY(ccd_detect(c));
+    if (c) PBD_TRY(ccd_detect_snapshot(c));
     for (int j = 0; j < a.chunk; ++j) {
         PBD_TRY(launch_sweep_dev(s, &s->loop.p->expk[j], c == nullptr));
         if (c) {
@@ -125,7 +132,9 @@ static int record_chunk(pbd_solver *s, pbd_colli *c, cudaGraphConditionalHandle 
             PBD_TRY(launch_obstacles(s));
         }
     }
-    return loop_ctl(s, kCheck, h, a);
+    PBD_TRY(loop_ctl(s, kCheck, h, a));
+    if (c) PBD_TRY(ccd_snapshot(c, s->obj->p.p));
+    return PBD_OK;
 }
 
 // warm start of the advected positions o->p0 (= o->p): prediction, guard,
@@ -146,10 +155,11 @@ static int warm_start(pbd_solver *s, cudaGraphConditionalHandle h, const ResArgs
 }
 
 // advect, warm start or plain start; the loop follows (graph or host)
-static int record_prologue(pbd_solver *s, float dt, cudaGraphConditionalHandle h,
+static int record_prologue(pbd_solver *s, float dt, pbd_colli *c, cudaGraphConditionalHandle h,
                            const ResArgs &a) {
     pbd_object *o = s->obj;
     PBD_TRY(launch_advect_p0(o, dt));
+    if (c) PBD_TRY(ccd_snapshot(c, o->p.p));
     if (s->ws) return warm_start(s, h, a);
     return loop_ctl(s, kStartPlain, h, a);
 }
@@ -180,7 +190,7 @@ static int eager_loop(pbd_solver *s, pbd_colli *c, const ResArgs &a) {
 }
 
 static int eager_substep(pbd_solver *s, float dt, pbd_colli *c, const ResArgs &a) {
-    PBD_TRY(record_prologue(s, dt, 0, a));
+    PBD_TRY(record_prologue(s, dt, c, 0, a));
     PBD_TRY(eager_loop(s, c, a));
     return record_epilogue(s, dt, c);
 }
@@ -204,7 +214,7 @@ static int capture_substeps(pbd_solver *s, float dt, int substeps, pbd_colli *c,
         PBD_CUDA(cudaStreamGetCaptureInfo(st, &cs, nullptr, &g, nullptr, nullptr, nullptr));
         cudaGraphConditionalHandle h;
         PBD_CUDA(cudaGraphConditionalHandleCreate(&h, g, 0, 0));
-        PBD_TRY(record_prologue(s, dt, h, a));
+        PBD_TRY(record_prologue(s, dt, c, h, a));
         const cudaGraphNode_t *deps = nullptr;
         size_t ndeps = 0;
         PBD_CUDA(cudaStreamGetCaptureInfo(st, &cs, nullptr, &g, &deps, nullptr, &ndeps));
@@ -284,6 +294,7 @@ static int ensure_ready(pbd_solver *s, pbd_colli *c) {
         PBD_CUDA(cudaMemsetAsync(s->loop.p, 0, sizeof(LoopState), o->stream));
     }
     PBD_TRY(build_feature_stencil(o));  // p0 / dprev buffers and stencils
+    if (c) PBD_TRY(ccd_prepare_all(c));   // the detection snapshot among them
     if (s->ws) PBD_TRY(ws_prepare(s->ws, o));
     PBD_TRY(prepare_gs_path(s));
     return PBD_OK;
@@ -360,6 +371,7 @@ int pbd_solver_project_to_residual(pbd_solver *s, pbd_colli *c, double target, i
     ResArgs a{target, max_sweeps, chunk, s->min_sweeps};
     PBD_CUDA(cudaMemcpyAsync(o->p0.p, o->p.p, sizeof(float4) * o->n, cudaMemcpyDeviceToDevice,
                              o->stream));
+    if (c) PBD_TRY(ccd_snapshot(c, o->p.p));
     PBD_TRY(loop_ctl(s, kStartPlain, 0, a));
     for (;;) {
         int cont = 0;
@@ -397,6 +409,7 @@ int pbd_solver_train_substep(pbd_solver *s, pbd_warmstart *w, float dt, pbd_coll
     ResArgs a{target, max_sweeps, chunk, s->min_sweeps};
     // the plain solve of the advected state gives the target
     PBD_TRY(launch_advect_p0(o, dt));
+    if (c) PBD_TRY(ccd_snapshot(c, o->p.p));
     PBD_TRY(ws_record(w, o));
     PBD_TRY(loop_ctl(s, kStartPlain, 0, a));
     PBD_TRY(eager_loop(s, c, a));
@@ -406,6 +419,7 @@ int pbd_solver_train_substep(pbd_solver *s, pbd_warmstart *w, float dt, pbd_coll
         // the trajectory continues from the warm-started solve of the same state
         PBD_CUDA(cudaMemcpyAsync(o->p.p, o->p0.p, sizeof(float4) * o->n, cudaMemcpyDeviceToDevice,
                                  o->stream));
+        if (c) PBD_TRY(ccd_snapshot(c, o->p.p));
         pbd_warmstart *keep = s->ws;
         s->ws = w;
         int r = warm_start(s, 0, a);

@@ -29,11 +29,14 @@ import time
 import numpy as np
 
 from . import scenes
-from .pbd import PBDObject, SolverPBD, WarmStart
+from .pbd import (RESPONSE_MASS_WEIGHTED, CollisionSolver, PBDObject, SolverPBD,
+                  SpatialHashSystem, WarmStart)
 
 DT = 1.0 / 600
 PKG = os.path.dirname(os.path.abspath(__file__))
 DEFAULT_WEIGHTS = os.path.join(PKG, "data", "warmstart.npz")
+# trained on the contact families (folds on the ground, drapes over a sphere)
+CONTACT_WEIGHTS = os.path.join(PKG, "data", "warmstart_contact.npz")
 
 N_IN, N_HID, N_OUT = 16, 64, 3
 N_PARAMS = N_HID * N_IN + N_HID * N_HID + N_HID + N_OUT * N_HID + N_OUT
@@ -205,6 +208,223 @@ def evaluate_same_state(params, scales, n_traj=8, substeps=40, target=1e-3, max_
     return out
 
 
+# ---- contact families: cloths on the ground and over a sphere ------------
+
+G0 = np.array([0.0, -9.8, 0.0], np.float32)
+
+
+def contact_scene(seed, family):
+    """one scene of a contact family, with its hash table size.
+    fold: a square cloth of side U{96..256} points at fold1024's spacing
+    (4 m / 1024), rotated, tilted and dropped onto the ground plane y = 0
+    so it folds onto itself; drape: a cloth of side U{64..192} over 2 m
+    whose free fall is fast-forwarded to just above an icosphere (level 4,
+    r = 0.4)."""
+    rng = np.random.default_rng(seed)
+    if family == "fold":
+        res = int(rng.integers(96, 257))
+        sc = scenes.folding_cloth(res=res, seed=seed, size=res * 4.0 / 1024)
+        return sc, 18
+    if family == "drape":
+        res = int(rng.integers(64, 193))
+        sc = scenes.drape_over_sphere(res=res, seed=seed, sphere_level=4, start="contact")
+        return sc, 18
+    raise ValueError("family must be 'fold' or 'drape'")
+
+
+def contact_solver(sc, log2):
+    """object, solver, hash and collision solver as the benchmark sets them up
+    (mass-weighted response, thickness and cell from the scene)"""
+    obj = PBDObject(sc, damping=1.0, gravity=G0)
+    obj.prepare()
+    s = SolverPBD(obj)
+    shs = SpatialHashSystem(obj, cell_size=sc["colli"]["cell"], log2_table=log2)
+    shs.init()
+    cs = CollisionSolver(obj, shs, thickness=sc["colli"]["thickness"], iterations=1,
+                         response=RESPONSE_MASS_WEIGHTED)
+    n = obj.n_points
+    cs.set_capacity(max(1 << 22, 64 * n), max(1 << 20, 4 * n))
+    if "ground" in sc["colli"]:
+        s.set_ground(True, sc["colli"]["ground"])
+    obj._keep = shs
+    return obj, s, cs
+
+
+def fit_contact_scales(seed=0, n_traj=6, families=("fold", "drape"), preroll=90, lead=3,
+                       substeps=6, sweeps=60, chunk=10):
+    """input / output scales (as fit_scales) from plain solves of contact
+    states of the families"""
+    ws = WarmStart()
+    rows = []
+    for k in range(n_traj):
+        fam = families[k % len(families)]
+        sc, log2 = contact_scene(60_000 + seed * 100_003 + k, fam)
+        obj, s, cs = contact_solver(sc, log2)
+        s.step(DT, preroll, 15, cs, True)
+        s.step_to_residual(DT, lead, 0.0, sweeps, chunk, cs, True)
+        for _ in range(substeps):
+            s.advect(DT)
+            rows.append(ws.features(obj))
+            s.project_to_residual(0.0, sweeps, chunk, cs)
+            s.integration(DT)
+        cs.close()
+        s.close()
+        obj.close()
+    X = np.concatenate(rows).astype(np.float64)
+
+    def inv_std(cols):
+        sd = float(np.sqrt(np.mean(X[:, cols] ** 2)))
+        return 1.0 / sd if sd > 1e-12 else 1.0
+
+    sc_ = np.ones(17, np.float32)
+    sc_[0:6] = inv_std(slice(0, 6))
+    sd_corr = 1.0 / inv_std(slice(6, 9))
+    sc_[6:9] = 1.0 / sd_corr
+    sc_[11:15] = inv_std(slice(11, 15))
+    sc_[16] = sd_corr
+    return sc_
+
+
+def train_contact(ws, n_traj, families=("fold", "drape"), preroll=(30, 150), substeps=30,
+                  sweeps=60, chunk=10, lr=1e-3, seed=0, on_policy=False, log=print,
+                  traj_offset=20_000):
+    """Training on contact states: each trajectory runs a random number of
+    plain fixed-15-iteration substeps (in `preroll`) to reach contacts, then
+    `substeps` training substeps: the advected state is solved by `sweeps`
+    plain sweeps (chunks of `chunk`, a detection per chunk, the response
+    after every sweep) and the network takes one Adam step on its points'
+    (features, correction) pairs."""
+    hist = []
+    t0 = time.time()
+    for k in range(n_traj):
+        fam = families[k % len(families)]
+        sd = traj_offset + seed * 100_003 + k
+        sc, log2 = contact_scene(sd, fam)
+        obj, s, cs = contact_solver(sc, log2)
+        rng = np.random.default_rng(sd)
+        s.step(DT, int(rng.integers(preroll[0], preroll[1] + 1)), 15, cs, True)
+        losses = []
+        for j in range(substeps):
+            losses.append(s.train_substep(ws, DT, 0.0, sweeps, chunk, lr, on_policy, colli=cs,
+                                          want_loss=(j % 10 == 9)))
+        ls = [x for x in losses if x is not None]
+        hist.append(float(np.mean(ls)) if ls else float("nan"))
+        if log and (k % 20 == 19 or k == n_traj - 1):
+            log(f"contact trajectory {k + 1}/{n_traj}: loss {np.mean(hist[-20:]):.4e}  "
+                f"{time.time() - t0:.0f}s")
+        cs.close()
+        s.close()
+        obj.close()
+    return hist
+
+
+def timed_solve(s, obj, cs, state, dprev, target, max_sweeps, chunk):
+    """one substep solved to `target` from `state` (positions, velocities)
+    with the solver's current warm start, through the CUDA graph of
+    pbd_solver_step_to_residual; the graph is built by a first untimed run
+    from the same state.  Returns (device ms, solve stats)."""
+    import torch
+    stream = torch.cuda.ExternalStream(obj.stream())
+    out = None
+    for rep in range(2):
+        obj.set_state(*state)
+        obj.set_correction(dprev)
+        obj.sync()
+        s.solve_stats(reset=True)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        s.step_to_residual(DT, 1, target, max_sweeps, chunk, cs, True)
+        e1.record(stream)
+        e1.synchronize()
+        out = (e0.elapsed_time(e1), s.solve_stats(reset=True))
+    return out
+
+
+def residual_curve(s, obj, cs, state, dprev, ks, chunk=10):
+    """stretch residual after k plain sweeps (chunks of `chunk`, a detection
+    per chunk, the response after every sweep) of one advected state, for
+    every k in ks"""
+    out = []
+    for k in ks:
+        obj.set_state(*state)
+        obj.set_correction(dprev)
+        s.advect(DT)
+        sw, r = s.project_to_residual(0.0, int(k), min(chunk, max(1, int(k))), cs)
+        out.append({"sweeps": int(sw), "stretch_residual": float(r)})
+    return out
+
+
+def evaluate_contact_same_state(params, scales, sc, log2, preroll, substeps=8, sweeps=60,
+                                chunk=10, lead=5, curve_ks=(0, 5, 10, 15, 30, 60, 120, 200)):
+    """The warm start against the plain sweeps on a contact workload, from
+    identical states along a plain trajectory: after `preroll` fixed
+    15-iteration substeps and `lead` plain solved substeps (so the previous
+    correction exists), each of `substeps` states is solved (a) plain with
+    `sweeps` sweeps, whose final stretch residual r_K becomes the target,
+    and (b) warm-started until the residual is at or below r_K (at most
+    `sweeps`).  Both solves detect their first contacts from the same
+    advected positions.  Reported: sweeps and device time of each solve
+    (CUDA graph of pbd_solver_step_to_residual, graph built beforehand),
+    the guard's rejections, and the plain residual curve of the first
+    state."""
+    obj, s, cs = contact_solver(sc, log2)
+    ws = WarmStart(params, scales)
+    s.step(DT, preroll, 15, cs, True)
+    s.step_to_residual(DT, lead, 0.0, sweeps, chunk, cs, True)
+    rows = []
+    curve = None
+    for j in range(substeps):
+        state = obj.get_state()
+        dprev = obj.correction()
+        if curve is None:
+            curve = residual_curve(s, obj, cs, state, dprev, curve_ks, chunk)
+        s.set_warmstart(None)
+        tp, stp = timed_solve(s, obj, cs, state, dprev, 0.0, sweeps, chunk)
+        rk = stp["last_residual"]
+        s.set_warmstart(ws)
+        tl, stl = timed_solve(s, obj, cs, state, dprev, rk * (1.0 + 1e-9), sweeps, chunk)
+        # the same state started from the previous substep's correction
+        # (p0 + dprev, kept only if it lowers the residual): the warm start
+        # without a network, for comparison (sweeps only)
+        s.set_warmstart(None)
+        obj.set_state(*state)
+        obj.set_correction(dprev)
+        s.advect(DT)
+        p0 = obj.predicted()
+        r0 = obj.residual_stretch()
+        obj.set_predicted(p0 + dprev)
+        if obj.residual_stretch() > r0:
+            obj.set_predicted(p0)
+        swd, rd = s.project_to_residual(rk * (1.0 + 1e-9), sweeps, chunk, cs)
+        rows.append({"plain_sweeps": stp["sweeps"], "plain_ms": tp, "target": rk,
+                     "learned_sweeps": stl["sweeps"], "learned_ms": tl,
+                     "learned_reached": int(stl["reached"]), "reverted": int(stl["reverts"]),
+                     "r_advected": stl["last_r0"], "r_predicted": stl["last_r1"],
+                     "previous_correction_sweeps": int(swd),
+                     "previous_correction_reached": int(rd <= rk * (1.0 + 1e-9))})
+        # the trajectory goes on with the plain solve
+        s.set_warmstart(None)
+        obj.set_state(*state)
+        obj.set_correction(dprev)
+        s.step_to_residual(DT, 1, 0.0, sweeps, chunk, cs, True)
+    s.set_warmstart(None)
+    cs.close()
+    s.close()
+    obj.close()
+    tp = sum(r["plain_ms"] for r in rows)
+    tl = sum(r["learned_ms"] for r in rows)
+    return {"substeps": len(rows), "sweeps_plain": sweeps, "chunk": chunk,
+            "plain_ms": tp, "learned_ms": tl, "speedup": tp / tl if tl else None,
+            "learned_reached": sum(r["learned_reached"] for r in rows),
+            "reverted": sum(r["reverted"] for r in rows),
+            "plain_sweeps": sum(r["plain_sweeps"] for r in rows),
+            "learned_sweeps": sum(r["learned_sweeps"] for r in rows),
+            "previous_correction_sweeps": sum(r["previous_correction_sweeps"] for r in rows),
+            "previous_correction_reached": sum(r["previous_correction_reached"] for r in rows),
+            "residual_curve_first_state": curve, "per_substep": rows}
+
+
 def save(path, params, scales, meta):
     os.makedirs(os.path.dirname(path), exist_ok=True)
     np.savez(path, params=np.asarray(params, np.float32), scales=np.asarray(scales, np.float32),
@@ -233,9 +453,22 @@ def main():
     ap.add_argument("--on-policy-trajectories", type=int, default=0,
                     help="then continue training on trajectories of the warm-started solver")
     ap.add_argument("--init", default=None, help="start from these weights (and scales)")
+    ap.add_argument("--contact-trajectories", type=int, default=0,
+                    help="train on contact states (folds on the ground, drapes over a sphere) "
+                         "instead of hanging cloths")
+    ap.add_argument("--contact-on-policy", type=int, default=0,
+                    help="then contact trajectories that follow the warm-started solve")
+    ap.add_argument("--families", default="fold,drape",
+                    help="contact families to train on (fold, drape)")
+    ap.add_argument("--contact-substeps", type=int, default=30)
+    ap.add_argument("--contact-sweeps", type=int, default=60)
+    ap.add_argument("--eval-only", default=None,
+                    help="evaluate these weights on the contact workloads and exit")
     ap.add_argument("--out", default=DEFAULT_WEIGHTS)
     a = ap.parse_args()
     t0 = time.time()
+    if a.contact_trajectories or a.contact_on_policy or a.eval_only:
+        return main_contact(a, t0)
     params = None
     if a.init:
         params, scales, _ = load_params(a.init)
@@ -265,6 +498,62 @@ def main():
     meta["scales"] = [float(x) for x in scales]
     save(a.out, params, scales, meta)
     print(json.dumps(meta, indent=1))
+
+
+def main_contact(a, t0):
+    """training on the contact families, evaluation on the fold1024 and
+    drape256 workloads (same-state, targets r_plain(K))"""
+    if a.eval_only:
+        params, scales, _ = load_params(a.eval_only)
+        print(json.dumps(evaluate_workloads(params, scales, a.contact_sweeps), indent=1))
+        return
+    fams = tuple(f for f in a.families.split(",") if f)
+    if a.init:
+        params, scales, _ = load_params(a.init)
+    else:
+        scales = fit_contact_scales(a.seed, families=fams)
+        params = init_params(a.seed)
+    ws = WarmStart(params, scales)
+    hist = []
+    if a.contact_trajectories:
+        hist += train_contact(ws, a.contact_trajectories, families=fams,
+                              substeps=a.contact_substeps, sweeps=a.contact_sweeps, lr=a.lr,
+                              seed=a.seed)
+    if a.contact_on_policy:
+        hist += train_contact(ws, a.contact_on_policy, families=fams, substeps=a.contact_substeps,
+                              sweeps=a.contact_sweeps, lr=a.lr, seed=a.seed, on_policy=True,
+                              traj_offset=420_000)
+    params = ws.params()
+    meta = {k: getattr(a, k) for k in ("contact_trajectories", "contact_on_policy",
+                                       "contact_substeps", "contact_sweeps", "lr", "seed",
+                                       "init")}
+    meta["families"] = list(fams)
+    meta["train_seconds"] = time.time() - t0
+    meta["final_loss"] = float(np.mean(hist[-20:])) if hist else None
+    meta["scales"] = [float(x) for x in scales]
+    meta["eval_contact"] = evaluate_workloads(params, scales, a.contact_sweeps)
+    save(a.out, params, scales, meta)
+    print(json.dumps(meta, indent=1))
+
+
+def workload_scene(name):
+    """the benchmark's contact workloads: (scene, log2 buckets, pre-roll)"""
+    if name == "fold1024":
+        return scenes.folding_cloth(res=1024, seed=0), 24, 120
+    if name == "drape256":
+        return scenes.drape_over_sphere(res=256, seed=0, start="contact"), 20, 0
+    raise ValueError(name)
+
+
+def evaluate_workloads(params, scales, sweeps=60, substeps=16, names=("fold1024", "drape256")):
+    out = {}
+    for name in names:
+        sc, log2, pre = workload_scene(name)
+        r = evaluate_contact_same_state(params, scales, sc, log2, pre, substeps=substeps,
+                                        sweeps=sweeps)
+        r.pop("per_substep")
+        out[name] = r
+    return out
 
 
 if __name__ == "__main__":

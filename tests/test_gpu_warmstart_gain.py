@@ -37,3 +37,23 @@ def test_closed_loop_sweeps_while_reachable(trained):
     assert p["early_reached"] == p["early_substeps"] == 20
     assert l["early_reached"] >= 19
     assert l["early_sweeps"] < p["early_sweeps"], r
+
+
+def test_contact_weights_cut_the_sweeps_of_a_held_out_fold():
+    """The network trained on contact states (folds on the ground, drapes
+    over a sphere) on a fold it was not trained on (seed outside the
+    training range): from identical states, the warm-started solve reaches
+    the residual of 60 plain sweeps with at most 3/4 of their sweeps in
+    total, on at least 5 of 6 substeps, and its device time is lower."""
+    from positionbaseddynamicsold_gb300 import scenes
+    assert os.path.exists(wt.CONTACT_WEIGHTS), "trained contact weights missing"
+    params, scales, meta = wt.load_params(wt.CONTACT_WEIGHTS)
+    sc = scenes.folding_cloth(res=160, seed=987_654, size=160 * 4.0 / 1024)
+    r = wt.evaluate_contact_same_state(params, scales, sc, 18, preroll=120, substeps=6,
+                                       sweeps=60, chunk=10)
+    assert r["learned_reached"] >= 5, r
+    assert r["learned_sweeps"] <= 0.75 * r["plain_sweeps"], r
+    assert r["learned_ms"] < r["plain_ms"], r
+    # the plain residual levels off: 200 sweeps take it little below 60
+    curve = {c["sweeps"]: c["stretch_residual"] for c in r["residual_curve_first_state"]}
+    assert curve[200] > 0.5 * curve[60] > 0.0
