@@ -335,6 +335,25 @@ int pbd_colli_get_contacts(pbd_colli *c, int *ids, int *face, float *t, double *
  * case; outputs hit (0/1), t, w (4 doubles), n (3 floats) per case. */
 int pbd_ccd_vf_test_batch(const float *x12, const float *p12, const float *thickness, int n,
                           int *hit, float *t, double *w, float *nrm);
+/* The vertex-face tests of the reference's detection drivers: */
+enum {
+    PBD_VFTEST_EXTENDED = 0, /* ExtendedVFTest (P/CCD.cpp:1733-1808), CCD_SH_Extended  */
+    PBD_VFTEST_NARROW = 1,   /* NarrowVFCCDTest (P/CCD.cpp:1810-1872), CCD_SH_Narrow   */
+    PBD_VFTEST_CCD = 2,      /* VFCCDTest, type VF (P/CCD.cpp:2308-2421)               */
+    PBD_VFTEST_DCD = 3,      /* VFDCDTest (P/CCD.cpp:2265-2306)                        */
+    PBD_VFTEST_VF = 4        /* VFTest = VFCCDTest || VFDCDTest (P/CCD.cpp:2229-2263),
+                                CCD_SH (P/CCD.cpp:2168-2227)                           */
+};
+/* pbd_ccd_vf_test_batch with the test chosen by mode (PBD_VFTEST_*).  A
+ * miss leaves in t, w and n what the test's last evaluated time wrote, as
+ * the reference leaves its Contact. */
+int pbd_ccd_vf_test_batch_mode(const float *x12, const float *p12, const float *thickness,
+                               int n, int mode, int *hit, float *t, double *w, float *nrm);
+/* the narrowphase test of a collision solver's detection (default
+ * PBD_VFTEST_EXTENDED, CCD_SH_Extended's): NARROW makes the detection
+ * CCD_SH_Narrow (P/CCD.cpp:1588-1731), VF makes it CCD_SH
+ * (P/CCD.cpp:2168-2227); the candidate pairs are the same in every mode */
+int pbd_colli_set_vf_test(pbd_colli *c, int mode);
 /* number of broadphase candidate pairs that reached the narrow phase in
  * the last CCD call, and the overflow word: 1 candidates, 2 contacts, 4 a
  * point with more than 16 incident triangles, 16 hash-search pairs,

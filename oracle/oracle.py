@@ -230,6 +230,17 @@ class Oracle:
         n = self.lib.orc_solve_cubic(a, b, c, d, x)
         return x[:n]
 
+    def vf_variant(self, kind, x, p, thickness, ids=(0, 1, 2, 3)):
+        """kind: 'vfccd' (VFCCDTest, type VF), 'vfdcd' (VFDCDTest) or 'vf'
+        (VFTest) -> (hit, t, w, n)"""
+        fn = {"vfccd": self.lib.orc_vf_ccd_test, "vfdcd": self.lib.orc_vf_dcd_test,
+              "vf": self.lib.orc_vf_test}[kind]
+        xs = np.ascontiguousarray(x, dtype=np.float32).reshape(12)
+        ps = np.ascontiguousarray(p, dtype=np.float32).reshape(12)
+        ct = OrcContact()
+        hit = fn(_ptr(xs), _ptr(ps), C.c_float(thickness), *[int(i) for i in ids], C.byref(ct))
+        return hit, ct.t, np.array(ct.w), np.array(ct.n, dtype=np.float32)
+
     def extended_vf_test(self, x, p, thickness, ids=(0, 1, 2, 3), narrow=False, fp64=False):
         """fp64: the all-double yardstick (orc_extended_vf_test_f64)"""
         xs = np.ascontiguousarray(x, dtype=np.float32).reshape(12)

@@ -924,6 +924,88 @@ int orc_narrow_vf_ccd_test(const float *x, const float *p, float thickness,
     return 0;
 }
 
+/* min(a, b, c) of the reference (P/CCD_Basic.h:184): std::min(a,
+ * std::min(b, c)), whose comparisons decide NaN cases */
+static double ref_min3(double a, double b, double c)
+{
+    double m = (c < b) ? c : b;
+    return (m < a) ? m : a;
+}
+
+/* free VFCCDTest with type VF (P/CCD.cpp:2308-2421): the cubic's roots in
+ * the order solve_cubic returns them (t = 1 is stored but never visited);
+ * a hit where the point lies in the triangle's plane (|d| < 1e-6) with
+ * every barycentric weight >= 1e-6 (no epsilon) */
+int orc_vf_ccd_test(const float *x, const float *p, float thickness, int i0, int i1, int i2,
+                    int i3, orc_contact *ct)
+{
+    (void)thickness;
+    (void)i0; (void)i1; (void)i2; (void)i3;
+    double a[4];
+    vf_cubic(x, p, a);
+    double t[4];
+    int nsol = orc_solve_cubic(a[3], a[2], a[1], a[0], t);
+    f3 X0 = ld3(x), X1 = ld3(x + 3), X2 = ld3(x + 6), X3 = ld3(x + 9);
+    f3 P0 = ld3(p), P1 = ld3(p + 3), P2 = ld3(p + 6), P3 = ld3(p + 9);
+    for (int i = 0; i < nsol; ++i) {
+        if (t[i] < 0 || t[i] > 1) continue;
+        f3 c0 = lerp_t(X0, P0, t[i]), c1 = lerp_t(X1, P1, t[i]);
+        f3 c2 = lerp_t(X2, P2, t[i]), c3 = lerp_t(X3, P3, t[i]);
+        f3 n = nrm(cross(sub(P2, P1), sub(P3, P1)));
+        f3 cn = nrm(cross(sub(c2, c1), sub(c3, c1)));
+        double d = dot(sub(c0, c1), cn);
+        f3 w = bary(c0, c1, c2, c3);
+        if (ct) {
+            ct->t = (float)t[i];
+            ct->n[0] = n.x; ct->n[1] = n.y; ct->n[2] = n.z;
+            ct->w[0] = 1; ct->w[1] = w.x; ct->w[2] = w.y; ct->w[3] = w.z;
+        }
+        if (fabs(d) < 1e-6 && ref_min3(w.x, w.y, w.z) >= 1e-6) return 1;
+    }
+    return 0;
+}
+
+/* Point2Plane (P/CCD.cpp:27-44): |n . v + D| / |n|, n the unnormalised
+ * face normal, in float */
+static float point_to_plane(f3 v, f3 p1, f3 p2, f3 p3)
+{
+    f3 N = cross(sub(p2, p1), sub(p3, p1));
+    float D = -(N.x * p1.x + N.y * p1.y + N.z * p1.z);
+    float mod = N.x * v.x + N.y * v.y + N.z * v.z + D;
+    float area = sqrtf(N.x * N.x + N.y * N.y + N.z * N.z);
+    return fabsf(mod) / area;
+}
+
+/* free VFDCDTest (P/CCD.cpp:2265-2306): the predicted point closer than
+ * 2 thickness to the predicted face's plane and inside it (every weight
+ * >= 1e-6); t = 0, the normal of the normalised edges */
+int orc_vf_dcd_test(const float *x, const float *p, float thickness, int i0, int i1, int i2,
+                    int i3, orc_contact *ct)
+{
+    (void)x;
+    (void)i0; (void)i1; (void)i2; (void)i3;
+    f3 P0 = ld3(p), P1 = ld3(p + 3), P2 = ld3(p + 6), P3 = ld3(p + 9);
+    float d = point_to_plane(P0, P1, P2, P3);
+    if ((double)(d - 2 * thickness) >= -1e-6) return 0;
+    f3 w = bary(P0, P1, P2, P3);
+    if (ct) {
+        ct->w[0] = 1; ct->w[1] = w.x; ct->w[2] = w.y; ct->w[3] = w.z;
+        f3 n = nrm(cross(nrm(sub(P2, P1)), nrm(sub(P3, P1))));
+        ct->n[0] = n.x; ct->n[1] = n.y; ct->n[2] = n.z;
+        ct->t = 0.0f;
+    }
+    return ref_min3(w.x, w.y, w.z) >= 1e-6;
+}
+
+/* free VFTest (P/CCD.cpp:2229-2263): VFCCDTest, else VFDCDTest (the
+ * second writes the contact over whatever the first left) */
+int orc_vf_test(const float *x, const float *p, float thickness, int i0, int i1, int i2, int i3,
+                orc_contact *ct)
+{
+    if (orc_vf_ccd_test(x, p, thickness, i0, i1, i2, i3, ct)) return 1;
+    return orc_vf_dcd_test(x, p, thickness, i0, i1, i2, i3, ct);
+}
+
 /* ExtendedVFTest restated entirely in FP64, the accuracy yardstick of the
  * reference-arithmetic test above (which mixes float geometry with double
  * cubic coefficients and stops Newton at |dx| < 1e-6): the same times 0,
@@ -1223,6 +1305,22 @@ static int cmp_hit(const void *a, const void *b)
     return ((const hit_rec *)a)->face - ((const hit_rec *)b)->face;
 }
 
+/* the test orc_ccd_vf_pairs runs (0 ExtendedVFTest, 1 NarrowVFCCDTest, 2
+ * VFCCDTest, 3 VFDCDTest, 4 VFTest) */
+static int g_vf_test = 0;
+void orc_set_vf_test(int mode) { g_vf_test = mode; }
+static int vf_test_by_mode(const float *x, const float *p, float th, int i0, int i1, int i2,
+                           int i3, orc_contact *ct)
+{
+    switch (g_vf_test) {
+        case 1: return orc_narrow_vf_ccd_test(x, p, th, i0, i1, i2, i3, ct);
+        case 2: return orc_vf_ccd_test(x, p, th, i0, i1, i2, i3, ct);
+        case 3: return orc_vf_dcd_test(x, p, th, i0, i1, i2, i3, ct);
+        case 4: return orc_vf_test(x, p, th, i0, i1, i2, i3, ct);
+        default: return orc_extended_vf_test(x, p, th, i0, i1, i2, i3, ct);
+    }
+}
+
 /* The hits of point v in face order (orc_ccd_vf_pairs' loop body); hits
  * and cc are the caller's scratch. */
 static int vf_pairs_point(const orc_grid *g, const cell_table *t, const int *cells,
@@ -1267,8 +1365,8 @@ static int vf_pairs_point(const orc_grid *g, const cell_table *t, const int *cel
                     gather4(ids, pos, xs);
                     gather4(ids, prdp, ps);
                     orc_contact ct;
-                    if (!orc_extended_vf_test(xs, ps, thickness, ids[0], ids[1], ids[2], ids[3],
-                                              &ct))
+                    memset(&ct, 0, sizeof(ct));
+                    if (!vf_test_by_mode(xs, ps, thickness, ids[0], ids[1], ids[2], ids[3], &ct))
                         continue;
                     ct.v = ids[0]; ct.f0 = ids[1]; ct.f1 = ids[2]; ct.f2 = ids[3];
                     ct.face = f;

@@ -229,6 +229,15 @@ int orc_extended_vf_test(const float *x, const float *p, float thickness,
 /* free NarrowVFCCDTest (P/CCD.cpp:1810-1872). */
 int orc_narrow_vf_ccd_test(const float *x, const float *p, float thickness,
                            int i0, int i1, int i2, int i3, orc_contact *ct);
+/* free VFCCDTest with type VF (P/CCD.cpp:2308-2421), VFDCDTest
+ * (P/CCD.cpp:2265-2306) and VFTest = VFCCDTest || VFDCDTest
+ * (P/CCD.cpp:2229-2263) */
+int orc_vf_ccd_test(const float *x, const float *p, float thickness, int i0, int i1, int i2,
+                    int i3, orc_contact *ct);
+int orc_vf_dcd_test(const float *x, const float *p, float thickness, int i0, int i1, int i2,
+                    int i3, orc_contact *ct);
+int orc_vf_test(const float *x, const float *p, float thickness, int i0, int i1, int i2, int i3,
+                orc_contact *ct);
 
 /* free CCD_SH_Extended (P/CCD.cpp:1522-1587) restated loop for loop:
  * triangles in id order, their points, neighbor triangles, IsDuplicated
@@ -266,6 +275,9 @@ int64_t orc_ccd_sh_extended_ref_range(const orc_grid *g, int n_tris, const int *
  * using point -> incident triangle lists (the evaluation order the CUDA
  * path uses); contacts sorted by (point, face triangle).  inst (may be
  * NULL) restricts pairs to points and triangles of the same instance. */
+/* the test orc_ccd_vf_pairs runs on each pair (0 ExtendedVFTest, default;
+ * 1 NarrowVFCCDTest; 2 VFCCDTest; 3 VFDCDTest; 4 VFTest), process-wide */
+void orc_set_vf_test(int mode);
 int64_t orc_ccd_vf_pairs(const orc_grid *g, int n_points, int n_tris,
                          const int *tri_idx, const int *tri_inst,
                          const int *point_inst, const float *pos,

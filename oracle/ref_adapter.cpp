@@ -200,6 +200,18 @@ int ref_solve_cubic(double a, double b, double c, double d, double *x) {
     return solve_cubic(a, b, c, d, x);
 }
 
+// The reference's solve_cubic reads xc[0] uninitialised when the derivative
+// quadratic has no usable root (a face moving with its point gives a = b =
+// 0, P/CCD.cpp:48-54); Newton then starts from whatever an earlier call left
+// on the stack and the root's last bits follow it.  Zeroing the stack below
+// the caller's frame before each test makes that start 0, the oracle's
+// choice, and the fixtures independent of call order.
+__attribute__((noinline)) static void scrub_stack() {
+    volatile char buf[32768];
+    memset((char *)buf, 0, sizeof(buf));
+    __asm__ __volatile__("" : : "r"(buf) : "memory");
+}
+
 static int vf_call(int which, const float *x, const float *p, float thickness,
                    int i0, int i1, int i2, int i3, float *t, double *w, float *n) {
     float3 X[4], P[4];
@@ -210,12 +222,23 @@ static int vf_call(int which, const float *x, const float *p, float thickness,
     Contact ct;
     memset(&ct, 0, sizeof(ct));
     bool hit;
+    Quiet q;  // VFCCDTest prints for one hard-coded id quadruple
+    scrub_stack();
     if (which == 0)
         hit = ExtendedVFTest(X[0], X[1], X[2], X[3], P[0], P[1], P[2], P[3], ct, thickness,
                              i0, i1, i2, i3);
-    else
+    else if (which == 1)
         hit = NarrowVFCCDTest(X[0], X[1], X[2], X[3], P[0], P[1], P[2], P[3], ct, thickness,
                               i0, i1, i2, i3);
+    else if (which == 2)
+        hit = VFCCDTest(X[0], X[1], X[2], X[3], P[0], P[1], P[2], P[3], Contact::VF, ct,
+                        thickness, i0, i1, i2, i3);
+    else if (which == 3)
+        hit = VFDCDTest(X[0], X[1], X[2], X[3], P[0], P[1], P[2], P[3], ct, thickness, i0, i1,
+                        i2, i3);
+    else
+        hit = VFTest(X[0], X[1], X[2], X[3], P[0], P[1], P[2], P[3], ct, thickness, i0, i1, i2,
+                     i3);
     *t = ct.t;
     for (int k = 0; k < 4; ++k) w[k] = ct.w[k];
     n[0] = ct.n.x; n[1] = ct.n.y; n[2] = ct.n.z;
@@ -232,6 +255,21 @@ int ref_extended_vf_test(const float *x, const float *p, float thickness, int i0
 int ref_narrow_vf_ccd_test(const float *x, const float *p, float thickness, int i0, int i1,
                            int i2, int i3, float *t, double *w, float *n) {
     return vf_call(1, x, p, thickness, i0, i1, i2, i3, t, w, n);
+}
+
+// free VFCCDTest with type VF (CCD.cpp:2308-2421), VFDCDTest
+// (CCD.cpp:2265-2306) and VFTest (CCD.cpp:2229-2263)
+int ref_vf_ccd_test(const float *x, const float *p, float thickness, int i0, int i1, int i2,
+                    int i3, float *t, double *w, float *n) {
+    return vf_call(2, x, p, thickness, i0, i1, i2, i3, t, w, n);
+}
+int ref_vf_dcd_test(const float *x, const float *p, float thickness, int i0, int i1, int i2,
+                    int i3, float *t, double *w, float *n) {
+    return vf_call(3, x, p, thickness, i0, i1, i2, i3, t, w, n);
+}
+int ref_vf_test(const float *x, const float *p, float thickness, int i0, int i1, int i2, int i3,
+                float *t, double *w, float *n) {
+    return vf_call(4, x, p, thickness, i0, i1, i2, i3, t, w, n);
 }
 
 // free CCD_SH_Extended (CCD.cpp:1522-1587).  The grid is built on prdp so

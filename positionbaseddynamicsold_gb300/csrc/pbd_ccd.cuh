@@ -268,6 +268,93 @@ __device__ bool extended_vf_test(const v3 *X, const v3 *P, float th, VFResult &r
     return extended_vf_roots(X, P, th, res);
 }
 
+// ---- the reference's other vertex-face tests ------------------------------
+// min(a, b, c) of the reference (P/CCD_Basic.h:184): std::min(a, std::min(b, c)),
+// whose comparisons decide NaN cases
+__device__ __forceinline__ double ref_min3(double a, double b, double c) {
+    double m = (c < b) ? c : b;
+    return (m < a) ? m : a;
+}
+
+// NarrowVFCCDTest (P/CCD.cpp:1810-1872) and VFCCDTest with type VF
+// (P/CCD.cpp:2308-2421): the coplanarity cubic's roots in [0, 1], in the
+// order solve_cubic returns them (t = 1 is stored but never visited, t = 0
+// not at all); a hit where the point lies in the plane (|d| < 1e-6) and
+// inside the triangle: within epsilon = thickness / mean predicted edge
+// (narrow) or with every weight >= 1e-6 (vfccd).  A miss leaves the last
+// evaluated root's t, w and n in res, as the reference leaves its Contact.
+__device__ bool vf_roots_test(const v3 *X, const v3 *P, float th, bool narrow, VFResult &res) {
+    double a[4];
+    vf_coeffs(X, P, a);
+    double t[4];
+    int nsol = solve_cubic(a[3], a[2], a[1], a[0], t);
+    for (int i = 0; i < nsol; ++i) {
+        if (t[i] < 0 || t[i] > 1) continue;
+        v3 c0 = lerp_t(X[0], P[0], t[i]), c1 = lerp_t(X[1], P[1], t[i]);
+        v3 c2 = lerp_t(X[2], P[2], t[i]), c3 = lerp_t(X[3], P[3], t[i]);
+        v3 n = nrm3(cross3(sub3(P[2], P[1]), sub3(P[3], P[1])));
+        v3 cn = nrm3(cross3(sub3(c2, c1), sub3(c3, c1)));
+        double d = dot3(sub3(c0, c1), cn);
+        v3 w = bary(c0, c1, c2, c3);
+        res.t = (float)t[i];
+        res.n = n;
+        res.w[0] = 1;
+        res.w[1] = w.x;
+        res.w[2] = w.y;
+        res.w[3] = w.z;
+        bool in;
+        if (narrow) {
+            float es = dist3(P[1], P[2]) + dist3(P[1], P[3]) + dist3(P[2], P[3]);
+            float eps = (float)((double)th / ((double)es / 3.0));
+            in = (w.x <= (1 + eps)) && (w.x >= (-eps)) && (w.y <= (1 + eps)) &&
+                 (w.y >= (-eps)) && (w.z <= (1 + eps)) && (w.z >= (-eps));
+        } else {
+            in = ref_min3(w.x, w.y, w.z) >= 1e-6;
+        }
+        if (fabs(d) < 1e-6 && in) return true;
+    }
+    return false;
+}
+
+// Point2Plane (P/CCD.cpp:27-44): |N . v + D| / |N|, N the face's
+// unnormalised normal, in float
+__device__ __forceinline__ float point_to_plane(v3 v, v3 p1, v3 p2, v3 p3) {
+    v3 N = cross3(sub3(p2, p1), sub3(p3, p1));
+    float D = -(N.x * p1.x + N.y * p1.y + N.z * p1.z);
+    float mod = N.x * v.x + N.y * v.y + N.z * v.z + D;
+    float area = sqrtf(N.x * N.x + N.y * N.y + N.z * N.z);
+    return fabsf(mod) / area;
+}
+
+// VFDCDTest (P/CCD.cpp:2265-2306): the predicted point within 2 thickness of
+// the predicted face's plane and inside it (every weight >= 1e-6); t = 0,
+// the normal of the normalised edges
+__device__ bool vf_dcd_test(const v3 *P, float th, VFResult &res) {
+    float d = point_to_plane(P[0], P[1], P[2], P[3]);
+    if ((double)(d - 2 * th) >= -1e-6) return false;
+    v3 w = bary(P[0], P[1], P[2], P[3]);
+    res.w[0] = 1;
+    res.w[1] = w.x;
+    res.w[2] = w.y;
+    res.w[3] = w.z;
+    res.n = nrm3(cross3(nrm3(sub3(P[2], P[1])), nrm3(sub3(P[3], P[1]))));
+    res.t = 0.0f;
+    return ref_min3(w.x, w.y, w.z) >= 1e-6;
+}
+
+// the narrowphase tests by PBD_VFTEST_* value: 0 ExtendedVFTest, 1
+// NarrowVFCCDTest, 2 VFCCDTest, 3 VFDCDTest, 4 VFTest = VFCCDTest ||
+// VFDCDTest (P/CCD.cpp:2229-2263)
+__device__ bool vf_test_mode(const v3 *X, const v3 *P, float th, int mode, VFResult &res) {
+    switch (mode) {
+        case 1: return vf_roots_test(X, P, th, true, res);
+        case 2: return vf_roots_test(X, P, th, false, res);
+        case 3: return vf_dcd_test(P, th, res);
+        case 4: return vf_roots_test(X, P, th, false, res) || vf_dcd_test(P, th, res);
+        default: return extended_vf_test(X, P, th, res);
+    }
+}
+
 // closest distance from point p to triangle abc (Ericson, Real-Time
 // Collision Detection, 5.1.5), float
 __device__ float point_tri_dist(v3 p, v3 a, v3 b, v3 c) {

@@ -464,13 +464,26 @@ __device__ __forceinline__ void store_contact(int *counters, long long ccap, int
 // no root near [0, 1]; a pair that needs the cubic's roots goes to the hard
 // list (counters[3]) so that the FP64 root isolation runs on full warps in
 // k_narrow_roots instead of stalling the warps of the common path
+// (mode: the narrowphase test, PBD_VFTEST_*; the tests that only look at
+// the cubic's roots cannot hit when it has no root near [0, 1])
+__device__ __forceinline__ int vf_first_mode(const v3 *X, const v3 *P, float th, int mode,
+                                             VFResult &r) {
+    if (mode == 0) return extended_vf_first(X, P, th, r);
+    if (mode == 3) return vf_dcd_test(P, th, r) ? 1 : 0;
+    double a[4];
+    vf_coeffs(X, P, a);
+    if (!no_root_near_unit(a[0], a[1], a[2], a[3])) return 2;
+    if (mode == 4) return vf_dcd_test(P, th, r) ? 1 : 0;
+    return 0;
+}
+
 __global__ void __launch_bounds__(128) k_narrow(const int2 *__restrict__ cand, long long cap,
                                                 int nt, float th,
                                                 const int4 *__restrict__ tri,
                                                 const float4 *__restrict__ x,
                                                 const float4 *__restrict__ p, int *counters,
                                                 long long ccap, int4 *cids, int *cface,
-                                                float4 *ctn, double4 *cw, int *hard) {
+                                                float4 *ctn, double4 *cw, int *hard, int mode) {
     long long n = counters[0];
     if (n > cap) n = cap;
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
@@ -480,7 +493,7 @@ __global__ void __launch_bounds__(128) k_narrow(const int2 *__restrict__ cand, l
         v3 X[4] = {ld3(x[c.x]), ld3(x[f.x]), ld3(x[f.y]), ld3(x[f.z])};
         v3 P[4] = {ld3(p[c.x]), ld3(p[f.x]), ld3(p[f.y]), ld3(p[f.z])};
         VFResult r;
-        int q = extended_vf_first(X, P, th, r);
+        int q = vf_first_mode(X, P, th, mode, r);
         if (q == 1) store_contact(counters, ccap, c, f, r, cids, cface, ctn, cw);
         if (q == 2) hard[agg_inc(counters + 3)] = (int)i;  // at most one entry per candidate
     }
@@ -493,7 +506,7 @@ __global__ void __launch_bounds__(128) k_narrow_roots(const int2 *__restrict__ c
                                                       const float4 *__restrict__ p,
                                                       int *counters, long long ccap, int4 *cids,
                                                       int *cface, float4 *ctn, double4 *cw,
-                                                      const int *__restrict__ hard) {
+                                                      const int *__restrict__ hard, int mode) {
     const int n = counters[3];
     for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
         int2 c = cand[hard[k]];
@@ -501,7 +514,8 @@ __global__ void __launch_bounds__(128) k_narrow_roots(const int2 *__restrict__ c
         v3 X[4] = {ld3(x[c.x]), ld3(x[f.x]), ld3(x[f.y]), ld3(x[f.z])};
         v3 P[4] = {ld3(p[c.x]), ld3(p[f.x]), ld3(p[f.y]), ld3(p[f.z])};
         VFResult r;
-        if (extended_vf_roots(X, P, th, r)) store_contact(counters, ccap, c, f, r, cids, cface, ctn, cw);
+        bool hit = mode == 0 ? extended_vf_roots(X, P, th, r) : vf_test_mode(X, P, th, mode, r);
+        if (hit) store_contact(counters, ccap, c, f, r, cids, cface, ctn, cw);
     }
 }
 
@@ -610,8 +624,8 @@ __global__ void __launch_bounds__(256) k_apply_deltas(int n, long long *acc, int
     }
 }
 
-__global__ void k_vf_batch(int n, const float *x12, const float *p12, const float *th, int *hit,
-                           float *t, double *w, float *nrm) {
+__global__ void k_vf_batch(int n, const float *x12, const float *p12, const float *th, int mode,
+                           int *hit, float *t, double *w, float *nrm) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     v3 X[4], P[4];
@@ -623,7 +637,7 @@ __global__ void k_vf_batch(int n, const float *x12, const float *p12, const floa
     r.t = 0.f;
     r.n = mk3(0.f, 0.f, 0.f);
     r.w[0] = r.w[1] = r.w[2] = r.w[3] = 0.0;
-    hit[i] = extended_vf_test(X, P, th[i], r) ? 1 : 0;
+    hit[i] = vf_test_mode(X, P, th[i], mode, r) ? 1 : 0;
     t[i] = r.t;
     for (int k = 0; k < 4; ++k) w[4 * i + k] = r.w[k];
     nrm[3 * i] = r.n.x;
@@ -736,10 +750,11 @@ static int ccd_detect_on(pbd_colli *c, cudaStream_t s, const float4 *psrc) {
     k_narrow<<<kPersistentBlocks, 128, 0, s>>>(c->cand.p, c->cand_cap, o->nt, th, o->tri.p,
                                                o->x.p, psrc, c->counters.p, c->contact_cap,
                                                c->cids.p, c->cface.p, c->ctn.p, c->cw.p,
-                                               c->hard.p);
+                                               c->hard.p, c->vf_test);
     k_narrow_roots<<<kPersistentBlocks, 128, 0, s>>>(c->cand.p, th, o->tri.p, o->x.p, psrc,
                                                      c->counters.p, c->contact_cap, c->cids.p,
-                                                     c->cface.p, c->ctn.p, c->cw.p, c->hard.p);
+                                                     c->cface.p, c->ctn.p, c->cw.p, c->hard.p,
+                                                     c->vf_test);
     k_clamp_counts<<<1, 32, 0, s>>>(c->counters.p, c->cand_cap, c->contact_cap);
     PBD_LAUNCH();
     return PBD_OK;
@@ -1079,6 +1094,13 @@ int pbd_colli_set_capacity(pbd_colli *c, long long cand, long long contacts) {
     return PBD_OK;
 }
 
+int pbd_colli_set_vf_test(pbd_colli *c, int mode) {
+    PBD_CHECK(c && mode >= PBD_VFTEST_EXTENDED && mode <= PBD_VFTEST_VF, PBD_ERR_ARG,
+              "bad vertex-face test");
+    c->vf_test = mode;
+    return PBD_OK;
+}
+
 int pbd_colli_set_overlap(pbd_colli *c, int on) {
     PBD_CHECK(c, PBD_ERR_ARG, "null argument");
     c->overlap = on ? 1 : 0;
@@ -1156,8 +1178,16 @@ int pbd_colli_get_contacts(pbd_colli *c, int *ids, int *face, float *t, double *
 
 int pbd_ccd_vf_test_batch(const float *x12, const float *p12, const float *thickness, int n,
                           int *hit, float *t, double *w, float *nrm) {
+    return pbd_ccd_vf_test_batch_mode(x12, p12, thickness, n, PBD_VFTEST_EXTENDED, hit, t, w,
+                                      nrm);
+}
+
+int pbd_ccd_vf_test_batch_mode(const float *x12, const float *p12, const float *thickness,
+                               int n, int mode, int *hit, float *t, double *w, float *nrm) {
     PBD_CHECK(x12 && p12 && thickness && hit && t && w && nrm && n >= 0, PBD_ERR_ARG,
               "null argument");
+    PBD_CHECK(mode >= PBD_VFTEST_EXTENDED && mode <= PBD_VFTEST_VF, PBD_ERR_ARG,
+              "bad vertex-face test %d", mode);
     if (n == 0) return PBD_OK;
     cudaStream_t s = nullptr;
     PBD_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
@@ -1171,7 +1201,8 @@ int pbd_ccd_vf_test_batch(const float *x12, const float *p12, const float *thick
         cudaStreamDestroy(s);
         return r;
     }
-    k_vf_batch<<<grid_for(n, 128), 128, 0, s>>>(n, dx.p, dp.p, dth.p, dh.p, dt.p, dw.p, dn.p);
+    k_vf_batch<<<grid_for(n, 128), 128, 0, s>>>(n, dx.p, dp.p, dth.p, mode, dh.p, dt.p, dw.p,
+                                                dn.p);
     cudaError_t e = cudaGetLastError();
     if (e == cudaSuccess) e = cudaMemcpyAsync(hit, dh.p, sizeof(int) * n, cudaMemcpyDeviceToHost, s);
     if (e == cudaSuccess) e = cudaMemcpyAsync(t, dt.p, sizeof(float) * n, cudaMemcpyDeviceToHost, s);

@@ -271,6 +271,7 @@ struct pbd_colli {
     float thickness = 0.0f;
     int iterations = 1;
     int response = PBD_RESPONSE_REFERENCE;
+    int vf_test = PBD_VFTEST_EXTENDED;  // narrowphase test of the detection
     long long cand_cap = 1 << 22;
     long long contact_cap = 1 << 20;
     long long task_cap = 1 << 22;

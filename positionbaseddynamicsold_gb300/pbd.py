@@ -75,7 +75,7 @@ EXPORTS = [
     "pbd_colli_ccd_sh_extended",
     "pbd_colli_collision_resolve_new", "pbd_colli_get_contacts", "pbd_colli_stats",
     "pbd_colli_get_pairs",
-    "pbd_ccd_vf_test_batch",
+    "pbd_ccd_vf_test_batch", "pbd_ccd_vf_test_batch_mode", "pbd_colli_set_vf_test",
     "pbd_residual_noalloc",
     "pbd_scene_read_cache", "pbd_scene_read_txt", "pbd_scene_desc", "pbd_scene_destroy",
     "pbd_scene_write_cache", "pbd_object_create_from_cache", "pbd_object_save_cache",
@@ -586,6 +586,11 @@ class CollisionSolver:
     def set_capacity(self, candidates, contacts):
         _check(self.L.pbd_colli_set_capacity(self.h, int(candidates), int(contacts)))
 
+    def set_vf_test(self, mode):
+        """narrowphase test of the detection (VFTEST_EXTENDED: CCD_SH_Extended,
+        VFTEST_NARROW: CCD_SH_Narrow, VFTEST_VF: CCD_SH)"""
+        _check(self.L.pbd_colli_set_vf_test(self.h, int(mode)))
+
     def set_overlap(self, on=True):
         """detections inside step / project_constraint_with_colli run beside
         the following sweep on a side stream (same results either way)"""
@@ -1008,9 +1013,13 @@ def ee_test_batch(X, P, thickness):
     return hit, tsu, m0
 
 
-def vf_test_batch(X, P, thickness):
-    """pbd_ccd_vf_test_batch: ExtendedVFTest on n (point, triangle) cases.
-    X, P: (n, 4, 3) start / predicted positions; thickness: (n,)."""
+VFTEST_EXTENDED, VFTEST_NARROW, VFTEST_CCD, VFTEST_DCD, VFTEST_VF = range(5)
+
+
+def vf_test_batch(X, P, thickness, mode=VFTEST_EXTENDED):
+    """pbd_ccd_vf_test_batch_mode: a vertex-face test (VFTEST_*; default
+    ExtendedVFTest) on n (point, triangle) cases.  X, P: (n, 4, 3) start /
+    predicted positions; thickness: (n,)."""
     L = load()
     X = np.ascontiguousarray(X, np.float32).reshape(-1, 12)
     P = np.ascontiguousarray(P, np.float32).reshape(-1, 12)
@@ -1020,5 +1029,6 @@ def vf_test_batch(X, P, thickness):
     t = np.zeros(n, np.float32)
     w = np.zeros((n, 4), np.float64)
     nrm = np.zeros((n, 3), np.float32)
-    _check(L.pbd_ccd_vf_test_batch(_p(X), _p(P), _p(th), n, _p(hit), _p(t), _p(w), _p(nrm)))
+    _check(L.pbd_ccd_vf_test_batch_mode(_p(X), _p(P), _p(th), n, int(mode), _p(hit), _p(t),
+                                        _p(w), _p(nrm)))
     return hit, t, w, nrm

@@ -222,6 +222,26 @@ def vf_cases(ref, n=1500, seed=17):
         q = p.copy()
         ref.lib.ref_vf_resolve_new(_ptr(x), _ptr(q), C.c_float(th[k]))
         rnew[k] = q.reshape(4, 3)
+    # VFCCDTest (type VF), VFDCDTest and VFTest on the same cases
+    extra = {}
+    for key, fn in (("vfccd", ref.lib.ref_vf_ccd_test), ("vfdcd", ref.lib.ref_vf_dcd_test),
+                    ("vf", ref.lib.ref_vf_test)):
+        eh = np.zeros(n, np.int32)
+        et = np.zeros(n, np.float32)
+        ew = np.zeros((n, 4), np.float64)
+        en = np.zeros((n, 3), np.float32)
+        for k in range(n):
+            x = np.ascontiguousarray(X[k].ravel())
+            p = np.ascontiguousarray(P[k].ravel())
+            t = C.c_float()
+            w = np.zeros(4, np.float64)
+            nv = np.zeros(3, np.float32)
+            eh[k] = fn(_ptr(x), _ptr(p), C.c_float(th[k]), 0, 1, 2, 3, C.byref(t), _ptr(w),
+                       _ptr(nv))
+            et[k] = t.value
+            ew[k] = w
+            en[k] = nv
+        extra.update({key + "_hit": eh, key + "_t": et, key + "_w": ew, key + "_n": en})
     coef = rng.normal(size=(500, 4))
     coef[:50, 0] = 0.0  # quadratic cases
     coef = np.concatenate([coef, [[1.0, -6.0, 11.0, -6.0]]])
@@ -234,7 +254,7 @@ def vf_cases(ref, n=1500, seed=17):
         roots[k, :m] = x[:m]
     np.savez_compressed(os.path.join(OUT, "vf_cases.npz"), X=X, P=P, thickness=th, hit=hit, t=tt,
                         w=ww, n=nn, narrow_hit=nhit, narrow_t=ntt, resolve_test=rtest,
-                        resolve_new=rnew, coef=coef, roots=roots, nroot=nroot)
+                        resolve_new=rnew, coef=coef, roots=roots, nroot=nroot, **extra)
 
 
 def _ref_read(ref, fn, args, cap=1 << 16):

@@ -284,3 +284,63 @@ def test_overlapped_detection_equals_sequential(graph):
         np.testing.assert_array_equal(res[0][0], res[1][0])
         np.testing.assert_array_equal(res[0][1], res[1][1])
         assert res[0][2] == res[1][2]
+
+
+@pytest.mark.parametrize("mode,key", [(1, "narrow"), (2, "vfccd"), (3, "vfdcd"), (4, "vf")])
+def test_other_vf_tests_match_reference(golden, mode, key):
+    """NarrowVFCCDTest, VFCCDTest, VFDCDTest and VFTest on the GPU against the
+    reference's own outputs on the 1,500 near-contact cases: hit and time
+    (and, where the fixture holds them, weights and normal) bit for bit,
+    misses included (a miss keeps what the last evaluated time wrote)."""
+    from positionbaseddynamicsold_gb300.pbd import vf_test_batch
+    g = golden("vf_cases")
+    hit, t, w, n = vf_test_batch(g["X"], g["P"], g["thickness"], mode)
+    np.testing.assert_array_equal(hit, g[key + "_hit"])
+    np.testing.assert_array_equal(t, g[key + "_t"])
+    if key + "_w" in g:
+        np.testing.assert_array_equal(w, g[key + "_w"])
+        np.testing.assert_array_equal(n, g[key + "_n"])
+    assert hit.sum() > 300
+
+
+@pytest.mark.parametrize("mode", [1, 2, 3, 4])
+def test_detection_with_other_vf_tests_matches_oracle(orc, mode):
+    """The detection run with CCD_SH_Narrow's, VFCCDTest's, VFDCDTest's or
+    CCD_SH's test in place of ExtendedVFTest: the same contacts (ids, face,
+    t, w, n) as the oracle's pair driver with that test, on a cloth folded
+    onto itself whose upper layer moves through the lower one."""
+    rng = np.random.default_rng(40 + mode)
+    res = 14
+    cloth = scenes.grid_cloth(res, res, 1.0, 1.0, jitter=0.0, seed=mode)
+    pos = cloth["pos"].astype(np.float64)
+    l = 1.0 / (res - 1)
+    h = 0.4 * l
+    fold = pos[:, 2] > 0.5
+    pos[fold, 2] = 1.0 - pos[fold, 2]
+    pos[fold, 1] += 1.5 * h
+    pos += rng.normal(0, 0.05 * l, pos.shape)
+    prd = pos + rng.normal(0, 0.1 * l, pos.shape)
+    prd[fold, 1] -= 2.2 * h
+    pos = pos.astype(np.float32)
+    prd = prd.astype(np.float32)
+    tri = cloth["tri_idx"]
+    cell = 2.0 * l
+    obj = mesh_object(pos, prd, tri)
+    shs = SpatialHashSystem(obj, cell_size=cell, log2_table=12)
+    shs.init()
+    cs = CollisionSolver(obj, shs, thickness=float(h), iterations=0)
+    cs.set_vf_test(mode)
+    cs.ccd_sh_extended()
+    got = cs.contacts()
+    orc.lib.orc_set_vf_test(mode)
+    try:
+        grid = orc.grid((0.0, 0.0, 0.0), None, cell, False)
+        want, nh = orc.ccd(grid, tri, pos, prd, float(h))
+    finally:
+        orc.lib.orc_set_vf_test(0)
+    assert nh > 10
+    np.testing.assert_array_equal(got["ids"], want["ids"])
+    np.testing.assert_array_equal(got["face"], want["face"])
+    np.testing.assert_array_equal(got["t"], want["t"])
+    np.testing.assert_array_equal(got["w"], want["w"])
+    np.testing.assert_array_equal(got["n"], want["n"])

@@ -136,6 +136,21 @@ def test_vf_cases(orc_pow, golden):
                                       g["resolve_new"][k])
 
 
+@pytest.mark.parametrize("kind", ["vfccd", "vfdcd", "vf"])
+def test_vf_variants_match_reference(orc_pow, golden, kind):
+    """VFCCDTest (type VF), VFDCDTest and VFTest (P/CCD.cpp:2229-2421) on the
+    1,500 near-contact cases: hit, time, weights and normal equal the
+    reference's own outputs (a miss leaves what the last evaluated time
+    wrote, compared too)"""
+    g = golden("vf_cases")
+    for k in range(len(g["hit"])):
+        hit, t, w, nv = orc_pow.vf_variant(kind, g["X"][k], g["P"][k], float(g["thickness"][k]))
+        assert hit == g[kind + "_hit"][k], k
+        assert np.float32(t) == g[kind + "_t"][k], k
+        np.testing.assert_array_equal(w, g[kind + "_w"][k])
+        np.testing.assert_array_equal(nv, g[kind + "_n"][k])
+
+
 def test_solve_cubic(orc_pow, golden):
     g = golden("vf_cases")
     for k, (a, b, c, d) in enumerate(g["coef"]):
