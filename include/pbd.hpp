@@ -121,6 +121,8 @@ public:
     void SetIterations(int i) { check(pbd_colli_set_iterations(h_, i)); }
     void SetResponse(int mode) { check(pbd_colli_set_response(h_, mode)); }
     void SetOverlap(bool on) { check(pbd_colli_set_overlap(h_, on ? 1 : 0)); }
+    // CollisionResolve (the older response), counters kept across calls
+    void CollisionResolve() { check(pbd_colli_collision_resolve_old(h_)); }
     // PBD_VFTEST_*: which driver's narrowphase test the detection runs
     void SetVFTest(int mode) { check(pbd_colli_set_vf_test(h_, mode)); }
     void CCD_SH_Extended() { check(pbd_colli_ccd_sh_extended(h_)); }

@@ -325,6 +325,20 @@ int pbd_colli_ccd_sh_extended(pbd_colli *c);
  * reads the pass-start positions and each point moves by the mean of its
  * active contacts' corrections. */
 int pbd_colli_collision_resolve_new(pbd_colli *c);
+/* The older response, CollisionResolve + VFResolve (P/CCD.cpp:2423-2650), on
+ * the current contacts: two passes over the contacts in stored order, each
+ * applied in place before the next is tested (one GPU thread walks the
+ * order, which decides the result); a contact is skipped while its point
+ * stays on its starting side at least 2 thickness from the predicted plane;
+ * a point closer than that on its side is pushed out by (2h - depth)/2, one
+ * that crossed by (depth + 2h)/2 when one of the four points was never
+ * resolved or VFCCDTest still finds the crossing.  The per-point resolve
+ * counters persist across calls, as the reference's resolveTimes buffer
+ * does.  The reference's debug output and cache saves are not reproduced. */
+int pbd_colli_collision_resolve_old(pbd_colli *c);
+/* copy out (out may be NULL) and optionally zero the resolve counters of
+ * pbd_colli_collision_resolve_old, one int per point of the target */
+int pbd_colli_resolve_times(pbd_colli *c, int *out, int reset);
 /* contactData (P/CCD_Basic.h:12-31) copy-out: ids 4 per contact (i0..i3),
  * face triangle, t, w (4 doubles), n (3 floats); any output may be NULL. */
 int pbd_colli_get_contacts(pbd_colli *c, int *ids, int *face, float *t, double *w, float *n,

@@ -282,6 +282,17 @@ class Oracle:
                                            C.c_float(thickness))
         return p
 
+    def resolve_old(self, ids, pos, prdp, resolve_times, thickness):
+        """CollisionResolve + VFResolve (the older response); resolve_times
+        (int32 per point) is updated in place; returns the new positions"""
+        p = np.ascontiguousarray(prdp, dtype=np.float32).copy()
+        x = np.ascontiguousarray(pos, dtype=np.float32)
+        assert resolve_times.dtype == np.int32 and resolve_times.flags.c_contiguous
+        arr = self._contacts_struct(ids)
+        self.lib.orc_collision_resolve_old(len(ids), arr, _ptr(x), _ptr(p), _ptr(resolve_times),
+                                           C.c_float(thickness))
+        return p
+
     def resolve_jacobi(self, ids, pos, prdp, mass, iterations, thickness, mass_weighted):
         p = np.ascontiguousarray(prdp, dtype=np.float32).copy()
         x = np.ascontiguousarray(pos, dtype=np.float32)

@@ -1507,6 +1507,70 @@ void orc_collision_resolve_ref(int n_contacts, const orc_contact *cts,
         }
 }
 
+/* VFResolve (P/CCD.cpp:2595-2650) on one contact, in place on p[12]:
+ * dp = (2h - depth)/2 when the point stayed on its side of the face and is
+ * closer than 2h to the predicted plane; (depth + 2h)/2 when it changed
+ * sides and some of the four points was never resolved, or VFCCDTest still
+ * finds the crossing; the point moves dp along the predicted normal
+ * towards its starting side, the face points the other way weighted
+ * w_i / sum w^2; the four counters count the contacts that moved them */
+static void vf_resolve_old(const float *x, float *p, float thickness, int *rt, const int *ids)
+{
+    f3 X0 = ld3(x), X1 = ld3(x + 3), X2 = ld3(x + 6), X3 = ld3(x + 9);
+    f3 P0 = ld3(p), P1 = ld3(p + 3), P2 = ld3(p + 6), P3 = ld3(p + 9);
+    f3 fn = nrm(cross(sub(X2, X1), sub(X3, X1)));
+    int pos_rel = side_of(X0, X1, fn);
+    f3 n = nrm(cross(sub(P2, P1), sub(P3, P1)));
+    float depth = point_to_plane(P0, P1, P2, P3);
+    int prd_rel = side_of(P0, P1, n);
+    float dp = 0.0f;
+    f3 w = bary(P0, P1, P2, P3);
+    if (pos_rel == prd_rel && depth < 2 * thickness) {
+        dp = (float)((double)(2 * thickness - depth) * 0.5);
+    } else if (pos_rel != prd_rel) {
+        if (rt[ids[0]] == 0 || rt[ids[1]] == 0 || rt[ids[2]] == 0 || rt[ids[3]] == 0)
+            dp = (float)((double)(depth + 2 * thickness) * 0.5);
+        else if (orc_vf_ccd_test(x, p, thickness, ids[0], ids[1], ids[2], ids[3], NULL))
+            dp = (float)((double)(depth + 2 * thickness) * 0.5);
+    }
+    if (dp != 0.0f)
+        for (int j = 0; j < 4; ++j) rt[ids[j]] += 1;
+    float sw = w.x * w.x + w.y * w.y + w.z * w.z;
+    f3 mn = mk(-n.x, -n.y, -n.z);
+    f3 a = pos_rel ? n : mn, b = pos_rel ? mn : n;
+    st3(p, add(P0, mul(a, dp)));
+    st3(p + 3, add(P1, divs(mul(mul(b, dp), w.x), sw)));
+    st3(p + 6, add(P2, divs(mul(mul(b, dp), w.y), sw)));
+    st3(p + 9, add(P3, divs(mul(mul(b, dp), w.z), sw)));
+}
+
+void orc_collision_resolve_old(int n_contacts, const orc_contact *cts, const float *pos,
+                               float *prdp, int *resolve_times, float thickness)
+{
+    /* CollisionResolve (P/CCD.cpp:2423-2593): two passes (its iteration
+     * argument is not used), contacts in stored order, in place; a contact
+     * is skipped when the point is on its starting side of the predicted
+     * face and at least 2h from its plane */
+    for (int it = 0; it < 2; ++it)
+        for (int c = 0; c < n_contacts; ++c) {
+            int ids[4] = {cts[c].v, cts[c].f0, cts[c].f1, cts[c].f2};
+            float xs[12], ps[12];
+            gather4(ids, pos, xs);
+            gather4(ids, prdp, ps);
+            f3 X0 = ld3(xs), X1 = ld3(xs + 3), X2 = ld3(xs + 6), X3 = ld3(xs + 9);
+            f3 P0 = ld3(ps), P1 = ld3(ps + 3), P2 = ld3(ps + 6), P3 = ld3(ps + 9);
+            f3 fn = nrm(cross(sub(X2, X1), sub(X3, X1)));
+            int f_rel = side_of(X0, X1, fn);
+            f3 nn = nrm(cross(sub(P2, P1), sub(P3, P1)));
+            int c_rel = side_of(P0, P1, nn);
+            float distance = point_to_plane(P0, P1, P2, P3);
+            if (c_rel == f_rel && distance >= 2 * thickness) continue;
+            vf_resolve_old(xs, ps, thickness, resolve_times, ids);
+            for (int j = 0; j < 4; ++j)
+                for (int k = 0; k < 3; ++k) prdp[3 * ids[j] + k] = ps[3 * j + k];
+        }
+}
+
 int orc_vf_resolve_deltas(const float *x, const float *p, const float *wm,
                           float thickness, int mass_weighted, float *delta)
 {

@@ -309,6 +309,11 @@ void orc_collision_resolve_ref(int n_contacts, const orc_contact *cts,
 void orc_collision_resolve_seq(int n_contacts, const orc_contact *cts, const float *pos,
                                float *prdp, const float *mass, int iterations,
                                float thickness, int mass_weighted);
+/* the older response CollisionResolve + VFResolve (P/CCD.cpp:2423-2650):
+ * two sequential in-place passes; resolve_times (one counter per point,
+ * kept by the caller between calls) gates the crossing case */
+void orc_collision_resolve_old(int n_contacts, const orc_contact *cts, const float *pos,
+                               float *prdp, int *resolve_times, float thickness);
 void orc_collision_resolve_jacobi(int n_points, int n_contacts,
                                   const orc_contact *cts, const float *pos,
                                   float *prdp, const float *mass, int iterations,

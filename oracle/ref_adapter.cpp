@@ -333,6 +333,36 @@ void ref_collision_resolve_new(int n_points, const float *pos, float *prdp,
     read_f3(P, prdp);
 }
 
+// free CollisionResolve (CCD.cpp:2423-2593) with VFResolve (CCD.cpp:2595-2650),
+// the older response: two in-place passes over the contacts in order, the
+// per-point resolve counters in resolve_times (in and out).  Its debug
+// output is silenced; the caches it tries to save go to a D:/ path that
+// does not open here, which it skips.
+void ref_collision_resolve_old(int n_points, const float *pos, float *prdp, int n_contacts,
+                               const int *ids, float thickness, int *resolve_times) {
+    Quiet q;
+    scrub_stack();
+    Topology topo;
+    fill_f3(topo.posBuffer, pos, n_points);
+    BufferVector3f P;
+    fill_f3(P, prdp, n_points);
+    ContactData cd;
+    for (int c = 0; c < n_contacts; ++c) {
+        Contact ct;
+        memset(&ct, 0, sizeof(ct));
+        ct.type = Contact::VF;
+        cd.ctxs.m_Data.push_back(ct);
+        cd.ctxStartNum.m_Data.push_back(make_int2(4 * c, 4));
+        for (int j = 0; j < 4; ++j) cd.ctxIndices.m_Data.push_back(ids[4 * c + j]);
+    }
+    int dbg = 0;
+    BufferInt vf, rt;
+    rt.m_Data.assign(resolve_times, resolve_times + n_points);
+    CollisionResolve(topo, P, cd, 2, thickness, dbg, vf, rt);
+    read_f3(P, prdp);
+    for (int i = 0; i < n_points; ++i) resolve_times[i] = rt.m_Data[i];
+}
+
 // free VFResolveTest (CCD.cpp:1996-2032); the reference prints for one
 // hard-wired id set, so ids are passed as 0..3.
 int ref_vf_resolve_test(const float *x, const float *p, float thickness) {

@@ -624,6 +624,80 @@ __global__ void __launch_bounds__(256) k_apply_deltas(int n, long long *acc, int
     }
 }
 
+// The older response, CollisionResolve + VFResolve (P/CCD.cpp:2423-2650):
+// two passes over the contacts in stored order, each applied in place
+// before the next is tested, the per-point resolve counters gating the
+// crossing case.  The result depends on the order, so one thread walks
+// it (the parallel response is k_contact_deltas / k_apply_deltas), in the
+// order the contacts are reported: by point, then face triangle.
+// sort keys of the contacts: (point, face triangle), the order the
+// contacts are reported in
+__global__ void k_old_keys(const int *counters, long long ccap, const int4 *ids, const int *face,
+                           long long nt, unsigned long long *key, int *val) {
+    long long n = counters[1];
+    if (n > ccap) n = ccap;
+    for (long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x; c < n;
+         c += (long long)gridDim.x * blockDim.x) {
+        key[c] = (unsigned long long)ids[c].x * (unsigned long long)nt +
+                 (unsigned long long)face[c];
+        val[c] = (int)c;
+    }
+}
+
+__global__ void k_resolve_old(const int *counters, long long ccap, const int4 *ids,
+                              const int *order, const float4 *__restrict__ x, float4 *p, int *rt,
+                              float th) {
+    if (blockIdx.x != 0 || threadIdx.x != 0) return;
+    long long n = counters[1];
+    if (n > ccap) n = ccap;
+    for (int it = 0; it < 2; ++it)
+        for (long long k = 0; k < n; ++k) {
+            const int4 id = ids[order[k]];
+            const int pid[4] = {id.x, id.y, id.z, id.w};
+            v3 X[4], P[4];
+            float4 q[4];
+            for (int j = 0; j < 4; ++j) {
+                X[j] = ld3(x[pid[j]]);
+                q[j] = p[pid[j]];
+                P[j] = ld3(q[j]);
+            }
+            // skip test of CollisionResolve (P/CCD.cpp:2470-2476, 2537-2539)
+            v3 fn = nrm3(cross3(sub3(X[2], X[1]), sub3(X[3], X[1])));
+            const bool f_rel = dot3(sub3(X[0], X[1]), fn) >= 0;
+            v3 nn = nrm3(cross3(sub3(P[2], P[1]), sub3(P[3], P[1])));
+            const bool c_rel = dot3(sub3(P[0], P[1]), nn) >= 0;
+            const float distance = point_to_plane(P[0], P[1], P[2], P[3]);
+            if (c_rel == f_rel && distance >= 2 * th) continue;
+            // VFResolve (P/CCD.cpp:2595-2650)
+            v3 n = nrm3(cross3(sub3(P[2], P[1]), sub3(P[3], P[1])));
+            const float depth = point_to_plane(P[0], P[1], P[2], P[3]);
+            const bool prd_rel = dot3(sub3(P[0], P[1]), n) >= 0;
+            float dp = 0.0f;
+            v3 w = bary(P[0], P[1], P[2], P[3]);
+            if (f_rel == prd_rel && depth < 2 * th) {
+                dp = (float)((double)(2 * th - depth) * 0.5);
+            } else if (f_rel != prd_rel) {
+                VFResult r;
+                if (rt[pid[0]] == 0 || rt[pid[1]] == 0 || rt[pid[2]] == 0 || rt[pid[3]] == 0 ||
+                    vf_roots_test(X, P, th, false, r))
+                    dp = (float)((double)(depth + 2 * th) * 0.5);
+            }
+            if (dp != 0.0f)
+                for (int j = 0; j < 4; ++j) rt[pid[j]] += 1;
+            const float sw = w.x * w.x + w.y * w.y + w.z * w.z;
+            const v3 mn = mk3(-n.x, -n.y, -n.z);
+            const v3 a = f_rel ? n : mn, b = f_rel ? mn : n;
+            v3 np0 = add3(P[0], mul3(a, dp));
+            v3 np1 = add3(P[1], div3(mul3(mul3(b, dp), w.x), sw));
+            v3 np2 = add3(P[2], div3(mul3(mul3(b, dp), w.y), sw));
+            v3 np3 = add3(P[3], div3(mul3(mul3(b, dp), w.z), sw));
+            p[pid[0]] = make_float4(np0.x, np0.y, np0.z, q[0].w);
+            p[pid[1]] = make_float4(np1.x, np1.y, np1.z, q[1].w);
+            p[pid[2]] = make_float4(np2.x, np2.y, np2.z, q[2].w);
+            p[pid[3]] = make_float4(np3.x, np3.y, np3.z, q[3].w);
+        }
+}
+
 __global__ void k_vf_batch(int n, const float *x12, const float *p12, const float *th, int mode,
                            int *hit, float *t, double *w, float *nrm) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1091,6 +1165,53 @@ int pbd_colli_set_capacity(pbd_colli *c, long long cand, long long contacts) {
     c->task_cap = cand;
     c->cand.release();
     c->cids.release();
+    return PBD_OK;
+}
+
+int pbd_colli_collision_resolve_old(pbd_colli *c) {
+    PBD_CHECK(c && c->obj, PBD_ERR_STATE, "collision solver has no target");
+    pbd_object *o = c->obj;
+    PBD_CHECK(c->cand.p && c->sized_n == o->n, PBD_ERR_STATE,
+              "no detection on the current target: detect before resolving");
+    if (!c->resolve_times.p || c->resolve_times.n < (size_t)o->n) {
+        PBD_TRY(c->resolve_times.alloc(o->n));
+        PBD_CUDA(cudaMemsetAsync(c->resolve_times.p, 0, sizeof(int) * o->n, o->stream));
+    }
+    // the contacts' reported order (the detection stores them as found)
+    const long long cap = c->contact_cap;
+    const int bits = round8(bits_for((long long)o->n * (long long)(o->nt > 0 ? o->nt : 1)));
+    PBD_TRY(c->old_key.alloc(cap));
+    PBD_TRY(c->old_key2.alloc(cap));
+    PBD_TRY(c->old_val.alloc(cap));
+    PBD_TRY(c->old_val2.alloc(cap));
+    PBD_TRY(radix_reserve(c->old_scr, cap, bits));
+    cudaStream_t s = o->stream;
+    k_old_keys<<<kResponseBlocks, 256, 0, s>>>(c->counters.p, cap, c->cids.p, c->cface.p, o->nt,
+                                               c->old_key.p, c->old_val.p);
+    PBD_LAUNCH();
+    unsigned long long *ko = nullptr;
+    int *vo = nullptr;
+    PBD_TRY(radix_sort<unsigned long long>(c->old_key.p, c->old_val.p, c->old_key2.p,
+                                           c->old_val2.p, cap, c->counters.p + 1, bits,
+                                           c->old_scr, s, &ko, &vo));
+    k_resolve_old<<<1, 32, 0, s>>>(c->counters.p, cap, c->cids.p, vo, o->x.p, o->p.p,
+                                   c->resolve_times.p, c->thickness);
+    PBD_LAUNCH();
+    return PBD_OK;
+}
+
+int pbd_colli_resolve_times(pbd_colli *c, int *out, int reset) {
+    PBD_CHECK(c && c->obj, PBD_ERR_STATE, "collision solver has no target");
+    pbd_object *o = c->obj;
+    if (!c->resolve_times.p || c->resolve_times.n < (size_t)o->n) {
+        PBD_TRY(c->resolve_times.alloc(o->n));
+        PBD_CUDA(cudaMemsetAsync(c->resolve_times.p, 0, sizeof(int) * o->n, o->stream));
+    }
+    if (out)
+        PBD_CUDA(cudaMemcpyAsync(out, c->resolve_times.p, sizeof(int) * o->n,
+                                 cudaMemcpyDeviceToHost, o->stream));
+    if (reset) PBD_CUDA(cudaMemsetAsync(c->resolve_times.p, 0, sizeof(int) * o->n, o->stream));
+    PBD_CUDA(cudaStreamSynchronize(o->stream));
     return PBD_OK;
 }
 

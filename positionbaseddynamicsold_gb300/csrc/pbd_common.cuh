@@ -291,6 +291,12 @@ struct pbd_colli {
     // between passes)
     pbd::DBuf<long long> acc;
     pbd::DBuf<int> acnt;
+    // the older response's per-point resolve counters (kept across calls)
+    // and the sort that puts its contacts in reported order
+    pbd::DBuf<int> resolve_times;
+    pbd::DBuf<unsigned long long> old_key, old_key2;
+    pbd::DBuf<int> old_val, old_val2;
+    pbd::SortScratch old_scr;
     // edge-edge CCD (off unless enabled): the object's unique edges (built
     // on first use; -1 = not yet), their grown swept boxes, the edge-cell
     // entries of the edge hash and their sort buffers, the edge pairs,

@@ -73,7 +73,8 @@ EXPORTS = [
     "pbd_colli_set_acce_struct", "pbd_colli_set_thickness", "pbd_colli_set_iterations",
     "pbd_colli_set_response", "pbd_colli_set_capacity", "pbd_colli_set_overlap",
     "pbd_colli_ccd_sh_extended",
-    "pbd_colli_collision_resolve_new", "pbd_colli_get_contacts", "pbd_colli_stats",
+    "pbd_colli_collision_resolve_new", "pbd_colli_collision_resolve_old",
+    "pbd_colli_resolve_times", "pbd_colli_get_contacts", "pbd_colli_stats",
     "pbd_colli_get_pairs",
     "pbd_ccd_vf_test_batch", "pbd_ccd_vf_test_batch_mode", "pbd_colli_set_vf_test",
     "pbd_residual_noalloc",
@@ -585,6 +586,17 @@ class CollisionSolver:
 
     def set_capacity(self, candidates, contacts):
         _check(self.L.pbd_colli_set_capacity(self.h, int(candidates), int(contacts)))
+
+    def collision_resolve_old(self):
+        """CollisionResolve + VFResolve, the reference's older response"""
+        _check(self.L.pbd_colli_collision_resolve_old(self.h))
+
+    def resolve_times(self, reset=False):
+        """the older response's per-point resolve counters (int32)"""
+        n = self.obj.n_points
+        out = np.zeros(n, np.int32)
+        _check(self.L.pbd_colli_resolve_times(self.h, _p(out), int(bool(reset))))
+        return out
 
     def set_vf_test(self, mode):
         """narrowphase test of the detection (VFTEST_EXTENDED: CCD_SH_Extended,

@@ -176,6 +176,40 @@ def ccd(ref):
                         ids=ids, t=t, w=w, n=nn, resolved=resolved)
 
 
+def resolve_old(ref):
+    """The older response CollisionResolve (three calls in a row on the ccd
+    fixture's contacts, positions and resolve counters carried over), with
+    a second contact set of sheets pushed further through each other."""
+    g = dict(np.load(os.path.join(OUT, "ccd.npz")))
+    out = {}
+    for case, push in (("a", 0.0), ("b", 0.012)):
+        prd = g["prdp"].copy()
+        prd[prd[:, 1] > np.median(prd[:, 1]), 1] -= np.float32(push)
+        ids = g["ids"] if push == 0.0 else None
+        if ids is None:
+            cap = 200000
+            ids = np.zeros((cap, 4), np.int32)
+            t = np.zeros(cap, np.float32)
+            w = np.zeros((cap, 4), np.float64)
+            nn = np.zeros((cap, 3), np.float32)
+            h = ref.lib.ref_ccd_sh_extended(_ptr(g["center"]), _ptr(g["size"]), _ptr(g["cell"]),
+                                            len(g["tri_idx"]), _ptr(g["tri_idx"]), len(g["pos"]),
+                                            _ptr(g["pos"]), _ptr(prd), C.c_float(g["thickness"]),
+                                            C.c_longlong(cap), _ptr(ids), _ptr(t), _ptr(w),
+                                            _ptr(nn))
+            ids = ids[:h].copy()
+        rt = np.zeros(len(g["pos"]), np.int32)
+        out[case + "_prdp0"] = prd.copy()
+        out[case + "_ids"] = ids
+        for k in range(3):
+            ref.lib.ref_collision_resolve_old(len(g["pos"]), _ptr(g["pos"]), _ptr(prd), len(ids),
+                                              _ptr(np.ascontiguousarray(ids)),
+                                              C.c_float(g["thickness"]), _ptr(rt))
+            out["%s_prdp%d" % (case, k + 1)] = prd.copy()
+            out["%s_rt%d" % (case, k + 1)] = rt.copy()
+    np.savez_compressed(os.path.join(OUT, "resolve_old.npz"), **out)
+
+
 def vf_cases(ref, n=1500, seed=17):
     """Random vertex/face motions close to contact, plus cubic roots."""
     rng = np.random.default_rng(seed)
@@ -333,6 +367,7 @@ def main():
     substep_gpu_pin(ref, orc)
     neighbors(ref)
     ccd(ref)
+    resolve_old(ref)
     vf_cases(ref)
     io_files(ref)
     for f in sorted(os.listdir(OUT)):

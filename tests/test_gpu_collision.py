@@ -344,3 +344,32 @@ def test_detection_with_other_vf_tests_matches_oracle(orc, mode):
     np.testing.assert_array_equal(got["t"], want["t"])
     np.testing.assert_array_equal(got["w"], want["w"])
     np.testing.assert_array_equal(got["n"], want["n"])
+
+
+@pytest.mark.parametrize("case", ["a", "b"])
+def test_old_response_matches_oracle(orc, golden, case):
+    """CollisionResolve + VFResolve (the older response) on the GPU: three
+    calls in a row on the detected contacts, positions and per-point
+    resolve counters equal the oracle's (which is pinned to the reference's
+    compiled code) run on the same contacts in the same stored order (the
+    GPU's detection stores them by point, then face)."""
+    g = golden("ccd")
+    r = golden("resolve_old")
+    obj = mesh_object(g["pos"], r[case + "_prdp0"], g["tri_idx"])
+    shs = SpatialHashSystem(obj, g["center"], g["size"], g["cell"])
+    shs.init()
+    cs = CollisionSolver(obj, shs, thickness=float(g["thickness"]), iterations=1)
+    cs.ccd_sh_extended()
+    ids = cs.contacts()["ids"]
+    assert len(ids) == len(r[case + "_ids"]) > 100
+    assert {tuple(v) for v in ids.tolist()} == {tuple(v) for v in r[case + "_ids"].tolist()}
+    prd = r[case + "_prdp0"]
+    rt = np.zeros(len(g["pos"]), np.int32)
+    for k in range(3):
+        cs.collision_resolve_old()
+        prd = orc.resolve_old(ids, g["pos"], prd, rt, float(g["thickness"]))
+        np.testing.assert_array_equal(obj.predicted(), prd)
+        np.testing.assert_array_equal(cs.resolve_times(), rt)
+    assert rt.sum() > 0
+    cs.resolve_times(reset=True)
+    assert cs.resolve_times().sum() == 0

@@ -159,3 +159,20 @@ def test_solve_cubic(orc_pow, golden):
         np.testing.assert_array_equal(x, g["roots"][k, :len(x)])
     x = orc_pow.solve_cubic(1.0, -6.0, 11.0, -6.0)
     assert np.allclose(x, [1, 2, 3], atol=1e-7)
+
+
+def test_old_response_matches_reference(orc_pow, golden):
+    """CollisionResolve + VFResolve (P/CCD.cpp:2423-2650), the older
+    response: three calls in a row with the positions and per-point resolve
+    counters carried over (the counters gate the crossing case from the
+    second call on), on two contact sets; positions and counters equal the
+    reference's own outputs."""
+    g = golden("ccd")
+    r = golden("resolve_old")
+    for case in "ab":
+        prd = r[case + "_prdp0"]
+        rt = np.zeros(len(g["pos"]), np.int32)
+        for k in range(1, 4):
+            prd = orc_pow.resolve_old(r[case + "_ids"], g["pos"], prd, rt, float(g["thickness"]))
+            np.testing.assert_array_equal(prd, r["%s_prdp%d" % (case, k)])
+            np.testing.assert_array_equal(rt, r["%s_rt%d" % (case, k)])
