@@ -71,6 +71,67 @@ def find_reference(ref_root: str | None = None) -> str | None:
     return None
 
 
+def _function_text(path: str, signature: str) -> str:
+    """The source text of one function of a reference file: from the line
+    holding `signature` to its closing brace (braces counted)."""
+    with open(path, encoding="utf-8-sig", errors="replace") as f:
+        text = f.read()
+    i = text.index(signature)
+    i = text.rfind("\n", 0, i) + 1
+    j = text.index("{", i)
+    depth = 0
+    for k in range(j, len(text)):
+        if text[k] == "{":
+            depth += 1
+        elif text[k] == "}":
+            depth -= 1
+            if depth == 0:
+                return text[i:k + 1]
+    raise ValueError("unbalanced braces after " + signature)
+
+
+def _kernel_host_unit(src: str) -> str:
+    """oracle/_ref/ref_kernel_host.cpp: ProjectContraintsGPUKernel and the
+    Distance it calls (P/PBD_cuda.cu), compiled for the host as written,
+    with threadIdx / blockIdx / blockDim as host variables; the entry
+    ref_project_colored_gpu_kernel runs one launch per color workset, every
+    index of it (the intended launch, without the integer-division grid)."""
+    pbd = os.path.join(src, "PBD_cuda.cu")
+    dist = _function_text(pbd, "KERNEL_FUNC float Distance(float3 p1, float3 p2)")
+    kern = _function_text(pbd, "void __global__ ProjectContraintsGPUKernel(")
+    return "\n".join([
+        "// generated by oracle/build_oracle.py from the reference's PBD_cuda.cu",
+        '#include "PBD_Basic.cuh"',
+        "static uint3 refk_tid, refk_bid;",
+        "static dim3 refk_bdim;",
+        "#define threadIdx refk_tid",
+        "#define blockIdx refk_bid",
+        "#define blockDim refk_bdim",
+        "#define Distance refk_Distance",
+        "#define ProjectContraintsGPUKernel refk_ProjectContraintsGPUKernel",
+        "static " + dist,
+        "static " + kern,
+        'extern "C" void ref_project_colored_gpu_kernel(',
+        "    int resY, int n_worksets, const int *worksets, int it0, int it1,",
+        "    int *sortedPrimId, int *indices, int *constraintType, float *massBuffer,",
+        "    float *restLengthBuffer, float *stiffnessBuffer, int2 *primList,",
+        "    float3 *prdPBuffer, float3 *restBuffer) {",
+        "    for (int it = it0; it < it1; ++it)",
+        "        for (int w = 0; w < n_worksets; ++w) {",
+        "            int start = worksets[2 * w], num = worksets[2 * w + 1];",
+        "            refk_bdim = dim3(512, 1, 1);",
+        "            for (int idx = 0; idx < num; ++idx) {",
+        "                refk_bid = make_uint3(idx / 512, 0, 0);",
+        "                refk_tid = make_uint3(idx % 512, 0, 0);",
+        "                refk_ProjectContraintsGPUKernel(resY, start, num, it, sortedPrimId,",
+        "                    indices, constraintType, massBuffer, restLengthBuffer,",
+        "                    stiffnessBuffer, primList, prdPBuffer, restBuffer);",
+        "            }",
+        "        }",
+        "}",
+        ""])
+
+
 def build_ref(ref_root: str | None = None, force: bool = False) -> str | None:
     """Compile the reference CPU path; returns the .so path or None if the
     reference sources are not present on this machine."""
@@ -101,6 +162,15 @@ def build_ref(ref_root: str | None = None, force: bool = False) -> str | None:
     objs.append(ao)
     if force or _stale(ao, [adapter]):
         jobs.append(gxx + incs + ["-c", adapter, "-o", ao])
+    # the GPU projection kernel's own code, compiled for the host
+    kcpp = os.path.join(REF_OUT, "ref_kernel_host.cpp")
+    ko = os.path.join(REF_OUT, "ref_kernel_host.o")
+    objs.append(ko)
+    pbd_src = os.path.join(src, "PBD_cuda.cu")
+    if force or _stale(ko, [pbd_src, os.path.abspath(__file__)]):
+        with open(kcpp, "w") as f:
+            f.write(_kernel_host_unit(src))
+        jobs.append(gxx + incs + ["-c", kcpp, "-o", ko])
     with ThreadPoolExecutor(max_workers=5) as ex:
         list(ex.map(_run, jobs))
     if force or jobs or not os.path.exists(REF_SO):

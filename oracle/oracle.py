@@ -147,6 +147,18 @@ class Oracle:
         """0: k = 1-(1-s)^(1/(iter+1)); 1: k = 1; 2: k = s (process-wide)"""
         self.lib.orc_set_stiffness_schedule(int(mode))
 
+    def project_colored(self, scene, prdp, mass, sorted_prim_id, worksets, it0, it1):
+        """the colored sweeps it0..it1-1 alone (orc_project_colored); returns
+        the new predicted positions"""
+        c = self.constraints(scene)
+        p = np.ascontiguousarray(prdp, dtype=np.float32).copy()
+        sid = np.ascontiguousarray(sorted_prim_id, dtype=np.int32)
+        ws = np.ascontiguousarray(worksets, dtype=np.int32)
+        m = np.ascontiguousarray(mass, dtype=np.float32)
+        self.lib.orc_project_colored(C.byref(c), _ptr(sid), len(ws), _ptr(ws), int(it0), int(it1),
+                                     _ptr(m), _ptr(p), 0)
+        return p
+
     def substep_gpu(self, scene, state, sorted_prim_id, worksets, iterations, dt, damping,
                     gravity, bending_fp64=False, colli=None, sphere=None, ground=None):
         """state: dict pos, vel (float32 (N,3)); modified in place.  sphere:

@@ -176,6 +176,34 @@ def ccd(ref):
                         ids=ids, t=t, w=w, n=nn, resolved=resolved)
 
 
+def gpu_kernel_schedule(ref, orc):
+    """ProjectContraintsGPUKernel (P/PBD_cuda.cu:1240-1306), compiled for the
+    host from the reference's own file, run colour by colour for 8
+    iterations on a jittered grid with distance stiffness below 1 (mixed
+    0.15 / 0.5 / 0.85), so the factor k = 1 - (1 - s)^(1/(iter+1)) is
+    exercised at every iteration count; pins and unequal masses included."""
+    sc = scenes.grid_cloth(11, 9, 1.0, 0.8, jitter=2e-2, seed=5, bending=False, pins=[0, 10])
+    rng = np.random.default_rng(5)
+    n = len(sc["pos"])
+    sc["stiffness"] = rng.choice(np.array([0.15, 0.5, 0.85], np.float32),
+                                 len(sc["stiffness"])).astype(np.float32)
+    mass = np.where(sc["mass"] > 0, rng.uniform(0.5, 2.0, n), 0.0).astype(np.float32)
+    color, _ = orc.edge_coloring(sc["prim_list"], sc["indices"], n)
+    _, sid, ws = orc.sort_worksets(color)
+    prd = (sc["pos"] + rng.normal(0, 0.03, sc["pos"].shape)).astype(np.float32)
+    out = prd.copy()
+    rest = np.zeros((2, 3), np.float32)
+    keep = [np.ascontiguousarray(a) for a in (sid, sc["indices"], sc["ctype"], mass,
+                                              sc["rest_length"], sc["stiffness"],
+                                              sc["prim_list"])]
+    ref.lib.ref_project_colored_gpu_kernel(11, len(ws), _ptr(np.ascontiguousarray(ws)), 0, 8,
+                                           *[_ptr(a) for a in keep], _ptr(out), _ptr(rest))
+    np.savez_compressed(os.path.join(OUT, "gpu_kernel_schedule.npz"), prim_list=sc["prim_list"],
+                        indices=sc["indices"], ctype=sc["ctype"], rest_length=sc["rest_length"],
+                        stiffness=sc["stiffness"], mass=mass, sorted_prim_id=sid, worksets=ws,
+                        prdp=prd, out=out)
+
+
 def resolve_old(ref):
     """The older response CollisionResolve (three calls in a row on the ccd
     fixture's contacts, positions and resolve counters carried over), with
@@ -368,6 +396,7 @@ def main():
     neighbors(ref)
     ccd(ref)
     resolve_old(ref)
+    gpu_kernel_schedule(ref, orc)
     vf_cases(ref)
     io_files(ref)
     for f in sorted(os.listdir(OUT)):

@@ -158,3 +158,23 @@ def test_anchor_target_arguments_are_checked():
         obj.set_anchor_targets([a], [[np.nan, 0.0, 0.0]])
     with pytest.raises(PBDError):
         obj.set_stiffness_schedule(7)
+
+
+def test_schedule_against_reference_gpu_kernel_fixture(golden):
+    """The GPU sweeps with stiffness below 1 against the reference's own
+    ProjectContraintsGPUKernel (its code run on the host; the fixture of
+    tests/golden/gpu_kernel_schedule.npz): the same coloring, 8 sweeps,
+    within 1e-5 m (device powf against the host's)."""
+    g = golden("gpu_kernel_schedule")
+    sc = scenes.grid_cloth(11, 9, 1.0, 0.8, jitter=2e-2, seed=5, bending=False, pins=[0, 10])
+    np.testing.assert_array_equal(sc["prim_list"], g["prim_list"])
+    sc["stiffness"] = g["stiffness"].copy()
+    sc["mass"] = g["mass"].copy()
+    obj = PBDObject(sc, damping=1.0, gravity=np.zeros(3, np.float32))
+    obj.prepare()
+    _, sid = obj.sorted()
+    np.testing.assert_array_equal(sid, g["sorted_prim_id"])
+    np.testing.assert_array_equal(obj.worksets(), g["worksets"])
+    obj.set_predicted(g["prdp"])
+    SolverPBD(obj).project_constraint(8)
+    assert np.abs(obj.predicted() - g["out"]).max() <= 1e-5

@@ -176,3 +176,16 @@ def test_old_response_matches_reference(orc_pow, golden):
             prd = orc_pow.resolve_old(r[case + "_ids"], g["pos"], prd, rt, float(g["thickness"]))
             np.testing.assert_array_equal(prd, r["%s_prdp%d" % (case, k)])
             np.testing.assert_array_equal(rt, r["%s_rt%d" % (case, k)])
+
+
+def test_stiffness_schedule_pinned_to_reference_gpu_kernel(orc_pow, golden):
+    """The colored projection with stiffness below 1 against the reference's
+    ProjectContraintsGPUKernel itself (P/PBD_cuda.cu:1240-1306, its code
+    compiled for the host by oracle/build_oracle.py and launched colour by
+    colour): 8 iterations, k = 1 - (1 - s)^(1/(iter+1)), bit for bit."""
+    g = golden("gpu_kernel_schedule")
+    sc = {k: g[k] for k in ("prim_list", "indices", "ctype", "rest_length", "stiffness")}
+    got = orc_pow.project_colored(sc, g["prdp"], g["mass"], g["sorted_prim_id"], g["worksets"],
+                                  0, 8)
+    np.testing.assert_array_equal(got, g["out"])
+    assert np.abs(g["out"] - g["prdp"]).max() > 1e-3
