@@ -39,11 +39,13 @@ __device__ __forceinline__ float dist3(v3 a, v3 b) {
     return sqrtf(dx * dx + dy * dy + dz * dz);
 }
 __device__ __forceinline__ float stp(v3 u, v3 v, v3 w) { return dot3(u, cross3(v, w)); }
-__device__ __forceinline__ v3 lerp_t(v3 a, v3 b, double t) {
-    float tf = (float)t;
+// a + t (b - a) with the time rounded to float, as the reference's
+// ExtendedVFTest and VFCCDTest interpolate
+__device__ __forceinline__ v3 lerp_f(v3 a, v3 b, float tf) {
     v3 d = sub3(b, a);
     return add3(a, mk3(tf * d.x, tf * d.y, tf * d.z));
 }
+__device__ __forceinline__ v3 lerp_t(v3 a, v3 b, double t) { return lerp_f(a, b, (float)t); }
 // BarycentricCoord (P/CCD.cpp:115-130)
 __device__ __forceinline__ v3 bary(v3 pos, v3 p0, v3 p1, v3 p2) {
     v3 ab = sub3(p0, p2), ac = sub3(p1, p2), ap = sub3(pos, p2);
@@ -117,29 +119,44 @@ __device__ int solve_cubic(double a, double b, double c, double d, double x[3]) 
     return i;
 }
 
+// A contact's weights are float values (the barycentric coordinates are
+// computed in float); the reference stores them as doubles, which the
+// contact store does (exactly) when it writes them out.
 struct VFResult {
     float t;
     v3 n;
-    double w[4];
+    float w[4];
 };
 
-// one evaluation of ExtendedVFTest's loop body at time t
-__device__ __forceinline__ bool vf_eval_at(const v3 *X, const v3 *P, float th, double t,
+// |d| - 2h < -1e-6 for float d and 2h, the difference taken in double as the
+// reference takes it.  The float difference is within 2^-24 of it
+// (relative), so it decides whenever it is more than 1e-6 (relative) from
+// the bound; otherwise (and for NaN) the double difference decides.
+__device__ __forceinline__ bool plane_close(float d, float th2) {
+    const float fd = fabsf(d) - th2;
+    if (fd < -1.000001e-6f) return true;
+    if (fd > -0.999999e-6f) return false;
+    return fabs((double)d) - (double)th2 < -1e-6;
+}
+
+// one evaluation of ExtendedVFTest's loop body at time tf (the cubic's root
+// rounded to float, or 0 or 1)
+__device__ __forceinline__ bool vf_eval_at(const v3 *X, const v3 *P, float th, float tf,
                                            VFResult &res) {
-    v3 c0 = lerp_t(X[0], P[0], t), c1 = lerp_t(X[1], P[1], t);
-    v3 c2 = lerp_t(X[2], P[2], t), c3 = lerp_t(X[3], P[3], t);
+    v3 c0 = lerp_f(X[0], P[0], tf), c1 = lerp_f(X[1], P[1], tf);
+    v3 c2 = lerp_f(X[2], P[2], tf), c3 = lerp_f(X[3], P[3], tf);
     v3 n = nrm3(cross3(sub3(P[2], P[1]), sub3(P[3], P[1])));
     v3 cn = nrm3(cross3(sub3(c2, c1), sub3(c3, c1)));
-    double dist = dot3(sub3(c0, c1), cn);
+    float dist = dot3(sub3(c0, c1), cn);
     v3 w = bary(c0, c1, c2, c3);
-    res.t = (float)t;
+    res.t = tf;
     res.n = n;
-    res.w[0] = 1;
+    res.w[0] = 1.f;
     res.w[1] = w.x;
     res.w[2] = w.y;
     res.w[3] = w.z;
     // the plane test first: the inside test only matters when it passes
-    if (!(fabs(dist) - (double)(2.0f * th) < -1e-6)) return false;
+    if (!plane_close(dist, 2.0f * th)) return false;
     float e1 = dist3(c1, c2), e2 = dist3(c1, c3), e3 = dist3(c2, c3);
     float es = e1 + e2 + e3;
     // epsilon = thickness / (edge sum / 3.0), a double division rounded to
@@ -183,9 +200,11 @@ __device__ __forceinline__ bool no_root_near_unit_f64(double a0, double a1, doub
 // values (the triple products are float); the float Bernstein coefficients
 // are within ~10 ulps of sum |a| of the double ones, so when all four
 // clear 1e-5 sum |a| with one sign, the double ones clear the 1e-9 sum |a|
-// tolerance with that sign too.  Otherwise the double evaluation decides.
-__device__ __forceinline__ bool no_root_near_unit(double a0, double a1, double a2, double a3) {
-    const float f0 = (float)a0, f1 = (float)a1, f2 = (float)a2, f3 = (float)a3;
+// tolerance with that sign too, and when one clears it above and another
+// below, the double ones have both signs as well (no decision of one sign:
+// false).  All four zero: false, as in double.  Otherwise the double
+// evaluation decides.
+__device__ __forceinline__ bool no_root_near_unit(float f0, float f1, float f2, float f3) {
     const float u = -1e-3f, L = 1.002f;
     float c0 = ((f3 * u + f2) * u + f1) * u + f0;
     float c1 = L * ((3.0f * f3 * u + 2.0f * f2) * u + f1);
@@ -198,8 +217,12 @@ __device__ __forceinline__ bool no_root_near_unit(double a0, double a1, double a
     if (tol > 0.f && isfinite(tol)) {
         if (b0 > tol && b1 > tol && b2 > tol && b3 > tol) return true;
         if (b0 < -tol && b1 < -tol && b2 < -tol && b3 < -tol) return true;
+        const bool above = b0 > tol || b1 > tol || b2 > tol || b3 > tol;
+        const bool below = b0 < -tol || b1 < -tol || b2 < -tol || b3 < -tol;
+        if (above && below) return false;
     }
-    return no_root_near_unit_f64(a0, a1, a2, a3);
+    if (f0 == 0.f && f1 == 0.f && f2 == 0.f && f3 == 0.f) return false;
+    return no_root_near_unit_f64(f0, f1, f2, f3);
 }
 
 // ExtendedVFTest (P/CCD.cpp:1733-1808); X/P = start/predicted positions of
@@ -217,7 +240,7 @@ __device__ __forceinline__ bool no_root_near_unit(double a0, double a1, double a
 // [0, 1], for t = 1 (returns 1 hit, 0 no hit, 2 roots needed);
 // extended_vf_roots finishes a pair that needs roots (t = 0 is known not to
 // hit).  extended_vf_test is the composition.
-__device__ __forceinline__ void vf_coeffs(const v3 *X, const v3 *P, double a[4]) {
+__device__ __forceinline__ void vf_coeffs(const v3 *X, const v3 *P, float a[4]) {
     v3 x0 = X[0], v0 = sub3(P[0], x0);
     v3 x1 = sub3(X[1], x0), x2 = sub3(X[2], x0), x3 = sub3(X[3], x0);
     v3 v1 = sub3(sub3(P[1], X[1]), v0), v2 = sub3(sub3(P[2], X[2]), v0),
@@ -230,15 +253,15 @@ __device__ __forceinline__ void vf_coeffs(const v3 *X, const v3 *P, double a[4])
 
 __device__ __forceinline__ int extended_vf_first(const v3 *X, const v3 *P, float th,
                                                  VFResult &res) {
-    double a[4];
+    float a[4];
     vf_coeffs(X, P, a);
-    if (vf_eval_at(X, P, th, 0.0, res)) return 1;
-    if (no_root_near_unit(a[0], a[1], a[2], a[3])) return vf_eval_at(X, P, th, 1.0, res) ? 1 : 0;
+    if (vf_eval_at(X, P, th, 0.0f, res)) return 1;
+    if (no_root_near_unit(a[0], a[1], a[2], a[3])) return vf_eval_at(X, P, th, 1.0f, res) ? 1 : 0;
     return 2;
 }
 
 __device__ bool extended_vf_roots(const v3 *X, const v3 *P, float th, VFResult &res) {
-    double a[4];
+    float a[4];
     vf_coeffs(X, P, a);
     const double a0 = a[0], a1 = a[1], a2 = a[2], a3 = a[3];
     double t[5];
@@ -257,7 +280,7 @@ __device__ bool extended_vf_roots(const v3 *X, const v3 *P, float th, VFResult &
     }
     for (int i = 0; i < m; ++i) {
         if (t[i] < 0 || t[i] > 1) continue;
-        if (vf_eval_at(X, P, th, t[i], res)) return true;
+        if (vf_eval_at(X, P, th, (float)t[i], res)) return true;
     }
     return false;
 }
@@ -284,7 +307,7 @@ __device__ __forceinline__ double ref_min3(double a, double b, double c) {
 // (narrow) or with every weight >= 1e-6 (vfccd).  A miss leaves the last
 // evaluated root's t, w and n in res, as the reference leaves its Contact.
 __device__ bool vf_roots_test(const v3 *X, const v3 *P, float th, bool narrow, VFResult &res) {
-    double a[4];
+    float a[4];
     vf_coeffs(X, P, a);
     double t[4];
     int nsol = solve_cubic(a[3], a[2], a[1], a[0], t);
@@ -298,7 +321,7 @@ __device__ bool vf_roots_test(const v3 *X, const v3 *P, float th, bool narrow, V
         v3 w = bary(c0, c1, c2, c3);
         res.t = (float)t[i];
         res.n = n;
-        res.w[0] = 1;
+        res.w[0] = 1.f;
         res.w[1] = w.x;
         res.w[2] = w.y;
         res.w[3] = w.z;
@@ -333,7 +356,7 @@ __device__ bool vf_dcd_test(const v3 *P, float th, VFResult &res) {
     float d = point_to_plane(P[0], P[1], P[2], P[3]);
     if ((double)(d - 2 * th) >= -1e-6) return false;
     v3 w = bary(P[0], P[1], P[2], P[3]);
-    res.w[0] = 1;
+    res.w[0] = 1.f;
     res.w[1] = w.x;
     res.w[2] = w.y;
     res.w[3] = w.z;

@@ -457,7 +457,7 @@ __device__ __forceinline__ void store_contact(int *counters, long long ccap, int
     cids[slot] = make_int4(c.x, f.x, f.y, f.z);
     cface[slot] = c.y;
     ctn[slot] = make_float4(r.t, r.n.x, r.n.y, r.n.z);
-    cw[slot] = make_double4(r.w[0], r.w[1], r.w[2], r.w[3]);
+    cw[slot] = make_double4((double)r.w[0], (double)r.w[1], (double)r.w[2], (double)r.w[3]);
 }
 
 // narrow phase, common path: t = 0, and t = 1 when the coplanarity cubic has
@@ -470,7 +470,7 @@ __device__ __forceinline__ int vf_first_mode(const v3 *X, const v3 *P, float th,
                                              VFResult &r) {
     if (mode == 0) return extended_vf_first(X, P, th, r);
     if (mode == 3) return vf_dcd_test(P, th, r) ? 1 : 0;
-    double a[4];
+    float a[4];
     vf_coeffs(X, P, a);
     if (!no_root_near_unit(a[0], a[1], a[2], a[3])) return 2;
     if (mode == 4) return vf_dcd_test(P, th, r) ? 1 : 0;
@@ -710,10 +710,10 @@ __global__ void k_vf_batch(int n, const float *x12, const float *p12, const floa
     VFResult r;
     r.t = 0.f;
     r.n = mk3(0.f, 0.f, 0.f);
-    r.w[0] = r.w[1] = r.w[2] = r.w[3] = 0.0;
+    r.w[0] = r.w[1] = r.w[2] = r.w[3] = 0.f;
     hit[i] = vf_test_mode(X, P, th[i], mode, r) ? 1 : 0;
     t[i] = r.t;
-    for (int k = 0; k < 4; ++k) w[4 * i + k] = r.w[k];
+    for (int k = 0; k < 4; ++k) w[4 * i + k] = (double)r.w[k];
     nrm[3 * i] = r.n.x;
     nrm[3 * i + 1] = r.n.y;
     nrm[3 * i + 2] = r.n.z;

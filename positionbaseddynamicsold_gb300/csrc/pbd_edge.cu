@@ -129,7 +129,7 @@ __device__ __forceinline__ bool ee_eval_at(const v3 *X, const v3 *P, float th, d
     v3 d;
     if (!ee_interior(c0, c1, c2, c3, s, u, d)) return false;
     float dist = sqrtf(dot3(d, d));
-    if (!((double)dist - (double)(2.0f * th) < -1e-6)) return false;
+    if (!plane_close(dist, 2.0f * th)) return false;
     h.t = (float)t;
     h.s = s;
     h.u = u;
@@ -150,10 +150,10 @@ __device__ bool ee_test(const v3 *X, const v3 *P, float th, EEHit &h) {
     v3 x1 = sub3(X[1], x0), x2 = sub3(X[2], x0), x3 = sub3(X[3], x0);
     v3 v1 = sub3(sub3(P[1], X[1]), v0), v2 = sub3(sub3(P[2], X[2]), v0),
        v3_ = sub3(sub3(P[3], X[3]), v0);
-    double a0 = stp(x1, x2, x3);
-    double a1 = stp(v1, x2, x3) + stp(x1, v2, x3) + stp(x1, x2, v3_);
-    double a2 = stp(x1, v2, v3_) + stp(v1, x2, v3_) + stp(v1, v2, x3);
-    double a3 = stp(v1, v2, v3_);
+    const float a0 = stp(x1, x2, x3);
+    const float a1 = stp(v1, x2, x3) + stp(x1, v2, x3) + stp(x1, x2, v3_);
+    const float a2 = stp(x1, v2, v3_) + stp(v1, x2, v3_) + stp(v1, v2, x3);
+    const float a3 = stp(v1, v2, v3_);
     if (ee_eval_at(X, P, th, 0.0, h)) return true;
     if (no_root_near_unit(a0, a1, a2, a3)) return ee_eval_at(X, P, th, 1.0, h);
     double t[5];

@@ -438,6 +438,42 @@ def load_params(path=DEFAULT_WEIGHTS):
             json.loads(str(d["meta"])))
 
 
+def apply_once(params, scales, side=1024, repeats=3, sweeps=15, seed=0):
+    """the network on one side^2 hanging cloth with eager launches (no
+    graph): per repeat one substep's advection, the features and inference
+    with the prediction applied (pbd_warmstart_predict), the recording, a
+    plain solve of `sweeps` sweeps and one training step
+    (pbd_warmstart_train_step); host-timed milliseconds per call, each call
+    synchronised"""
+    sc = scenes.grid_cloth(side, side, 1.0, 1.0, jitter=1e-3, seed=seed,
+                           pins=np.array([0, side - 1]))
+    obj = PBDObject(sc, damping=1.0, gravity=(0.0, -9.8, 0.0))
+    obj.prepare()
+    s = SolverPBD(obj)
+    ws = WarmStart(params, scales)
+    t = {"predict": [], "train_step": []}
+    for _ in range(repeats):
+        s.advect(DT)
+        obj.sync()
+        t0 = time.perf_counter()
+        ws.predict(obj)
+        obj.sync()
+        t["predict"].append(1e3 * (time.perf_counter() - t0))
+        ws.record(obj)
+        s.project_constraint(sweeps)
+        obj.sync()
+        t0 = time.perf_counter()
+        ws.train_step(obj, want_loss=True)
+        t["train_step"].append(1e3 * (time.perf_counter() - t0))
+        s.integration(DT)
+    out = {"points": obj.n_points, "repeats": repeats,
+           "predict_ms": t["predict"], "train_step_ms": t["train_step"]}
+    ws.close()
+    s.close()
+    obj.close()
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--trajectories", type=int, default=2000)
@@ -464,9 +500,16 @@ def main():
     ap.add_argument("--contact-sweeps", type=int, default=60)
     ap.add_argument("--eval-only", default=None,
                     help="evaluate these weights on the contact workloads and exit")
+    ap.add_argument("--apply-once", type=int, default=0, metavar="SIDE",
+                    help="apply the network (weights from --init, else the contact-trained "
+                         "ones) to a SIDE^2 hanging cloth with eager launches and exit")
     ap.add_argument("--out", default=DEFAULT_WEIGHTS)
     a = ap.parse_args()
     t0 = time.time()
+    if a.apply_once:
+        params, scales, _ = load_params(a.init or CONTACT_WEIGHTS)
+        print(json.dumps(apply_once(params, scales, a.apply_once)))
+        return
     if a.contact_trajectories or a.contact_on_policy or a.eval_only:
         return main_contact(a, t0)
     params = None

@@ -1,13 +1,16 @@
 """Substeps solved to a residual target: the device-side loop (CUDA graph
 WHILE node) stops where the residual first reaches the target, its result
 equals the oracle's substep with that many sweeps, and the graph and eager
-forms agree bit for bit, with and without collisions."""
+forms agree bit for bit, with and without collisions.  With collisions the
+loop equals the same substep composed of the public fixed-step calls, with
+no chunk, one or two."""
 import numpy as np
 import pytest
 
 from positionbaseddynamicsold_gb300 import scenes
-from positionbaseddynamicsold_gb300.pbd import (RESPONSE_MASS_WEIGHTED, CollisionSolver,
-                                                PBDObject, SolverPBD, SpatialHashSystem)
+from positionbaseddynamicsold_gb300.pbd import (RESPONSE_MASS_WEIGHTED, SCHEDULE_DIRECT,
+                                                CollisionSolver, PBDObject, SolverPBD,
+                                                SpatialHashSystem)
 
 pytestmark = pytest.mark.gpu
 
@@ -104,3 +107,45 @@ def test_graph_equals_eager(colli):
     np.testing.assert_array_equal(res[0][0], res[1][0])
     assert res[0][1] == res[1][1]
     assert res[0][1]["substeps"] == 8
+
+
+def drape_solver(sc):
+    obj = PBDObject(sc, damping=1.0, gravity=G)
+    obj.prepare()
+    # k = s in every sweep, so a sweep of the loop is one project_constraint(1)
+    obj.set_stiffness_schedule(SCHEDULE_DIRECT)
+    s = SolverPBD(obj)
+    shs = SpatialHashSystem(obj, cell_size=sc["cell"], log2_table=16)
+    shs.init()
+    cs = CollisionSolver(obj, shs, thickness=1e-3, iterations=1, response=RESPONSE_MASS_WEIGHTED)
+    return obj, s, shs, cs
+
+
+@pytest.mark.parametrize("chunks", [0, 1, 2])
+def test_collision_loop_equals_composed_calls(chunks):
+    """advect; the contacts of the advected positions; per chunk 10 x (sweep,
+    response) and the detection from the chunk's final positions; the
+    response to the last contacts; integrate.  No chunk (target above the
+    residual): the last contacts are those of the advected positions."""
+    sc = drape(seed=3)
+    got = []
+    for graph in (False, True):
+        obj, s, shs, cs = drape_solver(sc)
+        s.step_to_residual(DT, 1, target=1.0 if chunks == 0 else 0.0,
+                           max_sweeps=max(10, 10 * chunks), chunk=10, colli=cs, use_graph=graph)
+        assert s.solve_stats()["last_sweeps"] == 10 * chunks
+        got.append((obj.positions(), cs.stats()["contacts"]))
+    obj, s, shs, cs = drape_solver(sc)
+    s.advect(DT)
+    cs.ccd_sh_extended()
+    assert cs.stats()["contacts"] > 0
+    for _ in range(chunks):
+        for _ in range(10):
+            s.project_constraint(1)
+            cs.collision_resolve_new()
+        cs.ccd_sh_extended()
+    cs.collision_resolve_new()
+    s.integration(DT)
+    for pos, nct in got:
+        np.testing.assert_array_equal(pos, obj.positions())
+        assert nct == cs.stats()["contacts"]
