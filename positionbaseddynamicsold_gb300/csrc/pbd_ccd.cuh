@@ -225,19 +225,107 @@ __device__ __forceinline__ bool no_root_near_unit(float f0, float f1, float f2, 
     return no_root_near_unit_f64(f0, f1, f2, f3);
 }
 
+// distance from the origin to the segment [a, b]
+__device__ __forceinline__ float seg_origin_dist(v3 a, v3 b) {
+    v3 d = sub3(b, a);
+    float dd = dot3(d, d);
+    float t = dd > 0.f ? fminf(fmaxf(-dot3(a, d) / dd, 0.f), 1.f) : 0.f;
+    v3 q = add3(a, mul3(d, t));
+    return sqrtf(dot3(q, q));
+}
+
+// Bernstein coefficients on [0, 1] of a x b for linear a (a0 -> a1) and b
+__device__ __forceinline__ void bern_cross(v3 a0, v3 a1, v3 b0, v3 b1, v3 c[3]) {
+    c[0] = cross3(a0, b0);
+    c[1] = mul3(add3(cross3(a0, b1), cross3(a1, b0)), 0.5f);
+    c[2] = cross3(a1, b1);
+}
+// Bernstein coefficients (degree 4) of u . v for quadratics u and v
+__device__ __forceinline__ void bern_dot(const v3 u[3], const v3 v[3], float c[5]) {
+    c[0] = dot3(u[0], v[0]);
+    c[1] = 0.5f * (dot3(u[0], v[1]) + dot3(u[1], v[0]));
+    c[2] = (dot3(u[0], v[2]) + 4.f * dot3(u[1], v[1]) + dot3(u[2], v[0])) * (1.f / 6.f);
+    c[3] = 0.5f * (dot3(u[1], v[2]) + dot3(u[2], v[1]));
+    c[4] = dot3(u[2], v[2]);
+}
+__device__ __forceinline__ float len3(v3 a) { return sqrtf(dot3(a, a)); }
+
+// True when no time of the step can pass ExtendedVFTest's inside test
+// (every weight >= -eps, eps = h / mean edge): across one edge line the
+// point stays outside the triangle by more than eps_max + 0.01 in
+// barycentric units for every t in [0, 1], eps_max = h / the mean of the
+// edges' smallest lengths over the step (edge vectors move linearly).
+// With r_v = v - point (linear in t) and n = (v2 - v1) x (v3 - v1), the
+// weight of vertex i is w_i = ((r_j x r_k) . n) / (n . n), (i, j, k) cyclic:
+// the barycentric coordinate of the point's projection onto the triangle's
+// plane.  Numerator and denominator are quartics in t; their Bernstein
+// coefficients follow from the linear factors', and a Bernstein polynomial
+// lies between its smallest and largest coefficient.  All five coefficients
+// of N_i + e D (e = eps_max + 0.01) below -tol, tol = 1e-4 of their
+// magnitude bound (well above this test's float rounding), put w_i below
+// -e on the whole interval.  The 0.01 covers the rounding of the
+// reference's float evaluation (interpolated positions, barycentric
+// coordinates), which the guards keep far below it: the triangle is no
+// sliver at either end (sin^2 of its angle at v1 >= 1e-4), n . n does not
+// dip below a quarter of its smaller end value, and coordinates are within
+// 1000 mean edges of the origin.
+__device__ bool vf_outside_all_step(const v3 *X, const v3 *P, float th) {
+    const v3 a0 = sub3(X[2], X[1]), a1 = sub3(P[2], P[1]);
+    const v3 b0 = sub3(X[3], X[1]), b1 = sub3(P[3], P[1]);
+    const v3 c0 = sub3(X[3], X[2]), c1 = sub3(P[3], P[2]);
+    const float es = seg_origin_dist(a0, a1) + seg_origin_dist(b0, b1) + seg_origin_dist(c0, c1);
+    if (!(es > 0.f)) return false;
+    float big = 0.f;
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+        big = fmaxf(big, fmaxf(fmaxf(fabsf(X[k].x), fabsf(X[k].y)),
+                               fmaxf(fmaxf(fabsf(X[k].z), fabsf(P[k].x)),
+                                     fmaxf(fabsf(P[k].y), fabsf(P[k].z)))));
+    if (!(big <= 1000.f * (es / 3.f))) return false;
+    v3 n[3];
+    bern_cross(a0, a1, b0, b1, n);
+    float D[5];
+    bern_dot(n, n, D);
+    if (!(D[0] >= 1e-4f * (dot3(a0, a0) * dot3(b0, b0)) &&
+          D[4] >= 1e-4f * (dot3(a1, a1) * dot3(b1, b1))))
+        return false;
+    const float dmin = 0.25f * fminf(D[0], D[4]);
+    if (!(D[1] >= dmin && D[2] >= dmin && D[3] >= dmin)) return false;
+    const float e = 3.f * th / es * 1.0001f + 0.01f;
+    const float nmag = len3(n[0]) + len3(n[1]) + len3(n[2]);
+    const v3 r0[3] = {sub3(X[1], X[0]), sub3(X[2], X[0]), sub3(X[3], X[0])};
+    const v3 r1[3] = {sub3(P[1], P[0]), sub3(P[2], P[0]), sub3(P[3], P[0])};
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        const int j = (i + 1) % 3, k = (i + 2) % 3;
+        v3 m[3];
+        bern_cross(r0[j], r1[j], r0[k], r1[k], m);
+        float C[5];
+        bern_dot(m, n, C);
+        const float tol =
+            1e-4f * ((len3(m[0]) + len3(m[1]) + len3(m[2])) * nmag + e * nmag * nmag);
+        if (C[0] + e * D[0] < -tol && C[1] + e * D[1] < -tol && C[2] + e * D[2] < -tol &&
+            C[3] + e * D[3] < -tol && C[4] + e * D[4] < -tol)
+            return true;
+    }
+    return false;
+}
+
 // ExtendedVFTest (P/CCD.cpp:1733-1808); X/P = start/predicted positions of
 // point, f0, f1, f2.  The reference evaluates t = 0, the cubic's roots in
-// [0, 1] and t = 1 in ascending order and stops at the first hit.  Two
+// [0, 1] and t = 1 in ascending order and stops at the first hit.  Three
 // shortcuts keep that result: t = 0 is always the first time evaluated, so
-// a hit there ends the test before any root is needed; and when the
+// a hit there ends the test before any root is needed; when the
 // coplanarity cubic provably has no root within 1e-3 of [0, 1], the root
 // solver (Newton iterations converging to roots outside that range) adds no
-// time to evaluate, leaving t = 1.  Only the remaining pairs run the FP64
-// root isolation.
+// time to evaluate, leaving t = 1; and when the point provably stays outside
+// the grown triangle over the whole step (vf_outside_all_step), no time can
+// hit.  Only the remaining pairs run the FP64 root isolation.
 //
 // Split in two so a kernel can keep the root isolation off its common path:
-// extended_vf_first answers for t = 0 and, when the cubic has no root near
-// [0, 1], for t = 1 (returns 1 hit, 0 no hit, 2 roots needed);
+// extended_vf_first answers for t = 0, for t = 1 when the cubic has no root
+// near [0, 1], and for the whole step when the point stays outside (returns
+// 1 hit, 0 no hit, 2 roots needed);
 // extended_vf_roots finishes a pair that needs roots (t = 0 is known not to
 // hit).  extended_vf_test is the composition.
 __device__ __forceinline__ void vf_coeffs(const v3 *X, const v3 *P, float a[4]) {
@@ -257,6 +345,8 @@ __device__ __forceinline__ int extended_vf_first(const v3 *X, const v3 *P, float
     vf_coeffs(X, P, a);
     if (vf_eval_at(X, P, th, 0.0f, res)) return 1;
     if (no_root_near_unit(a[0], a[1], a[2], a[3])) return vf_eval_at(X, P, th, 1.0f, res) ? 1 : 0;
+    // neither a root of the cubic nor t = 1 can pass the inside test
+    if (vf_outside_all_step(X, P, th)) return 0;
     return 2;
 }
 

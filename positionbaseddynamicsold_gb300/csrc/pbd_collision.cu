@@ -367,15 +367,6 @@ __global__ void __launch_bounds__(32 * kTaskWarps) k_point_pairs(
     if (scnt) warp_flush_pairs(stage, scnt, lane, pairs, cap, counters + 4, counters + 2, 16);
 }
 
-// distance from the origin to the segment [a, b]
-__device__ __forceinline__ float seg_origin_dist(v3 a, v3 b) {
-    v3 d = sub3(b, a);
-    float dd = dot3(d, d);
-    float t = dd > 0.f ? fminf(fmaxf(-dot3(a, d) / dd, 0.f), 1.f) : 0.f;
-    v3 q = add3(a, mul3(d, t));
-    return sqrtf(dot3(q, q));
-}
-
 // stage 3: one thread per AABB-overlapping pair.  The pair goes on to the
 // narrow phase unless the point is a vertex of the triangle or no time of
 // the step can pass ExtendedVFTest's two conditions: plane distance < 2h and
