@@ -323,9 +323,8 @@ __device__ bool vf_outside_all_step(const v3 *X, const v3 *P, float th) {
 // hit.  Only the remaining pairs run the FP64 root isolation.
 //
 // Split in two so a kernel can keep the root isolation off its common path:
-// extended_vf_first answers for t = 0, for t = 1 when the cubic has no root
-// near [0, 1], and for the whole step when the point stays outside (returns
-// 1 hit, 0 no hit, 2 roots needed);
+// extended_vf_first answers for t = 0 and, when the cubic has no root near
+// [0, 1], for t = 1 (returns 1 hit, 0 no hit, 2 roots needed);
 // extended_vf_roots finishes a pair that needs roots (t = 0 is known not to
 // hit).  extended_vf_test is the composition.
 __device__ __forceinline__ void vf_coeffs(const v3 *X, const v3 *P, float a[4]) {
@@ -345,8 +344,6 @@ __device__ __forceinline__ int extended_vf_first(const v3 *X, const v3 *P, float
     vf_coeffs(X, P, a);
     if (vf_eval_at(X, P, th, 0.0f, res)) return 1;
     if (no_root_near_unit(a[0], a[1], a[2], a[3])) return vf_eval_at(X, P, th, 1.0f, res) ? 1 : 0;
-    // neither a root of the cubic nor t = 1 can pass the inside test
-    if (vf_outside_all_step(X, P, th)) return 0;
     return 2;
 }
 
@@ -375,10 +372,17 @@ __device__ bool extended_vf_roots(const v3 *X, const v3 *P, float th, VFResult &
     return false;
 }
 
+// a pair extended_vf_first left open: no hit when the point stays outside
+// over the whole step, else the roots
+__device__ bool extended_vf_rest(const v3 *X, const v3 *P, float th, VFResult &res) {
+    if (vf_outside_all_step(X, P, th)) return false;
+    return extended_vf_roots(X, P, th, res);
+}
+
 __device__ bool extended_vf_test(const v3 *X, const v3 *P, float th, VFResult &res) {
     int r = extended_vf_first(X, P, th, res);
     if (r != 2) return r == 1;
-    return extended_vf_roots(X, P, th, res);
+    return extended_vf_rest(X, P, th, res);
 }
 
 // ---- the reference's other vertex-face tests ------------------------------

@@ -490,7 +490,9 @@ __global__ void __launch_bounds__(128) k_narrow(const int2 *__restrict__ cand, l
     }
 }
 
-// narrow phase, hard pairs: the cubic's roots in [0, 1] and t = 1
+// narrow phase, hard pairs: no hit when the point stays outside the grown
+// triangle over the whole step (nearly all of them), else the cubic's roots
+// in [0, 1] and t = 1
 __global__ void __launch_bounds__(128) k_narrow_roots(const int2 *__restrict__ cand, float th,
                                                       const int4 *__restrict__ tri,
                                                       const float4 *__restrict__ x,
@@ -505,7 +507,7 @@ __global__ void __launch_bounds__(128) k_narrow_roots(const int2 *__restrict__ c
         v3 X[4] = {ld3(x[c.x]), ld3(x[f.x]), ld3(x[f.y]), ld3(x[f.z])};
         v3 P[4] = {ld3(p[c.x]), ld3(p[f.x]), ld3(p[f.y]), ld3(p[f.z])};
         VFResult r;
-        bool hit = mode == 0 ? extended_vf_roots(X, P, th, r) : vf_test_mode(X, P, th, mode, r);
+        bool hit = mode == 0 ? extended_vf_rest(X, P, th, r) : vf_test_mode(X, P, th, mode, r);
         if (hit) store_contact(counters, ccap, c, f, r, cids, cface, ctn, cw);
     }
 }
