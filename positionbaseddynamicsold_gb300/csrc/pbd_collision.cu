@@ -12,10 +12,11 @@
 //      cell of the union of the 27-cell neighbourhoods of the centroid cells
 //      of its incident triangles (CCD_SH_Extended, P/CCD.cpp:1541-1586,
 //      tests every (point, neighbour) pair; the union holds each distinct
-//      pair once); a cell whose bucket AABB misses the point's swept AABB
-//      grown by 3.61 h yields nothing; the kept buckets' entries are spread
-//      over the lanes (warp prefix sum), each entry checked for its exact
-//      cell and swept-AABB overlap, the point's own triangles dropped;
+//      pair once); a cell whose bucket AABB is farther than 3.61 h
+//      (Euclidean gap) from the point's swept AABB yields nothing; the kept
+//      buckets' entries are spread over the lanes (warp prefix sum), each
+//      entry checked for its exact cell and for a swept AABB within 3.61 h
+//      of the point's, the point's own triangles dropped;
 //      found pairs are staged per warp in shared memory and appended with
 //      one atomic per batch (warps loop over points, so a batch spans many
 //      points);
@@ -178,18 +179,30 @@ __global__ void k_find_neighbors(int nt, GridParams g, const int4 *tcell, const 
     if (cnt) cnt[t] = k;
 }
 
+// squared Euclidean gap between boxes [pl, ph] and [l, h] (0 when they meet;
+// an infinite box meets everything)
+__device__ __forceinline__ float box_gap2(float plx, float ply, float plz, float phx, float phy,
+                                          float phz, float lx, float ly, float lz, float hx,
+                                          float hy, float hz) {
+    const float gx = fmaxf(0.f, fmaxf(lx - phx, plx - hx));
+    const float gy = fmaxf(0.f, fmaxf(ly - phy, ply - hy));
+    const float gz = fmaxf(0.f, fmaxf(lz - phz, plz - hz));
+    return (gx * gx + gy * gy) + gz * gz;
+}
+
 // Candidate search, one warp per point.  The point's candidate cells are
 // the union of the 27-cell neighbourhoods of its incident triangles'
 // centroid cells (FindNeighbors around every triangle that holds the point,
 // P/SpatialHashSystem.cpp:134-187, as CCD_SH_Extended visits them,
 // P/CCD.cpp:1522-1587).  A round takes 32 candidate cells, one per lane; a
-// lane keeps its cell when the bucket is non-empty and the bucket's AABB meets
-// the point's grown swept AABB.  The kept buckets' entries are then
+// lane keeps its cell when the bucket is non-empty and the bucket's AABB lies
+// within the reach margin (Euclidean gap) of the point's swept AABB.  The
+// kept buckets' entries are then
 // spread over the 32 lanes by a warp prefix sum (lane j of the warp takes
 // flat entries j, j+32, ...), so a bucket of any size costs ceil(entries/32)
 // coalesced steps; an entry yields a (point, triangle) pair when its cell is
-// the lane's cell (the hash may mix cells), its swept AABB meets the point's
-// and it belongs to the point's instance.
+// the lane's cell (the hash may mix cells), its swept AABB lies within the
+// margin of the point's and it belongs to the point's instance.
 constexpr int kTaskWarps = 8;
 constexpr int kPointPairStage = 256;  // pairs staged per warp, appended with one atomic
 constexpr unsigned long long kNear3 = 0x0000077707770777ull;  // 3x3x3 corner of a 4x4x4 block
@@ -235,9 +248,13 @@ __global__ void __launch_bounds__(32 * kTaskWarps) k_point_pairs(
         const int hy = __reduce_max_sync(0xffffffffu, valid ? mc.y : INT_MIN);
         const int hz = __reduce_max_sync(0xffffffffu, valid ? mc.z : INT_MIN);
         v3 X0 = ld3(xv), P0 = ld3(pv);
-        const float plx = fminf(X0.x, P0.x) - margin, phx = fmaxf(X0.x, P0.x) + margin;
-        const float ply = fminf(X0.y, P0.y) - margin, phy = fmaxf(X0.y, P0.y) + margin;
-        const float plz = fminf(X0.z, P0.z) - margin, phz = fmaxf(X0.z, P0.z) + margin;
+        // the point's swept box; a box within Euclidean distance `margin` of
+        // it can hold a hit (the point and the triangle at one time t lie in
+        // their swept boxes, and a hit needs them within the reach)
+        const float plx = fminf(X0.x, P0.x), phx = fmaxf(X0.x, P0.x);
+        const float ply = fminf(X0.y, P0.y), phy = fmaxf(X0.y, P0.y);
+        const float plz = fminf(X0.z, P0.z), phz = fmaxf(X0.z, P0.z);
+        const float m2 = margin * margin;
         // Incident cells within a 2 x 2 x 2 block (nearly always): the union
         // of their 27-neighbourhoods is a mask over the 4 x 4 x 4 block at
         // (lx - 1, ly - 1, lz - 1), bit x + 4 y + 16 z, OR-reduced over the
@@ -310,8 +327,9 @@ __global__ void __launch_bounds__(32 * kTaskWarps) k_point_pairs(
                 // range and box in one sector, loaded together
                 const float4 b0 = btab[2 * (size_t)b], b1 = btab[2 * (size_t)b + 1];
                 const int rs = __float_as_int(b0.x), re = __float_as_int(b0.y);
-                if (rs < re && !(plx > b1.y || phx < b0.z || ply > b1.z || phy < b0.w ||
-                                 plz > b1.w || phz < b1.x)) {
+                if (rs < re &&
+                    box_gap2(plx, ply, plz, phx, phy, phz, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w) <=
+                        m2) {
                     cnt = re - rs;
                     start = rs;
                 }
@@ -350,8 +368,8 @@ __global__ void __launch_bounds__(32 * kTaskWarps) k_point_pairs(
                     tri = __float_as_int(e0.w);
                     hit = __float_as_int(e0.x) == ox && __float_as_int(e0.y) == oy &&
                           __float_as_int(e0.z) == oz &&
-                          !(plx > th.x || phx < tl.x || ply > th.y || phy < tl.y ||
-                            plz > th.z || phz < tl.z) &&
+                          box_gap2(plx, ply, plz, phx, phy, phz, tl.x, tl.y, tl.z, th.x, th.y,
+                                   th.z) <= m2 &&
                           (!point_inst || tri_inst[tri] == inst);
                 }
                 // a triangle of the point itself is no candidate (the point is

@@ -2,8 +2,8 @@
 definition: every (point, triangle) pair of the reference's candidate set
 (CCD_SH_Extended, P/CCD.cpp:1541-1586: the triangle's centroid cell lies in
 the 27-cell neighbourhood of a centroid cell of one of the point's incident
-triangles) whose swept boxes meet -- the point's box grown by 3.61 h, a
-sliver triangle's box unbounded -- of one instance, the point's own
+triangles) whose swept boxes are within 3.61 h of each other (Euclidean gap;
+a sliver triangle's box unbounded) -- of one instance, the point's own
 triangles left out.  Centroids, cells and boxes follow the kernels' float32
 expressions.
 
@@ -53,8 +53,9 @@ def brute_pairs(pos, prd, tris, cell, start, h, size=None, point_inst=None, inst
     sl = sliver(a, b, c) | sliver(pos[tris[:, 0]], pos[tris[:, 1]], pos[tris[:, 2]])
     tlo[sl], thi[sl] = -np.inf, np.inf
     margin = f32(3.61) * f32(h) * f32(1.001) + f32(2e-6)
-    plo = np.minimum(pos, prd) - margin
-    phi = np.maximum(pos, prd) + margin
+    m2 = margin * margin
+    plo = np.minimum(pos, prd)
+    phi = np.maximum(pos, prd)
     inc = [[] for _ in range(n)]
     for t, (i, j, k) in enumerate(tris):
         for v in (i, j, k):
@@ -64,7 +65,10 @@ def brute_pairs(pos, prd, tris, cell, start, h, size=None, point_inst=None, inst
         cells = tc[[t for t in inc[v] if inside[t]]]
         if len(cells) == 0:
             continue
-        ok = inside & np.all((plo[v] <= thi) & (phi[v] >= tlo), 1)
+        with np.errstate(invalid="ignore"):
+            g = np.maximum(f32(0), np.maximum(tlo - phi[v], plo[v] - thi))
+        g = np.nan_to_num(g, nan=0.0)
+        ok = inside & (((g[:, 0] * g[:, 0] + g[:, 1] * g[:, 1]) + g[:, 2] * g[:, 2]) <= m2)
         if point_inst is not None:
             ok &= tinst == point_inst[v]
         cand = np.nonzero(ok)[0]
