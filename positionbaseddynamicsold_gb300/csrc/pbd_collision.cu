@@ -55,7 +55,24 @@ namespace cg = cooperative_groups;
 namespace pbd {
 namespace {
 
-constexpr int kMaxInc = 16;  // incident triangles considered per point
+constexpr int kMaxInc = 16;     // incident triangles considered per point
+constexpr int kPointSlots = 8;  // incident cells kept per point by the hash update
+
+// the slot of every (triangle, vertex) among the vertex's first kPointSlots
+// incident triangles (the point -> triangle lists are static)
+__global__ void k_tri_slots(int n, const int *__restrict__ pt_first,
+                            const int *__restrict__ pt_last, const int *__restrict__ pt_tri,
+                            const int4 *__restrict__ tri, int *tri_slot) {
+    int v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= n) return;
+    const int f0 = pt_first[v], m = min(pt_last[v] - f0, kPointSlots);
+    for (int j = 0; j < m; ++j) {
+        const int t = pt_tri[f0 + j];
+        const int4 f = tri[t];
+        const int k = f.x == v ? 0 : f.y == v ? 1 : 2;
+        tri_slot[3 * (size_t)t + k] = v * kPointSlots + j;
+    }
+}
 
 // ---------------------------------------------------------------------------
 // Clears the buckets the previous update filled: its sorted keys (all nt
@@ -81,7 +98,9 @@ __global__ void __launch_bounds__(256) k_tri_cells(int nt, GridParams g, float m
                                                    const float4 *__restrict__ x,
                                                    const float4 *__restrict__ p, int4 *tcell,
                                                    float4 *tlo, float4 *thi, uint32_t *key,
-                                                   int *id, int *n_valid) {
+                                                   int *id, int *n_valid,
+                                                   const int *__restrict__ tri_slot,
+                                                   int4 *pt_cell) {
     int t = blockIdx.x * blockDim.x + threadIdx.x;
     bool valid = false;
     if (t < nt) {
@@ -101,6 +120,12 @@ __global__ void __launch_bounds__(256) k_tri_cells(int nt, GridParams g, float m
         int iz = (int)floorf((cz - g.start.z) / cell.z);
         valid = g.hashed || !outside(g, ix, iy, iz);
         tcell[t] = make_int4(ix, iy, iz, f.w);
+        // the cell in its vertices' slots
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            const int sl = tri_slot[3 * (size_t)t + k];
+            if (sl >= 0) pt_cell[sl] = make_int4(ix, iy, iz, t);
+        }
         key[t] = valid ? bucket_of(g, ix, iy, iz, f.w) : g.nb;
         id[t] = t;
         v3 xa = ld3(x[f.x]), xb = ld3(x[f.y]), xc = ld3(x[f.z]);
@@ -212,7 +237,7 @@ __global__ void __launch_bounds__(32 * kTaskWarps) k_point_pairs(
     const int *__restrict__ point_inst, const int *__restrict__ tri_inst,
     const float4 *__restrict__ x, const float4 *__restrict__ p, const int4 *__restrict__ tcell,
     const float4 *__restrict__ btab, const float4 *__restrict__ etab, int2 *pairs, long long cap,
-    int *counters) {
+    int *counters, const int4 *__restrict__ pt_cell) {
     __shared__ int2 stage_all[kTaskWarps][kPointPairStage];
     const int lane = threadIdx.x & 31;
     const int warp0 = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -220,10 +245,14 @@ __global__ void __launch_bounds__(32 * kTaskWarps) k_point_pairs(
     int2 *stage = stage_all[threadIdx.x >> 5];
     int scnt = 0;  // pairs staged by this warp
     for (int v = warp0; v < n; v += nwarps) {
-        // the point's own positions first: their loads overlap the chain
-        // point -> incident triangles -> their cells
+        // one round of independent loads: the point's positions, its
+        // incidence range and the slots with its first incident triangles'
+        // cells; a point with more incident triangles than slots reads its
+        // list and their cells (two more dependent loads)
         const float4 xv = x[v], pv = p[v];
         int f0 = pt_first[v], f1 = pt_last[v];
+        const int4 sl = lane < kPointSlots ? pt_cell[(size_t)v * kPointSlots + lane]
+                                           : make_int4(0, 0, 0, -1);
         int ninc = f1 - f0;
         if (ninc > kMaxInc) {
             if (lane == 0) atomicOr(counters + 2, 4);
@@ -234,8 +263,13 @@ __global__ void __launch_bounds__(32 * kTaskWarps) k_point_pairs(
         bool valid = false;
         int inc_tri = -1;  // this lane's incident triangle
         if (lane < ninc) {
-            inc_tri = pt_tri[f0 + lane];
-            mc = tcell[inc_tri];
+            if (ninc <= kPointSlots) {
+                inc_tri = sl.w;
+                mc = sl;
+            } else {
+                inc_tri = pt_tri[f0 + lane];
+                mc = tcell[inc_tri];
+            }
             valid = g.hashed || !outside(g, mc.x, mc.y, mc.z);
         }
         const unsigned vm = __ballot_sync(0xffffffffu, valid);
@@ -760,7 +794,8 @@ static int shs_update_on(pbd_shs *h, cudaStream_t s, const float4 *psrc, int *ze
     k_tri_cells<<<grid_for(o->nt, 256), 256, 0, s>>>(o->nt, g, 0.0f, h->inst_cell.p,
                                                      h->n_inst_cell, o->tri.p, o->x.p, psrc,
                                                      h->tcell.p, h->tlo.p, h->thi.p, h->key.p,
-                                                     h->id.p, h->n_valid.p);
+                                                     h->id.p, h->n_valid.p, h->tri_slot.p,
+                                                     h->pt_cell.p);
     PBD_LAUNCH();
     PBD_TRY(radix_sort<uint32_t>(h->key.p, h->id.p, h->key_alt.p, h->id_alt.p, o->nt, nullptr,
                                  round8(h->key_bits), h->scr, s, &h->skey, &h->sid));
@@ -826,7 +861,8 @@ static int ccd_detect_on(pbd_colli *c, cudaStream_t s, const float4 *psrc) {
     k_point_pairs<<<pp_blocks, 32 * kTaskWarps, 0, s>>>(
         o->n, g, margin, o->pt_tri_first.p, o->pt_tri_last.p, o->pt_tri.p,
         o->has_inst ? o->point_inst.p : nullptr, o->has_inst ? o->tri_inst.p : nullptr, o->x.p,
-        psrc, h->tcell.p, h->btab.p, h->etab.p, c->pairs.p, c->task_cap, c->counters.p);
+        psrc, h->tcell.p, h->btab.p, h->etab.p, c->pairs.p, c->task_cap, c->counters.p,
+        h->pt_cell.p);
     PBD_LAUNCH();
     k_dist_filter<<<kPersistentBlocks, 256, 0, s>>>(c->pairs.p, c->task_cap, th, o->tri.p,
                                                     o->x.p, psrc, c->cand.p, c->cand_cap,
@@ -955,6 +991,14 @@ static int shs_alloc(pbd_shs *h) {
     PBD_TRY(h->id_alt.alloc(nt));
     PBD_TRY(h->etab.alloc(3 * nt));
     PBD_TRY(h->n_valid.alloc(1));
+    PBD_TRY(h->pt_cell.alloc((size_t)(o->n ? o->n : 1) * kPointSlots));
+    PBD_TRY(h->tri_slot.alloc(3 * nt));
+    PBD_CUDA(cudaMemsetAsync(h->tri_slot.p, 0xff, sizeof(int) * 3 * nt, o->stream));
+    if (o->n && o->nt) {
+        k_tri_slots<<<grid_for(o->n, 256), 256, 0, o->stream>>>(
+            o->n, o->pt_tri_first.p, o->pt_tri_last.p, o->pt_tri.p, o->tri.p, h->tri_slot.p);
+        PBD_LAUNCH();
+    }
     PBD_TRY(h->btab.alloc(2 * ((size_t)h->n_buckets + 1)));
     PBD_TRY(radix_reserve(h->scr, (long long)nt, round8(h->key_bits)));
     PBD_CUDA(cudaMemsetAsync(h->btab.p, 0, sizeof(float4) * 2 * (h->n_buckets + 1), o->stream));

@@ -263,6 +263,13 @@ struct pbd_shs {
     // batched cloth gets the cells it would get alone; 0 instances = one cell
     pbd::DBuf<float4> inst_cell;
     int n_inst_cell = 0;
+    // per point, kPointSlots slots: the cell (xyz) and id (w) of its first
+    // incident triangles (the point -> triangle lists' order), rewritten by
+    // each update, so the candidate search finds a point's incident cells
+    // in one load; tri_slot: per triangle and vertex, that slot (-1 when the
+    // vertex has more incident triangles than slots)
+    pbd::DBuf<int4> pt_cell;
+    pbd::DBuf<int> tri_slot;
 };
 
 struct pbd_colli {
