@@ -67,10 +67,11 @@ sys.path.insert(0, ROOT)
 
 METRIC = "cloth substeps/s"
 # DRAM bytes per launch of the dominant kernel (the per-color GS launch),
-# dram__bytes_read.sum + dram__bytes_write.sum from one ncu capture of the
-# workload on the current kernels (the profile named beside each)
-TRAFFIC_BYTES = {"drape256": 1398705.0}
-TRAFFIC_SOURCE = {"drape256": "profiles/drape256_kernels.md"}
+# dram__bytes_read.sum + dram__bytes_write.sum averaged over one ncu capture
+# of 40-60 launches of the workload on the current kernel (the profile
+# named beside each)
+TRAFFIC_BYTES = {"drape256": 1355614.0, "fold1024": 21407981.0, "batch512": 64789632.0}
+TRAFFIC_SOURCE = {w: "profiles/k_project_color_traffic.md" for w in TRAFFIC_BYTES}
 G = np.array([0.0, -9.8, 0.0], np.float32)
 DT = 1.0 / 600.0
 ITERS = 15
