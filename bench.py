@@ -41,9 +41,10 @@ target (--target, at most --max-sweeps sweeps in chunks of --chunk, the loop
 on the device in a CUDA graph), --learned adds the trained warm start,
 the autotuner picks the GS launch form after the pre-roll (--no-autotune
 keeps the default form).  `learned_warm_start` in the line compares the
-network trained on contact states with the plain sweeps on fold1024 and
-drape256, solve by solve from identical states, at the residual the plain
-solve reaches with 60 sweeps (see learned_eval).
+trained network of each workload's family (contact states for fold1024 and
+drape256, pinned hanging cloths for batch512) with the plain sweeps, solve
+by solve from identical states, at the residual the plain solve reaches
+with 60 sweeps (see learned_eval).
 
 Multi-GPU: a single cloth does not shard; N GPUs run N independent replicas
 (value = replicas x substeps / slowest replica's time).  batch512 shards its
@@ -446,10 +447,13 @@ def run_ours(args, rank, world):
 
 
 def learned_eval(substeps=12, sweeps=60):
-    """The learned warm start (weights trained on the contact families)
-    against the plain sweeps on the contact workloads fold1024 and drape256,
-    from identical states along a plain trajectory after each workload's
-    pre-roll: the plain solve runs `sweeps` sweeps (chunks of 10, a CCD
+    """The learned warm start against the plain sweeps on fold1024, drape256
+    and batch512 (config 4 with and without the warm start), each with the
+    network trained on its family: the contact-state network (folds on the
+    ground, drapes over a sphere) for fold1024 and drape256, the hanging-cloth
+    network (square cloths with pinned corners) for the batch's pinned cloths.
+    From identical states along a plain trajectory after each workload's
+    pre-roll, the plain solve runs `sweeps` sweeps (chunks of 10, a CCD
     detection per chunk, the response after every sweep) and its final
     stretch residual r_K is the target the warm-started solve must reach.
     Both solves detect their first contacts from the same advected
@@ -458,13 +462,21 @@ def learned_eval(substeps=12, sweeps=60):
     residual after 0..200 sweeps of the first state (it levels off: the
     contact response and the pins keep a floor far above 1e-4)."""
     from positionbaseddynamicsold_gb300 import warmstart_train as wt
-    try:
-        params, scales, meta = wt.load_params(wt.CONTACT_WEIGHTS)
-    except FileNotFoundError:
-        return {"unavailable": "no trained weights at " + wt.CONTACT_WEIGHTS}
-    out = {"weights": os.path.relpath(wt.CONTACT_WEIGHTS, ROOT),
-           "trained_on": meta.get("families"), "target": "r_plain(%d sweeps)" % sweeps}
-    out.update(wt.evaluate_workloads(params, scales, sweeps, substeps))
+    out = {"target": "r_plain(%d sweeps)" % sweeps}
+    for path, names in ((wt.CONTACT_WEIGHTS, ("fold1024", "drape256")),
+                        (wt.DEFAULT_WEIGHTS, ("batch512",))):
+        try:
+            params, scales, meta = wt.load_params(path)
+        except FileNotFoundError:
+            for name in names:
+                out[name] = {"unavailable": "no trained weights at " + path}
+            continue
+        fam = meta.get("families") or ["hanging"]
+        for name, r in wt.evaluate_workloads(params, scales, sweeps, substeps,
+                                             names=names).items():
+            r["weights"] = os.path.relpath(path, ROOT)
+            r["trained_on"] = fam
+            out[name] = r
     return out
 
 

@@ -246,6 +246,10 @@ def contact_solver(sc, log2):
     cs.set_capacity(max(1 << 22, 64 * n), max(1 << 20, 4 * n))
     if "ground" in sc["colli"]:
         s.set_ground(True, sc["colli"]["ground"])
+    if "spheres" in sc["colli"]:
+        s.set_instance_spheres(sc["colli"]["spheres"])
+    if "instance_cells" in sc["colli"]:
+        shs.set_instance_cells(sc["colli"]["instance_cells"])
     obj._keep = shs
     return obj, s, cs
 
@@ -585,6 +589,13 @@ def workload_scene(name):
         return scenes.folding_cloth(res=1024, seed=0), 24, 120
     if name == "drape256":
         return scenes.drape_over_sphere(res=256, seed=0, start="contact"), 20, 0
+    if name == "batch512":
+        # 512 cloths in one object, each hashed with its own cell and kept
+        # off its own sphere (the batch the benchmark times)
+        sc = scenes.batched_cloths(512, seed=0)
+        sc["colli"] = {"cell": 2.0 * scenes.mean_rest_edge(sc), "thickness": 1e-3,
+                       "spheres": sc["spheres"], "instance_cells": scenes.instance_cells(sc)}
+        return sc, 24, 120
     raise ValueError(name)
 
 
