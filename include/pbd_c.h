@@ -376,7 +376,8 @@ int pbd_colli_set_vf_test(pbd_colli *c, int mode);
 int pbd_colli_stats(pbd_colli *c, long long *candidates, long long *contacts, int *overflow);
 /* The (point, triangle) pairs the last CCD call's hash search handed to
  * the distance filter, in device order: pairs of the reference's candidate
- * set (CCD_SH_Extended, P/CCD.cpp:1541-1586) whose swept boxes meet, the
+ * set (CCD_SH_Extended, P/CCD.cpp:1541-1586) whose swept boxes lie within
+ * 3.61 thicknesses of each other (Euclidean gap between the boxes), the
  * point's own triangles left out.  *n = their count; min(*n, cap) pairs
  * (point, triangle) are written to pairs when it is not NULL. */
 int pbd_colli_get_pairs(pbd_colli *c, int *pairs, long long cap, long long *n);
