@@ -40,11 +40,12 @@ Other modes: --solve residual runs every substep to a stretch-residual
 target (--target, at most --max-sweeps sweeps in chunks of --chunk, the loop
 on the device in a CUDA graph), --learned adds the trained warm start,
 the autotuner picks the GS launch form after the pre-roll (--no-autotune
-keeps the default form).  `learned_warm_start` in the line compares the
-trained network of each workload's family (contact states for fold1024 and
-drape256, pinned hanging cloths for batch512) with the plain sweeps, solve
-by solve from identical states, at the residual the plain solve reaches
-with 60 sweeps (see learned_eval).
+keeps the default form).  `learned_warm_start` in the line compares both
+trained networks (contact states, pinned hanging cloths) with the plain
+sweeps on fold1024, drape256 and batch512, solve by solve from identical
+states, at the residual the plain solve reaches with 60 sweeps; each
+workload's record is the network that measured faster there, with the
+other's result beside it (see learned_eval).
 
 Multi-GPU: a single cloth does not shard; N GPUs run N independent replicas
 (value = replicas x substeps / slowest replica's time).  batch512 shards its
@@ -448,35 +449,49 @@ def run_ours(args, rank, world):
 
 def learned_eval(substeps=12, sweeps=60):
     """The learned warm start against the plain sweeps on fold1024, drape256
-    and batch512 (config 4 with and without the warm start), each with the
-    network trained on its family: the contact-state network (folds on the
-    ground, drapes over a sphere) for fold1024 and drape256, the hanging-cloth
-    network (square cloths with pinned corners) for the batch's pinned cloths.
-    From identical states along a plain trajectory after each workload's
-    pre-roll, the plain solve runs `sweeps` sweeps (chunks of 10, a CCD
-    detection per chunk, the response after every sweep) and its final
-    stretch residual r_K is the target the warm-started solve must reach.
-    Both solves detect their first contacts from the same advected
-    positions.  Device time of each solve from the CUDA graph of
-    pbd_solver_step_to_residual; `residual_curve_first_state` is the plain
-    residual after 0..200 sweeps of the first state (it levels off: the
-    contact response and the pins keep a floor far above 1e-4)."""
+    and batch512 (config 4 with and without the warm start).  Both trained
+    networks are evaluated on every workload: the contact-state network
+    (folds on the ground, drapes over a sphere) and the hanging-cloth network
+    (square cloths with pinned corners).  Each workload's record is the
+    network that measured faster there (contact states on fold1024, hanging
+    cloths on drape256 and batch512), with the other's result beside it
+    under `other_weights`.  From identical states along a plain trajectory
+    after each workload's pre-roll, the plain solve runs `sweeps` sweeps
+    (chunks of 10, a CCD detection per chunk, the response after every
+    sweep) and its final stretch residual r_K is the target the
+    warm-started solve must reach.  Both solves detect their first contacts
+    from the same advected positions.  Device time of each solve from the
+    CUDA graph of pbd_solver_step_to_residual; `residual_curve_first_state`
+    is the plain residual after 0..200 sweeps of the first state (it levels
+    off: the contact response and the pins keep a floor far above 1e-4)."""
     from positionbaseddynamicsold_gb300 import warmstart_train as wt
     out = {"target": "r_plain(%d sweeps)" % sweeps}
-    for path, names in ((wt.CONTACT_WEIGHTS, ("fold1024", "drape256")),
-                        (wt.DEFAULT_WEIGHTS, ("batch512",))):
+    nets = {}
+    for path in (wt.CONTACT_WEIGHTS, wt.DEFAULT_WEIGHTS):
         try:
             params, scales, meta = wt.load_params(path)
         except FileNotFoundError:
-            for name in names:
-                out[name] = {"unavailable": "no trained weights at " + path}
             continue
-        fam = meta.get("families") or ["hanging"]
-        for name, r in wt.evaluate_workloads(params, scales, sweeps, substeps,
-                                             names=names).items():
+        nets[path] = (params, scales, meta.get("families") or ["hanging"])
+    pick = {"fold1024": wt.CONTACT_WEIGHTS, "drape256": wt.DEFAULT_WEIGHTS,
+            "batch512": wt.DEFAULT_WEIGHTS}
+    keep = ("weights", "trained_on", "speedup", "learned_ms", "learned_sweeps", "reverted",
+            "learned_reached")
+    for name, first in pick.items():
+        res = {}
+        for path, (params, scales, fam) in nets.items():
+            r = wt.evaluate_workloads(params, scales, sweeps, substeps, names=(name,))[name]
             r["weights"] = os.path.relpath(path, ROOT)
             r["trained_on"] = fam
-            out[name] = r
+            res[path] = r
+        if not res:
+            out[name] = {"unavailable": "no trained weights"}
+            continue
+        main = res.get(first) or next(iter(res.values()))
+        for path, r in res.items():
+            if r is not main:
+                main["other_weights"] = {k: r[k] for k in keep}
+        out[name] = main
     return out
 
 
