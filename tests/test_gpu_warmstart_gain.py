@@ -57,3 +57,20 @@ def test_contact_weights_cut_the_sweeps_of_a_held_out_fold():
     # the plain residual levels off: 200 sweeps take it little below 60
     curve = {c["sweeps"]: c["stretch_residual"] for c in r["residual_curve_first_state"]}
     assert curve[200] > 0.5 * curve[60] > 0.0
+
+
+def test_hanging_weights_cut_the_sweeps_of_a_held_out_drape():
+    """The network trained on pinned hanging cloths on a scene family it was
+    not trained on, a drape over a sphere (a 128² cloth in contact from its
+    first substep): from identical states the warm-started solve reaches the
+    residual of 60 plain sweeps with at most 3/4 of their sweeps in total,
+    on at least 5 of 6 substeps, and its device time is lower."""
+    from positionbaseddynamicsold_gb300 import scenes
+    assert os.path.exists(wt.DEFAULT_WEIGHTS), "trained hanging-cloth weights missing"
+    params, scales, meta = wt.load_params(wt.DEFAULT_WEIGHTS)
+    sc = scenes.drape_over_sphere(res=128, seed=765_432, start="contact")
+    r = wt.evaluate_contact_same_state(params, scales, sc, 18, preroll=0, substeps=6,
+                                       sweeps=60, chunk=10)
+    assert r["learned_reached"] >= 5, r
+    assert r["learned_sweeps"] <= 0.75 * r["plain_sweeps"], r
+    assert r["learned_ms"] < r["plain_ms"], r
