@@ -58,8 +58,11 @@ namespace {
 constexpr int kMaxInc = 16;     // incident triangles considered per point
 constexpr int kPointSlots = 8;  // incident cells kept per point by the hash update
 
-// the slot of every (triangle, vertex) among the vertex's first kPointSlots
-// incident triangles (the point -> triangle lists are static)
+// the slot of every (triangle, corner) among the corner point's first
+// kPointSlots incident triangles (the point -> triangle lists are static,
+// one entry per corner: a triangle that repeats a point appears once per
+// corner, and its i-th appearance in the point's list takes its i-th corner
+// holding the point, so every slot in use is written by some corner)
 __global__ void k_tri_slots(int n, const int *__restrict__ pt_first,
                             const int *__restrict__ pt_last, const int *__restrict__ pt_tri,
                             const int4 *__restrict__ tri, int *tri_slot) {
@@ -68,9 +71,14 @@ __global__ void k_tri_slots(int n, const int *__restrict__ pt_first,
     const int f0 = pt_first[v], m = min(pt_last[v] - f0, kPointSlots);
     for (int j = 0; j < m; ++j) {
         const int t = pt_tri[f0 + j];
+        int occ = 0;  // earlier appearances of t in this point's list
+        for (int i = 0; i < j; ++i) occ += pt_tri[f0 + i] == t;
         const int4 f = tri[t];
-        const int k = f.x == v ? 0 : f.y == v ? 1 : 2;
-        tri_slot[3 * (size_t)t + k] = v * kPointSlots + j;
+        const int c[3] = {f.x, f.y, f.z};
+        int k = -1;
+        for (int q = 0; q < 3 && k < 0; ++q)
+            if (c[q] == v && occ-- == 0) k = q;
+        if (k >= 0) tri_slot[3 * (size_t)t + k] = v * kPointSlots + j;
     }
 }
 
