@@ -9,8 +9,9 @@ expressions.
 
 Cases: the hashed grid; cells finer than the triangles (incident cells
 spread beyond a 2 x 2 x 2 block); a sliver (the search window is then the
-whole neighbourhood); a bounded grid (cells outside it hold nothing); a
-batch with a cell size per instance.
+whole neighbourhood); a triangle that repeats a corner point; a bounded
+grid (cells outside it hold nothing); a batch with a cell size per
+instance.
 """
 import numpy as np
 import pytest
@@ -139,6 +140,22 @@ def test_pairs_with_a_sliver():
     cell = f32(2.0 * scenes.mean_rest_edge(sc))
     got = search(sc, q, cell)
     want = brute_pairs(p, q, tris, (cell,) * 3, (0, 0, 0), H)
+    assert np.any(want[:, 1] == len(tris) - 1)
+    np.testing.assert_array_equal(got, want)
+
+
+def test_pairs_with_a_repeated_corner():
+    """a triangle whose first two corners are one point: that point's
+    incidence list holds it twice, and both of its incident-cell slots are
+    written"""
+    sc, prd = crumpled(seed=4)
+    res = 24
+    r = res // 2
+    tris = np.concatenate([sc["tri_idx"], [[r * res + 5, r * res + 5, r * res + 6]]]).astype(np.int32)
+    sc = dict(sc, tri_idx=tris)
+    cell = f32(2.0 * scenes.mean_rest_edge(sc))
+    got = search(sc, prd, cell)
+    want = brute_pairs(sc["pos"], prd, tris, (cell,) * 3, (0, 0, 0), H)
     assert np.any(want[:, 1] == len(tris) - 1)
     np.testing.assert_array_equal(got, want)
 
