@@ -23,6 +23,9 @@ the state bench.py times, and checked against the oracle from that state:
   oracle run on each instance alone with its own cell and sphere, within
   1e-5 m, contact counts equal.
 
+Every benchmark object's coloring is also validated: no two constraints of
+one color share a point (test_bench_colorings_are_valid).
+
 The oracle runs its independent loops on every host core (the results do
 not depend on the thread count).
 """
@@ -141,3 +144,20 @@ def test_batch512_instances_match_oracle(orc_mt):
     assert p0 == len(got)
     assert cs.stats()["contacts"] == total
     assert total > 0
+
+
+@pytest.mark.parametrize("name", ["drape256", "fold1024", "batch512"])
+def test_bench_colorings_are_valid(name):
+    """the device coloring of each benchmark object: every constraint has a
+    color, and no two constraints of one color share a point"""
+    sc, cfg, colli_on, tl, preroll = bench.make_workload(name)
+    obj, solver, shs, cs = bench.setup(sc, colli_on, tl)
+    colors = obj.colors().astype(np.int64)
+    assert colors.min() >= 0
+    pl = sc["prim_list"].astype(np.int64)
+    cnt = pl[:, 1]
+    owner = np.repeat(np.arange(len(pl)), cnt)
+    pos = np.repeat(pl[:, 0], cnt) + (np.arange(cnt.sum()) - np.repeat(np.cumsum(cnt) - cnt, cnt))
+    pts = sc["indices"].astype(np.int64)[pos]
+    keys = colors[owner] * (int(pts.max()) + 1) + pts
+    assert len(np.unique(keys)) == len(keys)
