@@ -25,14 +25,17 @@
 //      sqrt((2h)^2 + r^2), r = 2h * longest / mean edge (at most 3.61 h).
 //      Neither filter can reject a pair ExtendedVFTest would accept.
 // Narrowphase: ExtendedVFTest (P/CCD.cpp:1733-1808) with the reference's
-// arithmetic: float triple products widened to double, the double cubic
-// solve (P/CCD.cpp:48-113), the float barycentric inside test.  One thread
-// per candidate evaluates t = 0 and, when the cubic has no root near [0, 1],
-// t = 1; the few pairs that need the roots are compacted into a list that a
-// second kernel solves on full warps (the FP64 root isolation is slow on
-// this GPU and would otherwise stall nearly every warp).  Contacts are kept
-// in discovery order on the device and sorted by (point, triangle) only
-// when copied out.
+// decisions: float triple products (widened to double for the root
+// isolation), the double cubic solve (P/CCD.cpp:48-113), the float
+// barycentric inside test; the double comparisons are taken in float where
+// the float result is provably the same (pbd_ccd.cuh).  One thread per
+// candidate evaluates t = 0 and, when the cubic has no root near [0, 1],
+// t = 1; the pairs that need the roots are compacted into a list for a
+// second kernel, which first drops the pairs whose point provably stays
+// outside the grown triangle over the whole step and solves the rest on
+// full warps (the FP64 root isolation is slow on this GPU).  Contacts are
+// kept in discovery order on the device and sorted by (point, triangle)
+// only when copied out.
 // Response: per pass every contact computes its four corrections from the
 // pass-start positions (VFResolveTest + VFResolveNew, P/CCD.cpp:1996-2090)
 // and adds them to per-point sums in 2^-32 m fixed point (integer atomics:
